@@ -1,0 +1,130 @@
+"""NumPy stand-in for the parts of ``jax`` that the reference's QG 1.5-layer
+model source (mapping/models/model_qg1l/jqgm.py) touches on its forward path.
+
+Fixture generation only: ``gen_golden.py`` installs these modules in
+``sys.modules`` and then loads the reference's own ``jqgm.py`` source, so that
+the golden vectors are produced by the reference's lines of code executed with
+NumPy float64 arithmetic in place of XLA. Nothing else imports this file.
+
+Semantics kept from jax.numpy:
+- ``x.at[idx].set(v)`` / ``.add(v)`` return a modified copy (functional update);
+- ``jit`` is the identity (it only traces/compiles in jax);
+- ``jnp.fft.irfft`` is NumPy's pocketfft with the same ``norm`` meaning.
+``jvp``/``vjp`` are not provided: the tangent/adjoint golden checks use finite
+differences of this forward instead.
+"""
+import sys
+import types
+import functools
+
+import numpy as np
+
+
+class JArray(np.ndarray):
+    """ndarray with the functional ``.at[...]`` update API of jax arrays."""
+
+    @property
+    def at(self):
+        return _AtIndexer(self)
+
+
+class _AtIndexer:
+    def __init__(self, arr):
+        self._arr = arr
+
+    def __getitem__(self, idx):
+        return _AtUpdate(self._arr, idx)
+
+
+class _AtUpdate:
+    def __init__(self, arr, idx):
+        self._arr = arr
+        self._idx = idx
+
+    def set(self, value):
+        out = np.array(self._arr, copy=True)
+        out[self._idx] = np.asarray(value)
+        return out.view(JArray)
+
+    def add(self, value):
+        out = np.array(self._arr, copy=True)
+        out[self._idx] += np.asarray(value)
+        return out.view(JArray)
+
+
+def _wrap(fn):
+    @functools.wraps(fn)
+    def inner(*args, **kwargs):
+        out = fn(*args, **kwargs)
+        if isinstance(out, np.ndarray) and not isinstance(out, JArray):
+            return out.view(JArray)
+        if isinstance(out, tuple):
+            return tuple(o.view(JArray) if isinstance(o, np.ndarray) else o for o in out)
+        return out
+    return inner
+
+
+class _NumpyNamespace(types.ModuleType):
+    """Module whose attributes are NumPy functions returning JArray."""
+
+    def __init__(self, name, base):
+        super().__init__(name)
+        self._base = base
+
+    def __getattr__(self, name):
+        attr = getattr(self._base, name)
+        if callable(attr) and not isinstance(attr, type):
+            return _wrap(attr)
+        return attr
+
+
+def _jit(fun=None, **kwargs):
+    if fun is None:
+        return lambda f: f
+    return fun
+
+
+def _unavailable(*args, **kwargs):
+    raise NotImplementedError("not available in the NumPy stand-in")
+
+
+def install(enable_x64=True):
+    """Register fake ``jax``, ``matplotlib`` and ``src.config`` modules."""
+    jax = types.ModuleType("jax")
+    jnp = _NumpyNamespace("jax.numpy", np)
+    jnp.fft = _NumpyNamespace("jax.numpy.fft", np.fft)
+    jax.numpy = jnp
+    jax.jit = _jit
+    jax.jvp = _unavailable
+    jax.vjp = _unavailable
+    jax.vmap = _unavailable
+    cfg = types.SimpleNamespace(update=lambda *a, **k: None)
+    jax.config = cfg
+    lax = types.ModuleType("jax.lax")
+    for name in ("scan", "fori_loop", "dynamic_slice", "dynamic_update_slice"):
+        setattr(lax, name, _unavailable)
+    jax.lax = lax
+    jsp = types.ModuleType("jax.scipy")
+    jsp_sparse = types.ModuleType("jax.scipy.sparse")
+    jsp_linalg = types.ModuleType("jax.scipy.sparse.linalg")
+    jsp_linalg.cg = _unavailable
+    jsp.sparse = jsp_sparse
+    jsp_sparse.linalg = jsp_linalg
+    jax.scipy = jsp
+
+    mpl = types.ModuleType("matplotlib")
+    pylab = types.ModuleType("matplotlib.pylab")
+    mpl.pylab = pylab
+
+    src = types.ModuleType("src")
+    src_config = types.ModuleType("src.config")
+    src_config.USE_FLOAT64 = bool(enable_x64)
+    src.config = src_config
+
+    sys.modules.update({
+        "jax": jax, "jax.numpy": jnp, "jax.numpy.fft": jnp.fft,
+        "jax.lax": lax, "jax.scipy": jsp, "jax.scipy.sparse": jsp_sparse,
+        "jax.scipy.sparse.linalg": jsp_linalg,
+        "matplotlib": mpl, "matplotlib.pylab": pylab,
+        "src": src, "src.config": src_config,
+    })
