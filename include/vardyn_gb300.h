@@ -1,0 +1,195 @@
+/*
+ * vardyn_gb300 — C ABI of the GB300 (sm_103a) backend for VarDyn's 4D-Var
+ * inner loop: the QG 1.5-layer model step, its tangent-linear and adjoint,
+ * the Helmholtz PV->SSH inversion and the along-track observation misfit.
+ *
+ * Conventions
+ *   - Every array argument is a DEVICE pointer unless its name ends in _host.
+ *   - Fields are row-major [batch][ny][nx] (the reference's (ny, nx) State
+ *     layout, mapping/src/state.py:52-56), contiguous, element type given by
+ *     the plan's dtype (VD_F32 = float, VD_F64 = double).
+ *   - Calls are stream-ordered on the caller's cudaStream_t (passed as void*),
+ *     do not synchronise, do not allocate device memory (scratch comes in as a
+ *     caller-owned workspace sized by the *_bytes queries), and return a
+ *     vd_status. Plans own their constant tables (allocated once at create).
+ *   - Batched calls advance `batch` independent windows of the same grid in
+ *     lockstep; `batch` = 1 is the reference's single-window call.
+ */
+#ifndef VARDYN_GB300_H
+#define VARDYN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int vd_status;
+#define VD_OK 0
+#define VD_ERR_ARG 1          /* bad dimension, null pointer, unknown option */
+#define VD_ERR_CUDA 2         /* a CUDA runtime call failed */
+#define VD_ERR_WORKSPACE 3    /* workspace smaller than the *_bytes query */
+#define VD_ERR_UNSUPPORTED 4  /* grid too small/large for the kernels */
+
+#define VD_F32 0
+#define VD_F64 1
+
+/* Time schemes of Qgm.one_step (mapping/models/model_qg1l/jqgm.py:493-498);
+ * VD_RK4 is an extension (classical Runge-Kutta 4), absent from Qgm. */
+#define VD_EULER 0
+#define VD_RK2 1
+#define VD_RK3 2
+#define VD_RK4 3
+
+typedef struct vd_qg1l_plan vd_qg1l_plan;
+
+/* Model constants, the arguments of Qgm.__init__
+ * (mapping/models/model_qg1l/jqgm.py:113-236). */
+typedef struct vd_qg1l_desc {
+    int ny, nx;            /* grid shape (>= 8 each) */
+    int dtype;             /* VD_F32 | VD_F64 */
+    int time_scheme;       /* VD_EULER | VD_RK2 | VD_RK3 | VD_RK4 */
+    double dx, dy;         /* grid spacing [m] (jqgm.py:126-131 centre value) */
+    double dt;             /* time step [s] */
+    double g;              /* gravity */
+    double f;              /* Coriolis (nanmean of the f field, jqgm.py:140) */
+    double c;              /* first baroclinic phase speed (jqgm.py:150-153) */
+    double Kdiffus;        /* PV diffusion; used only if has_Kdiffus */
+    int has_Kdiffus;
+    const int8_t* mask_host;   /* [ny][nx] mask of jqgm.py:178-217 (0 land,
+                                  1/2 rings, 3 interior); NULL = no land */
+    const double* beta_host;   /* [ny][nx] beta at each T point, rows 1..ny-2
+                                  used (jqgm.py:143,356-358); NULL = f-plane */
+    const double* fbathy_host; /* [ny][nx] f*bathymetry_PV_term (jqgm.py:351-353);
+                                  NULL = none */
+} vd_qg1l_desc;
+
+/* Build a plan: DST-I half matrices, tridiagonal multipliers, mask, beta and
+ * bathymetry tables on the current device. Replaces the constant set-up of
+ * Qgm.__init__ (jqgm.py:113-236). */
+vd_status vd_qg1l_plan_create(vd_qg1l_plan** plan, const vd_qg1l_desc* desc);
+vd_status vd_qg1l_plan_destroy(vd_qg1l_plan* plan);
+
+/* Workspace for one call of `batch` windows (forward, tangent, adjoint and
+ * the solve all fit in it). */
+size_t vd_qg1l_workspace_bytes(const vd_qg1l_plan* plan, int batch);
+/* Trajectory storage of `nstep` steps: every stage state (h_s, q_s) of every
+ * step plus the final state, as the adjoint needs them. */
+size_t vd_qg1l_traj_bytes(const vd_qg1l_plan* plan, int batch, int nstep);
+/* Index-free description of the trajectory layout: slot(n, s) = n*nstage+s,
+ * each slot holds h then q, each [batch][ny][nx]. */
+int vd_qg1l_nstage(const vd_qg1l_plan* plan);
+
+/* SSH -> PV (Qgm.h2pv, jqgm.py:264-293). */
+vd_status vd_qg1l_h2pv(const vd_qg1l_plan* plan, int batch, const void* h,
+                       const void* hb, void* q, void* stream);
+/* SSH -> geostrophic u, v (Qgm.h2uv, jqgm.py:238-262). */
+vd_status vd_qg1l_h2uv(const vd_qg1l_plan* plan, int batch, const void* h,
+                       void* u, void* v, void* stream);
+/* PV tendency (Qgm.rhs, jqgm.py:321-375, way=+1). */
+vd_status vd_qg1l_rhs(const vd_qg1l_plan* plan, int batch, const void* u,
+                      const void* v, const void* q, void* rhs, void* stream);
+/* PV -> SSH: h = L^-1(q - qb) on the interior + hb (Qgm.pv2h, jqgm.py:295-319,
+ * inverse_elliptic_dst 83-91), by x-DST-I, y-tridiagonal solve, x-DST-I. */
+vd_status vd_qg1l_pv2h(const vd_qg1l_plan* plan, int batch, const void* q,
+                       const void* hb, const void* qb, void* h, void* work,
+                       size_t work_bytes, void* stream);
+
+/* Forward model: Qgm.step (jqgm.py:517-557). h_out = M^nstep(h0) with
+ * q0 = h2pv(h0, hb), land set to NaN. If traj != NULL (sized by
+ * vd_qg1l_traj_bytes) every stage state is stored for a later adjoint.
+ * h_out may alias h0. */
+vd_status vd_qg1l_step(const vd_qg1l_plan* plan, int batch, const void* h0,
+                       const void* hb, int nstep, void* h_out, void* traj,
+                       void* work, size_t work_bytes, void* stream);
+/* Tangent linear: Qgm.step_tgl (jqgm.py:559-563), dh_out = M'(h0) dh0. */
+vd_status vd_qg1l_step_tgl(const vd_qg1l_plan* plan, int batch, const void* dh0,
+                           const void* h0, const void* hb, int nstep,
+                           void* dh_out, void* work, size_t work_bytes,
+                           void* stream);
+/* Adjoint: Qgm.step_adj (jqgm.py:565-569), adh_out = M'(h0)^T adh1.
+ * traj must hold the trajectory of vd_qg1l_step(h0, hb, nstep); if
+ * traj_ready == 0 it is recomputed into traj first. adh_out may alias adh1. */
+vd_status vd_qg1l_step_adj(const vd_qg1l_plan* plan, int batch, const void* adh1,
+                           const void* h0, const void* hb, int nstep,
+                           void* adh_out, void* traj, int traj_ready,
+                           void* work, size_t work_bytes, void* stream);
+
+/* Lower-level state API used by the 4D-Var window engine: the state is the
+ * pair (h, q) of Qgm.one_step (jqgm.py:480-503). */
+/* q = h2pv(h, hb) and qb = h2pv(hb, hb) (jqgm.py:536-537). */
+vd_status vd_qg1l_init_state(const vd_qg1l_plan* plan, int batch, const void* h,
+                             const void* hb, void* q, void* qb, void* stream);
+/* nstep steps from traj slot (first_step*nstage) onwards; the starting state
+ * must already be in that slot. Writes every stage slot and the slot of the
+ * state after the last step. */
+vd_status vd_qg1l_advance(const vd_qg1l_plan* plan, int batch, void* traj,
+                          int traj_steps, int first_step, int nstep,
+                          const void* hb, const void* qb, void* work,
+                          size_t work_bytes, void* stream);
+/* Reverse of vd_qg1l_advance over the same steps: (adh, adq) holds the
+ * adjoint of the state after step first_step+nstep-1 on entry and of the
+ * state at first_step on exit. */
+vd_status vd_qg1l_advance_adj(const vd_qg1l_plan* plan, int batch,
+                              const void* traj, int traj_steps, int first_step,
+                              int nstep, void* adh, void* adq, void* work,
+                              size_t work_bytes, void* stream);
+/* adh += h2pv'(h)^T adq (adjoint of jqgm.py:536, hb fixed). */
+vd_status vd_qg1l_init_state_adj(const vd_qg1l_plan* plan, int batch,
+                                 const void* h, const void* adq, void* adh,
+                                 void* stream);
+/* Output of a step call: land -> NaN, walls -> hb, plus coef*forcing if
+ * forcing != NULL (jqgm.py:550-551 and mod.py:911-913). */
+vd_status vd_qg1l_finalize(const vd_qg1l_plan* plan, int batch, const void* h,
+                           const void* hb, const void* forcing, double coef,
+                           void* h_out, void* stream);
+
+/* Along-track observation operator (Obsop_interp_l3_jax, mapping/src/obsop.py
+ * 375-678). H is stored per observation as up to 4 (grid index, weight) pairs
+ * (index -1 = unused), already restricted to the valid neighbours of
+ * _sparse_op (obsop.py:417-460). obs_field[o] selects which field of `fields`
+ * (stride field_stride elements) observation o reads. */
+/* misfit[o] = inverr[o] * (sum_m w[o,m] x[idx[o,m]] - y[o]), NaN -> 0
+ * (obsop.py:610-628). */
+vd_status vd_obs_misfit(int dtype, int nobs, const void* fields,
+                        long long field_stride, const int32_t* obs_field,
+                        const int32_t* idx4, const void* w4, const void* yobs,
+                        const void* inverr, void* misfit, void* stream);
+/* Adjoint (obsop.py:630-678): ad[field][g] += sum over the CSR list of grid
+ * point g of w * inverr[o] * cot[o]. The CSR (rows = touched grid points,
+ * entries = observation/weight pairs) is built once on the host. */
+vd_status vd_obs_adjoint(int dtype, int npoints, void* ad_fields,
+                         long long field_stride, const int32_t* pt_field,
+                         const int32_t* pt_index, const int32_t* rowptr,
+                         const int32_t* ent_obs, const void* ent_w,
+                         const void* inverr, const void* cot, void* stream);
+
+/* Deterministic FP64 reductions (Jo, Jb, gradient norms, dot-product test,
+ * tools_4Dvar.py:265,292,326). nseg segments given by seg_off[nseg+1]. */
+vd_status vd_sumsq_f64(int dtype, int nseg, const int32_t* seg_off,
+                       const void* x, double* out, void* stream);
+/* out[s] = scale * sum over k in [seg_off[s], seg_off[s+1]) of x[perm[k]]^2
+ * (per-window Jo when observations are stored in time-major order). */
+vd_status vd_sumsq_gather_f64(int dtype, int nseg, const int32_t* seg_off,
+                              const int32_t* perm, const void* x, double scale,
+                              double* out, void* stream);
+/* out[0] = sum x*y in FP64; out must hold VD_DOT_SCRATCH doubles (the
+ * partial sums live in out[1..]) so that the call allocates nothing. */
+#define VD_DOT_SCRATCH 1025
+vd_status vd_dot_f64(int dtype, long long n, const void* x, const void* y,
+                     double* out, void* stream);
+/* y = a*x + b*y elementwise (n elements). */
+vd_status vd_axpby(int dtype, long long n, double a, const void* x, double b,
+                   void* y, void* stream);
+/* y = x (n elements of the dtype); y = value. */
+vd_status vd_copy(int dtype, long long n, const void* x, void* y, void* stream);
+vd_status vd_fill(int dtype, long long n, double value, void* y, void* stream);
+
+/* Version / build information string. */
+const char* vd_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VARDYN_GB300_H */

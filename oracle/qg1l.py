@@ -413,7 +413,8 @@ class QgmOracle:
             dq = dq + sum(b[s] * dks[s] for s in range(len(b)))
             dh = self.pv2h_tl(dq)
         dh = dh.copy()
-        dh[self.ind0] = np.nan
+        # jqgm.py:551 overwrites land with a constant (NaN): its tangent is 0
+        dh[self.ind0] = 0.0
         return dh
 
     # ---------------- adjoint ----------------

@@ -85,6 +85,7 @@ def test_tangent_matches_finite_differences(scheme):
     tl = m.step_tgl(dh, h0, hb, nstep=4)
     eps = 1e-4
     fd = (m.step(h0 + eps * dh, hb, 4) - m.step(h0 - eps * dh, hb, 4)) / (2 * eps)
+    fd[m.ind0] = 0.0    # land is overwritten with NaN: zero tangent there
     assert rel(tl, fd) < 1e-6
 
 

@@ -1,0 +1,96 @@
+"""ctypes binding of libvardyn_gb300.so (the C ABI in include/vardyn_gb300.h).
+
+There is no fallback: if the shared library is missing or a call returns a
+non-zero status, a RuntimeError is raised.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libvardyn_gb300.so")
+
+VD_F32, VD_F64 = 0, 1
+VD_EULER, VD_RK2, VD_RK3, VD_RK4 = 0, 1, 2, 3
+SCHEMES = {"Euler": VD_EULER, "euler": VD_EULER, "rk2": VD_RK2, "rk3": VD_RK3, "rk4": VD_RK4}
+DOT_SCRATCH = 1025   # doubles needed by vd_dot_f64's `out`
+
+_STATUS = {0: "VD_OK", 1: "VD_ERR_ARG", 2: "VD_ERR_CUDA", 3: "VD_ERR_WORKSPACE", 4: "VD_ERR_UNSUPPORTED"}
+
+
+class VdDesc(ctypes.Structure):
+    _fields_ = [
+        ("ny", ctypes.c_int), ("nx", ctypes.c_int), ("dtype", ctypes.c_int),
+        ("time_scheme", ctypes.c_int),
+        ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dt", ctypes.c_double),
+        ("g", ctypes.c_double), ("f", ctypes.c_double), ("c", ctypes.c_double),
+        ("Kdiffus", ctypes.c_double), ("has_Kdiffus", ctypes.c_int),
+        ("mask_host", ctypes.POINTER(ctypes.c_int8)),
+        ("beta_host", ctypes.POINTER(ctypes.c_double)),
+        ("fbathy_host", ctypes.POINTER(ctypes.c_double)),
+    ]
+
+
+P = ctypes.c_void_p
+I = ctypes.c_int
+LL = ctypes.c_longlong
+SZ = ctypes.c_size_t
+D = ctypes.c_double
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "vd_version": (ctypes.c_char_p, []),
+    "vd_qg1l_plan_create": (I, [ctypes.POINTER(P), ctypes.POINTER(VdDesc)]),
+    "vd_qg1l_plan_destroy": (I, [P]),
+    "vd_qg1l_workspace_bytes": (SZ, [P, I]),
+    "vd_qg1l_traj_bytes": (SZ, [P, I, I]),
+    "vd_qg1l_nstage": (I, [P]),
+    "vd_qg1l_h2pv": (I, [P, I, P, P, P, P]),
+    "vd_qg1l_h2uv": (I, [P, I, P, P, P, P]),
+    "vd_qg1l_rhs": (I, [P, I, P, P, P, P, P]),
+    "vd_qg1l_pv2h": (I, [P, I, P, P, P, P, P, SZ, P]),
+    "vd_qg1l_step": (I, [P, I, P, P, I, P, P, P, SZ, P]),
+    "vd_qg1l_step_tgl": (I, [P, I, P, P, P, I, P, P, SZ, P]),
+    "vd_qg1l_step_adj": (I, [P, I, P, P, P, I, P, P, I, P, SZ, P]),
+    "vd_qg1l_init_state": (I, [P, I, P, P, P, P, P]),
+    "vd_qg1l_advance": (I, [P, I, P, I, I, I, P, P, P, SZ, P]),
+    "vd_qg1l_advance_adj": (I, [P, I, P, I, I, I, P, P, P, SZ, P]),
+    "vd_qg1l_init_state_adj": (I, [P, I, P, P, P, P]),
+    "vd_qg1l_finalize": (I, [P, I, P, P, P, D, P, P]),
+    "vd_obs_misfit": (I, [I, I, P, LL, P, P, P, P, P, P, P]),
+    "vd_obs_adjoint": (I, [I, I, P, LL, P, P, P, P, P, P, P, P]),
+    "vd_sumsq_f64": (I, [I, I, P, P, P, P]),
+    "vd_sumsq_gather_f64": (I, [I, I, P, P, P, D, P, P]),
+    "vd_dot_f64": (I, [I, LL, P, P, P, P]),
+    "vd_axpby": (I, [I, LL, D, P, D, P, P]),
+    "vd_copy": (I, [I, LL, P, P, P]),
+    "vd_fill": (I, [I, LL, D, P, P]),
+}
+
+_lib = None
+
+
+def load():
+    """Load the shared library (built by vardyn_gb300.build)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: build it with `python -m vardyn_gb300.build` "
+                "(the CUDA backend has no fallback)")
+        lib = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def check(status, what):
+    if status != 0:
+        raise RuntimeError(f"{what} failed: {_STATUS.get(status, status)}")
+    return status
+
+
+def call(name, *args):
+    return check(getattr(load(), name)(*args), name)

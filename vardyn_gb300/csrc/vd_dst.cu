@@ -1,0 +1,487 @@
+// Helmholtz PV->SSH inversion on a rectangle with Dirichlet walls.
+//
+// The reference inverts g/f*lap5 - g*f/c^2 by a 2-D orthonormal DST-I,
+// division by the operator's eigenvalues and a second 2-D DST-I
+// (mapping/models/model_qg1l/jqgm.py:75-91, eigenvalues 166-172). DST-I
+// vectors are the exact eigenvectors of the 1-D Dirichlet second difference,
+// so the same solution is obtained with ONE transform direction:
+//
+//   1. DST-I along x of every interior row          (dense half-size GEMMs)
+//   2. for every x-wavenumber k, the tridiagonal system along y
+//        a*X[j-1] + b_k*X[j] + a*X[j+1] = F[j],  a = g/f/dy^2,
+//        b_k = g/f*(-2/dy^2 + mu_k) - g*f/c^2,  mu_k = 2(cos(pi(k+1)/(nx-1))-1)/dx^2
+//      (Thomas algorithm with precomputed multipliers)
+//   3. DST-I along x again (the orthonormal DST-I is its own inverse).
+//
+// DST-I even/odd split: with n = nx-2, S[p][k] = sqrt(2/(n+1)) sin(pi(p+1)(k+1)/(n+1))
+// satisfies S[n-1-p][k] = (-1)^k S[p][k], so
+//   forward:  F_even-k = (x[p] + x[n-1-p]) . Wodd,   F_odd-k = (x[p] - x[n-1-p]) . Weven
+//   inverse:  A = Xe . Wodd^T, B = Xo . Weven;  y[p] = A+B, y[n-1-p] = A-B
+// which halves the multiply-adds of a dense transform. Spectral rows are kept
+// in parity-split order: columns [0, ne) hold k = 0,2,4..., [ne, n) hold k = 1,3,...
+#include "vd_internal.cuh"
+#include <vector>
+#include <mutex>
+#include <algorithm>
+#include <cmath>
+
+namespace vd {
+
+template <typename T> struct Vec8;
+template <> struct Vec8<float> {
+    static __device__ __forceinline__ void load(const float* p, float (&r)[8]) {
+        float4 a = *reinterpret_cast<const float4*>(p);
+        float4 b = *reinterpret_cast<const float4*>(p + 4);
+        r[0] = a.x; r[1] = a.y; r[2] = a.z; r[3] = a.w;
+        r[4] = b.x; r[5] = b.y; r[6] = b.z; r[7] = b.w;
+    }
+};
+template <> struct Vec8<double> {
+    static __device__ __forceinline__ void load(const double* p, double (&r)[8]) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            double2 a = reinterpret_cast<const double2*>(p)[i];
+            r[2 * i] = a.x; r[2 * i + 1] = a.y;
+        }
+    }
+};
+
+struct GemmGeom {
+    int n, ne, no, my, nx;
+    long long fs;
+    int R;          // rows = nfields * my
+    int kpad, ldw, lds;
+};
+
+enum { MODE_FWD = 0, MODE_INV = 1 };
+
+template <int TR> struct GemmShape {
+    static constexpr int NT = 2 * (TR / 8) * 16;   // threads per CTA
+};
+
+template <typename T, int TR>
+__host__ __device__ constexpr size_t gemm_smem_elems(int kpad) {
+    return size_t(2) * kpad * TR +
+           (size_t(2) * DST_KC * DST_NC > size_t(TR) * DST_NC ? size_t(2) * DST_KC * DST_NC
+                                                              : size_t(TR) * DST_NC);
+}
+
+// One CTA: TR interior rows x DST_NC output columns of BOTH halves.
+// Threads [0, NT/2) multiply by W1 (the even-k half), [NT/2, NT) by W2.
+template <typename T, int TR, int MODE, int EPI>
+__global__ void __launch_bounds__(GemmShape<TR>::NT)
+dst_gemm_kernel(GemmGeom g, const T* __restrict__ W1, const T* __restrict__ W2,
+                const T* __restrict__ src, const T* __restrict__ sub, int sub_batches,
+                T* __restrict__ spec, T* __restrict__ out, const T* __restrict__ add,
+                int add_batches, const int8_t* __restrict__ mask)
+{
+    constexpr int NT = GemmShape<TR>::NT;
+    constexpr int NC = DST_NC;
+    constexpr int KC = DST_KC;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* As = reinterpret_cast<T*>(smem_raw);
+    T* Bs = As + size_t(g.kpad) * TR;
+    T* Ws = Bs + size_t(g.kpad) * TR;     // W1 chunk | W2 chunk, later the exchange tile
+    T* W1s = Ws;
+    T* W2s = Ws + KC * NC;
+
+    const int tid = threadIdx.x;
+    const int row0 = blockIdx.y * TR;
+    const int c0 = blockIdx.x * NC;
+    const int n = g.n, ne = g.ne, no = g.no, my = g.my;
+
+    // ---- prologue: operands, transposed to [k][row] -------------------------
+    for (int idx = tid; idx < g.kpad * TR; idx += NT) {
+        const int r = idx % TR;
+        const int p = idx / TR;
+        const int row = row0 + r;
+        T a = T(0), b = T(0);
+        if (row < g.R) {
+            if (MODE == MODE_FWD) {
+                if (p < ne) {
+                    const int f = row / my;
+                    const int j = row - f * my + 1;
+                    const T* s = src + f * g.fs + (long long)j * g.nx + 1;
+                    const T* sb = (sub != nullptr && f < sub_batches)
+                                      ? sub + f * g.fs + (long long)j * g.nx + 1 : nullptr;
+                    T x1 = s[p];
+                    if (sb) x1 -= sb[p];
+                    if (p < no) {
+                        T x2 = s[n - 1 - p];
+                        if (sb) x2 -= sb[n - 1 - p];
+                        a = x1 + x2;
+                        b = x1 - x2;
+                    } else {
+                        a = x1;   // middle point of an odd-length transform
+                    }
+                }
+            } else {
+                const T* s = spec + (long long)row * g.lds;
+                if (p < ne) a = s[p];
+                if (p < no) b = s[ne + p];
+            }
+        }
+        As[p * TR + r] = a;
+        Bs[p * TR + r] = b;
+    }
+
+    const int grp = tid / (NT / 2);
+    const int lt = tid % (NT / 2);
+    const int ty = lt / 16;
+    const int tx = lt % 16;
+    const T* Aop = grp == 0 ? As : Bs;
+    const T* Wop = grp == 0 ? W1s : W2s;
+
+    T acc[8][8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = T(0);
+
+    for (int k0 = 0; k0 < g.kpad; k0 += KC) {
+        __syncthreads();
+        for (int e = tid; e < KC * NC; e += NT) {
+            const int kk = e / NC;
+            const int cc = e - kk * NC;
+            const size_t goff = size_t(k0 + kk) * g.ldw + c0 + cc;
+            W1s[e] = W1[goff];
+            W2s[e] = W2[goff];
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int kk = 0; kk < KC; ++kk) {
+            T a[8], w[8];
+            Vec8<T>::load(Aop + (k0 + kk) * TR + ty * 8, a);
+            Vec8<T>::load(Wop + kk * NC + tx * 8, w);
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+#pragma unroll
+                for (int j = 0; j < 8; ++j) acc[i][j] = fma(a[i], w[j], acc[i][j]);
+        }
+    }
+
+    const int rb = row0 + ty * 8;
+    const int cb = c0 + tx * 8;
+    if (MODE == MODE_FWD) {
+        const int lim = grp == 0 ? ne : no;
+        const int coff = grp == 0 ? 0 : ne;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            const int row = rb + i;
+            if (row >= g.R) continue;
+            T* d = spec + (long long)row * g.lds + coff;
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int t = cb + j;
+                if (t < lim) d[t] = acc[i][j];
+            }
+        }
+    } else {
+        __syncthreads();
+        T* X = Ws;   // [TR][NC] exchange tile
+        if (grp == 1) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+#pragma unroll
+                for (int j = 0; j < 8; ++j) X[(ty * 8 + i) * NC + tx * 8 + j] = acc[i][j];
+        }
+        __syncthreads();
+        if (grp == 0) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int row = rb + i;
+                if (row >= g.R) continue;
+                const int f = row / my;
+                const int j = row - f * my + 1;
+                const long long base = f * g.fs + (long long)j * g.nx + 1;
+#pragma unroll
+                for (int jj = 0; jj < 8; ++jj) {
+                    const int p = cb + jj;
+                    if (p >= ne) continue;
+                    const T A = acc[i][jj];
+                    const T B = (p < no) ? X[(ty * 8 + i) * NC + tx * 8 + jj] : T(0);
+                    const int ps[2] = {p, n - 1 - p};
+                    const T ys[2] = {A + B, A - B};
+                    const int cnt = (p < no) ? 2 : 1;
+                    for (int u = 0; u < cnt; ++u) {
+                        const long long o = base + ps[u];
+                        if (EPI == EPI_H) {
+                            T y = ys[u];
+                            if (add != nullptr && f < add_batches) y += add[o];
+                            out[o] = y;
+                        } else {
+                            const int mi = j * g.nx + 1 + ps[u];
+                            out[o] = (mask[mi] == 3) ? ys[u] + add[o] : T(0);
+                        }
+                    }
+                }
+            }
+        }
+    }
+}
+
+// Thomas algorithm along y for 32 spectral columns of one field per CTA. The
+// column block is staged in shared memory; one warp runs the recurrences.
+template <typename T>
+__global__ void __launch_bounds__(128)
+tridiag_kernel(T* __restrict__ spec, const T* __restrict__ trim, int my, int n, int lds, T a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* F = reinterpret_cast<T*>(smem_raw);   // [my][32]
+    const int f = blockIdx.y;
+    const int t0 = blockIdx.x * 32;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    T* S = spec + (long long)f * my * lds;
+    const int t = t0 + tx;
+    for (int j = ty; j < my; j += 4) F[j * 32 + tx] = (t < n) ? S[(long long)j * lds + t] : T(0);
+    __syncthreads();
+    if (ty == 0 && t < n) {
+        const T* M = trim + t;
+        T d = F[tx] * __ldg(M);
+        F[tx] = d;
+#pragma unroll 8
+        for (int j = 1; j < my; ++j) {
+            const T m = __ldg(M + (long long)j * lds);
+            d = (F[j * 32 + tx] - a * d) * m;
+            F[j * 32 + tx] = d;
+        }
+        T x = d;
+#pragma unroll 8
+        for (int j = my - 2; j >= 0; --j) {
+            const T m = __ldg(M + (long long)j * lds);
+            x = F[j * 32 + tx] - a * m * x;
+            F[j * 32 + tx] = x;
+        }
+    }
+    __syncthreads();
+    if (t < n)
+        for (int j = ty; j < my; j += 4) S[(long long)j * lds + t] = F[j * 32 + tx];
+}
+
+// Same recurrences directly on the spectral buffer, for column blocks too tall
+// for shared memory (float64 at the largest grids).
+template <typename T>
+__global__ void __launch_bounds__(32)
+tridiag_global_kernel(T* __restrict__ spec, const T* __restrict__ trim, int my, int n, int lds, T a)
+{
+    const int f = blockIdx.y;
+    const int t = blockIdx.x * 32 + threadIdx.x;
+    if (t >= n) return;
+    T* S = spec + (long long)f * my * lds + t;
+    const T* M = trim + t;
+    T d = S[0] * __ldg(M);
+    S[0] = d;
+    for (int j = 1; j < my; ++j) {
+        d = (S[(long long)j * lds] - a * d) * __ldg(M + (long long)j * lds);
+        S[(long long)j * lds] = d;
+    }
+    T x = d;
+    for (int j = my - 2; j >= 0; --j) {
+        x = S[(long long)j * lds] - a * __ldg(M + (long long)j * lds) * x;
+        S[(long long)j * lds] = x;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+size_t spec_bytes(const vd_qg1l_plan* p, int nf)
+{
+    return size_t(nf) * p->dst.my * p->dst.lds * elem_size(p->d.dtype);
+}
+
+template <typename T>
+static int upload(const std::vector<double>& h, void** d)
+{
+    std::vector<T> tmp(h.begin(), h.end());
+    VD_CUDA_TRY(cudaMalloc(d, tmp.size() * sizeof(T)));
+    VD_CUDA_TRY(cudaMemcpy(*d, tmp.data(), tmp.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return VD_OK;
+}
+
+int build_dst_tables(vd_qg1l_plan* p)
+{
+    DSTTables& t = p->dst;
+    const int n = p->d.nx - 2;
+    const int my = p->d.ny - 2;
+    t.n = n;
+    t.my = my;
+    t.no = n / 2;
+    t.ne = n - t.no;
+    t.ncol_tiles = (t.ne + DST_NC - 1) / DST_NC;
+    t.kpad = ((t.ne + DST_KC - 1) / DST_KC) * DST_KC;
+    t.ldw = t.ncol_tiles * DST_NC;
+    t.lds = ((n + 3) / 4) * 4;
+
+    const double scale = std::sqrt(2.0 / (n + 1));
+    const long long period = 2LL * (n + 1);   // sin(pi*m/(n+1)) has period 2(n+1) in m
+    auto s = [&](long long m) {
+        m %= period;
+        return scale * std::sin(M_PI * double(m) / double(n + 1));
+    };
+    std::vector<double> wodd(size_t(t.kpad) * t.ldw, 0.0), woddT(wodd.size(), 0.0),
+        weven(wodd.size(), 0.0);
+    for (int a = 0; a < t.ne; ++a)
+        for (int b = 0; b < t.ne; ++b) {
+            const double v = s((long long)(a + 1) * (2 * b + 1));
+            wodd[size_t(a) * t.ldw + b] = v;
+            woddT[size_t(b) * t.ldw + a] = v;
+        }
+    for (int a = 0; a < t.no; ++a)
+        for (int b = 0; b < t.no; ++b)
+            weven[size_t(a) * t.ldw + b] = s((long long)(a + 1) * (2 * b + 2));
+
+    // Thomas multipliers per spectral column (parity-split order)
+    const double gf = p->d.g / p->d.f;
+    const double gfc2 = p->d.g * p->d.f / (p->d.c * p->d.c);
+    const double dx = p->d.dx, dy = p->d.dy;
+    const double a = gf / (dy * dy);
+    t.tri_a = a;
+    std::vector<double> trim(size_t(my) * t.lds, 0.0);
+    for (int col = 0; col < n; ++col) {
+        const int k = col < t.ne ? 2 * col : 2 * (col - t.ne) + 1;   // 0-based wavenumber
+        const double mu = 2.0 * (std::cos(M_PI / (p->d.nx - 1) * (k + 1)) - 1.0) / (dx * dx);
+        const double bk = gf * (-2.0 / (dy * dy) + mu) - gfc2;
+        double c_prev = 0.0;
+        for (int j = 0; j < my; ++j) {
+            const double m = 1.0 / (bk - a * c_prev);
+            trim[size_t(j) * t.lds + col] = m;
+            c_prev = a * m;
+        }
+    }
+    int rc;
+    if (p->d.dtype == VD_F32) {
+        if ((rc = upload<float>(wodd, &t.Wodd))) return rc;
+        if ((rc = upload<float>(woddT, &t.WoddT))) return rc;
+        if ((rc = upload<float>(weven, &t.Weven))) return rc;
+        if ((rc = upload<float>(trim, &t.trim))) return rc;
+    } else {
+        if ((rc = upload<double>(wodd, &t.Wodd))) return rc;
+        if ((rc = upload<double>(woddT, &t.WoddT))) return rc;
+        if ((rc = upload<double>(weven, &t.Weven))) return rc;
+        if ((rc = upload<double>(trim, &t.trim))) return rc;
+    }
+    return VD_OK;
+}
+
+void free_dst_tables(vd_qg1l_plan* p)
+{
+    cudaFree(p->dst.Wodd);
+    cudaFree(p->dst.WoddT);
+    cudaFree(p->dst.Weven);
+    cudaFree(p->dst.trim);
+}
+
+template <typename T, int TR>
+static cudaError_t set_smem_attrs()
+{
+    const int maxb = 227 * 1024;
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(dst_gemm_kernel<T, TR, MODE_FWD, EPI_H>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, maxb))) return e;
+    if ((e = cudaFuncSetAttribute(dst_gemm_kernel<T, TR, MODE_INV, EPI_H>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, maxb))) return e;
+    return cudaFuncSetAttribute(dst_gemm_kernel<T, TR, MODE_INV, EPI_ADJQ>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, maxb);
+}
+
+static std::once_flag g_attr_once;
+static cudaError_t g_attr_err = cudaSuccess;
+
+static cudaError_t configure_kernels()
+{
+    std::call_once(g_attr_once, [] {
+        cudaError_t e = cudaSuccess;
+        if (!e) e = set_smem_attrs<float, 16>();
+        if (!e) e = set_smem_attrs<float, 32>();
+        if (!e) e = set_smem_attrs<float, 64>();
+        if (!e) e = set_smem_attrs<double, 16>();
+        if (!e) e = set_smem_attrs<double, 32>();
+        if (!e) e = cudaFuncSetAttribute(tridiag_kernel<float>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        if (!e) e = cudaFuncSetAttribute(tridiag_kernel<double>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        g_attr_err = e;
+    });
+    return g_attr_err;
+}
+
+template <typename T, int TR>
+static int launch_pair(const vd_qg1l_plan* p, const GemmGeom& g, const SolveArgs& a,
+                       T* spec, cudaStream_t st, bool fwd)
+{
+    const DSTTables& t = p->dst;
+    constexpr int NT = GemmShape<TR>::NT;
+    const size_t smem = gemm_smem_elems<T, TR>(g.kpad) * sizeof(T);
+    dim3 grid(t.ncol_tiles, (g.R + TR - 1) / TR);
+    if (fwd) {
+        dst_gemm_kernel<T, TR, MODE_FWD, EPI_H><<<grid, NT, smem, st>>>(
+            g, (const T*)t.Wodd, (const T*)t.Weven, (const T*)a.src, (const T*)a.sub,
+            a.sub_batches, spec, nullptr, nullptr, 0, nullptr);
+    } else if (a.epi == EPI_H) {
+        dst_gemm_kernel<T, TR, MODE_INV, EPI_H><<<grid, NT, smem, st>>>(
+            g, (const T*)t.WoddT, (const T*)t.Weven, nullptr, nullptr, 0, spec, (T*)a.out,
+            (const T*)a.add, a.add_batches, p->d_mask);
+    } else {
+        dst_gemm_kernel<T, TR, MODE_INV, EPI_ADJQ><<<grid, NT, smem, st>>>(
+            g, (const T*)t.WoddT, (const T*)t.Weven, nullptr, nullptr, 0, spec, (T*)a.out,
+            (const T*)a.add, a.add_batches, p->d_mask);
+    }
+    VD_LAUNCH_CHECK();
+    return VD_OK;
+}
+
+// Rows per CTA: the largest tile that still gives about two waves of CTAs on
+// the 152 SMs and fits shared memory.
+template <typename T>
+static int pick_tr(const vd_qg1l_plan* p, int R)
+{
+    const DSTTables& t = p->dst;
+    const int cand[3] = {64, 32, 16};
+    for (int c : cand) {
+        if (sizeof(T) == 8 && c == 64) continue;
+        const size_t smem = (size_t(2) * t.kpad * c + size_t(std::max(2 * DST_KC * DST_NC, c * DST_NC))) * sizeof(T);
+        if (smem > 200 * 1024) continue;
+        const long long ctas = (long long)t.ncol_tiles * ((R + c - 1) / c);
+        if (ctas >= 2 * 152) return c;
+    }
+    return 16;
+}
+
+template <typename T>
+int helmholtz_solve(const vd_qg1l_plan* p, int nf, const SolveArgs& a, T* spec, cudaStream_t st)
+{
+    if (configure_kernels() != cudaSuccess) return VD_ERR_CUDA;
+    const DSTTables& t = p->dst;
+    GemmGeom g;
+    g.n = t.n; g.ne = t.ne; g.no = t.no; g.my = t.my; g.nx = p->d.nx;
+    g.fs = (long long)p->d.ny * p->d.nx;
+    g.R = nf * t.my;
+    g.kpad = t.kpad; g.ldw = t.ldw; g.lds = t.lds;
+    const int tr = pick_tr<T>(p, g.R);
+    int rc;
+    auto run = [&](bool fwd) -> int {
+        if constexpr (sizeof(T) == 4) {
+            if (tr == 64) return launch_pair<T, 64>(p, g, a, spec, st, fwd);
+        }
+        if (tr == 32) return launch_pair<T, 32>(p, g, a, spec, st, fwd);
+        return launch_pair<T, 16>(p, g, a, spec, st, fwd);
+    };
+    if ((rc = run(true))) return rc;
+    dim3 tgrid((t.n + 31) / 32, nf);
+    const size_t tsmem = size_t(t.my) * 32 * sizeof(T);
+    if (tsmem <= 200 * 1024) {
+        tridiag_kernel<T><<<tgrid, dim3(32, 4), tsmem, st>>>(
+            spec, (const T*)t.trim, t.my, t.n, t.lds, (T)t.tri_a);
+    } else {
+        tridiag_global_kernel<T><<<tgrid, 32, 0, st>>>(
+            spec, (const T*)t.trim, t.my, t.n, t.lds, (T)t.tri_a);
+    }
+    VD_LAUNCH_CHECK();
+    return run(false);
+}
+
+template int helmholtz_solve<float>(const vd_qg1l_plan*, int, const SolveArgs&, float*, cudaStream_t);
+template int helmholtz_solve<double>(const vd_qg1l_plan*, int, const SolveArgs&, double*, cudaStream_t);
+
+}  // namespace vd

@@ -1,0 +1,113 @@
+// Internal declarations shared by the translation units of libvardyn_gb300.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+#include <math.h>
+#include "../../include/vardyn_gb300.h"
+
+#define VD_CUDA_TRY(expr)                                  \
+    do {                                                   \
+        cudaError_t _e = (expr);                           \
+        if (_e != cudaSuccess) return VD_ERR_CUDA;         \
+    } while (0)
+
+#define VD_LAUNCH_CHECK() VD_CUDA_TRY(cudaGetLastError())
+
+namespace vd {
+
+// ---------------------------------------------------------------------------
+// Grid constants passed to every QG kernel by value.
+// ---------------------------------------------------------------------------
+struct QGGeom {
+    int ny, nx;
+    long long fs;            // field stride = ny*nx
+    double gf;               // g/f
+    double gfc2;             // g*f/c^2
+    double cu;               // -g/f/(4 dy)   (u = cu * 4-point y-difference)
+    double cv;               //  g/f/(4 dx)
+    double cx, cy;           // 1/(6 dx), 1/(6 dy)
+    double idx2, idy2;       // 1/dx^2, 1/dy^2
+    double Kx, Ky;           // Kdiffus/dx^2, Kdiffus/dy^2 (0 when absent)
+    int hasK;
+    const int8_t* mask;      // [ny][nx]
+    const void* beta;        // T[ny][nx] or nullptr
+    const void* fB;          // T[ny][nx] or nullptr
+};
+
+// DST-I / tridiagonal tables of one grid (typed by the plan dtype).
+struct DSTTables {
+    int n;        // interior columns = nx-2 (transform length)
+    int my;       // interior rows = ny-2 (tridiagonal length)
+    int ne, no;   // odd-output / even-output counts (ne = ceil(n/2), no = floor(n/2))
+    int ncol_tiles;  // ceil(ne / DST_NC)
+    int kpad;     // rows of the half matrices, padded to DST_KC
+    int ldw;      // padded columns of the half matrices = ncol_tiles*DST_NC
+    int lds;      // leading dimension of the spectral buffer
+    void* Wodd;   // [kpad][ldw]  Wodd[p][t] = c sin(pi (p+1)(2t+1)/(n+1))
+    void* WoddT;  // [kpad][ldw]  transpose of Wodd
+    void* Weven;  // [kpad][ldw]  Weven[p][t] = c sin(pi (p+1)(2t+2)/(n+1)) (symmetric)
+    void* trim;   // [my][lds] Thomas multipliers m_j per spectral column
+    double tri_a; // off-diagonal g/f/dy^2
+};
+
+constexpr int DST_NC = 128;   // output columns per CTA tile
+constexpr int DST_KC = 16;    // k rows per shared-memory chunk of the half matrices
+
+// Epilogue kinds of the inverse transform
+enum InvEpilogue { EPI_H = 0, EPI_ADJQ = 1 };
+
+struct SolveArgs {
+    // forward (physical -> spectral): x = src - sub over the interior
+    const void* src;
+    const void* sub;     // nullable; used for batches < sub_batches
+    int sub_batches;
+    // inverse (spectral -> physical)
+    void* out;
+    const void* add;     // EPI_H: hb (used for batches < add_batches); EPI_ADJQ: addend field
+    int add_batches;
+    int epi;
+};
+
+}  // namespace vd
+
+struct vd_qg1l_plan {
+    vd_qg1l_desc d;
+    int nstage;
+    double A[4][4];      // Butcher matrix with dt folded in
+    double b[4];
+    vd::QGGeom geom;     // device pointers inside
+    vd::DSTTables dst;
+    int8_t* d_mask;
+    void* d_beta;
+    void* d_fB;
+    int device;
+};
+
+namespace vd {
+
+size_t elem_size(int dtype);
+
+// Helmholtz solve over `nf` fields (each [ny][nx]), spectral scratch `spec`.
+template <typename T>
+int helmholtz_solve(const vd_qg1l_plan* p, int nf, const SolveArgs& a, T* spec,
+                    cudaStream_t st);
+
+size_t spec_bytes(const vd_qg1l_plan* p, int nf);
+int build_dst_tables(vd_qg1l_plan* p);
+void free_dst_tables(vd_qg1l_plan* p);
+
+// Bump allocator over a caller workspace.
+struct Arena {
+    char* base;
+    size_t cap;
+    size_t off;
+    void* take(size_t bytes) {
+        size_t a = (off + 255) & ~size_t(255);
+        if (a + bytes > cap) return nullptr;
+        off = a + bytes;
+        return base + a;
+    }
+};
+
+}  // namespace vd

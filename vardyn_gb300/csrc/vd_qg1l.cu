@@ -1,0 +1,683 @@
+// QG 1.5-layer model kernels: SSH->PV, the fused Runge-Kutta stage (geostrophic
+// velocities, 3rd-order upwind PV advection, beta, bathymetry and diffusion
+// terms, masks, stage combination), its tangent-linear and adjoint, and the
+// host-side drivers that chain them with the Helmholtz solve.
+//
+// Reference: mapping/models/model_qg1l/jqgm.py, class Qgm — h2uv 238-262,
+// h2pv 264-293, rhs 321-375, adv 377-396, euler/rk2/rk3 398-477,
+// one_step 480-503, step 517-557, step_tgl/step_adj 559-569.
+//
+// Masks. mask==3 ("M3") marks the points where the PV tendency is computed
+// (jqgm.py:372-373 zero it on mask 1/2 and on land); they lie in rows/cols
+// 2..n-4 and have no land within two cells (jqgm.py:196-211). Consequently the
+// NaN guards on u, v (jqgm.py:259-260) never act on a value that reaches an M3
+// tendency unless the caller's SSH holds NaN away from the land of the mask;
+// the adjoint kernels rely on this and omit the u, v guard.
+#include "vd_internal.cuh"
+
+namespace vd {
+
+template <typename T> __device__ __forceinline__ T guard0(T x) { return isnan(x) ? T(0) : x; }
+
+template <typename T>
+struct Cross {
+    T c, e1, e2, w1, w2, n1, n2, s1, s2;   // (j,i), (j,i+1), (j,i+2), (j,i-1), ... (j-1,i), (j-2,i)
+    __device__ __forceinline__ void load(const T* __restrict__ p, int nx) {
+        c = p[0]; e1 = p[1]; e2 = p[2]; w1 = p[-1]; w2 = p[-2];
+        n1 = p[nx]; n2 = p[2 * nx]; s1 = p[-nx]; s2 = p[-2 * nx];
+    }
+    __device__ __forceinline__ void add(const Cross& o) {
+        c += o.c; e1 += o.e1; e2 += o.e2; w1 += o.w1; w2 += o.w2;
+        n1 += o.n1; n2 += o.n2; s1 += o.s1; s2 += o.s2;
+    }
+    __device__ __forceinline__ T Dpx() const { return T(2) * e1 + T(3) * c - T(6) * w1 + w2; }
+    __device__ __forceinline__ T Dmx() const { return e2 - T(6) * e1 + T(3) * c + T(2) * w1; }
+    __device__ __forceinline__ T Dpy() const { return T(2) * n1 + T(3) * c - T(6) * s1 + s2; }
+    __device__ __forceinline__ T Dmy() const { return n2 - T(6) * n1 + T(3) * c + T(2) * s1; }
+};
+
+// Staggered velocities around T point (j,i): u(j,i), u(j,i+1), v(j,i), v(j+1,i)
+template <typename T>
+struct Vel {
+    T u0, u1, v0, v1;
+    __device__ __forceinline__ void load(const QGGeom& G, const T* __restrict__ hc) {
+        const int nx = G.nx;
+        const T hn_w = hc[nx - 1], hn_c = hc[nx], hn_e = hc[nx + 1];
+        const T hs_w = hc[-nx - 1], hs_c = hc[-nx], hs_e = hc[-nx + 1];
+        const T h_w = hc[-1], h_e = hc[1];
+        const T cu = T(G.cu), cv = T(G.cv);
+        u0 = cu * (hn_w + hn_c - hs_c - hs_w);
+        u1 = cu * (hn_c + hn_e - hs_e - hs_c);
+        v0 = cv * (h_e + hs_e - hs_w - h_w);
+        v1 = cv * (hn_e + h_e - h_w - hn_w);
+    }
+};
+
+// Raw PV tendency at an M3 point from velocities and PV crosses.
+template <typename T>
+__device__ __forceinline__ T tendency(const QGGeom& G, const Vel<T>& V, const Cross<T>& qa,
+                                      const Cross<T>& q, T beta)
+{
+    const T uT = T(0.5) * (V.u0 + V.u1);
+    const T vT = T(0.5) * (V.v0 + V.v1);
+    const T up = uT < T(0) ? T(0) : uT;
+    const T um = uT > T(0) ? T(0) : uT;
+    const T vp = vT < T(0) ? T(0) : vT;
+    const T vm = vT > T(0) ? T(0) : vT;
+    const T cx = T(G.cx), cy = T(G.cy);
+    T r = -up * cx * qa.Dpx() + um * cx * qa.Dmx() - vp * cy * qa.Dpy() + vm * cy * qa.Dmy();
+    r -= beta * ((V.v0 + V.v1) / T(2));
+    if (G.hasK)
+        r += T(G.Kx) * (q.e1 + q.w1 - T(2) * q.c) + T(G.Ky) * (q.n1 + q.s1 - T(2) * q.c);
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// h2pv (jqgm.py:264-293). Fields f >= ntan0 are tangents: their ring value is
+// 0 (hb fixed) and their NaN guard follows the primal field f - ntan0.
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T lap_helm(const QGGeom& G, const T* __restrict__ hc)
+{
+    const int nx = G.nx;
+    const T c = hc[0];
+    return T(G.gf) * ((hc[nx] + hc[-nx] - T(2) * c) * T(G.idy2) +
+                      (hc[1] + hc[-1] - T(2) * c) * T(G.idx2)) - T(G.gfc2) * c;
+}
+
+template <typename T>
+__global__ void k_h2pv(QGGeom G, int nf, int ntan0, const T* __restrict__ h,
+                       const T* __restrict__ hb, T* __restrict__ q)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int f = blockIdx.z;
+    if (i >= G.nx || j >= G.ny || f >= nf) return;
+    const long long o = f * G.fs + (long long)j * G.nx + i;
+    const int m = G.mask[j * G.nx + i];
+    T val = T(0);
+    if (m == 3) {
+        val = lap_helm<T>(G, h + o);
+        if (f >= ntan0) {
+            const T prim = lap_helm<T>(G, h + o - ntan0 * G.fs);
+            if (isnan(prim)) val = T(0);
+        } else {
+            val = guard0(val);
+        }
+    } else if (m != 0 && f < ntan0) {
+        val = -T(G.gfc2) * hb[o];
+    }
+    q[o] = val;
+}
+
+// adh += (d h2pv / d h)^T adq, masked to M3 points whose primal PV was finite.
+template <typename T>
+__global__ void k_h2pv_adj(QGGeom G, int nf, const T* __restrict__ h, const T* __restrict__ adq,
+                           T* __restrict__ adh)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int f = blockIdx.z;
+    if (i >= G.nx || j >= G.ny || f >= nf) return;
+    const long long o = f * G.fs + (long long)j * G.nx + i;
+    const T gfy = T(G.gf) * T(G.idy2), gfx = T(G.gf) * T(G.idx2);
+    const int di[5] = {0, 1, -1, 0, 0};
+    const int dj[5] = {0, 0, 0, 1, -1};
+    T acc = T(0);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+        const int jj = j + dj[k], ii = i + di[k];
+        if (jj < 0 || jj >= G.ny || ii < 0 || ii >= G.nx) continue;
+        if (G.mask[jj * G.nx + ii] != 3) continue;
+        const long long po = f * G.fs + (long long)jj * G.nx + ii;
+        if (isnan(lap_helm<T>(G, h + po))) continue;
+        const T coef = (k == 0) ? (-T(2) * gfy - T(2) * gfx - T(G.gfc2)) : (k < 3 ? gfx : gfy);
+        acc += coef * adq[po];
+    }
+    adh[o] += acc;
+}
+
+// ---------------------------------------------------------------------------
+// Forward stage: k = rhs(h2uv(hs), qs); qout = qbase + sum_i cin[i] k_i + cself k
+// ---------------------------------------------------------------------------
+template <typename T>
+struct StageIn {
+    const T* k[4];
+    T c[4];
+    int nk;
+};
+
+template <typename T>
+__global__ void k_stage_fwd(QGGeom G, int nf, const T* __restrict__ hs, const T* __restrict__ qs,
+                            const T* __restrict__ qbase, StageIn<T> kin, T cself,
+                            T* __restrict__ kout, T* __restrict__ qout)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int f = blockIdx.z;
+    if (i >= G.nx || j >= G.ny || f >= nf) return;
+    const long long o = f * G.fs + (long long)j * G.nx + i;
+    const long long go = (long long)j * G.nx + i;
+    T r = T(0);
+    if (G.mask[go] == 3) {
+        Vel<T> V;
+        V.load(G, hs + o);
+        V.u0 = guard0(V.u0); V.u1 = guard0(V.u1); V.v0 = guard0(V.v0); V.v1 = guard0(V.v1);
+        Cross<T> q;
+        q.load(qs + o, G.nx);
+        Cross<T> qa = q;
+        if (G.fB) { Cross<T> b; b.load((const T*)G.fB + go, G.nx); qa.add(b); }
+        const T beta = G.beta ? ((const T*)G.beta)[go] : T(0);
+        r = guard0(tendency<T>(G, V, qa, q, beta));
+    }
+    T acc = qbase[o];
+    for (int t = 0; t < kin.nk; ++t) acc += kin.c[t] * kin.k[t][o];
+    acc += cself * r;
+    qout[o] = acc;
+    if (kout) kout[o] = r;
+}
+
+// Tangent stage on dual arrays: fields [0, B) primal, [B, 2B) tangent.
+template <typename T>
+__global__ void k_stage_tl(QGGeom G, int B, const T* __restrict__ hs, const T* __restrict__ qs,
+                           const T* __restrict__ qbase, StageIn<T> kin, T cself,
+                           T* __restrict__ kout, T* __restrict__ qout)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int f = blockIdx.z;
+    if (i >= G.nx || j >= G.ny || f >= B) return;
+    const long long o = f * G.fs + (long long)j * G.nx + i;
+    const long long od = o + B * G.fs;
+    const long long go = (long long)j * G.nx + i;
+    T r = T(0), dr = T(0);
+    if (G.mask[go] == 3) {
+        Vel<T> V, dV;
+        V.load(G, hs + o);
+        dV.load(G, hs + od);
+        if (isnan(V.u0)) { V.u0 = T(0); dV.u0 = T(0); }
+        if (isnan(V.u1)) { V.u1 = T(0); dV.u1 = T(0); }
+        if (isnan(V.v0)) { V.v0 = T(0); dV.v0 = T(0); }
+        if (isnan(V.v1)) { V.v1 = T(0); dV.v1 = T(0); }
+        Cross<T> q, dq;
+        q.load(qs + o, G.nx);
+        dq.load(qs + od, G.nx);
+        Cross<T> qa = q;
+        if (G.fB) { Cross<T> b; b.load((const T*)G.fB + go, G.nx); qa.add(b); }
+        const T beta = G.beta ? ((const T*)G.beta)[go] : T(0);
+        const T raw = tendency<T>(G, V, qa, q, beta);
+        if (!isnan(raw)) {
+            r = raw;
+            const T uT = T(0.5) * (V.u0 + V.u1), vT = T(0.5) * (V.v0 + V.v1);
+            const T duT = T(0.5) * (dV.u0 + dV.u1), dvT = T(0.5) * (dV.v0 + dV.v1);
+            const T up = uT < T(0) ? T(0) : uT, um = uT > T(0) ? T(0) : uT;
+            const T vp = vT < T(0) ? T(0) : vT, vm = vT > T(0) ? T(0) : vT;
+            const T dup = uT < T(0) ? T(0) : duT, dum = uT > T(0) ? T(0) : duT;
+            const T dvp = vT < T(0) ? T(0) : dvT, dvm = vT > T(0) ? T(0) : dvT;
+            const T cx = T(G.cx), cy = T(G.cy);
+            dr = -dup * cx * qa.Dpx() + dum * cx * qa.Dmx() - dvp * cy * qa.Dpy() + dvm * cy * qa.Dmy()
+                 - up * cx * dq.Dpx() + um * cx * dq.Dmx() - vp * cy * dq.Dpy() + vm * cy * dq.Dmy();
+            dr -= beta * ((dV.v0 + dV.v1) / T(2));
+            if (G.hasK)
+                dr += T(G.Kx) * (dq.e1 + dq.w1 - T(2) * dq.c) + T(G.Ky) * (dq.n1 + dq.s1 - T(2) * dq.c);
+        }
+    }
+    T acc = qbase[o], dacc = qbase[od];
+    for (int t = 0; t < kin.nk; ++t) {
+        acc += kin.c[t] * kin.k[t][o];
+        dacc += kin.c[t] * kin.k[t][od];
+    }
+    qout[o] = acc + cself * r;
+    qout[od] = dacc + cself * dr;
+    if (kout) { kout[o] = r; kout[od] = dr; }
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint stage, phase A (per M3 point P): lk = sum_t c_t G_t(P);
+//   AUT(P) = d J / d uT(P), AVT(P) = d J / d vT(P) (incl. beta), and the
+//   primal uT, vT for phase B. Non-M3 points get zeros.
+// ---------------------------------------------------------------------------
+template <typename T>
+struct AdjTemps {
+    T* lk; T* ut; T* vt; T* aut; T* avt;
+};
+
+template <typename T>
+__global__ void k_adj_phaseA(QGGeom G, int nf, const T* __restrict__ hs, const T* __restrict__ qs,
+                             StageIn<T> gin, AdjTemps<T> W)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int f = blockIdx.z;
+    if (i >= G.nx || j >= G.ny || f >= nf) return;
+    const long long o = f * G.fs + (long long)j * G.nx + i;
+    const long long go = (long long)j * G.nx + i;
+    T lk = T(0), uT = T(0), vT = T(0), aut = T(0), avt = T(0);
+    if (G.mask[go] == 3) {
+        for (int t = 0; t < gin.nk; ++t) lk += gin.c[t] * gin.k[t][o];
+        Vel<T> V;
+        V.load(G, hs + o);
+        V.u0 = guard0(V.u0); V.u1 = guard0(V.u1); V.v0 = guard0(V.v0); V.v1 = guard0(V.v1);
+        Cross<T> q;
+        q.load(qs + o, G.nx);
+        Cross<T> qa = q;
+        if (G.fB) { Cross<T> b; b.load((const T*)G.fB + go, G.nx); qa.add(b); }
+        const T beta = G.beta ? ((const T*)G.beta)[go] : T(0);
+        if (isnan(tendency<T>(G, V, qa, q, beta))) lk = T(0);
+        uT = T(0.5) * (V.u0 + V.u1);
+        vT = T(0.5) * (V.v0 + V.v1);
+        const T cx = T(G.cx), cy = T(G.cy);
+        const T gu = (uT >= T(0) ? -cx * qa.Dpx() : T(0)) + (uT <= T(0) ? cx * qa.Dmx() : T(0));
+        const T gv = (vT >= T(0) ? -cy * qa.Dpy() : T(0)) + (vT <= T(0) ? cy * qa.Dmy() : T(0));
+        aut = lk * gu;
+        avt = lk * gv - beta * lk;
+    }
+    W.lk[o] = lk; W.ut[o] = uT; W.vt[o] = vT; W.aut[o] = aut; W.avt[o] = avt;
+}
+
+// Phase B (every point X): adjoint w.r.t. q from the advection/diffusion
+// stencils of the M3 points around X, and w.r.t. h through h2uv and the
+// T-point averages. If gacc.nk > 0 the q-adjoint is returned as
+// M3 * (sum_t G_t + local) (the final combination of a step).
+template <typename T>
+__device__ __forceinline__ T at0(const T* __restrict__ p, long long fo, int j, int i, const QGGeom& G)
+{
+    return (j < 0 || j >= G.ny || i < 0 || i >= G.nx) ? T(0) : p[fo + (long long)j * G.nx + i];
+}
+
+template <typename T>
+__global__ void k_adj_phaseB(QGGeom G, int nf, AdjTemps<T> W, StageIn<T> gacc,
+                             T* __restrict__ adq_out, T* __restrict__ adh_out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int f = blockIdx.z;
+    if (i >= G.nx || j >= G.ny || f >= nf) return;
+    const long long fo = f * G.fs;
+    const long long o = fo + (long long)j * G.nx + i;
+    const T cx = T(G.cx), cy = T(G.cy);
+    // products lk*up, lk*um (x) and lk*vp, lk*vm (y) at a point
+    auto UP = [&](int jj, int ii) { T l = at0(W.lk, fo, jj, ii, G); T u = at0(W.ut, fo, jj, ii, G); return l * (u < T(0) ? T(0) : u); };
+    auto UM = [&](int jj, int ii) { T l = at0(W.lk, fo, jj, ii, G); T u = at0(W.ut, fo, jj, ii, G); return l * (u > T(0) ? T(0) : u); };
+    auto VP = [&](int jj, int ii) { T l = at0(W.lk, fo, jj, ii, G); T v = at0(W.vt, fo, jj, ii, G); return l * (v < T(0) ? T(0) : v); };
+    auto VM = [&](int jj, int ii) { T l = at0(W.lk, fo, jj, ii, G); T v = at0(W.vt, fo, jj, ii, G); return l * (v > T(0) ? T(0) : v); };
+
+    T aq = cx * (-T(2) * UP(j, i - 1) - T(6) * UM(j, i - 1)
+                 - T(3) * UP(j, i) + T(3) * UM(j, i)
+                 + T(6) * UP(j, i + 1) + T(2) * UM(j, i + 1)
+                 - UP(j, i + 2) + UM(j, i - 2))
+         + cy * (-T(2) * VP(j - 1, i) - T(6) * VM(j - 1, i)
+                 - T(3) * VP(j, i) + T(3) * VM(j, i)
+                 + T(6) * VP(j + 1, i) + T(2) * VM(j + 1, i)
+                 - VP(j + 2, i) + VM(j - 2, i));
+    if (G.hasK) {
+        const T lc = at0(W.lk, fo, j, i, G);
+        aq += T(G.Kx) * (at0(W.lk, fo, j, i - 1, G) + at0(W.lk, fo, j, i + 1, G) - T(2) * lc)
+            + T(G.Ky) * (at0(W.lk, fo, j - 1, i, G) + at0(W.lk, fo, j + 1, i, G) - T(2) * lc);
+    }
+    const bool m3 = G.mask[(long long)j * G.nx + i] == 3;
+    if (gacc.nk > 0) {
+        T s = aq;
+        for (int t = 0; t < gacc.nk; ++t) s += gacc.k[t][o];
+        adq_out[o] = m3 ? s : T(0);
+    } else {
+        adq_out[o] = m3 ? aq : T(0);
+    }
+    const T hu = T(0.5) * T(G.cu), hv = T(0.5) * T(G.cv);
+    const T ah = hu * (at0(W.aut, fo, j - 1, i - 1, G) + T(2) * at0(W.aut, fo, j - 1, i, G) + at0(W.aut, fo, j - 1, i + 1, G)
+                       - at0(W.aut, fo, j + 1, i - 1, G) - T(2) * at0(W.aut, fo, j + 1, i, G) - at0(W.aut, fo, j + 1, i + 1, G))
+               + hv * (at0(W.avt, fo, j - 1, i - 1, G) + T(2) * at0(W.avt, fo, j, i - 1, G) + at0(W.avt, fo, j + 1, i - 1, G)
+                       - at0(W.avt, fo, j - 1, i + 1, G) - T(2) * at0(W.avt, fo, j, i + 1, G) - at0(W.avt, fo, j + 1, i + 1, G));
+    adh_out[o] = ah;
+}
+
+// ---------------------------------------------------------------------------
+// Small kernels: copies, finalize, h2uv / rhs on given fields (API pieces)
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_copy_masked(QGGeom G, int nf, const T* __restrict__ src, T* __restrict__ dst, int zero_land)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int f = blockIdx.z;
+    if (i >= G.nx || j >= G.ny || f >= nf) return;
+    const long long o = f * G.fs + (long long)j * G.nx + i;
+    T v = src[o];
+    if (zero_land && G.mask[(long long)j * G.nx + i] == 0) v = T(0);
+    dst[o] = v;
+}
+
+template <typename T>
+__global__ void k_fill(long long n, T v, T* __restrict__ x)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) x[k] = v;
+}
+
+// out = (land ? {h, NaN, 0}[land_mode] : (wall ? (hb or 0) : h)) + coef*forcing
+template <typename T>
+__global__ void k_finalize(QGGeom G, int nf, const T* __restrict__ h, const T* __restrict__ hb,
+                           const T* __restrict__ forcing, T coef, int land_mode, T* __restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int f = blockIdx.z;
+    if (i >= G.nx || j >= G.ny || f >= nf) return;
+    const long long o = f * G.fs + (long long)j * G.nx + i;
+    const bool wall = (i == 0 || j == 0 || i == G.nx - 1 || j == G.ny - 1);
+    T v;
+    if (wall)
+        v = hb ? hb[o] : T(0);
+    else
+        v = h[o];
+    if (G.mask[(long long)j * G.nx + i] == 0 && land_mode != 0)
+        v = land_mode == 1 ? T(NAN) : T(0);
+    if (forcing) v += coef * forcing[o];
+    out[o] = v;
+}
+
+template <typename T>
+__global__ void k_h2uv(QGGeom G, int nf, const T* __restrict__ h, T* __restrict__ u, T* __restrict__ v)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int f = blockIdx.z;
+    if (i >= G.nx || j >= G.ny || f >= nf) return;
+    const long long o = f * G.fs + (long long)j * G.nx + i;
+    const int nx = G.nx;
+    T uu = T(0), vv = T(0);
+    if (j >= 1 && j <= G.ny - 2 && i >= 1)
+        uu = T(G.cu) * (h[o + nx - 1] + h[o + nx] - h[o - nx] - h[o - nx - 1]);
+    if (j >= 1 && i >= 1 && i <= G.nx - 2)
+        vv = T(G.cv) * (h[o + 1] + h[o - nx + 1] - h[o - nx - 1] - h[o - 1]);
+    u[o] = guard0(uu);
+    v[o] = guard0(vv);
+}
+
+template <typename T>
+__global__ void k_rhs_uv(QGGeom G, int nf, const T* __restrict__ u, const T* __restrict__ v,
+                         const T* __restrict__ q, T* __restrict__ rhs)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int f = blockIdx.z;
+    if (i >= G.nx || j >= G.ny || f >= nf) return;
+    const long long o = f * G.fs + (long long)j * G.nx + i;
+    const long long go = (long long)j * G.nx + i;
+    T r = T(0);
+    if (G.mask[go] == 3) {
+        Vel<T> V;
+        V.u0 = u[o]; V.u1 = u[o + 1]; V.v0 = v[o]; V.v1 = v[o + G.nx];
+        Cross<T> qq;
+        qq.load(q + o, G.nx);
+        Cross<T> qa = qq;
+        if (G.fB) { Cross<T> b; b.load((const T*)G.fB + go, G.nx); qa.add(b); }
+        const T beta = G.beta ? ((const T*)G.beta)[go] : T(0);
+        r = guard0(tendency<T>(G, V, qa, qq, beta));
+    }
+    rhs[o] = r;
+}
+
+// ---------------------------------------------------------------------------
+// Host drivers
+// ---------------------------------------------------------------------------
+static inline dim3 pgrid(const vd_qg1l_plan* p, int nf) { return dim3((p->d.nx + 31) / 32, (p->d.ny + 7) / 8, nf); }
+static const dim3 kBlock(32, 8);
+
+template <typename T> static QGGeom geomT(const vd_qg1l_plan* p) { return p->geom; }
+
+// Does a later combination use k_s?  (stage s writes q_{s+1}; k_s is needed by
+// stages t >= s+2 or by the final combination when s is not the last stage)
+static bool need_k(const vd_qg1l_plan* p, int s)
+{
+    const int S = p->nstage;
+    if (s == S - 1) return false;
+    if (p->b[s] != 0.0) return true;
+    for (int t = s + 2; t < S; ++t)
+        if (p->A[t][s] != 0.0) return true;
+    return false;
+}
+
+template <typename T>
+struct TrajView {
+    T* base;
+    int S;
+    long long fb;   // elements per batch-field (nf * fs)
+    T* h(int n, int s) const { return base + ((long long)(n * S + s) * 2 + 0) * fb; }
+    T* q(int n, int s) const { return base + ((long long)(n * S + s) * 2 + 1) * fb; }
+};
+
+// One forward step (stage loop) between explicit buffers.
+template <typename T>
+static int step_once(const vd_qg1l_plan* p, int nf, T* const* hsv, T* const* qsv, T* hnew, T* qnew,
+                     T* const* kbuf, const T* hb, const T* qb, T* spec, cudaStream_t st, bool tangent)
+{
+    const int S = p->nstage;
+    const int B = tangent ? nf / 2 : nf;
+    for (int s = 0; s < S; ++s) {
+        const bool last = (s == S - 1);
+        StageIn<T> kin;
+        kin.nk = 0;
+        for (int i = 0; i < s; ++i) {
+            const double c = last ? p->b[i] : p->A[s + 1][i];
+            if (c != 0.0) { kin.k[kin.nk] = kbuf[i]; kin.c[kin.nk] = (T)c; ++kin.nk; }
+        }
+        const T cself = (T)(last ? p->b[s] : p->A[s + 1][s]);
+        T* kout = need_k(p, s) ? kbuf[s] : nullptr;
+        T* qo = last ? qnew : qsv[s + 1];
+        T* ho = last ? hnew : hsv[s + 1];
+        if (tangent)
+            k_stage_tl<T><<<pgrid(p, B), kBlock, 0, st>>>(p->geom, B, hsv[s], qsv[s], qsv[0], kin, cself, kout, qo);
+        else
+            k_stage_fwd<T><<<pgrid(p, nf), kBlock, 0, st>>>(p->geom, nf, hsv[s], qsv[s], qsv[0], kin, cself, kout, qo);
+        VD_LAUNCH_CHECK();
+        SolveArgs a;
+        a.src = qo; a.sub = qb; a.sub_batches = B;
+        a.out = ho; a.add = hb; a.add_batches = B; a.epi = EPI_H;
+        int rc = helmholtz_solve<T>(p, nf, a, spec, st);
+        if (rc) return rc;
+    }
+    return VD_OK;
+}
+
+template <typename T>
+int advance_impl(const vd_qg1l_plan* p, int nf, T* traj, int traj_steps, int first, int nstep,
+                 const T* hb, const T* qb, Arena& ws, cudaStream_t st)
+{
+    if (first < 0 || nstep < 0 || first + nstep > traj_steps) return VD_ERR_ARG;
+    const int S = p->nstage;
+    const long long fb = (long long)nf * p->geom.fs;
+    TrajView<T> tv{traj, S, fb};
+    T* kbuf[4] = {nullptr, nullptr, nullptr, nullptr};
+    for (int s = 0; s < S; ++s)
+        if (need_k(p, s) && !(kbuf[s] = (T*)ws.take(fb * sizeof(T)))) return VD_ERR_WORKSPACE;
+    T* spec = (T*)ws.take(spec_bytes(p, nf));
+    if (!spec) return VD_ERR_WORKSPACE;
+    for (int n = first; n < first + nstep; ++n) {
+        T* hs[4]; T* qs[4];
+        for (int s = 0; s < S; ++s) { hs[s] = tv.h(n, s); qs[s] = tv.q(n, s); }
+        int rc = step_once<T>(p, nf, hs, qs, tv.h(n + 1, 0), tv.q(n + 1, 0), kbuf, hb, qb, spec, st, false);
+        if (rc) return rc;
+    }
+    return VD_OK;
+}
+
+// Forward without trajectory: ping-pong states in the workspace.
+template <typename T>
+int forward_nostore(const vd_qg1l_plan* p, int nf, T* h, T* q, int nstep, const T* hb, const T* qb,
+                    Arena& ws, cudaStream_t st, bool tangent)
+{
+    const int S = p->nstage;
+    const long long fb = (long long)nf * p->geom.fs;
+    T* kbuf[4] = {nullptr, nullptr, nullptr, nullptr};
+    for (int s = 0; s < S; ++s)
+        if (need_k(p, s) && !(kbuf[s] = (T*)ws.take(fb * sizeof(T)))) return VD_ERR_WORKSPACE;
+    T* hs[4]; T* qs[4];
+    hs[0] = h; qs[0] = q;
+    for (int s = 1; s < S; ++s) {
+        hs[s] = (T*)ws.take(fb * sizeof(T));
+        qs[s] = (T*)ws.take(fb * sizeof(T));
+        if (!hs[s] || !qs[s]) return VD_ERR_WORKSPACE;
+    }
+    T* h2 = (T*)ws.take(fb * sizeof(T));
+    T* q2 = (T*)ws.take(fb * sizeof(T));
+    T* spec = (T*)ws.take(spec_bytes(p, nf));
+    if (!h2 || !q2 || !spec) return VD_ERR_WORKSPACE;
+    T* cur_h = h; T* cur_q = q; T* nxt_h = h2; T* nxt_q = q2;
+    for (int n = 0; n < nstep; ++n) {
+        hs[0] = cur_h; qs[0] = cur_q;
+        int rc = step_once<T>(p, nf, hs, qs, nxt_h, nxt_q, kbuf, hb, qb, spec, st, tangent);
+        if (rc) return rc;
+        T* t1 = cur_h; cur_h = nxt_h; nxt_h = t1;
+        T* t2 = cur_q; cur_q = nxt_q; nxt_q = t2;
+    }
+    if (cur_h != h) {
+        VD_CUDA_TRY(cudaMemcpyAsync(h, cur_h, fb * sizeof(T), cudaMemcpyDeviceToDevice, st));
+        VD_CUDA_TRY(cudaMemcpyAsync(q, cur_q, fb * sizeof(T), cudaMemcpyDeviceToDevice, st));
+    }
+    return VD_OK;
+}
+
+template <typename T>
+int advance_adj_impl(const vd_qg1l_plan* p, int nf, const T* traj, int traj_steps, int first, int nstep,
+                     T* adh, T* adq, Arena& ws, cudaStream_t st)
+{
+    if (first < 0 || nstep < 0 || first + nstep > traj_steps) return VD_ERR_ARG;
+    const int S = p->nstage;
+    const long long fb = (long long)nf * p->geom.fs;
+    TrajView<T> tv{const_cast<T*>(traj), S, fb};
+    T* Gb[4];
+    for (int s = 0; s < S; ++s)
+        if (!(Gb[s] = (T*)ws.take(fb * sizeof(T)))) return VD_ERR_WORKSPACE;
+    AdjTemps<T> W;
+    W.lk = (T*)ws.take(fb * sizeof(T));
+    W.ut = (T*)ws.take(fb * sizeof(T));
+    W.vt = (T*)ws.take(fb * sizeof(T));
+    W.aut = (T*)ws.take(fb * sizeof(T));
+    W.avt = (T*)ws.take(fb * sizeof(T));
+    T* adql = (T*)ws.take(fb * sizeof(T));
+    T* adhs = (T*)ws.take(fb * sizeof(T));
+    T* spec = (T*)ws.take(spec_bytes(p, nf));
+    if (!W.lk || !W.ut || !W.vt || !W.aut || !W.avt || !adql || !adhs || !spec) return VD_ERR_WORKSPACE;
+
+    for (int n = first + nstep - 1; n >= first; --n) {
+        // adjoint of h_{n+1} = I(q_{n+1}): G0 = M3*(solve(adh) + adq)
+        SolveArgs a0;
+        a0.src = adh; a0.sub = nullptr; a0.sub_batches = 0;
+        a0.out = Gb[0]; a0.add = adq; a0.add_batches = nf; a0.epi = EPI_ADJQ;
+        int rc = helmholtz_solve<T>(p, nf, a0, spec, st);
+        if (rc) return rc;
+        for (int s = S - 1; s >= 0; --s) {
+            StageIn<T> gin;
+            gin.nk = 0;
+            if (p->b[s] != 0.0) { gin.k[gin.nk] = Gb[0]; gin.c[gin.nk] = (T)p->b[s]; ++gin.nk; }
+            for (int t = s + 1; t < S; ++t)
+                if (p->A[t][s] != 0.0) { gin.k[gin.nk] = Gb[t]; gin.c[gin.nk] = (T)p->A[t][s]; ++gin.nk; }
+            k_adj_phaseA<T><<<pgrid(p, nf), kBlock, 0, st>>>(p->geom, nf, tv.h(n, s), tv.q(n, s), gin, W);
+            VD_LAUNCH_CHECK();
+            if (s >= 1) {
+                StageIn<T> none;
+                none.nk = 0;
+                k_adj_phaseB<T><<<pgrid(p, nf), kBlock, 0, st>>>(p->geom, nf, W, none, adql, adhs);
+                VD_LAUNCH_CHECK();
+                SolveArgs a;
+                a.src = adhs; a.sub = nullptr; a.sub_batches = 0;
+                a.out = Gb[s]; a.add = adql; a.add_batches = nf; a.epi = EPI_ADJQ;
+                rc = helmholtz_solve<T>(p, nf, a, spec, st);
+                if (rc) return rc;
+            } else {
+                StageIn<T> acc;
+                acc.nk = 0;
+                for (int t = 0; t < S; ++t) { acc.k[acc.nk] = Gb[t]; acc.c[acc.nk] = T(1); ++acc.nk; }
+                k_adj_phaseB<T><<<pgrid(p, nf), kBlock, 0, st>>>(p->geom, nf, W, acc, adq, adh);
+                VD_LAUNCH_CHECK();
+            }
+        }
+    }
+    return VD_OK;
+}
+
+template <typename T>
+int init_state_impl(const vd_qg1l_plan* p, int nf, int ntan0, const T* h, const T* hb, T* q, T* qb,
+                    cudaStream_t st)
+{
+    k_h2pv<T><<<pgrid(p, nf), kBlock, 0, st>>>(p->geom, nf, ntan0, h, hb, q);
+    VD_LAUNCH_CHECK();
+    if (qb) {
+        k_h2pv<T><<<pgrid(p, ntan0), kBlock, 0, st>>>(p->geom, ntan0, ntan0, hb, hb, qb);
+        VD_LAUNCH_CHECK();
+    }
+    return VD_OK;
+}
+
+template <typename T>
+int init_state_adj_impl(const vd_qg1l_plan* p, int nf, const T* h, const T* adq, T* adh, cudaStream_t st)
+{
+    k_h2pv_adj<T><<<pgrid(p, nf), kBlock, 0, st>>>(p->geom, nf, h, adq, adh);
+    VD_LAUNCH_CHECK();
+    return VD_OK;
+}
+
+template <typename T>
+int finalize_impl(const vd_qg1l_plan* p, int nf, const T* h, const T* hb, const T* forcing, double coef,
+                  int land_mode, T* out, cudaStream_t st)
+{
+    k_finalize<T><<<pgrid(p, nf), kBlock, 0, st>>>(p->geom, nf, h, hb, forcing, (T)coef, land_mode, out);
+    VD_LAUNCH_CHECK();
+    return VD_OK;
+}
+
+template <typename T>
+int copy_impl(const vd_qg1l_plan* p, int nf, const T* src, T* dst, int zero_land, cudaStream_t st)
+{
+    k_copy_masked<T><<<pgrid(p, nf), kBlock, 0, st>>>(p->geom, nf, src, dst, zero_land);
+    VD_LAUNCH_CHECK();
+    return VD_OK;
+}
+
+template <typename T>
+int zero_impl(long long n, T* x, cudaStream_t st)
+{
+    if (n <= 0) return VD_OK;
+    k_fill<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, T(0), x);
+    VD_LAUNCH_CHECK();
+    return VD_OK;
+}
+
+template <typename T>
+int h2uv_impl(const vd_qg1l_plan* p, int nf, const T* h, T* u, T* v, cudaStream_t st)
+{
+    k_h2uv<T><<<pgrid(p, nf), kBlock, 0, st>>>(p->geom, nf, h, u, v);
+    VD_LAUNCH_CHECK();
+    return VD_OK;
+}
+
+template <typename T>
+int rhs_impl(const vd_qg1l_plan* p, int nf, const T* u, const T* v, const T* q, T* r, cudaStream_t st)
+{
+    k_rhs_uv<T><<<pgrid(p, nf), kBlock, 0, st>>>(p->geom, nf, u, v, q, r);
+    VD_LAUNCH_CHECK();
+    return VD_OK;
+}
+
+#define VD_INST(T)                                                                                        \
+    template int advance_impl<T>(const vd_qg1l_plan*, int, T*, int, int, int, const T*, const T*, Arena&, \
+                                 cudaStream_t);                                                           \
+    template int forward_nostore<T>(const vd_qg1l_plan*, int, T*, T*, int, const T*, const T*, Arena&,    \
+                                    cudaStream_t, bool);                                                  \
+    template int advance_adj_impl<T>(const vd_qg1l_plan*, int, const T*, int, int, int, T*, T*, Arena&,   \
+                                     cudaStream_t);                                                       \
+    template int init_state_impl<T>(const vd_qg1l_plan*, int, int, const T*, const T*, T*, T*,            \
+                                    cudaStream_t);                                                        \
+    template int init_state_adj_impl<T>(const vd_qg1l_plan*, int, const T*, const T*, T*, cudaStream_t);  \
+    template int finalize_impl<T>(const vd_qg1l_plan*, int, const T*, const T*, const T*, double, int,    \
+                                  T*, cudaStream_t);                                                      \
+    template int copy_impl<T>(const vd_qg1l_plan*, int, const T*, T*, int, cudaStream_t);                 \
+    template int zero_impl<T>(long long, T*, cudaStream_t);                                               \
+    template int h2uv_impl<T>(const vd_qg1l_plan*, int, const T*, T*, T*, cudaStream_t);                  \
+    template int rhs_impl<T>(const vd_qg1l_plan*, int, const T*, const T*, const T*, T*, cudaStream_t);
+
+VD_INST(float)
+VD_INST(double)
+
+}  // namespace vd

@@ -1,0 +1,124 @@
+"""Drop-in QG 1.5-layer model class backed by the GB300 kernels.
+
+Point the reference's ``config.MOD.dir_model`` at this directory: the model
+wrapper loads ``{dir_model}/jqgm.py`` by path and instantiates
+``getattr(module, config.MOD.name_class)`` with the keyword arguments of
+mapping/src/mod.py:697-718, then calls ``step_jit(X, Xb, nstep=)``,
+``step_tgl_jit(dX, X, Xb, nstep=)`` and ``step_adj_jit(adX, X, Xb, nstep=)``
+(mod.py:721-723, 892, 991, 1055). ``Qgm`` here keeps those names, arguments
+and return values (mapping/models/model_qg1l/jqgm.py:108-569); arrays may be
+NumPy (returned as NumPy) or CUDA torch tensors (returned as tensors).
+
+Precision follows the reference's global flag: float32 unless
+``VARDYN_GB300_FLOAT64=1`` is set or ``dtype='float64'`` is passed.
+"""
+import os
+
+import numpy as np
+import torch
+
+from vardyn_gb300.qg1l import QG1LPlan, build_mask
+
+
+def _default_dtype():
+    return torch.float64 if os.environ.get("VARDYN_GB300_FLOAT64", "0") == "1" else torch.float32
+
+
+class Qgm:
+    """QG 1.5-layer model with the constructor of jqgm.py:113."""
+
+    def __init__(self, dx=None, dy=None, dt=None, SSH=None, c=None, Kdiffus=None, upwind=3,
+                 g=9.81, f=1e-4, time_scheme="Euler", compile=True, mdt=None,
+                 bathymetry_PV_term=None, dtype=None, device=None, **kwargs):
+        if dtype is None:
+            dtype = _default_dtype()
+        elif isinstance(dtype, str):
+            dtype = torch.float64 if dtype == "float64" else torch.float32
+        self.dtype = dtype
+        ny, nx = np.shape(dx)
+        self.ny, self.nx = ny, nx
+        self.dx = float(np.asarray(dx)[int(ny / 2), int(nx / 2)])       # jqgm.py:126-131
+        self.dy = float(np.asarray(dy)[int(ny / 2), int(nx / 2)])
+        self.dt = float(dt)
+        self.g = float(g)
+        beta = None
+        if np.ndim(f) > 0:                                               # jqgm.py:137-146
+            fa = np.asarray(f, dtype=np.float64)
+            self.f = float(np.nanmean(fa))
+            beta = np.zeros((ny, nx))
+            beta[1:-1, :] = (fa[2:, :] - fa[:-2, :]) / (2 * self.dy)
+        else:
+            self.f = float(f)
+        self.c = float(np.nanmean(c)) if np.ndim(c) > 0 else float(c)  # jqgm.py:149-153
+        self.upwind = upwind
+        self.time_scheme = time_scheme
+        self.Kdiffus = Kdiffus
+        self.mask = build_mask(ny, nx, None if SSH is None else np.asarray(SSH))
+        self.ind0 = self.mask == 0
+        fb = None
+        if bathymetry_PV_term is not None:
+            fb = self.f * np.asarray(bathymetry_PV_term, dtype=np.float64)
+        self.plan = QG1LPlan(ny, nx, self.dx, self.dy, self.dt, self.f, self.c, g=self.g,
+                             time_scheme=time_scheme, dtype=dtype, Kdiffus=Kdiffus,
+                             mask=self.mask, beta=beta, fbathy=fb, device=device)
+        self.device = self.plan.device
+        self._mdt = None if mdt is None else self._to_dev(mdt)
+        # the reference binds jitted aliases (jqgm.py:221-236)
+        self.h2uv_jit = self.h2uv
+        self.h2pv_jit = self.h2pv
+        self.pv2h_jit = self.pv2h
+        self.rhs_jit = self.rhs
+        self.step_jit = self.step
+        self.step_tgl_jit = self.step_tgl
+        self.step_adj_jit = self.step_adj
+
+    # ---------------- conversions ----------------
+    def _to_dev(self, x):
+        if isinstance(x, torch.Tensor):
+            return x.to(device=self.device, dtype=self.dtype).contiguous()
+        return torch.as_tensor(np.asarray(x, dtype=np.float64), device=self.device).to(self.dtype).contiguous()
+
+    def _wrap(self, like, *outs):
+        res = [o.squeeze(0) if like.dim() == 2 else o for o in outs] if isinstance(like, torch.Tensor) else \
+            [o.squeeze(0).cpu().numpy() if np.ndim(like) == 2 else o.cpu().numpy() for o in outs]
+        return res[0] if len(res) == 1 else tuple(res)
+
+    # ---------------- pieces ----------------
+    def h2uv(self, h):
+        u, v = self.plan.h2uv(self._to_dev(h))
+        return self._wrap(h, u, v)
+
+    def h2pv(self, h, hb, c=None):
+        return self._wrap(h, self.plan.h2pv(self._to_dev(h), self._to_dev(hb)))
+
+    def pv2h(self, q, hb, qb):
+        return self._wrap(q, self.plan.pv2h(self._to_dev(q), self._to_dev(hb), self._to_dev(qb)))
+
+    def rhs(self, u, v, q, way=1):
+        if way != 1:
+            raise NotImplementedError("way=-1 is not used by any caller of the reference")
+        return self._wrap(q, self.plan.rhs(self._to_dev(u), self._to_dev(v), self._to_dev(q)))
+
+    # ---------------- model ----------------
+    def _mdt_in(self, h0, hb):
+        if self._mdt is None:
+            return h0, hb
+        return h0 + self._mdt, hb + self._mdt
+
+    def step(self, h0, hb, nstep=1):
+        """nstep steps of the model from SSH h0 (jqgm.py:517-557)."""
+        H0, HB = self._mdt_in(self._to_dev(h0), self._to_dev(hb))
+        out = self.plan.step(H0, HB, int(nstep))
+        if self._mdt is not None:
+            out = out - self._mdt
+        return self._wrap(h0, out)
+
+    def step_tgl(self, dh0, h0, hb, nstep=1):
+        """Tangent linear of :meth:`step` w.r.t. h0 (jqgm.py:559-563)."""
+        H0, HB = self._mdt_in(self._to_dev(h0), self._to_dev(hb))
+        return self._wrap(h0, self.plan.step_tgl(self._to_dev(dh0), H0, HB, int(nstep)))
+
+    def step_adj(self, adh0, h0, hb, nstep=1):
+        """Adjoint of :meth:`step` w.r.t. h0 (jqgm.py:565-569)."""
+        H0, HB = self._mdt_in(self._to_dev(h0), self._to_dev(hb))
+        return self._wrap(h0, self.plan.step_adj(self._to_dev(adh0), H0, HB, int(nstep)))
