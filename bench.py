@@ -1,0 +1,387 @@
+"""Benchmark: 4D-Var cost+gradient evaluations per second, QG 1.5-layer,
+512 x 512, 30-day window, on one GB300.
+
+Workload (one "step" of this benchmark = one batched evaluation):
+  QG 1.5-layer model, 512^2 grid, dx = dy = 5 km, f0 = 1e-4, c = 2.7 m/s,
+  dt = 900 s, rk2 (the reference example's scheme), 2880 steps (30 days),
+  control = initial SSH of each window, 20 000 along-track observations per
+  window (seeded straight tracks, 7 km spacing, sigma = 0.03 m), FP32 bulk
+  with FP64 cost reductions. ``--batch`` independent windows advance in one
+  launch sequence, the whole evaluation (forward + adjoint) replayed as one
+  CUDA graph; the trajectory is stored in full (plain storage) when it fits.
+
+Arms:
+  default            this framework on the GPU
+  --impl reference   the CPU restatement of the reference path (float64
+                     NumPy/SciPy, oracle/), timed on the host cores on a
+                     bounded sample and scaled to the metric's unit.
+"""
+import argparse
+import json
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "4D-Var cost+grad evals/sec, QG1.5L 512^2 30-day window; HBM GB/s vs peak"
+UNIT = "evals/s"
+NY = NX = 512
+DX = 5.0e3
+DT = 900.0
+NSTEP = 2880
+NOBS = 20000
+SIGMA = 0.03
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="vardyn", choices=["vardyn", "reference"])
+    ap.add_argument("--batch", type=int, default=16, help="windows per GPU")
+    ap.add_argument("--nstep", type=int, default=NSTEP)
+    ap.add_argument("--size", type=int, default=NY)
+    ap.add_argument("--no-plain", action="store_true", help="skip the single-window plain form")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--profile-small", action="store_true",
+                    help="short window for profiler captures (not a bench value)")
+    return ap.parse_args()
+
+
+# ----------------------------------------------------------------------------
+# Synthetic windows
+# ----------------------------------------------------------------------------
+def make_windows(B, n, nstep, nobs, seed0=1000):
+    from vardyn_gb300.synthetic import kminus3_ssh, satellite_tracks
+    truths, guesses, wins = [], [], []
+    for b in range(B):
+        rng = np.random.default_rng(seed0 + b)
+        truths.append(kminus3_ssh(n, n, DX, DX, rng, rms=0.1, cutoff_km=50.0))
+        guesses.append(kminus3_ssh(n, n, DX, DX, rng, rms=0.1, cutoff_km=50.0))
+        x, y, st = satellite_tracks(n, n, DX, DX, nstep, nobs, rng, spacing_km=7.0)
+        wins.append(dict(x_km=x, y_km=y, step=st, err=np.full(x.size, SIGMA),
+                         yobs=np.zeros(x.size), noise=SIGMA * rng.standard_normal(x.size)))
+    return np.stack(truths), np.stack(guesses), wins
+
+
+def setup_engine(B, n, nstep, nobs, checkpoint=None):
+    import torch
+    from vardyn_gb300.fourdvar import QGWindows4DVar
+    from vardyn_gb300.obsop import AlongTrackObs
+    from vardyn_gb300.qg1l import QG1LPlan
+    truths, guesses, wins = make_windows(B, n, nstep, nobs)
+    plan = QG1LPlan(n, n, DX, DX, DT, 1e-4, 2.7, time_scheme="rk2", dtype=torch.float32)
+    obs = AlongTrackObs(wins, n, n, DX, DX, dtype=torch.float32)
+    hb = torch.zeros(B, n, n, dtype=torch.float32, device="cuda")
+    eng = QGWindows4DVar(plan, hb, nstep, obs, checkpoint=checkpoint)
+    # observations = H(truth trajectory) + noise, computed with the engine
+    # itself (yobs = 0 and inverr = 1/sigma give misfit = H x / sigma)
+    eng.cost_and_grad(torch.as_tensor(truths, dtype=torch.float32, device="cuda"))
+    torch.cuda.synchronize()
+    hx = obs.misfit[:obs.nobs].double().cpu().numpy() * SIGMA
+    noise = np.concatenate([w["noise"] for w in wins])
+    order = np.lexsort((np.concatenate([np.full(w["x_km"].size, b) for b, w in enumerate(wins)]),
+                        np.concatenate([w["step"] for w in wins])))
+    obs.d_y.copy_(torch.as_tensor(hx + noise[order], dtype=torch.float32, device="cuda"))
+    return plan, obs, eng, guesses
+
+
+# ----------------------------------------------------------------------------
+# Clocks
+# ----------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        exe = shutil.which("nvidia-smi")
+        if exe is None:
+            return
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        self.f = open(self.path, "w")
+        dev = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0] or "0"
+        self.proc = subprocess.Popen([exe, f"--id={dev}" if dev.isdigit() else "--id=0",
+                                      f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                      "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)),
+                "power_w_median": float(np.median(power)), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+# ----------------------------------------------------------------------------
+# CPU restatement (reference arm and cpu_baseline)
+# ----------------------------------------------------------------------------
+def cpu_sample(nstep_sample=6, n=NY, nobs=NOBS):
+    """Time the float64 NumPy/SciPy restatement of the reference's cost and
+    gradient (oracle/) on one 512^2 window over ``nstep_sample`` model steps
+    with the full observation count; scale to a 2880-step window."""
+    import scipy.fft
+    from oracle.fourdvar import ObsSet, cost_and_grad_h0
+    from oracle.qg1l import QgmOracle
+    from vardyn_gb300.synthetic import kminus3_ssh, satellite_tracks
+    cores = len(os.sched_getaffinity(0))
+    rng = np.random.default_rng(7)
+    h0 = kminus3_ssh(n, n, DX, DX, rng)
+    x, y, st = satellite_tracks(n, n, DX, DX, nstep_sample, nobs, rng, spacing_km=7.0)
+    obs = ObsSet(x, y, st, 0.03 * rng.standard_normal(x.size), np.full(x.size, SIGMA), n, n, DX, DX)
+    dxa = np.full((n, n), DX)
+    m = QgmOracle(dx=dxa, dy=dxa, dt=DT, c=2.7, f=1e-4, time_scheme="rk2")
+    with scipy.fft.set_workers(cores):
+        t0 = time.perf_counter()
+        cost_and_grad_h0(m, h0, np.zeros((n, n)), nstep_sample, obs)
+        t = time.perf_counter() - t0
+    per_eval = t * NSTEP / nstep_sample
+    return {"value": 1.0 / per_eval, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": (f"float64 NumPy/SciPy restatement of Variational.cost_and_grad + Qgm "
+                       f"(oracle/), one 512^2 window, {nstep_sample} rk2 steps forward+adjoint "
+                       f"with {nobs} obs in {t:.2f} s, scaled x{NSTEP / nstep_sample:.0f} to the "
+                       f"2880-step window; scipy.fft workers={cores}"),
+            "seconds_per_eval": per_eval}
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    samples = []
+    for _ in range(max(args.warmup, 0)):
+        cpu_sample(nstep_sample=2)
+    for _ in range(max(args.steps, 1)):
+        samples.append(cpu_sample(nstep_sample=6))
+    v = float(np.median([s["value"] for s in samples]))
+    cb = dict(samples[-1])
+    cb["value"] = v
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 / v, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": "QG1.5L 512x512 dx=5km dt=900s rk2, 2880-step (30-day) window, "
+                                   "20000 along-track obs, control h0, one window",
+                       "note": "reference is JAX (not installable here); its CPU path is timed "
+                               "through the float64 NumPy restatement in oracle/"},
+            "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ----------------------------------------------------------------------------
+# GPU arm
+# ----------------------------------------------------------------------------
+def time_graph(eng, x, warmup, steps, sampler=None):
+    import torch
+    for _ in range(warmup):
+        eng.cost_and_grad(x)
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if sampler:
+        sampler.start()
+    e0.record(st)
+    for _ in range(steps):
+        eng.cost_and_grad(x)
+    e1.record(st)
+    torch.cuda.synchronize()
+    clocks = sampler.stop() if sampler else None
+    return e0.elapsed_time(e1) / steps, clocks
+
+
+def dominant_kernel_roofline(plan, B, peaks, reps=50):
+    """Average duration of the x-direction DST-I GEMM pass (the dominant
+    kernel) on B windows, timed with CUDA events on the launching stream."""
+    import ctypes
+    import torch
+    from vardyn_gb300 import _lib
+    n = plan.nx - 2
+    f = torch.randn(B, plan.ny, plan.nx, device="cuda", dtype=plan.dtype)
+    spec = torch.empty(_lib.load().vd_qg1l_spec_bytes(plan.handle, B) // 4, device="cuda", dtype=plan.dtype)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    call = lambda: _lib.call("vd_qg1l_dst_x", plan.handle, B, ctypes.c_void_p(f.data_ptr()),
+                             ctypes.c_void_p(spec.data_ptr()), 0, None, st)
+    for _ in range(5):
+        call()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        call()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    rows = B * (plan.ny - 2)
+    ne, no = (n + 1) // 2, n // 2
+    flops = 2.0 * rows * (ne * ne + no * no)              # even/odd half GEMMs
+    bytes_alg = rows * n * 4 * 2                          # read rows, write spectra
+    return ms, flops, bytes_alg
+
+
+def gpu_arm(args):
+    import torch
+    dist = args.gpus > 1 or "RANK" in os.environ
+    rank, world = 0, 1
+    if dist:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl")
+        rank, world = tdist.get_rank(), tdist.get_world_size()
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", rank)))
+    from vardyn_gb300 import build, _lib
+    build.build()
+    L = _lib.load()
+    n = args.size
+    nstep = 64 if args.profile_small else args.nstep
+    B = args.batch
+    peaks = {}
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+    F = n * n * 4
+    traj_bytes = (nstep * 2 + 1) * 2 * B * F
+    free, total = torch.cuda.mem_get_info()
+    checkpoint = None if traj_bytes < 0.6 * free else int(np.ceil(np.sqrt(nstep)))
+    plan, obs, eng, guesses = setup_engine(B, n, nstep, NOBS)
+    x = torch.as_tensor(guesses, dtype=torch.float32, device="cuda")
+    c0 = L.vd_launch_count()
+    eng.capture()
+    launches_per_eval = (L.vd_launch_count() - c0) // 2   # warm-up run + captured run
+    if dist:
+        torch.distributed.barrier()
+    sampler = ClockSampler() if rank == 0 else None
+    ms, clocks = time_graph(eng, x, args.warmup, args.steps, sampler)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t)
+    value = world * B / (ms / 1e3)
+
+    # e2e through the public API: pinned host h0 -> device, evaluation,
+    # J and gradient back to pinned host memory, every step
+    h_host = torch.empty(B, n, n, dtype=torch.float32).pin_memory()
+    h_host.copy_(torch.as_tensor(guesses, dtype=torch.float32))
+    g_host = torch.empty(B, n, n, dtype=torch.float32).pin_memory()
+    j_host = torch.empty(B, dtype=torch.float64).pin_memory()
+    dev_in = torch.empty(B, n, n, dtype=torch.float32, device="cuda")
+    st = torch.cuda.current_stream()
+
+    def e2e_step():
+        dev_in.copy_(h_host, non_blocking=True)
+        J, G = eng.cost_and_grad(dev_in)
+        g_host.copy_(G, non_blocking=True)
+        j_host.copy_(J, non_blocking=True)
+    for _ in range(max(1, args.warmup // 2)):
+        e2e_step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    ke = max(2, args.steps // 2)
+    for _ in range(ke):
+        e2e_step()
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms_e2e = e0.elapsed_time(e1) / ke
+    e2e = {"value": world * B / (ms_e2e / 1e3), "unit": UNIT, "h2d_bytes_per_step": B * F,
+           "d2h_bytes_per_step": B * F + B * 8,
+           "path": "QGWindows4DVar.cost_and_grad (ctypes -> libvardyn_gb300 C ABI), pinned host buffers"}
+
+    # plain form: one window, full stored trajectory, no graph
+    plain = None
+    if rank == 0 and not args.no_plain:
+        p1, o1, e_1, g1 = setup_engine(1, n, nstep, NOBS)
+        x1 = torch.as_tensor(g1[:1], dtype=torch.float32, device="cuda")
+        e_1.cost_and_grad(x1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e_1.cost_and_grad(x1)
+        torch.cuda.synchronize()
+        plain = 1.0 / (time.perf_counter() - t0)
+        del p1, o1, e_1
+
+    # roofline of the dominant kernel
+    kms, kflops, kbytes = dominant_kernel_roofline(plan, B, peaks)
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    # whole evaluation: algorithmic bytes 46 F per step per window (RK2 forward
+    # 13F + recompute-free adjoint 20F + stored-trajectory reads 13F)
+    eval_bytes = 46.0 * F * nstep
+    achieved_eval = eval_bytes * B / (ms / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"QG1.5L {n}x{n} dx=5km dt=900s rk2, {nstep}-step window, "
+                               f"{NOBS} along-track obs/window, control h0, {B} windows per GPU "
+                               f"batched, whole evaluation replayed as one CUDA graph",
+                   "windows_per_gpu": B, "nstep": nstep,
+                   "trajectory": "full" if checkpoint is None else f"checkpoint every {checkpoint} steps",
+                   "l2": f"inputs larger than L2: trajectory {eng.memory_bytes() / 1e9:.1f} GB per GPU",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "kernel": "dst_gemm_kernel (x-direction DST-I, FP32 FMA)",
+                     "achieved": kbytes / (kms / 1e3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": kbytes / (kms / 1e3) / 1e9 / hbm_peak, "traffic": None,
+                     "kernel_ms": kms,
+                     "kernel_tflops": kflops / (kms / 1e3) / 1e12,
+                     "eval_achieved_gbs": achieved_eval, "eval_frac": achieved_eval / hbm_peak,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback"},
+        "e2e": e2e,
+        "gpu_launches": int(launches_per_eval * args.steps),
+        "clocks": clocks,
+        "plain_evals_per_s": plain,
+        "batched_over_plain": (value / world) / plain if plain else None,
+    }
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_sample()
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

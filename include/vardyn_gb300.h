@@ -63,7 +63,12 @@ typedef struct vd_qg1l_desc {
                                   used (jqgm.py:143,356-358); NULL = f-plane */
     const double* fbathy_host; /* [ny][nx] f*bathymetry_PV_term (jqgm.py:351-353);
                                   NULL = none */
+    int dst_engine;            /* VD_DST_AUTO: tensor cores (tcgen05, 3xTF32)
+                                  for float32 plans; VD_DST_FMA: CUDA-core FMA */
 } vd_qg1l_desc;
+
+#define VD_DST_AUTO 0
+#define VD_DST_FMA 1
 
 /* Build a plan: DST-I half matrices, tridiagonal multipliers, mask, beta and
  * bathymetry tables on the current device. Replaces the constant set-up of
@@ -96,6 +101,15 @@ vd_status vd_qg1l_pv2h(const vd_qg1l_plan* plan, int batch, const void* q,
                        const void* hb, const void* qb, void* h, void* work,
                        size_t work_bytes, void* stream);
 
+/* The x-direction orthonormal DST-I of the solve alone (dstI1D along the
+ * last axis, jqgm.py:75-77, applied to the (ny-2) x (nx-2) interior).
+ * inverse == 0: field interior -> spec; inverse != 0: spec -> out interior.
+ * spec rows hold the even wavenumbers (k = 0, 2, ...) first, then the odd
+ * ones; its size is vd_qg1l_spec_bytes(plan, batch). */
+size_t vd_qg1l_spec_bytes(const vd_qg1l_plan* plan, int batch);
+vd_status vd_qg1l_dst_x(const vd_qg1l_plan* plan, int batch, const void* field,
+                        void* spec, int inverse, void* out, void* stream);
+
 /* Forward model: Qgm.step (jqgm.py:517-557). h_out = M^nstep(h0) with
  * q0 = h2pv(h0, hb), land set to NaN. If traj != NULL (sized by
  * vd_qg1l_traj_bytes) every stage state is stored for a later adjoint.
@@ -123,7 +137,7 @@ vd_status vd_qg1l_init_state(const vd_qg1l_plan* plan, int batch, const void* h,
                              const void* hb, void* q, void* qb, void* stream);
 /* nstep steps from traj slot (first_step*nstage) onwards; the starting state
  * must already be in that slot. Writes every stage slot and the slot of the
- * state after the last step. */
+ * state after the last step. qb may be NULL when hb == 0 (then qb == 0). */
 vd_status vd_qg1l_advance(const vd_qg1l_plan* plan, int batch, void* traj,
                           int traj_steps, int first_step, int nstep,
                           const void* hb, const void* qb, void* work,
@@ -188,6 +202,13 @@ vd_status vd_fill(int dtype, long long n, double value, void* y, void* stream);
 
 /* Version / build information string. */
 const char* vd_version(void);
+/* Number of kernels this library has launched in the process so far (also
+ * counts launches recorded into a CUDA graph during capture). */
+long long vd_launch_count(void);
+/* Device-side error bits set by bounded waits that ran out (1: stage
+ * recycle, 2: operand arrival, 4: accumulator completion); 0 = none.
+ * Synchronous; reset != 0 clears them. */
+vd_status vd_device_error(int* flags, int reset);
 
 #ifdef __cplusplus
 }

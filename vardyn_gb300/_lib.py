@@ -27,7 +27,11 @@ class VdDesc(ctypes.Structure):
         ("mask_host", ctypes.POINTER(ctypes.c_int8)),
         ("beta_host", ctypes.POINTER(ctypes.c_double)),
         ("fbathy_host", ctypes.POINTER(ctypes.c_double)),
+        ("dst_engine", ctypes.c_int),
     ]
+
+
+VD_DST_AUTO, VD_DST_FMA = 0, 1
 
 
 P = ctypes.c_void_p
@@ -39,6 +43,8 @@ D = ctypes.c_double
 # name -> (restype, argtypes)
 SIGNATURES = {
     "vd_version": (ctypes.c_char_p, []),
+    "vd_launch_count": (LL, []),
+    "vd_device_error": (I, [ctypes.POINTER(ctypes.c_int), I]),
     "vd_qg1l_plan_create": (I, [ctypes.POINTER(P), ctypes.POINTER(VdDesc)]),
     "vd_qg1l_plan_destroy": (I, [P]),
     "vd_qg1l_workspace_bytes": (SZ, [P, I]),
@@ -48,6 +54,8 @@ SIGNATURES = {
     "vd_qg1l_h2uv": (I, [P, I, P, P, P, P]),
     "vd_qg1l_rhs": (I, [P, I, P, P, P, P, P]),
     "vd_qg1l_pv2h": (I, [P, I, P, P, P, P, P, SZ, P]),
+    "vd_qg1l_spec_bytes": (SZ, [P, I]),
+    "vd_qg1l_dst_x": (I, [P, I, P, P, I, P, P]),
     "vd_qg1l_step": (I, [P, I, P, P, I, P, P, P, SZ, P]),
     "vd_qg1l_step_tgl": (I, [P, I, P, P, P, I, P, P, SZ, P]),
     "vd_qg1l_step_adj": (I, [P, I, P, P, P, I, P, P, I, P, SZ, P]),

@@ -4,7 +4,12 @@
 #include <new>
 #include <cstring>
 
+#include <atomic>
+
 namespace vd {
+
+static std::atomic<long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 size_t elem_size(int dtype) { return dtype == VD_F64 ? 8 : 4; }
 
@@ -87,6 +92,28 @@ using namespace vd;
 #define VD_DISPATCH(p, FN, ...)                                              \
     ((p)->d.dtype == VD_F32 ? FN<float>(__VA_ARGS__) : FN<double>(__VA_ARGS__))
 
+extern "C" long long vd_launch_count(void) { return g_launches.load(); }
+
+namespace vd {
+template <typename T>
+int dst_x_only(const vd_qg1l_plan*, int, const T*, T*, int, T*, cudaStream_t);
+}
+
+extern "C" size_t vd_qg1l_spec_bytes(const vd_qg1l_plan* p, int batch)
+{
+    return (p && batch > 0) ? spec_bytes(p, batch) : 0;
+}
+
+extern "C" vd_status vd_qg1l_dst_x(const vd_qg1l_plan* p, int B, const void* field, void* spec, int inverse,
+                                   void* out, void* stream)
+{
+    if (!p || B <= 0 || !spec || (!inverse && !field) || (inverse && !out)) return VD_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    return p->d.dtype == VD_F32
+               ? dst_x_only<float>(p, B, (const float*)field, (float*)spec, inverse, (float*)out, st)
+               : dst_x_only<double>(p, B, (const double*)field, (double*)spec, inverse, (double*)out, st);
+}
+
 extern "C" const char* vd_version(void)
 {
     return "vardyn_gb300 0.1 (sm_103a; QG1.5L step/TL/adjoint, DST-x + tridiagonal-y Helmholtz, obs misfit)";
@@ -100,6 +127,7 @@ extern "C" vd_status vd_qg1l_plan_create(vd_qg1l_plan** out, const vd_qg1l_desc*
     if (d->nx - 2 > 4096 || d->ny - 2 > 4096) return VD_ERR_UNSUPPORTED;
     if (d->dtype != VD_F32 && d->dtype != VD_F64) return VD_ERR_ARG;
     if (d->time_scheme < VD_EULER || d->time_scheme > VD_RK4) return VD_ERR_ARG;
+    if (d->dst_engine != VD_DST_AUTO && d->dst_engine != VD_DST_FMA) return VD_ERR_ARG;
     if (!(d->dx > 0) || !(d->dy > 0) || !(d->f != 0) || !(d->c > 0) || !(d->g != 0)) return VD_ERR_ARG;
     vd_qg1l_plan* p = new (std::nothrow) vd_qg1l_plan();
     if (!p) return VD_ERR_ARG;
@@ -156,6 +184,9 @@ extern "C" vd_status vd_qg1l_plan_create(vd_qg1l_plan** out, const vd_qg1l_desc*
     G.beta = p->d_beta;
     G.fB = p->d_fB;
     if ((rc = build_dst_tables(p))) return fail(rc);
+    if (d->dtype == VD_F32 && d->dst_engine == VD_DST_AUTO) {
+        if ((rc = build_tc_images(p))) return fail(rc);
+    }
     *out = p;
     return VD_OK;
 }
@@ -163,6 +194,7 @@ extern "C" vd_status vd_qg1l_plan_create(vd_qg1l_plan** out, const vd_qg1l_desc*
 extern "C" vd_status vd_qg1l_plan_destroy(vd_qg1l_plan* p)
 {
     if (!p) return VD_OK;
+    free_tc_images(p);
     free_dst_tables(p);
     cudaFree(p->d_mask);
     cudaFree(p->d_beta);
@@ -374,7 +406,9 @@ extern "C" vd_status vd_qg1l_advance(const vd_qg1l_plan* p, int B, void* traj, i
                                      int nstep, const void* hb, const void* qb, void* work, size_t work_bytes,
                                      void* stream)
 {
-    if (!p || B <= 0 || !traj || !hb || !qb || !work) return VD_ERR_ARG;
+    // qb == NULL means a zero background PV (hb == 0): the solve then skips
+    // the subtraction.
+    if (!p || B <= 0 || !traj || !hb || !work) return VD_ERR_ARG;
     Arena ws{(char*)work, work_bytes, 0};
     cudaStream_t st = (cudaStream_t)stream;
     return p->d.dtype == VD_F32

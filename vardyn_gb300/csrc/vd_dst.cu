@@ -220,42 +220,110 @@ dst_gemm_kernel(GemmGeom g, const T* __restrict__ W1, const T* __restrict__ W2,
     }
 }
 
-// Thomas algorithm along y for 32 spectral columns of one field per CTA. The
-// column block is staged in shared memory; one warp runs the recurrences.
-template <typename T>
-__global__ void __launch_bounds__(128)
-tridiag_kernel(T* __restrict__ spec, const T* __restrict__ trim, int my, int n, int lds, T a)
+// Chunked Thomas algorithm: 32 spectral columns per CTA (one per lane), the
+// column block staged in shared memory, warp w owning rows [32w, 32w+32).
+// Both sweeps are first-order linear recurrences with the multiplier
+// alpha_j = -a*m_j:  forward d_j = m_j F_j + alpha_j d_{j-1},
+// backward x_j = d_j + alpha_j x_{j+1}. Each warp runs its piece from a zero
+// carry while accumulating the product of its alphas, one warp chains the
+// piece-end values (at most 32 steps), and each warp adds carry * partial
+// product to its rows. |alpha| < 1 (diagonal dominance), so the products
+// only shrink.
+template <typename T, int CH>
+__global__ void __launch_bounds__(512)
+tridiag_chunked_kernel(T* __restrict__ spec, const T* __restrict__ trim, int my, int n, int lds, T a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* F = reinterpret_cast<T*>(smem_raw);   // [my][32]
+    T* F = reinterpret_cast<T*>(smem_raw);          // [my][32]
+    T* cD = F + (size_t)my * 32;                    // [nw][32] piece-end values / carries
+    T* cP = cD + 16 * 32;                           // [nw][32] piece products
     const int f = blockIdx.y;
-    const int t0 = blockIdx.x * 32;
-    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int lane = threadIdx.x, w = threadIdx.y, nw = blockDim.y;
+    const int t = blockIdx.x * 32 + lane;
+    const bool col_ok = t < n;
     T* S = spec + (long long)f * my * lds;
-    const int t = t0 + tx;
-    for (int j = ty; j < my; j += 4) F[j * 32 + tx] = (t < n) ? S[(long long)j * lds + t] : T(0);
+    for (int j = w; j < my; j += nw) F[j * 32 + lane] = col_ok ? S[(long long)j * lds + t] : T(0);
+
+    const int j0 = w * CH;
+    const int cnt = max(0, min(CH, my - j0));
+    T mm[CH];
+#pragma unroll
+    for (int i = 0; i < CH; ++i)
+        mm[i] = (col_ok && i < cnt) ? __ldg(trim + (long long)(j0 + i) * lds + t) : T(0);
     __syncthreads();
-    if (ty == 0 && t < n) {
-        const T* M = trim + t;
-        T d = F[tx] * __ldg(M);
-        F[tx] = d;
-#pragma unroll 8
-        for (int j = 1; j < my; ++j) {
-            const T m = __ldg(M + (long long)j * lds);
-            d = (F[j * 32 + tx] - a * d) * m;
-            F[j * 32 + tx] = d;
+
+    // forward sweep, piece-local
+    T d = T(0), P = T(1);
+#pragma unroll
+    for (int i = 0; i < CH; ++i) {
+        if (i < cnt) {
+            const T al = -a * mm[i];
+            d = mm[i] * F[(j0 + i) * 32 + lane] + al * d;
+            F[(j0 + i) * 32 + lane] = d;
+            P *= al;
         }
-        T x = d;
-#pragma unroll 8
-        for (int j = my - 2; j >= 0; --j) {
-            const T m = __ldg(M + (long long)j * lds);
-            x = F[j * 32 + tx] - a * m * x;
-            F[j * 32 + tx] = x;
+    }
+    cD[w * 32 + lane] = d;
+    cP[w * 32 + lane] = P;
+    __syncthreads();
+    if (w == 0) {
+        T c = T(0);
+        for (int q = 0; q < nw; ++q) {
+            c = cD[q * 32 + lane] + cP[q * 32 + lane] * c;
+            cD[q * 32 + lane] = c;
         }
     }
     __syncthreads();
-    if (t < n)
-        for (int j = ty; j < my; j += 4) S[(long long)j * lds + t] = F[j * 32 + tx];
+    if (w > 0) {
+        const T cin = cD[(w - 1) * 32 + lane];
+        T p = T(1);
+#pragma unroll
+        for (int i = 0; i < CH; ++i) {
+            if (i < cnt) {
+                p *= -a * mm[i];
+                F[(j0 + i) * 32 + lane] += p * cin;
+            }
+        }
+    }
+    __syncthreads();
+
+    // backward sweep, piece-local from the piece end
+    T x = T(0);
+    P = T(1);
+#pragma unroll
+    for (int i = CH - 1; i >= 0; --i) {
+        if (i < cnt) {
+            const T al = -a * mm[i];
+            x = F[(j0 + i) * 32 + lane] + al * x;
+            F[(j0 + i) * 32 + lane] = x;
+            P *= al;
+        }
+    }
+    cD[w * 32 + lane] = x;
+    cP[w * 32 + lane] = P;
+    __syncthreads();
+    if (w == 0) {
+        T c = T(0);
+        for (int q = nw - 1; q >= 0; --q) {
+            c = cD[q * 32 + lane] + cP[q * 32 + lane] * c;
+            cD[q * 32 + lane] = c;
+        }
+    }
+    __syncthreads();
+    if (w < nw - 1) {
+        const T cin = cD[(w + 1) * 32 + lane];
+        T p = T(1);
+#pragma unroll
+        for (int i = CH - 1; i >= 0; --i) {
+            if (i < cnt) {
+                p *= -a * mm[i];
+                F[(j0 + i) * 32 + lane] += p * cin;
+            }
+        }
+    }
+    __syncthreads();
+    if (col_ok)
+        for (int j = w; j < my; j += nw) S[(long long)j * lds + t] = F[j * 32 + lane];
 }
 
 // Same recurrences directly on the spectral buffer, for column blocks too tall
@@ -397,9 +465,11 @@ static cudaError_t configure_kernels()
         if (!e) e = set_smem_attrs<float, 64>();
         if (!e) e = set_smem_attrs<double, 16>();
         if (!e) e = set_smem_attrs<double, 32>();
-        if (!e) e = cudaFuncSetAttribute(tridiag_kernel<float>,
+        if (!e) e = cudaFuncSetAttribute(tridiag_chunked_kernel<float, 32>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        if (!e) e = cudaFuncSetAttribute(tridiag_kernel<double>,
+        if (!e) e = cudaFuncSetAttribute(tridiag_chunked_kernel<float, 64>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        if (!e) e = cudaFuncSetAttribute(tridiag_chunked_kernel<double, 32>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
         g_attr_err = e;
     });
@@ -462,6 +532,7 @@ int helmholtz_solve(const vd_qg1l_plan* p, int nf, const SolveArgs& a, T* spec, 
     int rc;
     auto run = [&](bool fwd) -> int {
         if constexpr (sizeof(T) == 4) {
+            if (p->dst.tc) return dst_pass_tc(p, nf, a, (float*)spec, fwd, st);
             if (tr == 64) return launch_pair<T, 64>(p, g, a, spec, st, fwd);
         }
         if (tr == 32) return launch_pair<T, 32>(p, g, a, spec, st, fwd);
@@ -469,10 +540,17 @@ int helmholtz_solve(const vd_qg1l_plan* p, int nf, const SolveArgs& a, T* spec, 
     };
     if ((rc = run(true))) return rc;
     dim3 tgrid((t.n + 31) / 32, nf);
-    const size_t tsmem = size_t(t.my) * 32 * sizeof(T);
-    if (tsmem <= 200 * 1024) {
-        tridiag_kernel<T><<<tgrid, dim3(32, 4), tsmem, st>>>(
+    const size_t csmem = (size_t(t.my) * 32 + 2 * 16 * 32) * sizeof(T);
+    if (t.my <= 512 && csmem <= 200 * 1024) {
+        const int nw = (t.my + 31) / 32;
+        tridiag_chunked_kernel<T, 32><<<tgrid, dim3(32, nw), csmem, st>>>(
             spec, (const T*)t.trim, t.my, t.n, t.lds, (T)t.tri_a);
+    } else if (sizeof(T) == 4 && t.my <= 1024 && csmem <= 200 * 1024) {
+        if constexpr (sizeof(T) == 4) {
+            const int nw = (t.my + 63) / 64;
+            tridiag_chunked_kernel<T, 64><<<tgrid, dim3(32, nw), csmem, st>>>(
+                spec, (const T*)t.trim, t.my, t.n, t.lds, (T)t.tri_a);
+        }
     } else {
         tridiag_global_kernel<T><<<tgrid, 32, 0, st>>>(
             spec, (const T*)t.trim, t.my, t.n, t.lds, (T)t.tri_a);
@@ -483,5 +561,32 @@ int helmholtz_solve(const vd_qg1l_plan* p, int nf, const SolveArgs& a, T* spec, 
 
 template int helmholtz_solve<float>(const vd_qg1l_plan*, int, const SolveArgs&, float*, cudaStream_t);
 template int helmholtz_solve<double>(const vd_qg1l_plan*, int, const SolveArgs&, double*, cudaStream_t);
+
+// The x-direction DST-I pass alone (forward: field interior -> spectral rows;
+// inverse: spectral rows -> field interior).
+template <typename T>
+int dst_x_only(const vd_qg1l_plan* p, int nf, const T* field, T* spec, int inverse, T* out, cudaStream_t st)
+{
+    if (configure_kernels() != cudaSuccess) return VD_ERR_CUDA;
+    const DSTTables& t = p->dst;
+    GemmGeom g;
+    g.n = t.n; g.ne = t.ne; g.no = t.no; g.my = t.my; g.nx = p->d.nx;
+    g.fs = (long long)p->d.ny * p->d.nx;
+    g.R = nf * t.my;
+    g.kpad = t.kpad; g.ldw = t.ldw; g.lds = t.lds;
+    SolveArgs a;
+    a.src = field; a.sub = nullptr; a.sub_batches = 0;
+    a.out = out; a.add = nullptr; a.add_batches = 0; a.epi = EPI_H;
+    const int tr = pick_tr<T>(p, g.R);
+    if constexpr (sizeof(T) == 4) {
+        if (p->dst.tc) return dst_pass_tc(p, nf, a, (float*)spec, !inverse, st);
+        if (tr == 64) return launch_pair<T, 64>(p, g, a, spec, st, !inverse);
+    }
+    if (tr == 32) return launch_pair<T, 32>(p, g, a, spec, st, !inverse);
+    return launch_pair<T, 16>(p, g, a, spec, st, !inverse);
+}
+
+template int dst_x_only<float>(const vd_qg1l_plan*, int, const float*, float*, int, float*, cudaStream_t);
+template int dst_x_only<double>(const vd_qg1l_plan*, int, const double*, double*, int, double*, cudaStream_t);
 
 }  // namespace vd

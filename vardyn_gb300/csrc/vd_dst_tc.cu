@@ -1,0 +1,628 @@
+// x-direction DST-I pass on the 5th-generation tensor cores (tcgen05, sm_103a)
+// for float32 plans.
+//
+// The pass is two dense half-size products per row block (even/odd split, see
+// vd_dst.cu). Each CTA owns 128 interior rows (UMMA M = 128) and one output
+// tile of up to 256 columns held in tensor memory (TMEM, fp32 accumulators).
+// Float32 accuracy comes from the 3xTF32 split: x = x_hi + x_lo with
+// x_hi = tf32(x), and x.w ~= x_hi.w_hi + x_hi.w_lo + x_lo.w_hi (the dropped
+// x_lo.w_lo term is ~2^-22 relative).
+//
+// Pipeline (per K chunk of 32 = one 128-byte swizzle row of fp32):
+//   warps 0-3  build the A chunk (butterfly or copy of the input rows, hi/lo
+//              split) in the 128B-swizzled K-major layout and arrive on fullA;
+//   thread 0   also issues the bulk copies (cp.async.bulk) of the
+//              pre-swizzled hi/lo chunks of the DST half matrix (fullB);
+//   warp 4     owns the TMEM allocation; its lane 0 issues 3 x 4 MMAs per
+//              chunk and commits to `empty` to recycle the stage;
+//   warps 0-3  finally read the accumulators (tcgen05.ld) and write rows.
+// Every mbarrier wait is bounded (2 s of %globaltimer); a timeout sets a bit
+// in a device flag (vd_device_error) and the CTA finishes without hanging.
+#include "vd_internal.cuh"
+#include <vector>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+
+namespace vd {
+
+__device__ int g_tc_error = 0;
+
+namespace tc {
+
+constexpr int BM = 128;
+constexpr int KCH = 32;
+constexpr int NPROD = 256;      // producer / epilogue threads (warps 0-7)
+constexpr int NTHREADS = NPROD + 32;   // + warp 8: TMEM owner and MMA issuer
+constexpr int STAGES = 2;
+constexpr int TMEM_COLS = 256;
+constexpr uint32_t A_TILE = BM * KCH * 4;          // 16 KB
+constexpr uint32_t B_TILE_MAX = 256 * KCH * 4;     // 32 KB
+constexpr uint32_t STAGE_BYTES = 2 * A_TILE + 2 * B_TILE_MAX;
+constexpr size_t SMEM_BYTES = STAGES * STAGE_BYTES + 1024;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t gtimer()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait on the phase of parity `parity`.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int code)
+{
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = gtimer();
+    while (true) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (gtimer() - t0 > 2000000000ull) {
+            atomicOr(&g_tc_error, code);
+            return false;
+        }
+    }
+}
+
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(dst), "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_alloc(uint32_t dst_smem, uint32_t ncols)
+{
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst_smem), "r"(ncols)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish()
+{
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols)
+{
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accum)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(dtmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum));
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+
+// 32 consecutive fp32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32])
+{
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                   "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                   "+r"(r[15]), "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]),
+                   "+r"(r[22]), "+r"(r[23]), "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]),
+                   "+r"(r[29]), "+r"(r[30]), "+r"(r[31])
+                 :
+                 : "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ float tf32_rna(float x)
+{
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart (SBO), descriptor version 1.
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr)
+{
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1u << 16) | ((uint64_t)(1024u >> 4) << 32) |
+           ((uint64_t)1u << 46) | ((uint64_t)2u << 61);
+}
+
+// Instruction descriptor of kind::tf32: fp32 accumulate, tf32 A and B, both
+// K-major, N>>3 at bit 17, M>>4 at bit 24.
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N)
+{
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// byte offset of fp32 element (r, k) in a [rows][32] 128B-swizzled tile
+__host__ __device__ constexpr uint32_t swz(int r, int k)
+{
+    return (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((((k >> 2) ^ (r & 7)) & 7) << 4) + (k & 3) * 4);
+}
+
+}  // namespace tc
+
+struct TcTab {
+    int kch;                 // K chunks of 32
+    int nt_t;                // forward output tiles (<= 256 columns each)
+    int Nt[8];
+    long long fwd_off[2][8]; // image offsets (floats): [half][tile]
+    int nt_p;                // inverse output tiles (<= 128 columns each)
+    int Np[16];
+    long long inv_off[2][16];
+};
+
+struct TcGeom {
+    int n, ne, no, my, nx;
+    long long fs;
+    int R, lds;
+};
+
+using namespace tc;
+
+template <int MODE, int EPI>
+__global__ void __launch_bounds__(NTHREADS, 1)
+dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* __restrict__ src,
+              const float* __restrict__ sub, int sub_batches, float* __restrict__ spec, float* __restrict__ out,
+              const float* __restrict__ add, int add_batches, const int8_t* __restrict__ mask)
+{
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bars[3 * STAGES + 1];
+    __shared__ uint32_t tmem_base_sh;
+    unsigned char* sm = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const uint32_t sbase = smem_u32(sm);
+    auto a_hi = [&](int s) { return sbase + s * STAGE_BYTES; };
+    auto a_lo = [&](int s) { return sbase + s * STAGE_BYTES + A_TILE; };
+    auto b_hi = [&](int s) { return sbase + s * STAGE_BYTES + 2 * A_TILE; };
+    auto b_lo = [&](int s) { return sbase + s * STAGE_BYTES + 2 * A_TILE + B_TILE_MAX; };
+    const uint32_t bar0 = smem_u32(&bars[0]);
+    auto fullA = [&](int s) { return bar0 + 8u * s; };
+    auto fullB = [&](int s) { return bar0 + 8u * (STAGES + s); };
+    auto empty = [&](int s) { return bar0 + 8u * (2 * STAGES + s); };
+    const uint32_t accf = bar0 + 8u * (3 * STAGES);
+
+    const int tid = threadIdx.x;
+    const int warp = tid >> 5;
+    const int lane = tid & 31;
+
+    // ---- job layout of this CTA --------------------------------------------
+    int njobs, N, half = 0, tile;
+    const float* jimg[2];
+    if (MODE == 0) {
+        half = blockIdx.x / tab.nt_t;
+        tile = blockIdx.x % tab.nt_t;
+        njobs = 1;
+        N = tab.Nt[tile];
+        jimg[0] = img + tab.fwd_off[half][tile];
+        jimg[1] = jimg[0];
+    } else {
+        tile = blockIdx.x;
+        njobs = 2;
+        N = tab.Np[tile];
+        jimg[0] = img + tab.inv_off[0][tile];
+        jimg[1] = img + tab.inv_off[1][tile];
+    }
+    const int nchunks = njobs * tab.kch;
+    const uint32_t b_bytes = (uint32_t)N * KCH * 4;
+
+    constexpr int MMA_WARP = NPROD / 32;
+    if (warp == MMA_WARP) {
+        tmem_alloc(smem_u32(&tmem_base_sh), TMEM_COLS);
+        tmem_relinquish();
+    }
+    if (tid == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(fullA(s), NPROD);
+            mbar_init(fullB(s), 1);
+            mbar_init(empty(s), 1);
+        }
+        mbar_init(accf, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base_sh;
+
+    const int n = g.n, ne = g.ne, no = g.no;
+    if (warp < MMA_WARP) {
+        // ------------------------------ producers ------------------------------
+        // warp w fills rows [16w, 16w+16) of the A chunk; lane l handles K
+        // index k0 + l, so every global load is one coalesced 128-byte row.
+        // Row addresses advance incrementally (next interior row: +nx, and
+        // +2nx more when crossing into the next field).
+        const int r0 = warp * 16;
+        const int row0 = blockIdx.y * BM + r0;
+        int f0 = 0, j0 = 1;
+        if (MODE == 0 && row0 < g.R) {
+            f0 = row0 / g.my;
+            j0 = row0 - f0 * g.my + 1;
+        }
+        const bool use_sub = (MODE == 0) && sub != nullptr;
+        // Loads of chunk c+1 are issued right after chunk c is stored, so
+        // their latency overlaps the wait for a free stage and the MMAs.
+        float x1[16], x2[16];
+        auto load_chunk = [&](int c) {
+            const int job = c / tab.kch;
+            const int kc = c - job * tab.kch;
+            const int p = kc * KCH + lane;
+            int lim, c1, c2;
+            if (MODE == 0) {
+                lim = half == 0 ? ne : no;
+                c1 = p;
+                c2 = n - 1 - p;
+            } else {
+                lim = job == 0 ? ne : no;
+                c1 = job == 0 ? p : ne + p;
+                c2 = 0;
+            }
+            const bool pv = p < lim;
+            const bool p2 = p < no;
+            int row = row0, f = f0, j = j0;
+            long long base = (MODE == 0) ? f0 * g.fs + (long long)j0 * g.nx + 1 : (long long)row0 * g.lds;
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                float a1 = 0.f, a2 = 0.f;
+                if (row < g.R && pv) {
+                    if (MODE == 0) {
+                        a1 = src[base + c1];
+                        if (p2) a2 = src[base + c2];
+                        if (use_sub && f < sub_batches) {
+                            a1 -= sub[base + c1];
+                            if (p2) a2 -= sub[base + c2];
+                        }
+                    } else {
+                        a1 = spec[base + c1];
+                    }
+                }
+                x1[i] = a1;
+                x2[i] = a2;
+                ++row;
+                if (MODE == 0) {
+                    base += g.nx;
+                    if (++j > g.my) {
+                        j = 1;
+                        ++f;
+                        base += 2 * g.nx;
+                    }
+                } else {
+                    base += g.lds;
+                }
+            }
+        };
+        load_chunk(0);
+        for (int c = 0; c < nchunks; ++c) {
+            const int s = c % STAGES;
+            const uint32_t u = c / STAGES;
+            const int job = c / tab.kch;
+            const int kc = c - job * tab.kch;
+            if (c >= STAGES) mbar_wait(empty(s), (u - 1) & 1, 1);
+            if (tid == 0) {
+                mbar_arrive_expect_tx(fullB(s), 2 * b_bytes);
+                const float* blk = jimg[job] + (size_t)kc * 2 * N * KCH;
+                bulk_g2s(b_hi(s), blk, b_bytes, fullB(s));
+                bulk_g2s(b_lo(s), blk + (size_t)N * KCH, b_bytes, fullB(s));
+            }
+            const int p = kc * KCH + lane;
+            const bool p2 = p < no;
+            const uint32_t ah = a_hi(s), al = a_lo(s);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                float val;
+                if (MODE == 0)
+                    val = p2 ? (half == 0 ? x1[i] + x2[i] : x1[i] - x2[i]) : x1[i];
+                else
+                    val = x1[i];
+                const float h = tf32_rna(val);
+                const float l = tf32_rna(val - h);
+                const uint32_t off = swz(r0 + i, lane);
+                asm volatile("st.shared.f32 [%0], %1;" ::"r"(ah + off), "f"(h) : "memory");
+                asm volatile("st.shared.f32 [%0], %1;" ::"r"(al + off), "f"(l) : "memory");
+            }
+            fence_async_smem();
+            mbar_arrive(fullA(s));
+            if (c + 1 < nchunks) load_chunk(c + 1);
+        }
+
+        // ------------------------------ epilogue -------------------------------
+        // accumulators -> shared staging tile [128][S], then coalesced row
+        // stores. Warps w and w+4 share TMEM lanes 32(w%4).. and split the
+        // columns. All stages are free once the last MMA has completed.
+        mbar_wait(accf, 0, 4);
+        tc_fence_after();
+        constexpr int S = 257;
+        float* ep = reinterpret_cast<float*>(sm);
+        const int sp = warp & 3;
+        const int hc = warp >> 2;
+        const int trow = sp * 32 + lane;
+        const uint32_t lane_base = tmem + ((uint32_t)(sp * 32) << 16);
+        int cbeg, cend;
+        if (MODE == 0) {
+            const int halfN = ((N / 2 + 31) / 32) * 32;
+            cbeg = hc == 0 ? 0 : halfN;
+            cend = hc == 0 ? halfN : N;
+        } else {
+            cbeg = hc * 128;
+            cend = hc * 128 + N;
+        }
+        for (int cg = cbeg; cg < cend; cg += 32) {
+            float vv[32];
+            tmem_ld32(lane_base + cg, vv);
+#pragma unroll
+            for (int i = 0; i < 32; ++i) ep[trow * S + cg + i] = vv[i];
+        }
+        asm volatile("bar.sync 1, 256;" ::: "memory");
+        if (MODE == 0) {
+            const int lim = half == 0 ? ne : no;
+            const int coff = half == 0 ? 0 : ne;
+            const int t0 = tile * 256;
+            for (int rr = 0; rr < 16; ++rr) {
+                const int r = r0 + rr;
+                const int row = blockIdx.y * BM + r;
+                if (row >= g.R) break;
+                float* drow = spec + (long long)row * g.lds + coff;
+                for (int cc = lane; cc < N; cc += 32) {
+                    const int t = t0 + cc;
+                    if (t < lim) drow[t] = ep[r * S + cc];
+                }
+            }
+        } else {
+            const int p0 = tile * 128;
+            for (int rr = 0; rr < 16; ++rr) {
+                const int r = r0 + rr;
+                const int row = blockIdx.y * BM + r;
+                if (row >= g.R) break;
+                const int f = row / g.my;
+                const int j = row - f * g.my + 1;
+                const long long base = f * g.fs + (long long)j * g.nx + 1;
+                const bool ha = add != nullptr && f < add_batches;
+                for (int cc = lane; cc < N; cc += 32) {
+                    const int p = p0 + cc;
+                    if (p >= ne) break;
+                    const float A = ep[r * S + cc];
+                    const float B = (p < no) ? ep[r * S + 128 + cc] : 0.f;
+                    {
+                        const long long o = base + p;
+                        const float y = A + B;
+                        if (EPI == EPI_H) out[o] = ha ? y + add[o] : y;
+                        else out[o] = (mask[j * g.nx + 1 + p] == 3) ? y + add[o] : 0.f;
+                    }
+                    if (p < no) {
+                        const int pp = n - 1 - p;
+                        const long long o = base + pp;
+                        const float y = A - B;
+                        if (EPI == EPI_H) out[o] = ha ? y + add[o] : y;
+                        else out[o] = (mask[j * g.nx + 1 + pp] == 3) ? y + add[o] : 0.f;
+                    }
+                }
+            }
+        }
+    } else if (lane == 0) {
+        // ------------------------------ MMA issuer -----------------------------
+        const uint32_t idesc = idesc_tf32(BM, N);
+        for (int c = 0; c < nchunks; ++c) {
+            const int s = c % STAGES;
+            const uint32_t u = c / STAGES;
+            const int job = c / tab.kch;
+            const int kc = c - job * tab.kch;
+            mbar_wait(fullA(s), u & 1, 2);
+            mbar_wait(fullB(s), u & 1, 2);
+            tc_fence_after();
+            const uint32_t d = tmem + (uint32_t)(job * 128);
+#pragma unroll
+            for (int kk = 0; kk < KCH / 8; ++kk) {
+                const uint64_t ah = sdesc_sw128(a_hi(s) + kk * 32);
+                const uint64_t al = sdesc_sw128(a_lo(s) + kk * 32);
+                const uint64_t bh = sdesc_sw128(b_hi(s) + kk * 32);
+                const uint64_t bl = sdesc_sw128(b_lo(s) + kk * 32);
+                mma_tf32(d, ah, bh, idesc, (kc > 0 || kk > 0) ? 1u : 0u);
+                mma_tf32(d, ah, bl, idesc, 1u);
+                mma_tf32(d, al, bh, idesc, 1u);
+            }
+            mma_commit(empty(s));
+        }
+        mma_commit(accf);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == MMA_WARP) {
+        tc_fence_after();
+        tmem_dealloc(tmem, TMEM_COLS);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host side: pre-swizzled hi/lo images of the half matrices
+// ---------------------------------------------------------------------------
+static float tf32_rna_host(float x)
+{
+    uint32_t b;
+    std::memcpy(&b, &x, 4);
+    if ((b & 0x7f800000u) != 0x7f800000u) {
+        b += 0x1000u;
+        b &= 0xFFFFE000u;
+    }
+    float r;
+    std::memcpy(&r, &b, 4);
+    return r;
+}
+
+struct TcPlanData {
+    float* img;
+    TcTab tab;
+};
+
+int build_tc_images(vd_qg1l_plan* p)
+{
+    const DSTTables& t = p->dst;
+    const int n = t.n, ne = t.ne, no = t.no;
+    TcPlanData* d = new TcPlanData();
+    std::memset(&d->tab, 0, sizeof(TcTab));
+    TcTab& tab = d->tab;
+    tab.kch = (ne + KCH - 1) / KCH;
+    tab.nt_t = (ne + 255) / 256;
+    tab.nt_p = (ne + 127) / 128;
+    if (tab.nt_t > 8 || tab.nt_p > 16) { delete d; return VD_ERR_UNSUPPORTED; }
+    const double scale = std::sqrt(2.0 / (n + 1));
+    const long long period = 2LL * (n + 1);
+    auto S = [&](long long m) { m %= period; return scale * std::sin(M_PI * double(m) / double(n + 1)); };
+    // B operands as [N row][K] functions
+    auto fwd_odd = [&](int tt, int pp) { return (tt < ne && pp < ne) ? S((long long)(pp + 1) * (2 * tt + 1)) : 0.0; };
+    auto fwd_even = [&](int tt, int pp) { return (tt < no && pp < no) ? S((long long)(pp + 1) * (2 * tt + 2)) : 0.0; };
+    auto inv_odd = [&](int pp, int tt) { return (pp < ne && tt < ne) ? S((long long)(pp + 1) * (2 * tt + 1)) : 0.0; };
+    auto inv_even = [&](int pp, int tt) { return (pp < no && tt < no) ? S((long long)(pp + 1) * (2 * tt + 2)) : 0.0; };
+
+    std::vector<float> img;
+    auto emit = [&](auto fn, int row0, int N) {
+        const long long off = (long long)img.size();
+        for (int c = 0; c < tab.kch; ++c) {
+            std::vector<float> hi(size_t(N) * KCH, 0.f), lo(size_t(N) * KCH, 0.f);
+            for (int r = 0; r < N; ++r)
+                for (int k = 0; k < KCH; ++k) {
+                    const float v = (float)fn(row0 + r, c * KCH + k);
+                    const float h = tf32_rna_host(v);
+                    const float l = tf32_rna_host(v - h);
+                    const uint32_t o = swz(r, k) / 4;
+                    hi[o] = h;
+                    lo[o] = l;
+                }
+            img.insert(img.end(), hi.begin(), hi.end());
+            img.insert(img.end(), lo.begin(), lo.end());
+        }
+        return off;
+    };
+    for (int tt = 0; tt < tab.nt_t; ++tt) {
+        const int N = std::min(256, ((ne - 256 * tt + 15) / 16) * 16);
+        tab.Nt[tt] = N;
+        tab.fwd_off[0][tt] = emit(fwd_odd, 256 * tt, N);
+        tab.fwd_off[1][tt] = emit(fwd_even, 256 * tt, N);
+    }
+    for (int q = 0; q < tab.nt_p; ++q) {
+        const int N = std::min(128, ((ne - 128 * q + 15) / 16) * 16);
+        tab.Np[q] = N;
+        tab.inv_off[0][q] = emit(inv_odd, 128 * q, N);
+        tab.inv_off[1][q] = emit(inv_even, 128 * q, N);
+    }
+    if (cudaMalloc(&d->img, img.size() * sizeof(float)) != cudaSuccess) { delete d; return VD_ERR_CUDA; }
+    if (cudaMemcpy(d->img, img.data(), img.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(d->img);
+        delete d;
+        return VD_ERR_CUDA;
+    }
+    p->dst.tc = d;
+    return VD_OK;
+}
+
+void free_tc_images(vd_qg1l_plan* p)
+{
+    TcPlanData* d = (TcPlanData*)p->dst.tc;
+    if (!d) return;
+    cudaFree(d->img);
+    delete d;
+    p->dst.tc = nullptr;
+}
+
+static std::once_flag g_tc_once;
+static cudaError_t g_tc_err = cudaSuccess;
+
+static cudaError_t tc_configure()
+{
+    std::call_once(g_tc_once, [] {
+        cudaError_t e = cudaFuncSetAttribute(dst_tc_kernel<0, EPI_H>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)SMEM_BYTES);
+        if (!e) e = cudaFuncSetAttribute(dst_tc_kernel<1, EPI_H>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)SMEM_BYTES);
+        if (!e) e = cudaFuncSetAttribute(dst_tc_kernel<1, EPI_ADJQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)SMEM_BYTES);
+        g_tc_err = e;
+    });
+    return g_tc_err;
+}
+
+// One x-direction pass on the tensor cores (forward: fields -> spec,
+// inverse: spec -> out with the epilogue of `a`).
+int dst_pass_tc(const vd_qg1l_plan* p, int nf, const SolveArgs& a, float* spec, bool fwd, cudaStream_t st)
+{
+    const TcPlanData* d = (const TcPlanData*)p->dst.tc;
+    if (!d) return VD_ERR_UNSUPPORTED;
+    if (tc_configure() != cudaSuccess) return VD_ERR_CUDA;
+    const DSTTables& t = p->dst;
+    TcGeom g;
+    g.n = t.n; g.ne = t.ne; g.no = t.no; g.my = t.my; g.nx = p->d.nx;
+    g.fs = (long long)p->d.ny * p->d.nx;
+    g.R = nf * t.my;
+    g.lds = t.lds;
+    const int rows = (g.R + BM - 1) / BM;
+    if (fwd) {
+        dim3 grid(2 * d->tab.nt_t, rows);
+        dst_tc_kernel<0, EPI_H><<<grid, NTHREADS, SMEM_BYTES, st>>>(
+            g, d->tab, d->img, (const float*)a.src, (const float*)a.sub, a.sub_batches, spec, nullptr, nullptr, 0,
+            nullptr);
+    } else if (a.epi == EPI_H) {
+        dim3 grid(d->tab.nt_p, rows);
+        dst_tc_kernel<1, EPI_H><<<grid, NTHREADS, SMEM_BYTES, st>>>(
+            g, d->tab, d->img, nullptr, nullptr, 0, spec, (float*)a.out, (const float*)a.add, a.add_batches,
+            p->d_mask);
+    } else {
+        dim3 grid(d->tab.nt_p, rows);
+        dst_tc_kernel<1, EPI_ADJQ><<<grid, NTHREADS, SMEM_BYTES, st>>>(
+            g, d->tab, d->img, nullptr, nullptr, 0, spec, (float*)a.out, (const float*)a.add, a.add_batches,
+            p->d_mask);
+    }
+    VD_LAUNCH_CHECK();
+    return VD_OK;
+}
+
+}  // namespace vd
+
+extern "C" vd_status vd_device_error(int* flags, int reset)
+{
+    if (!flags) return VD_ERR_ARG;
+    VD_CUDA_TRY(cudaMemcpyFromSymbol(flags, vd::g_tc_error, sizeof(int)));
+    if (reset) {
+        const int zero = 0;
+        VD_CUDA_TRY(cudaMemcpyToSymbol(vd::g_tc_error, &zero, sizeof(int)));
+    }
+    return VD_OK;
+}

@@ -12,7 +12,17 @@
         if (_e != cudaSuccess) return VD_ERR_CUDA;         \
     } while (0)
 
-#define VD_LAUNCH_CHECK() VD_CUDA_TRY(cudaGetLastError())
+namespace vd {
+void count_launch();
+}
+
+// Every kernel launch site of the library is followed by this check; it also
+// counts the launch (vd_launch_count).
+#define VD_LAUNCH_CHECK()                  \
+    do {                                   \
+        vd::count_launch();                \
+        VD_CUDA_TRY(cudaGetLastError());   \
+    } while (0)
 
 namespace vd {
 
@@ -49,6 +59,7 @@ struct DSTTables {
     void* Weven;  // [kpad][ldw]  Weven[p][t] = c sin(pi (p+1)(2t+2)/(n+1)) (symmetric)
     void* trim;   // [my][lds] Thomas multipliers m_j per spectral column
     double tri_a; // off-diagonal g/f/dy^2
+    void* tc;     // tensor-core images and tile table (float32 plans), or nullptr
 };
 
 constexpr int DST_NC = 128;   // output columns per CTA tile
@@ -96,6 +107,9 @@ int helmholtz_solve(const vd_qg1l_plan* p, int nf, const SolveArgs& a, T* spec,
 size_t spec_bytes(const vd_qg1l_plan* p, int nf);
 int build_dst_tables(vd_qg1l_plan* p);
 void free_dst_tables(vd_qg1l_plan* p);
+int build_tc_images(vd_qg1l_plan* p);
+void free_tc_images(vd_qg1l_plan* p);
+int dst_pass_tc(const vd_qg1l_plan* p, int nf, const SolveArgs& a, float* spec, bool fwd, cudaStream_t st);
 
 // Bump allocator over a caller workspace.
 struct Arena {

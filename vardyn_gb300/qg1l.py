@@ -73,7 +73,7 @@ class QG1LPlan:
 
     def __init__(self, ny, nx, dx, dy, dt, f, c, g=9.81, time_scheme="rk2",
                  dtype=torch.float32, Kdiffus=None, mask=None, beta=None, fbathy=None,
-                 device=None):
+                 device=None, dst_engine="auto"):
         if not torch.cuda.is_available():
             raise RuntimeError("vardyn_gb300 needs a CUDA device (no CPU path)")
         self.device = torch.device(device if device is not None else "cuda")
@@ -91,6 +91,10 @@ class QG1LPlan:
         d.time_scheme = _lib.SCHEMES[time_scheme]
         d.dx, d.dy, d.dt = float(dx), float(dy), float(dt)
         d.g, d.f, d.c = float(g), float(f), float(c)
+        if dst_engine not in ("auto", "fma"):
+            raise ValueError("dst_engine is 'auto' (tensor cores for float32) or 'fma'")
+        d.dst_engine = _lib.VD_DST_AUTO if dst_engine == "auto" else _lib.VD_DST_FMA
+        self.dst_engine = dst_engine
         d.has_Kdiffus = 0 if Kdiffus is None else 1
         d.Kdiffus = 0.0 if Kdiffus is None else float(Kdiffus)
         m = np.ascontiguousarray(self.mask, dtype=np.int8)
