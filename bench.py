@@ -227,9 +227,22 @@ def time_graph(eng, x, warmup, steps, sampler=None):
     return e0.elapsed_time(e1) / steps, clocks
 
 
+def profiled_traffic(kernel_key):
+    """DRAM bytes per launch of a kernel from the committed ncu summary
+    (profiles/*.md lines 'traffic_bytes_per_launch <key> <bytes>')."""
+    import glob
+    for path in glob.glob(os.path.join(ROOT, "profiles", "*.md")):
+        for line in open(path):
+            parts = line.split()
+            if len(parts) == 3 and parts[0] == "traffic_bytes_per_launch" and parts[1] == kernel_key:
+                return float(parts[2])
+    return None
+
+
 def dominant_kernel_roofline(plan, B, peaks, reps=50):
-    """Average duration of the x-direction DST-I GEMM pass (the dominant
-    kernel) on B windows, timed with CUDA events on the launching stream."""
+    """Average duration of the x-direction DST-I pass (the dominant kernel:
+    tcgen05 3xTF32 for float32 plans) on B windows, timed with CUDA events on
+    the launching stream."""
     import ctypes
     import torch
     from vardyn_gb300 import _lib
@@ -278,7 +291,7 @@ def gpu_arm(args):
     F = n * n * 4
     traj_bytes = (nstep * 2 + 1) * 2 * B * F
     free, total = torch.cuda.mem_get_info()
-    checkpoint = None if traj_bytes < 0.6 * free else int(np.ceil(np.sqrt(nstep)))
+    checkpoint = None if traj_bytes < 0.75 * free else int(np.ceil(np.sqrt(nstep)))
     plan, obs, eng, guesses = setup_engine(B, n, nstep, NOBS)
     x = torch.as_tensor(guesses, dtype=torch.float32, device="cuda")
     c0 = L.vd_launch_count()
@@ -354,13 +367,17 @@ def gpu_arm(args):
                    "trajectory": "full" if checkpoint is None else f"checkpoint every {checkpoint} steps",
                    "l2": f"inputs larger than L2: trajectory {eng.memory_bytes() / 1e9:.1f} GB per GPU",
                    "parallelism": f"replicas x{world}"},
-        "roofline": {"bound": "hbm", "kernel": "dst_gemm_kernel (x-direction DST-I, FP32 FMA)",
+        "roofline": {"bound": "hbm", "kernel": "dst_tc_kernel<0,0> (x-direction DST-I pass, tcgen05 3xTF32)",
                      "achieved": kbytes / (kms / 1e3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": kbytes / (kms / 1e3) / 1e9 / hbm_peak, "traffic": None,
-                     "kernel_ms": kms,
-                     "kernel_tflops": kflops / (kms / 1e3) / 1e12,
+                     "frac": kbytes / (kms / 1e3) / 1e9 / hbm_peak,
+                     "traffic": profiled_traffic(f"dst_tc_fwd_{n}_b{B}"),
+                     "algorithmic_bytes_per_launch": kbytes, "kernel_ms": kms,
+                     "tensor": {"algorithmic_tflops": kflops / (kms / 1e3) / 1e12,
+                                "issued_tflops_3xtf32": 3 * kflops / (kms / 1e3) / 1e12,
+                                "peak_bf16_tflops": peaks.get("bf16_tflops"),
+                                "note": "TF32 dense rate is half the bf16 rate"},
                      "eval_achieved_gbs": achieved_eval, "eval_frac": achieved_eval / hbm_peak,
-                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback"},
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6.8 TB/s"},
         "e2e": e2e,
         "gpu_launches": int(launches_per_eval * args.steps),
         "clocks": clocks,
@@ -368,7 +385,7 @@ def gpu_arm(args):
         "batched_over_plain": (value / world) / plain if plain else None,
     }
     if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_sample()
+        line["cpu_baseline"] = cpu_sample(nstep_sample=12)
     if rank == 0:
         print(json.dumps(line))
     if dist:
