@@ -31,6 +31,8 @@ typedef int vd_status;
 #define VD_ERR_CUDA 2         /* a CUDA runtime call failed */
 #define VD_ERR_WORKSPACE 3    /* workspace smaller than the *_bytes query */
 #define VD_ERR_UNSUPPORTED 4  /* grid too small/large for the kernels */
+#define VD_ERR_SIZE 5         /* request larger than the fixed scratch of
+                                 vd_qg1l_pv2h_noalloc */
 
 #define VD_F32 0
 #define VD_F64 1
@@ -100,6 +102,22 @@ vd_status vd_qg1l_rhs(const vd_qg1l_plan* plan, int batch, const void* u,
 vd_status vd_qg1l_pv2h(const vd_qg1l_plan* plan, int batch, const void* q,
                        const void* hb, const void* qb, void* h, void* work,
                        size_t work_bytes, void* stream);
+
+/* PV -> SSH inversion that allocates nothing. No counterpart in the
+ * reference: it exists for callers that cannot allocate GPU memory (code
+ * inside a frozen CUDA-graph memory plan, plugins whose GPU memory belongs to
+ * another allocator, FFI hosts that only pass buffers they own). Same result
+ * as vd_qg1l_pv2h, but the spectral intermediate lives in a fixed array
+ * compiled into the library (vd_qg1l_pv2h_noalloc_max_bytes(), 16 MiB; one
+ * copy per device, held until the process exits): requests needing more
+ * return VD_ERR_SIZE. The first call on a device looks up that array's
+ * device address, so make it before capturing a stream. All calls share the
+ * array: calls that may overlap on the GPU (other streams, other threads)
+ * race on it and must be serialised by the caller. */
+size_t vd_qg1l_pv2h_noalloc_max_bytes(void);
+vd_status vd_qg1l_pv2h_noalloc(const vd_qg1l_plan* plan, int batch, const void* q,
+                               const void* hb, const void* qb, void* h,
+                               void* stream);
 
 /* The x-direction orthonormal DST-I of the solve alone (dstI1D along the
  * last axis, jqgm.py:75-77, applied to the (ny-2) x (nx-2) interior).

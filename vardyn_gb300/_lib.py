@@ -14,7 +14,8 @@ VD_EULER, VD_RK2, VD_RK3, VD_RK4 = 0, 1, 2, 3
 SCHEMES = {"Euler": VD_EULER, "euler": VD_EULER, "rk2": VD_RK2, "rk3": VD_RK3, "rk4": VD_RK4}
 DOT_SCRATCH = 1025   # doubles needed by vd_dot_f64's `out`
 
-_STATUS = {0: "VD_OK", 1: "VD_ERR_ARG", 2: "VD_ERR_CUDA", 3: "VD_ERR_WORKSPACE", 4: "VD_ERR_UNSUPPORTED"}
+_STATUS = {0: "VD_OK", 1: "VD_ERR_ARG", 2: "VD_ERR_CUDA", 3: "VD_ERR_WORKSPACE", 4: "VD_ERR_UNSUPPORTED",
+           5: "VD_ERR_SIZE"}
 
 
 class VdDesc(ctypes.Structure):
@@ -54,6 +55,8 @@ SIGNATURES = {
     "vd_qg1l_h2uv": (I, [P, I, P, P, P, P]),
     "vd_qg1l_rhs": (I, [P, I, P, P, P, P, P]),
     "vd_qg1l_pv2h": (I, [P, I, P, P, P, P, P, SZ, P]),
+    "vd_qg1l_pv2h_noalloc_max_bytes": (SZ, []),
+    "vd_qg1l_pv2h_noalloc": (I, [P, I, P, P, P, P, P]),
     "vd_qg1l_spec_bytes": (SZ, [P, I]),
     "vd_qg1l_dst_x": (I, [P, I, P, P, I, P, P]),
     "vd_qg1l_step": (I, [P, I, P, P, I, P, P, P, SZ, P]),
