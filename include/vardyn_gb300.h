@@ -125,6 +125,12 @@ vd_status vd_qg1l_pv2h_noalloc(const vd_qg1l_plan* plan, int batch, const void* 
  * spec rows hold the even wavenumbers (k = 0, 2, ...) first, then the odd
  * ones; its size is vd_qg1l_spec_bytes(plan, batch). */
 size_t vd_qg1l_spec_bytes(const vd_qg1l_plan* plan, int batch);
+/* The y-direction part of the solve alone, in place on spectral rows: for
+ * every x-wavenumber k the tridiagonal system
+ * g/f*(X[j-1] - 2X[j] + X[j+1])/dy^2 + (g/f*mu_k - g*f/c^2) X[j] = F[j]
+ * with X = 0 beyond the walls (equal to the y-DST / eigenvalue division /
+ * y-DST of inverse_elliptic_dst, jqgm.py:83-91). */
+vd_status vd_qg1l_tridiag_y(const vd_qg1l_plan* plan, int batch, void* spec, void* stream);
 vd_status vd_qg1l_dst_x(const vd_qg1l_plan* plan, int batch, const void* field,
                         void* spec, int inverse, void* out, void* stream);
 
@@ -155,7 +161,8 @@ vd_status vd_qg1l_init_state(const vd_qg1l_plan* plan, int batch, const void* h,
                              const void* hb, void* q, void* qb, void* stream);
 /* nstep steps from traj slot (first_step*nstage) onwards; the starting state
  * must already be in that slot. Writes every stage slot and the slot of the
- * state after the last step. qb may be NULL when hb == 0 (then qb == 0). */
+ * state after the last step. hb and qb may be NULL when the background SSH
+ * is zero (then qb == 0 too); the solves then skip them. */
 vd_status vd_qg1l_advance(const vd_qg1l_plan* plan, int batch, void* traj,
                           int traj_steps, int first_step, int nstep,
                           const void* hb, const void* qb, void* work,

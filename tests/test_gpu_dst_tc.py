@@ -113,3 +113,37 @@ def test_tc_adjoint_epilogue_and_step():
     assert device_error() == 0
     assert np.linalg.norm(out_tc - out_f) / np.linalg.norm(out_f) < 2e-6
     assert np.linalg.norm(adj_tc - adj_f) / np.linalg.norm(adj_f) < 2e-5
+
+
+@pytest.mark.parametrize("ny,nx,dtype,tol", [(40, 66, torch.float64, 1e-12), (514, 512, torch.float32, 2e-6),
+                                            (130, 201, torch.float32, 2e-6)])
+def test_tridiagonal_y_solve_matches_banded_solver(ny, nx, dtype, tol):
+    """vd_qg1l_tridiag_y against scipy's banded solver on the same systems."""
+    import scipy.linalg
+    from vardyn_gb300 import _lib
+    from vardyn_gb300.qg1l import QG1LPlan
+    dx, dy, g, f, c = 5e3, 4e3, 9.81, 1e-4, 2.7
+    p = QG1LPlan(ny, nx, dx, dy, 900.0, f, c, g=g, dtype=dtype)
+    n, my = nx - 2, ny - 2
+    ne = n - n // 2
+    lds = ((n + 3) // 4) * 4
+    rng = np.random.default_rng(ny)
+    B = 2
+    F = rng.standard_normal((B, my, lds))
+    spec = torch.as_tensor(F, dtype=dtype, device="cuda").contiguous()
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _lib.call("vd_qg1l_tridiag_y", p.handle, B, ctypes.c_void_p(spec.data_ptr()), st)
+    got = spec.cpu().numpy()
+    a = g / f / dy ** 2
+    for col in range(n):
+        k = 2 * col if col < ne else 2 * (col - ne) + 1
+        mu = 2 * (np.cos(np.pi / (nx - 1) * (k + 1)) - 1) / dx ** 2
+        bk = g / f * (-2 / dy ** 2 + mu) - g * f / c ** 2
+        ab = np.zeros((3, my))
+        ab[0, 1:] = a
+        ab[1, :] = bk
+        ab[2, :-1] = a
+        for b in range(B):
+            x = scipy.linalg.solve_banded((1, 1), ab, F[b, :, col])
+            err = np.linalg.norm(got[b, :, col] - x) / np.linalg.norm(x)
+            assert err < tol, (col, err)

@@ -99,6 +99,19 @@ template <typename T>
 int dst_x_only(const vd_qg1l_plan*, int, const T*, T*, int, T*, cudaStream_t);
 }
 
+namespace vd {
+template <typename T>
+int tridiag_only(const vd_qg1l_plan*, int, T*, cudaStream_t);
+}
+
+extern "C" vd_status vd_qg1l_tridiag_y(const vd_qg1l_plan* p, int B, void* spec, void* stream)
+{
+    if (!p || B <= 0 || !spec) return VD_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    return p->d.dtype == VD_F32 ? tridiag_only<float>(p, B, (float*)spec, st)
+                                : tridiag_only<double>(p, B, (double*)spec, st);
+}
+
 extern "C" size_t vd_qg1l_spec_bytes(const vd_qg1l_plan* p, int batch)
 {
     return (p && batch > 0) ? spec_bytes(p, batch) : 0;
@@ -406,9 +419,9 @@ extern "C" vd_status vd_qg1l_advance(const vd_qg1l_plan* p, int B, void* traj, i
                                      int nstep, const void* hb, const void* qb, void* work, size_t work_bytes,
                                      void* stream)
 {
-    // qb == NULL means a zero background PV (hb == 0): the solve then skips
-    // the subtraction.
-    if (!p || B <= 0 || !traj || !hb || !work) return VD_ERR_ARG;
+    // hb == NULL / qb == NULL mean a zero background SSH / PV: the solves then
+    // skip the addition / subtraction.
+    if (!p || B <= 0 || !traj || !work) return VD_ERR_ARG;
     Arena ws{(char*)work, work_bytes, 0};
     cudaStream_t st = (cudaStream_t)stream;
     return p->d.dtype == VD_F32

@@ -586,6 +586,33 @@ int dst_x_only(const vd_qg1l_plan* p, int nf, const T* field, T* spec, int inver
     return launch_pair<T, 16>(p, g, a, spec, st, !inverse);
 }
 
+// The y-direction tridiagonal solve alone, in place on spectral rows.
+template <typename T>
+int tridiag_only(const vd_qg1l_plan* p, int nf, T* spec, cudaStream_t st)
+{
+    if (configure_kernels() != cudaSuccess) return VD_ERR_CUDA;
+    const DSTTables& t = p->dst;
+    dim3 tgrid((t.n + 31) / 32, nf);
+    const size_t csmem = (size_t(t.my) * 32 + 2 * 16 * 32) * sizeof(T);
+    if (t.my <= 512 && csmem <= 200 * 1024) {
+        const int nw = (t.my + 31) / 32;
+        tridiag_chunked_kernel<T, 32><<<tgrid, dim3(32, nw), csmem, st>>>(spec, (const T*)t.trim, t.my, t.n, t.lds,
+                                                                           (T)t.tri_a);
+    } else if (sizeof(T) == 4 && t.my <= 1024 && csmem <= 200 * 1024) {
+        if constexpr (sizeof(T) == 4) {
+            const int nw = (t.my + 63) / 64;
+            tridiag_chunked_kernel<T, 64><<<tgrid, dim3(32, nw), csmem, st>>>(spec, (const T*)t.trim, t.my, t.n,
+                                                                               t.lds, (T)t.tri_a);
+        }
+    } else {
+        tridiag_global_kernel<T><<<tgrid, 32, 0, st>>>(spec, (const T*)t.trim, t.my, t.n, t.lds, (T)t.tri_a);
+    }
+    VD_LAUNCH_CHECK();
+    return VD_OK;
+}
+
+template int tridiag_only<float>(const vd_qg1l_plan*, int, float*, cudaStream_t);
+template int tridiag_only<double>(const vd_qg1l_plan*, int, double*, cudaStream_t);
 template int dst_x_only<float>(const vd_qg1l_plan*, int, const float*, float*, int, float*, cudaStream_t);
 template int dst_x_only<double>(const vd_qg1l_plan*, int, const double*, double*, int, double*, cudaStream_t);
 

@@ -280,10 +280,10 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
             j0 = row0 - f0 * g.my + 1;
         }
         const bool use_sub = (MODE == 0) && sub != nullptr;
-        // Loads of chunk c+1 are issued right after chunk c is stored, so
-        // their latency overlaps the wait for a free stage and the MMAs.
-        float x1[16], x2[16];
-        auto load_chunk = [&](int c) {
+        // Two register buffers: the loads of chunk c+2 are issued right after
+        // chunk c is stored, so their latency overlaps the processing of
+        // chunk c+1, the wait for a free stage and the MMAs.
+        auto load_chunk = [&](int c, float (&x1)[16], float (&x2)[16]) {
             const int job = c / tab.kch;
             const int kc = c - job * tab.kch;
             const int p = kc * KCH + lane;
@@ -301,23 +301,44 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
             const bool p2 = p < no;
             int row = row0, f = f0, j = j0;
             long long base = (MODE == 0) ? f0 * g.fs + (long long)j0 * g.nx + 1 : (long long)row0 * g.lds;
+            // Unconditional loads at clamped addresses (rows past the end
+            // repeat the last valid row, columns past the end read column 0);
+            // validity is applied when the chunk is processed, so no load
+            // result is consumed here.
+            const int cc1 = pv ? c1 : 0;
+            const int cc2 = (pv && p2) ? c2 : 0;
+            long long lastbase = base;
+            if (MODE == 0 && use_sub) {
+                // nonzero background PV: subtract it (rare path)
 #pragma unroll
-            for (int i = 0; i < 16; ++i) {
-                float a1 = 0.f, a2 = 0.f;
-                if (row < g.R && pv) {
-                    if (MODE == 0) {
-                        a1 = src[base + c1];
-                        if (p2) a2 = src[base + c2];
-                        if (use_sub && f < sub_batches) {
-                            a1 -= sub[base + c1];
-                            if (p2) a2 -= sub[base + c2];
-                        }
-                    } else {
-                        a1 = spec[base + c1];
+                for (int i = 0; i < 16; ++i) {
+                    const long long bb = (row < g.R) ? base : lastbase;
+                    const float s1 = f < sub_batches ? __ldg(sub + bb + cc1) : 0.f;
+                    const float s2 = f < sub_batches ? __ldg(sub + bb + cc2) : 0.f;
+                    x1[i] = __ldg(src + bb + cc1) - s1;
+                    x2[i] = __ldg(src + bb + cc2) - s2;
+                    if (row < g.R) lastbase = base;
+                    ++row;
+                    base += g.nx;
+                    if (++j > g.my) {
+                        j = 1;
+                        ++f;
+                        base += 2 * g.nx;
                     }
                 }
-                x1[i] = a1;
-                x2[i] = a2;
+                return;
+            }
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                const long long bb = (row < g.R) ? base : lastbase;
+                if (MODE == 0) {
+                    x1[i] = __ldg(src + bb + cc1);
+                    x2[i] = __ldg(src + bb + cc2);
+                } else {
+                    x1[i] = __ldg(spec + bb + cc1);
+                    x2[i] = 0.f;
+                }
+                if (row < g.R) lastbase = base;
                 ++row;
                 if (MODE == 0) {
                     base += g.nx;
@@ -331,8 +352,7 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
                 }
             }
         };
-        load_chunk(0);
-        for (int c = 0; c < nchunks; ++c) {
+        auto process = [&](int c, const float (&x1)[16], const float (&x2)[16]) {
             const int s = c % STAGES;
             const uint32_t u = c / STAGES;
             const int job = c / tab.kch;
@@ -346,6 +366,8 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
             }
             const int p = kc * KCH + lane;
             const bool p2 = p < no;
+            const int limv = (MODE == 0) ? (half == 0 ? ne : no) : (job == 0 ? ne : no);
+            const bool pv = p < limv;
             const uint32_t ah = a_hi(s), al = a_lo(s);
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
@@ -354,6 +376,8 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
                     val = p2 ? (half == 0 ? x1[i] + x2[i] : x1[i] - x2[i]) : x1[i];
                 else
                     val = x1[i];
+                const bool rvalid = blockIdx.y * BM + r0 + i < g.R;
+                val = (pv && rvalid) ? val : 0.f;
                 const float h = tf32_rna(val);
                 const float l = tf32_rna(val - h);
                 const uint32_t off = swz(r0 + i, lane);
@@ -362,7 +386,17 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
             }
             fence_async_smem();
             mbar_arrive(fullA(s));
-            if (c + 1 < nchunks) load_chunk(c + 1);
+        };
+        float xa1[16], xa2[16], xb1[16], xb2[16];
+        load_chunk(0, xa1, xa2);
+        if (nchunks > 1) load_chunk(1, xb1, xb2);
+        for (int c = 0; c < nchunks; c += 2) {
+            process(c, xa1, xa2);
+            if (c + 2 < nchunks) load_chunk(c + 2, xa1, xa2);
+            if (c + 1 < nchunks) {
+                process(c + 1, xb1, xb2);
+                if (c + 3 < nchunks) load_chunk(c + 3, xb1, xb2);
+            }
         }
 
         // ------------------------------ epilogue -------------------------------
@@ -408,32 +442,58 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
                 }
             }
         } else {
+            // Rows in batches of 4: all addend / mask loads of a batch (4 rows x
+            // 4 column groups x both mirror positions) are issued before any
+            // store, so their latencies overlap.
             const int p0 = tile * 128;
-            for (int rr = 0; rr < 16; ++rr) {
-                const int r = r0 + rr;
-                const int row = blockIdx.y * BM + r;
-                if (row >= g.R) break;
-                const int f = row / g.my;
-                const int j = row - f * g.my + 1;
-                const long long base = f * g.fs + (long long)j * g.nx + 1;
-                const bool ha = add != nullptr && f < add_batches;
-                for (int cc = lane; cc < N; cc += 32) {
-                    const int p = p0 + cc;
-                    if (p >= ne) break;
-                    const float A = ep[r * S + cc];
-                    const float B = (p < no) ? ep[r * S + 128 + cc] : 0.f;
-                    {
-                        const long long o = base + p;
-                        const float y = A + B;
-                        if (EPI == EPI_H) out[o] = ha ? y + add[o] : y;
-                        else out[o] = (mask[j * g.nx + 1 + p] == 3) ? y + add[o] : 0.f;
+            constexpr int RB = 4;
+            for (int rb = 0; rb < 16; rb += RB) {
+                float add1[RB][4], add2[RB][4];
+                bool m1[RB][4], m2[RB][4];
+                long long bases[RB];
+                int js[RB];
+#pragma unroll
+                for (int q = 0; q < RB; ++q) {
+                    const int row = blockIdx.y * BM + r0 + rb + q;
+                    const bool rv = row < g.R;
+                    const int f = rv ? row / g.my : 0;
+                    const int j = rv ? row - f * g.my + 1 : 1;
+                    bases[q] = rv ? f * g.fs + (long long)j * g.nx + 1 : -1;
+                    js[q] = j;
+                    const bool ha = rv && add != nullptr && (EPI != EPI_H || f < add_batches);
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int cc = lane + 32 * u;
+                        const int p = p0 + cc;
+                        const bool v1 = rv && cc < N && p < ne;
+                        const bool v2 = v1 && p < no;
+                        add1[q][u] = (v1 && ha) ? add[bases[q] + p] : 0.f;
+                        add2[q][u] = (v2 && ha) ? add[bases[q] + (n - 1 - p)] : 0.f;
+                        if (EPI == EPI_ADJQ) {
+                            m1[q][u] = v1 && mask[j * g.nx + 1 + p] == 3;
+                            m2[q][u] = v2 && mask[j * g.nx + 1 + (n - 1 - p)] == 3;
+                        }
                     }
-                    if (p < no) {
-                        const int pp = n - 1 - p;
-                        const long long o = base + pp;
-                        const float y = A - B;
-                        if (EPI == EPI_H) out[o] = ha ? y + add[o] : y;
-                        else out[o] = (mask[j * g.nx + 1 + pp] == 3) ? y + add[o] : 0.f;
+                }
+#pragma unroll
+                for (int q = 0; q < RB; ++q) {
+                    if (bases[q] < 0) continue;
+                    const int r = r0 + rb + q;
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int cc = lane + 32 * u;
+                        const int p = p0 + cc;
+                        if (cc >= N || p >= ne) continue;
+                        const float A = ep[r * S + cc];
+                        const float B = (p < no) ? ep[r * S + 128 + cc] : 0.f;
+                        const long long o1 = bases[q] + p;
+                        if (EPI == EPI_H) out[o1] = A + B + add1[q][u];
+                        else out[o1] = m1[q][u] ? A + B + add1[q][u] : 0.f;
+                        if (p < no) {
+                            const long long o2 = bases[q] + (n - 1 - p);
+                            if (EPI == EPI_H) out[o2] = A - B + add2[q][u];
+                            else out[o2] = m2[q][u] ? A - B + add2[q][u] : 0.f;
+                        }
                     }
                 }
             }

@@ -14,6 +14,7 @@
 // tendency unless the caller's SSH holds NaN away from the land of the mask;
 // the adjoint kernels rely on this and omit the u, v guard.
 #include "vd_internal.cuh"
+#include <mutex>
 
 namespace vd {
 
@@ -171,7 +172,9 @@ __global__ void k_stage_fwd(QGGeom G, int nf, const T* __restrict__ hs, const T*
         r = guard0(tendency<T>(G, V, qa, q, beta));
     }
     T acc = qbase[o];
-    for (int t = 0; t < kin.nk; ++t) acc += kin.c[t] * kin.k[t][o];
+#pragma unroll
+    for (int t = 0; t < 4; ++t)
+        if (t < kin.nk) acc += kin.c[t] * kin.k[t][o];
     acc += cself * r;
     qout[o] = acc;
     if (kout) kout[o] = r;
@@ -223,7 +226,9 @@ __global__ void k_stage_tl(QGGeom G, int B, const T* __restrict__ hs, const T* _
         }
     }
     T acc = qbase[o], dacc = qbase[od];
-    for (int t = 0; t < kin.nk; ++t) {
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        if (t >= kin.nk) break;
         acc += kin.c[t] * kin.k[t][o];
         dacc += kin.c[t] * kin.k[t][od];
     }
@@ -233,102 +238,141 @@ __global__ void k_stage_tl(QGGeom G, int B, const T* __restrict__ hs, const T* _
 }
 
 // ---------------------------------------------------------------------------
-// Adjoint stage, phase A (per M3 point P): lk = sum_t c_t G_t(P);
-//   AUT(P) = d J / d uT(P), AVT(P) = d J / d vT(P) (incl. beta), and the
-//   primal uT, vT for phase B. Non-M3 points get zeros.
+// Adjoint of one Runge-Kutta stage, in gather form, one 32x32 tile per CTA.
+//   phase A (tile + 2-cell halo, per tendency point P): lk = sum_t c_t G_t(P)
+//     (the stage-increment adjoint), the T-point velocities uT, vT and their
+//     adjoints aut = lk * d(adv)/d(uT), avt = lk * d(adv)/d(vT) - beta*lk,
+//     with jax's where-derivative convention (uT >= 0 feeds up, uT <= 0 um);
+//   phase B (tile, every point X): the PV adjoint from the upwind and
+//     diffusion stencils of the tendency points around X, and the SSH adjoint
+//     through the T-point averages and h2uv (a Sobel-like 3x3 stencil of
+//     aut / avt). With gacc.nk > 0 the PV adjoint is returned as
+//     M3 * (sum of gacc + local), the final combination of a step.
+// h (halo 3) and q (halo 4) are staged in shared memory once; the phase-A
+// quantities never leave shared memory.
 // ---------------------------------------------------------------------------
+constexpr int AT_Y = 32, AT_X = 32;                 // output tile
+constexpr int AH_Y = AT_Y + 6, AH_X = AT_X + 6;     // h tile (halo 3)
+constexpr int AQ_Y = AT_Y + 8, AQ_X = AT_X + 8;     // q tile (halo 4)
+constexpr int AA_Y = AT_Y + 4, AA_X = AT_X + 4;     // phase-A region (halo 2)
+
 template <typename T>
-struct AdjTemps {
-    T* lk; T* ut; T* vt; T* aut; T* avt;
+struct AdjTile {
+    T h[AH_Y][AH_X];
+    T q[AQ_Y][AQ_X];
+    T qa[AQ_Y][AQ_X];        // q + f*bathymetry (only when present)
+    T lk[AA_Y][AA_X];
+    T ut[AA_Y][AA_X];
+    T vt[AA_Y][AA_X];
+    T aut[AA_Y][AA_X];
+    T avt[AA_Y][AA_X];
 };
 
 template <typename T>
-__global__ void k_adj_phaseA(QGGeom G, int nf, const T* __restrict__ hs, const T* __restrict__ qs,
-                             StageIn<T> gin, AdjTemps<T> W)
+__global__ void __launch_bounds__(256)
+k_adj_stage_fused(QGGeom G, int nf, const T* __restrict__ hs, const T* __restrict__ qs, StageIn<T> gin,
+                  StageIn<T> gacc, T* __restrict__ adq_out, T* __restrict__ adh_out)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    AdjTile<T>& S = *reinterpret_cast<AdjTile<T>*>(smem_raw);
     const int f = blockIdx.z;
-    if (i >= G.nx || j >= G.ny || f >= nf) return;
-    const long long o = f * G.fs + (long long)j * G.nx + i;
-    const long long go = (long long)j * G.nx + i;
-    T lk = T(0), uT = T(0), vT = T(0), aut = T(0), avt = T(0);
-    if (G.mask[go] == 3) {
-        for (int t = 0; t < gin.nk; ++t) lk += gin.c[t] * gin.k[t][o];
-        Vel<T> V;
-        V.load(G, hs + o);
-        V.u0 = guard0(V.u0); V.u1 = guard0(V.u1); V.v0 = guard0(V.v0); V.v1 = guard0(V.v1);
-        Cross<T> q;
-        q.load(qs + o, G.nx);
-        Cross<T> qa = q;
-        if (G.fB) { Cross<T> b; b.load((const T*)G.fB + go, G.nx); qa.add(b); }
-        const T beta = G.beta ? ((const T*)G.beta)[go] : T(0);
-        if (isnan(tendency<T>(G, V, qa, q, beta))) lk = T(0);
-        uT = T(0.5) * (V.u0 + V.u1);
-        vT = T(0.5) * (V.v0 + V.v1);
-        const T cx = T(G.cx), cy = T(G.cy);
-        const T gu = (uT >= T(0) ? -cx * qa.Dpx() : T(0)) + (uT <= T(0) ? cx * qa.Dmx() : T(0));
-        const T gv = (vT >= T(0) ? -cy * qa.Dpy() : T(0)) + (vT <= T(0) ? cy * qa.Dmy() : T(0));
-        aut = lk * gu;
-        avt = lk * gv - beta * lk;
-    }
-    W.lk[o] = lk; W.ut[o] = uT; W.vt[o] = vT; W.aut[o] = aut; W.avt[o] = avt;
-}
-
-// Phase B (every point X): adjoint w.r.t. q from the advection/diffusion
-// stencils of the M3 points around X, and w.r.t. h through h2uv and the
-// T-point averages. If gacc.nk > 0 the q-adjoint is returned as
-// M3 * (sum_t G_t + local) (the final combination of a step).
-template <typename T>
-__device__ __forceinline__ T at0(const T* __restrict__ p, long long fo, int j, int i, const QGGeom& G)
-{
-    return (j < 0 || j >= G.ny || i < 0 || i >= G.nx) ? T(0) : p[fo + (long long)j * G.nx + i];
-}
-
-template <typename T>
-__global__ void k_adj_phaseB(QGGeom G, int nf, AdjTemps<T> W, StageIn<T> gacc,
-                             T* __restrict__ adq_out, T* __restrict__ adh_out)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int f = blockIdx.z;
-    if (i >= G.nx || j >= G.ny || f >= nf) return;
+    const int j0 = blockIdx.y * AT_Y, i0 = blockIdx.x * AT_X;
+    const int tid = threadIdx.y * 32 + threadIdx.x;
     const long long fo = f * G.fs;
-    const long long o = fo + (long long)j * G.nx + i;
-    const T cx = T(G.cx), cy = T(G.cy);
-    // products lk*up, lk*um (x) and lk*vp, lk*vm (y) at a point
-    auto UP = [&](int jj, int ii) { T l = at0(W.lk, fo, jj, ii, G); T u = at0(W.ut, fo, jj, ii, G); return l * (u < T(0) ? T(0) : u); };
-    auto UM = [&](int jj, int ii) { T l = at0(W.lk, fo, jj, ii, G); T u = at0(W.ut, fo, jj, ii, G); return l * (u > T(0) ? T(0) : u); };
-    auto VP = [&](int jj, int ii) { T l = at0(W.lk, fo, jj, ii, G); T v = at0(W.vt, fo, jj, ii, G); return l * (v < T(0) ? T(0) : v); };
-    auto VM = [&](int jj, int ii) { T l = at0(W.lk, fo, jj, ii, G); T v = at0(W.vt, fo, jj, ii, G); return l * (v > T(0) ? T(0) : v); };
-
-    T aq = cx * (-T(2) * UP(j, i - 1) - T(6) * UM(j, i - 1)
-                 - T(3) * UP(j, i) + T(3) * UM(j, i)
-                 + T(6) * UP(j, i + 1) + T(2) * UM(j, i + 1)
-                 - UP(j, i + 2) + UM(j, i - 2))
-         + cy * (-T(2) * VP(j - 1, i) - T(6) * VM(j - 1, i)
-                 - T(3) * VP(j, i) + T(3) * VM(j, i)
-                 + T(6) * VP(j + 1, i) + T(2) * VM(j + 1, i)
-                 - VP(j + 2, i) + VM(j - 2, i));
-    if (G.hasK) {
-        const T lc = at0(W.lk, fo, j, i, G);
-        aq += T(G.Kx) * (at0(W.lk, fo, j, i - 1, G) + at0(W.lk, fo, j, i + 1, G) - T(2) * lc)
-            + T(G.Ky) * (at0(W.lk, fo, j - 1, i, G) + at0(W.lk, fo, j + 1, i, G) - T(2) * lc);
+    const bool hasB = G.fB != nullptr;
+    // ---- stage h and q ----
+    for (int e = tid; e < AH_Y * AH_X; e += 256) {
+        const int a = e / AH_X, b = e - a * AH_X;
+        const int j = j0 - 3 + a, i = i0 - 3 + b;
+        S.h[a][b] = (j >= 0 && j < G.ny && i >= 0 && i < G.nx) ? hs[fo + (long long)j * G.nx + i] : T(0);
     }
-    const bool m3 = G.mask[(long long)j * G.nx + i] == 3;
-    if (gacc.nk > 0) {
+    for (int e = tid; e < AQ_Y * AQ_X; e += 256) {
+        const int a = e / AQ_X, b = e - a * AQ_X;
+        const int j = j0 - 4 + a, i = i0 - 4 + b;
+        const bool in = (j >= 0 && j < G.ny && i >= 0 && i < G.nx);
+        const T qv = in ? qs[fo + (long long)j * G.nx + i] : T(0);
+        S.q[a][b] = qv;
+        if (hasB) S.qa[a][b] = qv + (in ? ((const T*)G.fB)[(long long)j * G.nx + i] : T(0));
+    }
+    __syncthreads();
+    // ---- phase A on the tile + halo 2 ----
+    const T cx = T(G.cx), cy = T(G.cy), cu = T(G.cu), cv = T(G.cv);
+    for (int e = tid; e < AA_Y * AA_X; e += 256) {
+        const int a = e / AA_X, b = e - a * AA_X;
+        const int j = j0 - 2 + a, i = i0 - 2 + b;
+        T lk = T(0), uT = T(0), vT = T(0), aut = T(0), avt = T(0);
+        if (j >= 0 && j < G.ny && i >= 0 && i < G.nx && G.mask[(long long)j * G.nx + i] == 3) {
+            const long long o = fo + (long long)j * G.nx + i;
+#pragma unroll
+            for (int t = 0; t < 4; ++t)
+                if (t < gin.nk) lk += gin.c[t] * gin.k[t][o];
+            const int ha = a + 1, hb = b + 1;     // h-tile index of P
+            Vel<T> V;
+            V.u0 = guard0(cu * (S.h[ha + 1][hb - 1] + S.h[ha + 1][hb] - S.h[ha - 1][hb] - S.h[ha - 1][hb - 1]));
+            V.u1 = guard0(cu * (S.h[ha + 1][hb] + S.h[ha + 1][hb + 1] - S.h[ha - 1][hb + 1] - S.h[ha - 1][hb]));
+            V.v0 = guard0(cv * (S.h[ha][hb + 1] + S.h[ha - 1][hb + 1] - S.h[ha - 1][hb - 1] - S.h[ha][hb - 1]));
+            V.v1 = guard0(cv * (S.h[ha + 1][hb + 1] + S.h[ha][hb + 1] - S.h[ha][hb - 1] - S.h[ha + 1][hb - 1]));
+            const int qa_ = a + 2, qb_ = b + 2;   // q-tile index of P
+            Cross<T> q;
+            q.c = S.q[qa_][qb_]; q.e1 = S.q[qa_][qb_ + 1]; q.e2 = S.q[qa_][qb_ + 2];
+            q.w1 = S.q[qa_][qb_ - 1]; q.w2 = S.q[qa_][qb_ - 2];
+            q.n1 = S.q[qa_ + 1][qb_]; q.n2 = S.q[qa_ + 2][qb_];
+            q.s1 = S.q[qa_ - 1][qb_]; q.s2 = S.q[qa_ - 2][qb_];
+            Cross<T> qa = q;
+            if (hasB) {
+                qa.c = S.qa[qa_][qb_]; qa.e1 = S.qa[qa_][qb_ + 1]; qa.e2 = S.qa[qa_][qb_ + 2];
+                qa.w1 = S.qa[qa_][qb_ - 1]; qa.w2 = S.qa[qa_][qb_ - 2];
+                qa.n1 = S.qa[qa_ + 1][qb_]; qa.n2 = S.qa[qa_ + 2][qb_];
+                qa.s1 = S.qa[qa_ - 1][qb_]; qa.s2 = S.qa[qa_ - 2][qb_];
+            }
+            const T beta = G.beta ? ((const T*)G.beta)[(long long)j * G.nx + i] : T(0);
+            if (isnan(tendency<T>(G, V, qa, q, beta))) lk = T(0);
+            uT = T(0.5) * (V.u0 + V.u1);
+            vT = T(0.5) * (V.v0 + V.v1);
+            const T gu = (uT >= T(0) ? -cx * qa.Dpx() : T(0)) + (uT <= T(0) ? cx * qa.Dmx() : T(0));
+            const T gv = (vT >= T(0) ? -cy * qa.Dpy() : T(0)) + (vT <= T(0) ? cy * qa.Dmy() : T(0));
+            aut = lk * gu;
+            avt = lk * gv - beta * lk;
+        }
+        S.lk[a][b] = lk; S.ut[a][b] = uT; S.vt[a][b] = vT; S.aut[a][b] = aut; S.avt[a][b] = avt;
+    }
+    __syncthreads();
+    // ---- phase B on the tile ----
+    for (int e = tid; e < AT_Y * AT_X; e += 256) {
+        const int a = e / AT_X, b = e - a * AT_X;
+        const int j = j0 + a, i = i0 + b;
+        if (j >= G.ny || i >= G.nx) continue;
+        const int A = a + 2, Bc = b + 2;    // phase-A index of X
+        auto UP = [&](int da, int db) { const T u = S.ut[A + da][Bc + db]; return S.lk[A + da][Bc + db] * (u < T(0) ? T(0) : u); };
+        auto UM = [&](int da, int db) { const T u = S.ut[A + da][Bc + db]; return S.lk[A + da][Bc + db] * (u > T(0) ? T(0) : u); };
+        auto VP = [&](int da, int db) { const T v = S.vt[A + da][Bc + db]; return S.lk[A + da][Bc + db] * (v < T(0) ? T(0) : v); };
+        auto VM = [&](int da, int db) { const T v = S.vt[A + da][Bc + db]; return S.lk[A + da][Bc + db] * (v > T(0) ? T(0) : v); };
+        T aq = cx * (-T(2) * UP(0, -1) - T(6) * UM(0, -1)
+                     - T(3) * UP(0, 0) + T(3) * UM(0, 0)
+                     + T(6) * UP(0, 1) + T(2) * UM(0, 1)
+                     - UP(0, 2) + UM(0, -2))
+             + cy * (-T(2) * VP(-1, 0) - T(6) * VM(-1, 0)
+                     - T(3) * VP(0, 0) + T(3) * VM(0, 0)
+                     + T(6) * VP(1, 0) + T(2) * VM(1, 0)
+                     - VP(2, 0) + VM(-2, 0));
+        if (G.hasK) {
+            const T lc = S.lk[A][Bc];
+            aq += T(G.Kx) * (S.lk[A][Bc - 1] + S.lk[A][Bc + 1] - T(2) * lc)
+                + T(G.Ky) * (S.lk[A - 1][Bc] + S.lk[A + 1][Bc] - T(2) * lc);
+        }
+        const long long o = fo + (long long)j * G.nx + i;
+        const bool m3 = G.mask[(long long)j * G.nx + i] == 3;
         T s = aq;
-        for (int t = 0; t < gacc.nk; ++t) s += gacc.k[t][o];
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+            if (t < gacc.nk) s += gacc.k[t][o];
         adq_out[o] = m3 ? s : T(0);
-    } else {
-        adq_out[o] = m3 ? aq : T(0);
+        const T hu = T(0.5) * cu, hv = T(0.5) * cv;
+        adh_out[o] = hu * (S.aut[A - 1][Bc - 1] + T(2) * S.aut[A - 1][Bc] + S.aut[A - 1][Bc + 1]
+                           - S.aut[A + 1][Bc - 1] - T(2) * S.aut[A + 1][Bc] - S.aut[A + 1][Bc + 1])
+                   + hv * (S.avt[A - 1][Bc - 1] + T(2) * S.avt[A][Bc - 1] + S.avt[A + 1][Bc - 1]
+                           - S.avt[A - 1][Bc + 1] - T(2) * S.avt[A][Bc + 1] - S.avt[A + 1][Bc + 1]);
     }
-    const T hu = T(0.5) * T(G.cu), hv = T(0.5) * T(G.cv);
-    const T ah = hu * (at0(W.aut, fo, j - 1, i - 1, G) + T(2) * at0(W.aut, fo, j - 1, i, G) + at0(W.aut, fo, j - 1, i + 1, G)
-                       - at0(W.aut, fo, j + 1, i - 1, G) - T(2) * at0(W.aut, fo, j + 1, i, G) - at0(W.aut, fo, j + 1, i + 1, G))
-               + hv * (at0(W.avt, fo, j - 1, i - 1, G) + T(2) * at0(W.avt, fo, j, i - 1, G) + at0(W.avt, fo, j + 1, i - 1, G)
-                       - at0(W.avt, fo, j - 1, i + 1, G) - T(2) * at0(W.avt, fo, j, i + 1, G) - at0(W.avt, fo, j + 1, i + 1, G));
-    adh_out[o] = ah;
 }
 
 // ---------------------------------------------------------------------------
@@ -549,16 +593,20 @@ int advance_adj_impl(const vd_qg1l_plan* p, int nf, const T* traj, int traj_step
     T* Gb[4];
     for (int s = 0; s < S; ++s)
         if (!(Gb[s] = (T*)ws.take(fb * sizeof(T)))) return VD_ERR_WORKSPACE;
-    AdjTemps<T> W;
-    W.lk = (T*)ws.take(fb * sizeof(T));
-    W.ut = (T*)ws.take(fb * sizeof(T));
-    W.vt = (T*)ws.take(fb * sizeof(T));
-    W.aut = (T*)ws.take(fb * sizeof(T));
-    W.avt = (T*)ws.take(fb * sizeof(T));
     T* adql = (T*)ws.take(fb * sizeof(T));
     T* adhs = (T*)ws.take(fb * sizeof(T));
     T* spec = (T*)ws.take(spec_bytes(p, nf));
-    if (!W.lk || !W.ut || !W.vt || !W.aut || !W.avt || !adql || !adhs || !spec) return VD_ERR_WORKSPACE;
+    if (!adql || !adhs || !spec) return VD_ERR_WORKSPACE;
+    static std::once_flag attr_once;
+    static cudaError_t attr_err = cudaSuccess;
+    std::call_once(attr_once, [] {
+        attr_err = cudaFuncSetAttribute(k_adj_stage_fused<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)sizeof(AdjTile<float>));
+        if (!attr_err)
+            attr_err = cudaFuncSetAttribute(k_adj_stage_fused<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)sizeof(AdjTile<double>));
+    });
+    if (attr_err != cudaSuccess) return VD_ERR_CUDA;
 
     for (int n = first + nstep - 1; n >= first; --n) {
         // adjoint of h_{n+1} = I(q_{n+1}): G0 = M3*(solve(adh) + adq)
@@ -573,12 +621,12 @@ int advance_adj_impl(const vd_qg1l_plan* p, int nf, const T* traj, int traj_step
             if (p->b[s] != 0.0) { gin.k[gin.nk] = Gb[0]; gin.c[gin.nk] = (T)p->b[s]; ++gin.nk; }
             for (int t = s + 1; t < S; ++t)
                 if (p->A[t][s] != 0.0) { gin.k[gin.nk] = Gb[t]; gin.c[gin.nk] = (T)p->A[t][s]; ++gin.nk; }
-            k_adj_phaseA<T><<<pgrid(p, nf), kBlock, 0, st>>>(p->geom, nf, tv.h(n, s), tv.q(n, s), gin, W);
-            VD_LAUNCH_CHECK();
+            const dim3 agrid((p->d.nx + AT_X - 1) / AT_X, (p->d.ny + AT_Y - 1) / AT_Y, nf);
             if (s >= 1) {
                 StageIn<T> none;
                 none.nk = 0;
-                k_adj_phaseB<T><<<pgrid(p, nf), kBlock, 0, st>>>(p->geom, nf, W, none, adql, adhs);
+                k_adj_stage_fused<T><<<agrid, kBlock, sizeof(AdjTile<T>), st>>>(p->geom, nf, tv.h(n, s),
+                                                                                 tv.q(n, s), gin, none, adql, adhs);
                 VD_LAUNCH_CHECK();
                 SolveArgs a;
                 a.src = adhs; a.sub = nullptr; a.sub_batches = 0;
@@ -589,7 +637,8 @@ int advance_adj_impl(const vd_qg1l_plan* p, int nf, const T* traj, int traj_step
                 StageIn<T> acc;
                 acc.nk = 0;
                 for (int t = 0; t < S; ++t) { acc.k[acc.nk] = Gb[t]; acc.c[acc.nk] = T(1); ++acc.nk; }
-                k_adj_phaseB<T><<<pgrid(p, nf), kBlock, 0, st>>>(p->geom, nf, W, acc, adq, adh);
+                k_adj_stage_fused<T><<<agrid, kBlock, sizeof(AdjTile<T>), st>>>(p->geom, nf, tv.h(n, s),
+                                                                                 tv.q(n, s), gin, acc, adq, adh);
                 VD_LAUNCH_CHECK();
             }
         }

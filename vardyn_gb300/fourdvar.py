@@ -66,7 +66,9 @@ class QGWindows4DVar:
         self.obs_steps = sorted(int(s) for s in obs.steps if 0 <= s <= self.nstep)
         # h2pv(0, 0) == 0: with a zero background the solves skip the
         # subtraction of the background PV
-        self.qb_arg = None if float(self.hb.abs().max()) == 0.0 else self.qb
+        zero_bg = float(self.hb.abs().max()) == 0.0
+        self.qb_arg = None if zero_bg else self.qb
+        self.hb_arg = None if zero_bg else self.hb
         self.checkpoint = checkpoint
         S = plan.nstage
         if checkpoint is None:
@@ -115,7 +117,7 @@ class QGWindows4DVar:
         for s in self.obs_steps + [self.nstep]:
             if s <= prev:
                 continue
-            p.advance(B, self.traj, self.traj_steps, prev, s - prev, self.hb, self.qb_arg)
+            p.advance(B, self.traj, self.traj_steps, prev, s - prev, self.hb_arg, self.qb_arg)
             prev = s
             self._obs_forward(s, self.tv[s * self.S, 0])
 
@@ -150,7 +152,7 @@ class QGWindows4DVar:
         for ls in local + [n]:
             if ls <= prev:
                 continue
-            p.advance(B, self.traj, self.traj_steps, prev, ls - prev, self.hb, self.qb_arg)
+            p.advance(B, self.traj, self.traj_steps, prev, ls - prev, self.hb_arg, self.qb_arg)
             prev = ls
             if with_obs:
                 self._obs_forward(a + ls, self.tv[ls * self.S, 0])
