@@ -183,6 +183,11 @@ vd_status vd_qg1l_init_state_adj(const vd_qg1l_plan* plan, int batch,
 vd_status vd_qg1l_finalize(const vd_qg1l_plan* plan, int batch, const void* h,
                            const void* hb, const void* forcing, double coef,
                            void* h_out, void* stream);
+/* Adjoint of vd_qg1l_finalize: adforcing += coef*adh_out (if adforcing !=
+ * NULL; mod.py:1058-1068) and adh = adh_out with the walls and land set to
+ * 0. adh may alias adh_out. */
+vd_status vd_qg1l_finalize_adj(const vd_qg1l_plan* plan, int batch, const void* adh_out,
+                               void* adforcing, double coef, void* adh, void* stream);
 
 /* Along-track observation operator (Obsop_interp_l3_jax, mapping/src/obsop.py
  * 375-678). H is stored per observation as up to 4 (grid index, weight) pairs
@@ -218,12 +223,90 @@ vd_status vd_sumsq_gather_f64(int dtype, int nseg, const int32_t* seg_off,
 #define VD_DOT_SCRATCH 1025
 vd_status vd_dot_f64(int dtype, long long n, const void* x, const void* y,
                      double* out, void* stream);
+/* out[i] = d[i % period] * x[i] + (y ? y[i] : 0) for i < n (diagonal
+ * covariance products of tools_4Dvar.py:28-45: X = Q X0 + Xb, G = Q adX + X0
+ * over `batch` control vectors of length period). out may alias x or y. */
+vd_status vd_diag_axpy(int dtype, long long n, long long period, const void* d,
+                       const void* x, const void* y, void* out, void* stream);
 /* y = a*x + b*y elementwise (n elements). */
 vd_status vd_axpby(int dtype, long long n, double a, const void* x, double b,
                    void* y, void* stream);
 /* y = x (n elements of the dtype); y = value. */
 vd_status vd_copy(int dtype, long long n, const void* x, void* y, void* stream);
 vd_status vd_fill(int dtype, long long n, double value, void* y, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Gaussian space-time reduced basis (Basis_gauss3d, mapping/src/basis.py
+ * 1170-1555; several components = Basis_multi, basis.py:4039-4135).
+ *
+ * The control vector X (nbasis coefficients per window) is the concatenation
+ * over components c of [ENST_c.size][Nx_c] blocks (time centre major, space
+ * centre minor, basis.py:1324,1441). At basis time k:
+ *   phi = sum_c G_c(t_k) X_c,   G_c(t) X_c = Gauss_xy_c (sum_it g_it(t) X_c[it,:])
+ * (operg, basis.py:1489-1524) and adX_c[it,:] += g_it(t_k) Gauss_xy_c^T adphi
+ * (operg_transpose, basis.py:1526-1555). The grid must be rectilinear: x (or
+ * longitude) depends on the column only and y (or latitude) on the row only.
+ * ---------------------------------------------------------------------- */
+typedef struct vd_basis_plan vd_basis_plan;
+
+typedef struct vd_basis_grid {
+    int ny, nx;
+    int dtype;                  /* VD_F32 | VD_F64 of X and phi */
+    int geographic;             /* 1: xc = longitude, yc = latitude in degrees
+                                   (km2deg = 1/110, cos(lat) stretch, lon wrap:
+                                   the reference's formulas); 0: x/y in km */
+    const double* xc_host;      /* [nx] column coordinate */
+    const double* yc_host;      /* [ny] row coordinate */
+    const int8_t* land_host;    /* [ny][nx] nonzero = excluded point, or NULL */
+    int ntime;                  /* basis times (days), the `time` argument */
+    const double* time_host;    /*   of set_basis (basis.py:1291) */
+    int host_only;              /* 1: build the tables on the host only, for
+                                   the queries below (no device needed) */
+} vd_basis_grid;
+
+/* Parameters of one Basis_gauss3d component (config.BASIS, basis.py:1176-1187). */
+typedef struct vd_gauss3d_params {
+    double sigma_D;             /* space half-width [km] */
+    double sigma_T;             /* time half-width [days] */
+    double facns, facnlt;       /* space / time lattice densities */
+    double sigma_Q;             /* prior std scale: Q = sigma_Q/sqrt(facns*facnlt) */
+    int normalize_fact;         /* divide the time window by its integral */
+    int flux;                   /* time window = mywindow_flux (basis.py:4142) */
+    int has_time_spinup;
+    double time_spinup;         /* [days], used if has_time_spinup */
+} vd_gauss3d_params;
+
+vd_status vd_basis_plan_create(vd_basis_plan** out, const vd_basis_grid* grid, int ncomp,
+                               const vd_gauss3d_params* comps);
+vd_status vd_basis_plan_destroy(vd_basis_plan* plan);
+/* Total number of coefficients (sum over components of ENST.size * Nx). */
+long long vd_basis_nbasis(const vd_basis_plan* plan);
+/* Per component: offset of its block in X, number of time centres, number of
+ * space centres. */
+vd_status vd_basis_component(const vd_basis_plan* plan, int comp, long long* offset,
+                             int* ntime_centres, int* nspace_centres);
+/* Host copies of the lattice of one component: ENST [ntime_centres],
+ * ENSLAT and ENSLON [nspace_centres] (basis.py:1304-1324); NULL skips one. */
+vd_status vd_basis_lattice(const vd_basis_plan* plan, int comp, double* enst_host,
+                           double* enslat_host, double* enslon_host);
+/* Prior standard deviation of every coefficient [nbasis] (basis.py:1359). */
+vd_status vd_basis_q(const vd_basis_plan* plan, double* q_host);
+/* Active time centres of component comp at basis time k: their count, and
+ * (it, weight) pairs if the arrays are non-NULL (at most the count). */
+vd_status vd_basis_time_weights(const vd_basis_plan* plan, int k, int comp, int* count,
+                                int* it_host, double* weight_host);
+/* Workspace of vd_basis_project / vd_basis_project_T for `batch` windows. */
+size_t vd_basis_workspace_bytes(const vd_basis_plan* plan, int batch);
+/* phi[b] = (accumulate ? phi[b] : 0) + sum_c G_c(t_k) X[b] for b < batch;
+ * X[b] starts at X + b*ldX, phi is [batch][ny][nx]; land points get 0. */
+vd_status vd_basis_project(const vd_basis_plan* plan, int batch, int k, const void* X,
+                           long long ldX, void* phi, int accumulate, void* workspace,
+                           size_t workspace_bytes, void* stream);
+/* adX[b] += G(t_k)^T adphi[b] over the coefficients active at t_k; adphi is
+ * read only (the reference's zeroing of adState.params is the caller's). */
+vd_status vd_basis_project_T(const vd_basis_plan* plan, int batch, int k, const void* adphi,
+                             void* adX, long long ldX, void* workspace,
+                             size_t workspace_bytes, void* stream);
 
 /* Version / build information string. */
 const char* vd_version(void);

@@ -1,0 +1,203 @@
+"""Oracle (test infrastructure only): restatement of the Gaussian space-time
+reduced basis of the reference in float64 NumPy/SciPy, in the reference's
+own sparse form (a CSC space matrix and a time-weight vector per basis time).
+
+  - Basis_gauss3d            mapping/src/basis.py:1170-1555
+    (lattice 1291-1324, Q 1359, space 1393-1421, time 1423-1446,
+     operg 1489-1524, operg_transpose 1526-1555, norm_fact 1278-1283)
+  - Basis_multi              mapping/src/basis.py:4039-4135
+  - mywindow / mywindow_flux mapping/src/basis.py:4138-4144
+
+Two coordinate forms:
+  geo=True   lon/lat in degrees, exactly the reference's formulas
+             (km2deg = 1/110, longitude spacing stretched by cos(lat),
+             longitude differences wrapped to [-180, 180)).
+  geo=False  planar x/y in km for the Cartesian synthetic grids: the same
+             formulas with km2deg = 1, cos(lat) = 1 and no wrap.
+
+Parity status: unpinned by reference data (the reference needs jax, xarray
+and netCDF inputs, none importable here); pinned by the transpose
+(dot-product) identity, by the analytic footprint values and by the GPU
+kernels' agreement with this restatement.
+"""
+import numpy as np
+from scipy.sparse import csc_matrix
+
+KM2DEG = 1. / 110
+
+
+def mywindow(x):
+    """cos^2 window (basis.py:4138-4140)."""
+    return np.cos(x * 0.5 * np.pi) ** 2
+
+
+def mywindow_flux(x):
+    """Flux window (basis.py:4142-4144)."""
+    return -np.pi * np.sin(x * 0.5 * np.pi) * np.cos(x * 0.5 * np.pi)
+
+
+class Gauss3dOracle:
+    """One Gaussian (cos^2) space-time basis component.
+
+    lon, lat: 2-D coordinate arrays of the grid (degrees if geo, km if not);
+    mask: 2-D bool, True = excluded (land), or None."""
+
+    def __init__(self, lon, lat, sigma_D, sigma_T, facns=2.0, facnlt=1.0, sigma_Q=0.01,
+                 normalize_fact=True, time_spinup=None, mask=None, flux=False, geo=False):
+        lon = np.asarray(lon, float)
+        lat = np.asarray(lat, float)
+        self.shape_phys = lon.shape
+        self.lon1d, self.lat1d = lon.ravel(), lat.ravel()
+        self.lon_min, self.lon_max = np.nanmin(lon), np.nanmax(lon)
+        self.lat_min, self.lat_max = np.nanmin(lat), np.nanmax(lat)
+        self.sigma_D, self.sigma_T = float(sigma_D), float(sigma_T)
+        self.facns, self.facnlt, self.sigma_Q = float(facns), float(facnlt), float(sigma_Q)
+        self.time_spinup = time_spinup
+        self.geo = geo
+        self.km2deg = KM2DEG if geo else 1.0
+        self.mask1d = None
+        if mask is not None and np.any(mask):
+            self.mask1d = np.asarray(mask, bool).ravel()
+        self.window = mywindow_flux if flux else mywindow
+        self.normalize_fact = normalize_fact
+        if normalize_fact:                                       # basis.py:1278-1283
+            tt = np.linspace(-self.sigma_T, self.sigma_T)
+            tmp = np.zeros_like(tt)
+            for i in range(tt.size - 1):
+                tmp[i + 1] = tmp[i] + self.window(tt[i] / self.sigma_T) * (tt[i + 1] - tt[i])
+            self.norm_fact = tmp.max()
+
+    def _cos(self, lat_deg):
+        return np.cos(lat_deg * np.pi / 180.) if self.geo else 1.0
+
+    def _dlon(self, d):
+        return np.mod(d + 180, 360) - 180 if self.geo else d
+
+    def set_basis(self, time):
+        """Lattice, prior std Q, space and time components (basis.py:1291-1390).
+        Returns (Xb, Q); Xb is zero (basis.py:1388-1389)."""
+        time = np.asarray(time, float)
+        TIME_MIN, TIME_MAX = time.min(), time.max()
+        LON_MIN, LON_MAX = self.lon_min, self.lon_max
+        LAT_MIN, LAT_MAX = self.lat_min, self.lat_max
+        if LON_MAX < LON_MIN:
+            LON_MAX = LON_MAX + 360.
+        k = self.km2deg
+        dlat = self.sigma_D / self.facns * k
+        lat0 = LAT_MIN - LAT_MIN % dlat - self.sigma_D * (1 - 1. / self.facns) * k
+        lat1 = LAT_MAX + 1.5 * dlat
+        ENSLAT1 = np.arange(lat0, lat1, dlat)
+        ENSLAT, ENSLON = [], []
+        for la in ENSLAT1:
+            cl = self._cos(la)
+            dlon = self.sigma_D / self.facns / cl * k
+            lon0 = LON_MIN - LON_MIN % dlon - self.sigma_D * (1 - 1. / self.facns) / cl * k
+            lon1 = LON_MAX + dlon * 1.5
+            ENSLON1 = np.arange(lon0, lon1, dlon)
+            ENSLAT.append(np.repeat(la, ENSLON1.size))
+            ENSLON.append(ENSLON1)
+        self.ENSLAT1 = ENSLAT1
+        self.ENSLAT = np.concatenate(ENSLAT)
+        self.ENSLON = np.concatenate(ENSLON)
+        self.ENST = np.arange(-self.sigma_T * (1 - 1. / self.facnlt),
+                              (TIME_MAX - TIME_MIN) + 1.5 * self.sigma_T / self.facnlt,
+                              self.sigma_T / self.facnlt)
+        self.Nx = self.ENSLAT.size
+        self.nbasis = self.ENST.size * self.Nx
+        self.Q = self.sigma_Q / ((self.facns * self.facnlt)) ** .5 * np.ones(self.nbasis)
+        self.Gauss_xy = self._space()
+        self.Gauss_t, self.Nt = self._time(time)
+        return np.zeros_like(self.Q), self.Q
+
+    def _space(self):
+        """cos^2 x cos^2 footprints of half-width sigma_D (basis.py:1393-1421)."""
+        k = self.km2deg
+        data, indices, sizes = [], [], []
+        for lat0, lon0 in zip(self.ENSLAT, self.ENSLON):
+            cl = self._cos(lat0)
+            xall = self._dlon(self.lon1d - lon0) / k * cl
+            yall = (self.lat1d - lat0) / k
+            ind = np.where((np.abs(xall) <= self.sigma_D) & (np.abs(yall) <= self.sigma_D))[0]
+            xx, yy = xall[ind], yall[ind]
+            if self.mask1d is not None:
+                keep = ~self.mask1d[ind]
+                ind, xx, yy = ind[keep], xx[keep], yy[keep]
+            data.append(mywindow(xx / self.sigma_D) * mywindow(yy / self.sigma_D))
+            indices.append(ind)
+            sizes.append(ind.size)
+        indptr = np.zeros(len(sizes) + 1, dtype=np.int64)
+        indptr[1:] = np.cumsum(sizes)
+        return csc_matrix((np.concatenate(data), np.concatenate(indices), indptr),
+                          shape=(self.lon1d.size, self.Nx))
+
+    def time_weights(self, t):
+        """[(it, fact)] of the time centres active at t (basis.py:1423-1446)."""
+        out = []
+        for it, tc in enumerate(self.ENST):
+            dt = t - tc
+            if abs(dt) < self.sigma_T:
+                fact = self.window(dt / self.sigma_T)
+                if self.normalize_fact:
+                    fact /= self.norm_fact
+                if self.time_spinup is not None and t < self.time_spinup:
+                    fact *= (1 - self.window(t / self.time_spinup))
+                if fact != 0:
+                    out.append((it, fact))
+        return out
+
+    def _time(self, time):
+        Gt, Nt = {}, {}
+        for t in time:
+            g = np.zeros(self.Nx * self.ENST.size)
+            act = self.time_weights(t)
+            for it, fact in act:
+                g[it * self.Nx:(it + 1) * self.Nx] = fact
+            Gt[float(t)], Nt[float(t)] = g, len(act)
+        return Gt, Nt
+
+    def operg(self, t, X):
+        """phi = G(t) X on the grid (basis.py:1489-1524)."""
+        g = self.Gauss_t[float(t)]
+        ind0 = np.nonzero(g)[0]
+        phi = np.zeros(self.lon1d.size)
+        if ind0.size:
+            GtX = (g * X)[ind0].reshape(self.Nt[float(t)], self.Nx)
+            phi += self.Gauss_xy.dot(GtX.sum(axis=0))
+        return phi.reshape(self.shape_phys)
+
+    def operg_transpose(self, t, adphi):
+        """adX = G(t)^T adphi (basis.py:1526-1555; the reference's JAX form
+        1686-1737 takes the vjp of operg, which is this product)."""
+        adX = np.zeros(self.nbasis)
+        g = self.Gauss_t[float(t)]
+        ind0 = np.nonzero(g)[0]
+        if ind0.size:
+            Gt = g[ind0].reshape(self.Nt[float(t)], self.Nx)
+            ad = self.Gauss_xy.T.dot(np.asarray(adphi).ravel())
+            adX[ind0] += (Gt * ad[None, :]).ravel()
+        return adX
+
+
+class MultiOracle:
+    """Concatenation of components (basis.py:4039-4135): the projections add
+    up into one field, the transpose concatenates."""
+
+    def __init__(self, comps):
+        self.comps = comps
+
+    def set_basis(self, time):
+        Xb, Q, self.slices, n = [], [], [], 0
+        for c in self.comps:
+            xb, q = c.set_basis(time)
+            self.slices.append(slice(n, n + c.nbasis))
+            n += c.nbasis
+            Xb.append(xb)
+            Q.append(q)
+        self.nbasis = n
+        return np.concatenate(Xb), np.concatenate(Q)
+
+    def operg(self, t, X):
+        return sum(c.operg(t, X[s]) for c, s in zip(self.comps, self.slices))
+
+    def operg_transpose(self, t, adphi):
+        return np.concatenate([c.operg_transpose(t, adphi) for c in self.comps])

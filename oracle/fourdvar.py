@@ -78,3 +78,76 @@ def cost_and_grad_h0(qgm, h0, hb, nstep, obs, sigma_R=1.0, sigma_B=None, hbg=Non
     if sigma_B is not None:
         ad = ad + (np.asarray(h0) - hbg) / sigma_B ** 2
     return J, ad
+
+
+def checkpoints(nstep, nstep_check, obs_steps):
+    """Model steps at which the cost function is evaluated
+    (mapping/src/inv.py:144-163): step 0, every observation step, every
+    nstep_check-th step, and the last step."""
+    obs_steps = set(int(s) for s in obs_steps)
+    cps, check = [0], 0
+    for i in range(nstep):
+        if i > 0 and (i in obs_steps or check == nstep_check):
+            cps.append(i)
+            if check == nstep_check:
+                check = 0
+        check += 1
+    cps.append(nstep)
+    return cps
+
+
+def cost_and_grad_basis(qgm, basis, time_basis, X0, Xb, Q, h_init, hb, nstep, nstep_check, obs,
+                        sigma_R=1.0, prec=True):
+    """J(X0) and dJ/dX0 for a reduced-basis control forcing the SSH
+    (tools_4Dvar.py:252-400 with Model_qg1l_jax.step / step_adj,
+    mod.py:867-913, 1020-1076): at every checkpoint that is a multiple of
+    nstep_check the basis writes the forcing F = G(t) X; every model call of
+    n steps ends with h += n*dt/86400*F; the adjoint adds n*dt/86400*adh to
+    the forcing adjoint before the model adjoint and maps it back with G^T at
+    the basis checkpoints. prec: X = Q*X0 + Xb, Jb = X0.X0, G = Q*adX + X0."""
+    dt = qgm.dt
+    steps = [int(s) for s in obs.steps if 0 <= s <= nstep]
+    obs_set = set(steps)
+    cps = checkpoints(nstep, nstep_check, [s for s in steps if 0 < s < nstep])
+    X0 = np.asarray(X0, np.float64)
+    if prec:
+        X = Q * X0 + Xb
+        Jb = X0.dot(X0)
+    else:
+        X = X0 + Xb
+        Jb = np.dot(X0, X0 / Q ** 2)
+    h = np.array(h_init, dtype=np.float64)
+    F = np.zeros_like(h)
+    Jo = 0.0
+    states, mis = {}, {}
+    for i in range(len(cps) - 1):
+        c, n = cps[i], cps[i + 1] - cps[i]
+        if c in obs_set:
+            mis[c] = obs.misfit(c, h)
+            Jo += mis[c].dot(mis[c]) / sigma_R ** 2
+        if c % nstep_check == 0:
+            F = basis.operg(time_basis[c // nstep_check], X)
+        states[c] = h
+        h = qgm.step(h, hb, n) + n * dt / (3600 * 24) * F
+    states[nstep] = h
+    if nstep in obs_set:
+        mis[nstep] = obs.misfit(nstep, h)
+        Jo += mis[nstep].dot(mis[nstep]) / sigma_R ** 2
+    J = 0.5 * (Jo + Jb)
+
+    adh = np.zeros_like(h)
+    adF = np.zeros_like(h)
+    adX = np.zeros_like(X)
+    if nstep in obs_set:
+        adh = adh + obs.adj(nstep, mis[nstep], states[nstep])
+    for i in reversed(range(len(cps) - 1)):
+        c, n = cps[i], cps[i + 1] - cps[i]
+        adF = adF + n * dt / (3600 * 24) * np.nan_to_num(adh)
+        adh = qgm.step_adj(adh, states[c], hb, n)
+        if c % nstep_check == 0:
+            adX = adX + basis.operg_transpose(time_basis[c // nstep_check], adF)
+            adF = np.zeros_like(adF)
+        if c in obs_set:
+            adh = adh + obs.adj(c, mis[c], states[c])
+    G = Q * adX + X0 if prec else adX + X0 / Q ** 2
+    return J, G

@@ -1,0 +1,169 @@
+"""Gaussian space-time basis on the GPU (vd_basis_project / _T) against the
+float64 oracle restatement of Basis_gauss3d / Basis_multi."""
+import types
+
+import numpy as np
+import pytest
+import torch
+
+from oracle.basis import Gauss3dOracle, MultiOracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from vardyn_gb300 import build
+    build.build()
+
+
+def rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+COMPS = [dict(sigma_D=100, sigma_T=5, facns=2, facnlt=2, sigma_Q=0.1),
+         dict(sigma_D=60, sigma_T=10, facns=1.5, facnlt=3, sigma_Q=0.2, time_spinup=3.0),
+         dict(sigma_D=80, sigma_T=4, facns=1, facnlt=1, sigma_Q=0.3, flux=True, normalize_fact=False)]
+
+
+def make(geo, dtype, land=True, ny=70, nx=90):
+    from vardyn_gb300.basis import BasisPlan, Gauss3dParams
+    if geo:
+        xc, yc = -70 + np.arange(nx) * 0.05, 30 + np.arange(ny) * 0.05
+    else:
+        xc, yc = np.arange(nx) * 5.0, 3.0 + np.arange(ny) * 5.0
+    mask = None
+    if land:
+        mask = np.zeros((ny, nx), bool)
+        mask[20:31, 40:47] = True
+        mask[-4:, :5] = True
+    time = np.arange(0, 12.01, 0.25)
+    params = [Gauss3dParams(**c) for c in COMPS]
+    plan = BasisPlan(xc, yc, time, params, land=mask, geographic=geo, dtype=dtype)
+    lon, lat = np.meshgrid(xc, yc)
+    orc = MultiOracle([Gauss3dOracle(lon, lat, mask=mask, geo=geo, **c) for c in COMPS])
+    orc.set_basis(time)
+    return plan, orc, time, mask
+
+
+@pytest.mark.parametrize("geo", [False, True])
+def test_project_fp64_matches_oracle(geo):
+    plan, orc, time, mask = make(geo, torch.float64)
+    rng = np.random.default_rng(5)
+    B = 3
+    X = rng.standard_normal((B, plan.nbasis))
+    Xd = torch.as_tensor(X, device="cuda")
+    for k in (0, 1, 7, 20, len(time) - 1):
+        phi = plan.project(k, Xd).cpu().numpy()
+        for b in range(B):
+            ref = orc.operg(time[k], X[b])
+            assert rel(phi[b], ref) < 1e-13, (k, b)
+            assert np.all(phi[b][mask] == 0)
+
+
+@pytest.mark.parametrize("geo", [False, True])
+def test_project_T_fp64_matches_oracle_and_accumulates(geo):
+    plan, orc, time, mask = make(geo, torch.float64)
+    rng = np.random.default_rng(6)
+    B = 2
+    A = rng.standard_normal((B, plan.ny, plan.nx))
+    X0 = rng.standard_normal((B, plan.nbasis))
+    adX = torch.as_tensor(X0.copy(), device="cuda")
+    Ad = torch.as_tensor(A, device="cuda")
+    ks = (0, 9, 33)
+    for k in ks:
+        plan.project_T(k, Ad, adX)
+    got = adX.cpu().numpy()
+    for b in range(B):
+        ref = X0[b] + sum(orc.operg_transpose(time[k], A[b]) for k in ks)
+        assert rel(got[b] - X0[b], ref - X0[b]) < 1e-13
+    # the adjoint input is read only
+    assert torch.equal(Ad.cpu(), torch.as_tensor(A))
+
+
+def test_dot_product_identity_fp64():
+    plan, orc, time, mask = make(False, torch.float64)
+    rng = np.random.default_rng(7)
+    X = torch.as_tensor(rng.standard_normal((1, plan.nbasis)), device="cuda")
+    A = torch.as_tensor(rng.standard_normal((1, plan.ny, plan.nx)), device="cuda")
+    for k in (2, 30):
+        phi = plan.project(k, X)
+        adX = torch.zeros_like(X)
+        plan.project_T(k, A, adX)
+        lhs = float((phi * A).sum())
+        rhs = float((X * adX).sum())
+        assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+
+
+def test_project_fp32_and_accumulate():
+    plan, orc, time, mask = make(False, torch.float32)
+    rng = np.random.default_rng(8)
+    X = rng.standard_normal((2, plan.nbasis))
+    Xd = torch.as_tensor(X, device="cuda", dtype=torch.float32)
+    base = torch.as_tensor(rng.standard_normal((2, plan.ny, plan.nx)), device="cuda", dtype=torch.float32)
+    out = base.clone()
+    plan.project(12, Xd, out=out, accumulate=True)
+    for b in range(2):
+        ref = orc.operg(time[12], X[b])
+        assert rel(out[b].double().cpu().numpy() - base[b].double().cpu().numpy(), ref) < 2e-6
+    A = rng.standard_normal((2, plan.ny, plan.nx))
+    adX = torch.zeros(2, plan.nbasis, device="cuda", dtype=torch.float32)
+    plan.project_T(12, torch.as_tensor(A, device="cuda", dtype=torch.float32), adX)
+    for b in range(2):
+        assert rel(adX[b].double().cpu().numpy(), orc.operg_transpose(time[12], A[b])) < 2e-6
+
+
+def test_reference_facing_classes():
+    """Basis_gauss3d / Basis_multi with the reference's (config, State)
+    construction and State-dict semantics."""
+    from vardyn_gb300.basis import Basis_gauss3d, Basis_multi
+    ny, nx = 50, 60
+    lon1, lat1 = -40 + np.arange(nx) * 0.05, 35 + np.arange(ny) * 0.05
+    lon, lat = np.meshgrid(lon1, lat1)
+    mask = np.zeros((ny, nx), bool)
+    mask[5:9, 10:20] = True
+    State = types.SimpleNamespace(lon=lon, lat=lat, mask=mask, ny=ny, nx=nx)
+
+    def cfg(c):
+        return types.SimpleNamespace(name_mod_var="ssh", flag_variable_Q=False, compute_velocities=False,
+                                     c_grid_var=None, normalize_fact=c.get("normalize_fact", True),
+                                     flux=c.get("flux", False), time_spinup=c.get("time_spinup"),
+                                     sigma_D=c["sigma_D"], sigma_T=c["sigma_T"], facns=c["facns"],
+                                     facnlt=c["facnlt"], sigma_Q=c["sigma_Q"])
+    time = np.arange(0, 6.01, 0.5)
+    rng = np.random.default_rng(9)
+    # single component
+    b1 = Basis_gauss3d(types.SimpleNamespace(BASIS=cfg(COMPS[0])), State, dtype=torch.float64)
+    Xb, Q = b1.set_basis(time, return_q=True)
+    o1 = Gauss3dOracle(lon, lat, mask=mask, geo=True, **COMPS[0])
+    Xb_o, Q_o = o1.set_basis(time)
+    assert np.array_equal(Q, Q_o) and np.array_equal(Xb, Xb_o)
+    X = rng.standard_normal(b1.nbasis)
+    params = {"ssh": np.zeros((ny, nx))}
+    b1.operg(2.5, X, State=params)
+    assert rel(params["ssh"], o1.operg(2.5, X)) < 1e-13
+    ad = {"ssh": rng.standard_normal((ny, nx))}
+    ad0 = ad["ssh"].copy()
+    adX = b1.operg_transpose(2.5, ad)
+    assert rel(adX, o1.operg_transpose(2.5, ad0)) < 1e-13
+    assert np.all(ad["ssh"] == 0)
+    # multi
+    bm = Basis_multi(types.SimpleNamespace(BASIS={"a": cfg(COMPS[0]), "b": cfg(COMPS[1])}), State,
+                     dtype=torch.float64)
+    Xb, Q = bm.set_basis(time, return_q=True)
+    om = MultiOracle([Gauss3dOracle(lon, lat, mask=mask, geo=True, **c) for c in COMPS[:2]])
+    _, Qm = om.set_basis(time)
+    assert np.array_equal(Q, Qm)
+    X = rng.standard_normal(bm.nbasis)
+    params = {"ssh": np.ones((ny, nx))}
+    bm.operg(4.0, X, State=params)
+    assert rel(params["ssh"], om.operg(4.0, X)) < 1e-13
+    cat = bm.operg(4.0, X)
+    parts = [c.operg(4.0, X[s]).ravel() for c, s in zip(om.comps, om.slices)]
+    assert rel(cat, np.concatenate(parts)) < 1e-13
+    ad = {"ssh": rng.standard_normal((ny, nx))}
+    ad0 = ad["ssh"].copy()
+    adX = bm.operg_transpose(4.0, ad)
+    assert rel(adX, om.operg_transpose(4.0, ad0)) < 1e-13
+    assert np.all(ad["ssh"] == 0)

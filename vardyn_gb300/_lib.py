@@ -35,6 +35,29 @@ class VdDesc(ctypes.Structure):
 VD_DST_AUTO, VD_DST_FMA = 0, 1
 
 
+class VdBasisGrid(ctypes.Structure):
+    _fields_ = [
+        ("ny", ctypes.c_int), ("nx", ctypes.c_int), ("dtype", ctypes.c_int),
+        ("geographic", ctypes.c_int),
+        ("xc_host", ctypes.POINTER(ctypes.c_double)),
+        ("yc_host", ctypes.POINTER(ctypes.c_double)),
+        ("land_host", ctypes.POINTER(ctypes.c_int8)),
+        ("ntime", ctypes.c_int),
+        ("time_host", ctypes.POINTER(ctypes.c_double)),
+        ("host_only", ctypes.c_int),
+    ]
+
+
+class VdGauss3dParams(ctypes.Structure):
+    _fields_ = [
+        ("sigma_D", ctypes.c_double), ("sigma_T", ctypes.c_double),
+        ("facns", ctypes.c_double), ("facnlt", ctypes.c_double),
+        ("sigma_Q", ctypes.c_double),
+        ("normalize_fact", ctypes.c_int), ("flux", ctypes.c_int),
+        ("has_time_spinup", ctypes.c_int), ("time_spinup", ctypes.c_double),
+    ]
+
+
 P = ctypes.c_void_p
 I = ctypes.c_int
 LL = ctypes.c_longlong
@@ -68,13 +91,26 @@ SIGNATURES = {
     "vd_qg1l_advance_adj": (I, [P, I, P, I, I, I, P, P, P, SZ, P]),
     "vd_qg1l_init_state_adj": (I, [P, I, P, P, P, P]),
     "vd_qg1l_finalize": (I, [P, I, P, P, P, D, P, P]),
+    "vd_qg1l_finalize_adj": (I, [P, I, P, P, D, P, P]),
     "vd_obs_misfit": (I, [I, I, P, LL, P, P, P, P, P, P, P]),
     "vd_obs_adjoint": (I, [I, I, P, LL, P, P, P, P, P, P, P, P]),
     "vd_sumsq_f64": (I, [I, I, P, P, P, P]),
     "vd_sumsq_gather_f64": (I, [I, I, P, P, P, D, P, P]),
     "vd_dot_f64": (I, [I, LL, P, P, P, P]),
     "vd_axpby": (I, [I, LL, D, P, D, P, P]),
+    "vd_diag_axpy": (I, [I, LL, LL, P, P, P, P, P]),
     "vd_copy": (I, [I, LL, P, P, P]),
+    "vd_basis_plan_create": (I, [ctypes.POINTER(P), ctypes.POINTER(VdBasisGrid), I,
+                                 ctypes.POINTER(VdGauss3dParams)]),
+    "vd_basis_plan_destroy": (I, [P]),
+    "vd_basis_nbasis": (LL, [P]),
+    "vd_basis_component": (I, [P, I, ctypes.POINTER(LL), ctypes.POINTER(I), ctypes.POINTER(I)]),
+    "vd_basis_lattice": (I, [P, I, P, P, P]),
+    "vd_basis_q": (I, [P, P]),
+    "vd_basis_time_weights": (I, [P, I, I, ctypes.POINTER(I), P, P]),
+    "vd_basis_workspace_bytes": (SZ, [P, I]),
+    "vd_basis_project": (I, [P, I, I, P, LL, P, I, P, SZ, P]),
+    "vd_basis_project_T": (I, [P, I, I, P, P, LL, P, SZ, P]),
     "vd_fill": (I, [I, LL, D, P, P]),
 }
 

@@ -1,0 +1,327 @@
+"""Gaussian space-time reduced basis on the GPU (Basis_gauss3d / Basis_multi).
+
+:class:`BasisPlan` owns one ``vd_basis_plan`` (lattice and banded footprint
+tables built by the library on the host, uploaded once) and projects batched
+control vectors with ``vd_basis_project`` / ``vd_basis_project_T`` on torch's
+current stream.
+
+:class:`Basis_gauss3d` and :class:`Basis_multi` mirror the reference classes
+(mapping/src/basis.py:1170-1555 and 4039-4135): the constructor takes
+``(config, State)``, ``set_basis(time, return_q=True)`` returns ``(Xb, Q)``,
+``operg(t, X, State=State.params)`` writes the projected field into the
+parameter dict, and ``operg_transpose(t, adState=adState.params)`` returns
+the coefficient adjoint and zeroes the parameter adjoint. ``t`` is looked up
+among the basis times by exact equality, as the reference does
+(basis.py:1636-1640).
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class Gauss3dParams:
+    """Parameters of one Basis_gauss3d component (config.BASIS fields,
+    basis.py:1176-1187)."""
+
+    def __init__(self, sigma_D, sigma_T, facns=1.0, facnlt=2.0, sigma_Q=1.0, normalize_fact=True,
+                 flux=False, time_spinup=None):
+        self.sigma_D = float(sigma_D)
+        self.sigma_T = float(sigma_T)
+        self.facns = float(facns)
+        self.facnlt = float(facnlt)
+        self.sigma_Q = float(sigma_Q)
+        self.normalize_fact = bool(normalize_fact)
+        self.flux = bool(flux)
+        self.time_spinup = time_spinup
+
+    def to_c(self):
+        return _lib.VdGauss3dParams(self.sigma_D, self.sigma_T, self.facns, self.facnlt, self.sigma_Q,
+                                    int(self.normalize_fact), int(self.flux),
+                                    int(self.time_spinup is not None),
+                                    float(self.time_spinup) if self.time_spinup is not None else 0.0)
+
+
+class BasisPlan:
+    """One or more Gaussian components on a rectilinear grid.
+
+    xc [nx], yc [ny]: column / row coordinates (km, or lon/lat in degrees when
+    ``geographic``); time: the basis times in days (set_basis's argument);
+    land: bool [ny, nx] (True = excluded) or None. ``host_only`` builds the
+    tables without a GPU (queries only)."""
+
+    def __init__(self, xc, yc, time, comps, land=None, geographic=False, dtype=torch.float32,
+                 device=None, host_only=False):
+        self.xc = np.ascontiguousarray(xc, dtype=np.float64)
+        self.yc = np.ascontiguousarray(yc, dtype=np.float64)
+        self.ny, self.nx = self.yc.size, self.xc.size
+        self.times = np.ascontiguousarray(np.atleast_1d(time), dtype=np.float64)
+        self.comps = list(comps)
+        self.dtype = dtype
+        self.host_only = host_only
+        self.device = None
+        if not host_only:
+            if not torch.cuda.is_available():
+                raise RuntimeError("vardyn_gb300 needs a CUDA device (no CPU path)")
+            dev = torch.device(device or "cuda")
+            self.device = torch.device("cuda", dev.index if dev.index is not None else torch.cuda.current_device())
+        self._land = None
+        if land is not None:
+            land = np.asarray(land, dtype=bool)
+            if land.shape != (self.ny, self.nx):
+                raise ValueError("land must be [ny, nx]")
+            self._land = np.ascontiguousarray(land.astype(np.int8))
+        dptr = ctypes.POINTER(ctypes.c_double)
+        grid = _lib.VdBasisGrid(
+            self.ny, self.nx, _lib.VD_F64 if dtype == torch.float64 else _lib.VD_F32, int(geographic),
+            self.xc.ctypes.data_as(dptr), self.yc.ctypes.data_as(dptr),
+            self._land.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)) if self._land is not None else None,
+            self.times.size, self.times.ctypes.data_as(dptr), int(host_only))
+        params = (_lib.VdGauss3dParams * len(self.comps))(*[c.to_c() for c in self.comps])
+        self.lib = _lib.load()
+        h = ctypes.c_void_p()
+        if not host_only:
+            torch.cuda.set_device(self.device)
+        _lib.check(self.lib.vd_basis_plan_create(ctypes.byref(h), ctypes.byref(grid), len(self.comps), params),
+                   "vd_basis_plan_create")
+        self._h = h
+        self.nbasis = int(self.lib.vd_basis_nbasis(h))
+        self._ws = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                self.lib.vd_basis_plan_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    # ------------------------------------------------------------ queries
+    def component(self, c):
+        off, nt, ns = ctypes.c_longlong(), ctypes.c_int(), ctypes.c_int()
+        _lib.check(self.lib.vd_basis_component(self._h, c, ctypes.byref(off), ctypes.byref(nt),
+                                               ctypes.byref(ns)), "vd_basis_component")
+        return off.value, nt.value, ns.value
+
+    def lattice(self, c):
+        """(ENST, ENSLAT, ENSLON) of component c."""
+        _, nt, ns = self.component(c)
+        enst, lat, lon = np.zeros(nt), np.zeros(ns), np.zeros(ns)
+        _lib.check(self.lib.vd_basis_lattice(self._h, c, enst.ctypes.data, lat.ctypes.data, lon.ctypes.data),
+                   "vd_basis_lattice")
+        return enst, lat, lon
+
+    def q(self):
+        """Prior standard deviation of every coefficient (float64 [nbasis])."""
+        q = np.zeros(self.nbasis)
+        _lib.check(self.lib.vd_basis_q(self._h, q.ctypes.data), "vd_basis_q")
+        return q
+
+    def time_weights(self, k, c):
+        n = ctypes.c_int()
+        _lib.check(self.lib.vd_basis_time_weights(self._h, k, c, ctypes.byref(n), None, None),
+                   "vd_basis_time_weights")
+        it = np.zeros(max(n.value, 1), dtype=np.int32)
+        w = np.zeros(max(n.value, 1))
+        _lib.check(self.lib.vd_basis_time_weights(self._h, k, c, ctypes.byref(n), it.ctypes.data,
+                                                  w.ctypes.data), "vd_basis_time_weights")
+        return list(zip(it[:n.value].tolist(), w[:n.value].tolist()))
+
+    def time_index(self, t):
+        """Index of basis time t (exact match, as basis.py:1636-1640)."""
+        k = np.nonzero(self.times == float(t))[0]
+        if k.size == 0:
+            raise KeyError(f"time {t} is not a basis time")
+        return int(k[0])
+
+    # ------------------------------------------------------------ compute
+    def workspace(self, batch):
+        n = int(self.lib.vd_basis_workspace_bytes(self._h, batch))
+        if self._ws is None or self._ws.numel() < n:
+            self._ws = torch.empty(max(n, 256), dtype=torch.uint8, device=self.device)
+        return self._ws
+
+    def _batch_X(self, X):
+        if X.dim() == 1:
+            X = X.unsqueeze(0)
+        if X.dim() != 2 or X.shape[1] != self.nbasis:
+            raise ValueError(f"control must be [batch, {self.nbasis}]")
+        if X.dtype != self.dtype or X.device != self.device or X.stride(1) != 1 or X.stride(0) < self.nbasis:
+            raise ValueError("control must be a contiguous tensor of the plan's dtype on its device")
+        return X
+
+    def project(self, k, X, out=None, accumulate=False):
+        """phi [B, ny, nx] = G(t_k) X (+ out if accumulate)."""
+        X = self._batch_X(X)
+        B = X.shape[0]
+        if out is None:
+            out = torch.empty(B, self.ny, self.nx, dtype=self.dtype, device=self.device)
+            accumulate = False
+        ws = self.workspace(B)
+        _lib.check(self.lib.vd_basis_project(self._h, B, int(k), _ptr(X), X.stride(0), _ptr(out),
+                                             int(bool(accumulate)), _ptr(ws), ws.numel(), _stream()),
+                   "vd_basis_project")
+        return out
+
+    def project_T(self, k, adphi, adX):
+        """adX [B, nbasis] += G(t_k)^T adphi [B, ny, nx]."""
+        adX = self._batch_X(adX)
+        B = adX.shape[0]
+        adphi = adphi.reshape(B, self.ny, self.nx)
+        if not adphi.is_contiguous():
+            raise ValueError("adphi must be contiguous")
+        ws = self.workspace(B)
+        _lib.check(self.lib.vd_basis_project_T(self._h, B, int(k), _ptr(adphi), _ptr(adX), adX.stride(0),
+                                               _ptr(ws), ws.numel(), _stream()), "vd_basis_project_T")
+        return adX
+
+
+# ---------------------------------------------------------------------------
+# Reference-facing classes
+# ---------------------------------------------------------------------------
+def _grid_axes(State):
+    """1-D axes of a rectilinear State grid (lon varies along columns only,
+    lat along rows only)."""
+    lon = np.asarray(State.lon, dtype=np.float64)
+    lat = np.asarray(State.lat, dtype=np.float64)
+    if lon.ndim == 1 and lat.ndim == 1:
+        return lon, lat
+    if not (np.all(lon == lon[:1, :]) and np.all(lat == lat[:, :1])):
+        raise NotImplementedError("the GPU basis needs a rectilinear grid (lon per column, lat per row)")
+    return lon[0, :].copy(), lat[:, 0].copy()
+
+
+def _params_from_config(cb):
+    for name, bad in (("flag_variable_Q", True), ("compute_velocities", True)):
+        if getattr(cb, name, False) == bad:
+            raise NotImplementedError(f"config.BASIS.{name} is not supported by the GPU basis")
+    if getattr(cb, "c_grid_var", None) is not None:
+        raise NotImplementedError("config.BASIS.c_grid_var is not supported by the GPU basis")
+    return Gauss3dParams(cb.sigma_D, cb.sigma_T, facns=cb.facns, facnlt=cb.facnlt, sigma_Q=cb.sigma_Q,
+                         normalize_fact=cb.normalize_fact, flux=getattr(cb, "flux", False),
+                         time_spinup=getattr(cb, "time_spinup", None))
+
+
+def _to_tensor(x, dtype, device):
+    if isinstance(x, torch.Tensor):
+        return x.to(device=device, dtype=dtype).contiguous(), True
+    return torch.as_tensor(np.asarray(x, dtype=np.float64), device=device).to(dtype).contiguous(), False
+
+
+class Basis_gauss3d:
+    """Drop-in for Basis_gauss3d / Basis_gauss3d_jax (basis.py:1170-1739)
+    with the GPU projection. Arrays may be NumPy (returned as NumPy) or torch
+    tensors (returned as tensors on the plan's device)."""
+
+    def __init__(self, config, State, multi_mode=False, dtype=torch.float32, device=None):
+        self.params = _params_from_config(config.BASIS)
+        self.name_mod_var = config.BASIS.name_mod_var
+        self.multi_mode = multi_mode
+        self.lon, self.lat = _grid_axes(State)
+        self.geographic = True
+        self.ny, self.nx = State.ny, State.nx
+        self.mask = None
+        if getattr(State, "mask", None) is not None and np.any(State.mask):
+            self.mask = np.asarray(State.mask, dtype=bool)
+        self.dtype = dtype
+        self.device = torch.device(device or "cuda")
+        self.plan = None
+
+    def _components(self):
+        return [self.params]
+
+    def set_basis(self, time, return_q=False, **kwargs):
+        self.plan = BasisPlan(self.lon, self.lat, time, self._components(), land=self.mask,
+                              geographic=self.geographic, dtype=self.dtype, device=self.device)
+        self.nbasis = self.plan.nbasis
+        self.time = np.asarray(time, dtype=np.float64)
+        if return_q:
+            Q = self.plan.q()
+            return np.zeros_like(Q), Q
+
+    def _phi(self, t, X):
+        Xt, is_t = _to_tensor(X, self.dtype, self.device)
+        phi = self.plan.project(self.plan.time_index(t), Xt.reshape(1, -1))[0]
+        return phi, is_t
+
+    def operg(self, t, X, State=None):
+        """Projection to the grid (basis.py:1489-1524, 1690-1717)."""
+        phi, is_t = self._phi(t, X)
+        if State is None:
+            return phi if is_t else phi.double().cpu().numpy()
+        cur = State.get(self.name_mod_var)
+        if not self.multi_mode or cur is None:
+            State[self.name_mod_var] = phi if is_t else phi.double().cpu().numpy()
+        else:
+            State[self.name_mod_var] = cur + (phi if isinstance(cur, torch.Tensor) else phi.double().cpu().numpy())
+
+    def operg_transpose(self, t, adState):
+        """Coefficient adjoint; zeroes adState[name_mod_var] unless in
+        multi mode (basis.py:1526-1555, 1719-1737)."""
+        ad = adState.get(self.name_mod_var)
+        if ad is None:
+            ad = np.zeros((self.ny, self.nx))
+        adt, is_t = _to_tensor(ad, self.dtype, self.device)
+        adX = torch.zeros(1, self.nbasis, dtype=self.dtype, device=self.device)
+        self.plan.project_T(self.plan.time_index(t), adt.reshape(1, self.ny, self.nx), adX)
+        if not self.multi_mode:
+            adState[self.name_mod_var] = ad * 0.
+        return adX[0] if is_t else adX[0].double().cpu().numpy()
+
+
+class Basis_multi:
+    """Drop-in for Basis_multi (basis.py:4039-4135) over Gaussian components.
+    ``config.BASIS`` maps names to component configs, as in the reference.
+    One plan holds every component, so one projection call sums them into
+    the parameter field (the reference zeroes it, then adds each component,
+    basis.py:4097-4106); without a State the components' fields come back
+    concatenated, as the reference's operg returns them (4108-4114)."""
+
+    def __init__(self, config, State, verbose=True, dtype=torch.float32, device=None):
+        subs = [config.BASIS[k] for k in config.BASIS]
+        self.params = [_params_from_config(b) for b in subs]
+        self.name_mod_var = subs[0].name_mod_var
+        if any(b.name_mod_var != self.name_mod_var for b in subs):
+            raise NotImplementedError("all components must project onto the same parameter")
+        self.lon, self.lat = _grid_axes(State)
+        self.ny, self.nx = State.ny, State.nx
+        self.mask = None
+        if getattr(State, "mask", None) is not None and np.any(State.mask):
+            self.mask = np.asarray(State.mask, dtype=bool)
+        self.dtype = dtype
+        self.device = torch.device(device or "cuda")
+        self.geographic = True
+        self.multi_mode = False
+        self.plan = None
+
+    def _components(self):
+        return list(self.params)
+
+    set_basis = Basis_gauss3d.set_basis
+    _phi = Basis_gauss3d._phi
+    operg_transpose = Basis_gauss3d.operg_transpose
+
+    def operg(self, t, X, State=None):
+        if State is not None:
+            return Basis_gauss3d.operg(self, t, X, State=State)
+        Xt, is_t = _to_tensor(X, self.dtype, self.device)
+        k = self.plan.time_index(t)
+        parts = []
+        for c in range(len(self.params)):
+            off, nt, ns = self.plan.component(c)
+            Xc = torch.zeros_like(Xt)
+            Xc[off:off + nt * ns] = Xt[off:off + nt * ns]
+            parts.append(self.plan.project(k, Xc.reshape(1, -1))[0].reshape(-1))
+        phi = torch.cat(parts)
+        return phi if is_t else phi.double().cpu().numpy()

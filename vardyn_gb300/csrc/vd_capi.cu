@@ -26,6 +26,8 @@ int init_state_adj_impl(const vd_qg1l_plan*, int, const T*, const T*, T*, cudaSt
 template <typename T>
 int finalize_impl(const vd_qg1l_plan*, int, const T*, const T*, const T*, double, int, T*, cudaStream_t);
 template <typename T>
+int finalize_adj_impl(const vd_qg1l_plan*, int, const T*, T*, double, T*, cudaStream_t);
+template <typename T>
 int copy_impl(const vd_qg1l_plan*, int, const T*, T*, int, cudaStream_t);
 template <typename T>
 int zero_impl(long long, T*, cudaStream_t);
@@ -465,4 +467,15 @@ extern "C" vd_status vd_qg1l_finalize(const vd_qg1l_plan* p, int B, const void* 
                                       (float*)h_out, st)
                : finalize_impl<double>(p, B, (const double*)h, (const double*)hb, (const double*)forcing, coef, 1,
                                        (double*)h_out, st);
+}
+
+extern "C" vd_status vd_qg1l_finalize_adj(const vd_qg1l_plan* p, int B, const void* adh_out, void* adforcing,
+                                          double coef, void* adh, void* stream)
+{
+    if (!p || B <= 0 || !adh_out || !adh) return VD_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    return p->d.dtype == VD_F32
+               ? finalize_adj_impl<float>(p, B, (const float*)adh_out, (float*)adforcing, coef, (float*)adh, st)
+               : finalize_adj_impl<double>(p, B, (const double*)adh_out, (double*)adforcing, coef, (double*)adh,
+                                           st);
 }

@@ -232,6 +232,16 @@ k_sumsq_gather(const int32_t* __restrict__ off, const int32_t* __restrict__ perm
 }
 
 template <typename T>
+__global__ void k_diag_axpy(long long n, long long period, const T* __restrict__ d, const T* x, const T* y,
+                            T* out)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const T v = d[k % period] * x[k] + (y ? y[k] : T(0));
+    out[k] = v;
+}
+
+template <typename T>
 __global__ void k_fill_value(long long n, T v, T* __restrict__ y)
 {
     const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -276,6 +286,24 @@ extern "C" vd_status vd_fill(int dtype, long long n, double value, void* y, void
         k_fill_value<float><<<grid, 256, 0, st>>>(n, (float)value, (float*)y);
     else
         k_fill_value<double><<<grid, 256, 0, st>>>(n, value, (double*)y);
+    VD_LAUNCH_CHECK();
+    return VD_OK;
+}
+
+extern "C" vd_status vd_diag_axpy(int dtype, long long n, long long period, const void* d, const void* x,
+                                  const void* y, void* out, void* stream)
+{
+    if (n < 0 || period <= 0 || (dtype != VD_F32 && dtype != VD_F64)) return VD_ERR_ARG;
+    if (n == 0) return VD_OK;
+    if (!d || !x || !out) return VD_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    const unsigned grid = (unsigned)((n + 255) / 256);
+    if (dtype == VD_F32)
+        k_diag_axpy<float><<<grid, 256, 0, st>>>(n, period, (const float*)d, (const float*)x, (const float*)y,
+                                                 (float*)out);
+    else
+        k_diag_axpy<double><<<grid, 256, 0, st>>>(n, period, (const double*)d, (const double*)x,
+                                                  (const double*)y, (double*)out);
     VD_LAUNCH_CHECK();
     return VD_OK;
 }

@@ -420,6 +420,24 @@ __global__ void k_finalize(QGGeom G, int nf, const T* __restrict__ h, const T* _
     out[o] = v;
 }
 
+// Adjoint of k_finalize: the forcing adjoint takes coef * adh_out everywhere
+// (mod.py:1058-1068); the state adjoint is adh_out except on the walls (set
+// to hb) and on land (set to a constant), where it is 0.
+template <typename T>
+__global__ void k_finalize_adj(QGGeom G, int nf, const T* __restrict__ adout, T* __restrict__ adforcing, T coef,
+                               T* __restrict__ adh)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int f = blockIdx.z;
+    if (i >= G.nx || j >= G.ny || f >= nf) return;
+    const long long o = f * G.fs + (long long)j * G.nx + i;
+    const T a = adout[o];
+    if (adforcing) adforcing[o] += coef * a;
+    const bool wall = (i == 0 || j == 0 || i == G.nx - 1 || j == G.ny - 1);
+    adh[o] = (wall || G.mask[(long long)j * G.nx + i] == 0) ? T(0) : a;
+}
+
 template <typename T>
 __global__ void k_h2uv(QGGeom G, int nf, const T* __restrict__ h, T* __restrict__ u, T* __restrict__ v)
 {
@@ -677,6 +695,15 @@ int finalize_impl(const vd_qg1l_plan* p, int nf, const T* h, const T* hb, const 
 }
 
 template <typename T>
+int finalize_adj_impl(const vd_qg1l_plan* p, int nf, const T* adout, T* adforcing, double coef, T* adh,
+                      cudaStream_t st)
+{
+    k_finalize_adj<T><<<pgrid(p, nf), kBlock, 0, st>>>(p->geom, nf, adout, adforcing, (T)coef, adh);
+    VD_LAUNCH_CHECK();
+    return VD_OK;
+}
+
+template <typename T>
 int copy_impl(const vd_qg1l_plan* p, int nf, const T* src, T* dst, int zero_land, cudaStream_t st)
 {
     k_copy_masked<T><<<pgrid(p, nf), kBlock, 0, st>>>(p->geom, nf, src, dst, zero_land);
@@ -721,6 +748,7 @@ int rhs_impl(const vd_qg1l_plan* p, int nf, const T* u, const T* v, const T* q, 
     template int init_state_adj_impl<T>(const vd_qg1l_plan*, int, const T*, const T*, T*, cudaStream_t);  \
     template int finalize_impl<T>(const vd_qg1l_plan*, int, const T*, const T*, const T*, double, int,    \
                                   T*, cudaStream_t);                                                      \
+    template int finalize_adj_impl<T>(const vd_qg1l_plan*, int, const T*, T*, double, T*, cudaStream_t);  \
     template int copy_impl<T>(const vd_qg1l_plan*, int, const T*, T*, int, cudaStream_t);                 \
     template int zero_impl<T>(long long, T*, cudaStream_t);                                               \
     template int h2uv_impl<T>(const vd_qg1l_plan*, int, const T*, T*, T*, cudaStream_t);                  \

@@ -27,10 +27,11 @@ sweep (one extra forward, memory (nstep/K)*2 + 2*nstage*K fields).
 import ctypes
 import math
 
+import numpy as np
 import torch
 
 from . import _lib
-from .qg1l import QG1LPlan
+from .qg1l import QG1LPlan, SECONDS_PER_DAY
 
 
 def _p(t):
@@ -224,6 +225,215 @@ class QGWindows4DVar:
         with torch.cuda.stream(s):
             with torch.cuda.graph(g, stream=s):
                 self._run(self.h0_static)
+        torch.cuda.current_stream().wait_stream(s)
+        torch.cuda.synchronize()
+        self.graph = g
+        return g
+
+
+def checkpoints(nstep, nstep_check, obs_steps):
+    """Model steps at which the cost function is evaluated
+    (mapping/src/inv.py:144-163): step 0, every observation step, every
+    nstep_check-th step, and the last step."""
+    obs_steps = set(int(s) for s in obs_steps)
+    cps, check = [0], 0
+    for i in range(nstep):
+        if i > 0 and (i in obs_steps or check == nstep_check):
+            cps.append(i)
+            if check == nstep_check:
+                check = 0
+        check += 1
+    cps.append(nstep)
+    return cps
+
+
+class QGBasis4DVar:
+    """Cost and gradient of ``B`` windows whose control is reduced-basis
+    coefficients forcing the SSH (the reference's Inv_4Dvar with a basis,
+    mapping/src/inv.py:142-215, tools_4Dvar.py:252-400).
+
+    Forward, per checkpoint interval [c_i, c_{i+1}) of n_i steps
+    (checkpoints of inv.py:144-163):
+      misfit at c_i if observed;
+      if c_i is a multiple of nstep_check: F = G(t_k) X with t_k the k-th
+        basis time, k = c_i / nstep_check (operg, tools_4Dvar.py:299-304);
+      h <- Qgm.step(h, hb, n_i) + n_i*dt/86400 * F (mod.py:867-913): PV is
+        re-derived from SSH at every interval start (jqgm.py:536).
+    Reverse: adF += n_i*dt/86400 * adh, model adjoint of the interval,
+    adX += G(t_k)^T adF and adF = 0 at basis checkpoints
+    (tools_4Dvar.py:355-392, mod.py:1058-1076).
+    Background term (tools_4Dvar.py:262-273, 342-349, 395-398):
+      prec=True   X = Q*X0 + Xb, Jb = X0.X0,      G = Q*adX + X0
+      prec=False  X = X0 + Xb,   Jb = X0.X0/Q^2,  G = adX + X0/Q^2
+    J = (Jo + Jb)/2 with Jo = sum misfit^2/sigma_R^2.
+
+    Storage: the SSH at every interval start ([ninterval, B, ny, nx]) and the
+    stage trajectory of one interval (recomputed per interval in reverse).
+    """
+
+    def __init__(self, plan: QG1LPlan, basis, h_init, hb, nstep, nstep_check, obs, Q=None, Xb=None,
+                 sigma_R=1.0, prec=True):
+        self.plan, self.basis, self.obs = plan, basis, obs
+        self.B = obs.B
+        self.nstep, self.nstep_check = int(nstep), int(nstep_check)
+        self.sigma_R = float(sigma_R)
+        self.prec = bool(prec)
+        B, ny, nx = self.B, plan.ny, plan.nx
+        dev, dt = plan.device, plan.dtype
+        if basis.dtype != dt:
+            raise TypeError("basis and model plans must share the dtype")
+        self.vd_dtype = _lib.VD_F64 if dt == torch.float64 else _lib.VD_F32
+        self.nb = basis.nbasis
+        need = self.nstep // self.nstep_check + 1
+        if basis.times.size < need:
+            raise ValueError(f"the basis has {basis.times.size} times, the window needs {need}")
+        self.hb = plan._as_batch(hb, "hb")
+        self.h_init = plan._as_batch(h_init, "h_init").clone()
+        if self.hb.shape[0] != B or self.h_init.shape[0] != B:
+            raise ValueError("hb and h_init must have one field per window")
+        zero_bg = float(self.hb.abs().max()) == 0.0
+        self.qb = torch.zeros(B, ny, nx, dtype=dt, device=dev)
+        self.hb_arg = None if zero_bg else self.hb
+        self.qb_arg = None if zero_bg else self.qb
+        q = basis.q() if Q is None else np.asarray(Q, dtype=np.float64)
+        self.Q = torch.as_tensor(q, device=dev).to(dt)
+        self.Qinv2 = torch.as_tensor(1.0 / q ** 2, device=dev).to(dt)
+        xb = np.zeros(self.nb) if Xb is None else np.asarray(Xb, dtype=np.float64)
+        self.Xb = torch.as_tensor(np.tile(xb, (B, 1)), device=dev).to(dt)
+        self.obs_steps = sorted(int(s) for s in obs.steps if 0 <= s <= self.nstep)
+        self.cps = checkpoints(self.nstep, self.nstep_check, [s for s in self.obs_steps if 0 < s < self.nstep])
+        self.nint = len(self.cps) - 1
+        K = max(self.cps[i + 1] - self.cps[i] for i in range(self.nint))
+        self.K = K
+        self.traj = plan.new_traj(B, K)
+        self.S = plan.nstage
+        self.tv = self.traj.view(-1, 2, B, ny, nx)
+        self.snap = torch.zeros(self.nint, B, ny, nx, dtype=dt, device=dev)
+        z = lambda: torch.zeros(B, ny, nx, dtype=dt, device=dev)  # noqa: E731
+        self.h, self.F, self.adh, self.adq, self.adF = z(), z(), z(), z(), z()
+        self.X = torch.zeros(B, self.nb, dtype=dt, device=dev)
+        self.adX = torch.zeros(B, self.nb, dtype=dt, device=dev)
+        self.gb = torch.zeros(B, self.nb, dtype=dt, device=dev)
+        self.grad = torch.zeros(B, self.nb, dtype=dt, device=dev)
+        self.J = torch.zeros(B, dtype=torch.float64, device=dev)
+        self.dot_scratch = torch.zeros(B, _lib.DOT_SCRATCH, dtype=torch.float64, device=dev)
+        self.graph = None
+
+    def memory_bytes(self):
+        n = 0
+        for t in (self.traj, self.snap):
+            n += t.numel() * t.element_size()
+        return n
+
+    # ------------------------------------------------------------------
+    def _fill0(self, t):
+        _lib.call("vd_fill", self.vd_dtype, ctypes.c_longlong(t.numel()), 0.0, _p(t), _stream())
+
+    def _copy(self, src, dst):
+        _lib.call("vd_copy", self.vd_dtype, ctypes.c_longlong(src.numel()), _p(src), _p(dst), _stream())
+
+    def _coef(self, n):
+        return n * self.plan.dt / SECONDS_PER_DAY
+
+    def _interval_forward(self, i):
+        """Recompute the stage trajectory of interval i from its start SSH."""
+        p, B = self.plan, self.B
+        n = self.cps[i + 1] - self.cps[i]
+        self._copy(self.snap[i], self.tv[0, 0])
+        p.init_state(self.tv[0, 0], self.hb, self.tv[0, 1], self.qb)
+        p.advance(B, self.traj, self.K, 0, n, self.hb_arg, self.qb_arg)
+        return n
+
+    def _run(self, X0):
+        p, B, nb = self.plan, self.B, self.nb
+        nbt = ctypes.c_longlong(B * nb)
+        # background term
+        if self.prec:
+            _lib.call("vd_diag_axpy", self.vd_dtype, nbt, ctypes.c_longlong(nb), _p(self.Q), _p(X0),
+                      _p(self.Xb), _p(self.X), _stream())
+            self._copy(X0, self.gb)
+        else:
+            _lib.call("vd_axpby", self.vd_dtype, nbt, 1.0, _p(X0), 0.0, _p(self.X), _stream())
+            _lib.call("vd_axpby", self.vd_dtype, nbt, 1.0, _p(self.Xb), 1.0, _p(self.X), _stream())
+            _lib.call("vd_diag_axpy", self.vd_dtype, nbt, ctypes.c_longlong(nb), _p(self.Qinv2), _p(X0),
+                      None, _p(self.gb), _stream())
+        for b in range(B):
+            _lib.call("vd_dot_f64", self.vd_dtype, ctypes.c_longlong(nb), _p(X0[b]), _p(self.gb[b]),
+                      _p(self.dot_scratch[b]), _stream())
+        # forward sweep
+        self._copy(self.h_init, self.h)
+        obs = self.obs
+        for i in range(self.nint):
+            c = self.cps[i]
+            if c in obs.step_range:
+                obs.apply_misfit(c, self.h)
+            if c % self.nstep_check == 0:
+                self.basis.project(c // self.nstep_check, self.X, out=self.F)
+            self._copy(self.h, self.snap[i])
+            self._copy(self.h, self.tv[0, 0])
+            p.init_state(self.tv[0, 0], self.hb, self.tv[0, 1], self.qb)
+            n = self.cps[i + 1] - c
+            p.advance(B, self.traj, self.K, 0, n, self.hb_arg, self.qb_arg)
+            p.finalize(B, self.tv[n * self.S, 0], self.hb, self.h, forcing=self.F, coef=self._coef(n))
+        if self.nstep in obs.step_range:
+            obs.apply_misfit(self.nstep, self.h)
+        obs.sumsq_per_window(self.J, 0.5 / self.sigma_R ** 2)
+        for b in range(B):   # J[b] += Jb[b]/2, Jb[b] = dot_scratch[b, 0]
+            _lib.call("vd_axpby", _lib.VD_F64, ctypes.c_longlong(1), 0.5, _p(self.dot_scratch[b]), 1.0,
+                      _p(self.J[b:b + 1]), _stream())
+        # reverse sweep
+        self._fill0(self.adh)
+        self._fill0(self.adF)
+        self._fill0(self.adX)
+        if self.nstep in obs.step_range:
+            obs.apply_adjoint(self.nstep, self.adh)
+        for i in reversed(range(self.nint)):
+            c = self.cps[i]
+            n = self._interval_forward(i)
+            # adF += coef*adh; adh <- adjoint at the end of the model call
+            _lib.call("vd_qg1l_finalize_adj", p._h, B, _p(self.adh), _p(self.adF), float(self._coef(n)),
+                      _p(self.adh), _stream())
+            self._fill0(self.adq)
+            p.advance_adj(B, self.traj, self.K, 0, n, self.adh, self.adq)
+            p.init_state_adj(B, self.tv[0, 0], self.adq, self.adh)
+            if c % self.nstep_check == 0:
+                self.basis.project_T(c // self.nstep_check, self.adF, self.adX)
+                self._fill0(self.adF)
+            if c in obs.step_range:
+                obs.apply_adjoint(c, self.adh)
+        if self.prec:
+            _lib.call("vd_diag_axpy", self.vd_dtype, nbt, ctypes.c_longlong(nb), _p(self.Q), _p(self.adX),
+                      _p(self.gb), _p(self.grad), _stream())
+        else:
+            self._copy(self.gb, self.grad)
+            _lib.call("vd_axpby", self.vd_dtype, nbt, 1.0, _p(self.adX), 1.0, _p(self.grad), _stream())
+
+    def cost_and_grad(self, X0):
+        """Returns (J [B] float64, grad [B, nbasis]) as device tensors (views of
+        internal buffers, overwritten by the next call)."""
+        if X0.dim() == 1:
+            X0 = X0.unsqueeze(0)
+        if X0.shape != (self.B, self.nb) or X0.dtype != self.plan.dtype:
+            raise ValueError(f"control must be [{self.B}, {self.nb}] of the plan dtype")
+        X0 = X0.contiguous()
+        if self.graph is not None:
+            self._copy(X0, self.X0_static)
+            self.graph.replay()
+        else:
+            self._run(X0)
+        return self.J, self.grad
+
+    def capture(self):
+        """Capture one whole evaluation into a CUDA graph."""
+        self.X0_static = torch.zeros(self.B, self.nb, dtype=self.plan.dtype, device=self.plan.device)
+        self._run(self.X0_static)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                self._run(self.X0_static)
         torch.cuda.current_stream().wait_stream(s)
         torch.cuda.synchronize()
         self.graph = g
