@@ -183,11 +183,17 @@ vd_status vd_qg1l_init_state_adj(const vd_qg1l_plan* plan, int batch,
 vd_status vd_qg1l_finalize(const vd_qg1l_plan* plan, int batch, const void* h,
                            const void* hb, const void* forcing, double coef,
                            void* h_out, void* stream);
-/* Adjoint of vd_qg1l_finalize: adforcing += coef*adh_out (if adforcing !=
- * NULL; mod.py:1058-1068) and adh = adh_out with the walls and land set to
- * 0. adh may alias adh_out. */
-vd_status vd_qg1l_finalize_adj(const vd_qg1l_plan* plan, int batch, const void* adh_out,
-                               void* adforcing, double coef, void* adh, void* stream);
+/* vd_qg1l_finalize with one forcing coefficient per window: coef is a
+ * DEVICE array of `batch` doubles (n*dt/86400 of each window's model call,
+ * mod.py:911-913; 0 for a window that does not end a call here). */
+vd_status vd_qg1l_force(const vd_qg1l_plan* plan, int batch, const void* h,
+                        const void* hb, const void* forcing, const double* coef,
+                        void* h_out, void* stream);
+/* Adjoint of vd_qg1l_force: adforcing[b] += coef[b]*adh_out[b]
+ * (mod.py:1058-1068) and adh = adh_out with the walls and land set to 0.
+ * adh may alias adh_out. */
+vd_status vd_qg1l_force_adj(const vd_qg1l_plan* plan, int batch, const void* adh_out,
+                            void* adforcing, const double* coef, void* adh, void* stream);
 
 /* Along-track observation operator (Obsop_interp_l3_jax, mapping/src/obsop.py
  * 375-678). H is stored per observation as up to 4 (grid index, weight) pairs

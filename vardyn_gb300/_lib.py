@@ -91,7 +91,8 @@ SIGNATURES = {
     "vd_qg1l_advance_adj": (I, [P, I, P, I, I, I, P, P, P, SZ, P]),
     "vd_qg1l_init_state_adj": (I, [P, I, P, P, P, P]),
     "vd_qg1l_finalize": (I, [P, I, P, P, P, D, P, P]),
-    "vd_qg1l_finalize_adj": (I, [P, I, P, P, D, P, P]),
+    "vd_qg1l_force": (I, [P, I, P, P, P, P, P, P]),
+    "vd_qg1l_force_adj": (I, [P, I, P, P, P, P, P]),
     "vd_obs_misfit": (I, [I, I, P, LL, P, P, P, P, P, P, P]),
     "vd_obs_adjoint": (I, [I, I, P, LL, P, P, P, P, P, P, P, P]),
     "vd_sumsq_f64": (I, [I, I, P, P, P, P]),

@@ -24,9 +24,10 @@ int init_state_impl(const vd_qg1l_plan*, int, int, const T*, const T*, T*, T*, c
 template <typename T>
 int init_state_adj_impl(const vd_qg1l_plan*, int, const T*, const T*, T*, cudaStream_t);
 template <typename T>
-int finalize_impl(const vd_qg1l_plan*, int, const T*, const T*, const T*, double, int, T*, cudaStream_t);
+int finalize_impl(const vd_qg1l_plan*, int, const T*, const T*, const T*, double, const double*, int, T*,
+                  cudaStream_t);
 template <typename T>
-int finalize_adj_impl(const vd_qg1l_plan*, int, const T*, T*, double, T*, cudaStream_t);
+int finalize_adj_impl(const vd_qg1l_plan*, int, const T*, T*, const double*, T*, cudaStream_t);
 template <typename T>
 int copy_impl(const vd_qg1l_plan*, int, const T*, T*, int, cudaStream_t);
 template <typename T>
@@ -282,7 +283,7 @@ static int pv2h_t(const vd_qg1l_plan* p, int B, const T* q, const T* hb, const T
     a.out = h; a.add = hb; a.add_batches = hb ? B : 0; a.epi = EPI_H;
     int rc = helmholtz_solve<T>(p, B, a, spec, st);
     if (rc) return rc;
-    return finalize_impl<T>(p, B, h, hb, nullptr, 0.0, 0, h, st);
+    return finalize_impl<T>(p, B, h, hb, nullptr, 0.0, nullptr, 0, h, st);
 }
 
 extern "C" vd_status vd_qg1l_pv2h(const vd_qg1l_plan* p, int B, const void* q, const void* hb, const void* qb,
@@ -311,7 +312,7 @@ static int step_t(const vd_qg1l_plan* p, int B, const T* h0, const T* hb, int ns
         if ((rc = init_state_impl<T>(p, B, B, h, hb, q, qb, st))) return rc;
         if ((rc = advance_impl<T>(p, B, traj, nstep, 0, nstep, hb, qb, ws, st))) return rc;
         const T* hN = traj + (long long)nstep * p->nstage * 2 * fb;
-        return finalize_impl<T>(p, B, hN, hb, nullptr, 0.0, 1, hout, st);
+        return finalize_impl<T>(p, B, hN, hb, nullptr, 0.0, nullptr, 1, hout, st);
     }
     T* h = (T*)ws.take(fb * sizeof(T));
     T* q = (T*)ws.take(fb * sizeof(T));
@@ -319,7 +320,7 @@ static int step_t(const vd_qg1l_plan* p, int B, const T* h0, const T* hb, int ns
     VD_CUDA_TRY(cudaMemcpyAsync(h, h0, fb * sizeof(T), cudaMemcpyDeviceToDevice, st));
     if ((rc = init_state_impl<T>(p, B, B, h, hb, q, qb, st))) return rc;
     if ((rc = forward_nostore<T>(p, B, h, q, nstep, hb, qb, ws, st, false))) return rc;
-    return finalize_impl<T>(p, B, h, hb, nullptr, 0.0, 1, hout, st);
+    return finalize_impl<T>(p, B, h, hb, nullptr, 0.0, nullptr, 1, hout, st);
 }
 
 extern "C" vd_status vd_qg1l_step(const vd_qg1l_plan* p, int B, const void* h0, const void* hb, int nstep,
@@ -349,7 +350,7 @@ static int step_tgl_t(const vd_qg1l_plan* p, int B, const T* dh0, const T* h0, c
     int rc;
     if ((rc = init_state_impl<T>(p, 2 * B, B, h, hb, q, qb, st))) return rc;
     if ((rc = forward_nostore<T>(p, 2 * B, h, q, nstep, hb, qb, ws, st, true))) return rc;
-    return finalize_impl<T>(p, B, h + fb, nullptr, nullptr, 0.0, 2, dhout, st);
+    return finalize_impl<T>(p, B, h + fb, nullptr, nullptr, 0.0, nullptr, 2, dhout, st);
 }
 
 extern "C" vd_status vd_qg1l_step_tgl(const vd_qg1l_plan* p, int B, const void* dh0, const void* h0,
@@ -463,19 +464,30 @@ extern "C" vd_status vd_qg1l_finalize(const vd_qg1l_plan* p, int B, const void* 
     if (!p || B <= 0 || !h || !h_out) return VD_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     return p->d.dtype == VD_F32
-               ? finalize_impl<float>(p, B, (const float*)h, (const float*)hb, (const float*)forcing, coef, 1,
-                                      (float*)h_out, st)
-               : finalize_impl<double>(p, B, (const double*)h, (const double*)hb, (const double*)forcing, coef, 1,
-                                       (double*)h_out, st);
+               ? finalize_impl<float>(p, B, (const float*)h, (const float*)hb, (const float*)forcing, coef, nullptr,
+                                      1, (float*)h_out, st)
+               : finalize_impl<double>(p, B, (const double*)h, (const double*)hb, (const double*)forcing, coef,
+                                       nullptr, 1, (double*)h_out, st);
 }
 
-extern "C" vd_status vd_qg1l_finalize_adj(const vd_qg1l_plan* p, int B, const void* adh_out, void* adforcing,
-                                          double coef, void* adh, void* stream)
+extern "C" vd_status vd_qg1l_force(const vd_qg1l_plan* p, int B, const void* h, const void* hb, const void* forcing,
+                                   const double* coef, void* h_out, void* stream)
 {
-    if (!p || B <= 0 || !adh_out || !adh) return VD_ERR_ARG;
+    if (!p || B <= 0 || !h || !h_out || !forcing || !coef) return VD_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    return p->d.dtype == VD_F32
+               ? finalize_impl<float>(p, B, (const float*)h, (const float*)hb, (const float*)forcing, 0.0, coef, 1,
+                                      (float*)h_out, st)
+               : finalize_impl<double>(p, B, (const double*)h, (const double*)hb, (const double*)forcing, 0.0, coef,
+                                       1, (double*)h_out, st);
+}
+
+extern "C" vd_status vd_qg1l_force_adj(const vd_qg1l_plan* p, int B, const void* adh_out, void* adforcing,
+                                       const double* coef, void* adh, void* stream)
+{
+    if (!p || B <= 0 || !adh_out || !adh || !adforcing || !coef) return VD_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     return p->d.dtype == VD_F32
                ? finalize_adj_impl<float>(p, B, (const float*)adh_out, (float*)adforcing, coef, (float*)adh, st)
-               : finalize_adj_impl<double>(p, B, (const double*)adh_out, (double*)adforcing, coef, (double*)adh,
-                                           st);
+               : finalize_adj_impl<double>(p, B, (const double*)adh_out, (double*)adforcing, coef, (double*)adh, st);
 }

@@ -23,7 +23,8 @@ static __device__ __align__(256) unsigned char g_pv2h_scratch[VD_NOALLOC_SCRATCH
 
 namespace vd {
 template <typename T>
-int finalize_impl(const vd_qg1l_plan*, int, const T*, const T*, const T*, double, int, T*, cudaStream_t);
+int finalize_impl(const vd_qg1l_plan*, int, const T*, const T*, const T*, double, const double*, int, T*,
+                  cudaStream_t);
 }
 
 namespace {
@@ -59,7 +60,7 @@ int pv2h_noalloc_t(const vd_qg1l_plan* p, int B, const T* q, const T* hb, const 
     a.out = h; a.add = hb; a.add_batches = hb ? B : 0; a.epi = vd::EPI_H;
     int rc = vd::helmholtz_solve<T>(p, B, a, spec, st);
     if (rc) return rc;
-    return vd::finalize_impl<T>(p, B, h, hb, nullptr, 0.0, 0, h, st);
+    return vd::finalize_impl<T>(p, B, h, hb, nullptr, 0.0, nullptr, 0, h, st);
 }
 
 }  // namespace

@@ -401,7 +401,8 @@ __global__ void k_fill(long long n, T v, T* __restrict__ x)
 // out = (land ? {h, NaN, 0}[land_mode] : (wall ? (hb or 0) : h)) + coef*forcing
 template <typename T>
 __global__ void k_finalize(QGGeom G, int nf, const T* __restrict__ h, const T* __restrict__ hb,
-                           const T* __restrict__ forcing, T coef, int land_mode, T* __restrict__ out)
+                           const T* __restrict__ forcing, T coef, const double* __restrict__ coefv,
+                           int land_mode, T* __restrict__ out)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -416,16 +417,16 @@ __global__ void k_finalize(QGGeom G, int nf, const T* __restrict__ h, const T* _
         v = h[o];
     if (G.mask[(long long)j * G.nx + i] == 0 && land_mode != 0)
         v = land_mode == 1 ? T(NAN) : T(0);
-    if (forcing) v += coef * forcing[o];
+    if (forcing) v += (coefv ? T(coefv[f]) : coef) * forcing[o];
     out[o] = v;
 }
 
-// Adjoint of k_finalize: the forcing adjoint takes coef * adh_out everywhere
-// (mod.py:1058-1068); the state adjoint is adh_out except on the walls (set
-// to hb) and on land (set to a constant), where it is 0.
+// Adjoint of k_finalize: the forcing adjoint takes coef[f] * adh_out
+// everywhere (mod.py:1058-1068); the state adjoint is adh_out except on the
+// walls (set to hb) and on land (set to a constant), where it is 0.
 template <typename T>
-__global__ void k_finalize_adj(QGGeom G, int nf, const T* __restrict__ adout, T* __restrict__ adforcing, T coef,
-                               T* __restrict__ adh)
+__global__ void k_finalize_adj(QGGeom G, int nf, const T* __restrict__ adout, T* __restrict__ adforcing,
+                               const double* __restrict__ coefv, T* __restrict__ adh)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -433,7 +434,7 @@ __global__ void k_finalize_adj(QGGeom G, int nf, const T* __restrict__ adout, T*
     if (i >= G.nx || j >= G.ny || f >= nf) return;
     const long long o = f * G.fs + (long long)j * G.nx + i;
     const T a = adout[o];
-    if (adforcing) adforcing[o] += coef * a;
+    if (adforcing) adforcing[o] += T(coefv[f]) * a;
     const bool wall = (i == 0 || j == 0 || i == G.nx - 1 || j == G.ny - 1);
     adh[o] = (wall || G.mask[(long long)j * G.nx + i] == 0) ? T(0) : a;
 }
@@ -687,18 +688,18 @@ int init_state_adj_impl(const vd_qg1l_plan* p, int nf, const T* h, const T* adq,
 
 template <typename T>
 int finalize_impl(const vd_qg1l_plan* p, int nf, const T* h, const T* hb, const T* forcing, double coef,
-                  int land_mode, T* out, cudaStream_t st)
+                  const double* coefv, int land_mode, T* out, cudaStream_t st)
 {
-    k_finalize<T><<<pgrid(p, nf), kBlock, 0, st>>>(p->geom, nf, h, hb, forcing, (T)coef, land_mode, out);
+    k_finalize<T><<<pgrid(p, nf), kBlock, 0, st>>>(p->geom, nf, h, hb, forcing, (T)coef, coefv, land_mode, out);
     VD_LAUNCH_CHECK();
     return VD_OK;
 }
 
 template <typename T>
-int finalize_adj_impl(const vd_qg1l_plan* p, int nf, const T* adout, T* adforcing, double coef, T* adh,
+int finalize_adj_impl(const vd_qg1l_plan* p, int nf, const T* adout, T* adforcing, const double* coefv, T* adh,
                       cudaStream_t st)
 {
-    k_finalize_adj<T><<<pgrid(p, nf), kBlock, 0, st>>>(p->geom, nf, adout, adforcing, (T)coef, adh);
+    k_finalize_adj<T><<<pgrid(p, nf), kBlock, 0, st>>>(p->geom, nf, adout, adforcing, coefv, adh);
     VD_LAUNCH_CHECK();
     return VD_OK;
 }
@@ -746,9 +747,10 @@ int rhs_impl(const vd_qg1l_plan* p, int nf, const T* u, const T* v, const T* q, 
     template int init_state_impl<T>(const vd_qg1l_plan*, int, int, const T*, const T*, T*, T*,            \
                                     cudaStream_t);                                                        \
     template int init_state_adj_impl<T>(const vd_qg1l_plan*, int, const T*, const T*, T*, cudaStream_t);  \
-    template int finalize_impl<T>(const vd_qg1l_plan*, int, const T*, const T*, const T*, double, int,    \
-                                  T*, cudaStream_t);                                                      \
-    template int finalize_adj_impl<T>(const vd_qg1l_plan*, int, const T*, T*, double, T*, cudaStream_t);  \
+    template int finalize_impl<T>(const vd_qg1l_plan*, int, const T*, const T*, const T*, double,         \
+                                  const double*, int, T*, cudaStream_t);                                  \
+    template int finalize_adj_impl<T>(const vd_qg1l_plan*, int, const T*, T*, const double*, T*,          \
+                                      cudaStream_t);                                                      \
     template int copy_impl<T>(const vd_qg1l_plan*, int, const T*, T*, int, cudaStream_t);                 \
     template int zero_impl<T>(long long, T*, cudaStream_t);                                               \
     template int h2uv_impl<T>(const vd_qg1l_plan*, int, const T*, T*, T*, cudaStream_t);                  \

@@ -267,6 +267,12 @@ class QGBasis4DVar:
       prec=False  X = X0 + Xb,   Jb = X0.X0/Q^2,  G = adX + X0/Q^2
     J = (Jo + Jb)/2 with Jo = sum misfit^2/sigma_R^2.
 
+    Batched windows keep their own checkpoint lists (their own observation
+    steps); the batch advances between the boundaries of the union of the
+    lists, with a per-window forcing coefficient table (0 where a window does
+    not end a model call), so that each window reproduces its single-window
+    evaluation.
+
     Storage: the SSH at every interval start ([ninterval, B, ny, nx]) and the
     stage trajectory of one interval (recomputed per interval in reverse).
     """
@@ -301,8 +307,30 @@ class QGBasis4DVar:
         xb = np.zeros(self.nb) if Xb is None else np.asarray(Xb, dtype=np.float64)
         self.Xb = torch.as_tensor(np.tile(xb, (B, 1)), device=dev).to(dt)
         self.obs_steps = sorted(int(s) for s in obs.steps if 0 <= s <= self.nstep)
-        self.cps = checkpoints(self.nstep, self.nstep_check, [s for s in self.obs_steps if 0 < s < self.nstep])
+        # Every window calls the model between its own checkpoints (its own
+        # observation steps and the regular ones); the batch runs from one
+        # boundary of the union of those lists to the next. A window ends a
+        # model call only at its own checkpoints: there its SSH takes the
+        # forcing n*dt/86400*F of that call; elsewhere its coefficient is 0 and
+        # it continues integrating (PV re-derivation from SSH is exact there).
+        self.win_cps = []
+        for b in range(B):
+            st = obs.obs_step[obs.obs_window == b]
+            self.win_cps.append(checkpoints(self.nstep, self.nstep_check,
+                                            [int(s) for s in np.unique(st) if 0 < s < self.nstep]))
+        self.cps = sorted(set().union(*[set(c) for c in self.win_cps]))
         self.nint = len(self.cps) - 1
+        coef = np.zeros((self.nint, B))
+        for b, wc in enumerate(self.win_cps):
+            wset = set(wc)
+            last = 0
+            for i in range(self.nint):
+                end = self.cps[i + 1]
+                if end in wset:
+                    coef[i, b] = (end - last) * plan.dt / SECONDS_PER_DAY
+                    last = end
+        self.coef_host = coef
+        self.coef = torch.as_tensor(coef, dtype=torch.float64, device=dev).contiguous()
         K = max(self.cps[i + 1] - self.cps[i] for i in range(self.nint))
         self.K = K
         self.traj = plan.new_traj(B, K)
@@ -331,9 +359,6 @@ class QGBasis4DVar:
 
     def _copy(self, src, dst):
         _lib.call("vd_copy", self.vd_dtype, ctypes.c_longlong(src.numel()), _p(src), _p(dst), _stream())
-
-    def _coef(self, n):
-        return n * self.plan.dt / SECONDS_PER_DAY
 
     def _interval_forward(self, i):
         """Recompute the stage trajectory of interval i from its start SSH."""
@@ -374,7 +399,8 @@ class QGBasis4DVar:
             p.init_state(self.tv[0, 0], self.hb, self.tv[0, 1], self.qb)
             n = self.cps[i + 1] - c
             p.advance(B, self.traj, self.K, 0, n, self.hb_arg, self.qb_arg)
-            p.finalize(B, self.tv[n * self.S, 0], self.hb, self.h, forcing=self.F, coef=self._coef(n))
+            _lib.call("vd_qg1l_force", p._h, B, _p(self.tv[n * self.S, 0]), _p(self.hb), _p(self.F),
+                      _p(self.coef[i]), _p(self.h), _stream())
         if self.nstep in obs.step_range:
             obs.apply_misfit(self.nstep, self.h)
         obs.sumsq_per_window(self.J, 0.5 / self.sigma_R ** 2)
@@ -390,8 +416,8 @@ class QGBasis4DVar:
         for i in reversed(range(self.nint)):
             c = self.cps[i]
             n = self._interval_forward(i)
-            # adF += coef*adh; adh <- adjoint at the end of the model call
-            _lib.call("vd_qg1l_finalize_adj", p._h, B, _p(self.adh), _p(self.adF), float(self._coef(n)),
+            # adF += coef*adh; adh <- adjoint at the end of the interval
+            _lib.call("vd_qg1l_force_adj", p._h, B, _p(self.adh), _p(self.adF), _p(self.coef[i]),
                       _p(self.adh), _stream())
             self._fill0(self.adq)
             p.advance_adj(B, self.traj, self.K, 0, n, self.adh, self.adq)
