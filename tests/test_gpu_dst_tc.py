@@ -50,7 +50,8 @@ def oracle_rows(field, ny, nx):
     return np.concatenate([y[..., 0::2], y[..., 1::2]], axis=-1)
 
 
-@pytest.mark.parametrize("ny,nx,B", [(64, 64, 1), (40, 66, 3), (130, 200, 2), (512, 512, 2), (300, 777, 1)])
+@pytest.mark.parametrize("ny,nx,B", [(64, 64, 1), (40, 66, 3), (130, 200, 2), (512, 512, 2), (300, 777, 1),
+                                     (1024, 1024, 1)])
 def test_tc_forward_pass_matches_oracle(ny, nx, B):
     rng = np.random.default_rng(ny + nx)
     f = rng.standard_normal((B, ny, nx)).astype(np.float32)
@@ -67,7 +68,7 @@ def test_tc_forward_pass_matches_oracle(ny, nx, B):
     assert err < 4e-6
 
 
-@pytest.mark.parametrize("ny,nx,B", [(64, 64, 1), (130, 200, 2), (512, 512, 4), (300, 777, 1)])
+@pytest.mark.parametrize("ny,nx,B", [(64, 64, 1), (130, 200, 2), (512, 512, 4), (300, 777, 1), (1024, 1024, 1)])
 def test_tc_solve_matches_fma_and_oracle(ny, nx, B):
     from oracle.qg1l import QgmOracle
     rng = np.random.default_rng(3 * ny + nx)
@@ -115,10 +116,15 @@ def test_tc_adjoint_epilogue_and_step():
     assert np.linalg.norm(adj_tc - adj_f) / np.linalg.norm(adj_f) < 2e-5
 
 
-@pytest.mark.parametrize("ny,nx,dtype,tol", [(40, 66, torch.float64, 1e-12), (514, 512, torch.float32, 2e-6),
-                                            (130, 201, torch.float32, 2e-6)])
-def test_tridiagonal_y_solve_matches_banded_solver(ny, nx, dtype, tol):
-    """vd_qg1l_tridiag_y against scipy's banded solver on the same systems."""
+@pytest.mark.parametrize("ny,nx,dtype,tol,B", [(40, 66, torch.float64, 1e-12, 2), (514, 512, torch.float32, 2e-6, 2),
+                                              (130, 201, torch.float32, 2e-6, 2),
+                                              (1024, 1024, torch.float32, 2e-6, 1),
+                                              (1024, 1024, torch.float32, 2e-6, 2),
+                                              (300, 500, torch.float64, 1e-12, 1),
+                                              (1500, 260, torch.float32, 2e-6, 1)])
+def test_tridiagonal_y_solve_matches_banded_solver(ny, nx, dtype, tol, B):
+    """vd_qg1l_tridiag_y against scipy's banded solver on the same systems
+    (column groups of 8, 16 and 32 per CTA, pieces of 32 and 64 rows)."""
     import scipy.linalg
     from vardyn_gb300 import _lib
     from vardyn_gb300.qg1l import QG1LPlan
@@ -128,7 +134,6 @@ def test_tridiagonal_y_solve_matches_banded_solver(ny, nx, dtype, tol):
     ne = n - n // 2
     lds = ((n + 3) // 4) * 4
     rng = np.random.default_rng(ny)
-    B = 2
     F = rng.standard_normal((B, my, lds))
     spec = torch.as_tensor(F, dtype=dtype, device="cuda").contiguous()
     st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)

@@ -229,22 +229,40 @@ dst_gemm_kernel(GemmGeom g, const T* __restrict__ W1, const T* __restrict__ W2,
 // piece-end values (at most 32 steps), and each warp adds carry * partial
 // product to its rows. |alpha| < 1 (diagonal dominance), so the products
 // only shrink.
-template <typename T, int CH>
+// CW spectral columns per CTA; the warp's lanes are CW columns x (32/CW)
+// row pieces, so a CTA holds nw*(32/CW) pieces of CH rows per column. Each
+// piece runs both Thomas sweeps locally (the recurrences are affine, so a
+// piece is summarised by its end value and the product of its multipliers);
+// CW threads then chain the pieces of their column and every piece applies
+// the carry it receives. Narrow CTAs (CW = 8) give enough CTAs to fill the
+// GPU when there are few columns (one 1024^2 field: 128 CTAs).
+template <typename T, int CW, int CH>
 __global__ void __launch_bounds__(512)
 tridiag_chunked_kernel(T* __restrict__ spec, const T* __restrict__ trim, int my, int n, int lds, T a)
 {
+    constexpr int SUB = 32 / CW;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* F = reinterpret_cast<T*>(smem_raw);          // [my][32]
-    T* cD = F + (size_t)my * 32;                    // [nw][32] piece-end values / carries
-    T* cP = cD + 16 * 32;                           // [nw][32] piece products
+    const int nw = blockDim.y;
+    const int NP = nw * SUB;
+    T* F = reinterpret_cast<T*>(smem_raw);          // [my][CW]
+    T* cD = F + (size_t)my * CW;                    // [NP][CW] piece-end values / carries
+    T* cP = cD + (size_t)NP * CW;                   // [NP][CW] piece products
     const int f = blockIdx.y;
-    const int lane = threadIdx.x, w = threadIdx.y, nw = blockDim.y;
-    const int t = blockIdx.x * 32 + lane;
+    const int lane = threadIdx.x, w = threadIdx.y;
+    const int tid = w * 32 + lane;
+    const int nthr = nw * 32;
+    const int c = lane % CW;
+    const int pc = w * SUB + lane / CW;
+    const int tbase = blockIdx.x * CW;
+    const int t = tbase + c;
     const bool col_ok = t < n;
     T* S = spec + (long long)f * my * lds;
-    for (int j = w; j < my; j += nw) F[j * 32 + lane] = col_ok ? S[(long long)j * lds + t] : T(0);
+    for (int e = tid; e < my * CW; e += nthr) {
+        const int j = e / CW, cc = e - j * CW;
+        F[e] = (tbase + cc < n) ? S[(long long)j * lds + tbase + cc] : T(0);
+    }
 
-    const int j0 = w * CH;
+    const int j0 = pc * CH;
     const int cnt = max(0, min(CH, my - j0));
     T mm[CH];
 #pragma unroll
@@ -258,30 +276,30 @@ tridiag_chunked_kernel(T* __restrict__ spec, const T* __restrict__ trim, int my,
     for (int i = 0; i < CH; ++i) {
         if (i < cnt) {
             const T al = -a * mm[i];
-            d = mm[i] * F[(j0 + i) * 32 + lane] + al * d;
-            F[(j0 + i) * 32 + lane] = d;
+            d = mm[i] * F[(j0 + i) * CW + c] + al * d;
+            F[(j0 + i) * CW + c] = d;
             P *= al;
         }
     }
-    cD[w * 32 + lane] = d;
-    cP[w * 32 + lane] = P;
+    cD[pc * CW + c] = d;
+    cP[pc * CW + c] = P;
     __syncthreads();
-    if (w == 0) {
-        T c = T(0);
-        for (int q = 0; q < nw; ++q) {
-            c = cD[q * 32 + lane] + cP[q * 32 + lane] * c;
-            cD[q * 32 + lane] = c;
+    if (tid < CW) {
+        T cr = T(0);
+        for (int q = 0; q < NP; ++q) {
+            cr = cD[q * CW + tid] + cP[q * CW + tid] * cr;
+            cD[q * CW + tid] = cr;
         }
     }
     __syncthreads();
-    if (w > 0) {
-        const T cin = cD[(w - 1) * 32 + lane];
-        T p = T(1);
+    if (pc > 0) {
+        const T cin = cD[(pc - 1) * CW + c];
+        T pr = T(1);
 #pragma unroll
         for (int i = 0; i < CH; ++i) {
             if (i < cnt) {
-                p *= -a * mm[i];
-                F[(j0 + i) * 32 + lane] += p * cin;
+                pr *= -a * mm[i];
+                F[(j0 + i) * CW + c] += pr * cin;
             }
         }
     }
@@ -294,36 +312,38 @@ tridiag_chunked_kernel(T* __restrict__ spec, const T* __restrict__ trim, int my,
     for (int i = CH - 1; i >= 0; --i) {
         if (i < cnt) {
             const T al = -a * mm[i];
-            x = F[(j0 + i) * 32 + lane] + al * x;
-            F[(j0 + i) * 32 + lane] = x;
+            x = F[(j0 + i) * CW + c] + al * x;
+            F[(j0 + i) * CW + c] = x;
             P *= al;
         }
     }
-    cD[w * 32 + lane] = x;
-    cP[w * 32 + lane] = P;
+    cD[pc * CW + c] = x;
+    cP[pc * CW + c] = P;
     __syncthreads();
-    if (w == 0) {
-        T c = T(0);
-        for (int q = nw - 1; q >= 0; --q) {
-            c = cD[q * 32 + lane] + cP[q * 32 + lane] * c;
-            cD[q * 32 + lane] = c;
+    if (tid < CW) {
+        T cr = T(0);
+        for (int q = NP - 1; q >= 0; --q) {
+            cr = cD[q * CW + tid] + cP[q * CW + tid] * cr;
+            cD[q * CW + tid] = cr;
         }
     }
     __syncthreads();
-    if (w < nw - 1) {
-        const T cin = cD[(w + 1) * 32 + lane];
-        T p = T(1);
+    if (pc < NP - 1) {
+        const T cin = cD[(pc + 1) * CW + c];
+        T pr = T(1);
 #pragma unroll
         for (int i = CH - 1; i >= 0; --i) {
             if (i < cnt) {
-                p *= -a * mm[i];
-                F[(j0 + i) * 32 + lane] += p * cin;
+                pr *= -a * mm[i];
+                F[(j0 + i) * CW + c] += pr * cin;
             }
         }
     }
     __syncthreads();
-    if (col_ok)
-        for (int j = w; j < my; j += nw) S[(long long)j * lds + t] = F[j * 32 + lane];
+    for (int e = tid; e < my * CW; e += nthr) {
+        const int j = e / CW, cc = e - j * CW;
+        if (tbase + cc < n) S[(long long)j * lds + tbase + cc] = F[e];
+    }
 }
 
 // Same recurrences directly on the spectral buffer, for column blocks too tall
@@ -453,6 +473,66 @@ static cudaError_t set_smem_attrs()
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, maxb);
 }
 
+template <typename T>
+static cudaError_t set_tridiag_attrs()
+{
+    const int maxb = 227 * 1024;
+    cudaError_t e;
+    if ((e = cudaFuncSetAttribute(tridiag_chunked_kernel<T, 32, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  maxb))) return e;
+    if ((e = cudaFuncSetAttribute(tridiag_chunked_kernel<T, 16, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  maxb))) return e;
+    if ((e = cudaFuncSetAttribute(tridiag_chunked_kernel<T, 8, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  maxb))) return e;
+    if constexpr (sizeof(T) == 4) {
+        if ((e = cudaFuncSetAttribute(tridiag_chunked_kernel<T, 32, 64>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, maxb))) return e;
+        if ((e = cudaFuncSetAttribute(tridiag_chunked_kernel<T, 16, 64>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, maxb))) return e;
+    }
+    return cudaSuccess;
+}
+
+// The y-direction tridiagonal solves of nf fields: the widest column group
+// (32, 16 or 8 columns per CTA) that still gives ~120 CTAs, pieces of 32
+// rows (64 for tall float32 fields with wide groups) in at most 16 warps;
+// very tall fields fall back to one sequential thread per column.
+template <typename T>
+static int launch_tridiag(const vd_qg1l_plan* p, int nf, T* spec, cudaStream_t st)
+{
+    const DSTTables& t = p->dst;
+    const T a = (T)t.tri_a;
+    for (int cw : {32, 16, 8}) {
+        const long long ctas = (long long)((t.n + cw - 1) / cw) * nf;
+        if (cw != 8 && ctas < 120) continue;
+        const int sub = 32 / cw;
+        for (int ch : {32, 64}) {
+            if (ch == 64 && (sizeof(T) == 8 || cw == 8)) continue;
+            const int np_need = (t.my + ch - 1) / ch;
+            const int nw = (np_need + sub - 1) / sub;
+            if (nw > 16) continue;
+            const size_t smem = (size_t(t.my) * cw + 2 * size_t(nw) * sub * cw) * sizeof(T);
+            if (smem > 200 * 1024) continue;
+            const dim3 grid((t.n + cw - 1) / cw, nf), block(32, nw);
+#define VD_TRI(CW, CH) tridiag_chunked_kernel<T, CW, CH><<<grid, block, smem, st>>>(spec, (const T*)t.trim, t.my, \
+                                                                                   t.n, t.lds, a)
+            if (cw == 32 && ch == 32) VD_TRI(32, 32);
+            else if (cw == 16 && ch == 32) VD_TRI(16, 32);
+            else if (cw == 8) VD_TRI(8, 32);
+            else if constexpr (sizeof(T) == 4) {
+                if (cw == 32) VD_TRI(32, 64);
+                else VD_TRI(16, 64);
+            }
+#undef VD_TRI
+            VD_LAUNCH_CHECK();
+            return VD_OK;
+        }
+    }
+    tridiag_global_kernel<T><<<dim3((t.n + 31) / 32, nf), 32, 0, st>>>(spec, (const T*)t.trim, t.my, t.n, t.lds, a);
+    VD_LAUNCH_CHECK();
+    return VD_OK;
+}
+
 static std::once_flag g_attr_once;
 static cudaError_t g_attr_err = cudaSuccess;
 
@@ -465,12 +545,8 @@ static cudaError_t configure_kernels()
         if (!e) e = set_smem_attrs<float, 64>();
         if (!e) e = set_smem_attrs<double, 16>();
         if (!e) e = set_smem_attrs<double, 32>();
-        if (!e) e = cudaFuncSetAttribute(tridiag_chunked_kernel<float, 32>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        if (!e) e = cudaFuncSetAttribute(tridiag_chunked_kernel<float, 64>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        if (!e) e = cudaFuncSetAttribute(tridiag_chunked_kernel<double, 32>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        if (!e) e = set_tridiag_attrs<float>();
+        if (!e) e = set_tridiag_attrs<double>();
         g_attr_err = e;
     });
     return g_attr_err;
@@ -532,30 +608,14 @@ int helmholtz_solve(const vd_qg1l_plan* p, int nf, const SolveArgs& a, T* spec, 
     int rc;
     auto run = [&](bool fwd) -> int {
         if constexpr (sizeof(T) == 4) {
-            if (p->dst.tc) return dst_pass_tc(p, nf, a, (float*)spec, fwd, st);
+            if (p->dst.tc && tc_fits(p, nf)) return dst_pass_tc(p, nf, a, (float*)spec, fwd, st);
             if (tr == 64) return launch_pair<T, 64>(p, g, a, spec, st, fwd);
         }
         if (tr == 32) return launch_pair<T, 32>(p, g, a, spec, st, fwd);
         return launch_pair<T, 16>(p, g, a, spec, st, fwd);
     };
     if ((rc = run(true))) return rc;
-    dim3 tgrid((t.n + 31) / 32, nf);
-    const size_t csmem = (size_t(t.my) * 32 + 2 * 16 * 32) * sizeof(T);
-    if (t.my <= 512 && csmem <= 200 * 1024) {
-        const int nw = (t.my + 31) / 32;
-        tridiag_chunked_kernel<T, 32><<<tgrid, dim3(32, nw), csmem, st>>>(
-            spec, (const T*)t.trim, t.my, t.n, t.lds, (T)t.tri_a);
-    } else if (sizeof(T) == 4 && t.my <= 1024 && csmem <= 200 * 1024) {
-        if constexpr (sizeof(T) == 4) {
-            const int nw = (t.my + 63) / 64;
-            tridiag_chunked_kernel<T, 64><<<tgrid, dim3(32, nw), csmem, st>>>(
-                spec, (const T*)t.trim, t.my, t.n, t.lds, (T)t.tri_a);
-        }
-    } else {
-        tridiag_global_kernel<T><<<tgrid, 32, 0, st>>>(
-            spec, (const T*)t.trim, t.my, t.n, t.lds, (T)t.tri_a);
-    }
-    VD_LAUNCH_CHECK();
+    if ((rc = launch_tridiag<T>(p, nf, spec, st))) return rc;
     return run(false);
 }
 
@@ -579,7 +639,7 @@ int dst_x_only(const vd_qg1l_plan* p, int nf, const T* field, T* spec, int inver
     a.out = out; a.add = nullptr; a.add_batches = 0; a.epi = EPI_H;
     const int tr = pick_tr<T>(p, g.R);
     if constexpr (sizeof(T) == 4) {
-        if (p->dst.tc) return dst_pass_tc(p, nf, a, (float*)spec, !inverse, st);
+        if (p->dst.tc && tc_fits(p, nf)) return dst_pass_tc(p, nf, a, (float*)spec, !inverse, st);
         if (tr == 64) return launch_pair<T, 64>(p, g, a, spec, st, !inverse);
     }
     if (tr == 32) return launch_pair<T, 32>(p, g, a, spec, st, !inverse);
@@ -591,24 +651,7 @@ template <typename T>
 int tridiag_only(const vd_qg1l_plan* p, int nf, T* spec, cudaStream_t st)
 {
     if (configure_kernels() != cudaSuccess) return VD_ERR_CUDA;
-    const DSTTables& t = p->dst;
-    dim3 tgrid((t.n + 31) / 32, nf);
-    const size_t csmem = (size_t(t.my) * 32 + 2 * 16 * 32) * sizeof(T);
-    if (t.my <= 512 && csmem <= 200 * 1024) {
-        const int nw = (t.my + 31) / 32;
-        tridiag_chunked_kernel<T, 32><<<tgrid, dim3(32, nw), csmem, st>>>(spec, (const T*)t.trim, t.my, t.n, t.lds,
-                                                                           (T)t.tri_a);
-    } else if (sizeof(T) == 4 && t.my <= 1024 && csmem <= 200 * 1024) {
-        if constexpr (sizeof(T) == 4) {
-            const int nw = (t.my + 63) / 64;
-            tridiag_chunked_kernel<T, 64><<<tgrid, dim3(32, nw), csmem, st>>>(spec, (const T*)t.trim, t.my, t.n,
-                                                                               t.lds, (T)t.tri_a);
-        }
-    } else {
-        tridiag_global_kernel<T><<<tgrid, 32, 0, st>>>(spec, (const T*)t.trim, t.my, t.n, t.lds, (T)t.tri_a);
-    }
-    VD_LAUNCH_CHECK();
-    return VD_OK;
+    return launch_tridiag<T>(p, nf, spec, st);
 }
 
 template int tridiag_only<float>(const vd_qg1l_plan*, int, float*, cudaStream_t);

@@ -2,23 +2,29 @@
 // for float32 plans.
 //
 // The pass is two dense half-size products per row block (even/odd split, see
-// vd_dst.cu). Each CTA owns 128 interior rows (UMMA M = 128) and one output
-// tile of up to 256 columns held in tensor memory (TMEM, fp32 accumulators).
+// vd_dst.cu). Each CTA owns 128 interior rows (UMMA M = 128) and a group of
+// consecutive 32-column output tiles (up to 256 columns forward, 128 per
+// parity inverse) held in tensor memory (TMEM, fp32 accumulators). The group
+// size is chosen per launch so that small batches still fill the GPU: the B
+// operand of a group is the concatenation of its tiles' pre-swizzled images,
+// because a 32-row slab of the 128B-swizzled K-major layout is exactly the
+// next 4 KB of the tile.
 // Float32 accuracy comes from the 3xTF32 split: x = x_hi + x_lo with
 // x_hi = tf32(x), and x.w ~= x_hi.w_hi + x_hi.w_lo + x_lo.w_hi (the dropped
 // x_lo.w_lo term is ~2^-22 relative).
 //
 // Pipeline (per K chunk of 32 = one 128-byte swizzle row of fp32):
-//   warps 0-3  build the A chunk (butterfly or copy of the input rows, hi/lo
+//   warps 0-7  build the A chunk (butterfly or copy of the input rows, hi/lo
 //              split) in the 128B-swizzled K-major layout and arrive on fullA;
 //   thread 0   also issues the bulk copies (cp.async.bulk) of the
 //              pre-swizzled hi/lo chunks of the DST half matrix (fullB);
-//   warp 4     owns the TMEM allocation; its lane 0 issues 3 x 4 MMAs per
+//   warp 8     owns the TMEM allocation; its lane 0 issues 3 x 4 MMAs per
 //              chunk and commits to `empty` to recycle the stage;
-//   warps 0-3  finally read the accumulators (tcgen05.ld) and write rows.
+//   warps 0-7  finally read the accumulators (tcgen05.ld) and write rows.
 // Every mbarrier wait is bounded (2 s of %globaltimer); a timeout sets a bit
 // in a device flag (vd_device_error) and the CTA finishes without hanging.
 #include "vd_internal.cuh"
+#include <algorithm>
 #include <vector>
 #include <cmath>
 #include <cstring>
@@ -34,12 +40,14 @@ constexpr int BM = 128;
 constexpr int KCH = 32;
 constexpr int NPROD = 256;      // producer / epilogue threads (warps 0-7)
 constexpr int NTHREADS = NPROD + 32;   // + warp 8: TMEM owner and MMA issuer
-constexpr int STAGES = 2;
+constexpr int MAX_STAGES = 6;
 constexpr int TMEM_COLS = 256;
+constexpr int TILE = 32;                           // columns of one B image tile
+constexpr uint32_t TILE_BYTES = TILE * 32 * 4;     // 4 KB: 32 rows of the swizzled layout
 constexpr uint32_t A_TILE = BM * KCH * 4;          // 16 KB
-constexpr uint32_t B_TILE_MAX = 256 * KCH * 4;     // 32 KB
-constexpr uint32_t STAGE_BYTES = 2 * A_TILE + 2 * B_TILE_MAX;
-constexpr size_t SMEM_BYTES = STAGES * STAGE_BYTES + 1024;
+constexpr size_t PIPE_BYTES = 200 * 1024;          // pipeline stages fit in this
+constexpr size_t EPI_BYTES = (size_t)BM * 257 * 4; // epilogue staging tile (reuses the stages)
+constexpr size_t SMEM_MAX = PIPE_BYTES + 1024;      // largest dynamic request of any launch
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -183,14 +191,20 @@ __host__ __device__ constexpr uint32_t swz(int r, int k)
 
 }  // namespace tc
 
+constexpr int MAX_TILES = 64;   // ne <= 2048
+
+// Images: per parity (forward) or job (inverse), per K chunk, the hi then the
+// lo part of the whole [Ntot][32] swizzled operand, so that the rows of any
+// run of consecutive 32-row tiles are one contiguous range.
 struct TcTab {
-    int kch;                 // K chunks of 32
-    int nt_t;                // forward output tiles (<= 256 columns each)
-    int Nt[8];
-    long long fwd_off[2][8]; // image offsets (floats): [half][tile]
-    int nt_p;                // inverse output tiles (<= 128 columns each)
-    int Np[16];
-    long long inv_off[2][16];
+    int kch;                         // K chunks of 32
+    int nt;                          // 32-column tiles over the ne output columns
+    int Ntot;                        // operand rows: 32*(nt-1) + last tile (a multiple of 16)
+    long long fwd_base[2];           // forward image offsets (floats) per parity
+    long long inv_base[2];           // inverse image offsets (floats) per job
+    int gf, gi;                      // tiles per CTA of this launch (forward <= 8, inverse <= 4)
+    int nst;                         // pipeline stages of this launch (<= MAX_STAGES)
+    uint32_t b_tile;                 // bytes of one B operand (hi or lo) in a stage
 };
 
 struct TcGeom {
@@ -208,14 +222,17 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
               const float* __restrict__ add, int add_batches, const int8_t* __restrict__ mask)
 {
     extern __shared__ unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t bars[3 * STAGES + 1];
+    __shared__ __align__(8) uint64_t bars[3 * MAX_STAGES + 1];
     __shared__ uint32_t tmem_base_sh;
     unsigned char* sm = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const uint32_t sbase = smem_u32(sm);
-    auto a_hi = [&](int s) { return sbase + s * STAGE_BYTES; };
-    auto a_lo = [&](int s) { return sbase + s * STAGE_BYTES + A_TILE; };
-    auto b_hi = [&](int s) { return sbase + s * STAGE_BYTES + 2 * A_TILE; };
-    auto b_lo = [&](int s) { return sbase + s * STAGE_BYTES + 2 * A_TILE + B_TILE_MAX; };
+    // stage s: A hi | A lo | B hi | B lo (every part 1024-byte aligned)
+    const int STAGES = tab.nst;
+    const uint32_t stage_bytes = 2 * A_TILE + 2 * tab.b_tile;
+    auto a_hi = [&](int s) { return sbase + s * stage_bytes; };
+    auto a_lo = [&](int s) { return sbase + s * stage_bytes + A_TILE; };
+    auto b_hi = [&](int s) { return sbase + s * stage_bytes + 2 * A_TILE; };
+    auto b_lo = [&](int s) { return sbase + s * stage_bytes + 2 * A_TILE + tab.b_tile; };
     const uint32_t bar0 = smem_u32(&bars[0]);
     auto fullA = [&](int s) { return bar0 + 8u * s; };
     auto fullB = [&](int s) { return bar0 + 8u * (STAGES + s); };
@@ -227,22 +244,21 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
     const int lane = tid & 31;
 
     // ---- job layout of this CTA --------------------------------------------
-    int njobs, N, half = 0, tile;
-    const float* jimg[2];
+    // tiles [t_first, t_first + ntl) of one parity (forward) or of both
+    // parities (inverse: job 0 odd, job 1 even rows of the spectrum)
+    int njobs, half = 0, t_first, ntl;
     if (MODE == 0) {
-        half = blockIdx.x / tab.nt_t;
-        tile = blockIdx.x % tab.nt_t;
+        const int G = (tab.nt + tab.gf - 1) / tab.gf;
+        half = blockIdx.x / G;
+        t_first = (blockIdx.x - half * G) * tab.gf;
+        ntl = min(tab.gf, tab.nt - t_first);
         njobs = 1;
-        N = tab.Nt[tile];
-        jimg[0] = img + tab.fwd_off[half][tile];
-        jimg[1] = jimg[0];
     } else {
-        tile = blockIdx.x;
+        t_first = blockIdx.x * tab.gi;
+        ntl = min(tab.gi, tab.nt - t_first);
         njobs = 2;
-        N = tab.Np[tile];
-        jimg[0] = img + tab.inv_off[0][tile];
-        jimg[1] = img + tab.inv_off[1][tile];
     }
+    const int N = min(TILE * ntl, tab.Ntot - TILE * t_first);
     const int nchunks = njobs * tab.kch;
     const uint32_t b_bytes = (uint32_t)N * KCH * 4;
 
@@ -270,16 +286,45 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
         // ------------------------------ producers ------------------------------
         // warp w fills rows [16w, 16w+16) of the A chunk; lane l handles K
         // index k0 + l, so every global load is one coalesced 128-byte row.
-        // Row addresses advance incrementally (next interior row: +nx, and
-        // +2nx more when crossing into the next field).
+        // The element offsets of the warp's 16 rows do not change from chunk
+        // to chunk: they are computed once (32-bit; the host checks that the
+        // arrays are smaller than 2^31 elements). Rows past the end repeat
+        // the last valid row and are zeroed when the chunk is stored.
         const int r0 = warp * 16;
         const int row0 = blockIdx.y * BM + r0;
-        int f0 = 0, j0 = 1;
-        if (MODE == 0 && row0 < g.R) {
-            f0 = row0 / g.my;
-            j0 = row0 - f0 * g.my + 1;
+        int roff[16];
+        uint32_t rvalid = 0;
+        {
+            int f = 0, j = 1;
+            if (MODE == 0) {
+                const int rr = min(row0, g.R - 1);
+                f = rr / g.my;
+                j = rr - f * g.my + 1;
+            }
+            int last = 0;
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                const int row = row0 + i;
+                const bool v = row < g.R;
+                int o;
+                if (MODE == 0) {
+                    o = f * (int)g.fs + j * g.nx + 1;
+                    if (v && ++j > g.my) {
+                        j = 1;
+                        ++f;
+                    }
+                } else {
+                    o = row * g.lds;
+                }
+                if (v) {
+                    last = o;
+                    rvalid |= 1u << i;
+                }
+                roff[i] = v ? o : last;
+            }
         }
         const bool use_sub = (MODE == 0) && sub != nullptr;
+        const float* __restrict__ base_ptr = (MODE == 0) ? src : spec;
         // Two register buffers: the loads of chunk c+2 are issued right after
         // chunk c is stored, so their latency overlaps the processing of
         // chunk c+1, the wait for a free stage and the MMAs.
@@ -298,60 +343,33 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
                 c2 = 0;
             }
             const bool pv = p < lim;
-            const bool p2 = p < no;
-            int row = row0, f = f0, j = j0;
-            long long base = (MODE == 0) ? f0 * g.fs + (long long)j0 * g.nx + 1 : (long long)row0 * g.lds;
-            // Unconditional loads at clamped addresses (rows past the end
-            // repeat the last valid row, columns past the end read column 0);
-            // validity is applied when the chunk is processed, so no load
-            // result is consumed here.
             const int cc1 = pv ? c1 : 0;
-            const int cc2 = (pv && p2) ? c2 : 0;
-            long long lastbase = base;
+            const int cc2 = (pv && p < no) ? c2 : 0;
+            const float* __restrict__ b1 = base_ptr + cc1;
+            const float* __restrict__ b2 = base_ptr + cc2;
             if (MODE == 0 && use_sub) {
                 // nonzero background PV: subtract it (rare path)
+                const float* __restrict__ s1 = sub + cc1;
+                const float* __restrict__ s2 = sub + cc2;
 #pragma unroll
                 for (int i = 0; i < 16; ++i) {
-                    const long long bb = (row < g.R) ? base : lastbase;
-                    const float s1 = f < sub_batches ? __ldg(sub + bb + cc1) : 0.f;
-                    const float s2 = f < sub_batches ? __ldg(sub + bb + cc2) : 0.f;
-                    x1[i] = __ldg(src + bb + cc1) - s1;
-                    x2[i] = __ldg(src + bb + cc2) - s2;
-                    if (row < g.R) lastbase = base;
-                    ++row;
-                    base += g.nx;
-                    if (++j > g.my) {
-                        j = 1;
-                        ++f;
-                        base += 2 * g.nx;
-                    }
+                    const bool hs = roff[i] < sub_batches * (int)g.fs;
+                    x1[i] = __ldg(b1 + roff[i]) - (hs ? __ldg(s1 + roff[i]) : 0.f);
+                    x2[i] = __ldg(b2 + roff[i]) - (hs ? __ldg(s2 + roff[i]) : 0.f);
                 }
                 return;
             }
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
-                const long long bb = (row < g.R) ? base : lastbase;
-                if (MODE == 0) {
-                    x1[i] = __ldg(src + bb + cc1);
-                    x2[i] = __ldg(src + bb + cc2);
-                } else {
-                    x1[i] = __ldg(spec + bb + cc1);
-                    x2[i] = 0.f;
-                }
-                if (row < g.R) lastbase = base;
-                ++row;
-                if (MODE == 0) {
-                    base += g.nx;
-                    if (++j > g.my) {
-                        j = 1;
-                        ++f;
-                        base += 2 * g.nx;
-                    }
-                } else {
-                    base += g.lds;
-                }
+                x1[i] = __ldg(b1 + roff[i]);
+                if (MODE == 0) x2[i] = __ldg(b2 + roff[i]);
             }
         };
+        // shared-memory byte offset of (row r0 + i, k = lane) in a swizzled
+        // [128][32] fp32 tile: r0 is a multiple of 16, so only i enters the
+        // XOR pattern (a compile-time constant per unrolled i)
+        const uint32_t sw_row = (uint32_t)warp * 2048u + (uint32_t)(lane & 3) * 4u;
+        const uint32_t sw_q = (uint32_t)(lane >> 2);
         auto process = [&](int c, const float (&x1)[16], const float (&x2)[16]) {
             const int s = c % STAGES;
             const uint32_t u = c / STAGES;
@@ -360,15 +378,17 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
             if (c >= STAGES) mbar_wait(empty(s), (u - 1) & 1, 1);
             if (tid == 0) {
                 mbar_arrive_expect_tx(fullB(s), 2 * b_bytes);
-                const float* blk = jimg[job] + (size_t)kc * 2 * N * KCH;
+                const long long base = MODE == 0 ? (half ? tab.fwd_base[1] : tab.fwd_base[0])
+                                                 : (job ? tab.inv_base[1] : tab.inv_base[0]);
+                const float* blk = img + base + (size_t)kc * 2 * tab.Ntot * KCH + (size_t)t_first * TILE * KCH;
                 bulk_g2s(b_hi(s), blk, b_bytes, fullB(s));
-                bulk_g2s(b_lo(s), blk + (size_t)N * KCH, b_bytes, fullB(s));
+                bulk_g2s(b_lo(s), blk + (size_t)tab.Ntot * KCH, b_bytes, fullB(s));
             }
             const int p = kc * KCH + lane;
             const bool p2 = p < no;
             const int limv = (MODE == 0) ? (half == 0 ? ne : no) : (job == 0 ? ne : no);
-            const bool pv = p < limv;
-            const uint32_t ah = a_hi(s), al = a_lo(s);
+            const uint32_t keep = (p < limv) ? rvalid : 0u;
+            const uint32_t ah = a_hi(s) + sw_row, al = a_lo(s) + sw_row;
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
                 float val;
@@ -376,11 +396,11 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
                     val = p2 ? (half == 0 ? x1[i] + x2[i] : x1[i] - x2[i]) : x1[i];
                 else
                     val = x1[i];
-                const bool rvalid = blockIdx.y * BM + r0 + i < g.R;
-                val = (pv && rvalid) ? val : 0.f;
+                val = ((keep >> i) & 1u) ? val : 0.f;
                 const float h = tf32_rna(val);
                 const float l = tf32_rna(val - h);
-                const uint32_t off = swz(r0 + i, lane);
+                const uint32_t off = (uint32_t)(i >> 3) * 1024u + (uint32_t)(i & 7) * 128u +
+                                     (((sw_q ^ (uint32_t)(i & 7)) & 7u) << 4);
                 asm volatile("st.shared.f32 [%0], %1;" ::"r"(ah + off), "f"(h) : "memory");
                 asm volatile("st.shared.f32 [%0], %1;" ::"r"(al + off), "f"(l) : "memory");
             }
@@ -430,7 +450,7 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
         if (MODE == 0) {
             const int lim = half == 0 ? ne : no;
             const int coff = half == 0 ? 0 : ne;
-            const int t0 = tile * 256;
+            const int t0 = t_first * TILE;
             for (int rr = 0; rr < 16; ++rr) {
                 const int r = r0 + rr;
                 const int row = blockIdx.y * BM + r;
@@ -445,7 +465,7 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
             // Rows in batches of 4: all addend / mask loads of a batch (4 rows x
             // 4 column groups x both mirror positions) are issued before any
             // store, so their latencies overlap.
-            const int p0 = tile * 128;
+            const int p0 = t_first * TILE;
             constexpr int RB = 4;
             for (int rb = 0; rb < 16; rb += RB) {
                 float add1[RB][4], add2[RB][4];
@@ -561,9 +581,8 @@ int build_tc_images(vd_qg1l_plan* p)
     std::memset(&d->tab, 0, sizeof(TcTab));
     TcTab& tab = d->tab;
     tab.kch = (ne + KCH - 1) / KCH;
-    tab.nt_t = (ne + 255) / 256;
-    tab.nt_p = (ne + 127) / 128;
-    if (tab.nt_t > 8 || tab.nt_p > 16) { delete d; return VD_ERR_UNSUPPORTED; }
+    tab.nt = (ne + TILE - 1) / TILE;
+    if (tab.nt > MAX_TILES) { delete d; return VD_ERR_UNSUPPORTED; }
     const double scale = std::sqrt(2.0 / (n + 1));
     const long long period = 2LL * (n + 1);
     auto S = [&](long long m) { m %= period; return scale * std::sin(M_PI * double(m) / double(n + 1)); };
@@ -592,18 +611,11 @@ int build_tc_images(vd_qg1l_plan* p)
         }
         return off;
     };
-    for (int tt = 0; tt < tab.nt_t; ++tt) {
-        const int N = std::min(256, ((ne - 256 * tt + 15) / 16) * 16);
-        tab.Nt[tt] = N;
-        tab.fwd_off[0][tt] = emit(fwd_odd, 256 * tt, N);
-        tab.fwd_off[1][tt] = emit(fwd_even, 256 * tt, N);
-    }
-    for (int q = 0; q < tab.nt_p; ++q) {
-        const int N = std::min(128, ((ne - 128 * q + 15) / 16) * 16);
-        tab.Np[q] = N;
-        tab.inv_off[0][q] = emit(inv_odd, 128 * q, N);
-        tab.inv_off[1][q] = emit(inv_even, 128 * q, N);
-    }
+    tab.Ntot = ((ne + 15) / 16) * 16;
+    tab.fwd_base[0] = emit(fwd_odd, 0, tab.Ntot);
+    tab.fwd_base[1] = emit(fwd_even, 0, tab.Ntot);
+    tab.inv_base[0] = emit(inv_odd, 0, tab.Ntot);
+    tab.inv_base[1] = emit(inv_even, 0, tab.Ntot);
     if (cudaMalloc(&d->img, img.size() * sizeof(float)) != cudaSuccess) { delete d; return VD_ERR_CUDA; }
     if (cudaMemcpy(d->img, img.data(), img.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) {
         cudaFree(d->img);
@@ -630,14 +642,22 @@ static cudaError_t tc_configure()
 {
     std::call_once(g_tc_once, [] {
         cudaError_t e = cudaFuncSetAttribute(dst_tc_kernel<0, EPI_H>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)SMEM_BYTES);
+                                             (int)SMEM_MAX);
         if (!e) e = cudaFuncSetAttribute(dst_tc_kernel<1, EPI_H>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)SMEM_BYTES);
+                                         (int)SMEM_MAX);
         if (!e) e = cudaFuncSetAttribute(dst_tc_kernel<1, EPI_ADJQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)SMEM_BYTES);
+                                         (int)SMEM_MAX);
         g_tc_err = e;
     });
     return g_tc_err;
+}
+
+// The producers address rows with 32-bit element offsets.
+bool tc_fits(const vd_qg1l_plan* p, int nf)
+{
+    const DSTTables& t = p->dst;
+    const long long fs = (long long)p->d.ny * p->d.nx;
+    return (long long)nf * fs < (1LL << 31) && (long long)nf * t.my * t.lds < (1LL << 31);
 }
 
 // One x-direction pass on the tensor cores (forward: fields -> spec,
@@ -645,7 +665,7 @@ static cudaError_t tc_configure()
 int dst_pass_tc(const vd_qg1l_plan* p, int nf, const SolveArgs& a, float* spec, bool fwd, cudaStream_t st)
 {
     const TcPlanData* d = (const TcPlanData*)p->dst.tc;
-    if (!d) return VD_ERR_UNSUPPORTED;
+    if (!d || !tc_fits(p, nf)) return VD_ERR_UNSUPPORTED;
     if (tc_configure() != cudaSuccess) return VD_ERR_CUDA;
     const DSTTables& t = p->dst;
     TcGeom g;
@@ -654,20 +674,39 @@ int dst_pass_tc(const vd_qg1l_plan* p, int nf, const SolveArgs& a, float* spec, 
     g.R = nf * t.my;
     g.lds = t.lds;
     const int rows = (g.R + BM - 1) / BM;
+    // Tiles per CTA: the widest group (fewest re-reads of the A rows) that
+    // still launches ~120 CTAs on the 152 SMs.
+    TcTab tab = d->tab;
+    const int nt = tab.nt;
+    auto groups = [&](int gsz) { return (nt + gsz - 1) / gsz; };
+    tab.gf = 1;
+    for (int gsz : {8, 4, 2}) {
+        if (2LL * groups(gsz) * rows >= 120) { tab.gf = gsz; break; }
+    }
+    tab.gi = 1;
+    for (int gsz : {4, 2}) {
+        if ((long long)groups(gsz) * rows >= 120) { tab.gi = gsz; break; }
+    }
+    // as many stages as the B operand size of the launch allows
+    const int gmax = fwd ? tab.gf : tab.gi;
+    tab.b_tile = (uint32_t)gmax * TILE_BYTES;
+    const size_t stage_bytes = 2 * (size_t)A_TILE + 2 * (size_t)tab.b_tile;
+    tab.nst = (int)std::min<size_t>(MAX_STAGES, PIPE_BYTES / stage_bytes);
+    const size_t smem = std::max<size_t>(tab.nst * stage_bytes, EPI_BYTES) + 1024;   // <= SMEM_MAX
     if (fwd) {
-        dim3 grid(2 * d->tab.nt_t, rows);
-        dst_tc_kernel<0, EPI_H><<<grid, NTHREADS, SMEM_BYTES, st>>>(
-            g, d->tab, d->img, (const float*)a.src, (const float*)a.sub, a.sub_batches, spec, nullptr, nullptr, 0,
+        dim3 grid(2 * groups(tab.gf), rows);
+        dst_tc_kernel<0, EPI_H><<<grid, NTHREADS, smem, st>>>(
+            g, tab, d->img, (const float*)a.src, (const float*)a.sub, a.sub_batches, spec, nullptr, nullptr, 0,
             nullptr);
     } else if (a.epi == EPI_H) {
-        dim3 grid(d->tab.nt_p, rows);
-        dst_tc_kernel<1, EPI_H><<<grid, NTHREADS, SMEM_BYTES, st>>>(
-            g, d->tab, d->img, nullptr, nullptr, 0, spec, (float*)a.out, (const float*)a.add, a.add_batches,
+        dim3 grid(groups(tab.gi), rows);
+        dst_tc_kernel<1, EPI_H><<<grid, NTHREADS, smem, st>>>(
+            g, tab, d->img, nullptr, nullptr, 0, spec, (float*)a.out, (const float*)a.add, a.add_batches,
             p->d_mask);
     } else {
-        dim3 grid(d->tab.nt_p, rows);
-        dst_tc_kernel<1, EPI_ADJQ><<<grid, NTHREADS, SMEM_BYTES, st>>>(
-            g, d->tab, d->img, nullptr, nullptr, 0, spec, (float*)a.out, (const float*)a.add, a.add_batches,
+        dim3 grid(groups(tab.gi), rows);
+        dst_tc_kernel<1, EPI_ADJQ><<<grid, NTHREADS, smem, st>>>(
+            g, tab, d->img, nullptr, nullptr, 0, spec, (float*)a.out, (const float*)a.add, a.add_batches,
             p->d_mask);
     }
     VD_LAUNCH_CHECK();

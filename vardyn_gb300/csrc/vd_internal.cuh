@@ -109,6 +109,8 @@ int build_dst_tables(vd_qg1l_plan* p);
 void free_dst_tables(vd_qg1l_plan* p);
 int build_tc_images(vd_qg1l_plan* p);
 void free_tc_images(vd_qg1l_plan* p);
+// Whether a batch of nf fields fits the tensor-core pass (32-bit row offsets).
+bool tc_fits(const vd_qg1l_plan* p, int nf);
 int dst_pass_tc(const vd_qg1l_plan* p, int nf, const SolveArgs& a, float* spec, bool fwd, cudaStream_t st);
 
 // Bump allocator over a caller workspace.
