@@ -14,13 +14,14 @@
 // x_lo.w_lo term is ~2^-22 relative).
 //
 // Pipeline (per K chunk of 32 = one 128-byte swizzle row of fp32):
-//   warps 0-7  build the A chunk (butterfly or copy of the input rows, hi/lo
-//              split) in the 128B-swizzled K-major layout and arrive on fullA;
+//   warps 0-15 build the A chunk (butterfly or copy of the input rows, hi/lo
+//              split; 8 rows each) in the 128B-swizzled K-major layout and
+//              arrive on fullA;
 //   thread 0   also issues the bulk copies (cp.async.bulk) of the
 //              pre-swizzled hi/lo chunks of the DST half matrix (fullB);
-//   warp 8     owns the TMEM allocation; its lane 0 issues 3 x 4 MMAs per
+//   warp 16    owns the TMEM allocation; its lane 0 issues 3 x 4 MMAs per
 //              chunk and commits to `empty` to recycle the stage;
-//   warps 0-7  finally read the accumulators (tcgen05.ld) and write rows.
+//   warps 0-15 finally read the accumulators (tcgen05.ld) and write rows.
 // Every mbarrier wait is bounded (2 s of %globaltimer); a timeout sets a bit
 // in a device flag (vd_device_error) and the CTA finishes without hanging.
 #include "vd_internal.cuh"
@@ -38,8 +39,10 @@ namespace tc {
 
 constexpr int BM = 128;
 constexpr int KCH = 32;
-constexpr int NPROD = 256;      // producer / epilogue threads (warps 0-7)
-constexpr int NTHREADS = NPROD + 32;   // + warp 8: TMEM owner and MMA issuer
+constexpr int NPW = 16;                // producer / epilogue warps
+constexpr int RPW = 128 / NPW;         // A rows per producer warp
+constexpr int NPROD = NPW * 32;
+constexpr int NTHREADS = NPROD + 32;   // + warp NPW: TMEM owner and MMA issuer
 constexpr int MAX_STAGES = 6;
 constexpr int TMEM_COLS = 256;
 constexpr int TILE = 32;                           // columns of one B image tile
@@ -94,6 +97,27 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int cod
             return false;
         }
     }
+}
+
+// Distributed shared memory of a 2-CTA cluster (the inverse pass).
+__device__ __forceinline__ uint32_t mapa_shared(uint32_t addr, uint32_t rank)
+{
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ float ld_cluster_f32(uint32_t addr)
+{
+    float v;
+    asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(addr) : "memory");
+    return v;
+}
+// Every thread of both CTAs arrives; shared-memory writes before the
+// barrier are visible to the peer CTA after it.
+__device__ __forceinline__ void cluster_sync_all()
+{
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\t"
+                 "barrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
 __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar)
@@ -244,20 +268,22 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
     const int lane = tid & 31;
 
     // ---- job layout of this CTA --------------------------------------------
-    // tiles [t_first, t_first + ntl) of one parity (forward) or of both
-    // parities (inverse: job 0 odd, job 1 even rows of the spectrum)
-    int njobs, half = 0, t_first, ntl;
+    // Forward: tiles [t_first, t_first + ntl) of one output parity. Inverse:
+    // the CTA pair of a cluster shares the rows and the tiles; rank 0 takes
+    // the odd-k rows of the spectrum (job 0), rank 1 the even-k rows (job 1),
+    // and the epilogue combines the two through distributed shared memory.
+    int half = 0, t_first, ntl, cjob = 0;
     if (MODE == 0) {
         const int G = (tab.nt + tab.gf - 1) / tab.gf;
         half = blockIdx.x / G;
         t_first = (blockIdx.x - half * G) * tab.gf;
         ntl = min(tab.gf, tab.nt - t_first);
-        njobs = 1;
     } else {
-        t_first = blockIdx.x * tab.gi;
+        cjob = blockIdx.x & 1;
+        t_first = (blockIdx.x >> 1) * tab.gi;
         ntl = min(tab.gi, tab.nt - t_first);
-        njobs = 2;
     }
+    const int njobs = 1;
     const int N = min(TILE * ntl, tab.Ntot - TILE * t_first);
     const int nchunks = njobs * tab.kch;
     const uint32_t b_bytes = (uint32_t)N * KCH * 4;
@@ -284,15 +310,15 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
     const int n = g.n, ne = g.ne, no = g.no;
     if (warp < MMA_WARP) {
         // ------------------------------ producers ------------------------------
-        // warp w fills rows [16w, 16w+16) of the A chunk; lane l handles K
+        // warp w fills rows [RPW w, RPW (w+1)) of the A chunk; lane l handles K
         // index k0 + l, so every global load is one coalesced 128-byte row.
         // The element offsets of the warp's 16 rows do not change from chunk
         // to chunk: they are computed once (32-bit; the host checks that the
         // arrays are smaller than 2^31 elements). Rows past the end repeat
         // the last valid row and are zeroed when the chunk is stored.
-        const int r0 = warp * 16;
+        const int r0 = warp * RPW;
         const int row0 = blockIdx.y * BM + r0;
-        int roff[16];
+        int roff[RPW];
         uint32_t rvalid = 0;
         {
             int f = 0, j = 1;
@@ -303,7 +329,7 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
             }
             int last = 0;
 #pragma unroll
-            for (int i = 0; i < 16; ++i) {
+            for (int i = 0; i < RPW; ++i) {
                 const int row = row0 + i;
                 const bool v = row < g.R;
                 int o;
@@ -328,9 +354,9 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
         // Two register buffers: the loads of chunk c+2 are issued right after
         // chunk c is stored, so their latency overlaps the processing of
         // chunk c+1, the wait for a free stage and the MMAs.
-        auto load_chunk = [&](int c, float (&x1)[16], float (&x2)[16]) {
-            const int job = c / tab.kch;
-            const int kc = c - job * tab.kch;
+        auto load_chunk = [&](int c, float (&x1)[RPW], float (&x2)[RPW]) {
+            const int job = cjob;
+            const int kc = c;
             const int p = kc * KCH + lane;
             int lim, c1, c2;
             if (MODE == 0) {
@@ -352,7 +378,7 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
                 const float* __restrict__ s1 = sub + cc1;
                 const float* __restrict__ s2 = sub + cc2;
 #pragma unroll
-                for (int i = 0; i < 16; ++i) {
+                for (int i = 0; i < RPW; ++i) {
                     const bool hs = roff[i] < sub_batches * (int)g.fs;
                     x1[i] = __ldg(b1 + roff[i]) - (hs ? __ldg(s1 + roff[i]) : 0.f);
                     x2[i] = __ldg(b2 + roff[i]) - (hs ? __ldg(s2 + roff[i]) : 0.f);
@@ -360,21 +386,28 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
                 return;
             }
 #pragma unroll
-            for (int i = 0; i < 16; ++i) {
+            for (int i = 0; i < RPW; ++i) {
                 x1[i] = __ldg(b1 + roff[i]);
                 if (MODE == 0) x2[i] = __ldg(b2 + roff[i]);
             }
         };
         // shared-memory byte offset of (row r0 + i, k = lane) in a swizzled
-        // [128][32] fp32 tile: r0 is a multiple of 16, so only i enters the
+        // [128][32] fp32 tile: r0 is a multiple of 8, so only i enters the
         // XOR pattern (a compile-time constant per unrolled i)
-        const uint32_t sw_row = (uint32_t)warp * 2048u + (uint32_t)(lane & 3) * 4u;
+        const uint32_t sw_row = (uint32_t)(r0 >> 3) * 1024u + (uint32_t)(lane & 3) * 4u;
         const uint32_t sw_q = (uint32_t)(lane >> 2);
-        auto process = [&](int c, const float (&x1)[16], const float (&x2)[16]) {
-            const int s = c % STAGES;
-            const uint32_t u = c / STAGES;
-            const int job = c / tab.kch;
-            const int kc = c - job * tab.kch;
+        // stage / phase of the next chunk to store (chunks are stored in order)
+        int ps = 0;
+        uint32_t pu = 0;
+        auto process = [&](int c, const float (&x1)[RPW], const float (&x2)[RPW]) {
+            const int s = ps;
+            const uint32_t u = pu;
+            if (++ps == STAGES) {
+                ps = 0;
+                ++pu;
+            }
+            const int job = cjob;
+            const int kc = c;
             if (c >= STAGES) mbar_wait(empty(s), (u - 1) & 1, 1);
             if (tid == 0) {
                 mbar_arrive_expect_tx(fullB(s), 2 * b_bytes);
@@ -390,7 +423,7 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
             const uint32_t keep = (p < limv) ? rvalid : 0u;
             const uint32_t ah = a_hi(s) + sw_row, al = a_lo(s) + sw_row;
 #pragma unroll
-            for (int i = 0; i < 16; ++i) {
+            for (int i = 0; i < RPW; ++i) {
                 float val;
                 if (MODE == 0)
                     val = p2 ? (half == 0 ? x1[i] + x2[i] : x1[i] - x2[i]) : x1[i];
@@ -407,7 +440,7 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
             fence_async_smem();
             mbar_arrive(fullA(s));
         };
-        float xa1[16], xa2[16], xb1[16], xb2[16];
+        float xa1[RPW], xa2[RPW], xb1[RPW], xb2[RPW];
         load_chunk(0, xa1, xa2);
         if (nchunks > 1) load_chunk(1, xb1, xb2);
         for (int c = 0; c < nchunks; c += 2) {
@@ -421,8 +454,8 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
 
         // ------------------------------ epilogue -------------------------------
         // accumulators -> shared staging tile [128][S], then coalesced row
-        // stores. Warps w and w+4 share TMEM lanes 32(w%4).. and split the
-        // columns. All stages are free once the last MMA has completed.
+        // stores. Warps w, w+4, w+8, w+12 share TMEM lanes 32(w%4).. and split
+        // the columns. All stages are free once the last MMA has completed.
         mbar_wait(accf, 0, 4);
         tc_fence_after();
         constexpr int S = 257;
@@ -431,27 +464,22 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
         const int hc = warp >> 2;
         const int trow = sp * 32 + lane;
         const uint32_t lane_base = tmem + ((uint32_t)(sp * 32) << 16);
-        int cbeg, cend;
-        if (MODE == 0) {
-            const int halfN = ((N / 2 + 31) / 32) * 32;
-            cbeg = hc == 0 ? 0 : halfN;
-            cend = hc == 0 ? halfN : N;
-        } else {
-            cbeg = hc * 128;
-            cend = hc * 128 + N;
-        }
+        constexpr int NQ = NPW / 4;     // warps per TMEM lane quarter
+        const int per = (((N + NQ - 1) / NQ + 31) / 32) * 32;
+        const int cbeg = min(N, hc * per);
+        const int cend = min(N, cbeg + per);
         for (int cg = cbeg; cg < cend; cg += 32) {
             float vv[32];
             tmem_ld32(lane_base + cg, vv);
 #pragma unroll
             for (int i = 0; i < 32; ++i) ep[trow * S + cg + i] = vv[i];
         }
-        asm volatile("bar.sync 1, 256;" ::: "memory");
         if (MODE == 0) {
+            asm volatile("bar.sync 1, %0;" ::"n"(NPROD) : "memory");
             const int lim = half == 0 ? ne : no;
             const int coff = half == 0 ? 0 : ne;
             const int t0 = t_first * TILE;
-            for (int rr = 0; rr < 16; ++rr) {
+            for (int rr = 0; rr < RPW; ++rr) {
                 const int r = r0 + rr;
                 const int row = blockIdx.y * BM + r;
                 if (row >= g.R) break;
@@ -461,75 +489,18 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
                     if (t < lim) drow[t] = ep[r * S + cc];
                 }
             }
-        } else {
-            // Rows in batches of 4: all addend / mask loads of a batch (4 rows x
-            // 4 column groups x both mirror positions) are issued before any
-            // store, so their latencies overlap.
-            const int p0 = t_first * TILE;
-            constexpr int RB = 4;
-            for (int rb = 0; rb < 16; rb += RB) {
-                float add1[RB][4], add2[RB][4];
-                bool m1[RB][4], m2[RB][4];
-                long long bases[RB];
-                int js[RB];
-#pragma unroll
-                for (int q = 0; q < RB; ++q) {
-                    const int row = blockIdx.y * BM + r0 + rb + q;
-                    const bool rv = row < g.R;
-                    const int f = rv ? row / g.my : 0;
-                    const int j = rv ? row - f * g.my + 1 : 1;
-                    bases[q] = rv ? f * g.fs + (long long)j * g.nx + 1 : -1;
-                    js[q] = j;
-                    const bool ha = rv && add != nullptr && (EPI != EPI_H || f < add_batches);
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const int cc = lane + 32 * u;
-                        const int p = p0 + cc;
-                        const bool v1 = rv && cc < N && p < ne;
-                        const bool v2 = v1 && p < no;
-                        add1[q][u] = (v1 && ha) ? add[bases[q] + p] : 0.f;
-                        add2[q][u] = (v2 && ha) ? add[bases[q] + (n - 1 - p)] : 0.f;
-                        if (EPI == EPI_ADJQ) {
-                            m1[q][u] = v1 && mask[j * g.nx + 1 + p] == 3;
-                            m2[q][u] = v2 && mask[j * g.nx + 1 + (n - 1 - p)] == 3;
-                        }
-                    }
-                }
-#pragma unroll
-                for (int q = 0; q < RB; ++q) {
-                    if (bases[q] < 0) continue;
-                    const int r = r0 + rb + q;
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const int cc = lane + 32 * u;
-                        const int p = p0 + cc;
-                        if (cc >= N || p >= ne) continue;
-                        const float A = ep[r * S + cc];
-                        const float B = (p < no) ? ep[r * S + 128 + cc] : 0.f;
-                        const long long o1 = bases[q] + p;
-                        if (EPI == EPI_H) out[o1] = A + B + add1[q][u];
-                        else out[o1] = m1[q][u] ? A + B + add1[q][u] : 0.f;
-                        if (p < no) {
-                            const long long o2 = bases[q] + (n - 1 - p);
-                            if (EPI == EPI_H) out[o2] = A - B + add2[q][u];
-                            else out[o2] = m2[q][u] ? A - B + add2[q][u] : 0.f;
-                        }
-                    }
-                }
-            }
         }
     } else if (lane == 0) {
         // ------------------------------ MMA issuer -----------------------------
         const uint32_t idesc = idesc_tf32(BM, N);
+        int s = 0;
+        uint32_t u = 0;
         for (int c = 0; c < nchunks; ++c) {
-            const int s = c % STAGES;
-            const uint32_t u = c / STAGES;
-            const int job = c / tab.kch;
-            const int kc = c - job * tab.kch;
+            const int kc = c;
             mbar_wait(fullA(s), u & 1, 2);
             mbar_wait(fullB(s), u & 1, 2);
             tc_fence_after();
-            const uint32_t d = tmem + (uint32_t)(job * 128);
+            const uint32_t d = tmem;
 #pragma unroll
             for (int kk = 0; kk < KCH / 8; ++kk) {
                 const uint64_t ah = sdesc_sw128(a_hi(s) + kk * 32);
@@ -541,8 +512,61 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
                 mma_tf32(d, al, bh, idesc, 1u);
             }
             mma_commit(empty(s));
+            if (++s == STAGES) {
+                s = 0;
+                ++u;
+            }
         }
         mma_commit(accf);
+    }
+    __syncwarp();
+    if constexpr (MODE == 1) {
+        // ---------------- inverse epilogue across the CTA pair ----------------
+        // Rank 0 (odd-k sum A) writes x[p] = A + B, rank 1 (even-k sum B)
+        // writes x[n-1-p] = A - B, each reading the peer's staged
+        // accumulators. Every thread of both CTAs reaches both barriers.
+        cluster_sync_all();
+        if (warp < MMA_WARP) {
+            constexpr int S = 257;
+            const float* ep = reinterpret_cast<const float*>(sm);
+            const uint32_t ep_peer = mapa_shared(smem_u32(sm), (uint32_t)(cjob ^ 1));
+            const int r0 = warp * RPW;
+            const int p0 = t_first * TILE;
+            const int lim = cjob == 0 ? ne : no;
+            for (int rr = 0; rr < RPW; ++rr) {
+                const int r = r0 + rr;
+                const int row = blockIdx.y * BM + r;
+                if (row >= g.R) break;
+                const int f = row / g.my;
+                const int j = row - f * g.my + 1;
+                const long long base = f * g.fs + (long long)j * g.nx + 1;
+                const bool ha = add != nullptr && (EPI != EPI_H || f < add_batches);
+                float av[8], own[8], oth[8];
+                bool mk[8];
+                // all loads of the row first, then the stores
+#pragma unroll
+                for (int u8 = 0; u8 < 8; ++u8) {
+                    const int cc = lane + 32 * u8;
+                    const int p = p0 + cc;
+                    const bool v = cc < N && p < lim;
+                    const int col = cjob == 0 ? p : n - 1 - p;
+                    av[u8] = (v && ha) ? add[base + col] : 0.f;
+                    mk[u8] = (EPI == EPI_ADJQ) ? (v && mask[j * g.nx + 1 + col] == 3) : v;
+                    own[u8] = v ? ep[r * S + cc] : 0.f;
+                    oth[u8] = v ? ld_cluster_f32(ep_peer + (uint32_t)(r * S + cc) * 4u) : 0.f;
+                }
+#pragma unroll
+                for (int u8 = 0; u8 < 8; ++u8) {
+                    const int cc = lane + 32 * u8;
+                    const int p = p0 + cc;
+                    if (!(cc < N && p < lim)) continue;
+                    const float val = cjob == 0 ? own[u8] + (p < no ? oth[u8] : 0.f) : oth[u8] - own[u8];
+                    const int col = cjob == 0 ? p : n - 1 - p;
+                    out[base + col] = mk[u8] ? val + av[u8] : 0.f;
+                }
+            }
+        }
+        cluster_sync_all();
     }
     tc_fence_before();
     __syncthreads();
@@ -684,8 +708,8 @@ int dst_pass_tc(const vd_qg1l_plan* p, int nf, const SolveArgs& a, float* spec, 
         if (2LL * groups(gsz) * rows >= 120) { tab.gf = gsz; break; }
     }
     tab.gi = 1;
-    for (int gsz : {4, 2}) {
-        if ((long long)groups(gsz) * rows >= 120) { tab.gi = gsz; break; }
+    for (int gsz : {8, 4, 2}) {
+        if (2LL * groups(gsz) * rows >= 120) { tab.gi = gsz; break; }
     }
     // as many stages as the B operand size of the launch allows
     const int gmax = fwd ? tab.gf : tab.gi;
@@ -698,16 +722,30 @@ int dst_pass_tc(const vd_qg1l_plan* p, int nf, const SolveArgs& a, float* spec, 
         dst_tc_kernel<0, EPI_H><<<grid, NTHREADS, smem, st>>>(
             g, tab, d->img, (const float*)a.src, (const float*)a.sub, a.sub_batches, spec, nullptr, nullptr, 0,
             nullptr);
-    } else if (a.epi == EPI_H) {
-        dim3 grid(groups(tab.gi), rows);
-        dst_tc_kernel<1, EPI_H><<<grid, NTHREADS, smem, st>>>(
-            g, tab, d->img, nullptr, nullptr, 0, spec, (float*)a.out, (const float*)a.add, a.add_batches,
-            p->d_mask);
     } else {
-        dim3 grid(groups(tab.gi), rows);
-        dst_tc_kernel<1, EPI_ADJQ><<<grid, NTHREADS, smem, st>>>(
-            g, tab, d->img, nullptr, nullptr, 0, spec, (float*)a.out, (const float*)a.add, a.add_batches,
-            p->d_mask);
+        // CTA pairs (clusters of 2): rank 0 the odd-k half, rank 1 the even-k half
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(2 * groups(tab.gi), rows);
+        cfg.blockDim = dim3(NTHREADS);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = st;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = 2;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        const float* add = (const float*)a.add;
+        float* outp = (float*)a.out;
+        const cudaError_t e = a.epi == EPI_H
+            ? cudaLaunchKernelEx(&cfg, dst_tc_kernel<1, EPI_H>, g, tab, (const float*)d->img, (const float*)nullptr,
+                                 (const float*)nullptr, 0, spec, outp, add, a.add_batches,
+                                 (const int8_t*)p->d_mask)
+            : cudaLaunchKernelEx(&cfg, dst_tc_kernel<1, EPI_ADJQ>, g, tab, (const float*)d->img,
+                                 (const float*)nullptr, (const float*)nullptr, 0, spec, outp, add, a.add_batches,
+                                 (const int8_t*)p->d_mask);
+        if (e != cudaSuccess) return VD_ERR_CUDA;
     }
     VD_LAUNCH_CHECK();
     return VD_OK;
