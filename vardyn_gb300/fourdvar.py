@@ -183,7 +183,6 @@ class QGWindows4DVar:
         p, B = self.plan, self.B
         self._copy(h0, self.tv[0, 0])
         p.init_state(self.tv[0, 0], self.hb, self.tv[0, 1], self.qb)
-        h0_keep = self.tmp if self.snap is None else None
         if self.snap is None:
             self._forward_full()
         else:
