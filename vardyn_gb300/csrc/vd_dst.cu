@@ -231,11 +231,12 @@ dst_gemm_kernel(GemmGeom g, const T* __restrict__ W1, const T* __restrict__ W2,
 // only shrink.
 // CW spectral columns per CTA; the warp's lanes are CW columns x (32/CW)
 // row pieces, so a CTA holds nw*(32/CW) pieces of CH rows per column. Each
-// piece runs both Thomas sweeps locally (the recurrences are affine, so a
-// piece is summarised by its end value and the product of its multipliers);
-// CW threads then chain the pieces of their column and every piece applies
-// the carry it receives. Narrow CTAs (CW = 8) give enough CTAs to fill the
-// GPU when there are few columns (one 1024^2 field: 128 CTAs).
+// thread keeps its piece (values and multipliers) in registers and runs both
+// Thomas sweeps locally (the recurrences are affine, so a piece is summarised
+// by its end value and the product of its multipliers); CW threads then chain
+// the pieces of their column through shared memory and every piece applies
+// the carry it receives. Eight columns per CTA: 1024 CTAs for 16 fields of
+// 512^2, 128 for one 1024^2 field.
 template <typename T, int CW, int CH>
 __global__ void __launch_bounds__(512)
 tridiag_chunked_kernel(T* __restrict__ spec, const T* __restrict__ trim, int my, int n, int lds, T a)
@@ -244,41 +245,37 @@ tridiag_chunked_kernel(T* __restrict__ spec, const T* __restrict__ trim, int my,
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nw = blockDim.y;
     const int NP = nw * SUB;
-    T* F = reinterpret_cast<T*>(smem_raw);          // [my][CW]
-    T* cD = F + (size_t)my * CW;                    // [NP][CW] piece-end values / carries
+    T* cD = reinterpret_cast<T*>(smem_raw);         // [NP][CW] piece-end values / carries
     T* cP = cD + (size_t)NP * CW;                   // [NP][CW] piece products
     const int f = blockIdx.y;
     const int lane = threadIdx.x, w = threadIdx.y;
     const int tid = w * 32 + lane;
-    const int nthr = nw * 32;
     const int c = lane % CW;
     const int pc = w * SUB + lane / CW;
-    const int tbase = blockIdx.x * CW;
-    const int t = tbase + c;
+    const int t = blockIdx.x * CW + c;
     const bool col_ok = t < n;
-    T* S = spec + (long long)f * my * lds;
-    for (int e = tid; e < my * CW; e += nthr) {
-        const int j = e / CW, cc = e - j * CW;
-        F[e] = (tbase + cc < n) ? S[(long long)j * lds + tbase + cc] : T(0);
+    T* S = spec + (long long)f * my * lds + t;
+    const T* M = trim + t;
+    const int j0 = pc * CH;
+    const int cnt = col_ok ? max(0, min(CH, my - j0)) : 0;
+    T x[CH], al[CH];
+#pragma unroll
+    for (int i = 0; i < CH; ++i) {
+        const bool v = i < cnt;
+        x[i] = v ? S[(long long)(j0 + i) * lds] : T(0);
+        al[i] = v ? __ldg(M + (long long)(j0 + i) * lds) : T(0);
     }
 
-    const int j0 = pc * CH;
-    const int cnt = max(0, min(CH, my - j0));
-    T mm[CH];
-#pragma unroll
-    for (int i = 0; i < CH; ++i)
-        mm[i] = (col_ok && i < cnt) ? __ldg(trim + (long long)(j0 + i) * lds + t) : T(0);
-    __syncthreads();
-
-    // forward sweep, piece-local
+    // forward sweep, piece-local: d_j = m_j F_j + (-a m_j) d_{j-1}
     T d = T(0), P = T(1);
 #pragma unroll
     for (int i = 0; i < CH; ++i) {
         if (i < cnt) {
-            const T al = -a * mm[i];
-            d = mm[i] * F[(j0 + i) * CW + c] + al * d;
-            F[(j0 + i) * CW + c] = d;
-            P *= al;
+            const T m = al[i];
+            al[i] = -a * m;
+            d = m * x[i] + al[i] * d;
+            x[i] = d;
+            P *= al[i];
         }
     }
     cD[pc * CW + c] = d;
@@ -298,26 +295,25 @@ tridiag_chunked_kernel(T* __restrict__ spec, const T* __restrict__ trim, int my,
 #pragma unroll
         for (int i = 0; i < CH; ++i) {
             if (i < cnt) {
-                pr *= -a * mm[i];
-                F[(j0 + i) * CW + c] += pr * cin;
+                pr *= al[i];
+                x[i] += pr * cin;
             }
         }
     }
     __syncthreads();
 
-    // backward sweep, piece-local from the piece end
-    T x = T(0);
+    // backward sweep, piece-local from the piece end: x_j = d_j + (-a m_j) x_{j+1}
+    T xr = T(0);
     P = T(1);
 #pragma unroll
     for (int i = CH - 1; i >= 0; --i) {
         if (i < cnt) {
-            const T al = -a * mm[i];
-            x = F[(j0 + i) * CW + c] + al * x;
-            F[(j0 + i) * CW + c] = x;
-            P *= al;
+            xr = x[i] + al[i] * xr;
+            x[i] = xr;
+            P *= al[i];
         }
     }
-    cD[pc * CW + c] = x;
+    cD[pc * CW + c] = xr;
     cP[pc * CW + c] = P;
     __syncthreads();
     if (tid < CW) {
@@ -334,16 +330,14 @@ tridiag_chunked_kernel(T* __restrict__ spec, const T* __restrict__ trim, int my,
 #pragma unroll
         for (int i = CH - 1; i >= 0; --i) {
             if (i < cnt) {
-                pr *= -a * mm[i];
-                F[(j0 + i) * CW + c] += pr * cin;
+                pr *= al[i];
+                x[i] += pr * cin;
             }
         }
     }
-    __syncthreads();
-    for (int e = tid; e < my * CW; e += nthr) {
-        const int j = e / CW, cc = e - j * CW;
-        if (tbase + cc < n) S[(long long)j * lds + tbase + cc] = F[e];
-    }
+#pragma unroll
+    for (int i = 0; i < CH; ++i)
+        if (i < cnt) S[(long long)(j0 + i) * lds] = x[i];
 }
 
 // Same recurrences directly on the spectral buffer, for column blocks too tall
@@ -473,62 +467,31 @@ static cudaError_t set_smem_attrs()
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, maxb);
 }
 
-template <typename T>
-static cudaError_t set_tridiag_attrs()
-{
-    const int maxb = 227 * 1024;
-    cudaError_t e;
-    if ((e = cudaFuncSetAttribute(tridiag_chunked_kernel<T, 32, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  maxb))) return e;
-    if ((e = cudaFuncSetAttribute(tridiag_chunked_kernel<T, 16, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  maxb))) return e;
-    if ((e = cudaFuncSetAttribute(tridiag_chunked_kernel<T, 8, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  maxb))) return e;
-    if constexpr (sizeof(T) == 4) {
-        if ((e = cudaFuncSetAttribute(tridiag_chunked_kernel<T, 32, 64>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, maxb))) return e;
-        if ((e = cudaFuncSetAttribute(tridiag_chunked_kernel<T, 16, 64>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, maxb))) return e;
-    }
-    return cudaSuccess;
-}
-
-// The y-direction tridiagonal solves of nf fields: the widest column group
-// (32, 16 or 8 columns per CTA) that still gives ~120 CTAs, pieces of 32
-// rows (64 for tall float32 fields with wide groups) in at most 16 warps;
-// very tall fields fall back to one sequential thread per column.
+// The y-direction tridiagonal solves of nf fields: 8 columns per CTA,
+// pieces of 16 rows (32 for fields of 1025-2048 rows) in at most 16 warps;
+// taller fields fall back to one sequential thread per column. (Measured on
+// GB300 against 32- and 16-column groups, shared-memory staging and a
+// warp-shuffle chain of the pieces: this form is the fastest or tied at both
+// 16 x 510^2 and 1 x 1022^2.)
 template <typename T>
 static int launch_tridiag(const vd_qg1l_plan* p, int nf, T* spec, cudaStream_t st)
 {
     const DSTTables& t = p->dst;
     const T a = (T)t.tri_a;
-    for (int cw : {32, 16, 8}) {
-        const long long ctas = (long long)((t.n + cw - 1) / cw) * nf;
-        if (cw != 8 && ctas < 120) continue;
-        const int sub = 32 / cw;
-        for (int ch : {32, 64}) {
-            if (ch == 64 && (sizeof(T) == 8 || cw == 8)) continue;
-            const int np_need = (t.my + ch - 1) / ch;
-            const int nw = (np_need + sub - 1) / sub;
-            if (nw > 16) continue;
-            const size_t smem = (size_t(t.my) * cw + 2 * size_t(nw) * sub * cw) * sizeof(T);
-            if (smem > 200 * 1024) continue;
-            const dim3 grid((t.n + cw - 1) / cw, nf), block(32, nw);
-#define VD_TRI(CW, CH) tridiag_chunked_kernel<T, CW, CH><<<grid, block, smem, st>>>(spec, (const T*)t.trim, t.my, \
-                                                                                   t.n, t.lds, a)
-            if (cw == 32 && ch == 32) VD_TRI(32, 32);
-            else if (cw == 16 && ch == 32) VD_TRI(16, 32);
-            else if (cw == 8) VD_TRI(8, 32);
-            else if constexpr (sizeof(T) == 4) {
-                if (cw == 32) VD_TRI(32, 64);
-                else VD_TRI(16, 64);
-            }
-#undef VD_TRI
-            VD_LAUNCH_CHECK();
-            return VD_OK;
-        }
+    constexpr int CW = 8, SUB = 32 / CW;
+    const dim3 grid((t.n + CW - 1) / CW, nf);
+    const int nw16 = ((t.my + 15) / 16 + SUB - 1) / SUB;
+    const int nw32 = ((t.my + 31) / 32 + SUB - 1) / SUB;
+    if (nw16 <= 16) {
+        tridiag_chunked_kernel<T, CW, 16><<<grid, dim3(32, nw16), 2 * nw16 * SUB * CW * sizeof(T), st>>>(
+            spec, (const T*)t.trim, t.my, t.n, t.lds, a);
+    } else if (nw32 <= 16) {
+        tridiag_chunked_kernel<T, CW, 32><<<grid, dim3(32, nw32), 2 * nw32 * SUB * CW * sizeof(T), st>>>(
+            spec, (const T*)t.trim, t.my, t.n, t.lds, a);
+    } else {
+        tridiag_global_kernel<T><<<dim3((t.n + 31) / 32, nf), 32, 0, st>>>(spec, (const T*)t.trim, t.my, t.n,
+                                                                           t.lds, a);
     }
-    tridiag_global_kernel<T><<<dim3((t.n + 31) / 32, nf), 32, 0, st>>>(spec, (const T*)t.trim, t.my, t.n, t.lds, a);
     VD_LAUNCH_CHECK();
     return VD_OK;
 }
@@ -545,8 +508,6 @@ static cudaError_t configure_kernels()
         if (!e) e = set_smem_attrs<float, 64>();
         if (!e) e = set_smem_attrs<double, 16>();
         if (!e) e = set_smem_attrs<double, 32>();
-        if (!e) e = set_tridiag_attrs<float>();
-        if (!e) e = set_tridiag_attrs<double>();
         g_attr_err = e;
     });
     return g_attr_err;

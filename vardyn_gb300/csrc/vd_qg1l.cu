@@ -280,32 +280,76 @@ k_adj_stage_fused(QGGeom G, int nf, const T* __restrict__ hs, const T* __restric
     const int tid = threadIdx.y * 32 + threadIdx.x;
     const long long fo = f * G.fs;
     const bool hasB = G.fB != nullptr;
-    // ---- stage h and q ----
-    for (int e = tid; e < AH_Y * AH_X; e += 256) {
-        const int a = e / AH_X, b = e - a * AH_X;
-        const int j = j0 - 3 + a, i = i0 - 3 + b;
-        S.h[a][b] = (j >= 0 && j < G.ny && i >= 0 && i < G.nx) ? hs[fo + (long long)j * G.nx + i] : T(0);
+    // ---- stage h and q: every load of the thread issued before any store ----
+    {
+        constexpr int NHL = (AH_Y * AH_X + 255) / 256, NQL = (AQ_Y * AQ_X + 255) / 256;
+        T hv[NHL], qv[NQL];
+#pragma unroll
+        for (int k = 0; k < NHL; ++k) {
+            const int e = tid + 256 * k;
+            const int a = e / AH_X, b = e - a * AH_X;
+            const int j = j0 - 3 + a, i = i0 - 3 + b;
+            hv[k] = (e < AH_Y * AH_X && j >= 0 && j < G.ny && i >= 0 && i < G.nx) ? hs[fo + (long long)j * G.nx + i]
+                                                                                  : T(0);
+        }
+#pragma unroll
+        for (int k = 0; k < NQL; ++k) {
+            const int e = tid + 256 * k;
+            const int a = e / AQ_X, b = e - a * AQ_X;
+            const int j = j0 - 4 + a, i = i0 - 4 + b;
+            qv[k] = (e < AQ_Y * AQ_X && j >= 0 && j < G.ny && i >= 0 && i < G.nx) ? qs[fo + (long long)j * G.nx + i]
+                                                                                  : T(0);
+        }
+#pragma unroll
+        for (int k = 0; k < NHL; ++k) {
+            const int e = tid + 256 * k;
+            if (e < AH_Y * AH_X) (&S.h[0][0])[e] = hv[k];
+        }
+#pragma unroll
+        for (int k = 0; k < NQL; ++k) {
+            const int e = tid + 256 * k;
+            if (e < AQ_Y * AQ_X) (&S.q[0][0])[e] = qv[k];
+        }
+        if (hasB) {
+            for (int e = tid; e < AQ_Y * AQ_X; e += 256) {
+                const int a = e / AQ_X, b = e - a * AQ_X;
+                const int j = j0 - 4 + a, i = i0 - 4 + b;
+                const bool in = (j >= 0 && j < G.ny && i >= 0 && i < G.nx);
+                S.qa[a][b] = S.q[a][b] + (in ? ((const T*)G.fB)[(long long)j * G.nx + i] : T(0));
+            }
+        }
     }
-    for (int e = tid; e < AQ_Y * AQ_X; e += 256) {
-        const int a = e / AQ_X, b = e - a * AQ_X;
-        const int j = j0 - 4 + a, i = i0 - 4 + b;
-        const bool in = (j >= 0 && j < G.ny && i >= 0 && i < G.nx);
-        const T qv = in ? qs[fo + (long long)j * G.nx + i] : T(0);
-        S.q[a][b] = qv;
-        if (hasB) S.qa[a][b] = qv + (in ? ((const T*)G.fB)[(long long)j * G.nx + i] : T(0));
+    // ---- per-point inputs of phase A (tendency adjoint, interior flag, beta) ----
+    constexpr int NAL = (AA_Y * AA_X + 255) / 256;
+    T lkv[NAL], bev[NAL];
+    bool m3a[NAL];
+#pragma unroll
+    for (int k = 0; k < NAL; ++k) {
+        const int e = tid + 256 * k;
+        const int a = e / AA_X, b = e - a * AA_X;
+        const int j = j0 - 2 + a, i = i0 - 2 + b;
+        const bool in = e < AA_Y * AA_X && j >= 0 && j < G.ny && i >= 0 && i < G.nx;
+        const long long g2 = (long long)j * G.nx + i;
+        const long long o = fo + g2;
+        T lk = T(0);
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+            if (t < gin.nk && in) lk += gin.c[t] * gin.k[t][o];
+        lkv[k] = lk;
+        m3a[k] = in && G.mask[g2] == 3;
+        bev[k] = (in && G.beta) ? ((const T*)G.beta)[g2] : T(0);
     }
     __syncthreads();
     // ---- phase A on the tile + halo 2 ----
     const T cx = T(G.cx), cy = T(G.cy), cu = T(G.cu), cv = T(G.cv);
-    for (int e = tid; e < AA_Y * AA_X; e += 256) {
-        const int a = e / AA_X, b = e - a * AA_X;
-        const int j = j0 - 2 + a, i = i0 - 2 + b;
-        T lk = T(0), uT = T(0), vT = T(0), aut = T(0), avt = T(0);
-        if (j >= 0 && j < G.ny && i >= 0 && i < G.nx && G.mask[(long long)j * G.nx + i] == 3) {
-            const long long o = fo + (long long)j * G.nx + i;
 #pragma unroll
-            for (int t = 0; t < 4; ++t)
-                if (t < gin.nk) lk += gin.c[t] * gin.k[t][o];
+    for (int k = 0; k < NAL; ++k) {
+        const int e = tid + 256 * k;
+        if (e >= AA_Y * AA_X) break;
+        const int a = e / AA_X, b = e - a * AA_X;
+        T lk = T(0), uT = T(0), vT = T(0), aut = T(0), avt = T(0);
+        if (m3a[k]) {
+            lk = lkv[k];
             const int ha = a + 1, hb = b + 1;     // h-tile index of P
             Vel<T> V;
             V.u0 = guard0(cu * (S.h[ha + 1][hb - 1] + S.h[ha + 1][hb] - S.h[ha - 1][hb] - S.h[ha - 1][hb - 1]));
@@ -325,7 +369,7 @@ k_adj_stage_fused(QGGeom G, int nf, const T* __restrict__ hs, const T* __restric
                 qa.n1 = S.qa[qa_ + 1][qb_]; qa.n2 = S.qa[qa_ + 2][qb_];
                 qa.s1 = S.qa[qa_ - 1][qb_]; qa.s2 = S.qa[qa_ - 2][qb_];
             }
-            const T beta = G.beta ? ((const T*)G.beta)[(long long)j * G.nx + i] : T(0);
+            const T beta = bev[k];
             if (isnan(tendency<T>(G, V, qa, q, beta))) lk = T(0);
             uT = T(0.5) * (V.u0 + V.u1);
             vT = T(0.5) * (V.v0 + V.v1);
@@ -337,11 +381,30 @@ k_adj_stage_fused(QGGeom G, int nf, const T* __restrict__ hs, const T* __restric
         S.lk[a][b] = lk; S.ut[a][b] = uT; S.vt[a][b] = vT; S.aut[a][b] = aut; S.avt[a][b] = avt;
     }
     __syncthreads();
-    // ---- phase B on the tile ----
-    for (int e = tid; e < AT_Y * AT_X; e += 256) {
+    // ---- phase B on the tile (accumulated adjoints and flags loaded first) ----
+    constexpr int NBL = (AT_Y * AT_X + 255) / 256;
+    T accv[NBL];
+    bool m3b[NBL];
+#pragma unroll
+    for (int k = 0; k < NBL; ++k) {
+        const int e = tid + 256 * k;
         const int a = e / AT_X, b = e - a * AT_X;
         const int j = j0 + a, i = i0 + b;
-        if (j >= G.ny || i >= G.nx) continue;
+        const bool in = e < AT_Y * AT_X && j < G.ny && i < G.nx;
+        const long long o = fo + (long long)j * G.nx + i;
+        T sacc = T(0);
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+            if (t < gacc.nk && in) sacc += gacc.k[t][o];
+        accv[k] = sacc;
+        m3b[k] = in && G.mask[(long long)j * G.nx + i] == 3;
+    }
+#pragma unroll
+    for (int k = 0; k < NBL; ++k) {
+        const int e = tid + 256 * k;
+        const int a = e / AT_X, b = e - a * AT_X;
+        const int j = j0 + a, i = i0 + b;
+        if (e >= AT_Y * AT_X || j >= G.ny || i >= G.nx) continue;
         const int A = a + 2, Bc = b + 2;    // phase-A index of X
         auto UP = [&](int da, int db) { const T u = S.ut[A + da][Bc + db]; return S.lk[A + da][Bc + db] * (u < T(0) ? T(0) : u); };
         auto UM = [&](int da, int db) { const T u = S.ut[A + da][Bc + db]; return S.lk[A + da][Bc + db] * (u > T(0) ? T(0) : u); };
@@ -361,12 +424,7 @@ k_adj_stage_fused(QGGeom G, int nf, const T* __restrict__ hs, const T* __restric
                 + T(G.Ky) * (S.lk[A - 1][Bc] + S.lk[A + 1][Bc] - T(2) * lc);
         }
         const long long o = fo + (long long)j * G.nx + i;
-        const bool m3 = G.mask[(long long)j * G.nx + i] == 3;
-        T s = aq;
-#pragma unroll
-        for (int t = 0; t < 4; ++t)
-            if (t < gacc.nk) s += gacc.k[t][o];
-        adq_out[o] = m3 ? s : T(0);
+        adq_out[o] = m3b[k] ? aq + accv[k] : T(0);
         const T hu = T(0.5) * cu, hv = T(0.5) * cv;
         adh_out[o] = hu * (S.aut[A - 1][Bc - 1] + T(2) * S.aut[A - 1][Bc] + S.aut[A - 1][Bc + 1]
                            - S.aut[A + 1][Bc - 1] - T(2) * S.aut[A + 1][Bc] - S.aut[A + 1][Bc + 1])
