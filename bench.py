@@ -53,9 +53,10 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--profile-small", action="store_true",
                     help="short window for profiler captures (not a bench value)")
-    ap.add_argument("--workload", default="qg512", choices=["qg512", "basis1024"],
+    ap.add_argument("--workload", default="qg512", choices=["qg512", "basis1024", "mixed64"],
                     help="qg512: control = initial SSH, 512^2, batched windows (the headline); "
-                         "basis1024: reduced-basis control forcing the SSH, 1024^2, one window")
+                         "basis1024: reduced-basis control forcing the SSH, 1024^2, one window; "
+                         "mixed64: 64 windows of mixed sizes 128^2..768^2, 10 days")
     return ap.parse_args()
 
 
@@ -567,12 +568,175 @@ def gpu_arm_basis(args):
     print(json.dumps(line))
 
 
+# ----------------------------------------------------------------------------
+# Mixed-size batch (64 windows, sides 128..768, 10 days)
+# ----------------------------------------------------------------------------
+M4_SIDES = (128, 192, 256, 384, 512, 768)
+M4_WINDOWS, M4_NSTEP, M4_NOBS, M4_SEED = 64, 960, 5000, 4000
+M4_METRIC = "4D-Var cost+grad evals/sec, QG1.5L 64 windows of sides 128..768, 10-day windows"
+
+
+def setup_mixed(nstep, windows=M4_WINDOWS):
+    import torch
+    from vardyn_gb300.fourdvar import MixedWindows4DVar, QGWindows4DVar
+    from vardyn_gb300.obsop import AlongTrackObs
+    from vardyn_gb300.qg1l import QG1LPlan
+    from vardyn_gb300.synthetic import kminus3_ssh, satellite_tracks
+    rng = np.random.default_rng(M4_SEED)
+    sides = rng.choice(M4_SIDES, size=windows)
+    counts = {int(n): int((sides == n).sum()) for n in M4_SIDES if (sides == n).any()}
+    free, _ = torch.cuda.mem_get_info()
+    # full trajectories where they fit in 60 % of the free memory, else
+    # checkpoints for the largest classes first
+    full = {n: (nstep * 2 + 1) * 2 * c * n * n * 4 for n, c in counts.items()}
+    ckpt = {n: None for n in counts}
+    total = sum(full.values())
+    for n in sorted(counts, reverse=True):
+        if total <= 0.6 * free:
+            break
+        K = int(np.ceil(np.sqrt(nstep)))
+        ckpt[n] = K
+        total -= full[n] - ((nstep // K + 1) * 2 + (2 * 2 * K + 1) * 2) * counts[n] * n * n * 4
+    engines, guesses, win_sets = [], [], []
+    for n, B in counts.items():
+        truths, g0, wins = [], [], []
+        for b in range(B):
+            r = np.random.default_rng(M4_SEED + 1000 * n + b)
+            truths.append(kminus3_ssh(n, n, DX, DX, r, rms=0.1, cutoff_km=50.0))
+            g0.append(kminus3_ssh(n, n, DX, DX, r, rms=0.1, cutoff_km=50.0))
+            x, y, st = satellite_tracks(n, n, DX, DX, nstep, M4_NOBS, r, spacing_km=7.0)
+            wins.append(dict(x_km=x, y_km=y, step=st, err=np.full(x.size, SIGMA), yobs=np.zeros(x.size),
+                             noise=SIGMA * r.standard_normal(x.size)))
+        plan = QG1LPlan(n, n, DX, DX, DT, 1e-4, 2.7, time_scheme="rk2", dtype=torch.float32)
+        obs = AlongTrackObs(wins, n, n, DX, DX, dtype=torch.float32)
+        eng = QGWindows4DVar(plan, torch.zeros(B, n, n, dtype=torch.float32, device="cuda"), nstep, obs,
+                             checkpoint=ckpt[n])
+        eng.cost_and_grad(torch.as_tensor(np.stack(truths), dtype=torch.float32, device="cuda"))
+        torch.cuda.synchronize()
+        hx = obs.misfit[:obs.nobs].double().cpu().numpy() * SIGMA
+        noise = np.concatenate([w["noise"] for w in wins])
+        field = np.concatenate([np.full(w["x_km"].size, b) for b, w in enumerate(wins)])
+        order = np.lexsort((field, np.concatenate([w["step"] for w in wins])))
+        y_sorted = hx + noise[order]
+        obs.d_y.copy_(torch.as_tensor(y_sorted, dtype=torch.float32, device="cuda"))
+        y_orig = np.empty_like(y_sorted)
+        y_orig[order] = y_sorted
+        off = 0
+        for w in wins:                       # per-window data in input order (plain form)
+            w["yobs"] = y_orig[off:off + w["x_km"].size]
+            off += w["x_km"].size
+        engines.append(eng)
+        guesses.append(np.stack(g0))
+        win_sets.append(wins)
+    return MixedWindows4DVar(engines), guesses, counts, ckpt, win_sets
+
+
+def gpu_arm_mixed(args):
+    import torch
+    from vardyn_gb300 import build, _lib
+    from vardyn_gb300.fourdvar import QGWindows4DVar
+    build.build()
+    L = _lib.load()
+    nstep = 64 if args.profile_small else (M4_NSTEP if args.nstep == NSTEP else args.nstep)
+    peaks = {}
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+    from vardyn_gb300.obsop import AlongTrackObs
+    mixed, guesses, counts, ckpt, win_sets = setup_mixed(nstep)
+    xs = [torch.as_tensor(g, dtype=torch.float32, device="cuda") for g in guesses]
+    c0 = L.vd_launch_count()
+    mixed.capture()
+    launches_per_eval = (L.vd_launch_count() - c0) // 2
+    for _ in range(args.warmup):
+        mixed.cost_and_grad(xs)
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    sampler = ClockSampler()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    sampler.start()
+    e0.record(st)
+    for _ in range(args.steps):
+        mixed.cost_and_grad(xs)
+    e1.record(st)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    nwin = sum(counts.values())
+    value = nwin / (ms / 1e3)
+    # e2e: pinned host controls in, J and gradients out, every step
+    hx = [torch.as_tensor(g, dtype=torch.float32).pin_memory() for g in guesses]
+    gh = [torch.empty_like(h).pin_memory() for h in hx]
+    jh = [torch.empty(h.shape[0], dtype=torch.float64).pin_memory() for h in hx]
+    dev = [torch.empty_like(x) for x in xs]
+
+    def e2e_step():
+        for d, h in zip(dev, hx):
+            d.copy_(h, non_blocking=True)
+        out = mixed.cost_and_grad(dev)
+        for (J, G), g, j in zip(out, gh, jh):
+            g.copy_(G, non_blocking=True)
+            j.copy_(J, non_blocking=True)
+    e2e_step()
+    torch.cuda.synchronize()
+    ke = max(2, args.steps // 2)
+    e0.record(st)
+    for _ in range(ke):
+        e2e_step()
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms_e2e = e0.elapsed_time(e1) / ke
+    bytes_io = sum(h.numel() * 4 for h in hx)
+    # plain form: one window of each size alone, no graph, scaled by the counts
+    plain_s = 0.0
+    plain_detail = {}
+    if not args.no_plain:
+        for eng, g, wins in zip(mixed.engines, guesses, win_sets):
+            n = eng.plan.nx
+            o1 = AlongTrackObs(wins[:1], n, n, DX, DX, dtype=torch.float32)
+            e1w = QGWindows4DVar(eng.plan, torch.zeros(1, n, n, dtype=torch.float32, device="cuda"), nstep, o1,
+                                 checkpoint=ckpt[n])
+            x1 = torch.as_tensor(g[:1], dtype=torch.float32, device="cuda")
+            e1w.cost_and_grad(x1)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            e1w.cost_and_grad(x1)
+            torch.cuda.synchronize()
+            dt1 = time.perf_counter() - t0
+            plain_detail[n] = dt1
+            plain_s += dt1 * counts[n]
+            del e1w
+    line = {
+        "metric": M4_METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"QG1.5L, {nwin} windows with sides drawn from {M4_SIDES} (seed {M4_SEED}), "
+                               f"dx=5km dt=900s rk2, {nstep}-step windows, {M4_NOBS} obs each, control h0; "
+                               f"one batched engine per size on its own stream, all captured as one CUDA graph",
+                   "windows_per_side": counts,
+                   "trajectory": {str(n): ("full" if ckpt[n] is None else f"checkpoint every {ckpt[n]} steps")
+                                  for n in counts},
+                   "l2": f"inputs larger than L2: {mixed.memory_bytes() / 1e9:.1f} GB of trajectories"},
+        "e2e": {"value": nwin / (ms_e2e / 1e3), "unit": UNIT, "h2d_bytes_per_step": bytes_io,
+                "d2h_bytes_per_step": bytes_io + 8 * nwin,
+                "path": "MixedWindows4DVar.cost_and_grad (ctypes -> libvardyn_gb300 C ABI), pinned host buffers"},
+        "gpu_launches": int(launches_per_eval * args.steps),
+        "clocks": clocks,
+        "plain_evals_per_s": (nwin / plain_s) if plain_s else None,
+        "batched_over_plain": (value * plain_s / nwin) if plain_s else None,
+        "plain_seconds_per_window": {str(k): v for k, v in plain_detail.items()},
+    }
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         reference_arm(args)
     elif args.workload == "basis1024":
         gpu_arm_basis(args)
+    elif args.workload == "mixed64":
+        gpu_arm_mixed(args)
     else:
         gpu_arm(args)
 

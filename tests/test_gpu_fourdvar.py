@@ -166,3 +166,41 @@ def test_gradient_central_differences_fp64():
     print("central-difference relative errors:", ["%.1e" % e for e in errs])
     assert min(errs) < 1e-7, errs
     assert errs[1] < errs[0] or errs[0] < 1e-7
+
+
+def test_mixed_sizes_match_single_windows_and_graph():
+    """Windows of three grid sizes on concurrent streams (and as one CUDA
+    graph) give each window's single-window cost and gradient."""
+    from vardyn_gb300.fourdvar import MixedWindows4DVar, QGWindows4DVar
+    from vardyn_gb300.obsop import AlongTrackObs
+    from vardyn_gb300.qg1l import QG1LPlan
+    dx, nstep = 5e3, 12
+    engines, xs, singles = [], [], []
+    for n, B, seed in ((40, 2, 1), (56, 1, 2), (72, 2, 3)):
+        wins, truths = make_windows(B, n, n, dx, nstep, 150, seed)
+        rng = np.random.default_rng(seed)
+        for w in wins:
+            w["yobs"] = 0.05 * rng.standard_normal(w["x_km"].size)
+        plan = QG1LPlan(n, n, dx, dx, 900.0, 1e-4, 2.7, time_scheme="rk2", dtype=torch.float64)
+        obs = AlongTrackObs(wins, n, n, dx, dx, dtype=torch.float64)
+        engines.append(QGWindows4DVar(plan, torch.zeros(B, n, n, dtype=torch.float64, device="cuda"), nstep, obs))
+        x = torch.as_tensor(0.5 * np.stack(truths), device="cuda")
+        xs.append(x)
+        for b in range(B):
+            o1 = AlongTrackObs(wins[b:b + 1], n, n, dx, dx, dtype=torch.float64)
+            e1 = QGWindows4DVar(plan, torch.zeros(1, n, n, dtype=torch.float64, device="cuda"), nstep, o1)
+            J1, G1 = e1.cost_and_grad(x[b:b + 1])
+            singles.append((float(J1[0]), G1[0].cpu().numpy().copy()))
+    mixed = MixedWindows4DVar(engines)
+    out = [(J.cpu().numpy().copy(), G.cpu().numpy().copy()) for J, G in mixed.cost_and_grad(xs)]
+    k = 0
+    for J, G in out:
+        for b in range(J.shape[0]):
+            Js, Gs = singles[k]
+            assert abs(J[b] - Js) <= 1e-12 * abs(Js)
+            assert rel(G[b], Gs) < 1e-12
+            k += 1
+    mixed.capture()
+    out2 = [(J.cpu().numpy().copy(), G.cpu().numpy().copy()) for J, G in mixed.cost_and_grad(xs)]
+    for (J, G), (J2, G2) in zip(out, out2):
+        assert np.array_equal(J, J2) and np.array_equal(G, G2)

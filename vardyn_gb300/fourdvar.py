@@ -463,3 +463,67 @@ class QGBasis4DVar:
         torch.cuda.synchronize()
         self.graph = g
         return g
+
+
+class MixedWindows4DVar:
+    """Windows of different grid sizes evaluated together (one batched
+    engine per size class, the layout of the reference's batch of
+    independent assimilation windows, run_assimilation.py:27-349).
+
+    Every engine runs on its own CUDA stream, forked from and joined back to
+    the caller's stream, so the small grids fill the SMs next to the large
+    ones; ``capture`` records the whole set (all streams) as one CUDA graph.
+    ``cost_and_grad(xs)`` takes one control tensor per engine and returns
+    [(J, grad)] in the same order."""
+
+    def __init__(self, engines):
+        self.engines = list(engines)
+        self.streams = [torch.cuda.Stream() for _ in self.engines]
+        self.graph = None
+        self.x_static = None
+
+    def _run(self, xs):
+        cur = torch.cuda.current_stream()
+        start = torch.cuda.Event()
+        start.record(cur)
+        done = []
+        for eng, s, x in zip(self.engines, self.streams, xs):
+            s.wait_event(start)
+            with torch.cuda.stream(s):
+                eng._run(x)
+                e = torch.cuda.Event()
+                e.record(s)
+                done.append(e)
+        for e in done:
+            cur.wait_event(e)
+
+    def cost_and_grad(self, xs):
+        if len(xs) != len(self.engines):
+            raise ValueError("one control per engine")
+        xs = [eng.plan._as_batch(x, "h0") for eng, x in zip(self.engines, xs)]
+        if self.graph is not None:
+            for eng, x, xst in zip(self.engines, xs, self.x_static):
+                eng._copy(x, xst)
+            self.graph.replay()
+        else:
+            self._run(xs)
+        return [(eng.J, eng.grad) for eng in self.engines]
+
+    def capture(self):
+        self.x_static = [torch.zeros(eng.B, eng.plan.ny, eng.plan.nx, dtype=eng.plan.dtype,
+                                     device=eng.plan.device) for eng in self.engines]
+        self._run(self.x_static)           # warm-up: workspaces, kernel attributes
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                self._run(self.x_static)
+        torch.cuda.current_stream().wait_stream(s)
+        torch.cuda.synchronize()
+        self.graph = g
+        return g
+
+    def memory_bytes(self):
+        return sum(eng.memory_bytes() for eng in self.engines)
