@@ -583,3 +583,65 @@ def model_step_adj(qgm, adssh, adFssh, ssh, hb, nstep):
     if adFssh is not None:
         adFssh = adFssh + nstep * qgm.dt / SECONDS_PER_DAY * adssh
     return new_ad, adFssh
+
+
+class QgmSfOracle:
+    """Restatement of ``Qgm_sf`` (jqgm.py:571-1031), the streamfunction form.
+
+    The state is phi = g/f h with f the (possibly varying) Coriolis field
+    (jqgm.py:1004-1005); PV q = lap(phi) - (f0/c)^2 phi (724-741), inversion
+    with lap_dst - (f0/c)^2 (627-631), velocities from phi without the g/f
+    factor (698-719), f0 = mean(f) (606), the bathymetry term f*bathymetry
+    with the f field (819-820), the same beta and mask as Qgm. In phi these
+    are exactly Qgm's equations with g = f = f0 and the bathymetry term
+    scaled by f/f0, so the model part is a ``QgmOracle`` built that way."""
+
+    def __init__(self, dx=None, dy=None, dt=None, SSH=None, c=None, Kdiffus=None,
+                 upwind=3, g=9.81, f=1e-4, time_scheme="Euler", mdt=None,
+                 bathymetry_PV_term=None, **kwargs):
+        ny, nx = np.shape(dx)
+        f_arr = np.broadcast_to(np.asarray(f, dtype="float64"), (ny, nx))
+        self.f0 = float(np.mean(f_arr))
+        self.g = float(g)
+        bathy = None
+        if bathymetry_PV_term is not None:
+            bathy = np.asarray(bathymetry_PV_term, dtype="float64") * (f_arr / self.f0)
+        self.core = QgmOracle(dx=dx, dy=dy, dt=dt, SSH=SSH, c=c, Kdiffus=Kdiffus, upwind=upwind,
+                              g=self.f0, f=(np.asarray(f, dtype="float64") if np.ndim(f) > 0 else self.f0),
+                              time_scheme=time_scheme, bathymetry_PV_term=bathy)
+        self.s = self.g / f_arr                 # h -> phi
+        self.mdt = None if mdt is None else np.asarray(mdt, dtype="float64")
+        self.mask = self.core.mask
+        self.ind0 = self.core.ind0
+
+    def phi2uv(self, phi):
+        return self.core.h2uv(phi)
+
+    def phi2pv(self, phi, phib):
+        return self.core.h2pv(phi, phib)
+
+    def pv2phi(self, q, phib, qb):
+        return self.core.pv2h(q, phib, qb)
+
+    def _in(self, h0, hb):
+        h0 = np.array(h0, dtype="float64")
+        hb = np.array(hb, dtype="float64")
+        if self.mdt is not None:
+            h0 = h0 + self.mdt
+            hb = hb + self.mdt
+        return self.s * h0, self.s * hb
+
+    def step(self, h0, hb, nstep=1):
+        phi0, phib = self._in(h0, hb)
+        h1 = self.core.step(phi0, phib, nstep) / self.s
+        if self.mdt is not None:
+            h1 = h1 - self.mdt
+        return h1
+
+    def step_tgl(self, dh0, h0, hb, nstep=1):
+        phi0, phib = self._in(h0, hb)
+        return self.core.step_tgl(self.s * np.asarray(dh0, dtype="float64"), phi0, phib, nstep) / self.s
+
+    def step_adj(self, adh1, h0, hb, nstep=1):
+        phi0, phib = self._in(h0, hb)
+        return self.s * self.core.step_adj(np.asarray(adh1, dtype="float64") / self.s, phi0, phib, nstep)

@@ -79,6 +79,25 @@ def small_case(ref, out):
     out["dst_out"] = np.asarray(ref.dstI2D(J(x)))
 
 
+def sf_case(ref, out):
+    """Qgm_sf (streamfunction form, jqgm.py:571-1031) on the small case: land,
+    f varying in y (phi = g/f h pointwise), diffusion, bathymetry, hb != 0."""
+    ssh, dx, dy, f = out["small_ssh"], out["small_dx"], out["small_dy"], out["small_f"]
+    bathy, hb = out["small_bathy"], out["small_hb"]
+    for scheme in ("Euler", "rk2", "rk3"):
+        m = ref.Qgm_sf(dx=dx, dy=dy, dt=1200.0, SSH=ssh, c=np.float64(2.7), g=9.81,
+                       f=f, time_scheme=scheme, Kdiffus=50.0, bathymetry_PV_term=bathy)
+        if scheme == "Euler":
+            out["sf_mask"] = np.asarray(m.mask)
+            phi = J(9.81 / f * np.nan_to_num(ssh))
+            phib = J(9.81 / f * hb)
+            q = m.phi2pv(phi, phib)
+            out["sf_phi2pv"] = np.asarray(q)
+            qb = m.phi2pv(phib, phib)
+            out["sf_pv2phi"] = np.asarray(m.pv2phi(q, phib, qb))
+        out[f"sf_step_{scheme}"] = np.asarray(m.step(J(ssh), J(hb), nstep=3))
+
+
 def c1_case(ref, out):
     """128x128, dx=dy=10 km, f0=1e-4, c=2.7, dt=1200 s, 72 steps, hb=0."""
     from vardyn_gb300.synthetic import kminus3_ssh
@@ -99,6 +118,7 @@ def main():
     ref = load_reference(ref_root)
     out = {}
     small_case(ref, out)
+    sf_case(ref, out)
     c1_case(ref, out)
     np.savez_compressed(os.path.join(HERE, "qg1l_golden.npz"), **out)
     print("wrote", sorted(out))

@@ -188,3 +188,40 @@ def test_helmholtz_512_fp32_error():
     assert err_f < 2e-6
     m64 = Qgm(dtype="float64", dx=dx, dy=dx, dt=900.0, c=2.7, f=1e-4, time_scheme="rk2")
     assert rel(m64.pv2h(q, hb, hb * 0), exp) < 1e-12
+
+
+def sf_kw(g, scheme):
+    return dict(dx=g["small_dx"], dy=g["small_dy"], dt=1200.0, SSH=g["small_ssh"], c=2.7, g=9.81,
+                f=g["small_f"], time_scheme=scheme, Kdiffus=50.0, bathymetry_PV_term=g["small_bathy"])
+
+
+@pytest.mark.parametrize("scheme", ["Euler", "rk2", "rk3"])
+def test_streamfunction_form_fp64_matches_reference(golden, scheme):
+    """Drop-in Qgm_sf (streamfunction form, jqgm.py:571-1031) against the
+    reference's own outputs: steps, phi2pv and pv2phi."""
+    from vardyn_gb300.model_qg1l.jqgm import Qgm_sf
+    m = Qgm_sf(dtype="float64", **sf_kw(golden, scheme))
+    out = m.step(golden["small_ssh"], golden["small_hb"], nstep=3)
+    assert rel(out, golden[f"sf_step_{scheme}"]) < 1e-11
+    if scheme == "Euler":
+        f, ssh, hb = golden["small_f"], golden["small_ssh"], golden["small_hb"]
+        phi, phib = 9.81 / f * np.nan_to_num(ssh), 9.81 / f * hb
+        q = m.phi2pv(phi, phib)
+        assert rel(q, golden["sf_phi2pv"]) < 1e-13
+        assert rel(m.pv2phi(q, phib, m.phi2pv(phib, phib)), golden["sf_pv2phi"]) < 1e-12
+
+
+def test_streamfunction_form_tangent_and_adjoint_fp64(golden):
+    from oracle.qg1l import QgmSfOracle
+    from vardyn_gb300.model_qg1l.jqgm import Qgm_sf
+    m = Qgm_sf(dtype="float64", **sf_kw(golden, "rk2"))
+    o = QgmSfOracle(**sf_kw(golden, "rk2"))
+    rng = np.random.default_rng(5)
+    h0 = np.nan_to_num(golden["small_ssh"])
+    hb = golden["small_hb"]
+    dh = rng.standard_normal(h0.shape) * 1e-2
+    ad = rng.standard_normal(h0.shape)
+    tl = m.step_tgl(dh, h0, hb, nstep=3)
+    assert rel(np.nan_to_num(tl), np.nan_to_num(o.step_tgl(dh, h0, hb, 3))) < 1e-10
+    adj = m.step_adj(ad, h0, hb, nstep=3)
+    assert rel(adj, o.step_adj(ad, h0, hb, 3)) < 1e-10

@@ -122,3 +122,72 @@ class Qgm:
         """Adjoint of :meth:`step` w.r.t. h0 (jqgm.py:565-569)."""
         H0, HB = self._mdt_in(self._to_dev(h0), self._to_dev(hb))
         return self._wrap(h0, self.plan.step_adj(self._to_dev(adh0), H0, HB, int(nstep)))
+
+
+class Qgm_sf(Qgm):
+    """Streamfunction form of the model with the constructor of jqgm.py:576.
+
+    The state is phi = g/f h with f the (possibly varying) Coriolis field
+    (jqgm.py:1004-1005); PV q = lap(phi) - (f0/c)^2 phi with f0 = mean(f)
+    (606, 724-741), the inversion lap_dst - (f0/c)^2 (627-631), velocities
+    from phi without the g/f factor (698-719), the bathymetry term f*bathymetry
+    with the f field (819-820), the same beta and mask as Qgm. In phi these
+    are Qgm's equations with g = f = f0 and the bathymetry term scaled by
+    f/f0, so the GPU plan is built that way; the conversions h <-> phi are
+    pointwise scalings (their own adjoints). ``phi2uv``, ``phi2pv``,
+    ``pv2phi`` and ``rhs`` act on phi as in the reference."""
+
+    def __init__(self, dx=None, dy=None, dt=None, SSH=None, c=None, Kdiffus=None, upwind=3,
+                 g=9.81, f=1e-4, time_scheme="Euler", compile=True, mdt=None,
+                 bathymetry_PV_term=None, dtype=None, device=None, **kwargs):
+        ny, nx = np.shape(dx)
+        f_arr = np.broadcast_to(np.asarray(f, dtype=np.float64), (ny, nx))
+        f0 = float(np.mean(f_arr))
+        bathy = None
+        if bathymetry_PV_term is not None:
+            bathy = np.asarray(bathymetry_PV_term, dtype=np.float64) * (f_arr / f0)
+        super().__init__(dx=dx, dy=dy, dt=dt, SSH=SSH, c=c, Kdiffus=Kdiffus, upwind=upwind, g=f0,
+                         f=(np.asarray(f, dtype=np.float64) if np.ndim(f) > 0 else f0),
+                         time_scheme=time_scheme, compile=compile, mdt=None, bathymetry_PV_term=bathy,
+                         dtype=dtype, device=device)
+        self.g = float(g)
+        self.f0 = f0
+        self._s = self._to_dev(self.g / f_arr)          # h -> phi
+        self._sinv = self._to_dev(f_arr / self.g)       # phi -> h
+        self._mdt = None if mdt is None else self._to_dev(mdt)
+        self.phi2uv_jit = self.phi2uv
+        self.phi2pv_jit = self.phi2pv
+        self.pv2phi_jit = self.pv2phi
+
+    def phi2uv(self, phi):
+        return Qgm.h2uv(self, phi)
+
+    def phi2pv(self, phi, phib, c=None):
+        return Qgm.h2pv(self, phi, phib)
+
+    def pv2phi(self, q, phib, qb):
+        return Qgm.pv2h(self, q, phib, qb)
+
+    def _phi_in(self, h0, hb):
+        H0, HB = self._mdt_in(self._to_dev(h0), self._to_dev(hb))
+        return self.plan.scale(H0, self._s), self.plan.scale(HB, self._s)
+
+    def step(self, h0, hb, nstep=1):
+        """nstep steps from SSH h0 (jqgm.py:981-1021)."""
+        P0, PB = self._phi_in(h0, hb)
+        out = self.plan.scale(self.plan.step(P0, PB, int(nstep)), self._sinv)
+        if self._mdt is not None:
+            out = out - self._mdt
+        return self._wrap(h0, out)
+
+    def step_tgl(self, dh0, h0, hb, nstep=1):
+        """Tangent linear of :meth:`step` w.r.t. h0 (jqgm.py:1023-1027)."""
+        P0, PB = self._phi_in(h0, hb)
+        dP = self.plan.scale(self._to_dev(dh0), self._s)
+        return self._wrap(h0, self.plan.scale(self.plan.step_tgl(dP, P0, PB, int(nstep)), self._sinv))
+
+    def step_adj(self, adh0, h0, hb, nstep=1):
+        """Adjoint of :meth:`step` w.r.t. h0 (jqgm.py:1029-1033)."""
+        P0, PB = self._phi_in(h0, hb)
+        adP = self.plan.scale(self._to_dev(adh0), self._sinv)
+        return self._wrap(h0, self.plan.scale(self.plan.step_adj(adP, P0, PB, int(nstep)), self._s))

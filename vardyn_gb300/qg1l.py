@@ -241,6 +241,16 @@ class QG1LPlan:
         _lib.call("vd_qg1l_finalize", self._h, batch, _ptr(h), _ptr(hb), _ptr(forcing),
                   float(coef), _ptr(out), _stream())
 
+    def scale(self, x, d):
+        """out[b] = d * x[b] elementwise (d: [ny, nx] on the device)."""
+        x = self._as_batch(x, "x")
+        d = self._as_batch(d, "d")
+        out = torch.empty_like(x)
+        _lib.call("vd_diag_axpy", _lib.VD_F64 if self.dtype == torch.float64 else _lib.VD_F32,
+                  ctypes.c_longlong(x.numel()), ctypes.c_longlong(self.ny * self.nx), _ptr(d), _ptr(x), None,
+                  _ptr(out), _stream())
+        return out
+
     def traj_view(self, traj, batch, nstep):
         """[nstep*nstage+1, 2, batch, ny, nx] view of a trajectory buffer."""
         return traj.view(nstep * self.nstage + 1, 2, batch, self.ny, self.nx)
