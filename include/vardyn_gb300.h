@@ -314,6 +314,53 @@ vd_status vd_basis_project_T(const vd_basis_plan* plan, int batch, int k, const 
                              void* adX, long long ldX, void* workspace,
                              size_t workspace_bytes, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Wave-packet reduced basis (Basis_bm / Basis_bm_jax, mapping/src/basis.py
+ * 472-1168) on a rectilinear grid given as for vd_basis_plan_create.
+ * Frequencies ff between 1/lmax and 1/lmin, directions theta, per frequency
+ * a lattice of centres and atoms sqrt(2) w(xx/DX) w(yy/DX) {cos, sin}(k.x);
+ * the control vector holds, per frequency, [time centre][space centre]
+ * [theta][cos, sin] coefficients (basis.py:775-781).
+ * ---------------------------------------------------------------------- */
+typedef struct vd_bm_plan vd_bm_plan;
+
+typedef struct vd_bm_params {
+    double npsp, facpsp;        /* wavelet extension / frequency step (basis.py:480-481) */
+    double lmin, lmax;          /* wavelength range [km] */
+    double facns, facnlt;       /* space / time lattice densities */
+    double tdecmin, tdecmax;    /* decorrelation time bounds [days] */
+    double factdec, sloptdec;   /* decorrelation time law (basis.py:651-656) */
+    double Qmax, slopQ;         /* prior std law (basis.py:675-683) */
+    double lmeso, tmeso;        /* mesoscale wavelength [km] and time [days] */
+    int norm_time;              /* divide the time window by its integral */
+    int flux;                   /* time window = mywindow_flux */
+    double time_ref;            /* days from 1950-01-01 to the window start
+                                   (delta_time_ref, basis.py:527) */
+} vd_bm_params;
+
+vd_status vd_bm_plan_create(vd_bm_plan** out, const vd_basis_grid* grid, const vd_bm_params* params);
+vd_status vd_bm_plan_destroy(vd_bm_plan* plan);
+long long vd_bm_nbasis(const vd_bm_plan* plan);
+/* Number of frequencies and directions; theta_host [ntheta] if non-NULL. */
+vd_status vd_bm_shape(const vd_bm_plan* plan, int* nf, int* ntheta, double* theta_host);
+/* Per frequency: ff [1/km], tdec [days], offset of its block in X, number of
+ * time centres and of space centres (any pointer may be NULL). */
+vd_status vd_bm_frequency(const vd_bm_plan* plan, int iff, double* ff, double* tdec,
+                          long long* offset, int* ntime_centres, int* nspace_centres);
+vd_status vd_bm_lattice(const vd_bm_plan* plan, int iff, double* enst_host,
+                        double* enslat_host, double* enslon_host);
+vd_status vd_bm_q(const vd_bm_plan* plan, double* q_host);
+vd_status vd_bm_time_weights(const vd_bm_plan* plan, int k, int iff, int* count,
+                             int* it_host, double* weight_host);
+size_t vd_bm_workspace_bytes(const vd_bm_plan* plan, int batch);
+/* phi[b] = (accumulate ? phi[b] : 0) + G(t_k) X[b]; adX[b] += G(t_k)^T adphi[b]. */
+vd_status vd_bm_project(const vd_bm_plan* plan, int batch, int k, const void* X, long long ldX,
+                        void* phi, int accumulate, void* workspace, size_t workspace_bytes,
+                        void* stream);
+vd_status vd_bm_project_T(const vd_bm_plan* plan, int batch, int k, const void* adphi,
+                          void* adX, long long ldX, void* workspace, size_t workspace_bytes,
+                          void* stream);
+
 /* Version / build information string. */
 const char* vd_version(void);
 /* Number of kernels this library has launched in the process so far (also

@@ -1,11 +1,13 @@
-"""Oracle (test infrastructure only): restatement of the Gaussian space-time
-reduced basis of the reference in float64 NumPy/SciPy, in the reference's
-own sparse form (a CSC space matrix and a time-weight vector per basis time).
+"""Oracle (test infrastructure only): restatement of the reduced bases of the
+reference (Gaussian space-time and wave-packet) in float64 NumPy/SciPy, in
+the reference's own sparse form (CSC space matrices and time weights per
+basis time).
 
   - Basis_gauss3d            mapping/src/basis.py:1170-1555
     (lattice 1291-1324, Q 1359, space 1393-1421, time 1423-1446,
      operg 1489-1524, operg_transpose 1526-1555, norm_fact 1278-1283)
   - Basis_multi              mapping/src/basis.py:4039-4135
+  - Basis_bm / Basis_bm_jax  mapping/src/basis.py:472-1168 (wave packets)
   - mywindow / mywindow_flux mapping/src/basis.py:4138-4144
 
 Two coordinate forms:
@@ -201,3 +203,179 @@ class MultiOracle:
 
     def operg_transpose(self, t, adphi):
         return np.concatenate([c.operg_transpose(t, adphi) for c in self.comps])
+
+
+class BMOracle:
+    """Wave-packet basis of the reference (Basis_bm / Basis_bm_jax,
+    mapping/src/basis.py:472-1168), in the reference's sparse form.
+
+    Frequencies ff (pseudo-wavelengths between lmin and lmax, 577-583),
+    directions theta (587), per frequency a lattice of centres spaced
+    DX/facns (611-649, centres whose footprint of radius 1/ff is fully
+    masked are dropped), atoms sqrt(2) cos^2(pi xx/2DX) cos^2(pi yy/2DX)
+    {cos, sin}(kx xx + ky yy) (736-772), per-frequency time centres spaced
+    tdec/facnlt from -time_ref mod tdec (652-667), time weights of the JAX
+    form (|dt| <= tdec, 1026-1035), prior std Q (671-690). Coefficients of
+    one frequency are ordered [time centre][space centre][theta][cos, sin].
+    geo=False: planar x/y in km (km2deg = 1, cos(lat) = 1)."""
+
+    def __init__(self, lon, lat, npsp=3.5, facpsp=1.5, lmin=80., lmax=900., facns=1., facnlt=2.,
+                 tdecmin=2., tdecmax=20., factdec=1., sloptdec=-1.28, Qmax=1e-3, slopQ=-2., lmeso=300.,
+                 tmeso=20., norm_time=True, flux=False, time_ref=0.0, mask=None, geo=False):
+        lon = np.asarray(lon, float)
+        lat = np.asarray(lat, float)
+        self.shape_phys = lon.shape
+        self.lon1d, self.lat1d = lon.ravel(), lat.ravel()
+        self.lon_min, self.lon_max = lon.min(), lon.max()
+        self.lat_min, self.lat_max = lat.min(), lat.max()
+        self.npsp, self.facpsp, self.lmin, self.lmax = float(npsp), float(facpsp), float(lmin), float(lmax)
+        self.facns, self.facnlt = float(facns), float(facnlt)
+        self.tdecmin, self.tdecmax, self.factdec, self.sloptdec = float(tdecmin), float(tdecmax), float(factdec), \
+            float(sloptdec)
+        self.Qmax, self.slopQ, self.lmeso, self.tmeso = float(Qmax), float(slopQ), float(lmeso), float(tmeso)
+        self.norm_time = norm_time
+        self.window = mywindow_flux if flux else mywindow
+        self.time_ref = float(time_ref)
+        self.geo = geo
+        self.km2deg = KM2DEG if geo else 1.0
+        self.mask1d = None
+        if mask is not None and np.any(mask):
+            self.mask1d = np.asarray(mask, bool).ravel()
+
+    def _cos(self, lat_deg):
+        return np.cos(lat_deg * np.pi / 180.) if self.geo else 1.0
+
+    def set_basis(self, time):
+        time = np.asarray(time, float)
+        TIME_MIN, TIME_MAX = time.min(), time.max()
+        LON_MIN, LON_MAX, LAT_MIN, LAT_MAX = self.lon_min, self.lon_max, self.lat_min, self.lat_max
+        k2 = self.km2deg
+        logff = np.arange(np.log(1. / self.lmin), np.log(1. / self.lmax) - np.log(1 + self.facpsp / self.npsp),
+                          -np.log(1 + self.facpsp / self.npsp))[::-1]
+        ff = np.exp(logff)
+        dff = ff[1:] - ff[:-1]
+        theta = np.linspace(0, np.pi, int(np.pi * ff[0] / dff[0] * self.facpsp))[:-1]
+        ntheta, nf = len(theta), len(ff)
+        deltat = TIME_MAX - TIME_MIN
+        DX = 1. / ff * self.npsp * 0.5
+        DXG = DX / self.facns
+        ENSLON, ENSLAT, enst, tdec, norm_fact = [], [], [], [], []
+        NP = np.zeros(nf, dtype=int)
+        for iff in range(nf):
+            el, ea = [], []
+            dlat = DXG[iff] * k2
+            lat0 = LAT_MIN - LAT_MIN % dlat - DX[iff] * k2
+            lat1 = LAT_MAX + DX[iff] * k2 * 1.5
+            for la in np.arange(lat0, lat1, dlat):
+                cl = self._cos(la)
+                dlon = DXG[iff] / cl * k2
+                lon0 = LON_MIN - LON_MIN % dlon - DX[iff] / cl * k2
+                lon1 = LON_MAX + DX[iff] / cl * k2 * 1.5
+                for lo in np.arange(lon0, lon1, dlon):
+                    if self.mask1d is not None:
+                        ind = np.where((np.abs((self.lon1d - lo) / k2 * self._cos(la)) <= 1. / ff[iff]) &
+                                       (np.abs((self.lat1d - la) / k2) <= 1. / ff[iff]))[0]
+                        if np.all(self.mask1d[ind]):
+                            continue
+                    el.append(lo)
+                    ea.append(la)
+            ENSLON.append(np.array(el))
+            ENSLAT.append(np.array(ea))
+            NP[iff] = len(el)
+            td = self.tmeso * self.lmeso ** self.sloptdec * ff[iff] ** self.sloptdec
+            td *= self.factdec
+            td = min(max(td, self.tdecmin), self.tdecmax)
+            tdec.append(td)
+            t0 = -self.time_ref % td
+            enst.append(np.arange(t0 - td / self.facnlt, deltat + td / self.facnlt, td / self.facnlt))
+            tt = np.linspace(-td, td)
+            tmp = np.zeros_like(tt)
+            for i in range(tt.size - 1):
+                tmp[i + 1] = tmp[i] + self.window(tt[i] / td) * (tt[i + 1] - tt[i])
+            norm_fact.append(tmp.max())
+        Q, bounds, iw = [], [], 0
+        for iff in range(nf):
+            bounds.append(iw)
+            n = 2 * len(enst[iff]) * ntheta * NP[iff]
+            if NP[iff] > 0:
+                if 1 / ff[iff] > self.lmeso:
+                    Q.append(self.Qmax / self.facns * np.ones(n))
+                else:
+                    Q.append(self.Qmax / self.facns * self.lmeso ** self.slopQ * ff[iff] ** self.slopQ * np.ones(n))
+                iw += n
+        bounds.append(iw)
+        self.ff, self.theta, self.ntheta, self.nf, self.DX = ff, theta, ntheta, nf, DX
+        self.ENSLON, self.ENSLAT, self.NP, self.enst, self.tdec, self.norm_fact = ENSLON, ENSLAT, NP, enst, tdec, \
+            norm_fact
+        self.k = 2 * np.pi * ff
+        self.bounds = bounds
+        self.nbasis = iw
+        self.Q = np.concatenate(Q) if Q else np.zeros(0)
+        self.Gx = [self._space(iff) for iff in range(nf)]
+        self.times = time
+        return np.zeros_like(self.Q), self.Q
+
+    def _space(self, iff):
+        k2 = self.km2deg
+        cols_data, cols_ind = [], []
+        for P in range(self.NP[iff]):
+            lo, la = self.ENSLON[iff][P], self.ENSLAT[iff][P]
+            cl = self._cos(la)
+            xall = (self.lon1d - lo) / k2 * cl
+            yall = (self.lat1d - la) / k2
+            ind = np.where((np.abs(xall) <= self.DX[iff]) & (np.abs(yall) <= self.DX[iff]))[0]
+            xx, yy = xall[ind], yall[ind]
+            if self.mask1d is not None:
+                keep = ~self.mask1d[ind]
+                ind, xx, yy = ind[keep], xx[keep], yy[keep]
+            facs = mywindow(xx / self.DX[iff]) * mywindow(yy / self.DX[iff])
+            for th in self.theta:
+                kx, ky = self.k[iff] * np.cos(th), self.k[iff] * np.sin(th)
+                cols_data.append(np.sqrt(2) * facs * np.cos(kx * xx + ky * yy))
+                cols_ind.append(ind)
+                cols_data.append(np.sqrt(2) * facs * np.sin(kx * xx + ky * yy))
+                cols_ind.append(ind)
+        sizes = [len(c) for c in cols_ind]
+        indptr = np.zeros(len(sizes) + 1, dtype=np.int64)
+        indptr[1:] = np.cumsum(sizes)
+        data = np.concatenate(cols_data) if cols_data else np.zeros(0)
+        indices = np.concatenate(cols_ind) if cols_ind else np.zeros(0, dtype=np.int64)
+        return csc_matrix((data, indices, indptr), shape=(self.lon1d.size, len(sizes)))
+
+    def time_weights(self, iff, t):
+        """[(it, fact)] of frequency iff at time t (JAX form, basis.py:1026-1035)."""
+        out = []
+        td = self.tdec[iff]
+        for it, tc in enumerate(self.enst[iff]):
+            dt = t - tc
+            if not (abs(dt) > td or np.isnan(tc)):
+                fact = self.window(dt / td)
+                if self.norm_time:
+                    fact /= self.norm_fact[iff]
+                out.append((it, fact))
+        return out
+
+    def operg(self, t, X):
+        phi = np.zeros(self.lon1d.size)
+        for iff in range(self.nf):
+            nx_ = 2 * self.ntheta * self.NP[iff]
+            Xf = X[self.bounds[iff]:self.bounds[iff + 1]].reshape(len(self.enst[iff]), nx_) if nx_ else None
+            if nx_ == 0:
+                continue
+            z = np.zeros(nx_)
+            for it, fct in self.time_weights(iff, t):
+                z += fct * Xf[it]
+            phi += self.Gx[iff].dot(z)
+        return phi.reshape(self.shape_phys)
+
+    def operg_transpose(self, t, adphi):
+        adX = np.zeros(self.nbasis)
+        for iff in range(self.nf):
+            nx_ = 2 * self.ntheta * self.NP[iff]
+            if nx_ == 0:
+                continue
+            ad = self.Gx[iff].T.dot(np.asarray(adphi).ravel())
+            blk = adX[self.bounds[iff]:self.bounds[iff + 1]].reshape(len(self.enst[iff]), nx_)
+            for it, fct in self.time_weights(iff, t):
+                blk[it] += fct * ad
+        return adX

@@ -167,3 +167,95 @@ def test_reference_facing_classes():
     adX = bm.operg_transpose(4.0, ad)
     assert rel(adX, om.operg_transpose(4.0, ad0)) < 1e-13
     assert np.all(ad["ssh"] == 0)
+
+
+BM_KW = dict(lmin=60, lmax=300, npsp=3.5, facpsp=1.5, lmeso=150, tmeso=10, time_ref=3.3, facns=1.2, facnlt=2.0)
+
+
+@pytest.mark.parametrize("geo", [False, True])
+def test_bm_project_and_transpose_fp64_match_oracle(geo):
+    from oracle.basis import BMOracle
+    from vardyn_gb300.basis import BMParams, BMPlan
+    if geo:
+        xc, yc = -60 + np.arange(110) * 0.05, 25 + np.arange(95) * 0.05
+    else:
+        xc, yc = np.arange(100) * 5.0, 2.0 + np.arange(90) * 5.0
+    mask = np.zeros((yc.size, xc.size), bool)
+    mask[:20, :30] = True
+    time = np.arange(0, 10.01, 0.25)
+    plan = BMPlan(xc, yc, time, BMParams(**BM_KW), land=mask, geographic=geo, dtype=torch.float64)
+    lon, lat = np.meshgrid(xc, yc)
+    o = BMOracle(lon, lat, mask=mask, geo=geo, **BM_KW)
+    o.set_basis(time)
+    rng = np.random.default_rng(11)
+    B = 2
+    X = rng.standard_normal((B, plan.nbasis))
+    Xd = torch.as_tensor(X, device="cuda")
+    for k in (0, 13, 40):
+        phi = plan.project(k, Xd).cpu().numpy()
+        for b in range(B):
+            assert rel(phi[b], o.operg(time[k], X[b])) < 1e-12
+    A = rng.standard_normal((B, yc.size, xc.size))
+    adX = torch.zeros(B, plan.nbasis, dtype=torch.float64, device="cuda")
+    for k in (5, 22):
+        plan.project_T(k, torch.as_tensor(A, device="cuda"), adX)
+    got = adX.cpu().numpy()
+    for b in range(B):
+        ref = o.operg_transpose(time[5], A[b]) + o.operg_transpose(time[22], A[b])
+        assert rel(got[b], ref) < 1e-12
+
+
+def test_bm_fp32_and_dot_product():
+    from vardyn_gb300.basis import BMParams, BMPlan
+    xc, yc = np.arange(120) * 4.0, np.arange(100) * 4.0
+    time = np.arange(0, 8.01, 0.5)
+    p64 = BMPlan(xc, yc, time, BMParams(**BM_KW), dtype=torch.float64)
+    p32 = BMPlan(xc, yc, time, BMParams(**BM_KW), dtype=torch.float32)
+    rng = np.random.default_rng(12)
+    X = torch.as_tensor(rng.standard_normal((1, p64.nbasis)), device="cuda")
+    A = torch.as_tensor(rng.standard_normal((1, yc.size, xc.size)), device="cuda")
+    phi = p64.project(7, X)
+    adX = torch.zeros_like(X)
+    p64.project_T(7, A, adX)
+    lhs, rhs = float((phi * A).sum()), float((X * adX).sum())
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+    phi32 = p32.project(7, X.float())
+    assert rel(phi32.double().cpu().numpy(), phi.cpu().numpy()) < 3e-6
+
+
+def test_bm_reference_facing_class():
+    """Basis_bm(config, State): the time reference comes from
+    config.EXP.init_date (basis.py:527); State-dict semantics as operg /
+    operg_transpose of the reference."""
+    import datetime
+    from oracle.basis import BMOracle
+    from vardyn_gb300.basis import Basis_bm
+    ny, nx = 60, 70
+    lon, lat = np.meshgrid(-40 + np.arange(nx) * 0.05, 35 + np.arange(ny) * 0.05)
+    mask = np.zeros((ny, nx), bool)
+    mask[5:12, 10:25] = True
+    State = types.SimpleNamespace(lon=lon, lat=lat, mask=mask, ny=ny, nx=nx)
+    kw = dict(BM_KW)
+    kw.pop("time_ref")
+    init = datetime.datetime(2012, 10, 3, 6)
+    tref = (init - datetime.datetime(1950, 1, 1)).total_seconds() / 86400
+    cfgB = types.SimpleNamespace(name_mod_var="ssh", compute_velocities=False, file_depth=None, norm_time=True,
+                                 flux=False, tdecmin=2.0, tdecmax=20.0, factdec=1.0, sloptdec=-1.28, Qmax=1e-3,
+                                 slopQ=-2.0, **kw)
+    config = types.SimpleNamespace(BASIS=cfgB, EXP=types.SimpleNamespace(init_date=init))
+    b = Basis_bm(config, State, dtype=torch.float64)
+    time = np.arange(0, 6.01, 0.5)
+    Xb, Q = b.set_basis(time, return_q=True)
+    o = BMOracle(lon, lat, mask=mask, geo=True, time_ref=tref, **kw)
+    _, Qo = o.set_basis(time)
+    assert np.array_equal(Q, Qo)
+    rng = np.random.default_rng(13)
+    X = rng.standard_normal(b.nbasis)
+    params = {"ssh": np.zeros((ny, nx))}
+    b.operg(3.0, X, State=params)
+    assert rel(params["ssh"], o.operg(3.0, X)) < 1e-12
+    ad = {"ssh": rng.standard_normal((ny, nx))}
+    ad0 = ad["ssh"].copy()
+    adX = b.operg_transpose(3.0, ad)
+    assert rel(adX, o.operg_transpose(3.0, ad0)) < 1e-12
+    assert np.all(ad["ssh"] == 0)

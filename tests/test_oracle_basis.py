@@ -149,3 +149,58 @@ def test_oracle_basis_4dvar_gradient_central_differences():
         Jm = cost_and_grad_basis(ref, basis, tb, X0 - eps * d, Xb, Q, h0, hb, nstep, nck, obs)[0]
         errs.append(abs((Jp - Jm) / (2 * eps) - gd) / abs(gd))
     assert min(errs) < 1e-7, errs
+
+
+@pytest.mark.parametrize("geo,land", [(False, False), (True, False), (False, True), (True, True)])
+def test_library_bm_tables_match_oracle(geo, land):
+    """Wave-packet basis: frequencies, directions, lattices (with masked
+    centres dropped), time centres, Q and time weights of the C++ builder
+    equal the oracle's restatement of Basis_bm exactly."""
+    from vardyn_gb300 import build
+    from vardyn_gb300.basis import BMParams, BMPlan
+    from oracle.basis import BMOracle
+    build.build()
+    if geo:
+        xc, yc = -60 + np.arange(110) * 0.05, 25 + np.arange(95) * 0.05
+    else:
+        xc, yc = np.arange(100) * 5.0, 2.0 + np.arange(90) * 5.0
+    mask = None
+    if land:
+        mask = np.zeros((yc.size, xc.size), bool)
+        mask[:30, :40] = True
+    time = np.arange(0, 10.01, 0.25)
+    kw = dict(lmin=60, lmax=300, npsp=3.5, facpsp=1.5, lmeso=150, tmeso=10, time_ref=3.3, facns=1.2, facnlt=2.0)
+    plan = BMPlan(xc, yc, time, BMParams(**kw), land=mask, geographic=geo, host_only=True)
+    lon, lat = np.meshgrid(xc, yc)
+    o = BMOracle(lon, lat, mask=mask, geo=geo, **kw)
+    _, Q = o.set_basis(time)
+    assert plan.nbasis == o.nbasis and plan.nf == o.nf and plan.ntheta == o.ntheta
+    assert np.array_equal(plan.theta, o.theta)
+    assert np.array_equal(plan.q(), Q)
+    for iff in range(o.nf):
+        ff, td, off, nt, ns = plan.frequency(iff)
+        assert ff == o.ff[iff] and td == o.tdec[iff] and off == o.bounds[iff]
+        enst, la, lo = plan.lattice(iff)
+        assert np.array_equal(enst, o.enst[iff])
+        assert np.array_equal(la, o.ENSLAT[iff]) and np.array_equal(lo, o.ENSLON[iff])
+        for k in range(0, time.size, 5):
+            got, want = plan.time_weights(k, iff), o.time_weights(iff, time[k])
+            assert [i for i, _ in got] == [i for i, _ in want]
+            assert np.allclose([w for _, w in got], [w for _, w in want], rtol=0, atol=1e-15)
+
+
+def test_bm_oracle_transpose_identity():
+    from oracle.basis import BMOracle
+    lon, lat = np.meshgrid(np.arange(70) * 5.0, np.arange(60) * 5.0)
+    mask = np.zeros(lon.shape, bool)
+    mask[10:20, 30:45] = True
+    o = BMOracle(lon, lat, lmin=60, lmax=250, lmeso=150, tmeso=10, mask=mask)
+    o.set_basis(np.arange(0, 6.01, 0.5))
+    rng = np.random.default_rng(2)
+    X = rng.standard_normal(o.nbasis)
+    a = rng.standard_normal(lon.shape)
+    for t in (0.0, 2.5, 6.0):
+        phi = o.operg(t, X)
+        assert np.all(phi[mask] == 0)
+        lhs, rhs = np.sum(phi * a), np.dot(X, o.operg_transpose(t, a))
+        assert abs(lhs - rhs) <= 1e-12 * max(abs(lhs), 1.0)

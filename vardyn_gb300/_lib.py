@@ -58,6 +58,20 @@ class VdGauss3dParams(ctypes.Structure):
     ]
 
 
+class VdBmParams(ctypes.Structure):
+    _fields_ = [
+        ("npsp", ctypes.c_double), ("facpsp", ctypes.c_double),
+        ("lmin", ctypes.c_double), ("lmax", ctypes.c_double),
+        ("facns", ctypes.c_double), ("facnlt", ctypes.c_double),
+        ("tdecmin", ctypes.c_double), ("tdecmax", ctypes.c_double),
+        ("factdec", ctypes.c_double), ("sloptdec", ctypes.c_double),
+        ("Qmax", ctypes.c_double), ("slopQ", ctypes.c_double),
+        ("lmeso", ctypes.c_double), ("tmeso", ctypes.c_double),
+        ("norm_time", ctypes.c_int), ("flux", ctypes.c_int),
+        ("time_ref", ctypes.c_double),
+    ]
+
+
 P = ctypes.c_void_p
 I = ctypes.c_int
 LL = ctypes.c_longlong
@@ -113,6 +127,18 @@ SIGNATURES = {
     "vd_basis_project": (I, [P, I, I, P, LL, P, I, P, SZ, P]),
     "vd_basis_project_T": (I, [P, I, I, P, P, LL, P, SZ, P]),
     "vd_fill": (I, [I, LL, D, P, P]),
+    "vd_bm_plan_create": (I, [ctypes.POINTER(P), ctypes.POINTER(VdBasisGrid), ctypes.POINTER(VdBmParams)]),
+    "vd_bm_plan_destroy": (I, [P]),
+    "vd_bm_nbasis": (LL, [P]),
+    "vd_bm_shape": (I, [P, ctypes.POINTER(I), ctypes.POINTER(I), P]),
+    "vd_bm_frequency": (I, [P, I, ctypes.POINTER(D), ctypes.POINTER(D), ctypes.POINTER(LL), ctypes.POINTER(I),
+                            ctypes.POINTER(I)]),
+    "vd_bm_lattice": (I, [P, I, P, P, P]),
+    "vd_bm_q": (I, [P, P]),
+    "vd_bm_time_weights": (I, [P, I, I, ctypes.POINTER(I), P, P]),
+    "vd_bm_workspace_bytes": (SZ, [P, I]),
+    "vd_bm_project": (I, [P, I, I, P, LL, P, I, P, SZ, P]),
+    "vd_bm_project_T": (I, [P, I, I, P, P, LL, P, SZ, P]),
 }
 
 _lib = None

@@ -52,21 +52,17 @@ class Gauss3dParams:
                                     float(self.time_spinup) if self.time_spinup is not None else 0.0)
 
 
-class BasisPlan:
-    """One or more Gaussian components on a rectilinear grid.
+class _SeparablePlan:
+    """Shared plumbing of the basis plans: grid description, workspace, batched
+    G / G^T calls on torch's current stream."""
 
-    xc [nx], yc [ny]: column / row coordinates (km, or lon/lat in degrees when
-    ``geographic``); time: the basis times in days (set_basis's argument);
-    land: bool [ny, nx] (True = excluded) or None. ``host_only`` builds the
-    tables without a GPU (queries only)."""
+    _prefix = None
 
-    def __init__(self, xc, yc, time, comps, land=None, geographic=False, dtype=torch.float32,
-                 device=None, host_only=False):
+    def _grid(self, xc, yc, time, land, geographic, dtype, device, host_only):
         self.xc = np.ascontiguousarray(xc, dtype=np.float64)
         self.yc = np.ascontiguousarray(yc, dtype=np.float64)
         self.ny, self.nx = self.yc.size, self.xc.size
         self.times = np.ascontiguousarray(np.atleast_1d(time), dtype=np.float64)
-        self.comps = list(comps)
         self.dtype = dtype
         self.host_only = host_only
         self.device = None
@@ -75,6 +71,7 @@ class BasisPlan:
                 raise RuntimeError("vardyn_gb300 needs a CUDA device (no CPU path)")
             dev = torch.device(device or "cuda")
             self.device = torch.device("cuda", dev.index if dev.index is not None else torch.cuda.current_device())
+            torch.cuda.set_device(self.device)
         self._land = None
         if land is not None:
             land = np.asarray(land, dtype=bool)
@@ -82,61 +79,22 @@ class BasisPlan:
                 raise ValueError("land must be [ny, nx]")
             self._land = np.ascontiguousarray(land.astype(np.int8))
         dptr = ctypes.POINTER(ctypes.c_double)
-        grid = _lib.VdBasisGrid(
+        self._gridc = _lib.VdBasisGrid(
             self.ny, self.nx, _lib.VD_F64 if dtype == torch.float64 else _lib.VD_F32, int(geographic),
             self.xc.ctypes.data_as(dptr), self.yc.ctypes.data_as(dptr),
             self._land.ctypes.data_as(ctypes.POINTER(ctypes.c_int8)) if self._land is not None else None,
             self.times.size, self.times.ctypes.data_as(dptr), int(host_only))
-        params = (_lib.VdGauss3dParams * len(self.comps))(*[c.to_c() for c in self.comps])
         self.lib = _lib.load()
-        h = ctypes.c_void_p()
-        if not host_only:
-            torch.cuda.set_device(self.device)
-        _lib.check(self.lib.vd_basis_plan_create(ctypes.byref(h), ctypes.byref(grid), len(self.comps), params),
-                   "vd_basis_plan_create")
-        self._h = h
-        self.nbasis = int(self.lib.vd_basis_nbasis(h))
         self._ws = None
 
     def __del__(self):
         h = getattr(self, "_h", None)
         if h is not None and h.value:
             try:
-                self.lib.vd_basis_plan_destroy(h)
+                getattr(self.lib, self._prefix + "_plan_destroy")(h)
             except Exception:
                 pass
             self._h = None
-
-    # ------------------------------------------------------------ queries
-    def component(self, c):
-        off, nt, ns = ctypes.c_longlong(), ctypes.c_int(), ctypes.c_int()
-        _lib.check(self.lib.vd_basis_component(self._h, c, ctypes.byref(off), ctypes.byref(nt),
-                                               ctypes.byref(ns)), "vd_basis_component")
-        return off.value, nt.value, ns.value
-
-    def lattice(self, c):
-        """(ENST, ENSLAT, ENSLON) of component c."""
-        _, nt, ns = self.component(c)
-        enst, lat, lon = np.zeros(nt), np.zeros(ns), np.zeros(ns)
-        _lib.check(self.lib.vd_basis_lattice(self._h, c, enst.ctypes.data, lat.ctypes.data, lon.ctypes.data),
-                   "vd_basis_lattice")
-        return enst, lat, lon
-
-    def q(self):
-        """Prior standard deviation of every coefficient (float64 [nbasis])."""
-        q = np.zeros(self.nbasis)
-        _lib.check(self.lib.vd_basis_q(self._h, q.ctypes.data), "vd_basis_q")
-        return q
-
-    def time_weights(self, k, c):
-        n = ctypes.c_int()
-        _lib.check(self.lib.vd_basis_time_weights(self._h, k, c, ctypes.byref(n), None, None),
-                   "vd_basis_time_weights")
-        it = np.zeros(max(n.value, 1), dtype=np.int32)
-        w = np.zeros(max(n.value, 1))
-        _lib.check(self.lib.vd_basis_time_weights(self._h, k, c, ctypes.byref(n), it.ctypes.data,
-                                                  w.ctypes.data), "vd_basis_time_weights")
-        return list(zip(it[:n.value].tolist(), w[:n.value].tolist()))
 
     def time_index(self, t):
         """Index of basis time t (exact match, as basis.py:1636-1640)."""
@@ -145,9 +103,8 @@ class BasisPlan:
             raise KeyError(f"time {t} is not a basis time")
         return int(k[0])
 
-    # ------------------------------------------------------------ compute
     def workspace(self, batch):
-        n = int(self.lib.vd_basis_workspace_bytes(self._h, batch))
+        n = int(getattr(self.lib, self._prefix + "_workspace_bytes")(self._h, batch))
         if self._ws is None or self._ws.numel() < n:
             self._ws = torch.empty(max(n, 256), dtype=torch.uint8, device=self.device)
         return self._ws
@@ -169,9 +126,9 @@ class BasisPlan:
             out = torch.empty(B, self.ny, self.nx, dtype=self.dtype, device=self.device)
             accumulate = False
         ws = self.workspace(B)
-        _lib.check(self.lib.vd_basis_project(self._h, B, int(k), _ptr(X), X.stride(0), _ptr(out),
-                                             int(bool(accumulate)), _ptr(ws), ws.numel(), _stream()),
-                   "vd_basis_project")
+        _lib.check(getattr(self.lib, self._prefix + "_project")(
+            self._h, B, int(k), _ptr(X), X.stride(0), _ptr(out), int(bool(accumulate)), _ptr(ws), ws.numel(),
+            _stream()), self._prefix + "_project")
         return out
 
     def project_T(self, k, adphi, adX):
@@ -182,9 +139,129 @@ class BasisPlan:
         if not adphi.is_contiguous():
             raise ValueError("adphi must be contiguous")
         ws = self.workspace(B)
-        _lib.check(self.lib.vd_basis_project_T(self._h, B, int(k), _ptr(adphi), _ptr(adX), adX.stride(0),
-                                               _ptr(ws), ws.numel(), _stream()), "vd_basis_project_T")
+        _lib.check(getattr(self.lib, self._prefix + "_project_T")(
+            self._h, B, int(k), _ptr(adphi), _ptr(adX), adX.stride(0), _ptr(ws), ws.numel(), _stream()),
+            self._prefix + "_project_T")
         return adX
+
+    def q(self):
+        """Prior standard deviation of every coefficient (float64 [nbasis])."""
+        q = np.zeros(self.nbasis)
+        _lib.check(getattr(self.lib, self._prefix + "_q")(self._h, q.ctypes.data), self._prefix + "_q")
+        return q
+
+
+class BasisPlan(_SeparablePlan):
+    """One or more Gaussian components on a rectilinear grid.
+
+    xc [nx], yc [ny]: column / row coordinates (km, or lon/lat in degrees when
+    ``geographic``); time: the basis times in days (set_basis's argument);
+    land: bool [ny, nx] (True = excluded) or None. ``host_only`` builds the
+    tables without a GPU (queries only)."""
+
+    _prefix = "vd_basis"
+
+    def __init__(self, xc, yc, time, comps, land=None, geographic=False, dtype=torch.float32,
+                 device=None, host_only=False):
+        self._grid(xc, yc, time, land, geographic, dtype, device, host_only)
+        self.comps = list(comps)
+        params = (_lib.VdGauss3dParams * len(self.comps))(*[c.to_c() for c in self.comps])
+        h = ctypes.c_void_p()
+        _lib.check(self.lib.vd_basis_plan_create(ctypes.byref(h), ctypes.byref(self._gridc), len(self.comps),
+                                                 params), "vd_basis_plan_create")
+        self._h = h
+        self.nbasis = int(self.lib.vd_basis_nbasis(h))
+
+    def component(self, c):
+        off, nt, ns = ctypes.c_longlong(), ctypes.c_int(), ctypes.c_int()
+        _lib.check(self.lib.vd_basis_component(self._h, c, ctypes.byref(off), ctypes.byref(nt),
+                                               ctypes.byref(ns)), "vd_basis_component")
+        return off.value, nt.value, ns.value
+
+    def lattice(self, c):
+        """(ENST, ENSLAT, ENSLON) of component c."""
+        _, nt, ns = self.component(c)
+        enst, lat, lon = np.zeros(nt), np.zeros(ns), np.zeros(ns)
+        _lib.check(self.lib.vd_basis_lattice(self._h, c, enst.ctypes.data, lat.ctypes.data, lon.ctypes.data),
+                   "vd_basis_lattice")
+        return enst, lat, lon
+
+    def time_weights(self, k, c):
+        n = ctypes.c_int()
+        _lib.check(self.lib.vd_basis_time_weights(self._h, k, c, ctypes.byref(n), None, None),
+                   "vd_basis_time_weights")
+        it = np.zeros(max(n.value, 1), dtype=np.int32)
+        w = np.zeros(max(n.value, 1))
+        _lib.check(self.lib.vd_basis_time_weights(self._h, k, c, ctypes.byref(n), it.ctypes.data,
+                                                  w.ctypes.data), "vd_basis_time_weights")
+        return list(zip(it[:n.value].tolist(), w[:n.value].tolist()))
+
+
+class BMParams:
+    """Parameters of the wave-packet basis (config.BASIS fields of Basis_bm,
+    basis.py:478-496); ``time_ref`` is the window start in days since
+    1950-01-01 (basis.py:527)."""
+
+    def __init__(self, npsp=3.5, facpsp=1.5, lmin=80., lmax=900., facns=1., facnlt=2., tdecmin=2.,
+                 tdecmax=20., factdec=1., sloptdec=-1.28, Qmax=1e-3, slopQ=-2., lmeso=300., tmeso=20.,
+                 norm_time=True, flux=False, time_ref=0.0):
+        self.__dict__.update(dict(npsp=npsp, facpsp=facpsp, lmin=lmin, lmax=lmax, facns=facns, facnlt=facnlt,
+                                  tdecmin=tdecmin, tdecmax=tdecmax, factdec=factdec, sloptdec=sloptdec,
+                                  Qmax=Qmax, slopQ=slopQ, lmeso=lmeso, tmeso=tmeso, norm_time=norm_time,
+                                  flux=flux, time_ref=time_ref))
+
+    def to_c(self):
+        return _lib.VdBmParams(*[float(getattr(self, k)) for k in (
+            "npsp", "facpsp", "lmin", "lmax", "facns", "facnlt", "tdecmin", "tdecmax", "factdec", "sloptdec",
+            "Qmax", "slopQ", "lmeso", "tmeso")], int(bool(self.norm_time)), int(bool(self.flux)),
+            float(self.time_ref))
+
+
+class BMPlan(_SeparablePlan):
+    """Wave-packet basis (Basis_bm, basis.py:472-1168) on a rectilinear grid."""
+
+    _prefix = "vd_bm"
+
+    def __init__(self, xc, yc, time, params, land=None, geographic=False, dtype=torch.float32, device=None,
+                 host_only=False):
+        self._grid(xc, yc, time, land, geographic, dtype, device, host_only)
+        self.params = params
+        h = ctypes.c_void_p()
+        pc = params.to_c()
+        _lib.check(self.lib.vd_bm_plan_create(ctypes.byref(h), ctypes.byref(self._gridc), ctypes.byref(pc)),
+                   "vd_bm_plan_create")
+        self._h = h
+        self.nbasis = int(self.lib.vd_bm_nbasis(h))
+        nf, nth = ctypes.c_int(), ctypes.c_int()
+        _lib.check(self.lib.vd_bm_shape(h, ctypes.byref(nf), ctypes.byref(nth), None), "vd_bm_shape")
+        self.nf, self.ntheta = nf.value, nth.value
+        self.theta = np.zeros(self.ntheta)
+        _lib.check(self.lib.vd_bm_shape(h, None, None, self.theta.ctypes.data), "vd_bm_shape")
+
+    def frequency(self, iff):
+        """(ff, tdec, offset, n time centres, n space centres) of frequency iff."""
+        ff, td, off, nt, ns = ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong(), ctypes.c_int(), \
+            ctypes.c_int()
+        _lib.check(self.lib.vd_bm_frequency(self._h, iff, ctypes.byref(ff), ctypes.byref(td), ctypes.byref(off),
+                                            ctypes.byref(nt), ctypes.byref(ns)), "vd_bm_frequency")
+        return ff.value, td.value, off.value, nt.value, ns.value
+
+    def lattice(self, iff):
+        _, _, _, nt, ns = self.frequency(iff)
+        enst, lat, lon = np.zeros(nt), np.zeros(ns), np.zeros(ns)
+        _lib.check(self.lib.vd_bm_lattice(self._h, iff, enst.ctypes.data, lat.ctypes.data, lon.ctypes.data),
+                   "vd_bm_lattice")
+        return enst, lat, lon
+
+    def time_weights(self, k, iff):
+        n = ctypes.c_int()
+        _lib.check(self.lib.vd_bm_time_weights(self._h, k, iff, ctypes.byref(n), None, None),
+                   "vd_bm_time_weights")
+        it = np.zeros(max(n.value, 1), dtype=np.int32)
+        w = np.zeros(max(n.value, 1))
+        _lib.check(self.lib.vd_bm_time_weights(self._h, k, iff, ctypes.byref(n), it.ctypes.data, w.ctypes.data),
+                   "vd_bm_time_weights")
+        return list(zip(it[:n.value].tolist(), w[:n.value].tolist()))
 
 
 # ---------------------------------------------------------------------------
@@ -241,9 +318,12 @@ class Basis_gauss3d:
     def _components(self):
         return [self.params]
 
+    def _make_plan(self, time):
+        return BasisPlan(self.lon, self.lat, time, self._components(), land=self.mask,
+                         geographic=self.geographic, dtype=self.dtype, device=self.device)
+
     def set_basis(self, time, return_q=False, **kwargs):
-        self.plan = BasisPlan(self.lon, self.lat, time, self._components(), land=self.mask,
-                              geographic=self.geographic, dtype=self.dtype, device=self.device)
+        self.plan = self._make_plan(time)
         self.nbasis = self.plan.nbasis
         self.time = np.asarray(time, dtype=np.float64)
         if return_q:
@@ -280,6 +360,41 @@ class Basis_gauss3d:
         return adX[0] if is_t else adX[0].double().cpu().numpy()
 
 
+class Basis_bm(Basis_gauss3d):
+    """Drop-in for Basis_bm / Basis_bm_jax (basis.py:472-1168) with the GPU
+    projection; ``config.EXP.init_date`` gives the time reference of the
+    wavelet time lattice (basis.py:527). Depth tapering (file_depth) and
+    background files are not supported."""
+
+    def __init__(self, config, State, multi_mode=False, dtype=torch.float32, device=None):
+        cb = config.BASIS
+        if getattr(cb, "file_depth", None) is not None:
+            raise NotImplementedError("config.BASIS.file_depth is not supported by the GPU basis")
+        if getattr(cb, "compute_velocities", False):
+            raise NotImplementedError("config.BASIS.compute_velocities is not supported by the GPU basis")
+        import datetime
+        tref = (config.EXP.init_date - datetime.datetime(1950, 1, 1, 0)).total_seconds() / 24 / 3600
+        self.params = BMParams(npsp=cb.npsp, facpsp=cb.facpsp, lmin=cb.lmin, lmax=cb.lmax, facns=cb.facns,
+                               facnlt=cb.facnlt, tdecmin=cb.tdecmin, tdecmax=cb.tdecmax, factdec=cb.factdec,
+                               sloptdec=cb.sloptdec, Qmax=cb.Qmax, slopQ=cb.slopQ, lmeso=cb.lmeso, tmeso=cb.tmeso,
+                               norm_time=cb.norm_time, flux=getattr(cb, "flux", False), time_ref=tref)
+        self.name_mod_var = cb.name_mod_var
+        self.multi_mode = multi_mode
+        self.lon, self.lat = _grid_axes(State)
+        self.geographic = True
+        self.ny, self.nx = State.ny, State.nx
+        self.mask = None
+        if getattr(State, "mask", None) is not None and np.any(State.mask):
+            self.mask = np.asarray(State.mask, dtype=bool)
+        self.dtype = dtype
+        self.device = torch.device(device or "cuda")
+        self.plan = None
+
+    def _make_plan(self, time):
+        return BMPlan(self.lon, self.lat, time, self.params, land=self.mask, geographic=self.geographic,
+                      dtype=self.dtype, device=self.device)
+
+
 class Basis_multi:
     """Drop-in for Basis_multi (basis.py:4039-4135) over Gaussian components.
     ``config.BASIS`` maps names to component configs, as in the reference.
@@ -308,6 +423,7 @@ class Basis_multi:
     def _components(self):
         return list(self.params)
 
+    _make_plan = Basis_gauss3d._make_plan
     set_basis = Basis_gauss3d.set_basis
     _phi = Basis_gauss3d._phi
     operg_transpose = Basis_gauss3d.operg_transpose

@@ -22,6 +22,7 @@
 // reference's formulas (including NumPy's arange/linspace value sequences),
 // so footprint membership and weights match the reference's CSC entries.
 #include "vd_internal.cuh"
+#include "vd_basis_host.h"
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -32,38 +33,7 @@
 
 namespace {
 
-// Python float modulo (result has the sign of the divisor).
-double pymod(double a, double b)
-{
-    double r = std::fmod(a, b);
-    if (r != 0.0 && ((r < 0.0) != (b < 0.0))) r += b;
-    return r;
-}
-
-// numpy.arange(start, stop, step) for float64: length ceil((stop-start)/step),
-// values start, start+step, then start + i*((start+step)-start).
-std::vector<double> np_arange(double start, double stop, double step)
-{
-    const double len = std::ceil((stop - start) / step);
-    const long n = len > 0 ? (long)len : 0;
-    std::vector<double> v((size_t)n);
-    if (n > 0) v[0] = start;
-    if (n > 1) v[1] = start + step;
-    const double delta = (start + step) - start;
-    for (long i = 2; i < n; ++i) v[(size_t)i] = start + (double)i * delta;
-    return v;
-}
-
-double mywindow(double x)
-{
-    const double c = std::cos(x * 0.5 * M_PI);
-    return c * c;
-}
-
-double mywindow_flux(double x)
-{
-    return -M_PI * std::sin(x * 0.5 * M_PI) * std::cos(x * 0.5 * M_PI);
-}
+using namespace vd::basis_host;
 
 struct HostComp {
     vd_gauss3d_params p;
@@ -436,25 +406,6 @@ int build_host(vd_basis_plan* p, const vd_basis_grid* g, const vd_gauss3d_params
     }
     return VD_OK;
 }
-
-// Packs host vectors into one device allocation; returns device pointers.
-struct Packer {
-    std::vector<unsigned char> blob;
-    template <typename V>
-    size_t add(const std::vector<V>& v)
-    {
-        size_t off = (blob.size() + 255) & ~size_t(255);
-        blob.resize(off + v.size() * sizeof(V) + 1);
-        if (!v.empty()) std::memcpy(blob.data() + off, v.data(), v.size() * sizeof(V));
-        return off;
-    }
-    template <typename T>
-    size_t add_as(const std::vector<double>& v)
-    {
-        std::vector<T> t(v.begin(), v.end());
-        return add(t);
-    }
-};
 
 template <typename T>
 int upload(vd_basis_plan* p, const Tables& tb, const int8_t* land_host)

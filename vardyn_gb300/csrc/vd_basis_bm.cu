@@ -1,0 +1,682 @@
+// Wave-packet reduced basis (Basis_bm / Basis_bm_jax, mapping/src/basis.py
+// 472-1168): phi = G(t) X and adX += G(t)^T adphi.
+//
+// Frequencies ff (577-583), directions theta (587), per frequency a lattice of
+// centres (611-649) and atoms
+//   sqrt(2) w(xx/DX) w(yy/DX) {cos, sin}(kx xx + ky yy),  w = cos^2 window,
+// kx = k cos(theta), ky = k sin(theta), k = 2 pi ff (736-772). With
+// cos(A + B) = cos A cos B - sin A sin B and sin(A + B) = sin A cos B +
+// cos A sin B every atom is a sum of two separable products, so G is two
+// banded passes with two channels per direction (no sparse matrix, no
+// atomics):
+//   x pass  T1[r][th][x] = sum_i wx (cos A Zc + sin A Zs)
+//           T2[r][th][x] = sum_i wx (cos A Zs - sin A Zc)
+//   y pass  phi[y][x]    = sum_f sum_th sum_j sqrt(2) wy (cos B T1 + sin B T2)
+// where Z{c,s}(i, th) = sum over active time centres of g_it X[it][i][th][c|s].
+// The transpose runs the passes backwards. Coefficients of one frequency are
+// ordered [time centre][space centre][theta][cos, sin] (basis.py:775-781).
+#include "vd_internal.cuh"
+#include "vd_basis_host.h"
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <new>
+#include <vector>
+
+namespace {
+
+using namespace vd::basis_host;
+
+struct BmFreq {
+    double ff = 0, k = 0, DX = 0, DXG = 0, tdec = 0, norm_fact = 1, Q = 0;
+    std::vector<double> enst;
+    std::vector<double> rows_lat;
+    std::vector<std::vector<double>> row_lons;
+    std::vector<double> enslat, enslon;
+    long long NP = 0;
+    long long boff = 0;
+    int rowoff = 0;
+};
+
+}  // namespace
+
+struct vd_bm_plan {
+    int ny = 0, nx = 0, dtype = VD_F32, geographic = 0, host_only = 0, ntime = 0;
+    int nf = 0, nth = 0;
+    long long nbasis = 0;
+    int R = 0, KX = 1, KY = 1, NA = 1;
+    vd_bm_params prm;
+    std::vector<double> theta;
+    std::vector<BmFreq> fr;
+    std::vector<double> times;
+    std::vector<int> tact_n, tact_it;
+    std::vector<double> tact_g;
+    void* dev = nullptr;
+    const int32_t *row_freq, *row_pat, *row_n, *fx_i, *tx_ptr, *tx_x, *tx_e, *pat_cbase, *fy_j, *ty_ptr, *ty_y,
+        *ty_e, *freq_rowoff, *d_tact_n, *d_tact_it;
+    const long long *row_cb, *freq_boff, *freq_np;
+    const void *fx_c, *fx_s, *fy_c, *fy_s, *d_tact_g;
+    const int8_t* land;
+};
+
+namespace vd {
+
+template <typename T>
+struct BmDev {
+    int ny, nx, R, KX, KY, NA, nf, nth;
+    const int32_t *row_freq, *row_pat, *row_n, *fx_i, *tx_ptr, *tx_x, *tx_e, *pat_cbase, *fy_j, *ty_ptr, *ty_y,
+        *ty_e, *freq_rowoff, *tact_n, *tact_it;
+    const long long *row_cb, *freq_boff, *freq_np;
+    const T *fx_c, *fx_s, *fy_c, *fy_s, *tact_g;
+    const int8_t* land;
+};
+
+template <typename T>
+BmDev<T> bm_view(const vd_bm_plan* p)
+{
+    BmDev<T> d;
+    d.ny = p->ny; d.nx = p->nx; d.R = p->R; d.KX = p->KX; d.KY = p->KY; d.NA = p->NA; d.nf = p->nf;
+    d.nth = p->nth;
+    d.row_freq = p->row_freq; d.row_pat = p->row_pat; d.row_n = p->row_n; d.fx_i = p->fx_i;
+    d.tx_ptr = p->tx_ptr; d.tx_x = p->tx_x; d.tx_e = p->tx_e; d.pat_cbase = p->pat_cbase;
+    d.fy_j = p->fy_j; d.ty_ptr = p->ty_ptr; d.ty_y = p->ty_y; d.ty_e = p->ty_e; d.freq_rowoff = p->freq_rowoff;
+    d.tact_n = p->d_tact_n; d.tact_it = p->d_tact_it;
+    d.row_cb = p->row_cb; d.freq_boff = p->freq_boff; d.freq_np = p->freq_np;
+    d.fx_c = (const T*)p->fx_c; d.fx_s = (const T*)p->fx_s; d.fy_c = (const T*)p->fy_c;
+    d.fy_s = (const T*)p->fy_s; d.tact_g = (const T*)p->d_tact_g;
+    d.land = p->land;
+    return d;
+}
+
+// x pass of G: one thread per (column x, lattice row r and direction th, window b)
+template <typename T>
+__global__ void __launch_bounds__(128)
+k_bm_xpass(BmDev<T> d, int k, const T* __restrict__ X, long long ldX, T* __restrict__ Tw)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int rt = blockIdx.y, b = blockIdx.z;
+    if (x >= d.nx) return;
+    const int r = rt / d.nth, th = rt - r * d.nth;
+    const int f = d.row_freq[r], p = d.row_pat[r];
+    const long long stride = 2LL * d.nth * d.freq_np[f];
+    const T* Xr = X + (long long)b * ldX + d.freq_boff[f] + (d.row_cb[r] * d.nth + th) * 2;
+    const int ta = (k * d.nf + f) * d.NA, na = d.tact_n[k * d.nf + f];
+    const long long e0 = ((long long)p * d.nx + x) * d.KX;
+    const long long w0 = (((long long)p * d.nth + th) * d.nx + x) * d.KX;
+    T t1 = T(0), t2 = T(0);
+    for (int e = 0; e < d.KX; ++e) {
+        const int i = d.fx_i[e0 + e];
+        if (i < 0) break;
+        T zc = T(0), zs = T(0);
+        for (int a = 0; a < na; ++a) {
+            const T g = d.tact_g[ta + a];
+            const long long o = d.tact_it[ta + a] * stride + (long long)i * 2 * d.nth;
+            zc += g * Xr[o];
+            zs += g * Xr[o + 1];
+        }
+        const T cw = d.fx_c[w0 + e], sw = d.fx_s[w0 + e];
+        t1 += cw * zc + sw * zs;
+        t2 += cw * zs - sw * zc;
+    }
+    T* o = Tw + (((long long)b * d.R + r) * d.nth + th) * 2 * d.nx + x;
+    o[0] = t1;
+    o[d.nx] = t2;
+}
+
+// y pass of G: one thread per (x, y, b), summing every frequency and direction
+template <typename T>
+__global__ void __launch_bounds__(128)
+k_bm_ypass(BmDev<T> d, const T* __restrict__ Tw, T* __restrict__ phi, int accumulate)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, b = blockIdx.z;
+    if (x >= d.nx) return;
+    const long long rowstride = (long long)d.nth * 2 * d.nx;
+    T acc = T(0);
+    for (int f = 0; f < d.nf; ++f) {
+        const long long e0 = ((long long)f * d.ny + y) * d.KY;
+        for (int th = 0; th < d.nth; ++th) {
+            const long long w0 = (((long long)f * d.nth + th) * d.ny + y) * d.KY;
+            const T* base = Tw + (((long long)b * d.R + d.freq_rowoff[f]) * d.nth + th) * 2 * d.nx + x;
+            for (int e = 0; e < d.KY; ++e) {
+                const int j = d.fy_j[e0 + e];
+                if (j < 0) break;
+                const T* t = base + j * rowstride;
+                acc += d.fy_c[w0 + e] * t[0] + d.fy_s[w0 + e] * t[d.nx];
+            }
+        }
+    }
+    const long long o = ((long long)b * d.ny + y) * d.nx + x;
+    if (d.land && d.land[(long long)y * d.nx + x]) acc = T(0);
+    phi[o] = accumulate ? phi[o] + acc : acc;
+}
+
+// y pass of G^T: one thread per (x, row r and direction th, b)
+template <typename T>
+__global__ void __launch_bounds__(128)
+k_bmT_ypass(BmDev<T> d, const T* __restrict__ adphi, T* __restrict__ Uw)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int rt = blockIdx.y, b = blockIdx.z;
+    if (x >= d.nx) return;
+    const int r = rt / d.nth, th = rt - r * d.nth;
+    const int f = d.row_freq[r];
+    const T* a = adphi + (long long)b * d.ny * d.nx + x;
+    T u1 = T(0), u2 = T(0);
+    for (int e = d.ty_ptr[r]; e < d.ty_ptr[r + 1]; ++e) {
+        const int y = d.ty_y[e];
+        const long long w = (((long long)f * d.nth + th) * d.ny + y) * d.KY + d.ty_e[e];
+        T v = a[(long long)y * d.nx];
+        if (d.land && d.land[(long long)y * d.nx + x]) v = T(0);
+        u1 += d.fy_c[w] * v;
+        u2 += d.fy_s[w] * v;
+    }
+    T* o = Uw + (((long long)b * d.R + r) * d.nth + th) * 2 * d.nx + x;
+    o[0] = u1;
+    o[d.nx] = u2;
+}
+
+// x pass of G^T: one CTA per (lattice row r, window b), threads over (centre, direction)
+template <typename T>
+__global__ void __launch_bounds__(128)
+k_bmT_xpass(BmDev<T> d, int k, const T* __restrict__ Uw, T* __restrict__ adX, long long ldX)
+{
+    const int r = blockIdx.x, b = blockIdx.y;
+    const int f = d.row_freq[r], p = d.row_pat[r];
+    const long long stride = 2LL * d.nth * d.freq_np[f];
+    const int ta = (k * d.nf + f) * d.NA, na = d.tact_n[k * d.nf + f];
+    const int base = d.pat_cbase[p];
+    T* A = adX + (long long)b * ldX + d.freq_boff[f] + d.row_cb[r] * 2 * d.nth;
+    for (int q = threadIdx.x; q < d.row_n[r] * d.nth; q += blockDim.x) {
+        const int i = q / d.nth, th = q - i * d.nth;
+        const T* U = Uw + (((long long)b * d.R + r) * d.nth + th) * 2 * d.nx;
+        T zc = T(0), zs = T(0);
+        for (int e = d.tx_ptr[base + i]; e < d.tx_ptr[base + i + 1]; ++e) {
+            const int x = d.tx_x[e];
+            const long long w = (((long long)p * d.nth + th) * d.nx + x) * d.KX + d.tx_e[e];
+            const T u1 = U[x], u2 = U[d.nx + x];
+            const T cw = d.fx_c[w], sw = d.fx_s[w];
+            zc += cw * u1 - sw * u2;
+            zs += sw * u1 + cw * u2;
+        }
+        for (int a = 0; a < na; ++a) {
+            const T g = d.tact_g[ta + a];
+            const long long o = d.tact_it[ta + a] * stride + ((long long)i * d.nth + th) * 2;
+            A[o] += g * zc;
+            A[o + 1] += g * zs;
+        }
+    }
+}
+
+}  // namespace vd
+
+namespace {
+
+struct BmTables {
+    std::vector<int32_t> row_freq, row_pat, row_n, fx_i, tx_ptr, tx_x, tx_e, pat_cbase, fy_j, ty_ptr, ty_y, ty_e,
+        freq_rowoff;
+    std::vector<long long> row_cb, freq_boff, freq_np;
+    std::vector<double> fx_c, fx_s, fy_c, fy_s;
+};
+
+int bm_build(vd_bm_plan* p, const vd_basis_grid* g, BmTables& tb)
+{
+    const vd_bm_params& q = p->prm;
+    const int ny = g->ny, nx = g->nx;
+    const bool geo = g->geographic != 0;
+    const double k2 = geo ? 1.0 / 110 : 1.0;
+    std::vector<double> xc(g->xc_host, g->xc_host + nx), yc(g->yc_host, g->yc_host + ny);
+    for (double v : xc) if (!std::isfinite(v)) return VD_ERR_ARG;
+    for (double v : yc) if (!std::isfinite(v)) return VD_ERR_ARG;
+    if (!(q.npsp > 0) || !(q.facpsp > 0) || !(q.lmin > 0) || !(q.lmax > q.lmin) || !(q.facns > 0) ||
+        !(q.facnlt > 0) || !(q.tdecmin > 0) || !(q.tdecmax >= q.tdecmin))
+        return VD_ERR_ARG;
+    const double LON_MIN = *std::min_element(xc.begin(), xc.end());
+    double LON_MAX = *std::max_element(xc.begin(), xc.end());
+    const double LAT_MIN = *std::min_element(yc.begin(), yc.end());
+    const double LAT_MAX = *std::max_element(yc.begin(), yc.end());
+    if (LON_MAX < LON_MIN) LON_MAX += 360.;
+    p->times.assign(g->time_host, g->time_host + g->ntime);
+    const double deltat = *std::max_element(p->times.begin(), p->times.end()) -
+                          *std::min_element(p->times.begin(), p->times.end());
+    auto cosd = [&](double lat) { return geo ? std::cos(lat * M_PI / 180.) : 1.0; };
+    auto window = [&](double x) { return q.flux ? mywindow_flux(x) : mywindow(x); };
+    std::vector<int8_t> land;
+    bool any_land = false;
+    if (g->land_host) {
+        land.assign(g->land_host, g->land_host + (size_t)ny * nx);
+        for (int8_t v : land) any_land |= (v != 0);
+    }
+
+    // frequencies and directions (basis.py:577-587)
+    const double lstep = std::log(1 + q.facpsp / q.npsp);
+    std::vector<double> logff = np_arange(std::log(1. / q.lmin), std::log(1. / q.lmax) - lstep, -lstep);
+    std::reverse(logff.begin(), logff.end());
+    if (logff.size() < 2) return VD_ERR_ARG;
+    std::vector<double> ff(logff.size());
+    for (size_t i = 0; i < ff.size(); ++i) ff[i] = std::exp(logff[i]);
+    const double dff0 = ff[1] - ff[0];
+    std::vector<double> th = np_linspace(0, M_PI, (int)(M_PI * ff[0] / dff0 * q.facpsp));
+    if (th.size() < 2) return VD_ERR_ARG;
+    th.pop_back();
+    p->theta = th;
+    p->nth = (int)th.size();
+    p->nf = (int)ff.size();
+    p->fr.resize(ff.size());
+
+    // lattices, time centres, Q (basis.py:603-690)
+    std::map<std::vector<double>, int> pat_of;
+    std::vector<std::vector<std::vector<std::pair<int, double>>>> pat_cols;  // [pat][x] -> (i, xx)
+    std::vector<int> pat_n, pat_freq;
+    long long boff = 0;
+    int rowoff = 0;
+    for (int iff = 0; iff < p->nf; ++iff) {
+        BmFreq& F = p->fr[iff];
+        F.ff = ff[iff];
+        F.k = 2 * M_PI * ff[iff];
+        F.DX = 1. / ff[iff] * q.npsp * 0.5;
+        F.DXG = F.DX / q.facns;
+        const double dlat = F.DXG * k2;
+        const double lat0 = LAT_MIN - pymod(LAT_MIN, dlat) - F.DX * k2;
+        const double lat1 = LAT_MAX + F.DX * k2 * 1.5;
+        F.rows_lat = np_arange(lat0, lat1, dlat);
+        F.rowoff = rowoff;
+        F.boff = boff;
+        long long cb = 0;
+        for (double la : F.rows_lat) {
+            const double cl = cosd(la);
+            const double dlon = F.DXG / cl * k2;
+            const double lon0 = LON_MIN - pymod(LON_MIN, dlon) - F.DX / cl * k2;
+            const double lon1 = LON_MAX + F.DX / cl * k2 * 1.5;
+            std::vector<double> lons0 = np_arange(lon0, lon1, dlon), lons;
+            for (double lo : lons0) {
+                if (any_land) {
+                    // keep a centre only if its box of radius 1/ff holds an unmasked point (basis.py:632-645)
+                    bool keep = false;
+                    for (int yy = 0; yy < ny && !keep; ++yy) {
+                        if (!(std::fabs((yc[yy] - la) / k2) <= 1. / ff[iff])) continue;
+                        for (int xx = 0; xx < nx; ++xx)
+                            if (std::fabs((xc[xx] - lo) / k2 * cl) <= 1. / ff[iff] && !land[(size_t)yy * nx + xx]) {
+                                keep = true;
+                                break;
+                            }
+                    }
+                    if (!keep) continue;
+                }
+                lons.push_back(lo);
+            }
+            // x pattern of this row: (centre, xx) per column within DX
+            std::vector<double> key = lons;
+            key.push_back(cl);
+            key.push_back((double)iff);
+            int pat;
+            auto it = pat_of.find(key);
+            if (it != pat_of.end()) {
+                pat = it->second;
+            } else {
+                pat = (int)pat_cols.size();
+                pat_of[key] = pat;
+                std::vector<std::vector<std::pair<int, double>>> cols((size_t)nx);
+                for (int x = 0; x < nx; ++x)
+                    for (int i = 0; i < (int)lons.size(); ++i) {
+                        const double xx = (xc[x] - lons[i]) / k2 * cl;
+                        if (std::fabs(xx) <= F.DX) cols[x].push_back({i, xx});
+                    }
+                pat_cols.push_back(std::move(cols));
+                pat_n.push_back((int)lons.size());
+                pat_freq.push_back(iff);
+            }
+            tb.row_freq.push_back(iff);
+            tb.row_pat.push_back(pat);
+            tb.row_n.push_back((int)lons.size());
+            tb.row_cb.push_back(cb);
+            F.row_lons.push_back(lons);
+            for (double lo : lons) {
+                F.enslat.push_back(la);
+                F.enslon.push_back(lo);
+            }
+            cb += (long long)lons.size();
+        }
+        F.NP = cb;
+        double td = q.tmeso * std::pow(q.lmeso, q.sloptdec) * std::pow(ff[iff], q.sloptdec);
+        td *= q.factdec;
+        if (td < q.tdecmin) td = q.tdecmin;
+        if (td > q.tdecmax) td = q.tdecmax;
+        F.tdec = td;
+        const double t0 = pymod(-q.time_ref, td);
+        F.enst = np_arange(t0 - td / q.facnlt, deltat + td / q.facnlt, td / q.facnlt);
+        F.norm_fact = window_norm(td, window);
+        F.Q = (1 / ff[iff] > q.lmeso) ? q.Qmax / q.facns
+                                      : q.Qmax / q.facns * std::pow(q.lmeso, q.slopQ) * std::pow(ff[iff], q.slopQ);
+        boff += (long long)F.enst.size() * 2 * p->nth * F.NP;
+        rowoff += (int)F.rows_lat.size();
+        tb.freq_rowoff.push_back(F.rowoff);
+        tb.freq_boff.push_back(F.boff);
+        tb.freq_np.push_back(F.NP);
+    }
+    p->nbasis = boff;
+    p->R = rowoff;
+
+    // x tables: ELL (centre) + per-direction weights; CSR per centre (x, slot)
+    int KX = 1;
+    for (auto& pc : pat_cols)
+        for (auto& col : pc) KX = std::max(KX, (int)col.size());
+    p->KX = KX;
+    const int P = (int)pat_cols.size(), nth = p->nth;
+    tb.fx_i.assign((size_t)P * nx * KX, -1);
+    tb.fx_c.assign((size_t)P * nth * nx * KX, 0.0);
+    tb.fx_s.assign((size_t)P * nth * nx * KX, 0.0);
+    tb.tx_ptr.push_back(0);
+    for (int pt = 0; pt < P; ++pt) {
+        const BmFreq& F = p->fr[pat_freq[pt]];
+        tb.pat_cbase.push_back((int)tb.tx_ptr.size() - 1);
+        std::vector<std::vector<std::pair<int, int>>> by_centre((size_t)pat_n[pt]);
+        for (int x = 0; x < nx; ++x) {
+            const auto& col = pat_cols[pt][x];
+            for (size_t e = 0; e < col.size(); ++e) {
+                const double xx = col[e].second;
+                const double wx = mywindow(xx / F.DX);
+                tb.fx_i[((size_t)pt * nx + x) * KX + e] = col[e].first;
+                for (int t = 0; t < nth; ++t) {
+                    const double kx = F.k * std::cos(th[t]);
+                    const size_t w = (((size_t)pt * nth + t) * nx + x) * KX + e;
+                    tb.fx_c[w] = wx * std::cos(kx * xx);
+                    tb.fx_s[w] = wx * std::sin(kx * xx);
+                }
+                by_centre[col[e].first].push_back({x, (int)e});
+            }
+        }
+        for (auto& lst : by_centre) {
+            for (auto& pr : lst) {
+                tb.tx_x.push_back(pr.first);
+                tb.tx_e.push_back(pr.second);
+            }
+            tb.tx_ptr.push_back((int32_t)tb.tx_x.size());
+        }
+    }
+
+    // y tables: ELL (row) + per-direction weights with sqrt(2); CSR per row (y, slot)
+    std::vector<std::vector<std::vector<std::pair<int, double>>>> ycols((size_t)p->nf);
+    int KY = 1;
+    for (int iff = 0; iff < p->nf; ++iff) {
+        const BmFreq& F = p->fr[iff];
+        ycols[iff].resize((size_t)ny);
+        for (int y = 0; y < ny; ++y)
+            for (int j = 0; j < (int)F.rows_lat.size(); ++j) {
+                const double yy = (yc[y] - F.rows_lat[j]) / k2;
+                if (std::fabs(yy) <= F.DX) ycols[iff][y].push_back({j, yy});
+            }
+        for (auto& l : ycols[iff]) KY = std::max(KY, (int)l.size());
+    }
+    p->KY = KY;
+    tb.fy_j.assign((size_t)p->nf * ny * KY, -1);
+    tb.fy_c.assign((size_t)p->nf * nth * ny * KY, 0.0);
+    tb.fy_s.assign((size_t)p->nf * nth * ny * KY, 0.0);
+    tb.ty_ptr.push_back(0);
+    for (int iff = 0; iff < p->nf; ++iff) {
+        const BmFreq& F = p->fr[iff];
+        std::vector<std::vector<std::pair<int, int>>> by_row(F.rows_lat.size());
+        for (int y = 0; y < ny; ++y) {
+            const auto& l = ycols[iff][y];
+            for (size_t e = 0; e < l.size(); ++e) {
+                const double yy = l[e].second;
+                const double wy = std::sqrt(2.0) * mywindow(yy / F.DX);
+                tb.fy_j[((size_t)iff * ny + y) * KY + e] = l[e].first;
+                for (int t = 0; t < nth; ++t) {
+                    const double ky = F.k * std::sin(th[t]);
+                    const size_t w = (((size_t)iff * nth + t) * ny + y) * KY + e;
+                    tb.fy_c[w] = wy * std::cos(ky * yy);
+                    tb.fy_s[w] = wy * std::sin(ky * yy);
+                }
+                by_row[l[e].first].push_back({y, (int)e});
+            }
+        }
+        for (auto& lst : by_row) {
+            for (auto& pr : lst) {
+                tb.ty_y.push_back(pr.first);
+                tb.ty_e.push_back(pr.second);
+            }
+            tb.ty_ptr.push_back((int32_t)tb.ty_y.size());
+        }
+    }
+
+    // time weights of the JAX form: |dt| <= tdec (basis.py:1026-1035)
+    std::vector<std::vector<std::pair<int, double>>> act((size_t)p->ntime * p->nf);
+    int NA = 1;
+    for (int kt = 0; kt < p->ntime; ++kt)
+        for (int iff = 0; iff < p->nf; ++iff) {
+            const BmFreq& F = p->fr[iff];
+            auto& lst = act[(size_t)kt * p->nf + iff];
+            for (int it = 0; it < (int)F.enst.size(); ++it) {
+                const double dt = p->times[kt] - F.enst[it];
+                if (!(std::fabs(dt) > F.tdec || std::isnan(F.enst[it]))) {
+                    double fact = window(dt / F.tdec);
+                    if (q.norm_time) fact /= F.norm_fact;
+                    lst.push_back({it, fact});
+                }
+            }
+            NA = std::max(NA, (int)lst.size());
+        }
+    p->NA = NA;
+    p->tact_n.assign((size_t)p->ntime * p->nf, 0);
+    p->tact_it.assign((size_t)p->ntime * p->nf * NA, 0);
+    p->tact_g.assign((size_t)p->ntime * p->nf * NA, 0.0);
+    for (size_t s = 0; s < act.size(); ++s) {
+        p->tact_n[s] = (int)act[s].size();
+        for (size_t a = 0; a < act[s].size(); ++a) {
+            p->tact_it[s * NA + a] = act[s][a].first;
+            p->tact_g[s * NA + a] = act[s][a].second;
+        }
+    }
+    return VD_OK;
+}
+
+template <typename T>
+int bm_upload(vd_bm_plan* p, const BmTables& tb, const int8_t* land_host)
+{
+    Packer pk;
+    const size_t o_rf = pk.add(tb.row_freq), o_rp = pk.add(tb.row_pat), o_rn = pk.add(tb.row_n),
+                 o_fxi = pk.add(tb.fx_i), o_txp = pk.add(tb.tx_ptr), o_txx = pk.add(tb.tx_x),
+                 o_txe = pk.add(tb.tx_e), o_pcb = pk.add(tb.pat_cbase), o_fyj = pk.add(tb.fy_j),
+                 o_typ = pk.add(tb.ty_ptr), o_tyy = pk.add(tb.ty_y), o_tye = pk.add(tb.ty_e),
+                 o_fro = pk.add(tb.freq_rowoff), o_tn = pk.add(p->tact_n), o_tit = pk.add(p->tact_it),
+                 o_rcb = pk.add(tb.row_cb), o_fbo = pk.add(tb.freq_boff), o_fnp = pk.add(tb.freq_np),
+                 o_fxc = pk.add_as<T>(tb.fx_c), o_fxs = pk.add_as<T>(tb.fx_s), o_fyc = pk.add_as<T>(tb.fy_c),
+                 o_fys = pk.add_as<T>(tb.fy_s), o_tg = pk.add_as<T>(p->tact_g);
+    size_t o_land = 0;
+    bool any_land = false;
+    std::vector<int8_t> land;
+    if (land_host) {
+        land.assign(land_host, land_host + (size_t)p->ny * p->nx);
+        for (int8_t v : land) any_land |= (v != 0);
+        if (any_land) o_land = pk.add(land);
+    }
+    VD_CUDA_TRY(cudaMalloc(&p->dev, pk.blob.size()));
+    VD_CUDA_TRY(cudaMemcpy(p->dev, pk.blob.data(), pk.blob.size(), cudaMemcpyHostToDevice));
+    unsigned char* b = (unsigned char*)p->dev;
+    p->row_freq = (const int32_t*)(b + o_rf);
+    p->row_pat = (const int32_t*)(b + o_rp);
+    p->row_n = (const int32_t*)(b + o_rn);
+    p->fx_i = (const int32_t*)(b + o_fxi);
+    p->tx_ptr = (const int32_t*)(b + o_txp);
+    p->tx_x = (const int32_t*)(b + o_txx);
+    p->tx_e = (const int32_t*)(b + o_txe);
+    p->pat_cbase = (const int32_t*)(b + o_pcb);
+    p->fy_j = (const int32_t*)(b + o_fyj);
+    p->ty_ptr = (const int32_t*)(b + o_typ);
+    p->ty_y = (const int32_t*)(b + o_tyy);
+    p->ty_e = (const int32_t*)(b + o_tye);
+    p->freq_rowoff = (const int32_t*)(b + o_fro);
+    p->d_tact_n = (const int32_t*)(b + o_tn);
+    p->d_tact_it = (const int32_t*)(b + o_tit);
+    p->row_cb = (const long long*)(b + o_rcb);
+    p->freq_boff = (const long long*)(b + o_fbo);
+    p->freq_np = (const long long*)(b + o_fnp);
+    p->fx_c = b + o_fxc;
+    p->fx_s = b + o_fxs;
+    p->fy_c = b + o_fyc;
+    p->fy_s = b + o_fys;
+    p->d_tact_g = b + o_tg;
+    p->land = any_land ? (const int8_t*)(b + o_land) : nullptr;
+    return VD_OK;
+}
+
+size_t bm_ws_bytes(const vd_bm_plan* p, int batch)
+{
+    return (size_t)batch * p->R * p->nth * 2 * p->nx * (p->dtype == VD_F64 ? 8 : 4);
+}
+
+template <typename T>
+int bm_project(const vd_bm_plan* p, int B, int k, const T* X, long long ldX, T* phi, int acc, T* ws,
+               cudaStream_t st)
+{
+    const vd::BmDev<T> d = vd::bm_view<T>(p);
+    const unsigned gx = (unsigned)((p->nx + 127) / 128);
+    vd::k_bm_xpass<T><<<dim3(gx, p->R * p->nth, B), 128, 0, st>>>(d, k, X, ldX, ws);
+    VD_LAUNCH_CHECK();
+    vd::k_bm_ypass<T><<<dim3(gx, p->ny, B), 128, 0, st>>>(d, ws, phi, acc);
+    VD_LAUNCH_CHECK();
+    return VD_OK;
+}
+
+template <typename T>
+int bm_project_T(const vd_bm_plan* p, int B, int k, const T* adphi, T* adX, long long ldX, T* ws, cudaStream_t st)
+{
+    const vd::BmDev<T> d = vd::bm_view<T>(p);
+    const unsigned gx = (unsigned)((p->nx + 127) / 128);
+    vd::k_bmT_ypass<T><<<dim3(gx, p->R * p->nth, B), 128, 0, st>>>(d, adphi, ws);
+    VD_LAUNCH_CHECK();
+    vd::k_bmT_xpass<T><<<dim3(p->R, B), 128, 0, st>>>(d, k, ws, adX, ldX);
+    VD_LAUNCH_CHECK();
+    return VD_OK;
+}
+
+int bm_check(const vd_bm_plan* p, int B, int k, long long ldX, const void* a, const void* b, void* ws, size_t wsb)
+{
+    if (!p || p->host_only || !p->dev) return VD_ERR_ARG;
+    if (B < 1 || B > 65535 || k < 0 || k >= p->ntime || !a || !b || !ws) return VD_ERR_ARG;
+    if (B > 1 && ldX < p->nbasis) return VD_ERR_ARG;
+    if (wsb < bm_ws_bytes(p, B)) return VD_ERR_WORKSPACE;
+    return VD_OK;
+}
+
+}  // namespace
+
+extern "C" vd_status vd_bm_plan_create(vd_bm_plan** out, const vd_basis_grid* g, const vd_bm_params* prm)
+{
+    if (!out || !g || !prm) return VD_ERR_ARG;
+    *out = nullptr;
+    if (g->ny < 1 || g->nx < 1 || !g->xc_host || !g->yc_host || g->ntime < 1 || !g->time_host) return VD_ERR_ARG;
+    if (g->dtype != VD_F32 && g->dtype != VD_F64) return VD_ERR_ARG;
+    for (int i = 0; i < g->ntime; ++i)
+        if (!std::isfinite(g->time_host[i])) return VD_ERR_ARG;
+    vd_bm_plan* p = new (std::nothrow) vd_bm_plan();
+    if (!p) return VD_ERR_ARG;
+    p->ny = g->ny; p->nx = g->nx; p->dtype = g->dtype; p->geographic = g->geographic;
+    p->host_only = g->host_only; p->ntime = g->ntime; p->prm = *prm;
+    BmTables tb;
+    int st = bm_build(p, g, tb);
+    if (st == VD_OK && ((long long)p->R * p->nth > 65535 || p->ny > 65535 || p->R > 65535)) st = VD_ERR_UNSUPPORTED;
+    if (st == VD_OK && !p->host_only)
+        st = p->dtype == VD_F64 ? bm_upload<double>(p, tb, g->land_host) : bm_upload<float>(p, tb, g->land_host);
+    if (st != VD_OK) {
+        if (p->dev) cudaFree(p->dev);
+        delete p;
+        return st;
+    }
+    *out = p;
+    return VD_OK;
+}
+
+extern "C" vd_status vd_bm_plan_destroy(vd_bm_plan* p)
+{
+    if (!p) return VD_ERR_ARG;
+    if (p->dev) cudaFree(p->dev);
+    delete p;
+    return VD_OK;
+}
+
+extern "C" long long vd_bm_nbasis(const vd_bm_plan* p) { return p ? p->nbasis : 0; }
+
+extern "C" vd_status vd_bm_shape(const vd_bm_plan* p, int* nf, int* ntheta, double* theta_host)
+{
+    if (!p) return VD_ERR_ARG;
+    if (nf) *nf = p->nf;
+    if (ntheta) *ntheta = p->nth;
+    if (theta_host) std::copy(p->theta.begin(), p->theta.end(), theta_host);
+    return VD_OK;
+}
+
+extern "C" vd_status vd_bm_frequency(const vd_bm_plan* p, int iff, double* ff, double* tdec, long long* offset,
+                                     int* ntime_centres, int* nspace_centres)
+{
+    if (!p || iff < 0 || iff >= p->nf) return VD_ERR_ARG;
+    const BmFreq& F = p->fr[iff];
+    if (ff) *ff = F.ff;
+    if (tdec) *tdec = F.tdec;
+    if (offset) *offset = F.boff;
+    if (ntime_centres) *ntime_centres = (int)F.enst.size();
+    if (nspace_centres) *nspace_centres = (int)F.NP;
+    return VD_OK;
+}
+
+extern "C" vd_status vd_bm_lattice(const vd_bm_plan* p, int iff, double* enst, double* enslat, double* enslon)
+{
+    if (!p || iff < 0 || iff >= p->nf) return VD_ERR_ARG;
+    const BmFreq& F = p->fr[iff];
+    if (enst) std::copy(F.enst.begin(), F.enst.end(), enst);
+    if (enslat) std::copy(F.enslat.begin(), F.enslat.end(), enslat);
+    if (enslon) std::copy(F.enslon.begin(), F.enslon.end(), enslon);
+    return VD_OK;
+}
+
+extern "C" vd_status vd_bm_q(const vd_bm_plan* p, double* q)
+{
+    if (!p || !q) return VD_ERR_ARG;
+    for (const BmFreq& F : p->fr) {
+        const long long n = (long long)F.enst.size() * 2 * p->nth * F.NP;
+        std::fill(q + F.boff, q + F.boff + n, F.Q);
+    }
+    return VD_OK;
+}
+
+extern "C" vd_status vd_bm_time_weights(const vd_bm_plan* p, int k, int iff, int* count, int* it, double* w)
+{
+    if (!p || !count || k < 0 || k >= p->ntime || iff < 0 || iff >= p->nf) return VD_ERR_ARG;
+    const size_t s = (size_t)k * p->nf + iff;
+    *count = p->tact_n[s];
+    for (int a = 0; a < p->tact_n[s]; ++a) {
+        if (it) it[a] = p->tact_it[s * p->NA + a];
+        if (w) w[a] = p->tact_g[s * p->NA + a];
+    }
+    return VD_OK;
+}
+
+extern "C" size_t vd_bm_workspace_bytes(const vd_bm_plan* p, int batch)
+{
+    if (!p || batch < 1) return 0;
+    return bm_ws_bytes(p, batch);
+}
+
+extern "C" vd_status vd_bm_project(const vd_bm_plan* p, int B, int k, const void* X, long long ldX, void* phi,
+                                   int accumulate, void* ws, size_t wsb, void* stream)
+{
+    const int st = bm_check(p, B, k, ldX, X, phi, ws, wsb);
+    if (st != VD_OK) return st;
+    if (p->dtype == VD_F64)
+        return bm_project<double>(p, B, k, (const double*)X, ldX, (double*)phi, accumulate, (double*)ws,
+                                  (cudaStream_t)stream);
+    return bm_project<float>(p, B, k, (const float*)X, ldX, (float*)phi, accumulate, (float*)ws,
+                             (cudaStream_t)stream);
+}
+
+extern "C" vd_status vd_bm_project_T(const vd_bm_plan* p, int B, int k, const void* adphi, void* adX,
+                                     long long ldX, void* ws, size_t wsb, void* stream)
+{
+    const int st = bm_check(p, B, k, ldX, adphi, adX, ws, wsb);
+    if (st != VD_OK) return st;
+    if (p->dtype == VD_F64)
+        return bm_project_T<double>(p, B, k, (const double*)adphi, (double*)adX, ldX, (double*)ws,
+                                    (cudaStream_t)stream);
+    return bm_project_T<float>(p, B, k, (const float*)adphi, (float*)adX, ldX, (float*)ws, (cudaStream_t)stream);
+}
