@@ -361,6 +361,43 @@ vd_status vd_bm_project_T(const vd_bm_plan* plan, int batch, int k, const void* 
                           void* adX, long long ldX, void* workspace, size_t workspace_bytes,
                           void* stream);
 
+/* ------------------------------------------------------------------------
+ * Masked multigrid Helmholtz solver (MG_Helmholtz,
+ * mapping/models/model_qgsw/helmholtz_multigrid.py:156-419):
+ *   div(c grad u) - lambda_b u = rhs_b  for b < nsys
+ * on cell centres of an n0 x n1 rectangle (row-major [nsys][n0][n1]; axis 0
+ * has spacing d0, axis 1 spacing d1), mask 1 inside / 0 outside, homogeneous
+ * Neumann walls on cell edges. Full-multigrid start then max_ite V-cycles of
+ * 6-sweep damped Jacobi smoothing; bottom solve by pseudo-inverse
+ * (niter_bottom <= 0) or niter_bottom Jacobi smooths.
+ * ---------------------------------------------------------------------- */
+typedef struct vd_mg_plan vd_mg_plan;
+
+typedef struct vd_mg_desc {
+    int n0, n1;                 /* grid; both divisible by 2^(n_levels-1) */
+    int nsys;                   /* systems solved together */
+    int dtype;                  /* VD_F32 | VD_F64 */
+    double d0, d1;              /* cell sizes along axis 0 and axis 1 */
+    const double* lambda_host;  /* [nsys] */
+    const double* mask_host;    /* [n0][n1], or NULL (no mask) */
+    const double* coef_u_host;  /* [n0+1][n1] coefficient on axis-0 edges */
+    const double* coef_v_host;  /* [n0][n1+1] coefficient on axis-1 edges */
+    int n_levels;               /* 0: compute_nlevels (helmholtz_multigrid.py:27-33) */
+    int max_ite;                /* final V-cycles (the reference's default is 20) */
+    int niter_bottom;           /* <= 0: pseudo-inverse bottom solve */
+} vd_mg_desc;
+
+vd_status vd_mg_plan_create(vd_mg_plan** out, const vd_mg_desc* desc);
+vd_status vd_mg_plan_destroy(vd_mg_plan* plan);
+int vd_mg_levels(const vd_mg_plan* plan);
+size_t vd_mg_workspace_bytes(const vd_mg_plan* plan);
+/* f = FMG_Helmholtz(rhs) (helmholtz_multigrid.py:380-419). */
+vd_status vd_mg_solve(const vd_mg_plan* plan, const void* rhs, void* f, void* workspace,
+                      size_t workspace_bytes, void* stream);
+/* res = rhs - H f on the finest level (helmholtz_multigrid.py:102-114). */
+vd_status vd_mg_residual(const vd_mg_plan* plan, const void* f, const void* rhs, void* res,
+                         void* stream);
+
 /* Version / build information string. */
 const char* vd_version(void);
 /* Number of kernels this library has launched in the process so far (also

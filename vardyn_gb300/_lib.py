@@ -72,6 +72,18 @@ class VdBmParams(ctypes.Structure):
     ]
 
 
+class VdMgDesc(ctypes.Structure):
+    _fields_ = [
+        ("n0", ctypes.c_int), ("n1", ctypes.c_int), ("nsys", ctypes.c_int), ("dtype", ctypes.c_int),
+        ("d0", ctypes.c_double), ("d1", ctypes.c_double),
+        ("lambda_host", ctypes.POINTER(ctypes.c_double)),
+        ("mask_host", ctypes.POINTER(ctypes.c_double)),
+        ("coef_u_host", ctypes.POINTER(ctypes.c_double)),
+        ("coef_v_host", ctypes.POINTER(ctypes.c_double)),
+        ("n_levels", ctypes.c_int), ("max_ite", ctypes.c_int), ("niter_bottom", ctypes.c_int),
+    ]
+
+
 P = ctypes.c_void_p
 I = ctypes.c_int
 LL = ctypes.c_longlong
@@ -127,6 +139,12 @@ SIGNATURES = {
     "vd_basis_project": (I, [P, I, I, P, LL, P, I, P, SZ, P]),
     "vd_basis_project_T": (I, [P, I, I, P, P, LL, P, SZ, P]),
     "vd_fill": (I, [I, LL, D, P, P]),
+    "vd_mg_plan_create": (I, [ctypes.POINTER(P), ctypes.POINTER(VdMgDesc)]),
+    "vd_mg_plan_destroy": (I, [P]),
+    "vd_mg_levels": (I, [P]),
+    "vd_mg_workspace_bytes": (SZ, [P]),
+    "vd_mg_solve": (I, [P, P, P, P, SZ, P]),
+    "vd_mg_residual": (I, [P, P, P, P, P]),
     "vd_bm_plan_create": (I, [ctypes.POINTER(P), ctypes.POINTER(VdBasisGrid), ctypes.POINTER(VdBmParams)]),
     "vd_bm_plan_destroy": (I, [P]),
     "vd_bm_nbasis": (LL, [P]),
