@@ -398,6 +398,27 @@ vd_status vd_mg_solve(const vd_mg_plan* plan, const void* rhs, void* f, void* wo
 vd_status vd_mg_residual(const vd_mg_plan* plan, const void* f, const void* rhs, void* res,
                          void* stream);
 
+/* ------------------------------------------------------------------------
+ * Spectral Helmholtz helpers (mapping/models/model_qgsw/helmholtz.py). The
+ * DST-I solve of one mode, div grad u - s u = rhs with Dirichlet walls
+ * (solve_helmholtz_dstI, 138-143), is vd_qg1l_pv2h of a plan built with
+ * g = f = 1 and c = 1/sqrt(s) on the (n0+1) x (n1+1) field.
+ * ---------------------------------------------------------------------- */
+/* dst[f][i][j] = src[f][clamp(i, 1, n0-2)][clamp(j, 1, n1-2)] * mask[i][j]
+ * for nfield [n0][n1] fields: the walls take the nearest interior value
+ * (jnp.pad mode='edge'), then the optional [n0][n1] mask multiplies. In place
+ * (src == dst) only without a mask. */
+vd_status vd_edge_pad(int dtype, int nfield, int n0, int n1, const void* src,
+                      const void* mask, void* dst, void* stream);
+/* Capacitance correction of solve_helmholtz_dstI_cmm (172-184) for nsys
+ * systems of nper fields each (field f = s * nper + r, system-major):
+ * out = rhs, then out[f][bidx[i]] += sum_j cap[s][i][j] * (-sol[f][bidx[j]])
+ * for the M irregular-boundary points bidx (flat indices into a field of
+ * field_elems elements; cap is [nsys][M][M]). out may alias rhs, not sol. */
+vd_status vd_cmm_correct(int dtype, int nsys, int nper, int M, long long field_elems,
+                         const void* cap, const int32_t* bidx, const void* sol,
+                         const void* rhs, void* out, void* stream);
+
 /* Version / build information string. */
 const char* vd_version(void);
 /* Number of kernels this library has launched in the process so far (also

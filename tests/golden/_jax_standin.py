@@ -1,5 +1,7 @@
 """NumPy stand-in for the parts of ``jax`` that the reference's QG 1.5-layer
-model source (mapping/models/model_qg1l/jqgm.py) touches on its forward path.
+model source (mapping/models/model_qg1l/jqgm.py) and its spectral Helmholtz
+solvers (mapping/models/model_qgsw/helmholtz.py) touch on their forward
+paths.
 
 Fixture generation only: ``gen_golden.py`` installs these modules in
 ``sys.modules`` and then loads the reference's own ``jqgm.py`` source, so that
@@ -114,7 +116,9 @@ def install(enable_x64=True):
 
     mpl = types.ModuleType("matplotlib")
     pylab = types.ModuleType("matplotlib.pylab")
+    pyplot = types.ModuleType("matplotlib.pyplot")
     mpl.pylab = pylab
+    mpl.pyplot = pyplot
 
     src = types.ModuleType("src")
     src_config = types.ModuleType("src.config")
@@ -125,6 +129,6 @@ def install(enable_x64=True):
         "jax": jax, "jax.numpy": jnp, "jax.numpy.fft": jnp.fft,
         "jax.lax": lax, "jax.scipy": jsp, "jax.scipy.sparse": jsp_sparse,
         "jax.scipy.sparse.linalg": jsp_linalg,
-        "matplotlib": mpl, "matplotlib.pylab": pylab,
+        "matplotlib": mpl, "matplotlib.pylab": pylab, "matplotlib.pyplot": pyplot,
         "src": src, "src.config": src_config,
     })

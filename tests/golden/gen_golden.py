@@ -98,6 +98,36 @@ def sf_case(ref, out):
         out[f"sf_step_{scheme}"] = np.asarray(m.step(J(ssh), J(hb), nstep=3))
 
 
+def helm_case(ref_root, out):
+    """Spectral Helmholtz solvers of mapping/models/model_qgsw/helmholtz.py:
+    DST-I solve with edge padding (138-143) for two modes, capacitance
+    matrices (146-169) and the capacitance-matrix solve (172-184) on a
+    domain with an island."""
+    sys.path.insert(0, os.path.join(ref_root, "mapping", "models", "model_qgsw"))
+    path = os.path.join(ref_root, "mapping", "models", "model_qgsw", "helmholtz.py")
+    hm = SourceFileLoader("helmholtz_reference", path).load_module()
+    rng = np.random.default_rng(77)
+    nx, ny, dx, dy = 40, 30, 2.0e3, 2.5e3
+    f0, lam = 1.0e-4, np.array([0.0, 3.0e-1 * 1e-6 / 1e-8])
+    lap = np.asarray(hm.compute_laplace_dstI(nx, ny, dx, dy, {"dtype": np.float64}))
+    helm = J(lap[None, None] - f0 ** 2 * lam.reshape(1, 2, 1, 1))
+    rhs = J(rng.standard_normal((1, 2, nx - 1, ny - 1)))
+    out["helm_lam"] = lam
+    out["helm_rhs"] = np.asarray(rhs)
+    out["helm_dst_sol"] = np.asarray(hm.solve_helmholtz_dstI(rhs, helm))
+    mask = np.ones((nx + 1, ny + 1))
+    mask[0, :] = mask[-1, :] = 0
+    mask[:, 0] = mask[:, -1] = 0
+    mask[14:20, 10:16] = 0                       # island on the W grid
+    isl = np.argwhere(mask[1:-1, 1:-1] == 0)     # its cells in interior indices
+    bx, by = isl[:, 0], isl[:, 1]
+    cap = hm.compute_capacitance_matrices(helm, bx, by)
+    out["helm_mask"] = mask
+    out["helm_bx"], out["helm_by"] = bx, by
+    out["helm_cap"] = np.asarray(cap)
+    out["helm_cmm_sol"] = np.asarray(hm.solve_helmholtz_dstI_cmm(rhs, helm, cap, bx, by, J(mask)))
+
+
 def c1_case(ref, out):
     """128x128, dx=dy=10 km, f0=1e-4, c=2.7, dt=1200 s, 72 steps, hb=0."""
     from vardyn_gb300.synthetic import kminus3_ssh
@@ -119,6 +149,7 @@ def main():
     out = {}
     small_case(ref, out)
     sf_case(ref, out)
+    helm_case(ref_root, out)
     c1_case(ref, out)
     np.savez_compressed(os.path.join(HERE, "qg1l_golden.npz"), **out)
     print("wrote", sorted(out))

@@ -139,6 +139,8 @@ SIGNATURES = {
     "vd_basis_project": (I, [P, I, I, P, LL, P, I, P, SZ, P]),
     "vd_basis_project_T": (I, [P, I, I, P, P, LL, P, SZ, P]),
     "vd_fill": (I, [I, LL, D, P, P]),
+    "vd_edge_pad": (I, [I, I, I, I, P, P, P, P]),
+    "vd_cmm_correct": (I, [I, I, I, I, LL, P, P, P, P, P, P]),
     "vd_mg_plan_create": (I, [ctypes.POINTER(P), ctypes.POINTER(VdMgDesc)]),
     "vd_mg_plan_destroy": (I, [P]),
     "vd_mg_levels": (I, [P]),
