@@ -419,6 +419,95 @@ vd_status vd_cmm_correct(int dtype, int nsys, int nper, int M, long long field_e
                          const void* cap, const int32_t* bidx, const void* sol,
                          const void* rhs, void* out, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Multilayer rotating shallow-water model (mapping/models/model_qgsw/sw.py
+ * SW with masks.py, flux.py, reconstruction.py, finite_diff.py).
+ * Layout is the reference's: [batch][layer][x][y], y contiguous; u fields
+ * are [nx+1][ny], v fields [nx][ny+1], h fields [nx][ny]. Step inputs and
+ * outputs are physical fields (SW.step, sw.py:752-904).
+ * ---------------------------------------------------------------------- */
+typedef struct vd_sw_plan vd_sw_plan;
+
+typedef struct vd_sw_desc {
+    int nx, ny, nl;               /* nl <= 8 */
+    int dtype;                    /* VD_F32 / VD_F64 */
+    const double* dx_host;        /* [nx][ny] metric terms (sw.py:142-167) */
+    const double* dy_host;        /* [nx][ny] */
+    const double* f_host;         /* [nx+1][ny+1] Coriolis on the vorticity grid */
+    const double* H_host;         /* [nl] or, with H_spatial, [nl][nx][ny] */
+    int H_spatial;
+    const double* g_prime_host;   /* [nl] */
+    const double* mask_host;      /* [nx][ny] 0/1 ocean mask, NULL = all ocean */
+    double slip_coef;             /* 1 free slip, 0 no slip */
+    double bottom_drag_coef;
+    double rho_water;             /* <= 0: 1025 */
+    double h_min;                 /* minimum thickness of smooth_clamp (0.1) */
+    double h_min_sharpness;       /* <= 0: 10 */
+    double visc_coef, diff_coef;
+    double dt;
+    double sponge_coef;
+    int flag_linear;
+    int forcing_momentum;         /* 0 'direct', 1 'mass_consistent' */
+    int h_wind_mode;              /* 0 none (reference thickness), 1 scalar, 2 field */
+    double h_wind_scalar;
+    const double* h_wind_host;    /* [nx][ny] */
+    double taux_scalar, tauy_scalar;
+    const double* taux_host;      /* [nx-1][ny] or NULL (scalar) */
+    const double* tauy_host;      /* [nx][ny-1] or NULL (scalar) */
+    const double* sponge_u_host;  /* [nx+1][ny] or NULL */
+    const double* sponge_v_host;  /* [nx][ny+1] or NULL */
+    const double* sponge_h_host;  /* [nx][ny] or NULL */
+} vd_sw_desc;
+
+/* Host-only: the flag bytes of the staggered masks (masks.py:57-158).
+ * fh [nx][ny] bit0 mask_h; fu [nx+1][ny] bit0 mask_u, bits 1-3 h-stencil
+ * eq2/eq4/gt6 along x, bits 4-6 w-stencil eq2/eq4/gt4 along y; fv
+ * [nx][ny+1] bit0 mask_v, bits 1-3 h-stencil along y, bits 4-6 w-stencil
+ * eq2/eq4/gt6 along x; fw [nx+1][ny+1] bits valid, cornerout, vertical,
+ * horizontal boundary, w, psi. Any output may be NULL. */
+vd_status vd_sw_masks(int nx, int ny, const double* mask, uint8_t* fh, uint8_t* fu,
+                      uint8_t* fv, uint8_t* fw);
+vd_status vd_sw_plan_create(vd_sw_plan** out, const vd_sw_desc* desc);
+void vd_sw_plan_destroy(vd_sw_plan* plan);
+size_t vd_sw_workspace_bytes(const vd_sw_plan* plan, int batch, int nstep);
+/* nstep RK3-SSP steps. ub/vb/hb (sponge targets) default to the initial
+ * state, Fu/Fv/Fh (forcing) to zero, taux [nx-1][ny] / tauy [nx][ny-1] to
+ * the plan's wind stress; all are physical, all nullable (in groups of
+ * three). */
+vd_status vd_sw_step(vd_sw_plan* plan, int batch, const void* u0, const void* v0,
+                     const void* h0, int nstep, const void* ub, const void* vb,
+                     const void* hb, const void* Fu, const void* Fv, const void* Fh,
+                     const void* taux, const void* tauy, void* u1, void* v1, void* h1,
+                     void* work, size_t work_bytes, void* stream);
+/* Tangent linear of vd_sw_step (jax.jvp, sw.py:906-922) in the initial state
+ * and, optionally, the sponge targets and the forcing. */
+vd_status vd_sw_step_tgl(vd_sw_plan* plan, int batch, const void* u0, const void* v0,
+                         const void* h0, const void* du0, const void* dv0, const void* dh0,
+                         int nstep, const void* ub, const void* vb, const void* hb,
+                         const void* dub, const void* dvb, const void* dhb,
+                         const void* Fu, const void* Fv, const void* Fh,
+                         const void* dFu, const void* dFv, const void* dFh,
+                         const void* taux, const void* tauy, void* du1, void* dv1,
+                         void* dh1, void* work, size_t work_bytes, void* stream);
+/* Adjoint of vd_sw_step (jax.vjp, sw.py:924-938): overwrites adu0/adv0/adh0;
+ * writes the adjoints of the sponge targets and of the forcing when asked
+ * (when the targets default to the initial state their adjoint is part of
+ * adu0/adv0/adh0). Atomic accumulation: results agree to rounding, not bit
+ * for bit, between runs. */
+vd_status vd_sw_step_adj(vd_sw_plan* plan, int batch, const void* u0, const void* v0,
+                         const void* h0, const void* adu1, const void* adv1,
+                         const void* adh1, int nstep, const void* ub, const void* vb,
+                         const void* hb, const void* Fu, const void* Fv, const void* Fh,
+                         const void* taux, const void* tauy, void* adu0, void* adv0,
+                         void* adh0, void* adub, void* advb, void* adhb, void* adFu,
+                         void* adFv, void* adFh, void* work, size_t work_bytes,
+                         void* stream);
+/* compute_time_derivatives (sw.py:720-750) of model-space fields (u dx,
+ * v dy, h area), without sponge. */
+vd_status vd_sw_rhs(vd_sw_plan* plan, int batch, const void* u, const void* v,
+                    const void* h, const void* taux, const void* tauy, void* du, void* dv,
+                    void* dh, void* work, size_t work_bytes, void* stream);
+
 /* Version / build information string. */
 const char* vd_version(void);
 /* Number of kernels this library has launched in the process so far (also

@@ -1,7 +1,8 @@
 """NumPy stand-in for the parts of ``jax`` that the reference's QG 1.5-layer
-model source (mapping/models/model_qg1l/jqgm.py) and its spectral Helmholtz
-solvers (mapping/models/model_qgsw/helmholtz.py) touch on their forward
-paths.
+model source (mapping/models/model_qg1l/jqgm.py), its spectral Helmholtz
+solvers (mapping/models/model_qgsw/helmholtz.py) and its shallow-water / QG
+models (mapping/models/model_qgsw/sw.py, qg.py and their helpers) touch on
+their forward paths.
 
 Fixture generation only: ``gen_golden.py`` installs these modules in
 ``sys.modules`` and then loads the reference's own ``jqgm.py`` source, so that
@@ -11,7 +12,11 @@ NumPy float64 arithmetic in place of XLA. Nothing else imports this file.
 Semantics kept from jax.numpy:
 - ``x.at[idx].set(v)`` / ``.add(v)`` return a modified copy (functional update);
 - ``jit`` is the identity (it only traces/compiles in jax);
-- ``jnp.fft.irfft`` is NumPy's pocketfft with the same ``norm`` meaning.
+- ``jnp.fft.irfft`` is NumPy's pocketfft with the same ``norm`` meaning;
+- ``lax.scan`` is a Python loop, ``checkpoint`` the identity (it only changes
+  what reverse mode stores), ``lax.reduce_window`` a sliding-window reduction,
+  ``nn.softplus`` is log(1 + e^x) by ``logaddexp``;
+- ``jnp.clip(x, a_min=...)`` accepts a missing bound, as jax's does.
 ``jvp``/``vjp`` are not provided: the tangent/adjoint golden checks use finite
 differences of this forward instead.
 """
@@ -86,6 +91,33 @@ def _jit(fun=None, **kwargs):
     return fun
 
 
+def _scan(f, init, xs, length=None, **kwargs):
+    carry, ys = init, []
+    n = length if xs is None else len(xs)
+    for k in range(n):
+        carry, y = f(carry, None if xs is None else xs[k])
+        ys.append(y)
+    return carry, (None if all(y is None for y in ys) else np.stack(ys))
+
+
+def _reduce_window(x, init, op, window_shape, window_strides, padding):
+    """lax.reduce_window for the sums that tools.avg_pool2d asks for."""
+    assert padding == "VALID"
+    x = np.asarray(x)
+    win = np.lib.stride_tricks.sliding_window_view(x, window_shape)
+    red = init + win.sum(axis=tuple(range(x.ndim, 2 * x.ndim)))
+    sl = tuple(slice(None, None, s) for s in window_strides)
+    return np.ascontiguousarray(red[sl]).view(JArray)
+
+
+def _clip(a, a_min=None, a_max=None, **kwargs):
+    return np.clip(a, a_min, a_max).view(JArray)
+
+
+def _softplus(x):
+    return np.logaddexp(np.asarray(x), 0.0).view(JArray)
+
+
 def _unavailable(*args, **kwargs):
     raise NotImplementedError("not available in the NumPy stand-in")
 
@@ -95,16 +127,25 @@ def install(enable_x64=True):
     jax = types.ModuleType("jax")
     jnp = _NumpyNamespace("jax.numpy", np)
     jnp.fft = _NumpyNamespace("jax.numpy.fft", np.fft)
+    jnp.linalg = _NumpyNamespace("jax.numpy.linalg", np.linalg)
+    jnp.clip = _clip
     jax.numpy = jnp
     jax.jit = _jit
+    jax.checkpoint = lambda f, **kw: f
+    nn = types.ModuleType("jax.nn")
+    nn.softplus = _softplus
+    jax.nn = nn
     jax.jvp = _unavailable
     jax.vjp = _unavailable
     jax.vmap = _unavailable
     cfg = types.SimpleNamespace(update=lambda *a, **k: None)
     jax.config = cfg
     lax = types.ModuleType("jax.lax")
-    for name in ("scan", "fori_loop", "dynamic_slice", "dynamic_update_slice"):
+    for name in ("fori_loop", "dynamic_slice", "dynamic_update_slice"):
         setattr(lax, name, _unavailable)
+    lax.scan = _scan
+    lax.reduce_window = _reduce_window
+    lax.add = np.add
     jax.lax = lax
     jsp = types.ModuleType("jax.scipy")
     jsp_sparse = types.ModuleType("jax.scipy.sparse")
@@ -127,7 +168,7 @@ def install(enable_x64=True):
 
     sys.modules.update({
         "jax": jax, "jax.numpy": jnp, "jax.numpy.fft": jnp.fft,
-        "jax.lax": lax, "jax.scipy": jsp, "jax.scipy.sparse": jsp_sparse,
+        "jax.lax": lax, "jax.nn": nn, "jax.numpy.linalg": jnp.linalg, "jax.scipy": jsp, "jax.scipy.sparse": jsp_sparse,
         "jax.scipy.sparse.linalg": jsp_linalg,
         "matplotlib": mpl, "matplotlib.pylab": pylab, "matplotlib.pyplot": pyplot,
         "src": src, "src.config": src_config,

@@ -84,6 +84,25 @@ class VdMgDesc(ctypes.Structure):
     ]
 
 
+_DP = ctypes.POINTER(ctypes.c_double)
+
+
+class VdSwDesc(ctypes.Structure):
+    _fields_ = [
+        ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nl", ctypes.c_int), ("dtype", ctypes.c_int),
+        ("dx_host", _DP), ("dy_host", _DP), ("f_host", _DP), ("H_host", _DP), ("H_spatial", ctypes.c_int),
+        ("g_prime_host", _DP), ("mask_host", _DP),
+        ("slip_coef", ctypes.c_double), ("bottom_drag_coef", ctypes.c_double), ("rho_water", ctypes.c_double),
+        ("h_min", ctypes.c_double), ("h_min_sharpness", ctypes.c_double), ("visc_coef", ctypes.c_double),
+        ("diff_coef", ctypes.c_double), ("dt", ctypes.c_double), ("sponge_coef", ctypes.c_double),
+        ("flag_linear", ctypes.c_int), ("forcing_momentum", ctypes.c_int), ("h_wind_mode", ctypes.c_int),
+        ("h_wind_scalar", ctypes.c_double), ("h_wind_host", _DP),
+        ("taux_scalar", ctypes.c_double), ("tauy_scalar", ctypes.c_double),
+        ("taux_host", _DP), ("tauy_host", _DP),
+        ("sponge_u_host", _DP), ("sponge_v_host", _DP), ("sponge_h_host", _DP),
+    ]
+
+
 P = ctypes.c_void_p
 I = ctypes.c_int
 LL = ctypes.c_longlong
@@ -141,6 +160,16 @@ SIGNATURES = {
     "vd_fill": (I, [I, LL, D, P, P]),
     "vd_edge_pad": (I, [I, I, I, I, P, P, P, P]),
     "vd_cmm_correct": (I, [I, I, I, I, LL, P, P, P, P, P, P]),
+    "vd_sw_masks": (I, [I, I, P, P, P, P, P]),
+    "vd_sw_plan_create": (I, [ctypes.POINTER(P), ctypes.POINTER(VdSwDesc)]),
+    "vd_sw_plan_destroy": (None, [P]),
+    "vd_sw_workspace_bytes": (SZ, [P, I, I]),
+    "vd_sw_step": (I, [P, I, P, P, P, I, P, P, P, P, P, P, P, P, P, P, P, P, SZ, P]),
+    "vd_sw_step_tgl": (I, [P, I, P, P, P, P, P, P, I, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P,
+                           P, SZ, P]),
+    "vd_sw_step_adj": (I, [P, I, P, P, P, P, P, P, I, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P,
+                           P, SZ, P]),
+    "vd_sw_rhs": (I, [P, I, P, P, P, P, P, P, P, P, P, SZ, P]),
     "vd_mg_plan_create": (I, [ctypes.POINTER(P), ctypes.POINTER(VdMgDesc)]),
     "vd_mg_plan_destroy": (I, [P]),
     "vd_mg_levels": (I, [P]),

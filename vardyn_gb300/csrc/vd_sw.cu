@@ -1,0 +1,1938 @@
+// Multilayer rotating shallow-water model (mapping/models/model_qgsw/sw.py
+// SW, with masks.py, flux.py, reconstruction.py, finite_diff.py): forward
+// RK3-SSP steps, their tangent-linear and adjoint, on one GPU.
+//
+// Layout is the reference's: [batch][layer][x][y] with y contiguous; u on
+// (nx+1, ny), v on (nx, ny+1), h on (nx, ny), vorticity on (nx+1, ny+1).
+// Inside the model the prognostic fields carry the metric terms
+// (u*dx, v*dy, h*area; sw.py:84-100).
+//
+// One right-hand side is three kernels:
+//   k_sw_diag    vorticity (sw.py:678-696), KE + pressure (698-718) and the
+//                clamped total thickness (468-481);
+//   k_sw_tend    u and v tendencies (483-568: vortex force by WENO-Z fluxes,
+//                Coriolis, KE + pressure gradient, wind, drag, viscosity) and
+//                the thickness fluxes through the u and v faces;
+//   k_sw_update  thickness divergence and diffusion, sponge and the RK3-SSP
+//                stage combination (831-877).
+// The kernels are templates over the arithmetic type: T for the forward,
+// a one-direction dual number for the tangent-linear (jax.jvp of step,
+// sw.py:906-922). The adjoint (jax.vjp, 924-938) recomputes each step from
+// its stored start and runs hand-written transposes: per face the local
+// gradient of the WENO flux (a 6-direction dual number through the same
+// reconstruction code) is scattered with atomics, then a gather kernel
+// transposes the diagnostics. max(u, 0) takes derivative 1/2 at u = 0, the
+// rule of jax's lax.max.
+#include "vd_internal.cuh"
+
+#include <cstring>
+#include <new>
+#include <type_traits>
+#include <vector>
+
+namespace vd {
+namespace sw {
+
+constexpr int MAXL = 8;
+constexpr double WENO_EPS = 1e-4;   // reconstruction.py:13
+
+// ------------------------------------------------------------------ duals
+template <typename T, int N>
+struct DN {
+    T v;
+    T d[N];
+};
+
+template <typename T> __device__ __forceinline__ T val(T x) { return x; }
+template <typename T, int N> __device__ __forceinline__ T val(const DN<T, N>& x) { return x.v; }
+
+#define DN_BIN(OP, DV)                                                                               \
+    template <typename T, int N>                                                                     \
+    __device__ __forceinline__ DN<T, N> operator OP(const DN<T, N>& a, const DN<T, N>& b)            \
+    {                                                                                                \
+        DN<T, N> r;                                                                                  \
+        r.v = a.v OP b.v;                                                                            \
+        _Pragma("unroll") for (int k = 0; k < N; ++k) r.d[k] = DV;                                   \
+        return r;                                                                                    \
+    }
+DN_BIN(+, a.d[k] + b.d[k])
+DN_BIN(-, a.d[k] - b.d[k])
+DN_BIN(*, a.d[k] * b.v + a.v * b.d[k])
+#undef DN_BIN
+
+template <typename T, int N>
+__device__ __forceinline__ DN<T, N> operator/(const DN<T, N>& a, const DN<T, N>& b)
+{
+    DN<T, N> r;
+    r.v = a.v / b.v;
+    const T ib = T(1) / b.v;
+#pragma unroll
+    for (int k = 0; k < N; ++k) r.d[k] = (a.d[k] - r.v * b.d[k]) * ib;
+    return r;
+}
+template <typename T, int N>
+__device__ __forceinline__ DN<T, N> operator*(T s, const DN<T, N>& a)
+{
+    DN<T, N> r;
+    r.v = s * a.v;
+#pragma unroll
+    for (int k = 0; k < N; ++k) r.d[k] = s * a.d[k];
+    return r;
+}
+template <typename T, int N>
+__device__ __forceinline__ DN<T, N> operator*(const DN<T, N>& a, T s) { return s * a; }
+template <typename T, int N>
+__device__ __forceinline__ DN<T, N> operator+(const DN<T, N>& a, T s)
+{
+    DN<T, N> r = a;
+    r.v = a.v + s;
+    return r;
+}
+template <typename T, int N>
+__device__ __forceinline__ DN<T, N> operator+(T s, const DN<T, N>& a) { return a + s; }
+template <typename T, int N>
+__device__ __forceinline__ DN<T, N> operator-(const DN<T, N>& a, T s)
+{
+    DN<T, N> r = a;
+    r.v = a.v - s;
+    return r;
+}
+template <typename T, int N>
+__device__ __forceinline__ DN<T, N> operator-(T s, const DN<T, N>& a)
+{
+    DN<T, N> r;
+    r.v = s - a.v;
+#pragma unroll
+    for (int k = 0; k < N; ++k) r.d[k] = -a.d[k];
+    return r;
+}
+template <typename T, int N>
+__device__ __forceinline__ DN<T, N> operator-(const DN<T, N>& a)
+{
+    DN<T, N> r;
+    r.v = -a.v;
+#pragma unroll
+    for (int k = 0; k < N; ++k) r.d[k] = -a.d[k];
+    return r;
+}
+template <typename T, int N>
+__device__ __forceinline__ DN<T, N> operator/(const DN<T, N>& a, T s)
+{
+    DN<T, N> r;
+    r.v = a.v / s;
+#pragma unroll
+    for (int k = 0; k < N; ++k) r.d[k] = a.d[k] / s;
+    return r;
+}
+template <typename T, int N>
+__device__ __forceinline__ DN<T, N> operator/(T s, const DN<T, N>& b)
+{
+    DN<T, N> r;
+    r.v = s / b.v;
+    const T f = -r.v / b.v;
+#pragma unroll
+    for (int k = 0; k < N; ++k) r.d[k] = f * b.d[k];
+    return r;
+}
+template <typename T, int N>
+__device__ __forceinline__ DN<T, N> dsqrt(const DN<T, N>& a)
+{
+    DN<T, N> r;
+    r.v = sqrt(a.v);
+    const T f = T(0.5) / r.v;
+#pragma unroll
+    for (int k = 0; k < N; ++k) r.d[k] = f * a.d[k];
+    return r;
+}
+template <typename T> __device__ __forceinline__ T dsqrt(T a) { return sqrt(a); }
+
+// max(x, 0) with jax's tie rule (derivative 1/2 at x = 0)
+template <typename T> __device__ __forceinline__ T relu(T x) { return x > T(0) ? x : T(0); }
+template <typename T, int N>
+__device__ __forceinline__ DN<T, N> relu(const DN<T, N>& x)
+{
+    DN<T, N> r;
+    const T s = x.v > T(0) ? T(1) : (x.v < T(0) ? T(0) : T(0.5));
+    r.v = x.v > T(0) ? x.v : T(0);
+#pragma unroll
+    for (int k = 0; k < N; ++k) r.d[k] = s * x.d[k];
+    return r;
+}
+
+// softplus(x) = log(1 + e^x) (jax.nn.softplus = logaddexp(x, 0)) and its slope
+template <typename T> __device__ __forceinline__ T softplus_v(T x) { return fmax(x, T(0)) + log1p(exp(-fabs(x))); }
+template <typename T> __device__ __forceinline__ T sigmoid_v(T x)
+{
+    if (x >= T(0)) return T(1) / (T(1) + exp(-x));
+    const T e = exp(x);
+    return e / (T(1) + e);
+}
+// smooth_clamp (sw.py:27-33): xmin + softplus((x - xmin) s) / s
+template <typename T> __device__ __forceinline__ T sclamp(T x, T xmin, T s) { return xmin + softplus_v((x - xmin) * s) / s; }
+template <typename T, int N>
+__device__ __forceinline__ DN<T, N> sclamp(const DN<T, N>& x, T xmin, T s)
+{
+    DN<T, N> r;
+    const T z = (x.v - xmin) * s;
+    r.v = xmin + softplus_v(z) / s;
+    const T g = sigmoid_v(z);
+#pragma unroll
+    for (int k = 0; k < N; ++k) r.d[k] = g * x.d[k];
+    return r;
+}
+
+template <typename S> __device__ __forceinline__ S sq(const S& x) { return x * x; }
+
+// ------------------------------------------------------------------ reconstructions
+// wenoz4_left / wenoz6_left (reconstruction.py:98-169)
+template <typename T, typename S>
+__device__ __forceinline__ S wenoz4(const S& qmm, const S& qm, const S& qp, const S& qpp)
+{
+    (void)qpp;
+    const S q1 = T(-0.5) * qmm + T(1.5) * qm;
+    const S q2 = T(0.5) * (qm + qp);
+    const S b1 = sq(qm - qmm), b2 = sq(qp - qm);
+    const S tau = dsqrt(sq(b2 - b1) + T(WENO_EPS * WENO_EPS));
+    const S w1 = T(1.0 / 3.0) * (T(1) + tau / (b1 + T(WENO_EPS)));
+    const S w2 = T(2.0 / 3.0) * (T(1) + tau / (b2 + T(WENO_EPS)));
+    return (w1 * q1 + w2 * q2) / (w1 + w2);
+}
+
+template <typename T, typename S>
+__device__ __forceinline__ S wenoz6(const S& q0, const S& q1, const S& q2, const S& q3, const S& q4, const S& q5)
+{
+    (void)q5;
+    const S r1 = T(1.0 / 3.0) * q0 - T(7.0 / 6.0) * q1 + T(11.0 / 6.0) * q2;
+    const S r2 = T(-1.0 / 6.0) * q1 + T(5.0 / 6.0) * q2 + T(1.0 / 3.0) * q3;
+    const S r3 = T(1.0 / 3.0) * q2 + T(5.0 / 6.0) * q3 - T(1.0 / 6.0) * q4;
+    const T k1 = T(13.0 / 12.0), k2 = T(0.25);
+    const S b1 = k1 * sq(q0 - T(2) * q1 + q2) + k2 * sq(q0 - T(4) * q1 + T(3) * q2);
+    const S b2 = k1 * sq(q1 - T(2) * q2 + q3) + k2 * sq(q1 - q3);
+    const S b3 = k1 * sq(q2 - T(2) * q3 + q4) + k2 * sq(T(3) * q2 - T(4) * q3 + q4);
+    const S tau = dsqrt(sq(b1 - b3) + T(WENO_EPS * WENO_EPS));
+    const S w1 = T(0.1) * (T(1) + tau / (b1 + T(WENO_EPS)));
+    const S w2 = T(0.6) * (T(1) + tau / (b2 + T(WENO_EPS)));
+    const S w3 = T(0.3) * (T(1) + tau / (b3 + T(WENO_EPS)));
+    return (w1 * r1 + w2 * r2 + w3 * r3) / (w1 + w2 + w3);
+}
+
+// Mask bits of one face: 1 = 2-point, 2 = 4-point, 4 = 6-point term.
+// ok4 / ok6: the face is at least 1 / 2 faces from the ends (else that
+// reconstruction is the reference's zero padding).
+template <typename T, typename S>
+__device__ __forceinline__ S recon(const S* q, int bits, bool ok4, bool ok6, bool reverse)
+{
+    S r = T(0) * q[2];
+    if (bits & 1) r = T(0.5) * (q[2] + q[3]);
+    if ((bits & 2) && ok4)
+        r = r + (reverse ? wenoz4<T>(q[4], q[3], q[2], q[1]) : wenoz4<T>(q[1], q[2], q[3], q[4]));
+    if ((bits & 4) && ok6)
+        r = r + (reverse ? wenoz6<T>(q[5], q[4], q[3], q[2], q[1], q[0]) : wenoz6<T>(q[0], q[1], q[2], q[3], q[4], q[5]));
+    return r;
+}
+
+// flux.py:39-90 at one face: q[0..5] = cells k-2..k+3 around face k.
+template <typename T, typename S>
+__device__ __forceinline__ S weno_flux(const S* q, const S& vel, int bits, bool ok4, bool ok6)
+{
+    const S up = relu(vel);
+    const S un = vel - up;
+    return up * recon<T>(q, bits, ok4, ok6, false) + un * recon<T>(q, bits, ok4, ok6, true);
+}
+
+// Local gradient of the face flux: F and dF/dq[0..5], dF/dvel.
+template <typename T>
+__device__ __forceinline__ void weno_flux_grad(const T* q, T vel, int bits, bool ok4, bool ok6, T* g, T& gv)
+{
+    if (vel == T(0)) {
+        const T P = recon<T>(q, bits, ok4, ok6, false), M = recon<T>(q, bits, ok4, ok6, true);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) g[k] = T(0);
+        gv = T(0.5) * (P + M);
+        return;
+    }
+    DN<T, 6> qd[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        qd[k].v = q[k];
+#pragma unroll
+        for (int m = 0; m < 6; ++m) qd[k].d[m] = (k == m) ? T(1) : T(0);
+    }
+    const DN<T, 6> R = recon<T>(qd, bits, ok4, ok6, vel < T(0));
+#pragma unroll
+    for (int k = 0; k < 6; ++k) g[k] = vel * R.d[k];
+    gv = R.v;
+}
+
+// ------------------------------------------------------------------ tables
+template <typename T>
+struct Tab {
+    int nx, ny, nl;
+    long long su, sv, sh, sw;     // per-layer slab sizes
+    const T *dxu, *dyu, *dxv, *dyv, *dxh, *dyh, *area, *areau, *areav;
+    const T *fsu, *fsv;           // f* on the u / v grids
+    const T *wa, *wb;             // omega = wa*dx(v) - wb*dy(u) (sw.py:687-696)
+    const T *wfu, *wfv;           // wind factors dx/(rho H_ref) on interior faces, masked
+    const T *href, *hrefu, *hrefv;   // [nl][...] reference thickness (H times area)
+    const T *dxp, *dyp;           // [nl][nx-1][ny], [nl][nx][ny-1] or null
+    const T *taux, *tauy;         // default wind stress [nx-1][ny], [nx][ny-1]
+    const T *gu, *gv, *gh;        // sponge rates (sponge_coef/dt) * sponge
+    const uint8_t *fh, *fu, *fv;  // flag bytes
+    T G[MAXL];                    // G[l] = sum_{k<=l} g'_k
+    T gp[MAXL];
+    T drag, visc, diff, hmin, sharp, dt;
+    int linear, has_sponge, hxy_dxp, hxy_dyp;
+};
+
+// u flags: 1 mask_u, 2/4/8 h-stencil x eq2/eq4/gt6, 16/32/64 w-stencil y eq2/eq4/gt4
+// v flags: 1 mask_v, 2/4/8 h-stencil y eq2/eq4/gt6, 16/32/64 w-stencil x eq2/eq4/gt6
+// h flags: 1 mask_h
+
+// ------------------------------------------------------------------ accessors
+template <typename T>
+struct R1 {
+    const T* p;
+    __device__ __forceinline__ T operator()(long long i) const { return p[i]; }
+};
+template <typename T>
+struct RD {
+    const T* p;
+    const T* d;
+    __device__ __forceinline__ DN<T, 1> operator()(long long i) const
+    {
+        DN<T, 1> r;
+        r.v = p[i];
+        r.d[0] = d[i];
+        return r;
+    }
+};
+template <typename T>
+struct W1 {
+    T* p;
+    __device__ __forceinline__ void operator()(long long i, T x) const { p[i] = x; }
+};
+template <typename T>
+struct WD {
+    T* p;
+    T* d;
+    __device__ __forceinline__ void operator()(long long i, const DN<T, 1>& x) const
+    {
+        p[i] = x.v;
+        d[i] = x.d[0];
+    }
+};
+
+template <typename R> struct Tri { R u, v, h; };
+
+// ------------------------------------------------------------------ k_sw_diag
+// One thread per (x, y) of the vorticity grid and batch member; loops over
+// layers (pressure is a cumulative sum over layers).
+template <typename T, typename S, typename R, typename W>
+__global__ void k_sw_diag(Tab<T> t, Tri<R> x, W om, W kp, W ht)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    const int b = blockIdx.z;
+    const int nx = t.nx, ny = t.ny, nl = t.nl;
+    if (i > nx || j > ny) return;
+    const long long wi = (long long)i * (ny + 1) + j;
+    const T wa = t.wa[wi], wb = t.wb[wi];
+    const bool hp = (i < nx && j < ny);
+    const long long hi = (long long)i * ny + j;
+    S pacc = T(0) * x.h((long long)b * nl * t.sh);
+    S hl[MAXL];
+    for (int l = 0; l < nl; ++l) {
+        const long long ob = (long long)(b * nl + l);
+        const R& U = x.u;
+        const R& V = x.v;
+        // omega: dx(v) with v = 0 outside x in [0, nx); dy(u) with u = 0 outside y in [0, ny)
+        const S z = T(0) * U(ob * t.su);
+        const S vr = (i < nx) ? V(ob * t.sv + (long long)i * (ny + 1) + j) : z;
+        const S vl = (i > 0) ? V(ob * t.sv + (long long)(i - 1) * (ny + 1) + j) : z;
+        const S uu = (j < ny) ? U(ob * t.su + (long long)i * ny + j) : z;
+        const S ud = (j > 0) ? U(ob * t.su + (long long)i * ny + j - 1) : z;
+        om(ob * t.sw + wi, wa * (vr - vl) - wb * (uu - ud));
+        if (hp) hl[l] = x.h(ob * t.sh + hi);
+    }
+    if (!hp) return;
+    const T mh = (t.fh[hi] & 1) ? T(1) : T(0);
+    const T ar = t.area[hi];
+    // eta_l = sum_{m>=l} h_m / area; p_l = sum_{k<=l} g'_k eta_k (sw.py:705-706)
+    S eta[MAXL];
+    {
+        S acc = hl[nl - 1] / ar;
+        eta[nl - 1] = acc;
+        for (int l = nl - 2; l >= 0; --l) {
+            acc = hl[l] / ar + acc;
+            eta[l] = acc;
+        }
+    }
+    for (int l = 0; l < nl; ++l) {
+        const long long ob = (long long)(b * nl + l);
+        pacc = pacc + t.gp[l] * eta[l];
+        // kinetic energy (finite_diff.py:20-24): 0.25 (u U + ... ) * mask_h
+        const long long u0 = ob * t.su + (long long)i * ny + j, u1 = u0 + ny;
+        const long long v0 = ob * t.sv + (long long)i * (ny + 1) + j, v1 = v0 + 1;
+        const S a = x.u(u1), c = x.u(u0), d = x.v(v1), e = x.v(v0);
+        const T dxu1 = t.dxu[(long long)(i + 1) * ny + j], dxu0 = t.dxu[(long long)i * ny + j];
+        const T dyv1 = t.dyv[(long long)i * (ny + 1) + j + 1], dyv0 = t.dyv[(long long)i * (ny + 1) + j];
+        const S ke = T(0.25) * (a * (a / (dxu1 * dxu1)) + c * (c / (dxu0 * dxu0)) + d * (d / (dyv1 * dyv1)) +
+                                e * (e / (dyv0 * dyv0))) * mh;
+        kp(ob * t.sh + hi, ke + pacc);
+        const T hr = t.href[(long long)l * t.sh + hi];
+        if (t.linear) ht(ob * t.sh + hi, hr + T(0) * hl[l]);
+        else ht(ob * t.sh + hi, sclamp(hr + hl[l], t.hmin * ar, t.sharp));
+    }
+}
+
+// ------------------------------------------------------------------ k_sw_tend
+// u / v tendencies (masked) and the thickness fluxes through interior faces.
+template <typename T, typename S, typename R, typename W>
+__global__ void k_sw_tend(Tab<T> t, Tri<R> x, R om, R kp, R ht, const T* taux, const T* tauy, W tu, W tv, W fx,
+                          W fy)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    const int bl = blockIdx.z;
+    const int nx = t.nx, ny = t.ny, nl = t.nl, l = bl % nl;
+    if (i > nx || j > ny) return;
+    const long long ob = bl;
+    const S z = T(0) * x.h(ob * t.sh);
+    // ---------------- u point (i, j)
+    if (j < ny) {
+        const long long ui = (long long)i * ny + j;
+        const int fl = t.fu[ui];
+        S du = z, F = z;
+        if (i >= 1 && i <= nx - 1) {
+            // V at u points: interp_TP(V) (finite_diff.py:6-7)
+            const long long vb = ob * t.sv;
+            auto Vv = [&](int a, int c) {
+                const long long k = (long long)a * (ny + 1) + c;
+                const T m = t.dyv[k];
+                return x.v(vb + k) / (m * m);
+            };
+            const S Vm = T(0.25) * (Vv(i, j + 1) + Vv(i, j) + Vv(i - 1, j + 1) + Vv(i - 1, j));
+            // vortex force: WENO flux of omega[i][.] along y through face j
+            S q[6];
+            const long long wb = ob * t.sw + (long long)i * (ny + 1);
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                const int jj = j - 2 + k;
+                q[k] = (jj >= 0 && jj <= ny) ? om(wb + jj) : z;
+            }
+            const int bits = (fl >> 4) & 7;
+            const S oVm = weno_flux<T>(q, Vm, bits, j >= 1 && j <= ny - 2, j >= 2 && j <= ny - 3);
+            du = oVm + t.fsu[ui] * Vm;
+            const S kpd = kp(ob * t.sh + ui) - kp(ob * t.sh + ui - ny);
+            du = du - (t.hxy_dxp ? kpd + t.dxp[(long long)l * (nx - 1) * ny + (long long)(i - 1) * ny + j] : kpd);
+            if (l == 0) du = du + (taux ? taux : t.taux)[(long long)(i - 1) * ny + j] * t.wfu[ui];
+            if (l == nl - 1) du = du - t.drag * x.u(ob * t.su + ui);
+            if (t.visc > T(0)) {
+                const long long ub = ob * t.su;
+                auto up = [&](int a, int c) {
+                    c = c < 0 ? 0 : (c > ny - 1 ? ny - 1 : c);
+                    const long long k = (long long)a * ny + c;
+                    return x.u(ub + k) / t.dxu[k];
+                };
+                const T dx = t.dxu[ui], dy = t.dyu[ui];
+                const S c0 = up(i, j);
+                const S lap = (up(i + 1, j) - T(2) * c0 + up(i - 1, j)) / (dx * dx) +
+                              (up(i, j + 1) - T(2) * c0 + up(i, j - 1)) / (dy * dy);
+                du = du + t.visc * lap * dx;
+            }
+            du = du * ((fl & 1) ? T(1) : T(0));
+            // thickness flux along x through u face i
+            const T dxu = t.dxu[ui];
+            const S Uf = x.u(ob * t.su + ui) / (dxu * dxu);
+            S hq[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                const int ii = i - 3 + k;   // cells i-3 .. i+2 around face i (between cells i-1, i)
+                hq[k] = (ii >= 0 && ii < nx) ? ht(ob * t.sh + (long long)ii * ny + j) : z;
+            }
+            F = weno_flux<T>(hq, Uf, (fl >> 1) & 7, i >= 2 && i <= nx - 2, i >= 3 && i <= nx - 3);
+        }
+        tu(ob * t.su + ui, du);
+        fx(ob * t.su + ui, F);
+    }
+    // ---------------- v point (i, j)
+    if (i < nx) {
+        const long long vi = (long long)i * (ny + 1) + j;
+        const int fl = t.fv[vi];
+        S dv = z, F = z;
+        if (j >= 1 && j <= ny - 1) {
+            const long long ub = ob * t.su;
+            auto Uu = [&](int a, int c) {
+                const long long k = (long long)a * ny + c;
+                const T m = t.dxu[k];
+                return x.u(ub + k) / (m * m);
+            };
+            const S Um = T(0.25) * (Uu(i + 1, j) + Uu(i + 1, j - 1) + Uu(i, j) + Uu(i, j - 1));
+            S q[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                const int ii = i - 2 + k;
+                q[k] = (ii >= 0 && ii <= nx) ? om(ob * t.sw + (long long)ii * (ny + 1) + j) : z;
+            }
+            const int bits = (fl >> 4) & 7;
+            const S oUm = weno_flux<T>(q, Um, bits, i >= 1 && i <= nx - 2, i >= 2 && i <= nx - 3);
+            dv = -(oUm + t.fsv[vi] * Um);
+            const long long hi = (long long)i * ny + j;
+            const S kpd = kp(ob * t.sh + hi) - kp(ob * t.sh + hi - 1);
+            dv = dv - (t.hxy_dyp ? kpd + t.dyp[(long long)l * nx * (ny - 1) + (long long)i * (ny - 1) + j - 1] : kpd);
+            if (l == 0) dv = dv + (tauy ? tauy : t.tauy)[(long long)i * (ny - 1) + j - 1] * t.wfv[vi];
+            if (l == nl - 1) dv = dv - t.drag * x.v(ob * t.sv + vi);
+            if (t.visc > T(0)) {
+                const long long vb = ob * t.sv;
+                auto vp = [&](int a, int c) {
+                    a = a < 0 ? 0 : (a > nx - 1 ? nx - 1 : a);
+                    const long long k = (long long)a * (ny + 1) + c;
+                    return x.v(vb + k) / t.dyv[k];
+                };
+                const T dx = t.dxv[vi], dy = t.dyv[vi];
+                const S c0 = vp(i, j);
+                const S lap = (vp(i + 1, j) - T(2) * c0 + vp(i - 1, j)) / (dx * dx) +
+                              (vp(i, j + 1) - T(2) * c0 + vp(i, j - 1)) / (dy * dy);
+                dv = dv + t.visc * lap * dy;
+            }
+            dv = dv * ((fl & 1) ? T(1) : T(0));
+            const T dyv = t.dyv[vi];
+            const S Vf = x.v(ob * t.sv + vi) / (dyv * dyv);
+            S hq[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                const int jj = j - 3 + k;
+                hq[k] = (jj >= 0 && jj < ny) ? ht(ob * t.sh + (long long)i * ny + jj) : z;
+            }
+            F = weno_flux<T>(hq, Vf, (fl >> 1) & 7, j >= 2 && j <= ny - 2, j >= 3 && j <= ny - 3);
+        }
+        tv(ob * t.sv + vi, dv);
+        fy(ob * t.sv + vi, F);
+    }
+}
+
+// ------------------------------------------------------------------ k_sw_update
+// k_s = tendency + sponge; next = RK3-SSP stage combination (+ forcing).
+struct StageArgs {
+    int stage;        // 0, 1, 2
+    int forcing;      // stage 2: add dt*F
+};
+
+template <typename T, typename S, typename R, typename W>
+__global__ void k_sw_update(Tab<T> t, StageArgs sa, Tri<R> x, R tu, R tv, R fx, R fy, Tri<R> k0, Tri<R> k1,
+                            Tri<R> xb, Tri<R> F, Tri<W> ks, Tri<W> nx_)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    const int bl = blockIdx.z;
+    const int nx = t.nx, ny = t.ny;
+    if (i > nx || j > ny) return;
+    const long long ob = bl;
+    const T dt = t.dt;
+    auto combine = [&](const S& xv, const S& k, const R& K0, const R& K1, const R& FF, long long idx, const W& wk,
+                       const W& wn) {
+        if (sa.stage == 0) {
+            wk(idx, k);
+            wn(idx, xv + dt * k);
+        } else if (sa.stage == 1) {
+            wk(idx, k);
+            wn(idx, xv + (dt / T(4)) * (k - T(3) * K0(idx)));
+        } else {
+            S n = xv + (dt / T(12)) * (T(8) * k - K1(idx) - K0(idx));
+            if (sa.forcing) n = n + dt * FF(idx);
+            wn(idx, n);
+        }
+    };
+    if (j < ny) {   // u point
+        const long long ui = (long long)i * ny + j, idx = ob * t.su + ui;
+        const S xv = x.u(idx);
+        S k = tu(idx);
+        if (t.has_sponge) k = k + t.gu[ui] * (xb.u(idx) - xv);
+        combine(xv, k, k0.u, k1.u, F.u, idx, ks.u, nx_.u);
+    }
+    if (i < nx) {   // v point
+        const long long vi = (long long)i * (ny + 1) + j, idx = ob * t.sv + vi;
+        const S xv = x.v(idx);
+        S k = tv(idx);
+        if (t.has_sponge) k = k + t.gv[vi] * (xb.v(idx) - xv);
+        combine(xv, k, k0.v, k1.v, F.v, idx, ks.v, nx_.v);
+    }
+    if (i < nx && j < ny) {   // h point
+        const long long hi = (long long)i * ny + j, idx = ob * t.sh + hi;
+        const S xv = x.h(idx);
+        const T mh = (t.fh[hi] & 1) ? T(1) : T(0);
+        // div_nofluxbc (finite_diff.py:44-52): no x (y) contribution in the
+        // first and last cells along x (y)
+        const S z = T(0) * xv;
+        S dvx = z, dvy = z;
+        if (i >= 1 && i <= nx - 2)
+            dvx = fx(ob * t.su + (long long)(i + 1) * ny + j) - fx(ob * t.su + (long long)i * ny + j);
+        if (j >= 1 && j <= ny - 2)
+            dvy = fy(ob * t.sv + (long long)i * (ny + 1) + j + 1) - fy(ob * t.sv + (long long)i * (ny + 1) + j);
+        S k = -(dvy + dvx) * mh;
+        if (t.diff > T(0)) {
+            auto hp = [&](int a, int c) {
+                a = a < 0 ? 0 : (a > nx - 1 ? nx - 1 : a);
+                c = c < 0 ? 0 : (c > ny - 1 ? ny - 1 : c);
+                const long long q = (long long)a * ny + c;
+                return x.h(ob * t.sh + q) / t.area[q];
+            };
+            const T dx = t.dxh[hi], dy = t.dyh[hi];
+            const S c0 = hp(i, j);
+            const S lap = (hp(i + 1, j) - T(2) * c0 + hp(i - 1, j)) / (dx * dx) +
+                          (hp(i, j + 1) - T(2) * c0 + hp(i, j - 1)) / (dy * dy);
+            k = k + t.diff * lap * t.area[hi] * mh;
+        }
+        if (t.has_sponge) k = k + t.gh[hi] * (xb.h(idx) - xv);
+        combine(xv, k, k0.h, k1.h, F.h, idx, ks.h, nx_.h);
+    }
+}
+
+// ------------------------------------------------------------------ mass-consistent forcing
+// replicate_pad (sw.py:36-48) value at padded cell (pi, pj) of field f.
+template <typename T, typename S, typename R>
+__device__ __forceinline__ S rep_pad(const Tab<T>& t, const R& f, long long base, int pi, int pj)
+{
+    const int nx = t.nx, ny = t.ny;
+    auto cl = [](int a, int n) { return a < 0 ? 0 : (a > n - 1 ? n - 1 : a); };
+    const int ci = cl(pi - 1, nx), cj = cl(pj - 1, ny);
+    if (t.fh[(long long)ci * ny + cj] & 1) return f(base + (long long)ci * ny + cj);
+    S s = T(0) * f(base);
+    int ms = 0;
+    for (int a = pi - 1; a <= pi + 1; ++a)
+        for (int c = pj - 1; c <= pj + 1; ++c) {
+            if (a < 0 || a > nx + 1 || c < 0 || c > ny + 1) continue;
+            const int ai = cl(a - 1, nx), aj = cl(c - 1, ny);
+            s = s + f(base + (long long)ai * ny + aj);
+            ms += (t.fh[(long long)ai * ny + aj] & 1);
+        }
+    return s / T(ms > 1 ? ms : 1);
+}
+
+template <typename T, typename S, typename R, typename W>
+__global__ void k_sw_force_mc(Tab<T> t, Tri<R> x, Tri<R> F, Tri<W> out)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    const int bl = blockIdx.z, l = bl % t.nl;
+    const int nx = t.nx, ny = t.ny;
+    if (i > nx || j > ny) return;
+    const long long ob = bl, hb = ob * t.sh;
+    const T dt = t.dt;
+    if (j < ny) {
+        const long long ui = (long long)i * ny + j, idx = ob * t.su + ui;
+        const S hu = T(0.5) * (rep_pad<T, S>(t, x.h, hb, i + 1, j + 1) + rep_pad<T, S>(t, x.h, hb, i, j + 1));
+        const S fu = T(0.5) * (rep_pad<T, S>(t, F.h, hb, i + 1, j + 1) + rep_pad<T, S>(t, F.h, hb, i, j + 1));
+        const S htu = sclamp(t.hrefu[(long long)l * t.su + ui] + hu, t.hmin * t.areau[ui], t.sharp);
+        const S u = x.u(idx);
+        S n = u + dt * ((-u) / htu * fu);
+        out.u(idx, n + dt * F.u(idx));
+    }
+    if (i < nx) {
+        const long long vi = (long long)i * (ny + 1) + j, idx = ob * t.sv + vi;
+        const S hv = T(0.5) * (rep_pad<T, S>(t, x.h, hb, i + 1, j + 1) + rep_pad<T, S>(t, x.h, hb, i + 1, j));
+        const S fv = T(0.5) * (rep_pad<T, S>(t, F.h, hb, i + 1, j + 1) + rep_pad<T, S>(t, F.h, hb, i + 1, j));
+        const S htv = sclamp(t.hrefv[(long long)l * t.sv + vi] + hv, t.hmin * t.areav[vi], t.sharp);
+        const S v = x.v(idx);
+        S n = v + dt * ((-v) / htv * fv);
+        out.v(idx, n + dt * F.v(idx));
+    }
+    if (i < nx && j < ny) {
+        const long long idx = hb + (long long)i * ny + j;
+        out.h(idx, x.h(idx) + dt * F.h(idx));
+    }
+}
+
+// ------------------------------------------------------------------ conversions
+// set_input_uvh (sw.py:432-450) and get_physical_uvh (421-427); the adjoint
+// of either is the same diagonal scaling.
+template <typename T>
+__global__ void k_sw_scale(Tab<T> t, int nf, int mode, const T* u, const T* v, const T* h, T* uo, T* vo, T* ho)
+{
+    // mode 0: to model (mask, times metric); 1: to physical (divide)
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    const int f = blockIdx.z;
+    const int nx = t.nx, ny = t.ny;
+    if (i > nx || j > ny || f >= nf) return;
+    if (j < ny && u) {
+        const long long k = (long long)i * ny + j, o = f * t.su + k;
+        uo[o] = mode == 0 ? u[o] * ((t.fu[k] & 1) ? T(1) : T(0)) * t.dxu[k] : u[o] / t.dxu[k];
+    }
+    if (i < nx && v) {
+        const long long k = (long long)i * (ny + 1) + j, o = f * t.sv + k;
+        vo[o] = mode == 0 ? v[o] * ((t.fv[k] & 1) ? T(1) : T(0)) * t.dyv[k] : v[o] / t.dyv[k];
+    }
+    if (i < nx && j < ny && h) {
+        const long long k = (long long)i * ny + j, o = f * t.sh + k;
+        ho[o] = mode == 0 ? h[o] * ((t.fh[k] & 1) ? T(1) : T(0)) * t.area[k] : h[o] / t.area[k];
+    }
+}
+
+// ------------------------------------------------------------------ adjoint kernels
+// Reverse of k_sw_update for one stage (elementwise): from the adjoint of the
+// stage output (adn, updated in place to the adjoint of the stage input's
+// direct path) build adk (adjoint of this stage's k) and accumulate the
+// adjoints of the earlier k's and of the sponge target.
+template <typename T>
+__global__ void k_sw_update_adj(Tab<T> t, int stage, int nf, T* adn_u, T* adn_v, T* adn_h, T* adk_u, T* adk_v,
+                                T* adk_h, T* a0_u, T* a0_v, T* a0_h, T* a1_u, T* a1_v, T* a1_h, T* ab_u, T* ab_v,
+                                T* ab_h)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    const int f = blockIdx.z;
+    const int nx = t.nx, ny = t.ny;
+    if (i > nx || j > ny || f >= nf) return;
+    const T dt = t.dt;
+    auto one = [&](long long o, T g, T* an, T* ak, T* a0, T* a1, T* ab) {
+        const T a = an[o];
+        T k;
+        if (stage == 2) {
+            k = (dt / T(12)) * T(8) * a;
+            a1[o] += -(dt / T(12)) * a;
+            a0[o] += -(dt / T(12)) * a;
+        } else if (stage == 1) {
+            k = a1[o] + (dt / T(4)) * a;
+            a0[o] += -(dt / T(4)) * T(3) * a;
+        } else {
+            k = a0[o] + dt * a;
+        }
+        ak[o] = k;
+        if (t.has_sponge) {
+            an[o] = a - g * k;
+            if (ab) ab[o] += g * k;
+        }
+    };
+    if (j < ny) {
+        const long long k = (long long)i * ny + j;
+        one(f * t.su + k, t.has_sponge ? t.gu[k] : T(0), adn_u, adk_u, a0_u, a1_u, ab_u);
+    }
+    if (i < nx) {
+        const long long k = (long long)i * (ny + 1) + j;
+        one(f * t.sv + k, t.has_sponge ? t.gv[k] : T(0), adn_v, adk_v, a0_v, a1_v, ab_v);
+    }
+    if (i < nx && j < ny) {
+        const long long k = (long long)i * ny + j;
+        one(f * t.sh + k, t.has_sponge ? t.gh[k] : T(0), adn_h, adk_h, a0_h, a1_h, ab_h);
+    }
+}
+
+template <typename T> __device__ __forceinline__ void aadd(T* p, T v) { atomicAdd(p, v); }
+
+// Adjoint of k_sw_tend and of the divergence / diffusion part of
+// k_sw_update: scatters into the adjoints of vorticity, KE + pressure and
+// clamped thickness (adom, adkp, adht) and, directly, of u, v, h (adx).
+template <typename T>
+__global__ void k_sw_tend_adj(Tab<T> t, const T* u, const T* v, const T* h, const T* om, const T* ht,
+                              const T* adk_u, const T* adk_v, const T* adk_h, T* adom, T* adkp, T* adht, T* adu,
+                              T* adv, T* adh)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    const int bl = blockIdx.z;
+    const int nx = t.nx, ny = t.ny, nl = t.nl, l = bl % nl;
+    if (i > nx || j > ny) return;
+    const long long ob = bl;
+    const T* hb = adk_h + ob * t.sh;
+    auto mh = [&](long long k) { return (t.fh[k] & 1) ? T(1) : T(0); };
+    // ---------------- u point
+    if (j < ny && i >= 1 && i <= nx - 1) {
+        const long long ui = (long long)i * ny + j;
+        const int fl = t.fu[ui];
+        const T a = adk_u[ob * t.su + ui] * ((fl & 1) ? T(1) : T(0));
+        if (a != T(0)) {
+            const long long vb = ob * t.sv;
+            auto Vv = [&](int p, int c) {
+                const long long k = (long long)p * (ny + 1) + c;
+                const T m = t.dyv[k];
+                return v[vb + k] / (m * m);
+            };
+            const T Vm = T(0.25) * (Vv(i, j + 1) + Vv(i, j) + Vv(i - 1, j + 1) + Vv(i - 1, j));
+            T q[6];
+            const long long wb = ob * t.sw + (long long)i * (ny + 1);
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                const int jj = j - 2 + k;
+                q[k] = (jj >= 0 && jj <= ny) ? om[wb + jj] : T(0);
+            }
+            T g[6], gv;
+            weno_flux_grad<T>(q, Vm, (fl >> 4) & 7, j >= 1 && j <= ny - 2, j >= 2 && j <= ny - 3, g, gv);
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                const int jj = j - 2 + k;
+                if (jj >= 0 && jj <= ny && g[k] != T(0)) aadd(&adom[wb + jj], a * g[k]);
+            }
+            const T aVm = T(0.25) * a * (gv + t.fsu[ui]);
+            auto addV = [&](int p, int c) {
+                const long long k = (long long)p * (ny + 1) + c;
+                const T m = t.dyv[k];
+                aadd(&adv[vb + k], aVm / (m * m));
+            };
+            addV(i, j + 1);
+            addV(i, j);
+            addV(i - 1, j + 1);
+            addV(i - 1, j);
+            aadd(&adkp[ob * t.sh + ui], -a);
+            aadd(&adkp[ob * t.sh + ui - ny], a);
+            const long long ub = ob * t.su;
+            if (l == nl - 1) aadd(&adu[ub + ui], -t.drag * a);
+            if (t.visc > T(0)) {
+                const T dx = t.dxu[ui], dy = t.dyu[ui];
+                const T c = t.visc * dx * a;
+                auto addu = [&](int p, int cc, T w) {
+                    cc = cc < 0 ? 0 : (cc > ny - 1 ? ny - 1 : cc);
+                    const long long k = (long long)p * ny + cc;
+                    aadd(&adu[ub + k], c * w / t.dxu[k]);
+                };
+                addu(i + 1, j, T(1) / (dx * dx));
+                addu(i - 1, j, T(1) / (dx * dx));
+                addu(i, j + 1, T(1) / (dy * dy));
+                addu(i, j - 1, T(1) / (dy * dy));
+                addu(i, j, -T(2) / (dx * dx) - T(2) / (dy * dy));
+            }
+        }
+        // thickness flux through u face i: dt_h[c] = -div_x[c] * mask_h[c]
+        T aF = T(0);
+        if (i - 1 >= 1 && i - 1 <= nx - 2) aF -= mh((long long)(i - 1) * ny + j) * hb[(long long)(i - 1) * ny + j];
+        if (i >= 1 && i <= nx - 2) aF += mh(ui) * hb[ui];
+        if (aF != T(0)) {
+            const T dxu = t.dxu[ui];
+            const T Uf = u[ob * t.su + ui] / (dxu * dxu);
+            T q[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                const int ii = i - 3 + k;
+                q[k] = (ii >= 0 && ii < nx) ? ht[ob * t.sh + (long long)ii * ny + j] : T(0);
+            }
+            T g[6], gv;
+            weno_flux_grad<T>(q, Uf, (fl >> 1) & 7, i >= 2 && i <= nx - 2, i >= 3 && i <= nx - 3, g, gv);
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                const int ii = i - 3 + k;
+                if (ii >= 0 && ii < nx && g[k] != T(0)) aadd(&adht[ob * t.sh + (long long)ii * ny + j], aF * g[k]);
+            }
+            aadd(&adu[ob * t.su + ui], aF * gv / (dxu * dxu));
+        }
+    }
+    // ---------------- v point
+    if (i < nx && j >= 1 && j <= ny - 1) {
+        const long long vi = (long long)i * (ny + 1) + j;
+        const int fl = t.fv[vi];
+        const T a = adk_v[ob * t.sv + vi] * ((fl & 1) ? T(1) : T(0));
+        if (a != T(0)) {
+            const long long ub = ob * t.su;
+            auto Uu = [&](int p, int c) {
+                const long long k = (long long)p * ny + c;
+                const T m = t.dxu[k];
+                return u[ub + k] / (m * m);
+            };
+            const T Um = T(0.25) * (Uu(i + 1, j) + Uu(i + 1, j - 1) + Uu(i, j) + Uu(i, j - 1));
+            T q[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                const int ii = i - 2 + k;
+                q[k] = (ii >= 0 && ii <= nx) ? om[ob * t.sw + (long long)ii * (ny + 1) + j] : T(0);
+            }
+            T g[6], gv;
+            weno_flux_grad<T>(q, Um, (fl >> 4) & 7, i >= 1 && i <= nx - 2, i >= 2 && i <= nx - 3, g, gv);
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                const int ii = i - 2 + k;
+                if (ii >= 0 && ii <= nx && g[k] != T(0)) aadd(&adom[ob * t.sw + (long long)ii * (ny + 1) + j], -a * g[k]);
+            }
+            const T aUm = -T(0.25) * a * (gv + t.fsv[vi]);
+            auto addU = [&](int p, int c) {
+                const long long k = (long long)p * ny + c;
+                const T m = t.dxu[k];
+                aadd(&adu[ub + k], aUm / (m * m));
+            };
+            addU(i + 1, j);
+            addU(i + 1, j - 1);
+            addU(i, j);
+            addU(i, j - 1);
+            const long long hi = (long long)i * ny + j;
+            aadd(&adkp[ob * t.sh + hi], -a);
+            aadd(&adkp[ob * t.sh + hi - 1], a);
+            const long long vb = ob * t.sv;
+            if (l == nl - 1) aadd(&adv[vb + vi], -t.drag * a);
+            if (t.visc > T(0)) {
+                const T dx = t.dxv[vi], dy = t.dyv[vi];
+                const T c = t.visc * dy * a;
+                auto addv = [&](int p, int cc, T w) {
+                    p = p < 0 ? 0 : (p > nx - 1 ? nx - 1 : p);
+                    const long long k = (long long)p * (ny + 1) + cc;
+                    aadd(&adv[vb + k], c * w / t.dyv[k]);
+                };
+                addv(i + 1, j, T(1) / (dx * dx));
+                addv(i - 1, j, T(1) / (dx * dx));
+                addv(i, j + 1, T(1) / (dy * dy));
+                addv(i, j - 1, T(1) / (dy * dy));
+                addv(i, j, -T(2) / (dx * dx) - T(2) / (dy * dy));
+            }
+        }
+        T aF = T(0);
+        const long long hj0 = (long long)i * ny + j - 1, hj1 = (long long)i * ny + j;
+        if (j - 1 >= 1 && j - 1 <= ny - 2) aF -= mh(hj0) * hb[hj0];
+        if (j >= 1 && j <= ny - 2) aF += mh(hj1) * hb[hj1];
+        if (aF != T(0)) {
+            const T dyv = t.dyv[vi];
+            const T Vf = v[ob * t.sv + vi] / (dyv * dyv);
+            T q[6];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                const int jj = j - 3 + k;
+                q[k] = (jj >= 0 && jj < ny) ? ht[ob * t.sh + (long long)i * ny + jj] : T(0);
+            }
+            T g[6], gv;
+            weno_flux_grad<T>(q, Vf, (fl >> 1) & 7, j >= 2 && j <= ny - 2, j >= 3 && j <= ny - 3, g, gv);
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                const int jj = j - 3 + k;
+                if (jj >= 0 && jj < ny && g[k] != T(0)) aadd(&adht[ob * t.sh + (long long)i * ny + jj], aF * g[k]);
+            }
+            aadd(&adv[ob * t.sv + vi], aF * gv / (dyv * dyv));
+        }
+    }
+    // ---------------- thickness diffusion
+    if (i < nx && j < ny && t.diff > T(0)) {
+        const long long hi = (long long)i * ny + j;
+        const T a = hb[hi] * mh(hi) * t.diff * t.area[hi];
+        if (a != T(0)) {
+            const T dx = t.dxh[hi], dy = t.dyh[hi];
+            auto addh = [&](int p, int c, T w) {
+                p = p < 0 ? 0 : (p > nx - 1 ? nx - 1 : p);
+                c = c < 0 ? 0 : (c > ny - 1 ? ny - 1 : c);
+                const long long k = (long long)p * ny + c;
+                aadd(&adh[ob * t.sh + k], a * w / t.area[k]);
+            };
+            addh(i + 1, j, T(1) / (dx * dx));
+            addh(i - 1, j, T(1) / (dx * dx));
+            addh(i, j + 1, T(1) / (dy * dy));
+            addh(i, j - 1, T(1) / (dy * dy));
+            addh(i, j, -T(2) / (dx * dx) - T(2) / (dy * dy));
+        }
+    }
+}
+
+// Adjoint of k_sw_diag (gather): adds into adu, adv, adh.
+template <typename T>
+__global__ void k_sw_diag_adj(Tab<T> t, const T* u, const T* v, const T* h, const T* adom, const T* adkp,
+                              const T* adht, T* adu, T* adv, T* adh)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    const int b = blockIdx.z;
+    const int nx = t.nx, ny = t.ny, nl = t.nl;
+    if (i > nx || j > ny) return;
+    auto mh = [&](int p, int c) { return (t.fh[(long long)p * ny + c] & 1) ? T(1) : T(0); };
+    for (int l = 0; l < nl; ++l) {
+        const long long ob = (long long)(b * nl + l);
+        const T* AO = adom + ob * t.sw;
+        const T* AK = adkp + ob * t.sh;
+        if (j < ny) {   // u point: dy(u) at w (i, j) (+) and (i, j+1) (-); KE of cells i-1, i
+            const long long ui = (long long)i * ny + j, o = ob * t.su + ui;
+            T a = -t.wb[(long long)i * (ny + 1) + j] * AO[(long long)i * (ny + 1) + j] +
+                  t.wb[(long long)i * (ny + 1) + j + 1] * AO[(long long)i * (ny + 1) + j + 1];
+            const T dx = t.dxu[ui];
+            T kk = T(0);
+            if (i >= 1) kk += mh(i - 1, j) * AK[(long long)(i - 1) * ny + j];
+            if (i < nx) kk += mh(i, j) * AK[(long long)i * ny + j];
+            a += T(0.5) * kk * u[o] / (dx * dx);
+            adu[o] += a;
+        }
+        if (i < nx) {   // v point: dx(v) at w (i, j) (+) and (i+1, j) (-); KE of cells j-1, j
+            const long long vi = (long long)i * (ny + 1) + j, o = ob * t.sv + vi;
+            T a = t.wa[(long long)i * (ny + 1) + j] * AO[(long long)i * (ny + 1) + j] -
+                  t.wa[(long long)(i + 1) * (ny + 1) + j] * AO[(long long)(i + 1) * (ny + 1) + j];
+            const T dy = t.dyv[vi];
+            T kk = T(0);
+            if (j >= 1) kk += mh(i, j - 1) * AK[(long long)i * ny + j - 1];
+            if (j < ny) kk += mh(i, j) * AK[(long long)i * ny + j];
+            a += T(0.5) * kk * v[o] / (dy * dy);
+            adv[o] += a;
+        }
+    }
+    if (i < nx && j < ny) {
+        const long long hi = (long long)i * ny + j;
+        const T ar = t.area[hi];
+        // pressure: p_l = sum_m h_m/area * G[min(l, m)]
+        T ap[MAXL];
+        for (int l = 0; l < nl; ++l) ap[l] = adkp[(long long)(b * nl + l) * t.sh + hi];
+        for (int m = 0; m < nl; ++m) {
+            const long long o = (long long)(b * nl + m) * t.sh + hi;
+            T a = T(0);
+            for (int l = 0; l < nl; ++l) a += ap[l] * t.G[l < m ? l : m];
+            a = a / ar;
+            if (!t.linear) {
+                const T z = (t.href[(long long)m * t.sh + hi] + h[o] - t.hmin * ar) * t.sharp;
+                a += adht[o] * sigmoid_v(z);
+            }
+            adh[o] += a;
+        }
+    }
+}
+
+// Adjoint of k_sw_force_mc (scatter to the thickness and Fh of the replicate
+// padding stencil, atomics). adn: adjoint of the output (in place: becomes the
+// adjoint of the input u, v, h direct paths).
+template <typename T>
+__device__ __forceinline__ void rep_pad_adj(const Tab<T>& t, T* ad, long long base, int pi, int pj, T a)
+{
+    const int nx = t.nx, ny = t.ny;
+    auto cl = [](int q, int n) { return q < 0 ? 0 : (q > n - 1 ? n - 1 : q); };
+    const int ci = cl(pi - 1, nx), cj = cl(pj - 1, ny);
+    if (t.fh[(long long)ci * ny + cj] & 1) {
+        aadd(&ad[base + (long long)ci * ny + cj], a);
+        return;
+    }
+    int ms = 0;
+    for (int p = pi - 1; p <= pi + 1; ++p)
+        for (int c = pj - 1; c <= pj + 1; ++c) {
+            if (p < 0 || p > nx + 1 || c < 0 || c > ny + 1) continue;
+            ms += (t.fh[(long long)cl(p - 1, nx) * ny + cl(c - 1, ny)] & 1);
+        }
+    const T w = a / T(ms > 1 ? ms : 1);
+    for (int p = pi - 1; p <= pi + 1; ++p)
+        for (int c = pj - 1; c <= pj + 1; ++c) {
+            if (p < 0 || p > nx + 1 || c < 0 || c > ny + 1) continue;
+            aadd(&ad[base + (long long)cl(p - 1, nx) * ny + cl(c - 1, ny)], w);
+        }
+}
+
+template <typename T>
+__global__ void k_sw_force_mc_adj(Tab<T> t, const T* u, const T* v, const T* h, const T* Fh, T* adu, T* adv,
+                                  T* adh_acc, T* adFh)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    const int bl = blockIdx.z, l = bl % t.nl;
+    const int nx = t.nx, ny = t.ny;
+    if (i > nx || j > ny) return;
+    const long long ob = bl, hb = ob * t.sh;
+    const T dt = t.dt;
+    R1<T> H{h}, FH{Fh};
+    if (j < ny) {
+        const long long ui = (long long)i * ny + j, idx = ob * t.su + ui;
+        const T hu = T(0.5) * (rep_pad<T, T>(t, H, hb, i + 1, j + 1) + rep_pad<T, T>(t, H, hb, i, j + 1));
+        const T fu = T(0.5) * (rep_pad<T, T>(t, FH, hb, i + 1, j + 1) + rep_pad<T, T>(t, FH, hb, i, j + 1));
+        const T xmin = t.hmin * t.areau[ui];
+        const T zz = (t.hrefu[(long long)l * t.su + ui] + hu - xmin) * t.sharp;
+        const T htu = xmin + softplus_v(zz) / t.sharp;
+        const T a = adu[idx];
+        const T uu = u[idx];
+        adu[idx] = a * (T(1) - dt * fu / htu);
+        const T aht = a * dt * uu * fu / (htu * htu) * sigmoid_v(zz);
+        const T afu = -a * dt * uu / htu;
+        rep_pad_adj(t, adh_acc, hb, i + 1, j + 1, T(0.5) * aht);
+        rep_pad_adj(t, adh_acc, hb, i, j + 1, T(0.5) * aht);
+        if (adFh) {
+            rep_pad_adj(t, adFh, hb, i + 1, j + 1, T(0.5) * afu);
+            rep_pad_adj(t, adFh, hb, i, j + 1, T(0.5) * afu);
+        }
+    }
+    if (i < nx) {
+        const long long vi = (long long)i * (ny + 1) + j, idx = ob * t.sv + vi;
+        const T hv = T(0.5) * (rep_pad<T, T>(t, H, hb, i + 1, j + 1) + rep_pad<T, T>(t, H, hb, i + 1, j));
+        const T fv = T(0.5) * (rep_pad<T, T>(t, FH, hb, i + 1, j + 1) + rep_pad<T, T>(t, FH, hb, i + 1, j));
+        const T xmin = t.hmin * t.areav[vi];
+        const T zz = (t.hrefv[(long long)l * t.sv + vi] + hv - xmin) * t.sharp;
+        const T htv = xmin + softplus_v(zz) / t.sharp;
+        const T a = adv[idx];
+        const T vv = v[idx];
+        adv[idx] = a * (T(1) - dt * fv / htv);
+        const T aht = a * dt * vv * fv / (htv * htv) * sigmoid_v(zz);
+        const T afv = -a * dt * vv / htv;
+        rep_pad_adj(t, adh_acc, hb, i + 1, j + 1, T(0.5) * aht);
+        rep_pad_adj(t, adh_acc, hb, i + 1, j, T(0.5) * aht);
+        if (adFh) {
+            rep_pad_adj(t, adFh, hb, i + 1, j + 1, T(0.5) * afv);
+            rep_pad_adj(t, adFh, hb, i + 1, j, T(0.5) * afv);
+        }
+    }
+}
+
+template <typename T>
+__global__ void k_axpy(long long n, T a, const T* x, T* y)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) y[k] += a * x[k];
+}
+template <typename T>
+__global__ void k_copy(long long n, const T* x, T* y)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) y[k] = x[k];
+}
+
+}  // namespace sw
+}  // namespace vd
+
+// ====================================================================== host
+using namespace vd::sw;
+using vd::Arena;
+
+struct vd_sw_plan {
+    vd_sw_desc d;
+    int nx, ny, nl;
+    size_t esz;
+    void* dev;           // one allocation for every table
+    size_t dev_bytes;
+    Tab<float> tf;
+    Tab<double> td;
+    int has_taux, has_tauy;
+};
+
+namespace {
+
+// window sums of a 0/1 field with zero padding (tools.py avg_pool2d)
+struct Grid2 {
+    int n0, n1;
+    std::vector<int> a;
+    int at(int i, int j) const { return (i < 0 || j < 0 || i >= n0 || j >= n1) ? 0 : a[(size_t)i * n1 + j]; }
+};
+static Grid2 pool(const Grid2& g, int k0, int k1, int p0, int p1)
+{
+    Grid2 r;
+    r.n0 = g.n0 + 2 * p0 - k0 + 1;
+    r.n1 = g.n1 + 2 * p1 - k1 + 1;
+    r.a.assign((size_t)r.n0 * r.n1, 0);
+    for (int i = 0; i < r.n0; ++i)
+        for (int j = 0; j < r.n1; ++j) {
+            int s = 0;
+            for (int a = 0; a < k0; ++a)
+                for (int b = 0; b < k1; ++b) s += g.at(i - p0 + a, j - p1 + b);
+            r.a[(size_t)i * r.n1 + j] = s;
+        }
+    return r;
+}
+
+struct SWMasksHost {
+    int nx, ny;
+    std::vector<uint8_t> fh, fu, fv, fw;   // fw bits: 1 valid, 2 cornerout, 4 vertical, 8 horizontal, 16 w, 32 psi
+};
+
+// masks.py:57-158 with averages compared through integer window sums
+static void build_masks(int nx, int ny, const double* mask, SWMasksHost& M)
+{
+    M.nx = nx;
+    M.ny = ny;
+    Grid2 h{nx, ny, std::vector<int>((size_t)nx * ny, 1)};
+    if (mask)
+        for (size_t k = 0; k < h.a.size(); ++k) h.a[k] = mask[k] > 0.5 ? 1 : 0;
+    Grid2 u2 = pool(h, 2, 1, 1, 0), v2 = pool(h, 1, 2, 0, 1), w4 = pool(h, 2, 2, 1, 1);
+    Grid2 U{nx + 1, ny, {}}, V{nx, ny + 1, {}}, W{nx + 1, ny + 1, {}};
+    U.a.resize((size_t)(nx + 1) * ny);
+    V.a.resize((size_t)nx * (ny + 1));
+    W.a.resize((size_t)(nx + 1) * (ny + 1));
+    for (size_t k = 0; k < U.a.size(); ++k) U.a[k] = u2.a[k] == 2;
+    for (size_t k = 0; k < V.a.size(); ++k) V.a[k] = v2.a[k] == 2;
+    for (size_t k = 0; k < W.a.size(); ++k) W.a[k] = w4.a[k] >= 1;
+    Grid2 nv = pool(V, 2, 1, 1, 0), nu = pool(U, 1, 2, 0, 1);
+    M.fw.assign(W.a.size(), 0);
+    for (size_t k = 0; k < W.a.size(); ++k) {
+        const bool w = W.a[k], a = nv.a[k] == 1, b = nu.a[k] == 1;
+        const bool vb = w && a && !b, hb = w && b && !a, co = w && a && b;
+        const bool valid = w && !vb && !hb && !co;
+        M.fw[k] = (valid ? 1 : 0) | (co ? 2 : 0) | (vb ? 4 : 0) | (hb ? 8 : 0) | (w ? 16 : 0) | (w4.a[k] == 4 ? 32 : 0);
+    }
+    M.fh.assign(h.a.size(), 0);
+    for (size_t k = 0; k < h.a.size(); ++k) M.fh[k] = h.a[k] ? 1 : 0;
+    // u grid: h stencils along x, w stencils along y
+    Grid2 hx4 = pool(h, 4, 1, 2, 0), hx6 = pool(h, 6, 1, 3, 0);
+    Grid2 wy2 = pool(W, 1, 2, 0, 0), wy4 = pool(W, 1, 4, 0, 1), wy6 = pool(W, 1, 6, 0, 2);
+    M.fu.assign(U.a.size(), 0);
+    for (size_t k = 0; k < U.a.size(); ++k) {
+        const bool u = U.a[k];
+        const bool heq2 = (u2.a[k] == 2) && hx4.a[k] < 4 && u;
+        const bool hgt4 = !heq2 && u;
+        const bool heq4 = hx6.a[k] < 6 && hgt4;
+        const bool hgt6 = !heq4 && hgt4;
+        const bool weq2 = (wy2.a[k] == 2) && wy4.a[k] < 4 && u;
+        const bool wgt4 = !weq2 && u;
+        const bool weq4 = wy6.a[k] < 6 && wgt4;
+        M.fu[k] = (u ? 1 : 0) | (heq2 ? 2 : 0) | (heq4 ? 4 : 0) | (hgt6 ? 8 : 0) | (weq2 ? 16 : 0) | (weq4 ? 32 : 0) |
+                  (wgt4 ? 64 : 0);
+    }
+    // v grid: h stencils along y, w stencils along x
+    Grid2 hy4 = pool(h, 1, 4, 0, 2), hy6 = pool(h, 1, 6, 0, 3);
+    Grid2 wx2 = pool(W, 2, 1, 0, 0), wx4 = pool(W, 4, 1, 1, 0), wx6 = pool(W, 6, 1, 2, 0);
+    M.fv.assign(V.a.size(), 0);
+    for (size_t k = 0; k < V.a.size(); ++k) {
+        const bool v = V.a[k];
+        const bool heq2 = (v2.a[k] == 2) && hy4.a[k] < 4 && v;
+        const bool hgt4 = !heq2 && v;
+        const bool heq4 = hy6.a[k] < 6 && hgt4;
+        const bool hgt6 = !heq4 && hgt4;
+        const bool weq2 = (wx2.a[k] == 2) && wx4.a[k] < 4 && v;
+        const bool wgt4 = !weq2 && v;
+        const bool weq4 = wx6.a[k] < 6 && wgt4;
+        const bool wgt6 = !weq4 && wgt4;
+        M.fv[k] = (v ? 1 : 0) | (heq2 ? 2 : 0) | (heq4 ? 4 : 0) | (hgt6 ? 8 : 0) | (weq2 ? 16 : 0) | (weq4 ? 32 : 0) |
+                  (wgt6 ? 64 : 0);
+    }
+}
+
+static void edge_avg0(const std::vector<double>& a, int n0, int n1, std::vector<double>& out)
+{   // n0 x n1 -> (n0+1) x n1, 0.5*(edge-padded neighbours) along axis 0
+    out.resize((size_t)(n0 + 1) * n1);
+    for (int i = 0; i <= n0; ++i)
+        for (int j = 0; j < n1; ++j) {
+            const int a0 = i - 1 < 0 ? 0 : i - 1, a1 = i > n0 - 1 ? n0 - 1 : i;
+            out[(size_t)i * n1 + j] = 0.5 * (a[(size_t)a1 * n1 + j] + a[(size_t)a0 * n1 + j]);
+        }
+}
+static void edge_avg1(const std::vector<double>& a, int n0, int n1, std::vector<double>& out)
+{   // n0 x n1 -> n0 x (n1+1) along axis 1
+    out.resize((size_t)n0 * (n1 + 1));
+    for (int i = 0; i < n0; ++i)
+        for (int j = 0; j <= n1; ++j) {
+            const int a0 = j - 1 < 0 ? 0 : j - 1, a1 = j > n1 - 1 ? n1 - 1 : j;
+            out[(size_t)i * (n1 + 1) + j] = 0.5 * (a[(size_t)i * n1 + a1] + a[(size_t)i * n1 + a0]);
+        }
+}
+
+template <typename T>
+static void fill_tab(Tab<T>& t, vd_sw_plan* p, const std::vector<size_t>& off)
+{
+    char* base = (char*)p->dev;
+    int k = 0;
+    auto P = [&](void) -> T* { return (T*)(base + off[k++]); };
+    t.dxu = P(); t.dyu = P(); t.dxv = P(); t.dyv = P(); t.dxh = P(); t.dyh = P(); t.area = P();
+    t.areau = P(); t.areav = P(); t.fsu = P(); t.fsv = P(); t.wa = P(); t.wb = P(); t.wfu = P(); t.wfv = P();
+    t.href = P(); t.hrefu = P(); t.hrefv = P(); t.dxp = P(); t.dyp = P(); t.taux = P(); t.tauy = P();
+    t.gu = P(); t.gv = P(); t.gh = P();
+    t.fh = (const uint8_t*)(base + off[k++]);
+    t.fu = (const uint8_t*)(base + off[k++]);
+    t.fv = (const uint8_t*)(base + off[k++]);
+}
+
+}  // namespace
+
+extern "C" vd_status vd_sw_masks(int nx, int ny, const double* mask, uint8_t* fh, uint8_t* fu, uint8_t* fv,
+                                 uint8_t* fw)
+{
+    if (nx < 2 || ny < 2) return VD_ERR_ARG;
+    SWMasksHost M;
+    build_masks(nx, ny, mask, M);
+    if (fh) std::memcpy(fh, M.fh.data(), M.fh.size());
+    if (fu) std::memcpy(fu, M.fu.data(), M.fu.size());
+    if (fv) std::memcpy(fv, M.fv.data(), M.fv.size());
+    if (fw) std::memcpy(fw, M.fw.data(), M.fw.size());
+    return VD_OK;
+}
+
+extern "C" vd_status vd_sw_plan_create(vd_sw_plan** out, const vd_sw_desc* d)
+{
+    if (!out || !d) return VD_ERR_ARG;
+    *out = nullptr;
+    const int nx = d->nx, ny = d->ny, nl = d->nl;
+    if (nx < 4 || ny < 4 || nl < 1 || nl > MAXL) return VD_ERR_ARG;
+    if (d->dtype != VD_F32 && d->dtype != VD_F64) return VD_ERR_ARG;
+    if (!d->dx_host || !d->dy_host || !d->f_host || !d->H_host || !d->g_prime_host) return VD_ERR_ARG;
+    if (!(d->dt > 0) || d->slip_coef < 0 || d->slip_coef > 1) return VD_ERR_ARG;
+    if (d->forcing_momentum != 0 && d->forcing_momentum != 1) return VD_ERR_ARG;
+    if (d->h_wind_mode < 0 || d->h_wind_mode > 2 || (d->h_wind_mode == 2 && !d->h_wind_host)) return VD_ERR_ARG;
+    const size_t su = (size_t)(nx + 1) * ny, sv = (size_t)nx * (ny + 1), sh = (size_t)nx * ny,
+                 sw = (size_t)(nx + 1) * (ny + 1);
+    SWMasksHost M;
+    build_masks(nx, ny, d->mask_host, M);
+    // metrics (sw.py:147-167)
+    std::vector<double> dx(d->dx_host, d->dx_host + sh), dy(d->dy_host, d->dy_host + sh), dxu, dyu, dxv, dyv;
+    for (size_t k = 0; k < sh; ++k)
+        if (!(dx[k] > 0) || !(dy[k] > 0)) return VD_ERR_ARG;
+    edge_avg0(dx, nx, ny, dxu);
+    edge_avg0(dy, nx, ny, dyu);
+    edge_avg1(dx, nx, ny, dxv);
+    edge_avg1(dy, nx, ny, dyv);
+    std::vector<double> area(sh), areau(su), areav(sv);
+    for (size_t k = 0; k < sh; ++k) area[k] = dx[k] * dy[k];
+    for (size_t k = 0; k < su; ++k) areau[k] = dxu[k] * dyu[k];
+    for (size_t k = 0; k < sv; ++k) areav[k] = dxv[k] * dyv[k];
+    // Coriolis on u / v grids times area (sw.py:193-201); f is [nx+1][ny+1]
+    const double* f = d->f_host;
+    std::vector<double> fsu(su), fsv(sv);
+    for (int i = 0; i <= nx; ++i)
+        for (int j = 0; j < ny; ++j)
+            fsu[(size_t)i * ny + j] = 0.5 * (f[(size_t)i * (ny + 1) + j + 1] + f[(size_t)i * (ny + 1) + j]) *
+                                      areau[(size_t)i * ny + j];
+    for (int i = 0; i < nx; ++i)
+        for (int j = 0; j <= ny; ++j)
+            fsv[(size_t)i * (ny + 1) + j] = 0.5 * (f[(size_t)(i + 1) * (ny + 1) + j] + f[(size_t)i * (ny + 1) + j]) *
+                                           areav[(size_t)i * (ny + 1) + j];
+    // vorticity coefficients (sw.py:687-696)
+    const double slip = d->slip_coef, alpha = 2 * (1 - slip);
+    std::vector<double> wa(sw), wb(sw);
+    for (size_t k = 0; k < sw; ++k) {
+        const int fw = M.fw[k];
+        const double c = ((fw & 1) ? 1.0 : 0.0) + ((fw & 2) ? (1 - slip) : 0.0);
+        wa[k] = c + ((fw & 4) ? alpha : 0.0);
+        wb[k] = c + ((fw & 8) ? alpha : 0.0);
+    }
+    // reference values (sw.py:385-410)
+    const int Hs = d->H_spatial ? 1 : 0;
+    std::vector<double> Hf((size_t)nl * sh);
+    for (int l = 0; l < nl; ++l)
+        for (size_t k = 0; k < sh; ++k) Hf[(size_t)l * sh + k] = Hs ? d->H_host[(size_t)l * sh + k] : d->H_host[l];
+    std::vector<double> href((size_t)nl * sh), hrefu((size_t)nl * su), hrefv((size_t)nl * sv);
+    for (int l = 0; l < nl; ++l) {
+        std::vector<double> hr(sh), a, b;
+        for (size_t k = 0; k < sh; ++k) hr[k] = Hf[(size_t)l * sh + k] * area[k];
+        std::copy(hr.begin(), hr.end(), href.begin() + (size_t)l * sh);
+        edge_avg0(hr, nx, ny, a);
+        edge_avg1(hr, nx, ny, b);
+        std::copy(a.begin(), a.end(), hrefu.begin() + (size_t)l * su);
+        std::copy(b.begin(), b.end(), hrefv.begin() + (size_t)l * sv);
+    }
+    // p_ref = cumsum_l(g'_l * eta_ref_l), eta_ref_l = -sum H + reverse_cumsum(H)_l
+    std::vector<double> pref((size_t)nl * sh);
+    for (size_t k = 0; k < sh; ++k) {
+        double tot = 0;
+        for (int l = 0; l < nl; ++l) tot += Hf[(size_t)l * sh + k];
+        double cs = 0, p = 0;
+        for (int l = 0; l < nl; ++l) {
+            // reverse_cumsum(x)_l = x_l + sum(x) - cumsum(x)_l
+            cs += Hf[(size_t)l * sh + k];
+            const double rc = Hf[(size_t)l * sh + k] + tot - cs;
+            p += d->g_prime_host[l] * (-tot + rc);
+            pref[(size_t)l * sh + k] = p;
+        }
+    }
+    std::vector<double> dxp, dyp;
+    if (Hs) {
+        dxp.assign((size_t)nl * (nx - 1) * ny, 0.0);
+        dyp.assign((size_t)nl * nx * (ny - 1), 0.0);
+        for (int l = 0; l < nl; ++l) {
+            for (int i = 0; i < nx - 1; ++i)
+                for (int j = 0; j < ny; ++j)
+                    dxp[((size_t)l * (nx - 1) + i) * ny + j] =
+                        pref[(size_t)l * sh + (size_t)(i + 1) * ny + j] - pref[(size_t)l * sh + (size_t)i * ny + j];
+            for (int i = 0; i < nx; ++i)
+                for (int j = 0; j < ny - 1; ++j)
+                    dyp[((size_t)l * nx + i) * (ny - 1) + j] =
+                        pref[(size_t)l * sh + (size_t)i * ny + j + 1] - pref[(size_t)l * sh + (size_t)i * ny + j];
+        }
+    }
+    // wind factors (sw.py:570-669): dx_u / (rho H_ref_u) on interior u faces, masked
+    const double rho = d->rho_water > 0 ? d->rho_water : 1025.0, hmin = d->h_min;
+    std::vector<double> wfu(su, 0.0), wfv(sv, 0.0);
+    for (int i = 1; i < nx; ++i)
+        for (int j = 0; j < ny; ++j) {
+            const size_t k = (size_t)i * ny + j;
+            if (!(M.fu[k] & 1)) continue;
+            double Hu;
+            if (d->h_wind_mode == 1) Hu = d->h_wind_scalar;
+            else if (d->h_wind_mode == 2) Hu = 0.5 * (d->h_wind_host[(size_t)(i - 1) * ny + j] + d->h_wind_host[(size_t)i * ny + j]);
+            else Hu = hrefu[k] / areau[k];
+            Hu = Hu > hmin ? Hu : hmin;
+            wfu[k] = dxu[k] / (rho * Hu);
+        }
+    for (int i = 0; i < nx; ++i)
+        for (int j = 1; j < ny; ++j) {
+            const size_t k = (size_t)i * (ny + 1) + j;
+            if (!(M.fv[k] & 1)) continue;
+            double Hv;
+            if (d->h_wind_mode == 1) Hv = d->h_wind_scalar;
+            else if (d->h_wind_mode == 2) Hv = 0.5 * (d->h_wind_host[(size_t)i * ny + j - 1] + d->h_wind_host[(size_t)i * ny + j]);
+            else Hv = hrefv[k] / areav[k];
+            Hv = Hv > hmin ? Hv : hmin;
+            wfv[k] = dyv[k] / (rho * Hv);
+        }
+    // default wind stress
+    std::vector<double> taux((size_t)(nx - 1) * ny), tauy((size_t)nx * (ny - 1));
+    for (size_t k = 0; k < taux.size(); ++k) taux[k] = d->taux_host ? d->taux_host[k] : d->taux_scalar;
+    for (size_t k = 0; k < tauy.size(); ++k) tauy[k] = d->tauy_host ? d->tauy_host[k] : d->tauy_scalar;
+    // sponge rates
+    const double gs = d->sponge_coef / d->dt;
+    std::vector<double> gu(su, 0.0), gv(sv, 0.0), gh(sh, 0.0);
+    int has_sponge = 0;
+    if (d->sponge_u_host) for (size_t k = 0; k < su; ++k) { gu[k] = gs * d->sponge_u_host[k]; has_sponge |= gu[k] != 0; }
+    if (d->sponge_v_host) for (size_t k = 0; k < sv; ++k) { gv[k] = gs * d->sponge_v_host[k]; has_sponge |= gv[k] != 0; }
+    if (d->sponge_h_host) for (size_t k = 0; k < sh; ++k) { gh[k] = gs * d->sponge_h_host[k]; has_sponge |= gh[k] != 0; }
+
+    // ---------------- upload: one allocation
+    const size_t esz = d->dtype == VD_F64 ? 8 : 4;
+    std::vector<const std::vector<double>*> arrs = {&dxu, &dyu, &dxv, &dyv, &dx, &dy, &area, &areau, &areav,
+                                                   &fsu, &fsv, &wa, &wb, &wfu, &wfv, &href, &hrefu, &hrefv,
+                                                   &dxp, &dyp, &taux, &tauy, &gu, &gv, &gh};
+    std::vector<size_t> off;
+    size_t tot = 0;
+    for (auto* a : arrs) {
+        off.push_back(tot);
+        tot += (a->size() * esz + 255) & ~size_t(255);
+    }
+    for (auto* a : {&M.fh, &M.fu, &M.fv}) {
+        off.push_back(tot);
+        tot += (a->size() + 255) & ~size_t(255);
+    }
+    std::vector<char> host(tot, 0);
+    for (size_t a = 0; a < arrs.size(); ++a) {
+        const auto& v = *arrs[a];
+        for (size_t k = 0; k < v.size(); ++k) {
+            if (esz == 8) ((double*)(host.data() + off[a]))[k] = v[k];
+            else ((float*)(host.data() + off[a]))[k] = (float)v[k];
+        }
+    }
+    std::memcpy(host.data() + off[arrs.size()], M.fh.data(), M.fh.size());
+    std::memcpy(host.data() + off[arrs.size() + 1], M.fu.data(), M.fu.size());
+    std::memcpy(host.data() + off[arrs.size() + 2], M.fv.data(), M.fv.size());
+    vd_sw_plan* p = new (std::nothrow) vd_sw_plan();
+    if (!p) return VD_ERR_CUDA;
+    p->d = *d;
+    p->d.mask_host = nullptr; p->d.dx_host = p->d.dy_host = p->d.f_host = p->d.H_host = p->d.g_prime_host = nullptr;
+    p->d.h_wind_host = p->d.taux_host = p->d.tauy_host = nullptr;
+    p->d.sponge_u_host = p->d.sponge_v_host = p->d.sponge_h_host = nullptr;
+    p->nx = nx; p->ny = ny; p->nl = nl; p->esz = esz;
+    if (cudaMalloc(&p->dev, tot) != cudaSuccess) {
+        delete p;
+        return VD_ERR_CUDA;
+    }
+    p->dev_bytes = tot;
+    if (cudaMemcpy(p->dev, host.data(), tot, cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(p->dev);
+        delete p;
+        return VD_ERR_CUDA;
+    }
+    auto common = [&](auto& t) {
+        using TT = std::remove_reference_t<decltype(t.drag)>;
+        t.nx = nx; t.ny = ny; t.nl = nl;
+        t.su = su; t.sv = sv; t.sh = sh; t.sw = sw;
+        double G = 0;
+        for (int l = 0; l < MAXL; ++l) {
+            const double g = l < nl ? d->g_prime_host[l] : 0.0;
+            G += g;
+            t.gp[l] = (TT)g;
+            t.G[l] = (TT)G;
+        }
+        t.drag = (TT)d->bottom_drag_coef; t.visc = (TT)(d->visc_coef > 0 ? d->visc_coef : 0);
+        t.diff = (TT)(d->diff_coef > 0 ? d->diff_coef : 0); t.hmin = (TT)hmin;
+        t.sharp = (TT)(d->h_min_sharpness > 0 ? d->h_min_sharpness : 10.0); t.dt = (TT)d->dt;
+        t.linear = d->flag_linear ? 1 : 0; t.has_sponge = has_sponge; t.hxy_dxp = Hs; t.hxy_dyp = Hs;
+        fill_tab(t, p, off);
+        if (!Hs) { t.dxp = nullptr; t.dyp = nullptr; }
+    };
+    if (esz == 8) common(p->td);
+    else common(p->tf);
+    *out = p;
+    return VD_OK;
+}
+
+extern "C" void vd_sw_plan_destroy(vd_sw_plan* p)
+{
+    if (!p) return;
+    if (p->dev) cudaFree(p->dev);
+    delete p;
+}
+
+// ---------------------------------------------------------------- drivers
+namespace {
+
+template <typename T> Tab<T>& tab(vd_sw_plan* p);
+template <> Tab<float>& tab<float>(vd_sw_plan* p) { return p->tf; }
+template <> Tab<double>& tab<double>(vd_sw_plan* p) { return p->td; }
+
+struct Sizes {
+    long long su, sv, sh, sw;   // per batch member (all layers)
+};
+static Sizes sizes(const vd_sw_plan* p)
+{
+    const long long nl = p->nl, nx = p->nx, ny = p->ny;
+    return {nl * (nx + 1) * ny, nl * nx * (ny + 1), nl * nx * ny, nl * (nx + 1) * (ny + 1)};
+}
+
+template <typename T>
+struct Fields {
+    T *u, *v, *h;
+};
+
+template <typename T>
+static bool take_uvh(Arena& ws, const Sizes& s, int B, Fields<T>& f)
+{
+    f.u = (T*)ws.take(sizeof(T) * s.su * B);
+    f.v = (T*)ws.take(sizeof(T) * s.sv * B);
+    f.h = (T*)ws.take(sizeof(T) * s.sh * B);
+    return f.u && f.v && f.h;
+}
+
+struct Launch {
+    dim3 grid, block;
+};
+static Launch lgrid(const vd_sw_plan* p, int z)
+{
+    Launch L;
+    L.block = dim3(32, 8, 1);
+    L.grid = dim3((unsigned)((p->ny + 1 + 31) / 32), (unsigned)((p->nx + 1 + 7) / 8), (unsigned)z);
+    return L;
+}
+
+// One RK3-SSP run of nstep steps in model space, forward (S = T) or
+// tangent-linear (S = DN<T,1>). State x is advanced in place; traj (forward
+// only) receives the state at the start of every step.
+template <typename T>
+struct Work {
+    Fields<T> x1, x2, k0, k1, tuvh;   // tuvh.u/.v = tendencies, tuvh.h unused
+    T *fx, *fy, *om, *kp, *ht;
+};
+
+template <typename T>
+static int take_work(Arena& ws, const Sizes& s, int B, Work<T>& w)
+{
+    if (!take_uvh(ws, s, B, w.x1) || !take_uvh(ws, s, B, w.x2) || !take_uvh(ws, s, B, w.k0) ||
+        !take_uvh(ws, s, B, w.k1))
+        return VD_ERR_WORKSPACE;
+    w.tuvh.u = (T*)ws.take(sizeof(T) * s.su * B);
+    w.tuvh.v = (T*)ws.take(sizeof(T) * s.sv * B);
+    w.tuvh.h = nullptr;
+    w.fx = (T*)ws.take(sizeof(T) * s.su * B);
+    w.fy = (T*)ws.take(sizeof(T) * s.sv * B);
+    w.om = (T*)ws.take(sizeof(T) * s.sw * B);
+    w.kp = (T*)ws.take(sizeof(T) * s.sh * B);
+    w.ht = (T*)ws.take(sizeof(T) * s.sh * B);
+    if (!w.tuvh.u || !w.tuvh.v || !w.fx || !w.fy || !w.om || !w.kp || !w.ht) return VD_ERR_WORKSPACE;
+    return VD_OK;
+}
+
+template <typename T>
+static size_t work_bytes(const Sizes& s, int B)
+{
+    const size_t F3 = sizeof(T) * (s.su + s.sv + s.sh) * B + 3 * 256;
+    return 4 * F3 + sizeof(T) * (3 * s.su + 3 * s.sv + s.sw + 2 * s.sh) * B + 8 * 256;
+}
+
+template <typename T>
+static R1<T> r(const T* p) { return R1<T>{p}; }
+template <typename T>
+static W1<T> w(T* p) { return W1<T>{p}; }
+template <typename T>
+static Tri<R1<T>> rt(const Fields<T>& f) { return {R1<T>{f.u}, R1<T>{f.v}, R1<T>{f.h}}; }
+template <typename T>
+static Tri<W1<T>> wt(const Fields<T>& f) { return {W1<T>{f.u}, W1<T>{f.v}, W1<T>{f.h}}; }
+template <typename T>
+static Tri<RD<T>> rtd(const Fields<T>& f, const Fields<T>& d) { return {RD<T>{f.u, d.u}, RD<T>{f.v, d.v}, RD<T>{f.h, d.h}}; }
+template <typename T>
+static Tri<WD<T>> wtd(const Fields<T>& f, const Fields<T>& d) { return {WD<T>{f.u, d.u}, WD<T>{f.v, d.v}, WD<T>{f.h, d.h}}; }
+
+// forward step loop
+template <typename T>
+static int run_fwd(vd_sw_plan* p, int B, Fields<T> x, int nstep, Fields<T> xb, Fields<T> F, int hasF, const T* taux,
+                   const T* tauy, Work<T>& wk, Fields<T>* traj, cudaStream_t st)
+{
+    Tab<T>& t = tab<T>(p);
+    const Sizes s = sizes(p);
+    const Launch Ld = lgrid(p, B), Ll = lgrid(p, B * p->nl);
+    const int mc = p->d.forcing_momentum == 1;
+    for (int n = 0; n < nstep; ++n) {
+        if (traj) {
+            k_copy<T><<<(unsigned)((s.su * B + 255) / 256), 256, 0, st>>>(s.su * B, x.u, traj[n].u);
+            VD_LAUNCH_CHECK();
+            k_copy<T><<<(unsigned)((s.sv * B + 255) / 256), 256, 0, st>>>(s.sv * B, x.v, traj[n].v);
+            VD_LAUNCH_CHECK();
+            k_copy<T><<<(unsigned)((s.sh * B + 255) / 256), 256, 0, st>>>(s.sh * B, x.h, traj[n].h);
+            VD_LAUNCH_CHECK();
+        }
+        Fields<T> cur = x;
+        for (int stg = 0; stg < 3; ++stg) {
+            k_sw_diag<T, T><<<Ld.grid, Ld.block, 0, st>>>(t, rt(cur), w(wk.om), w(wk.kp), w(wk.ht));
+            VD_LAUNCH_CHECK();
+            k_sw_tend<T, T><<<Ll.grid, Ll.block, 0, st>>>(t, rt(cur), r<T>(wk.om), r<T>(wk.kp), r<T>(wk.ht), taux,
+                                                           tauy, w(wk.tuvh.u), w(wk.tuvh.v), w(wk.fx), w(wk.fy));
+            VD_LAUNCH_CHECK();
+            Fields<T> nxt = stg == 0 ? wk.x1 : (stg == 1 ? wk.x2 : (mc ? wk.x1 : x));
+            StageArgs sa{stg, (stg == 2 && hasF && !mc) ? 1 : 0};
+            Fields<T> ks = stg == 0 ? wk.k0 : wk.k1;
+            k_sw_update<T, T><<<Ll.grid, Ll.block, 0, st>>>(t, sa, rt(cur), r<T>(wk.tuvh.u), r<T>(wk.tuvh.v),
+                                                             r<T>(wk.fx), r<T>(wk.fy), rt(wk.k0), rt(wk.k1), rt(xb),
+                                                             rt(F), wt(ks), wt(nxt));
+            VD_LAUNCH_CHECK();
+            cur = nxt;
+        }
+        if (mc) {
+            k_sw_force_mc<T, T><<<Ll.grid, Ll.block, 0, st>>>(t, rt(wk.x1), rt(F), wt(x));
+            VD_LAUNCH_CHECK();
+        }
+    }
+    return VD_OK;
+}
+
+// tangent-linear step loop (x, dx advanced in place)
+template <typename T>
+static int run_tgl(vd_sw_plan* p, int B, Fields<T> x, Fields<T> dx, int nstep, Fields<T> xb, Fields<T> dxb,
+                   Fields<T> F, Fields<T> dF, int hasF, const T* taux, const T* tauy, Work<T>& wk, Work<T>& dk,
+                   cudaStream_t st)
+{
+    Tab<T>& t = tab<T>(p);
+    const Launch Ld = lgrid(p, B), Ll = lgrid(p, B * p->nl);
+    const int mc = p->d.forcing_momentum == 1;
+    using S = DN<T, 1>;
+    for (int n = 0; n < nstep; ++n) {
+        Fields<T> cur = x, dcur = dx;
+        for (int stg = 0; stg < 3; ++stg) {
+            k_sw_diag<T, S><<<Ld.grid, Ld.block, 0, st>>>(t, rtd(cur, dcur), WD<T>{wk.om, dk.om}, WD<T>{wk.kp, dk.kp},
+                                                           WD<T>{wk.ht, dk.ht});
+            VD_LAUNCH_CHECK();
+            k_sw_tend<T, S><<<Ll.grid, Ll.block, 0, st>>>(
+                t, rtd(cur, dcur), RD<T>{wk.om, dk.om}, RD<T>{wk.kp, dk.kp}, RD<T>{wk.ht, dk.ht}, taux, tauy,
+                WD<T>{wk.tuvh.u, dk.tuvh.u}, WD<T>{wk.tuvh.v, dk.tuvh.v}, WD<T>{wk.fx, dk.fx}, WD<T>{wk.fy, dk.fy});
+            VD_LAUNCH_CHECK();
+            Fields<T> nxt = stg == 0 ? wk.x1 : (stg == 1 ? wk.x2 : (mc ? wk.x1 : x));
+            Fields<T> dnxt = stg == 0 ? dk.x1 : (stg == 1 ? dk.x2 : (mc ? dk.x1 : dx));
+            StageArgs sa{stg, (stg == 2 && hasF && !mc) ? 1 : 0};
+            Fields<T> ks = stg == 0 ? wk.k0 : wk.k1, dks = stg == 0 ? dk.k0 : dk.k1;
+            k_sw_update<T, S><<<Ll.grid, Ll.block, 0, st>>>(
+                t, sa, rtd(cur, dcur), RD<T>{wk.tuvh.u, dk.tuvh.u}, RD<T>{wk.tuvh.v, dk.tuvh.v}, RD<T>{wk.fx, dk.fx},
+                RD<T>{wk.fy, dk.fy}, rtd(wk.k0, dk.k0), rtd(wk.k1, dk.k1), rtd(xb, dxb), rtd(F, dF), wtd(ks, dks),
+                wtd(nxt, dnxt));
+            VD_LAUNCH_CHECK();
+            cur = nxt;
+            dcur = dnxt;
+        }
+        if (mc) {
+            k_sw_force_mc<T, S><<<Ll.grid, Ll.block, 0, st>>>(t, rtd(wk.x1, dk.x1), rtd(F, dF), wtd(x, dx));
+            VD_LAUNCH_CHECK();
+        }
+    }
+    return VD_OK;
+}
+
+template <typename T>
+static int scale(vd_sw_plan* p, int B, int mode, const T* u, const T* v, const T* h, T* uo, T* vo, T* ho,
+                 cudaStream_t st)
+{
+    const Launch L = lgrid(p, B * p->nl);
+    k_sw_scale<T><<<L.grid, L.block, 0, st>>>(tab<T>(p), B * p->nl, mode, u, v, h, uo, vo, ho);
+    VD_LAUNCH_CHECK();
+    return VD_OK;
+}
+
+template <typename T>
+static int zero(Fields<T> f, const Sizes& s, int B, cudaStream_t st)
+{
+    VD_CUDA_TRY(cudaMemsetAsync(f.u, 0, sizeof(T) * s.su * B, st));
+    VD_CUDA_TRY(cudaMemsetAsync(f.v, 0, sizeof(T) * s.sv * B, st));
+    VD_CUDA_TRY(cudaMemsetAsync(f.h, 0, sizeof(T) * s.sh * B, st));
+    return VD_OK;
+}
+
+template <typename T>
+static int addto(Fields<T> y, T a, Fields<T> x, const Sizes& s, int B, cudaStream_t st)
+{
+    const long long n[3] = {s.su * B, s.sv * B, s.sh * B};
+    T* ys[3] = {y.u, y.v, y.h};
+    const T* xs[3] = {x.u, x.v, x.h};
+    for (int k = 0; k < 3; ++k) {
+        k_axpy<T><<<(unsigned)((n[k] + 255) / 256), 256, 0, st>>>(n[k], a, xs[k], ys[k]);
+        VD_LAUNCH_CHECK();
+    }
+    return VD_OK;
+}
+
+// Inputs shared by the drivers: physical fields (device pointers, nullable
+// where optional) converted to model space in the workspace.
+template <typename T>
+struct Inputs {
+    Fields<T> x, xb, F;
+    int hasb, hasF;
+};
+
+template <typename T>
+static int prep_inputs(vd_sw_plan* p, int B, const void* u0, const void* v0, const void* h0, const void* ub,
+                       const void* vb, const void* hb, const void* Fu, const void* Fv, const void* Fh, Arena& ws,
+                       Inputs<T>& in, cudaStream_t st)
+{
+    const Sizes s = sizes(p);
+    if (!take_uvh(ws, s, B, in.x) || !take_uvh(ws, s, B, in.xb) || !take_uvh(ws, s, B, in.F)) return VD_ERR_WORKSPACE;
+    int rc = scale<T>(p, B, 0, (const T*)u0, (const T*)v0, (const T*)h0, in.x.u, in.x.v, in.x.h, st);
+    if (rc) return rc;
+    in.hasb = (ub || vb || hb) ? 1 : 0;
+    rc = scale<T>(p, B, 0, (const T*)(ub ? ub : u0), (const T*)(vb ? vb : v0), (const T*)(hb ? hb : h0), in.xb.u,
+                  in.xb.v, in.xb.h, st);
+    if (rc) return rc;
+    in.hasF = (Fu || Fv || Fh) ? 1 : 0;
+    if ((rc = zero(in.F, s, B, st))) return rc;
+    if (in.hasF) rc = scale<T>(p, B, 0, (const T*)Fu, (const T*)Fv, (const T*)Fh, in.F.u, in.F.v, in.F.h, st);
+    return rc;
+}
+
+}  // namespace
+
+extern "C" size_t vd_sw_workspace_bytes(const vd_sw_plan* p, int batch, int nstep)
+{
+    if (!p || batch <= 0 || nstep < 0) return 0;
+    const Sizes s = sizes(p);
+    const size_t esz = p->esz;
+    const size_t F3 = esz * (s.su + s.sv + s.sh) * batch + 3 * 256;
+    const size_t wk = (esz == 8 ? work_bytes<double>(s, batch) : work_bytes<float>(s, batch));
+    // inputs (x, xb, F), their tangents / adjoints, two work sets, adjoint
+    // accumulators, and the per-step trajectory
+    return 14 * F3 + 2 * wk + (size_t)nstep * F3 + esz * (s.sw + 2 * s.sh) * batch + 64 * 256;
+}
+
+namespace {
+
+template <typename T>
+static int sw_step_t(vd_sw_plan* p, int B, const void* u0, const void* v0, const void* h0, int nstep, const void* ub,
+                     const void* vb, const void* hb, const void* Fu, const void* Fv, const void* Fh, const void* taux,
+                     const void* tauy, void* u1, void* v1, void* h1, Arena& ws, cudaStream_t st)
+{
+    Inputs<T> in;
+    int rc = prep_inputs<T>(p, B, u0, v0, h0, ub, vb, hb, Fu, Fv, Fh, ws, in, st);
+    if (rc) return rc;
+    Work<T> wk;
+    if ((rc = take_work<T>(ws, sizes(p), B, wk))) return rc;
+    rc = run_fwd<T>(p, B, in.x, nstep, in.xb, in.F, in.hasF, (const T*)taux, (const T*)tauy, wk, nullptr, st);
+    if (rc) return rc;
+    return scale<T>(p, B, 1, in.x.u, in.x.v, in.x.h, (T*)u1, (T*)v1, (T*)h1, st);
+}
+
+template <typename T>
+static int sw_tgl_t(vd_sw_plan* p, int B, const void* u0, const void* v0, const void* h0, const void* du0,
+                    const void* dv0, const void* dh0, int nstep, const void* ub, const void* vb, const void* hb,
+                    const void* dub, const void* dvb, const void* dhb, const void* Fu, const void* Fv, const void* Fh,
+                    const void* dFu, const void* dFv, const void* dFh, const void* taux, const void* tauy, void* du1,
+                    void* dv1, void* dh1, Arena& ws, cudaStream_t st)
+{
+    Inputs<T> in, din;
+    int rc = prep_inputs<T>(p, B, u0, v0, h0, ub, vb, hb, Fu, Fv, Fh, ws, in, st);
+    if (rc) return rc;
+    // tangents: boundary fields default to the initial state's tangent when
+    // the boundary fields themselves default to the initial state
+    const void* tub = ub ? dub : du0;
+    const void* tvb = vb ? dvb : dv0;
+    const void* thb = hb ? dhb : dh0;
+    const Sizes s = sizes(p);
+    if (!take_uvh(ws, s, B, din.x) || !take_uvh(ws, s, B, din.xb) || !take_uvh(ws, s, B, din.F))
+        return VD_ERR_WORKSPACE;
+    if ((rc = scale<T>(p, B, 0, (const T*)du0, (const T*)dv0, (const T*)dh0, din.x.u, din.x.v, din.x.h, st))) return rc;
+    if ((rc = zero(din.xb, s, B, st))) return rc;
+    if ((rc = scale<T>(p, B, 0, (const T*)tub, (const T*)tvb, (const T*)thb, din.xb.u, din.xb.v, din.xb.h, st))) return rc;
+    if ((rc = zero(din.F, s, B, st))) return rc;
+    if ((rc = scale<T>(p, B, 0, (const T*)dFu, (const T*)dFv, (const T*)dFh, din.F.u, din.F.v, din.F.h, st))) return rc;
+    Work<T> wk, dk;
+    if ((rc = take_work<T>(ws, s, B, wk)) || (rc = take_work<T>(ws, s, B, dk))) return rc;
+    rc = run_tgl<T>(p, B, in.x, din.x, nstep, in.xb, din.xb, in.F, din.F, in.hasF || dFu || dFv || dFh,
+                    (const T*)taux, (const T*)tauy, wk, dk, st);
+    if (rc) return rc;
+    return scale<T>(p, B, 1, din.x.u, din.x.v, din.x.h, (T*)du1, (T*)dv1, (T*)dh1, st);
+}
+
+// adjoint of one right-hand side at state x (model space): adk -> adx (+=)
+template <typename T>
+static int rhs_adj(vd_sw_plan* p, int B, Fields<T> x, Fields<T> adk, Fields<T> adx, Work<T>& wk, T* adom, T* adkp,
+                   T* adht, cudaStream_t st)
+{
+    Tab<T>& t = tab<T>(p);
+    const Sizes s = sizes(p);
+    const Launch Ld = lgrid(p, B), Ll = lgrid(p, B * p->nl);
+    k_sw_diag<T, T><<<Ld.grid, Ld.block, 0, st>>>(t, rt(x), w(wk.om), w(wk.kp), w(wk.ht));
+    VD_LAUNCH_CHECK();
+    VD_CUDA_TRY(cudaMemsetAsync(adom, 0, sizeof(T) * s.sw * B, st));
+    VD_CUDA_TRY(cudaMemsetAsync(adkp, 0, sizeof(T) * s.sh * B, st));
+    VD_CUDA_TRY(cudaMemsetAsync(adht, 0, sizeof(T) * s.sh * B, st));
+    k_sw_tend_adj<T><<<Ll.grid, Ll.block, 0, st>>>(t, x.u, x.v, x.h, wk.om, wk.ht, adk.u, adk.v, adk.h, adom, adkp,
+                                                    adht, adx.u, adx.v, adx.h);
+    VD_LAUNCH_CHECK();
+    k_sw_diag_adj<T><<<Ld.grid, Ld.block, 0, st>>>(t, x.u, x.v, x.h, adom, adkp, adht, adx.u, adx.v, adx.h);
+    VD_LAUNCH_CHECK();
+    return VD_OK;
+}
+
+template <typename T>
+static int sw_adj_t(vd_sw_plan* p, int B, const void* u0, const void* v0, const void* h0, const void* adu1,
+                    const void* adv1, const void* adh1, int nstep, const void* ub, const void* vb, const void* hb,
+                    const void* Fu, const void* Fv, const void* Fh, const void* taux, const void* tauy, void* adu0,
+                    void* adv0, void* adh0, void* adub, void* advb, void* adhb, void* adFu, void* adFv, void* adFh,
+                    Arena& ws, cudaStream_t st)
+{
+    Inputs<T> in;
+    int rc = prep_inputs<T>(p, B, u0, v0, h0, ub, vb, hb, Fu, Fv, Fh, ws, in, st);
+    if (rc) return rc;
+    const Sizes s = sizes(p);
+    Work<T> wk;
+    if ((rc = take_work<T>(ws, s, B, wk))) return rc;
+    std::vector<Fields<T>> traj((size_t)(nstep > 0 ? nstep : 1));
+    for (int n = 0; n < nstep; ++n)
+        if (!take_uvh(ws, s, B, traj[n])) return VD_ERR_WORKSPACE;
+    Fields<T> ad, adk, a0, a1, adb, adF, x1, x2;
+    if (!take_uvh(ws, s, B, ad) || !take_uvh(ws, s, B, adk) || !take_uvh(ws, s, B, a0) || !take_uvh(ws, s, B, a1) ||
+        !take_uvh(ws, s, B, adb) || !take_uvh(ws, s, B, adF) || !take_uvh(ws, s, B, x1) || !take_uvh(ws, s, B, x2))
+        return VD_ERR_WORKSPACE;
+    T* adom = (T*)ws.take(sizeof(T) * s.sw * B);
+    T* adkp = (T*)ws.take(sizeof(T) * s.sh * B);
+    T* adht = (T*)ws.take(sizeof(T) * s.sh * B);
+    if (!adom || !adkp || !adht) return VD_ERR_WORKSPACE;
+    // forward sweep storing the state at the start of every step
+    Fields<T> xr;
+    if (!take_uvh(ws, s, B, xr)) return VD_ERR_WORKSPACE;
+    VD_CUDA_TRY(cudaMemcpyAsync(xr.u, in.x.u, sizeof(T) * s.su * B, cudaMemcpyDeviceToDevice, st));
+    VD_CUDA_TRY(cudaMemcpyAsync(xr.v, in.x.v, sizeof(T) * s.sv * B, cudaMemcpyDeviceToDevice, st));
+    VD_CUDA_TRY(cudaMemcpyAsync(xr.h, in.x.h, sizeof(T) * s.sh * B, cudaMemcpyDeviceToDevice, st));
+    rc = run_fwd<T>(p, B, xr, nstep, in.xb, in.F, in.hasF, (const T*)taux, (const T*)tauy, wk, traj.data(), st);
+    if (rc) return rc;
+    // adjoint of the physical output -> model space
+    if ((rc = scale<T>(p, B, 1, (const T*)adu1, (const T*)adv1, (const T*)adh1, ad.u, ad.v, ad.h, st))) return rc;
+    if ((rc = zero(adb, s, B, st)) || (rc = zero(adF, s, B, st))) return rc;
+    Tab<T>& t = tab<T>(p);
+    const Launch Ll = lgrid(p, B * p->nl);
+    const int mc = p->d.forcing_momentum == 1;
+    for (int n = nstep - 1; n >= 0; --n) {
+        // recompute the stage states of step n
+        Fields<T> stages[3] = {traj[n], x1, x2};
+        {
+            Fields<T> cur = traj[n];
+            const Launch Ld = lgrid(p, B);
+            for (int stg = 0; stg < 2; ++stg) {
+                k_sw_diag<T, T><<<Ld.grid, Ld.block, 0, st>>>(t, rt(cur), w(wk.om), w(wk.kp), w(wk.ht));
+                VD_LAUNCH_CHECK();
+                k_sw_tend<T, T><<<Ll.grid, Ll.block, 0, st>>>(t, rt(cur), r<T>(wk.om), r<T>(wk.kp), r<T>(wk.ht),
+                                                               (const T*)taux, (const T*)tauy, w(wk.tuvh.u),
+                                                               w(wk.tuvh.v), w(wk.fx), w(wk.fy));
+                VD_LAUNCH_CHECK();
+                Fields<T> nxt = stg == 0 ? x1 : x2;
+                StageArgs sa{stg, 0};
+                Fields<T> ks = stg == 0 ? wk.k0 : wk.k1;
+                k_sw_update<T, T><<<Ll.grid, Ll.block, 0, st>>>(t, sa, rt(cur), r<T>(wk.tuvh.u), r<T>(wk.tuvh.v),
+                                                                 r<T>(wk.fx), r<T>(wk.fy), rt(wk.k0), rt(wk.k1),
+                                                                 rt(in.xb), rt(in.F), wt(ks), wt(nxt));
+                VD_LAUNCH_CHECK();
+                cur = nxt;
+            }
+            if (mc) {
+                // x3 (before the forcing) is needed by the forcing adjoint: rebuild it in wk.x1
+                k_sw_diag<T, T><<<Ld.grid, Ld.block, 0, st>>>(t, rt(x2), w(wk.om), w(wk.kp), w(wk.ht));
+                VD_LAUNCH_CHECK();
+                k_sw_tend<T, T><<<Ll.grid, Ll.block, 0, st>>>(t, rt(x2), r<T>(wk.om), r<T>(wk.kp), r<T>(wk.ht),
+                                                               (const T*)taux, (const T*)tauy, w(wk.tuvh.u),
+                                                               w(wk.tuvh.v), w(wk.fx), w(wk.fy));
+                VD_LAUNCH_CHECK();
+                StageArgs sa{2, 0};
+                k_sw_update<T, T><<<Ll.grid, Ll.block, 0, st>>>(t, sa, rt(x2), r<T>(wk.tuvh.u), r<T>(wk.tuvh.v),
+                                                                 r<T>(wk.fx), r<T>(wk.fy), rt(wk.k0), rt(wk.k1),
+                                                                 rt(in.xb), rt(in.F), wt(wk.k1), wt(wk.x1));
+                VD_LAUNCH_CHECK();
+            }
+        }
+        // forcing adjoints
+        if (in.hasF || adFu || adFv || adFh) {
+            if ((rc = addto(adF, t.dt, ad, s, B, st))) return rc;
+        }
+        if (mc) {
+            // u_new = u3 - dt u3 Fh_u / htot_u(h3): ad -> ad(u3), ad(h3) (+= into ad.h), ad(Fh)
+            k_sw_force_mc_adj<T><<<Ll.grid, Ll.block, 0, st>>>(t, wk.x1.u, wk.x1.v, wk.x1.h, in.F.h, ad.u, ad.v,
+                                                               ad.h, adF.h);
+            VD_LAUNCH_CHECK();
+        }
+        if ((rc = zero(a0, s, B, st)) || (rc = zero(a1, s, B, st))) return rc;
+        for (int stg = 2; stg >= 0; --stg) {
+            k_sw_update_adj<T><<<Ll.grid, Ll.block, 0, st>>>(t, stg, B * p->nl, ad.u, ad.v, ad.h, adk.u, adk.v, adk.h,
+                                                             a0.u, a0.v, a0.h, a1.u, a1.v, a1.h, adb.u, adb.v, adb.h);
+            VD_LAUNCH_CHECK();
+            if ((rc = rhs_adj<T>(p, B, stages[stg], adk, ad, wk, adom, adkp, adht, st))) return rc;
+        }
+    }
+    // boundary fields that default to the initial state feed its adjoint
+    if (!in.hasb) {
+        if ((rc = addto(ad, T(1), adb, s, B, st))) return rc;
+    }
+    if ((rc = scale<T>(p, B, 0, ad.u, ad.v, ad.h, (T*)adu0, (T*)adv0, (T*)adh0, st))) return rc;
+    if (in.hasb && (adub || advb || adhb)) {
+        if ((rc = scale<T>(p, B, 0, adb.u, adb.v, adb.h, (T*)adub, (T*)advb, (T*)adhb, st))) return rc;
+    }
+    if (adFu || adFv || adFh) {
+        if ((rc = scale<T>(p, B, 0, adF.u, adF.v, adF.h, (T*)adFu, (T*)adFv, (T*)adFh, st))) return rc;
+    }
+    return VD_OK;
+}
+
+template <typename T>
+static int sw_rhs_t(vd_sw_plan* p, int B, const void* u, const void* v, const void* h, const void* taux,
+                    const void* tauy, void* du, void* dv, void* dh, Arena& ws, cudaStream_t st)
+{
+    Tab<T>& t = tab<T>(p);
+    const Sizes s = sizes(p);
+    Work<T> wk;
+    int rc = take_work<T>(ws, s, B, wk);
+    if (rc) return rc;
+    const Launch Ld = lgrid(p, B), Ll = lgrid(p, B * p->nl);
+    Fields<T> x{(T*)u, (T*)v, (T*)h};
+    k_sw_diag<T, T><<<Ld.grid, Ld.block, 0, st>>>(t, rt(x), w(wk.om), w(wk.kp), w(wk.ht));
+    VD_LAUNCH_CHECK();
+    k_sw_tend<T, T><<<Ll.grid, Ll.block, 0, st>>>(t, rt(x), r<T>(wk.om), r<T>(wk.kp), r<T>(wk.ht), (const T*)taux,
+                                                   (const T*)tauy, w(wk.tuvh.u), w(wk.tuvh.v), w(wk.fx), w(wk.fy));
+    VD_LAUNCH_CHECK();
+    // stage-0 update with dt*k into a scratch state, k0 = tendency (no sponge: zero rates are
+    // not guaranteed, so the sponge is removed by passing x as its own target)
+    Fields<T> k{(T*)du, (T*)dv, (T*)dh};
+    StageArgs sa{0, 0};
+    k_sw_update<T, T><<<Ll.grid, Ll.block, 0, st>>>(t, sa, rt(x), r<T>(wk.tuvh.u), r<T>(wk.tuvh.v), r<T>(wk.fx),
+                                                     r<T>(wk.fy), rt(wk.k0), rt(wk.k1), rt(x), rt(x), wt(k), wt(wk.x1));
+    VD_LAUNCH_CHECK();
+    return VD_OK;
+}
+
+}  // namespace
+
+#define SW_DISPATCH(fn, ...) \
+    (p->esz == 8 ? fn<double>(__VA_ARGS__) : fn<float>(__VA_ARGS__))
+
+extern "C" vd_status vd_sw_step(vd_sw_plan* p, int batch, const void* u0, const void* v0, const void* h0, int nstep,
+                                const void* ub, const void* vb, const void* hb, const void* Fu, const void* Fv,
+                                const void* Fh, const void* taux, const void* tauy, void* u1, void* v1, void* h1,
+                                void* work, size_t work_bytes_, void* stream)
+{
+    if (!p || batch <= 0 || nstep < 0 || !u0 || !v0 || !h0 || !u1 || !v1 || !h1 || !work) return VD_ERR_ARG;
+    if ((Fu || Fv || Fh) && !(Fu && Fv && Fh)) return VD_ERR_ARG;
+    if ((ub || vb || hb) && !(ub && vb && hb)) return VD_ERR_ARG;
+    if ((long long)batch * p->nl > 65535) return VD_ERR_ARG;
+    Arena ws{(char*)work, work_bytes_, 0};
+    return SW_DISPATCH(sw_step_t, p, batch, u0, v0, h0, nstep, ub, vb, hb, Fu, Fv, Fh, taux, tauy, u1, v1, h1, ws,
+                       (cudaStream_t)stream);
+}
+
+extern "C" vd_status vd_sw_step_tgl(vd_sw_plan* p, int batch, const void* u0, const void* v0, const void* h0,
+                                    const void* du0, const void* dv0, const void* dh0, int nstep, const void* ub,
+                                    const void* vb, const void* hb, const void* dub, const void* dvb, const void* dhb,
+                                    const void* Fu, const void* Fv, const void* Fh, const void* dFu, const void* dFv,
+                                    const void* dFh, const void* taux, const void* tauy, void* du1, void* dv1,
+                                    void* dh1, void* work, size_t work_bytes_, void* stream)
+{
+    if (!p || batch <= 0 || nstep < 0 || !u0 || !v0 || !h0 || !du0 || !dv0 || !dh0 || !du1 || !dv1 || !dh1 || !work)
+        return VD_ERR_ARG;
+    if ((Fu || Fv || Fh) && !(Fu && Fv && Fh)) return VD_ERR_ARG;
+    if ((dFu || dFv || dFh) && !(dFu && dFv && dFh)) return VD_ERR_ARG;
+    if ((ub || vb || hb) && !(ub && vb && hb)) return VD_ERR_ARG;
+    if ((dub || dvb || dhb) && !(ub && dub && dvb && dhb)) return VD_ERR_ARG;
+    if ((long long)batch * p->nl > 65535) return VD_ERR_ARG;
+    Arena ws{(char*)work, work_bytes_, 0};
+    return SW_DISPATCH(sw_tgl_t, p, batch, u0, v0, h0, du0, dv0, dh0, nstep, ub, vb, hb, dub, dvb, dhb, Fu, Fv, Fh,
+                       dFu, dFv, dFh, taux, tauy, du1, dv1, dh1, ws, (cudaStream_t)stream);
+}
+
+extern "C" vd_status vd_sw_step_adj(vd_sw_plan* p, int batch, const void* u0, const void* v0, const void* h0,
+                                    const void* adu1, const void* adv1, const void* adh1, int nstep, const void* ub,
+                                    const void* vb, const void* hb, const void* Fu, const void* Fv, const void* Fh,
+                                    const void* taux, const void* tauy, void* adu0, void* adv0, void* adh0,
+                                    void* adub, void* advb, void* adhb, void* adFu, void* adFv, void* adFh,
+                                    void* work, size_t work_bytes_, void* stream)
+{
+    if (!p || batch <= 0 || nstep < 0 || !u0 || !v0 || !h0 || !adu1 || !adv1 || !adh1 || !adu0 || !adv0 || !adh0 ||
+        !work)
+        return VD_ERR_ARG;
+    if ((Fu || Fv || Fh) && !(Fu && Fv && Fh)) return VD_ERR_ARG;
+    if ((ub || vb || hb) && !(ub && vb && hb)) return VD_ERR_ARG;
+    if ((adub || advb || adhb) && !(adub && advb && adhb)) return VD_ERR_ARG;
+    if ((adFu || adFv || adFh) && !(adFu && adFv && adFh)) return VD_ERR_ARG;
+    if ((long long)batch * p->nl > 65535) return VD_ERR_ARG;
+    Arena ws{(char*)work, work_bytes_, 0};
+    return SW_DISPATCH(sw_adj_t, p, batch, u0, v0, h0, adu1, adv1, adh1, nstep, ub, vb, hb, Fu, Fv, Fh, taux, tauy,
+                       adu0, adv0, adh0, adub, advb, adhb, adFu, adFv, adFh, ws, (cudaStream_t)stream);
+}
+
+extern "C" vd_status vd_sw_rhs(vd_sw_plan* p, int batch, const void* u, const void* v, const void* h,
+                               const void* taux, const void* tauy, void* du, void* dv, void* dh, void* work,
+                               size_t work_bytes_, void* stream)
+{
+    if (!p || batch <= 0 || !u || !v || !h || !du || !dv || !dh || !work) return VD_ERR_ARG;
+    if ((long long)batch * p->nl > 65535) return VD_ERR_ARG;
+    Arena ws{(char*)work, work_bytes_, 0};
+    return SW_DISPATCH(sw_rhs_t, p, batch, u, v, h, taux, tauy, du, dv, dh, ws, (cudaStream_t)stream);
+}
