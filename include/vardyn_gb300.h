@@ -410,6 +410,11 @@ vd_status vd_mg_residual(const vd_mg_plan* plan, const void* f, const void* rhs,
  * (src == dst) only without a mask. */
 vd_status vd_edge_pad(int dtype, int nfield, int n0, int n1, const void* src,
                       const void* mask, void* dst, void* stream);
+/* Transpose of vd_edge_pad (mask applied first): the interior of out
+ * [n0][n1] gathers from every position that copies it; walls are zero.
+ * out must not alias ad. */
+vd_status vd_edge_pad_adj(int dtype, int nfield, int n0, int n1, const void* ad,
+                          const void* mask, void* out, void* stream);
 /* Capacitance correction of solve_helmholtz_dstI_cmm (172-184) for nsys
  * systems of nper fields each (field f = s * nper + r, system-major):
  * out = rhs, then out[f][bidx[i]] += sum_j cap[s][i][j] * (-sol[f][bidx[j]])
@@ -507,6 +512,71 @@ vd_status vd_sw_step_adj(vd_sw_plan* plan, int batch, const void* u0, const void
 vd_status vd_sw_rhs(vd_sw_plan* plan, int batch, const void* u, const void* v,
                     const void* h, const void* taux, const void* tauy, void* du, void* dv,
                     void* dh, void* work, size_t work_bytes, void* stream);
+
+/* Shallow-water building blocks for drivers that insert an operator between
+ * the right-hand side and the RK3-SSP combination (the QG model projects
+ * every tendency). All fields are model-space (u dx, v dy, h area).
+ * vd_sw_rhs_tgl: right-hand side and its tangent. vd_sw_rhs_adj: adds the
+ * transpose of the right-hand side's Jacobian at (u, v, h) applied to
+ * (aku, akv, akh) into (adu, adv, adh). */
+vd_status vd_sw_rhs_tgl(vd_sw_plan* plan, int batch, const void* u, const void* v,
+                        const void* h, const void* du, const void* dv, const void* dh,
+                        const void* taux, const void* tauy, void* ku, void* kv, void* kh,
+                        void* dku, void* dkv, void* dkh, void* work, size_t work_bytes,
+                        void* stream);
+vd_status vd_sw_rhs_adj(vd_sw_plan* plan, int batch, const void* u, const void* v,
+                        const void* h, const void* aku, const void* akv, const void* akh,
+                        void* adu, void* adv, void* adh, void* work, size_t work_bytes,
+                        void* stream);
+/* One RK3-SSP stage (sw.py:831-877): fields[24] = x(u,v,h), rhs, k0, k1,
+ * sponge target, forcing (nullable; added at stage 2), k_out (stages 0, 1),
+ * next. k = rhs + sponge rate * (target - x). */
+vd_status vd_sw_stage(vd_sw_plan* plan, int batch, int stage, const void* const* fields,
+                      void* stream);
+/* Transpose of vd_sw_stage: fields[15] = adjoint of next (in place: becomes
+ * the direct adjoint of x), adk out, adk0 / adk1 accumulators, sponge-target
+ * adjoint accumulator. */
+vd_status vd_sw_stage_adj(vd_sw_plan* plan, int batch, int stage, void* const* fields,
+                          void* stream);
+/* physical <-> model space: to_physical = 0 masks and multiplies by the
+ * metrics (set_input_uvh), 1 divides (get_physical_uvh). Nullable fields. */
+vd_status vd_sw_scale(vd_sw_plan* plan, int batch, int to_physical, const void* u,
+                      const void* v, const void* h, void* uo, void* vo, void* ho,
+                      void* stream);
+/* mass-consistent forcing (sw.py:880-898): fields[9] = x, F, out; its
+ * transpose: fields[8] = u, v, h, Fh, adu, adv (in place), adh (+=), adFh
+ * (+=, nullable). */
+vd_status vd_sw_force_mc(vd_sw_plan* plan, int batch, const void* const* fields, void* stream);
+vd_status vd_sw_force_mc_adj(vd_sw_plan* plan, int batch, const void* const* fields,
+                             void* stream);
+
+/* ------------------------------------------------------------------------
+ * QG projector of the multilayer QG model (mapping/models/model_qgsw/qg.py:
+ * G 198-219, QoG_inv 222-298, Q 300-308) around the spectral Helmholtz
+ * solves. Uniform dx, dy (the reference's QG operators need scalars).
+ * ---------------------------------------------------------------------- */
+typedef struct vd_qgp_plan vd_qgp_plan;
+typedef struct vd_qgp_desc {
+    int nx, ny, nl, dtype;
+    double dx, dy, f0;
+    const double* H_host;      /* [nl] */
+    const double* A_host;      /* [nl][nl] layer coupling (qg.py:45-59) */
+    const double* Cl2m_host;   /* [nl][nl] layer -> mode */
+    const double* Cm2l_host;   /* [nl][nl] mode -> layer */
+    const double* mask_host;   /* [nx][ny] h mask, NULL = all ocean */
+    int cmm;                   /* 1: multiply the modal right-hand side by psi */
+} vd_qgp_desc;
+vd_status vd_qgp_plan_create(vd_qgp_plan** out, const vd_qgp_desc* desc);
+void vd_qgp_plan_destroy(vd_qgp_plan* plan);
+/* op 0 Q (u, v, h -> modes [nl][batch][nx+1][ny+1], walls 0); 1 its
+ * transpose (modes -> adu, adv, adh); 2 per-field float64 sums (x, weights
+ * [nl][nx+1][ny+1] or NULL, out [nl*batch]); 3 modal solutions, their sums,
+ * homsol means [nl] (float64) and homsol -> p_qg [batch][nl][nx+1][ny+1];
+ * 4 transpose of the mode -> layer mixing; 5 transpose of the homogeneous
+ * correction (sums of homsol * ad, means, ad in place); 6 G (p_qg -> u, v,
+ * h); 7 its transpose. */
+vd_status vd_qgp_op(const vd_qgp_plan* plan, int op, int batch, const void* const* args,
+                    void* stream);
 
 /* Version / build information string. */
 const char* vd_version(void);

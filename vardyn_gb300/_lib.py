@@ -103,6 +103,15 @@ class VdSwDesc(ctypes.Structure):
     ]
 
 
+class VdQgpDesc(ctypes.Structure):
+    _fields_ = [
+        ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nl", ctypes.c_int), ("dtype", ctypes.c_int),
+        ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("f0", ctypes.c_double),
+        ("H_host", _DP), ("A_host", _DP), ("Cl2m_host", _DP), ("Cm2l_host", _DP), ("mask_host", _DP),
+        ("cmm", ctypes.c_int),
+    ]
+
+
 P = ctypes.c_void_p
 I = ctypes.c_int
 LL = ctypes.c_longlong
@@ -170,6 +179,17 @@ SIGNATURES = {
     "vd_sw_step_adj": (I, [P, I, P, P, P, P, P, P, I, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P,
                            P, SZ, P]),
     "vd_sw_rhs": (I, [P, I, P, P, P, P, P, P, P, P, P, SZ, P]),
+    "vd_sw_rhs_tgl": (I, [P, I, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, SZ, P]),
+    "vd_sw_rhs_adj": (I, [P, I, P, P, P, P, P, P, P, P, P, P, SZ, P]),
+    "vd_sw_stage": (I, [P, I, I, P, P]),
+    "vd_sw_stage_adj": (I, [P, I, I, P, P]),
+    "vd_sw_scale": (I, [P, I, I, P, P, P, P, P, P, P]),
+    "vd_sw_force_mc": (I, [P, I, P, P]),
+    "vd_sw_force_mc_adj": (I, [P, I, P, P]),
+    "vd_qgp_plan_create": (I, [ctypes.POINTER(P), ctypes.POINTER(VdQgpDesc)]),
+    "vd_qgp_plan_destroy": (None, [P]),
+    "vd_qgp_op": (I, [P, I, I, P, P]),
+    "vd_edge_pad_adj": (I, [I, I, I, I, P, P, P, P]),
     "vd_mg_plan_create": (I, [ctypes.POINTER(P), ctypes.POINTER(VdMgDesc)]),
     "vd_mg_plan_destroy": (I, [P]),
     "vd_mg_levels": (I, [P]),

@@ -98,3 +98,51 @@ extern "C" vd_status vd_cmm_correct(int dtype, int nsys, int nper, int M, long l
     VD_LAUNCH_CHECK();
     return VD_OK;
 }
+
+namespace vd {
+// Transpose of k_edge_pad: interior cell (i, j) gathers mask * ad from every
+// padded position that copies it (itself and, on the interior's edge, the
+// adjacent wall and corner cells); walls of the result are zero.
+template <typename T>
+__global__ void k_edge_pad_adj(int n0, int n1, const T* __restrict__ ad, const T* __restrict__ mask, T* __restrict__ out)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y, b = blockIdx.z;
+    if (j >= n1) return;
+    const long long base = (long long)b * n0 * n1;
+    if (i == 0 || i == n0 - 1 || j == 0 || j == n1 - 1) {
+        out[base + (long long)i * n1 + j] = T(0);
+        return;
+    }
+    int is[3], js[3], ni = 0, nj = 0;
+    is[ni++] = i;
+    if (i == 1) is[ni++] = 0;
+    if (i == n0 - 2) is[ni++] = n0 - 1;
+    js[nj++] = j;
+    if (j == 1) js[nj++] = 0;
+    if (j == n1 - 2) js[nj++] = n1 - 1;
+    T a = T(0);
+    for (int p = 0; p < ni; ++p)
+        for (int q = 0; q < nj; ++q) {
+            const long long k = (long long)is[p] * n1 + js[q];
+            a += mask ? mask[k] * ad[base + k] : ad[base + k];
+        }
+    out[base + (long long)i * n1 + j] = a;
+}
+}  // namespace vd
+
+extern "C" vd_status vd_edge_pad_adj(int dtype, int nfield, int n0, int n1, const void* ad, const void* mask,
+                                     void* out, void* stream)
+{
+    if (nfield < 0 || n0 < 3 || n1 < 3 || (dtype != VD_F32 && dtype != VD_F64)) return VD_ERR_ARG;
+    if (nfield == 0) return VD_OK;
+    if (!ad || !out || ad == out || nfield > 65535 || n0 > 65535) return VD_ERR_ARG;
+    const dim3 g((unsigned)((n1 + 127) / 128), (unsigned)n0, (unsigned)nfield);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (dtype == VD_F32)
+        vd::k_edge_pad_adj<float><<<g, 128, 0, st>>>(n0, n1, (const float*)ad, (const float*)mask, (float*)out);
+    else
+        vd::k_edge_pad_adj<double><<<g, 128, 0, st>>>(n0, n1, (const double*)ad, (const double*)mask, (double*)out);
+    VD_LAUNCH_CHECK();
+    return VD_OK;
+}

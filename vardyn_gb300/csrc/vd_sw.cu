@@ -1936,3 +1936,222 @@ extern "C" vd_status vd_sw_rhs(vd_sw_plan* p, int batch, const void* u, const vo
     Arena ws{(char*)work, work_bytes_, 0};
     return SW_DISPATCH(sw_rhs_t, p, batch, u, v, h, taux, tauy, du, dv, dh, ws, (cudaStream_t)stream);
 }
+
+// ---------------------------------------------------------------- building blocks
+// Model-space pieces for drivers that insert an operator between the
+// right-hand side and the RK3-SSP combination (the QG model projects every
+// SW tendency, qg.py:335-345).
+namespace {
+
+template <typename T>
+static int sw_rhs_tgl_t(vd_sw_plan* p, int B, const void* u, const void* v, const void* h, const void* du,
+                        const void* dv, const void* dh, const void* taux, const void* tauy, void* ku, void* kv,
+                        void* kh, void* dku, void* dkv, void* dkh, Arena& ws, cudaStream_t st)
+{
+    Tab<T>& t = tab<T>(p);
+    const Sizes s = sizes(p);
+    Work<T> wk, dk;
+    int rc = take_work<T>(ws, s, B, wk);
+    if (rc || (rc = take_work<T>(ws, s, B, dk))) return rc;
+    const Launch Ld = lgrid(p, B), Ll = lgrid(p, B * p->nl);
+    Fields<T> x{(T*)u, (T*)v, (T*)h}, dx{(T*)du, (T*)dv, (T*)dh};
+    using S = DN<T, 1>;
+    k_sw_diag<T, S><<<Ld.grid, Ld.block, 0, st>>>(t, rtd(x, dx), WD<T>{wk.om, dk.om}, WD<T>{wk.kp, dk.kp},
+                                                   WD<T>{wk.ht, dk.ht});
+    VD_LAUNCH_CHECK();
+    k_sw_tend<T, S><<<Ll.grid, Ll.block, 0, st>>>(t, rtd(x, dx), RD<T>{wk.om, dk.om}, RD<T>{wk.kp, dk.kp},
+                                                   RD<T>{wk.ht, dk.ht}, (const T*)taux, (const T*)tauy,
+                                                   WD<T>{wk.tuvh.u, dk.tuvh.u}, WD<T>{wk.tuvh.v, dk.tuvh.v},
+                                                   WD<T>{wk.fx, dk.fx}, WD<T>{wk.fy, dk.fy});
+    VD_LAUNCH_CHECK();
+    Fields<T> k{(T*)ku, (T*)kv, (T*)kh}, dkk{(T*)dku, (T*)dkv, (T*)dkh};
+    StageArgs sa{0, 0};
+    k_sw_update<T, S><<<Ll.grid, Ll.block, 0, st>>>(t, sa, rtd(x, dx), RD<T>{wk.tuvh.u, dk.tuvh.u},
+                                                     RD<T>{wk.tuvh.v, dk.tuvh.v}, RD<T>{wk.fx, dk.fx},
+                                                     RD<T>{wk.fy, dk.fy}, rtd(wk.k0, dk.k0), rtd(wk.k1, dk.k1),
+                                                     rtd(x, dx), rtd(x, dx), wtd(k, dkk), wtd(wk.x1, dk.x1));
+    VD_LAUNCH_CHECK();
+    return VD_OK;
+}
+
+template <typename T>
+static int sw_rhs_adj_t(vd_sw_plan* p, int B, const void* u, const void* v, const void* h, const void* aku,
+                        const void* akv, const void* akh, void* adu, void* adv, void* adh, Arena& ws, cudaStream_t st)
+{
+    const Sizes s = sizes(p);
+    Work<T> wk;
+    int rc = take_work<T>(ws, s, B, wk);
+    if (rc) return rc;
+    T* adom = (T*)ws.take(sizeof(T) * s.sw * B);
+    T* adkp = (T*)ws.take(sizeof(T) * s.sh * B);
+    T* adht = (T*)ws.take(sizeof(T) * s.sh * B);
+    if (!adom || !adkp || !adht) return VD_ERR_WORKSPACE;
+    Fields<T> x{(T*)u, (T*)v, (T*)h}, ak{(T*)aku, (T*)akv, (T*)akh}, ad{(T*)adu, (T*)adv, (T*)adh};
+    return rhs_adj<T>(p, B, x, ak, ad, wk, adom, adkp, adht, st);
+}
+
+// elementwise stage combination: k = rhs + sponge; stage 0/1 store k
+template <typename T>
+__global__ void k_sw_stage(Tab<T> t, int stage, int nf, int forcing, Fields<T> x, Fields<T> r, Fields<T> k0,
+                           Fields<T> k1, Fields<T> xb, Fields<T> F, Fields<T> ks, Fields<T> nx_)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    const int f = blockIdx.z;
+    const int nx = t.nx, ny = t.ny;
+    if (i > nx || j > ny || f >= nf) return;
+    const T dt = t.dt;
+    auto one = [&](long long o, T g, const T* X, const T* R, const T* K0, const T* K1, const T* XB, const T* FF, T* KS,
+                   T* NX) {
+        const T xv = X[o];
+        T k = R[o];
+        if (t.has_sponge) k = k + g * (XB[o] - xv);
+        if (stage == 0) {
+            KS[o] = k;
+            NX[o] = xv + dt * k;
+        } else if (stage == 1) {
+            KS[o] = k;
+            NX[o] = xv + (dt / T(4)) * (k - T(3) * K0[o]);
+        } else {
+            T n = xv + (dt / T(12)) * (T(8) * k - K1[o] - K0[o]);
+            if (forcing) n = n + dt * FF[o];
+            NX[o] = n;
+        }
+    };
+    if (j < ny) {
+        const long long q = (long long)i * ny + j;
+        one(f * t.su + q, t.has_sponge ? t.gu[q] : T(0), x.u, r.u, k0.u, k1.u, xb.u, F.u, ks.u, nx_.u);
+    }
+    if (i < nx) {
+        const long long q = (long long)i * (ny + 1) + j;
+        one(f * t.sv + q, t.has_sponge ? t.gv[q] : T(0), x.v, r.v, k0.v, k1.v, xb.v, F.v, ks.v, nx_.v);
+    }
+    if (i < nx && j < ny) {
+        const long long q = (long long)i * ny + j;
+        one(f * t.sh + q, t.has_sponge ? t.gh[q] : T(0), x.h, r.h, k0.h, k1.h, xb.h, F.h, ks.h, nx_.h);
+    }
+}
+
+template <typename T>
+static Fields<T> F3(const void* a, const void* b, const void* c) { return Fields<T>{(T*)a, (T*)b, (T*)c}; }
+
+}  // namespace
+
+extern "C" vd_status vd_sw_rhs_tgl(vd_sw_plan* p, int batch, const void* u, const void* v, const void* h,
+                                   const void* du, const void* dv, const void* dh, const void* taux,
+                                   const void* tauy, void* ku, void* kv, void* kh, void* dku, void* dkv, void* dkh,
+                                   void* work, size_t work_bytes_, void* stream)
+{
+    if (!p || batch <= 0 || !u || !v || !h || !du || !dv || !dh || !ku || !kv || !kh || !dku || !dkv || !dkh || !work)
+        return VD_ERR_ARG;
+    if ((long long)batch * p->nl > 65535) return VD_ERR_ARG;
+    Arena ws{(char*)work, work_bytes_, 0};
+    return SW_DISPATCH(sw_rhs_tgl_t, p, batch, u, v, h, du, dv, dh, taux, tauy, ku, kv, kh, dku, dkv, dkh, ws,
+                       (cudaStream_t)stream);
+}
+
+extern "C" vd_status vd_sw_rhs_adj(vd_sw_plan* p, int batch, const void* u, const void* v, const void* h,
+                                   const void* aku, const void* akv, const void* akh, void* adu, void* adv,
+                                   void* adh, void* work, size_t work_bytes_, void* stream)
+{
+    if (!p || batch <= 0 || !u || !v || !h || !aku || !akv || !akh || !adu || !adv || !adh || !work)
+        return VD_ERR_ARG;
+    if ((long long)batch * p->nl > 65535) return VD_ERR_ARG;
+    Arena ws{(char*)work, work_bytes_, 0};
+    return SW_DISPATCH(sw_rhs_adj_t, p, batch, u, v, h, aku, akv, akh, adu, adv, adh, ws, (cudaStream_t)stream);
+}
+
+namespace {
+template <typename T>
+static int sw_stage_t(vd_sw_plan* p, int B, int stage, const void* const* f, cudaStream_t st)
+{
+    const Launch L = lgrid(p, B * p->nl);
+    const int forcing = f[15] != nullptr;
+    k_sw_stage<T><<<L.grid, L.block, 0, st>>>(tab<T>(p), stage, B * p->nl, forcing, F3<T>(f[0], f[1], f[2]),
+                                              F3<T>(f[3], f[4], f[5]), F3<T>(f[6], f[7], f[8]),
+                                              F3<T>(f[9], f[10], f[11]), F3<T>(f[12], f[13], f[14]),
+                                              F3<T>(f[15], f[16], f[17]), F3<T>(f[18], f[19], f[20]),
+                                              F3<T>(f[21], f[22], f[23]));
+    VD_LAUNCH_CHECK();
+    return VD_OK;
+}
+template <typename T>
+static int sw_stage_adj_t(vd_sw_plan* p, int B, int stage, void* const* f, cudaStream_t st)
+{
+    const Launch L = lgrid(p, B * p->nl);
+    k_sw_update_adj<T><<<L.grid, L.block, 0, st>>>(tab<T>(p), stage, B * p->nl, (T*)f[0], (T*)f[1], (T*)f[2],
+                                                   (T*)f[3], (T*)f[4], (T*)f[5], (T*)f[6], (T*)f[7], (T*)f[8],
+                                                   (T*)f[9], (T*)f[10], (T*)f[11], (T*)f[12], (T*)f[13], (T*)f[14]);
+    VD_LAUNCH_CHECK();
+    return VD_OK;
+}
+template <typename T>
+static int sw_force_mc_t(vd_sw_plan* p, int B, const void* const* f, cudaStream_t st)
+{
+    const Launch L = lgrid(p, B * p->nl);
+    k_sw_force_mc<T, T><<<L.grid, L.block, 0, st>>>(tab<T>(p), rt(F3<T>(f[0], f[1], f[2])),
+                                                     rt(F3<T>(f[3], f[4], f[5])), wt(F3<T>(f[6], f[7], f[8])));
+    VD_LAUNCH_CHECK();
+    return VD_OK;
+}
+template <typename T>
+static int sw_force_mc_adj_t(vd_sw_plan* p, int B, const void* const* f, cudaStream_t st)
+{
+    const Launch L = lgrid(p, B * p->nl);
+    k_sw_force_mc_adj<T><<<L.grid, L.block, 0, st>>>(tab<T>(p), (const T*)f[0], (const T*)f[1], (const T*)f[2],
+                                                     (const T*)f[3], (T*)f[4], (T*)f[5], (T*)f[6], (T*)f[7]);
+    VD_LAUNCH_CHECK();
+    return VD_OK;
+}
+}  // namespace
+
+extern "C" vd_status vd_sw_stage(vd_sw_plan* p, int batch, int stage, const void* const* fields, void* stream)
+{
+    if (!p || batch <= 0 || stage < 0 || stage > 2 || !fields) return VD_ERR_ARG;
+    for (int k = 0; k < 24; ++k) {
+        const bool optional = (k >= 15 && k < 18) || (k >= 6 && k < 12 && stage == 0) || (k >= 9 && k < 12 && stage == 1) ||
+                              (k >= 18 && k < 21 && stage == 2);
+        if (!fields[k] && !optional) return VD_ERR_ARG;
+    }
+    if ((long long)batch * p->nl > 65535) return VD_ERR_ARG;
+    return SW_DISPATCH(sw_stage_t, p, batch, stage, fields, (cudaStream_t)stream);
+}
+
+extern "C" vd_status vd_sw_stage_adj(vd_sw_plan* p, int batch, int stage, void* const* fields, void* stream)
+{
+    if (!p || batch <= 0 || stage < 0 || stage > 2 || !fields) return VD_ERR_ARG;
+    for (int k = 0; k < 15; ++k)
+        if (!fields[k]) return VD_ERR_ARG;
+    if ((long long)batch * p->nl > 65535) return VD_ERR_ARG;
+    return SW_DISPATCH(sw_stage_adj_t, p, batch, stage, fields, (cudaStream_t)stream);
+}
+
+extern "C" vd_status vd_sw_scale(vd_sw_plan* p, int batch, int to_physical, const void* u, const void* v,
+                                 const void* h, void* uo, void* vo, void* ho, void* stream)
+{
+    if (!p || batch <= 0 || (u && !uo) || (v && !vo) || (h && !ho)) return VD_ERR_ARG;
+    if ((long long)batch * p->nl > 65535) return VD_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    return p->esz == 8 ? scale<double>(p, batch, to_physical ? 1 : 0, (const double*)u, (const double*)v,
+                                       (const double*)h, (double*)uo, (double*)vo, (double*)ho, st)
+                       : scale<float>(p, batch, to_physical ? 1 : 0, (const float*)u, (const float*)v,
+                                      (const float*)h, (float*)uo, (float*)vo, (float*)ho, st);
+}
+
+extern "C" vd_status vd_sw_force_mc(vd_sw_plan* p, int batch, const void* const* fields, void* stream)
+{
+    if (!p || batch <= 0 || !fields) return VD_ERR_ARG;
+    for (int k = 0; k < 9; ++k)
+        if (!fields[k]) return VD_ERR_ARG;
+    if ((long long)batch * p->nl > 65535) return VD_ERR_ARG;
+    return SW_DISPATCH(sw_force_mc_t, p, batch, fields, (cudaStream_t)stream);
+}
+
+extern "C" vd_status vd_sw_force_mc_adj(vd_sw_plan* p, int batch, const void* const* fields, void* stream)
+{
+    if (!p || batch <= 0 || !fields) return VD_ERR_ARG;
+    for (int k = 0; k < 7; ++k)
+        if (!fields[k]) return VD_ERR_ARG;
+    if ((long long)batch * p->nl > 65535) return VD_ERR_ARG;
+    return SW_DISPATCH(sw_force_mc_adj_t, p, batch, fields, (cudaStream_t)stream);
+}

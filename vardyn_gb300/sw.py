@@ -73,6 +73,7 @@ class SWPlan:
         self.device = torch.device(device if device is not None else "cuda")
         self.nx, self.ny, self.nl = int(nx), int(ny), int(nl)
         self.dtype = dtype
+        self.dt = float(dt)
         nx, ny, nl = self.nx, self.ny, self.nl
         if forcing_momentum not in _FORCING:
             raise ValueError(f"forcing_momentum must be one of {sorted(_FORCING)}")
@@ -261,3 +262,47 @@ class SWPlan:
         _lib.call("vd_sw_rhs", self._h, B, _ptr(u), _ptr(v), _ptr(h), _ptr(tx), _ptr(ty), _ptr(du), _ptr(dv),
                   _ptr(dh), _ptr(ws), ws.numel(), _stream())
         return du, dv, dh
+
+    # ---------------- building blocks (model space) ----------------
+    def rhs_tgl(self, u, v, h, du, dv, dh, taux=None, tauy=None):
+        B = self._batch(u)
+        u, v, h = self._uvh(u, v, h, B)
+        du, dv, dh = self._uvh(du, dv, dh, B, "d")
+        tx, ty = self._tau(taux, tauy)
+        k = [torch.empty_like(a) for a in (u, v, h)]
+        dk = [torch.empty_like(a) for a in (u, v, h)]
+        ws = self.workspace(B, 0)
+        _lib.call("vd_sw_rhs_tgl", self._h, B, _ptr(u), _ptr(v), _ptr(h), _ptr(du), _ptr(dv), _ptr(dh), _ptr(tx),
+                  _ptr(ty), *[_ptr(a) for a in k + dk], _ptr(ws), ws.numel(), _stream())
+        return tuple(k), tuple(dk)
+
+    def rhs_adj(self, u, v, h, aku, akv, akh, out):
+        """out (adu, adv, adh) += J_rhs(u, v, h)^T (aku, akv, akh)."""
+        B = self._batch(u)
+        ws = self.workspace(B, 0)
+        _lib.call("vd_sw_rhs_adj", self._h, B, _ptr(u), _ptr(v), _ptr(h), _ptr(aku), _ptr(akv), _ptr(akh),
+                  _ptr(out[0]), _ptr(out[1]), _ptr(out[2]), _ptr(ws), ws.numel(), _stream())
+
+    @staticmethod
+    def _ptrs(fields):
+        arr = (ctypes.c_void_p * len(fields))(*[None if f is None else f.data_ptr() for f in fields])
+        return arr
+
+    def stage(self, B, stage, x, r, k0, k1, xb, F, ks, nxt):
+        f = list(x) + list(r) + list(k0 or (None,) * 3) + list(k1 or (None,) * 3) + list(xb) + \
+            list(F or (None,) * 3) + list(ks or (None,) * 3) + list(nxt)
+        _lib.call("vd_sw_stage", self._h, B, stage, self._ptrs(f), _stream())
+
+    def stage_adj(self, B, stage, adn, adk, a0, a1, adb):
+        _lib.call("vd_sw_stage_adj", self._h, B, stage, self._ptrs(list(adn) + list(adk) + list(a0) + list(a1) +
+                                                                   list(adb)), _stream())
+
+    def scale(self, B, to_physical, x, out):
+        _lib.call("vd_sw_scale", self._h, B, 1 if to_physical else 0, *[_ptr(a) for a in x],
+                  *[_ptr(a) for a in out], _stream())
+
+    def force_mc(self, B, x, F, out):
+        _lib.call("vd_sw_force_mc", self._h, B, self._ptrs(list(x) + list(F) + list(out)), _stream())
+
+    def force_mc_adj(self, B, x, Fh, ad, adFh):
+        _lib.call("vd_sw_force_mc_adj", self._h, B, self._ptrs(list(x) + [Fh] + list(ad) + [adFh]), _stream())
