@@ -1,0 +1,161 @@
+"""Model_qgsw drop-in (State conventions, boundary fields, forcing, chunked
+stepping) on the GPU against the float64 oracle, and its tangent / adjoint
+through State objects by a dot-product test (the form of mod.py:5367-5446)."""
+from datetime import datetime, timedelta
+from types import SimpleNamespace
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+NAMES = {"U": "u", "V": "v", "SSH": "ssh"}
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from vardyn_gb300 import build
+    build.build()
+
+
+class FakeState:
+    def __init__(self, ny, nx, dx, dy, f, mask):
+        self.ny, self.nx = ny, nx
+        self.DX, self.DY = np.full((ny, nx), dx), np.full((ny, nx), dy)
+        self.f, self.mask = f, mask
+        self.var, self.params = {}, {}
+
+    def getvar(self, name_var=None):
+        return self.var[name_var]
+
+    def setvar(self, var, name_var=None):
+        self.var[name_var] = np.asarray(var)
+
+    def copy(self):
+        s = FakeState.__new__(FakeState)
+        s.__dict__.update({k: v for k, v in self.__dict__.items() if k not in ("var", "params")})
+        s.var = {k: np.array(v) for k, v in self.var.items()}
+        s.params = {k: np.array(v) for k, v in self.params.items()}
+        return s
+
+
+def setup(name_class, nl, island=False, ny=20, nx=26):
+    yy = np.arange(ny)[:, None] * 4.0e3 + np.zeros((1, nx))
+    f = 1.0e-4 + 1.6e-11 * (yy - yy.mean())
+    mask = np.zeros((ny, nx), dtype=bool)   # True = land
+    if island:
+        mask[8:12, 10:14] = True
+    st = FakeState(ny, nx, 5.0e3 if name_class == "QG" else 4.5e3, 5.0e3 if name_class == "QG" else 4.0e3, f, mask)
+    H = [350.0, 750.0, 2900.0][:nl]
+    gp = [9.81, 0.025, 0.0125][:nl]
+    MOD = SimpleNamespace(name_var=NAMES, nl=nl, name_class=name_class, f0=None, constant_f=False, c0=2.7,
+                          g_prime=gp, H=H, dtmodel=15.0 if name_class == "SW" else 300.0, cfl=None,
+                          bottom_drag_coef=2e-7, slip_coef=0.5, visc_coef=30.0, diff_coef=20.0, sponge_coef=0.0,
+                          max_nstep=2, name_params=["bc"], init_from_bc=None)
+    EXP = SimpleNamespace(init_date=datetime(2020, 1, 1), final_date=datetime(2020, 1, 2))
+    config = SimpleNamespace(MOD=MOD, EXP=EXP, GRID=None)
+    from vardyn_gb300.mod_qgsw import Model_qgsw
+    M = Model_qgsw(config, st)
+    rng = np.random.default_rng(5)
+    ocean = ~mask
+    st.var["u_layers"] = 0.05 * rng.standard_normal((nl, ny, nx + 1))
+    st.var["v_layers"] = 0.05 * rng.standard_normal((nl, ny + 1, nx))
+    st.var["h_layers"] = 0.2 * rng.standard_normal((nl, ny, nx)) * ocean
+    st.var["u"] = st.var["u_layers"][0].copy()
+    st.var["v"] = st.var["v_layers"][0].copy()
+    st.var["ssh"] = st.var["h_layers"].sum(0)
+    st.params["u"] = 0.1 * rng.standard_normal((ny, nx + 1))
+    st.params["v"] = 0.1 * rng.standard_normal((ny + 1, nx))
+    st.params["ssh"] = 0.3 * rng.standard_normal((ny, nx))
+    st.params["u_b"] = 0.01 * rng.standard_normal((ny, nx + 1))
+    st.params["v_b"] = 0.01 * rng.standard_normal((ny + 1, nx))
+    st.params["h_b"] = 0.02 * rng.standard_normal((ny, nx))
+    tb = [0.0, 30.0]
+    M.set_bc(tb, {"SSH": [0.05 * rng.standard_normal((ny, nx)) for _ in tb],
+                  "U": [0.02 * rng.standard_normal((ny, nx + 1)) for _ in tb],
+                  "V": [0.02 * rng.standard_normal((ny + 1, nx)) for _ in tb]})
+    return M, st
+
+
+def _oracle_run(M, st, nstep, name_class, island):
+    """The reference's chunked stepping (mod.py:3288-3346) restated on the oracle."""
+    from oracle.qg_ml import QGOracle
+    from oracle.sw import SWOracle
+    nl, ny, nx = M.nl, M.ny, M.nx
+    p = dict(nx=nx, ny=ny, nl=nl, dx=st.DX.T, dy=st.DY.T, H=np.asarray(M.H0), g_prime=np.array([9.81, 0.025, 0.0125][:nl]),
+             f=np.pad(M.f.T, ((0, 1), (0, 1)), mode="edge"), taux=0., tauy=0., bottom_drag_coef=2e-7, dt=M.dt,
+             mask=(1 - st.mask.astype(int).T), slip_coef=0.5, visc_coef=30.0, diff_coef=20.0, sponge_coef=0.0)
+    o = QGOracle(p) if name_class == "QG" else SWOracle(p)
+    u = st.var["u_layers"].transpose(0, 2, 1)[None]
+    v = st.var["v_layers"].transpose(0, 2, 1)[None]
+    h = st.var["h_layers"].transpose(0, 2, 1)[None]
+    lay0 = lambda a, s=1.0: np.concatenate([a.T[None] * s, np.zeros((nl - 1,) + a.T.shape)])[None]
+    F = [lay0(st.params[k], 1.0 / 86400) for k in ("u", "v", "ssh")]
+    done, t = 0, 0.0
+    while done < nstep:
+        n = min(nstep - done, M.max_nstep)
+        tc = t + done * M.dt
+        ub, vb, hb = M._apply_bc(tc, int(tc + n * M.dt))
+        ub, vb, hb = ub + st.params["u_b"], vb + st.params["v_b"], hb + st.params["h_b"]
+        u, v, h = o.step(u, v, h, nstep=n, u_b=lay0(ub), v_b=lay0(vb), h_b=lay0(hb), Fu=F[0], Fv=F[1], Fh=F[2])
+        done += n
+    return u, v, h
+
+
+@pytest.mark.parametrize("name_class,nl,island", [("SW", 2, True), ("QG", 3, True)])
+def test_step_matches_oracle(name_class, nl, island):
+    M, st = setup(name_class, nl, island)
+    ref = _oracle_run(M, st, 5, name_class, island)
+    s2 = st.copy()
+    M.step(s2, nstep=5, t=0)
+    for k, r in zip(("u_layers", "v_layers", "h_layers"), ref):
+        a = s2.var[k]
+        b = r[0].transpose(0, 2, 1)
+        assert np.abs(a - b).max() <= 1e-10 * np.abs(b).max(), k
+    assert np.allclose(s2.var["ssh"], s2.var["h_layers"].sum(0))
+
+
+@pytest.mark.parametrize("name_class,nl,island", [("SW", 2, True), ("SW", 1, False), ("QG", 3, True)])
+def test_state_level_adjoint(name_class, nl, island):
+    M, st = setup(name_class, nl, island)
+    rng = np.random.default_rng(9)
+    ny, nx = M.ny, M.nx
+    ocean = ~st.mask
+    d = st.copy()
+    for k in list(d.var):
+        d.var[k] = rng.standard_normal(d.var[k].shape) * (ocean if d.var[k].shape[-2:] == (ny, nx) else 1)
+    if nl > 1:
+        d.var["u"], d.var["v"] = d.var["u_layers"][0].copy(), d.var["v_layers"][0].copy()
+        d.var["ssh"] = d.var["h_layers"].sum(0)
+    for k in list(d.params):
+        d.params[k] = rng.standard_normal(d.params[k].shape)
+    M.step_tgl(d, st, nstep=3, t=0)
+    w = st.copy()
+    for k in list(w.var):
+        w.var[k] = rng.standard_normal(w.var[k].shape)
+    for k in list(w.params):
+        w.params[k] = np.zeros_like(w.params[k])
+    d0 = st.copy()
+    rng2 = np.random.default_rng(9)
+    for k in list(d0.var):
+        d0.var[k] = rng2.standard_normal(d0.var[k].shape) * (ocean if d0.var[k].shape[-2:] == (ny, nx) else 1)
+    if nl > 1:
+        d0.var["u"], d0.var["v"] = d0.var["u_layers"][0].copy(), d0.var["v_layers"][0].copy()
+        d0.var["ssh"] = d0.var["h_layers"].sum(0)
+    for k in list(d0.params):
+        d0.params[k] = rng2.standard_normal(d0.params[k].shape)
+    a = w.copy()
+    M.step_adj(a, st, nstep=3, t=0)
+    if nl > 1:
+        keys = ["u_layers", "v_layers", "h_layers"]
+        lhs = sum(float((d.var[k] * w.var[k]).sum()) for k in keys)
+        # the surface diagnostics of the tangent are functions of the layers
+        lhs += float((d.var["ssh"] * w.var["ssh"]).sum() + (d.var["u"] * w.var["u"]).sum()
+                     + (d.var["v"] * w.var["v"]).sum())
+    else:
+        keys = ["u", "v", "ssh"]
+        lhs = sum(float((d.var[k] * w.var[k]).sum()) for k in keys)
+    rhs = sum(float((d0.var[k] * a.var[k]).sum()) for k in keys)
+    rhs += sum(float((d0.params[k] * a.params[k]).sum()) for k in a.params)
+    assert abs(lhs - rhs) <= 1e-9 * abs(lhs)
