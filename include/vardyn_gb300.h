@@ -578,6 +578,25 @@ void vd_qgp_plan_destroy(vd_qgp_plan* plan);
 vd_status vd_qgp_op(const vd_qgp_plan* plan, int op, int batch, const void* const* args,
                     void* stream);
 
+/* ------------------------------------------------------------------------
+ * Batched float64 vector kernels of the outer minimisation (L-BFGS without
+ * bounds for batch independent windows, mapping/src/inv.py:309-414):
+ * arrays are [batch][n]; coefficients are per-window device arrays so the
+ * two-loop recursion needs no host round trip.
+ * ---------------------------------------------------------------------- */
+size_t vd_bdot_workspace_bytes(int batch, long long n);
+/* out[b] = c0[b] + c1[b] * (x[b] . y[b]); c0 / c1 nullable (0 / 1);
+ * deterministic (fixed reduction order). */
+vd_status vd_bdot_f64(int batch, long long n, const double* x, const double* y,
+                      const double* c0, const double* c1, double* out, void* work,
+                      size_t work_bytes, void* stream);
+/* y[b] = beta * y[b] + scale * coef[b] * x[b]; coef nullable (1). */
+vd_status vd_baxpy_f64(int batch, long long n, double scale, const double* coef,
+                       const double* x, double beta, double* y, void* stream);
+/* z[b] = x[b] + coef[b] * y[b] */
+vd_status vd_bxpay_f64(int batch, long long n, const double* x, const double* coef,
+                       const double* y, double* z, void* stream);
+
 /* Version / build information string. */
 const char* vd_version(void);
 /* Number of kernels this library has launched in the process so far (also

@@ -190,6 +190,10 @@ SIGNATURES = {
     "vd_qgp_plan_destroy": (None, [P]),
     "vd_qgp_op": (I, [P, I, I, P, P]),
     "vd_edge_pad_adj": (I, [I, I, I, I, P, P, P, P]),
+    "vd_bdot_workspace_bytes": (SZ, [I, LL]),
+    "vd_bdot_f64": (I, [I, LL, P, P, P, P, P, P, SZ, P]),
+    "vd_baxpy_f64": (I, [I, LL, D, P, P, D, P, P]),
+    "vd_bxpay_f64": (I, [I, LL, P, P, P, P, P]),
     "vd_mg_plan_create": (I, [ctypes.POINTER(P), ctypes.POINTER(VdMgDesc)]),
     "vd_mg_plan_destroy": (I, [P]),
     "vd_mg_levels": (I, [P]),
