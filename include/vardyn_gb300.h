@@ -578,6 +578,17 @@ void vd_qgp_plan_destroy(vd_qgp_plan* plan);
 vd_status vd_qgp_op(const vd_qgp_plan* plan, int op, int batch, const void* const* args,
                     void* stream);
 
+/* Observation-operator construction on the device (obsop.py:417-460): for
+ * each of nobs planar positions (km) the npix <= 4 nearest points of the
+ * uniform (ny, nx) grid with spacing dx_km, dy_km (point (i, j) at (i dx,
+ * j dy)), neighbours beyond dmax_km dropped (index -1, weight 0), Gaussian
+ * weights exp(-D^2 / (2 (dmax/2)^2)) normalised per observation (npix = 1:
+ * weight 1). idx [nobs][4] = j * nx + i, w [nobs][4] (float64). Ties in
+ * distance go to the smaller index. */
+vd_status vd_obs_knn(long long nobs, const double* x_km, const double* y_km, int ny, int nx,
+                     double dx_km, double dy_km, int npix, double dmax_km, long long* idx,
+                     double* w, void* stream);
+
 /* ------------------------------------------------------------------------
  * Batched float64 vector kernels of the outer minimisation (L-BFGS without
  * bounds for batch independent windows, mapping/src/inv.py:309-414):

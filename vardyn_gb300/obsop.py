@@ -2,12 +2,15 @@
 
 Mirrors ``Obsop_interp_l3_jax`` (mapping/src/obsop.py:375-678):
 
-- operator construction on the host, once per window set, as the reference
-  does in ``process_obs``/``_sparse_op`` (obsop.py:417-460, 486-604): the
-  ``npix`` nearest grid points by KDTree, neighbours beyond ``dmax``
-  (obsop.py:406) dropped, Gaussian weights exp(-d^2/(2(dmax/2)^2))
-  normalised per observation. Synthetic Cartesian grids use planar km
-  coordinates where the reference uses 3-D Cartesian km from lon/lat;
+- operator construction once per window set, as the reference does in
+  ``process_obs``/``_sparse_op`` (obsop.py:417-460, 486-604): the ``npix``
+  nearest grid points, neighbours beyond ``dmax`` (obsop.py:406) dropped,
+  Gaussian weights exp(-d^2/(2(dmax/2)^2)) normalised per observation. The
+  neighbour search and the weights run on the GPU (vd_obs_knn, a scan of the
+  dmax disc: exactly the valid neighbours of a k-nearest search);
+  ``build='host'`` uses a KDTree on the host instead. Synthetic Cartesian
+  grids use planar km coordinates where the reference uses 3-D Cartesian km
+  from lon/lat;
 - misfit ``inverr*(Hx - y)`` with NaN -> 0 (obsop.py:610-628) and its adjoint
   (obsop.py:630-678) as GPU kernels (vd_obs_misfit / vd_obs_adjoint).
 
@@ -51,6 +54,19 @@ def interp_rows(x_km, y_km, ny, nx, dx, dy, npix=4):
     return idx, w
 
 
+def interp_rows_gpu(x_km, y_km, ny, nx, dx, dy, npix=4, device="cuda"):
+    """interp_rows on the GPU (vd_obs_knn); returns host arrays (idx with
+    -1 for dropped neighbours, w), shapes [n, npix]."""
+    x = torch.as_tensor(np.ascontiguousarray(x_km, dtype=np.float64), device=device)
+    y = torch.as_tensor(np.ascontiguousarray(y_km, dtype=np.float64), device=device)
+    n = x.numel()
+    idx = torch.empty((max(n, 1), 4), dtype=torch.int64, device=device)
+    w = torch.empty((max(n, 1), 4), dtype=torch.float64, device=device)
+    _lib.call("vd_obs_knn", n, _p(x), _p(y), ny, nx, dx / 1e3, dy / 1e3, npix, dmax_km(dx, dy, npix), _p(idx), _p(w),
+              _stream())
+    return idx[:n, :npix].cpu().numpy(), w[:n, :npix].cpu().numpy()
+
+
 def _p(t):
     return ctypes.c_void_p(t.data_ptr())
 
@@ -66,9 +82,12 @@ class AlongTrackObs:
     ``step`` (model step index at which the point is observed), ``yobs`` and
     ``err`` (observation error, the reference's ``errobs``)."""
 
-    def __init__(self, windows, ny, nx, dx, dy, dtype=torch.float32, device="cuda", npix=4):
+    def __init__(self, windows, ny, nx, dx, dy, dtype=torch.float32, device="cuda", npix=4, build="gpu"):
         if npix > 4:
             raise ValueError("at most 4 neighbours per observation")
+        if build not in ("gpu", "host"):
+            raise ValueError("build is 'gpu' or 'host'")
+        rows = interp_rows_gpu if build == "gpu" else interp_rows
         self.B = len(windows)
         self.ny, self.nx = ny, nx
         self.dtype = dtype
@@ -77,7 +96,7 @@ class AlongTrackObs:
         fields, steps, idxs, ws, ys, errs = [], [], [], [], [], []
         for b, win in enumerate(windows):
             x = np.asarray(win["x_km"], dtype=np.float64)
-            idx, w = interp_rows(x, np.asarray(win["y_km"], dtype=np.float64), ny, nx, dx, dy, npix)
+            idx, w = rows(x, np.asarray(win["y_km"], dtype=np.float64), ny, nx, dx, dy, npix)
             pad = 4 - npix
             if pad:
                 idx = np.pad(idx, ((0, 0), (0, pad)), constant_values=-1)
