@@ -339,6 +339,21 @@ typedef struct vd_bm_params {
 } vd_bm_params;
 
 vd_status vd_bm_plan_create(vd_bm_plan** out, const vd_basis_grid* grid, const vd_bm_params* params);
+
+/* Wavelet basis (Basis_wavelet3d, basis.py:2640-2985): the same atoms as the
+ * wave packets, a lattice laid out from the domain centre, time centres of
+ * every time frequency (Gaspari-Cohn windows) shared by all space
+ * frequencies. The plan is a vd_bm_plan: every vd_bm_* query and projection
+ * below applies (vd_bm_frequency's tdec is the first time scale). */
+typedef struct vd_wavelet_params {
+    double npsp, facpsp;        /* wavelet extension / frequency step (2647-2649) */
+    double facnst;              /* lattice density in space and time */
+    double lmin, lmax;          /* wavelength range [km] */
+    double tmin, tmax;          /* period range [days] */
+    double sigma_Q;             /* prior std of every coefficient */
+} vd_wavelet_params;
+vd_status vd_wavelet_plan_create(vd_bm_plan** out, const vd_basis_grid* grid,
+                                 const vd_wavelet_params* params);
 vd_status vd_bm_plan_destroy(vd_bm_plan* plan);
 long long vd_bm_nbasis(const vd_bm_plan* plan);
 /* Number of frequencies and directions; theta_host [ntheta] if non-NULL. */

@@ -379,3 +379,121 @@ class BMOracle:
             for it, fct in self.time_weights(iff, t):
                 blk[it] += fct * ad
         return adX
+
+
+def gaspari_cohn(r, c=1):
+    """Gaspari-Cohn taper of mapping/src/tools.py:16-46 (scalar r)."""
+    if c <= 0:
+        return 0.0
+    ra = 2 * abs(r) / c
+    if ra <= 1.:
+        return -0.25 * ra ** 5 + 0.5 * ra ** 4 + 0.625 * ra ** 3 - 5. / 3. * ra ** 2 + 1.
+    if 1. < ra <= 2.:
+        return 1. / 12. * ra ** 5 - 0.5 * ra ** 4 + 0.625 * ra ** 3 + 5. / 3. * ra ** 2 - 5. * ra + 4. - 2. / 3. / ra
+    return 0.0
+
+
+class WaveletOracle(BMOracle):
+    """Wavelet basis of the reference (Basis_wavelet3d, mapping/src/basis.py:
+    2640-2985; the numpy form: the jax subclass's time routine reads
+    attributes the class never sets).
+
+    Space and time pseudo-frequencies between lmin..lmax and tmin..tmax
+    (2689-2707, periods above the maximum dropped), directions (2710), per
+    space frequency a lattice laid out from the domain centre with spacing
+    DXs/facnst (2717-2771; a centre whose box of half-width 0.5/fs is fully
+    masked is dropped), per time frequency centres from the time centre with
+    spacing DXt/facnst (2773-2796), Gaspari-Cohn time weights divided by the
+    running integral's maximum (|dt| < DXt, kept when non-zero, 2902-2922),
+    Q = sigma_Q. Coefficients of one space frequency: [time centre over all
+    time frequencies][space centre][theta][cos, sin]."""
+
+    def __init__(self, lon, lat, npsp=3.5, facpsp=1.5, facnst=1., lmin=80., lmax=900., tmin=2., tmax=20.,
+                 sigma_Q=1.0, mask=None, geo=False):
+        super().__init__(lon, lat, npsp=npsp, facpsp=facpsp, lmin=lmin, lmax=lmax, mask=mask, geo=geo)
+        self.facnst, self.tmin, self.tmax, self.sigma_Q = float(facnst), float(tmin), float(tmax), float(sigma_Q)
+
+    @staticmethod
+    def _centred(c, lo, hi, step):
+        return np.concatenate((np.arange(c, lo, -step)[::-1], np.arange(c, hi, step)[1:]))
+
+    def set_basis(self, time):
+        time = np.asarray(time, float)
+        TIME_MIN, TIME_MAX = time.min(), time.max()
+        LON_MIN, LON_MAX, LAT_MIN, LAT_MAX = self.lon_min, self.lon_max, self.lat_min, self.lat_max
+        if LON_MAX < LON_MIN:
+            LON_MAX = LON_MAX + 360.
+        k2 = self.km2deg
+        step = np.log(1 + self.facpsp / self.npsp)
+        logfs = np.arange(np.log(1. / self.lmin), np.log(1. / self.lmax) - step, -step)[::-1]
+        fs = np.exp(logfs)
+        fs = fs[1 / fs <= self.lmax]
+        dfs = fs[1:] - fs[:-1]
+        logft = np.arange(np.log(1. / self.tmin), np.log(1. / self.tmax) - step, -step)[::-1]
+        ft = np.exp(logft)
+        ft = ft[1 / ft <= self.tmax]
+        theta = np.linspace(0, np.pi, int(np.pi * fs[0] / dfs[0] * self.facpsp))[:-1]
+        ntheta, nf = len(theta), len(fs)
+        DXs = 1. / fs * self.npsp * 0.5
+        ENSLON, ENSLAT = [], []
+        NS = np.zeros(nf, dtype=int)
+        for iff in range(nf):
+            el, ea = [], []
+            lats = self._centred((LAT_MIN + LAT_MAX) / 2, LAT_MIN - DXs[iff] * k2, LAT_MAX + DXs[iff] * k2,
+                                 DXs[iff] / self.facnst * k2)
+            for la in lats:
+                cl = self._cos(la)
+                lons = self._centred((LON_MIN + LON_MAX) / 2, LON_MIN - DXs[iff] / cl * k2,
+                                     LON_MAX + DXs[iff] / cl * k2, DXs[iff] / self.facnst / cl * k2)
+                for lo in lons:
+                    if self.mask1d is not None:
+                        ind = np.where((np.abs((self.lon1d - lo) / k2 * cl) <= .5 / fs[iff]) &
+                                       (np.abs((self.lat1d - la) / k2) <= .5 / fs[iff]))[0]
+                        if np.all(self.mask1d[ind]):
+                            continue
+                    el.append(lo)
+                    ea.append(la)
+            ENSLON.append(np.array(el))
+            ENSLAT.append(np.array(ea))
+            NS[iff] = len(el)
+        DXt = 1. / ft * self.npsp * 0.5
+        enst, tsc, tnorm = [], [], []
+        for ift in range(len(ft)):
+            e = self._centred((TIME_MIN + TIME_MAX) / 2, TIME_MIN - DXt[ift], TIME_MAX + DXt[ift],
+                              DXt[ift] / self.facnst)
+            tt = np.linspace(-DXt[ift], DXt[ift])
+            tmp = np.zeros_like(tt)
+            for i in range(tt.size - 1):
+                tmp[i + 1] = tmp[i] + gaspari_cohn(tt[i], DXt[ift]) * (tt[i + 1] - tt[i])
+            enst.extend(e.tolist())
+            tsc.extend([DXt[ift]] * e.size)
+            tnorm.extend([tmp.max()] * e.size)
+        Q, bounds, iw = [], [], 0
+        for iff in range(nf):
+            bounds.append(iw)
+            if NS[iff] > 0:
+                n = 2 * len(enst) * ntheta * NS[iff]
+                Q.append(self.sigma_Q * np.ones(n))
+                iw += n
+        bounds.append(iw)
+        self.ff, self.theta, self.ntheta, self.nf, self.DX = fs, theta, ntheta, nf, DXs
+        self.ENSLON, self.ENSLAT, self.NP = ENSLON, ENSLAT, NS
+        self.enst = [np.array(enst)] * nf
+        self.tscale, self.tnorm = np.array(tsc), np.array(tnorm)
+        self.k = 2 * np.pi * fs
+        self.bounds = bounds
+        self.nbasis = iw
+        self.Q = np.concatenate(Q) if Q else np.zeros(0)
+        self.Gx = [self._space(iff) for iff in range(nf)]
+        self.times = time
+        return np.zeros_like(self.Q), self.Q
+
+    def time_weights(self, iff, t):
+        out = []
+        for it, tc in enumerate(self.enst[iff]):
+            dt = t - tc
+            if abs(dt) < self.tscale[it]:
+                fact = gaspari_cohn(dt, self.tscale[it]) / self.tnorm[it]
+                if fact != 0:
+                    out.append((it, fact))
+        return out

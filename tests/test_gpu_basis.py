@@ -259,3 +259,32 @@ def test_bm_reference_facing_class():
     adX = b.operg_transpose(3.0, ad)
     assert rel(adX, o.operg_transpose(3.0, ad0)) < 1e-12
     assert np.all(ad["ssh"] == 0)
+
+
+def test_wavelet_projection_matches_oracle():
+    """Wavelet basis G and G^T (wave-packet kernels on the wavelet tables)
+    against the oracle's sparse form, float64, with land."""
+    from oracle.basis import WaveletOracle
+    from vardyn_gb300.basis import WaveletParams, WaveletPlan
+    x = np.arange(64) * 8.0
+    y = np.arange(48) * 8.0
+    prm = dict(npsp=3.5, facpsp=1.5, facnst=1., lmin=60., lmax=250., tmin=3., tmax=15., sigma_Q=0.02)
+    land = np.zeros((48, 64), bool)
+    land[20:30, 25:40] = True
+    time = np.arange(0, 20, 0.5)
+    pl = WaveletPlan(x, y, time, WaveletParams(**prm), land=land, dtype=torch.float64)
+    X2, Y2 = np.meshgrid(x, y)
+    o = WaveletOracle(X2, Y2, mask=land, **prm)
+    o.set_basis(time)
+    rng = np.random.default_rng(3)
+    X = rng.standard_normal((2, pl.nbasis))
+    ad = rng.standard_normal((2, 48, 64))
+    for k in (0, 9, 25, time.size - 1):
+        phi = pl.project(k, torch.as_tensor(X, device="cuda")).cpu().numpy()
+        adX = torch.zeros((2, pl.nbasis), dtype=torch.float64, device="cuda")
+        pl.project_T(k, torch.as_tensor(ad, device="cuda"), adX)
+        for b in range(2):
+            ref = o.operg(time[k], X[b])
+            assert np.abs(phi[b] - ref).max() <= 1e-12 * max(1.0, np.abs(ref).max())
+            refT = o.operg_transpose(time[k], ad[b])
+            assert np.abs(adX[b].cpu().numpy() - refT).max() <= 1e-12 * max(1.0, np.abs(refT).max())

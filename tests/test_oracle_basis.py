@@ -204,3 +204,37 @@ def test_bm_oracle_transpose_identity():
         assert np.all(phi[mask] == 0)
         lhs, rhs = np.sum(phi * a), np.dot(X, o.operg_transpose(t, a))
         assert abs(lhs - rhs) <= 1e-12 * max(abs(lhs), 1.0)
+
+
+@pytest.mark.parametrize("geo", [False, True])
+def test_wavelet_host_tables_match_oracle(geo):
+    """Wavelet basis (Basis_wavelet3d): lattice and time centres equal the
+    oracle's exactly, time weights and Q to rounding."""
+    from oracle.basis import WaveletOracle
+    from vardyn_gb300.basis import WaveletParams, WaveletPlan
+    if geo:
+        x = 5.0 + np.arange(40) * 0.08
+        y = 35.0 + np.arange(36) * 0.07
+        prm = dict(npsp=3.5, facpsp=1.5, facnst=1., lmin=60., lmax=250., tmin=3., tmax=15., sigma_Q=0.02)
+    else:
+        x = np.arange(60) * 8.0
+        y = np.arange(50) * 8.0
+        prm = dict(npsp=3.5, facpsp=1.5, facnst=1.2, lmin=60., lmax=250., tmin=3., tmax=15., sigma_Q=0.02)
+    land = np.zeros((y.size, x.size), bool)
+    land[10:20, 12:25] = True
+    time = np.arange(0, 30, 0.25)
+    pl = WaveletPlan(x, y, time, WaveletParams(**prm), land=land, geographic=geo, host_only=True)
+    X2, Y2 = np.meshgrid(x, y)
+    o = WaveletOracle(X2, Y2, mask=land, geo=geo, **prm)
+    _, Q = o.set_basis(time)
+    assert (pl.nbasis, pl.nf, pl.ntheta) == (o.nbasis, o.nf, o.ntheta)
+    for iff in range(o.nf):
+        enst, lat, lon = pl.lattice(iff)
+        assert np.array_equal(enst, o.enst[iff])
+        assert np.array_equal(lat, o.ENSLAT[iff]) and np.array_equal(lon, o.ENSLON[iff])
+    for k in range(0, time.size, 7):
+        for iff in range(o.nf):
+            a, b = pl.time_weights(k, iff), o.time_weights(iff, time[k])
+            assert [i for i, _ in a] == [i for i, _ in b]
+            assert all(abs(u[1] - v[1]) <= 1e-14 for u, v in zip(a, b))
+    assert np.array_equal(pl.q(), Q)

@@ -103,6 +103,11 @@ class VdSwDesc(ctypes.Structure):
     ]
 
 
+class VdWaveletParams(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_double) for k in ("npsp", "facpsp", "facnst", "lmin", "lmax", "tmin", "tmax",
+                                                "sigma_Q")]
+
+
 class VdQgpDesc(ctypes.Structure):
     _fields_ = [
         ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nl", ctypes.c_int), ("dtype", ctypes.c_int),
@@ -202,6 +207,7 @@ SIGNATURES = {
     "vd_mg_solve": (I, [P, P, P, P, SZ, P]),
     "vd_mg_residual": (I, [P, P, P, P, P]),
     "vd_bm_plan_create": (I, [ctypes.POINTER(P), ctypes.POINTER(VdBasisGrid), ctypes.POINTER(VdBmParams)]),
+    "vd_wavelet_plan_create": (I, [ctypes.POINTER(P), ctypes.POINTER(VdBasisGrid), ctypes.POINTER(VdWaveletParams)]),
     "vd_bm_plan_destroy": (I, [P]),
     "vd_bm_nbasis": (LL, [P]),
     "vd_bm_shape": (I, [P, ctypes.POINTER(I), ctypes.POINTER(I), P]),

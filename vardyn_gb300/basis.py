@@ -264,6 +264,41 @@ class BMPlan(_SeparablePlan):
         return list(zip(it[:n.value].tolist(), w[:n.value].tolist()))
 
 
+class WaveletParams:
+    """Parameters of the wavelet basis (config.BASIS fields of
+    Basis_wavelet3d, basis.py:2647-2656)."""
+
+    def __init__(self, npsp=3.5, facpsp=1.5, facnst=1., lmin=80., lmax=900., tmin=2., tmax=20., sigma_Q=1.0):
+        self.__dict__.update(dict(npsp=npsp, facpsp=facpsp, facnst=facnst, lmin=lmin, lmax=lmax, tmin=tmin,
+                                  tmax=tmax, sigma_Q=sigma_Q))
+
+    def to_c(self):
+        return _lib.VdWaveletParams(*[float(getattr(self, k)) for k in (
+            "npsp", "facpsp", "facnst", "lmin", "lmax", "tmin", "tmax", "sigma_Q")])
+
+
+class WaveletPlan(BMPlan):
+    """Wavelet basis (Basis_wavelet3d, basis.py:2640-2985) on a rectilinear
+    grid: the wave-packet plan's atoms and kernels with the wavelet lattice
+    and Gaspari-Cohn time weights."""
+
+    def __init__(self, xc, yc, time, params, land=None, geographic=False, dtype=torch.float32, device=None,
+                 host_only=False):
+        self._grid(xc, yc, time, land, geographic, dtype, device, host_only)
+        self.params = params
+        h = ctypes.c_void_p()
+        pc = params.to_c()
+        _lib.check(self.lib.vd_wavelet_plan_create(ctypes.byref(h), ctypes.byref(self._gridc), ctypes.byref(pc)),
+                   "vd_wavelet_plan_create")
+        self._h = h
+        self.nbasis = int(self.lib.vd_bm_nbasis(h))
+        nf, nth = ctypes.c_int(), ctypes.c_int()
+        _lib.check(self.lib.vd_bm_shape(h, ctypes.byref(nf), ctypes.byref(nth), None), "vd_bm_shape")
+        self.nf, self.ntheta = nf.value, nth.value
+        self.theta = np.zeros(self.ntheta)
+        _lib.check(self.lib.vd_bm_shape(h, None, None, self.theta.ctypes.data), "vd_bm_shape")
+
+
 # ---------------------------------------------------------------------------
 # Reference-facing classes
 # ---------------------------------------------------------------------------
@@ -441,3 +476,33 @@ class Basis_multi:
             parts.append(self.plan.project(k, Xc.reshape(1, -1))[0].reshape(-1))
         phi = torch.cat(parts)
         return phi if is_t else phi.double().cpu().numpy()
+
+
+class Basis_wavelet3d(Basis_gauss3d):
+    """Drop-in for Basis_wavelet3d (basis.py:2640-2985) with the GPU
+    projection; background files (path_background) are not supported."""
+
+    def __init__(self, config, State, multi_mode=False, dtype=torch.float32, device=None):
+        cb = config.BASIS
+        pb = getattr(cb, "path_background", None)
+        if pb is not None:
+            import os
+            if os.path.exists(pb):
+                raise NotImplementedError("config.BASIS.path_background is not supported by the GPU basis")
+        self.params = WaveletParams(npsp=cb.npsp, facpsp=cb.facpsp, facnst=cb.facnst, lmin=cb.lmin, lmax=cb.lmax,
+                                    tmin=cb.tmin, tmax=cb.tmax, sigma_Q=cb.sigma_Q)
+        self.name_mod_var = cb.name_mod_var
+        self.multi_mode = multi_mode
+        self.lon, self.lat = _grid_axes(State)
+        self.geographic = True
+        self.ny, self.nx = State.ny, State.nx
+        self.mask = None
+        if getattr(State, "mask", None) is not None and np.any(State.mask):
+            self.mask = np.asarray(State.mask, dtype=bool)
+        self.dtype = dtype
+        self.device = torch.device(device or "cuda")
+        self.plan = None
+
+    def _make_plan(self, time):
+        return WaveletPlan(self.lon, self.lat, time, self.params, land=self.mask, geographic=self.geographic,
+                           dtype=self.dtype, device=self.device)

@@ -30,6 +30,7 @@ using namespace vd::basis_host;
 struct BmFreq {
     double ff = 0, k = 0, DX = 0, DXG = 0, tdec = 0, norm_fact = 1, Q = 0;
     std::vector<double> enst;
+    std::vector<double> tscale, tnorm;   // wavelet basis: per time centre DXt and norm_fact
     std::vector<double> rows_lat;
     std::vector<std::vector<double>> row_lons;
     std::vector<double> enslat, enslon;
@@ -46,6 +47,8 @@ struct vd_bm_plan {
     long long nbasis = 0;
     int R = 0, KX = 1, KY = 1, NA = 1;
     vd_bm_params prm;
+    int kind = 0;                 // 0 wave packets (Basis_bm), 1 wavelets (Basis_wavelet3d)
+    vd_wavelet_params wprm;
     std::vector<double> theta;
     std::vector<BmFreq> fr;
     std::vector<double> times;
@@ -219,6 +222,156 @@ struct BmTables {
     std::vector<double> fx_c, fx_s, fy_c, fy_s;
 };
 
+// Lattice rows share x patterns: same centres, same cos(lat), same frequency.
+struct PatState {
+    std::map<std::vector<double>, int> pat_of;
+    std::vector<std::vector<std::vector<std::pair<int, double>>>> pat_cols;   // [pat][x] -> (i, xx)
+    std::vector<int> pat_n, pat_freq;
+};
+
+void add_row(vd_bm_plan* p, BmTables& tb, PatState& ps, int iff, double la, double cl,
+             const std::vector<double>& lons, const std::vector<double>& xc, double k2, long long& cb)
+{
+    BmFreq& F = p->fr[iff];
+    const int nx = (int)xc.size();
+    std::vector<double> key = lons;
+    key.push_back(cl);
+    key.push_back((double)iff);
+    int pat;
+    auto it = ps.pat_of.find(key);
+    if (it != ps.pat_of.end()) {
+        pat = it->second;
+    } else {
+        pat = (int)ps.pat_cols.size();
+        ps.pat_of[key] = pat;
+        std::vector<std::vector<std::pair<int, double>>> cols((size_t)nx);
+        for (int x = 0; x < nx; ++x)
+            for (int i = 0; i < (int)lons.size(); ++i) {
+                const double xx = (xc[x] - lons[i]) / k2 * cl;
+                if (std::fabs(xx) <= F.DX) cols[x].push_back({i, xx});
+            }
+        ps.pat_cols.push_back(std::move(cols));
+        ps.pat_n.push_back((int)lons.size());
+        ps.pat_freq.push_back(iff);
+    }
+    tb.row_freq.push_back(iff);
+    tb.row_pat.push_back(pat);
+    tb.row_n.push_back((int)lons.size());
+    tb.row_cb.push_back(cb);
+    F.row_lons.push_back(lons);
+    for (double lo : lons) {
+        F.enslat.push_back(la);
+        F.enslon.push_back(lo);
+    }
+    cb += (long long)lons.size();
+}
+
+// x tables (ELL per pattern and column, CSR per centre) and y tables (ELL per
+// frequency and row, CSR per lattice row), with the per-direction cos / sin
+// factors of the angle-sum split (sqrt(2) folded into y).
+void build_xy(vd_bm_plan* p, BmTables& tb, const PatState& ps, const std::vector<double>& yc, double k2, int ny,
+              int nx)
+{
+    const std::vector<double>& th = p->theta;
+    int KX = 1;
+    for (auto& pc : ps.pat_cols)
+        for (auto& col : pc) KX = std::max(KX, (int)col.size());
+    p->KX = KX;
+    const int P = (int)ps.pat_cols.size(), nth = p->nth;
+    tb.fx_i.assign((size_t)P * nx * KX, -1);
+    tb.fx_c.assign((size_t)P * nth * nx * KX, 0.0);
+    tb.fx_s.assign((size_t)P * nth * nx * KX, 0.0);
+    tb.tx_ptr.push_back(0);
+    for (int pt = 0; pt < P; ++pt) {
+        const BmFreq& F = p->fr[ps.pat_freq[pt]];
+        tb.pat_cbase.push_back((int)tb.tx_ptr.size() - 1);
+        std::vector<std::vector<std::pair<int, int>>> by_centre((size_t)ps.pat_n[pt]);
+        for (int x = 0; x < nx; ++x) {
+            const auto& col = ps.pat_cols[pt][x];
+            for (size_t e = 0; e < col.size(); ++e) {
+                const double xx = col[e].second;
+                const double wx = mywindow(xx / F.DX);
+                tb.fx_i[((size_t)pt * nx + x) * KX + e] = col[e].first;
+                for (int t = 0; t < nth; ++t) {
+                    const double kx = F.k * std::cos(th[t]);
+                    const size_t w = (((size_t)pt * nth + t) * nx + x) * KX + e;
+                    tb.fx_c[w] = wx * std::cos(kx * xx);
+                    tb.fx_s[w] = wx * std::sin(kx * xx);
+                }
+                by_centre[col[e].first].push_back({x, (int)e});
+            }
+        }
+        for (auto& lst : by_centre) {
+            for (auto& pr : lst) {
+                tb.tx_x.push_back(pr.first);
+                tb.tx_e.push_back(pr.second);
+            }
+            tb.tx_ptr.push_back((int32_t)tb.tx_x.size());
+        }
+    }
+    std::vector<std::vector<std::vector<std::pair<int, double>>>> ycols((size_t)p->nf);
+    int KY = 1;
+    for (int iff = 0; iff < p->nf; ++iff) {
+        const BmFreq& F = p->fr[iff];
+        ycols[iff].resize((size_t)ny);
+        for (int y = 0; y < ny; ++y)
+            for (int j = 0; j < (int)F.rows_lat.size(); ++j) {
+                const double yy = (yc[y] - F.rows_lat[j]) / k2;
+                if (std::fabs(yy) <= F.DX) ycols[iff][y].push_back({j, yy});
+            }
+        for (auto& l : ycols[iff]) KY = std::max(KY, (int)l.size());
+    }
+    p->KY = KY;
+    tb.fy_j.assign((size_t)p->nf * ny * KY, -1);
+    tb.fy_c.assign((size_t)p->nf * nth * ny * KY, 0.0);
+    tb.fy_s.assign((size_t)p->nf * nth * ny * KY, 0.0);
+    tb.ty_ptr.push_back(0);
+    for (int iff = 0; iff < p->nf; ++iff) {
+        const BmFreq& F = p->fr[iff];
+        std::vector<std::vector<std::pair<int, int>>> by_row(F.rows_lat.size());
+        for (int y = 0; y < ny; ++y) {
+            const auto& l = ycols[iff][y];
+            for (size_t e = 0; e < l.size(); ++e) {
+                const double yy = l[e].second;
+                const double wy = std::sqrt(2.0) * mywindow(yy / F.DX);
+                tb.fy_j[((size_t)iff * ny + y) * KY + e] = l[e].first;
+                for (int t = 0; t < nth; ++t) {
+                    const double ky = F.k * std::sin(th[t]);
+                    const size_t w = (((size_t)iff * nth + t) * ny + y) * KY + e;
+                    tb.fy_c[w] = wy * std::cos(ky * yy);
+                    tb.fy_s[w] = wy * std::sin(ky * yy);
+                }
+                by_row[l[e].first].push_back({y, (int)e});
+            }
+        }
+        for (auto& lst : by_row) {
+            for (auto& pr : lst) {
+                tb.ty_y.push_back(pr.first);
+                tb.ty_e.push_back(pr.second);
+            }
+            tb.ty_ptr.push_back((int32_t)tb.ty_y.size());
+        }
+    }
+}
+
+// active (time centre, weight) lists per (basis time, frequency), padded to NA
+void pack_time(vd_bm_plan* p, const std::vector<std::vector<std::pair<int, double>>>& act)
+{
+    int NA = 1;
+    for (auto& l : act) NA = std::max(NA, (int)l.size());
+    p->NA = NA;
+    p->tact_n.assign((size_t)p->ntime * p->nf, 0);
+    p->tact_it.assign((size_t)p->ntime * p->nf * NA, 0);
+    p->tact_g.assign((size_t)p->ntime * p->nf * NA, 0.0);
+    for (size_t s = 0; s < act.size(); ++s) {
+        p->tact_n[s] = (int)act[s].size();
+        for (size_t a = 0; a < act[s].size(); ++a) {
+            p->tact_it[s * NA + a] = act[s][a].first;
+            p->tact_g[s * NA + a] = act[s][a].second;
+        }
+    }
+}
+
 int bm_build(vd_bm_plan* p, const vd_basis_grid* g, BmTables& tb)
 {
     const vd_bm_params& q = p->prm;
@@ -265,9 +418,7 @@ int bm_build(vd_bm_plan* p, const vd_basis_grid* g, BmTables& tb)
     p->fr.resize(ff.size());
 
     // lattices, time centres, Q (basis.py:603-690)
-    std::map<std::vector<double>, int> pat_of;
-    std::vector<std::vector<std::vector<std::pair<int, double>>>> pat_cols;  // [pat][x] -> (i, xx)
-    std::vector<int> pat_n, pat_freq;
+    PatState ps;
     long long boff = 0;
     int rowoff = 0;
     for (int iff = 0; iff < p->nf; ++iff) {
@@ -305,37 +456,7 @@ int bm_build(vd_bm_plan* p, const vd_basis_grid* g, BmTables& tb)
                 }
                 lons.push_back(lo);
             }
-            // x pattern of this row: (centre, xx) per column within DX
-            std::vector<double> key = lons;
-            key.push_back(cl);
-            key.push_back((double)iff);
-            int pat;
-            auto it = pat_of.find(key);
-            if (it != pat_of.end()) {
-                pat = it->second;
-            } else {
-                pat = (int)pat_cols.size();
-                pat_of[key] = pat;
-                std::vector<std::vector<std::pair<int, double>>> cols((size_t)nx);
-                for (int x = 0; x < nx; ++x)
-                    for (int i = 0; i < (int)lons.size(); ++i) {
-                        const double xx = (xc[x] - lons[i]) / k2 * cl;
-                        if (std::fabs(xx) <= F.DX) cols[x].push_back({i, xx});
-                    }
-                pat_cols.push_back(std::move(cols));
-                pat_n.push_back((int)lons.size());
-                pat_freq.push_back(iff);
-            }
-            tb.row_freq.push_back(iff);
-            tb.row_pat.push_back(pat);
-            tb.row_n.push_back((int)lons.size());
-            tb.row_cb.push_back(cb);
-            F.row_lons.push_back(lons);
-            for (double lo : lons) {
-                F.enslat.push_back(la);
-                F.enslon.push_back(lo);
-            }
-            cb += (long long)lons.size();
+            add_row(p, tb, ps, iff, la, cl, lons, xc, k2, cb);
         }
         F.NP = cb;
         double td = q.tmeso * std::pow(q.lmeso, q.sloptdec) * std::pow(ff[iff], q.sloptdec);
@@ -356,93 +477,10 @@ int bm_build(vd_bm_plan* p, const vd_basis_grid* g, BmTables& tb)
     }
     p->nbasis = boff;
     p->R = rowoff;
-
-    // x tables: ELL (centre) + per-direction weights; CSR per centre (x, slot)
-    int KX = 1;
-    for (auto& pc : pat_cols)
-        for (auto& col : pc) KX = std::max(KX, (int)col.size());
-    p->KX = KX;
-    const int P = (int)pat_cols.size(), nth = p->nth;
-    tb.fx_i.assign((size_t)P * nx * KX, -1);
-    tb.fx_c.assign((size_t)P * nth * nx * KX, 0.0);
-    tb.fx_s.assign((size_t)P * nth * nx * KX, 0.0);
-    tb.tx_ptr.push_back(0);
-    for (int pt = 0; pt < P; ++pt) {
-        const BmFreq& F = p->fr[pat_freq[pt]];
-        tb.pat_cbase.push_back((int)tb.tx_ptr.size() - 1);
-        std::vector<std::vector<std::pair<int, int>>> by_centre((size_t)pat_n[pt]);
-        for (int x = 0; x < nx; ++x) {
-            const auto& col = pat_cols[pt][x];
-            for (size_t e = 0; e < col.size(); ++e) {
-                const double xx = col[e].second;
-                const double wx = mywindow(xx / F.DX);
-                tb.fx_i[((size_t)pt * nx + x) * KX + e] = col[e].first;
-                for (int t = 0; t < nth; ++t) {
-                    const double kx = F.k * std::cos(th[t]);
-                    const size_t w = (((size_t)pt * nth + t) * nx + x) * KX + e;
-                    tb.fx_c[w] = wx * std::cos(kx * xx);
-                    tb.fx_s[w] = wx * std::sin(kx * xx);
-                }
-                by_centre[col[e].first].push_back({x, (int)e});
-            }
-        }
-        for (auto& lst : by_centre) {
-            for (auto& pr : lst) {
-                tb.tx_x.push_back(pr.first);
-                tb.tx_e.push_back(pr.second);
-            }
-            tb.tx_ptr.push_back((int32_t)tb.tx_x.size());
-        }
-    }
-
-    // y tables: ELL (row) + per-direction weights with sqrt(2); CSR per row (y, slot)
-    std::vector<std::vector<std::vector<std::pair<int, double>>>> ycols((size_t)p->nf);
-    int KY = 1;
-    for (int iff = 0; iff < p->nf; ++iff) {
-        const BmFreq& F = p->fr[iff];
-        ycols[iff].resize((size_t)ny);
-        for (int y = 0; y < ny; ++y)
-            for (int j = 0; j < (int)F.rows_lat.size(); ++j) {
-                const double yy = (yc[y] - F.rows_lat[j]) / k2;
-                if (std::fabs(yy) <= F.DX) ycols[iff][y].push_back({j, yy});
-            }
-        for (auto& l : ycols[iff]) KY = std::max(KY, (int)l.size());
-    }
-    p->KY = KY;
-    tb.fy_j.assign((size_t)p->nf * ny * KY, -1);
-    tb.fy_c.assign((size_t)p->nf * nth * ny * KY, 0.0);
-    tb.fy_s.assign((size_t)p->nf * nth * ny * KY, 0.0);
-    tb.ty_ptr.push_back(0);
-    for (int iff = 0; iff < p->nf; ++iff) {
-        const BmFreq& F = p->fr[iff];
-        std::vector<std::vector<std::pair<int, int>>> by_row(F.rows_lat.size());
-        for (int y = 0; y < ny; ++y) {
-            const auto& l = ycols[iff][y];
-            for (size_t e = 0; e < l.size(); ++e) {
-                const double yy = l[e].second;
-                const double wy = std::sqrt(2.0) * mywindow(yy / F.DX);
-                tb.fy_j[((size_t)iff * ny + y) * KY + e] = l[e].first;
-                for (int t = 0; t < nth; ++t) {
-                    const double ky = F.k * std::sin(th[t]);
-                    const size_t w = (((size_t)iff * nth + t) * ny + y) * KY + e;
-                    tb.fy_c[w] = wy * std::cos(ky * yy);
-                    tb.fy_s[w] = wy * std::sin(ky * yy);
-                }
-                by_row[l[e].first].push_back({y, (int)e});
-            }
-        }
-        for (auto& lst : by_row) {
-            for (auto& pr : lst) {
-                tb.ty_y.push_back(pr.first);
-                tb.ty_e.push_back(pr.second);
-            }
-            tb.ty_ptr.push_back((int32_t)tb.ty_y.size());
-        }
-    }
+    build_xy(p, tb, ps, yc, k2, ny, nx);
 
     // time weights of the JAX form: |dt| <= tdec (basis.py:1026-1035)
     std::vector<std::vector<std::pair<int, double>>> act((size_t)p->ntime * p->nf);
-    int NA = 1;
     for (int kt = 0; kt < p->ntime; ++kt)
         for (int iff = 0; iff < p->nf; ++iff) {
             const BmFreq& F = p->fr[iff];
@@ -455,19 +493,169 @@ int bm_build(vd_bm_plan* p, const vd_basis_grid* g, BmTables& tb)
                     lst.push_back({it, fact});
                 }
             }
-            NA = std::max(NA, (int)lst.size());
         }
-    p->NA = NA;
-    p->tact_n.assign((size_t)p->ntime * p->nf, 0);
-    p->tact_it.assign((size_t)p->ntime * p->nf * NA, 0);
-    p->tact_g.assign((size_t)p->ntime * p->nf * NA, 0.0);
-    for (size_t s = 0; s < act.size(); ++s) {
-        p->tact_n[s] = (int)act[s].size();
-        for (size_t a = 0; a < act[s].size(); ++a) {
-            p->tact_it[s * NA + a] = act[s][a].first;
-            p->tact_g[s * NA + a] = act[s][a].second;
+    pack_time(p, act);
+    return VD_OK;
+}
+
+// Gaspari-Cohn function of mapping/src/tools.py:16-46 for one value
+double gaspari_cohn(double r, double c)
+{
+    if (c <= 0) return 0.0;
+    const double ra = 2 * std::fabs(r) / c;
+    if (ra <= 1.)
+        return -0.25 * std::pow(ra, 5) + 0.5 * std::pow(ra, 4) + 0.625 * std::pow(ra, 3) - 5. / 3. * (ra * ra) + 1.;
+    if (ra > 1. && ra <= 2.)
+        return 1. / 12. * std::pow(ra, 5) - 0.5 * std::pow(ra, 4) + 0.625 * std::pow(ra, 3) + 5. / 3. * (ra * ra) -
+               5. * ra + 4. - 2. / 3. / ra;
+    return 0.0;
+}
+
+// np.arange(c, lo, -step)[::-1] followed by np.arange(c, hi, step)[1:]
+std::vector<double> centred_axis(double c, double lo, double hi, double step)
+{
+    std::vector<double> a = np_arange(c, lo, -step);
+    std::reverse(a.begin(), a.end());
+    std::vector<double> b = np_arange(c, hi, step);
+    for (size_t i = 1; i < b.size(); ++i) a.push_back(b[i]);
+    return a;
+}
+
+// Basis_wavelet3d.set_basis (basis.py:2684-2843)
+int wav_build(vd_bm_plan* p, const vd_basis_grid* g, BmTables& tb)
+{
+    const vd_wavelet_params& q = p->wprm;
+    const int ny = g->ny, nx = g->nx;
+    const bool geo = g->geographic != 0;
+    const double k2 = geo ? 1.0 / 110 : 1.0;
+    std::vector<double> xc(g->xc_host, g->xc_host + nx), yc(g->yc_host, g->yc_host + ny);
+    for (double v : xc) if (!std::isfinite(v)) return VD_ERR_ARG;
+    for (double v : yc) if (!std::isfinite(v)) return VD_ERR_ARG;
+    if (!(q.npsp > 0) || !(q.facpsp > 0) || !(q.lmin > 0) || !(q.lmax > q.lmin) || !(q.facnst > 0) ||
+        !(q.tmin > 0) || !(q.tmax > q.tmin))
+        return VD_ERR_ARG;
+    const double LON_MIN = *std::min_element(xc.begin(), xc.end());
+    double LON_MAX = *std::max_element(xc.begin(), xc.end());
+    const double LAT_MIN = *std::min_element(yc.begin(), yc.end());
+    const double LAT_MAX = *std::max_element(yc.begin(), yc.end());
+    if (LON_MAX < LON_MIN) LON_MAX += 360.;
+    p->times.assign(g->time_host, g->time_host + g->ntime);
+    const double TIME_MIN = *std::min_element(p->times.begin(), p->times.end());
+    const double TIME_MAX = *std::max_element(p->times.begin(), p->times.end());
+    auto cosd = [&](double lat) { return geo ? std::cos(lat * M_PI / 180.) : 1.0; };
+    std::vector<int8_t> land;
+    bool any_land = false;
+    if (g->land_host) {
+        land.assign(g->land_host, g->land_host + (size_t)ny * nx);
+        for (int8_t v : land) any_land |= (v != 0);
+    }
+    // pseudo-frequencies in space and time, directions (2689-2715)
+    const double lstep = std::log(1 + q.facpsp / q.npsp);
+    auto freqs = [&](double lo, double hi) {
+        std::vector<double> l = np_arange(std::log(1. / lo), std::log(1. / hi) - lstep, -lstep);
+        std::reverse(l.begin(), l.end());
+        std::vector<double> f;
+        for (double v : l) {
+            const double e = std::exp(v);
+            if (1. / e <= hi) f.push_back(e);
+        }
+        return f;
+    };
+    std::vector<double> fs = freqs(q.lmin, q.lmax), ft = freqs(q.tmin, q.tmax);
+    if (fs.size() < 2 || ft.empty()) return VD_ERR_ARG;
+    std::vector<double> th = np_linspace(0, M_PI, (int)(M_PI * fs[0] / (fs[1] - fs[0]) * q.facpsp));
+    if (th.size() < 2) return VD_ERR_ARG;
+    th.pop_back();
+    p->theta = th;
+    p->nth = (int)th.size();
+    p->nf = (int)fs.size();
+    p->fr.resize(fs.size());
+    // time centres of every time frequency, shared by all space frequencies (2773-2796)
+    std::vector<double> enst, tscale, tnorm;
+    for (double f : ft) {
+        const double DXt = 1. / f * q.npsp * 0.5;
+        std::vector<double> e = centred_axis((TIME_MIN + TIME_MAX) / 2, TIME_MIN - DXt, TIME_MAX + DXt, DXt / q.facnst);
+        // norm_fact: running integral of the window on linspace(-DXt, DXt) (50 points), its maximum
+        std::vector<double> tt = np_linspace(-DXt, DXt, 50);
+        double acc = 0, mx = 0;
+        for (size_t i = 0; i + 1 < tt.size(); ++i) {
+            acc = acc + gaspari_cohn(tt[i], DXt) * (tt[i + 1] - tt[i]);
+            mx = std::max(mx, acc);
+        }
+        for (double c : e) {
+            enst.push_back(c);
+            tscale.push_back(DXt);
+            tnorm.push_back(mx);
         }
     }
+    // space lattices (2717-2771)
+    PatState ps;
+    long long boff = 0;
+    int rowoff = 0;
+    for (int iff = 0; iff < p->nf; ++iff) {
+        BmFreq& F = p->fr[iff];
+        F.ff = fs[iff];
+        F.k = 2 * M_PI * fs[iff];
+        F.DX = 1. / fs[iff] * q.npsp * 0.5;
+        F.DXG = F.DX / q.facnst;
+        F.rows_lat = centred_axis((LAT_MIN + LAT_MAX) / 2, LAT_MIN - F.DX * k2, LAT_MAX + F.DX * k2, F.DXG * k2);
+        F.rowoff = rowoff;
+        F.boff = boff;
+        long long cb = 0;
+        std::vector<double> kept_lat;
+        for (double la : F.rows_lat) {
+            const double cl = cosd(la);
+            std::vector<double> lons0 = centred_axis((LON_MIN + LON_MAX) / 2, LON_MIN - F.DX / cl * k2,
+                                                     LON_MAX + F.DX / cl * k2, F.DXG / cl * k2),
+                                lons;
+            for (double lo : lons0) {
+                if (any_land) {
+                    // drop a centre whose box of half-width 0.5/fs holds only masked points (2752-2764)
+                    bool keep = false;
+                    for (int yy = 0; yy < ny && !keep; ++yy) {
+                        if (!(std::fabs((yc[yy] - la) / k2) <= .5 / fs[iff])) continue;
+                        for (int xx = 0; xx < nx; ++xx)
+                            if (std::fabs((xc[xx] - lo) / k2 * cl) <= .5 / fs[iff] && !land[(size_t)yy * nx + xx]) {
+                                keep = true;
+                                break;
+                            }
+                    }
+                    if (!keep) continue;
+                }
+                lons.push_back(lo);
+            }
+            add_row(p, tb, ps, iff, la, cl, lons, xc, k2, cb);
+        }
+        F.NP = cb;
+        F.enst = enst;
+        F.tscale = tscale;
+        F.tnorm = tnorm;
+        F.tdec = tscale.empty() ? 0.0 : tscale[0];
+        F.Q = q.sigma_Q;
+        boff += (long long)enst.size() * 2 * p->nth * F.NP;
+        rowoff += (int)F.rows_lat.size();
+        tb.freq_rowoff.push_back(F.rowoff);
+        tb.freq_boff.push_back(F.boff);
+        tb.freq_np.push_back(F.NP);
+    }
+    p->nbasis = boff;
+    p->R = rowoff;
+    build_xy(p, tb, ps, yc, k2, ny, nx);
+    // time weights (2902-2922): |dt| < DXt, Gaspari-Cohn / norm_fact, kept when non-zero
+    std::vector<std::vector<std::pair<int, double>>> act((size_t)p->ntime * p->nf);
+    for (int kt = 0; kt < p->ntime; ++kt)
+        for (int iff = 0; iff < p->nf; ++iff) {
+            const BmFreq& F = p->fr[iff];
+            auto& lst = act[(size_t)kt * p->nf + iff];
+            for (int it = 0; it < (int)F.enst.size(); ++it) {
+                const double dt = p->times[kt] - F.enst[it];
+                if (std::fabs(dt) < F.tscale[it]) {
+                    const double fact = gaspari_cohn(dt, F.tscale[it]) / F.tnorm[it];
+                    if (fact != 0) lst.push_back({it, fact});
+                }
+            }
+        }
+    pack_time(p, act);
     return VD_OK;
 }
 
@@ -562,9 +750,10 @@ int bm_check(const vd_bm_plan* p, int B, int k, long long ldX, const void* a, co
 
 }  // namespace
 
-extern "C" vd_status vd_bm_plan_create(vd_bm_plan** out, const vd_basis_grid* g, const vd_bm_params* prm)
+static vd_status bm_create(vd_bm_plan** out, const vd_basis_grid* g, const vd_bm_params* prm,
+                           const vd_wavelet_params* wprm)
 {
-    if (!out || !g || !prm) return VD_ERR_ARG;
+    if (!out || !g || (!prm && !wprm)) return VD_ERR_ARG;
     *out = nullptr;
     if (g->ny < 1 || g->nx < 1 || !g->xc_host || !g->yc_host || g->ntime < 1 || !g->time_host) return VD_ERR_ARG;
     if (g->dtype != VD_F32 && g->dtype != VD_F64) return VD_ERR_ARG;
@@ -573,9 +762,14 @@ extern "C" vd_status vd_bm_plan_create(vd_bm_plan** out, const vd_basis_grid* g,
     vd_bm_plan* p = new (std::nothrow) vd_bm_plan();
     if (!p) return VD_ERR_ARG;
     p->ny = g->ny; p->nx = g->nx; p->dtype = g->dtype; p->geographic = g->geographic;
-    p->host_only = g->host_only; p->ntime = g->ntime; p->prm = *prm;
+    p->host_only = g->host_only; p->ntime = g->ntime;
+    if (prm) p->prm = *prm;
+    if (wprm) {
+        p->kind = 1;
+        p->wprm = *wprm;
+    }
     BmTables tb;
-    int st = bm_build(p, g, tb);
+    int st = p->kind == 1 ? wav_build(p, g, tb) : bm_build(p, g, tb);
     if (st == VD_OK && ((long long)p->R * p->nth > 65535 || p->ny > 65535 || p->R > 65535)) st = VD_ERR_UNSUPPORTED;
     if (st == VD_OK && !p->host_only)
         st = p->dtype == VD_F64 ? bm_upload<double>(p, tb, g->land_host) : bm_upload<float>(p, tb, g->land_host);
@@ -586,6 +780,16 @@ extern "C" vd_status vd_bm_plan_create(vd_bm_plan** out, const vd_basis_grid* g,
     }
     *out = p;
     return VD_OK;
+}
+
+extern "C" vd_status vd_bm_plan_create(vd_bm_plan** out, const vd_basis_grid* g, const vd_bm_params* prm)
+{
+    return prm ? bm_create(out, g, prm, nullptr) : VD_ERR_ARG;
+}
+
+extern "C" vd_status vd_wavelet_plan_create(vd_bm_plan** out, const vd_basis_grid* g, const vd_wavelet_params* prm)
+{
+    return prm ? bm_create(out, g, nullptr, prm) : VD_ERR_ARG;
 }
 
 extern "C" vd_status vd_bm_plan_destroy(vd_bm_plan* p)
