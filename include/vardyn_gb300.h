@@ -585,7 +585,8 @@ vd_status vd_qgp_plan_create(vd_qgp_plan** out, const vd_qgp_desc* desc);
 void vd_qgp_plan_destroy(vd_qgp_plan* plan);
 /* op 0 Q (u, v, h -> modes [nl][batch][nx+1][ny+1], walls 0); 1 its
  * transpose (modes -> adu, adv, adh); 2 per-field float64 sums (x, weights
- * [nl][nx+1][ny+1] or NULL, out [nl*batch]); 3 modal solutions, their sums,
+ * [nl][nx+1][ny+1] or NULL, out: nl*batch sums followed by nl*batch*64
+ * partials of scratch); 3 modal solutions, their sums,
  * homsol means [nl] (float64) and homsol -> p_qg [batch][nl][nx+1][ny+1];
  * 4 transpose of the mode -> layer mixing; 5 transpose of the homogeneous
  * correction (sums of homsol * ad, means, ad in place); 6 G (p_qg -> u, v,

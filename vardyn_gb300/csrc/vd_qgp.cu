@@ -88,16 +88,20 @@ __global__ void k_qgp_Q_adj(Tab<T> t, const T* ad, T* adu, T* adv, T* adh)
     }
 }
 
-// per-field sums (optionally weighted by a per-mode field) in float64
+// per-field sums (optionally weighted by a per-mode field) in float64: block
+// partial sums, then a fixed-order sum per field (deterministic)
+constexpr int SUM_BLOCKS = 64;
+
 template <typename T>
-__global__ void k_qgp_sum(Tab<T> t, const T* x, const T* wgt, double* out)
+__global__ void k_qgp_sum_part(Tab<T> t, const T* x, const T* wgt, double* part)
 {
-    const int f = blockIdx.x;   // mode * B + batch
+    const int f = blockIdx.y;   // mode * B + batch
     const int m = f / t.B;
     const T* X = x + (long long)f * t.sw;
     const T* W = wgt ? wgt + (long long)m * t.sw : nullptr;
     double a = 0;
-    for (long long k = threadIdx.x; k < t.sw; k += blockDim.x) a += W ? (double)W[k] * (double)X[k] : (double)X[k];
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < t.sw; k += (long long)gridDim.x * blockDim.x)
+        a += W ? (double)W[k] * (double)X[k] : (double)X[k];
     __shared__ double red[256];
     red[threadIdx.x] = a;
     __syncthreads();
@@ -105,7 +109,16 @@ __global__ void k_qgp_sum(Tab<T> t, const T* x, const T* wgt, double* out)
         if ((int)threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
         __syncthreads();
     }
-    if (threadIdx.x == 0) out[f] = red[0];
+    if (threadIdx.x == 0) part[(long long)f * gridDim.x + blockIdx.x] = red[0];
+}
+
+__global__ void k_qgp_sum_final(int nf, int nb, const double* part, double* out)
+{
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nf) return;
+    double s = 0;
+    for (int k = 0; k < nb; ++k) s += part[(long long)f * nb + k];
+    out[f] = s;
 }
 
 // p_qg[b][l] = sum_m Cm2l[l][m] (p_m + alpha_m homsol_m), alpha = -mean(p_m)/hmean_m
@@ -345,9 +358,14 @@ static int op_t(const vd_qgp_plan* p, int op, int B, const void* const* a, cudaS
     case 1:   // Q^T: modes -> adu, adv, adh
         k_qgp_Q_adj<T><<<wgrid(p, B), blk, 0, st>>>(t, (const T*)a[0], (T*)a[1], (T*)a[2], (T*)a[3]);
         break;
-    case 2:   // sums: x, weight (nullable) -> double[nl*B]
-        k_qgp_sum<T><<<(unsigned)(p->nl * B), 256, 0, st>>>(t, (const T*)a[0], (const T*)a[1], (double*)a[2]);
+    case 2: {   // sums: x, weight (nullable) -> double[nl*B]; partials in out[nl*B ..]
+        const int nf = p->nl * B;
+        double* part = (double*)a[2] + nf;
+        k_qgp_sum_part<T><<<dim3(SUM_BLOCKS, (unsigned)nf), 256, 0, st>>>(t, (const T*)a[0], (const T*)a[1], part);
+        VD_LAUNCH_CHECK();
+        k_qgp_sum_final<<<(unsigned)((nf + 127) / 128), 128, 0, st>>>(nf, SUM_BLOCKS, part, (double*)a[2]);
         break;
+    }
     case 3:   // P: pm, sums, hmean, homsol -> pqg
         k_qgp_P<T><<<dim3(nb, (unsigned)B), 256, 0, st>>>(t, (const T*)a[0], (const double*)a[1],
                                                           (const double*)a[2], (const T*)a[3], (T*)a[4]);

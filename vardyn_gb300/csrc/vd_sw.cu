@@ -232,12 +232,25 @@ __device__ __forceinline__ S recon(const S* q, int bits, bool ok4, bool ok6, boo
 }
 
 // flux.py:39-90 at one face: q[0..5] = cells k-2..k+3 around face k.
+// The velocity's sign selects the upwind stencil: the 6 values are reversed
+// lane by lane (selects, no divergent branch) and one reconstruction is
+// formed, F = vel * R, which equals up * P + un * N (the other product is an
+// exact zero). At vel = 0 the tangent takes both reconstructions with weight
+// 1/2 (jax's tie rule for max), a rare branch.
 template <typename T, typename S>
 __device__ __forceinline__ S weno_flux(const S* q, const S& vel, int bits, bool ok4, bool ok6)
 {
-    const S up = relu(vel);
-    const S un = vel - up;
-    return up * recon<T>(q, bits, ok4, ok6, false) + un * recon<T>(q, bits, ok4, ok6, true);
+    const bool rev = val(vel) < T(0);
+    S qq[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) qq[k] = rev ? q[5 - k] : q[k];
+    S F = vel * recon<T>(qq, bits, ok4, ok6, false);
+    if (val(vel) == T(0)) {
+        const S up = relu(vel);
+        const S un = vel - up;
+        F = up * recon<T>(q, bits, ok4, ok6, false) + un * recon<T>(q, bits, ok4, ok6, true);
+    }
+    return F;
 }
 
 // Local gradient of the face flux: F and dF/dq[0..5], dF/dvel.
@@ -251,16 +264,17 @@ __device__ __forceinline__ void weno_flux_grad(const T* q, T vel, int bits, bool
         gv = T(0.5) * (P + M);
         return;
     }
+    const bool rev = vel < T(0);
     DN<T, 6> qd[6];
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
-        qd[k].v = q[k];
+        qd[k].v = rev ? q[5 - k] : q[k];
 #pragma unroll
         for (int m = 0; m < 6; ++m) qd[k].d[m] = (k == m) ? T(1) : T(0);
     }
-    const DN<T, 6> R = recon<T>(qd, bits, ok4, ok6, vel < T(0));
+    const DN<T, 6> R = recon<T>(qd, bits, ok4, ok6, false);
 #pragma unroll
-    for (int k = 0; k < 6; ++k) g[k] = vel * R.d[k];
+    for (int k = 0; k < 6; ++k) g[k] = vel * (rev ? R.d[5 - k] : R.d[k]);
     gv = R.v;
 }
 

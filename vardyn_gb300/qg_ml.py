@@ -181,7 +181,7 @@ class QGPlan:
         modes = torch.empty((nl, B, X, Y), dtype=self.dtype, device=self.device)
         self._op(0, B, u, v, h, modes)
         pm = self._solve(modes)
-        sums = torch.empty(nl * B, dtype=torch.float64, device=self.device)
+        sums = torch.empty(nl * B * 65, dtype=torch.float64, device=self.device)
         self._op(2, B, pm, None, sums)
         pqg = torch.empty((B, nl, X, Y), dtype=self.dtype, device=self.device)
         self._op(3, B, pm, sums, self.hmean, self.homsol, pqg)
@@ -196,7 +196,7 @@ class QGPlan:
         self._op(7, B, au.contiguous(), av.contiguous(), ah.contiguous(), apqg)
         apm = torch.empty((nl, B, X, Y), dtype=self.dtype, device=self.device)
         self._op(4, B, apqg, apm)
-        sums = torch.empty(nl * B, dtype=torch.float64, device=self.device)
+        sums = torch.empty(nl * B * 65, dtype=torch.float64, device=self.device)
         self._op(2, B, apm, self.homsol, sums)
         self._op(5, B, sums, self.hmean, apm)
         aq = self._solve_adj(apm)
