@@ -291,6 +291,9 @@ struct Tab {
     const T *dxp, *dyp;           // [nl][nx-1][ny], [nl][nx][ny-1] or null
     const T *taux, *tauy;         // default wind stress [nx-1][ny], [nx][ny-1]
     const T *gu, *gv, *gh;        // sponge rates (sponge_coef/dt) * sponge
+    const T *idxu2, *idxu, *idyu2;   // reciprocals on the u grid: 1/dx^2, 1/dx, 1/dy^2
+    const T *idyv2, *idyv, *idxv2;   // on the v grid: 1/dy^2, 1/dy, 1/dx^2
+    const T *iarea, *idx2h, *idy2h;  // on the h grid: 1/area, 1/dx^2, 1/dy^2
     const uint8_t *fh, *fu, *fv;  // flag bytes
     T G[MAXL];                    // G[l] = sum_{k<=l} g'_k
     T gp[MAXL];
@@ -370,14 +373,14 @@ __global__ void k_sw_diag(Tab<T> t, Tri<R> x, W om, W kp, W ht)
     }
     if (!hp) return;
     const T mh = (t.fh[hi] & 1) ? T(1) : T(0);
-    const T ar = t.area[hi];
+    const T ar = t.area[hi], iar = t.iarea[hi];
     // eta_l = sum_{m>=l} h_m / area; p_l = sum_{k<=l} g'_k eta_k (sw.py:705-706)
     S eta[MAXL];
     {
-        S acc = hl[nl - 1] / ar;
+        S acc = hl[nl - 1] * iar;
         eta[nl - 1] = acc;
         for (int l = nl - 2; l >= 0; --l) {
-            acc = hl[l] / ar + acc;
+            acc = hl[l] * iar + acc;
             eta[l] = acc;
         }
     }
@@ -388,10 +391,9 @@ __global__ void k_sw_diag(Tab<T> t, Tri<R> x, W om, W kp, W ht)
         const long long u0 = ob * t.su + (long long)i * ny + j, u1 = u0 + ny;
         const long long v0 = ob * t.sv + (long long)i * (ny + 1) + j, v1 = v0 + 1;
         const S a = x.u(u1), c = x.u(u0), d = x.v(v1), e = x.v(v0);
-        const T dxu1 = t.dxu[(long long)(i + 1) * ny + j], dxu0 = t.dxu[(long long)i * ny + j];
-        const T dyv1 = t.dyv[(long long)i * (ny + 1) + j + 1], dyv0 = t.dyv[(long long)i * (ny + 1) + j];
-        const S ke = T(0.25) * (a * (a / (dxu1 * dxu1)) + c * (c / (dxu0 * dxu0)) + d * (d / (dyv1 * dyv1)) +
-                                e * (e / (dyv0 * dyv0))) * mh;
+        const T iu1 = t.idxu2[(long long)(i + 1) * ny + j], iu0 = t.idxu2[(long long)i * ny + j];
+        const T iv1 = t.idyv2[(long long)i * (ny + 1) + j + 1], iv0 = t.idyv2[(long long)i * (ny + 1) + j];
+        const S ke = T(0.25) * (a * (a * iu1) + c * (c * iu0) + d * (d * iv1) + e * (e * iv0)) * mh;
         kp(ob * t.sh + hi, ke + pacc);
         const T hr = t.href[(long long)l * t.sh + hi];
         if (t.linear) ht(ob * t.sh + hi, hr + T(0) * hl[l]);
@@ -422,8 +424,7 @@ __global__ void k_sw_tend(Tab<T> t, Tri<R> x, R om, R kp, R ht, const T* taux, c
             const long long vb = ob * t.sv;
             auto Vv = [&](int a, int c) {
                 const long long k = (long long)a * (ny + 1) + c;
-                const T m = t.dyv[k];
-                return x.v(vb + k) / (m * m);
+                return x.v(vb + k) * t.idyv2[k];
             };
             const S Vm = T(0.25) * (Vv(i, j + 1) + Vv(i, j) + Vv(i - 1, j + 1) + Vv(i - 1, j));
             // vortex force: WENO flux of omega[i][.] along y through face j
@@ -446,18 +447,16 @@ __global__ void k_sw_tend(Tab<T> t, Tri<R> x, R om, R kp, R ht, const T* taux, c
                 auto up = [&](int a, int c) {
                     c = c < 0 ? 0 : (c > ny - 1 ? ny - 1 : c);
                     const long long k = (long long)a * ny + c;
-                    return x.u(ub + k) / t.dxu[k];
+                    return x.u(ub + k) * t.idxu[k];
                 };
-                const T dx = t.dxu[ui], dy = t.dyu[ui];
                 const S c0 = up(i, j);
-                const S lap = (up(i + 1, j) - T(2) * c0 + up(i - 1, j)) / (dx * dx) +
-                              (up(i, j + 1) - T(2) * c0 + up(i, j - 1)) / (dy * dy);
-                du = du + t.visc * lap * dx;
+                const S lap = (up(i + 1, j) - T(2) * c0 + up(i - 1, j)) * t.idxu2[ui] +
+                              (up(i, j + 1) - T(2) * c0 + up(i, j - 1)) * t.idyu2[ui];
+                du = du + t.visc * lap * t.dxu[ui];
             }
             du = du * ((fl & 1) ? T(1) : T(0));
             // thickness flux along x through u face i
-            const T dxu = t.dxu[ui];
-            const S Uf = x.u(ob * t.su + ui) / (dxu * dxu);
+            const S Uf = x.u(ob * t.su + ui) * t.idxu2[ui];
             S hq[6];
 #pragma unroll
             for (int k = 0; k < 6; ++k) {
@@ -478,8 +477,7 @@ __global__ void k_sw_tend(Tab<T> t, Tri<R> x, R om, R kp, R ht, const T* taux, c
             const long long ub = ob * t.su;
             auto Uu = [&](int a, int c) {
                 const long long k = (long long)a * ny + c;
-                const T m = t.dxu[k];
-                return x.u(ub + k) / (m * m);
+                return x.u(ub + k) * t.idxu2[k];
             };
             const S Um = T(0.25) * (Uu(i + 1, j) + Uu(i + 1, j - 1) + Uu(i, j) + Uu(i, j - 1));
             S q[6];
@@ -501,17 +499,15 @@ __global__ void k_sw_tend(Tab<T> t, Tri<R> x, R om, R kp, R ht, const T* taux, c
                 auto vp = [&](int a, int c) {
                     a = a < 0 ? 0 : (a > nx - 1 ? nx - 1 : a);
                     const long long k = (long long)a * (ny + 1) + c;
-                    return x.v(vb + k) / t.dyv[k];
+                    return x.v(vb + k) * t.idyv[k];
                 };
-                const T dx = t.dxv[vi], dy = t.dyv[vi];
                 const S c0 = vp(i, j);
-                const S lap = (vp(i + 1, j) - T(2) * c0 + vp(i - 1, j)) / (dx * dx) +
-                              (vp(i, j + 1) - T(2) * c0 + vp(i, j - 1)) / (dy * dy);
-                dv = dv + t.visc * lap * dy;
+                const S lap = (vp(i + 1, j) - T(2) * c0 + vp(i - 1, j)) * t.idxv2[vi] +
+                              (vp(i, j + 1) - T(2) * c0 + vp(i, j - 1)) * t.idyv2[vi];
+                dv = dv + t.visc * lap * t.dyv[vi];
             }
             dv = dv * ((fl & 1) ? T(1) : T(0));
-            const T dyv = t.dyv[vi];
-            const S Vf = x.v(ob * t.sv + vi) / (dyv * dyv);
+            const S Vf = x.v(ob * t.sv + vi) * t.idyv2[vi];
             S hq[6];
 #pragma unroll
             for (int k = 0; k < 6; ++k) {
@@ -589,12 +585,11 @@ __global__ void k_sw_update(Tab<T> t, StageArgs sa, Tri<R> x, R tu, R tv, R fx, 
                 a = a < 0 ? 0 : (a > nx - 1 ? nx - 1 : a);
                 c = c < 0 ? 0 : (c > ny - 1 ? ny - 1 : c);
                 const long long q = (long long)a * ny + c;
-                return x.h(ob * t.sh + q) / t.area[q];
+                return x.h(ob * t.sh + q) * t.iarea[q];
             };
-            const T dx = t.dxh[hi], dy = t.dyh[hi];
             const S c0 = hp(i, j);
-            const S lap = (hp(i + 1, j) - T(2) * c0 + hp(i - 1, j)) / (dx * dx) +
-                          (hp(i, j + 1) - T(2) * c0 + hp(i, j - 1)) / (dy * dy);
+            const S lap = (hp(i + 1, j) - T(2) * c0 + hp(i - 1, j)) * t.idx2h[hi] +
+                          (hp(i, j + 1) - T(2) * c0 + hp(i, j - 1)) * t.idy2h[hi];
             k = k + t.diff * lap * t.area[hi] * mh;
         }
         if (t.has_sponge) k = k + t.gh[hi] * (xb.h(idx) - xv);
@@ -759,8 +754,7 @@ __global__ void k_sw_tend_adj(Tab<T> t, const T* u, const T* v, const T* h, cons
             const long long vb = ob * t.sv;
             auto Vv = [&](int p, int c) {
                 const long long k = (long long)p * (ny + 1) + c;
-                const T m = t.dyv[k];
-                return v[vb + k] / (m * m);
+                return v[vb + k] * t.idyv2[k];
             };
             const T Vm = T(0.25) * (Vv(i, j + 1) + Vv(i, j) + Vv(i - 1, j + 1) + Vv(i - 1, j));
             T q[6];
@@ -780,8 +774,7 @@ __global__ void k_sw_tend_adj(Tab<T> t, const T* u, const T* v, const T* h, cons
             const T aVm = T(0.25) * a * (gv + t.fsu[ui]);
             auto addV = [&](int p, int c) {
                 const long long k = (long long)p * (ny + 1) + c;
-                const T m = t.dyv[k];
-                aadd(&adv[vb + k], aVm / (m * m));
+                aadd(&adv[vb + k], aVm * t.idyv2[k]);
             };
             addV(i, j + 1);
             addV(i, j);
@@ -792,18 +785,18 @@ __global__ void k_sw_tend_adj(Tab<T> t, const T* u, const T* v, const T* h, cons
             const long long ub = ob * t.su;
             if (l == nl - 1) aadd(&adu[ub + ui], -t.drag * a);
             if (t.visc > T(0)) {
-                const T dx = t.dxu[ui], dy = t.dyu[ui];
-                const T c = t.visc * dx * a;
+                const T ix2 = t.idxu2[ui], iy2 = t.idyu2[ui];
+                const T c = t.visc * t.dxu[ui] * a;
                 auto addu = [&](int p, int cc, T w) {
                     cc = cc < 0 ? 0 : (cc > ny - 1 ? ny - 1 : cc);
                     const long long k = (long long)p * ny + cc;
-                    aadd(&adu[ub + k], c * w / t.dxu[k]);
+                    aadd(&adu[ub + k], c * w * t.idxu[k]);
                 };
-                addu(i + 1, j, T(1) / (dx * dx));
-                addu(i - 1, j, T(1) / (dx * dx));
-                addu(i, j + 1, T(1) / (dy * dy));
-                addu(i, j - 1, T(1) / (dy * dy));
-                addu(i, j, -T(2) / (dx * dx) - T(2) / (dy * dy));
+                addu(i + 1, j, ix2);
+                addu(i - 1, j, ix2);
+                addu(i, j + 1, iy2);
+                addu(i, j - 1, iy2);
+                addu(i, j, -T(2) * ix2 - T(2) * iy2);
             }
         }
         // thickness flux through u face i: dt_h[c] = -div_x[c] * mask_h[c]
@@ -811,8 +804,8 @@ __global__ void k_sw_tend_adj(Tab<T> t, const T* u, const T* v, const T* h, cons
         if (i - 1 >= 1 && i - 1 <= nx - 2) aF -= mh((long long)(i - 1) * ny + j) * hb[(long long)(i - 1) * ny + j];
         if (i >= 1 && i <= nx - 2) aF += mh(ui) * hb[ui];
         if (aF != T(0)) {
-            const T dxu = t.dxu[ui];
-            const T Uf = u[ob * t.su + ui] / (dxu * dxu);
+            const T iu2 = t.idxu2[ui];
+            const T Uf = u[ob * t.su + ui] * iu2;
             T q[6];
 #pragma unroll
             for (int k = 0; k < 6; ++k) {
@@ -826,7 +819,7 @@ __global__ void k_sw_tend_adj(Tab<T> t, const T* u, const T* v, const T* h, cons
                 const int ii = i - 3 + k;
                 if (ii >= 0 && ii < nx && g[k] != T(0)) aadd(&adht[ob * t.sh + (long long)ii * ny + j], aF * g[k]);
             }
-            aadd(&adu[ob * t.su + ui], aF * gv / (dxu * dxu));
+            aadd(&adu[ob * t.su + ui], aF * gv * iu2);
         }
     }
     // ---------------- v point
@@ -838,8 +831,7 @@ __global__ void k_sw_tend_adj(Tab<T> t, const T* u, const T* v, const T* h, cons
             const long long ub = ob * t.su;
             auto Uu = [&](int p, int c) {
                 const long long k = (long long)p * ny + c;
-                const T m = t.dxu[k];
-                return u[ub + k] / (m * m);
+                return u[ub + k] * t.idxu2[k];
             };
             const T Um = T(0.25) * (Uu(i + 1, j) + Uu(i + 1, j - 1) + Uu(i, j) + Uu(i, j - 1));
             T q[6];
@@ -858,8 +850,7 @@ __global__ void k_sw_tend_adj(Tab<T> t, const T* u, const T* v, const T* h, cons
             const T aUm = -T(0.25) * a * (gv + t.fsv[vi]);
             auto addU = [&](int p, int c) {
                 const long long k = (long long)p * ny + c;
-                const T m = t.dxu[k];
-                aadd(&adu[ub + k], aUm / (m * m));
+                aadd(&adu[ub + k], aUm * t.idxu2[k]);
             };
             addU(i + 1, j);
             addU(i + 1, j - 1);
@@ -871,18 +862,18 @@ __global__ void k_sw_tend_adj(Tab<T> t, const T* u, const T* v, const T* h, cons
             const long long vb = ob * t.sv;
             if (l == nl - 1) aadd(&adv[vb + vi], -t.drag * a);
             if (t.visc > T(0)) {
-                const T dx = t.dxv[vi], dy = t.dyv[vi];
-                const T c = t.visc * dy * a;
+                const T ix2 = t.idxv2[vi], iy2 = t.idyv2[vi];
+                const T c = t.visc * t.dyv[vi] * a;
                 auto addv = [&](int p, int cc, T w) {
                     p = p < 0 ? 0 : (p > nx - 1 ? nx - 1 : p);
                     const long long k = (long long)p * (ny + 1) + cc;
-                    aadd(&adv[vb + k], c * w / t.dyv[k]);
+                    aadd(&adv[vb + k], c * w * t.idyv[k]);
                 };
-                addv(i + 1, j, T(1) / (dx * dx));
-                addv(i - 1, j, T(1) / (dx * dx));
-                addv(i, j + 1, T(1) / (dy * dy));
-                addv(i, j - 1, T(1) / (dy * dy));
-                addv(i, j, -T(2) / (dx * dx) - T(2) / (dy * dy));
+                addv(i + 1, j, ix2);
+                addv(i - 1, j, ix2);
+                addv(i, j + 1, iy2);
+                addv(i, j - 1, iy2);
+                addv(i, j, -T(2) * ix2 - T(2) * iy2);
             }
         }
         T aF = T(0);
@@ -890,8 +881,8 @@ __global__ void k_sw_tend_adj(Tab<T> t, const T* u, const T* v, const T* h, cons
         if (j - 1 >= 1 && j - 1 <= ny - 2) aF -= mh(hj0) * hb[hj0];
         if (j >= 1 && j <= ny - 2) aF += mh(hj1) * hb[hj1];
         if (aF != T(0)) {
-            const T dyv = t.dyv[vi];
-            const T Vf = v[ob * t.sv + vi] / (dyv * dyv);
+            const T iv2 = t.idyv2[vi];
+            const T Vf = v[ob * t.sv + vi] * iv2;
             T q[6];
 #pragma unroll
             for (int k = 0; k < 6; ++k) {
@@ -905,7 +896,7 @@ __global__ void k_sw_tend_adj(Tab<T> t, const T* u, const T* v, const T* h, cons
                 const int jj = j - 3 + k;
                 if (jj >= 0 && jj < ny && g[k] != T(0)) aadd(&adht[ob * t.sh + (long long)i * ny + jj], aF * g[k]);
             }
-            aadd(&adv[ob * t.sv + vi], aF * gv / (dyv * dyv));
+            aadd(&adv[ob * t.sv + vi], aF * gv * iv2);
         }
     }
     // ---------------- thickness diffusion
@@ -913,18 +904,18 @@ __global__ void k_sw_tend_adj(Tab<T> t, const T* u, const T* v, const T* h, cons
         const long long hi = (long long)i * ny + j;
         const T a = hb[hi] * mh(hi) * t.diff * t.area[hi];
         if (a != T(0)) {
-            const T dx = t.dxh[hi], dy = t.dyh[hi];
+            const T ix2 = t.idx2h[hi], iy2 = t.idy2h[hi];
             auto addh = [&](int p, int c, T w) {
                 p = p < 0 ? 0 : (p > nx - 1 ? nx - 1 : p);
                 c = c < 0 ? 0 : (c > ny - 1 ? ny - 1 : c);
                 const long long k = (long long)p * ny + c;
-                aadd(&adh[ob * t.sh + k], a * w / t.area[k]);
+                aadd(&adh[ob * t.sh + k], a * w * t.iarea[k]);
             };
-            addh(i + 1, j, T(1) / (dx * dx));
-            addh(i - 1, j, T(1) / (dx * dx));
-            addh(i, j + 1, T(1) / (dy * dy));
-            addh(i, j - 1, T(1) / (dy * dy));
-            addh(i, j, -T(2) / (dx * dx) - T(2) / (dy * dy));
+            addh(i + 1, j, ix2);
+            addh(i - 1, j, ix2);
+            addh(i, j + 1, iy2);
+            addh(i, j - 1, iy2);
+            addh(i, j, -T(2) * ix2 - T(2) * iy2);
         }
     }
 }
@@ -948,22 +939,20 @@ __global__ void k_sw_diag_adj(Tab<T> t, const T* u, const T* v, const T* h, cons
             const long long ui = (long long)i * ny + j, o = ob * t.su + ui;
             T a = -t.wb[(long long)i * (ny + 1) + j] * AO[(long long)i * (ny + 1) + j] +
                   t.wb[(long long)i * (ny + 1) + j + 1] * AO[(long long)i * (ny + 1) + j + 1];
-            const T dx = t.dxu[ui];
             T kk = T(0);
             if (i >= 1) kk += mh(i - 1, j) * AK[(long long)(i - 1) * ny + j];
             if (i < nx) kk += mh(i, j) * AK[(long long)i * ny + j];
-            a += T(0.5) * kk * u[o] / (dx * dx);
+            a += T(0.5) * kk * u[o] * t.idxu2[ui];
             adu[o] += a;
         }
         if (i < nx) {   // v point: dx(v) at w (i, j) (+) and (i+1, j) (-); KE of cells j-1, j
             const long long vi = (long long)i * (ny + 1) + j, o = ob * t.sv + vi;
             T a = t.wa[(long long)i * (ny + 1) + j] * AO[(long long)i * (ny + 1) + j] -
                   t.wa[(long long)(i + 1) * (ny + 1) + j] * AO[(long long)(i + 1) * (ny + 1) + j];
-            const T dy = t.dyv[vi];
             T kk = T(0);
             if (j >= 1) kk += mh(i, j - 1) * AK[(long long)i * ny + j - 1];
             if (j < ny) kk += mh(i, j) * AK[(long long)i * ny + j];
-            a += T(0.5) * kk * v[o] / (dy * dy);
+            a += T(0.5) * kk * v[o] * t.idyv2[vi];
             adv[o] += a;
         }
     }
@@ -977,7 +966,7 @@ __global__ void k_sw_diag_adj(Tab<T> t, const T* u, const T* v, const T* h, cons
             const long long o = (long long)(b * nl + m) * t.sh + hi;
             T a = T(0);
             for (int l = 0; l < nl; ++l) a += ap[l] * t.G[l < m ? l : m];
-            a = a / ar;
+            a = a * t.iarea[hi];
             if (!t.linear) {
                 const T z = (t.href[(long long)m * t.sh + hi] + h[o] - t.hmin * ar) * t.sharp;
                 a += adht[o] * sigmoid_v(z);
@@ -1216,6 +1205,8 @@ static void fill_tab(Tab<T>& t, vd_sw_plan* p, const std::vector<size_t>& off)
     t.areau = P(); t.areav = P(); t.fsu = P(); t.fsv = P(); t.wa = P(); t.wb = P(); t.wfu = P(); t.wfv = P();
     t.href = P(); t.hrefu = P(); t.hrefv = P(); t.dxp = P(); t.dyp = P(); t.taux = P(); t.tauy = P();
     t.gu = P(); t.gv = P(); t.gh = P();
+    t.idxu2 = P(); t.idxu = P(); t.idyu2 = P(); t.idyv2 = P(); t.idyv = P(); t.idxv2 = P();
+    t.iarea = P(); t.idx2h = P(); t.idy2h = P();
     t.fh = (const uint8_t*)(base + off[k++]);
     t.fu = (const uint8_t*)(base + off[k++]);
     t.fv = (const uint8_t*)(base + off[k++]);
@@ -1364,11 +1355,23 @@ extern "C" vd_status vd_sw_plan_create(vd_sw_plan** out, const vd_sw_desc* d)
     if (d->sponge_v_host) for (size_t k = 0; k < sv; ++k) { gv[k] = gs * d->sponge_v_host[k]; has_sponge |= gv[k] != 0; }
     if (d->sponge_h_host) for (size_t k = 0; k < sh; ++k) { gh[k] = gs * d->sponge_h_host[k]; has_sponge |= gh[k] != 0; }
 
+    // reciprocal metric tables (products instead of divisions in the kernels)
+    auto recip = [](const std::vector<double>& a, int pw) {
+        std::vector<double> r(a.size());
+        for (size_t k = 0; k < a.size(); ++k) r[k] = pw == 2 ? 1.0 / (a[k] * a[k]) : 1.0 / a[k];
+        return r;
+    };
+    std::vector<double> idxu2 = recip(dxu, 2), idxu = recip(dxu, 1), idyu2 = recip(dyu, 2);
+    std::vector<double> idyv2 = recip(dyv, 2), idyv = recip(dyv, 1), idxv2 = recip(dxv, 2);
+    std::vector<double> iarea = recip(area, 1), idx2h = recip(dx, 2), idy2h = recip(dy, 2);
+
     // ---------------- upload: one allocation
     const size_t esz = d->dtype == VD_F64 ? 8 : 4;
     std::vector<const std::vector<double>*> arrs = {&dxu, &dyu, &dxv, &dyv, &dx, &dy, &area, &areau, &areav,
                                                    &fsu, &fsv, &wa, &wb, &wfu, &wfv, &href, &hrefu, &hrefv,
-                                                   &dxp, &dyp, &taux, &tauy, &gu, &gv, &gh};
+                                                   &dxp, &dyp, &taux, &tauy, &gu, &gv, &gh,
+                                                   &idxu2, &idxu, &idyu2, &idyv2, &idyv, &idxv2,
+                                                   &iarea, &idx2h, &idy2h};
     std::vector<size_t> off;
     size_t tot = 0;
     for (auto* a : arrs) {
