@@ -183,6 +183,22 @@ __device__ __forceinline__ DN<T, N> sclamp(const DN<T, N>& x, T xmin, T s)
 
 template <typename S> __device__ __forceinline__ S sq(const S& x) { return x * x; }
 
+// Division of the WENO-Z weights: IEEE in float64; the fast intrinsic (at
+// most 2 ulp) in float32, whose results are compared within float32
+// tolerances. The tangent and the local gradient use the same quotient.
+__device__ __forceinline__ float qdiv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double qdiv(double a, double b) { return a / b; }
+template <typename T, int N>
+__device__ __forceinline__ DN<T, N> qdiv(const DN<T, N>& a, const DN<T, N>& b)
+{
+    DN<T, N> r;
+    r.v = qdiv(a.v, b.v);
+    const T ib = qdiv(T(1), b.v);
+#pragma unroll
+    for (int k = 0; k < N; ++k) r.d[k] = (a.d[k] - r.v * b.d[k]) * ib;
+    return r;
+}
+
 // ------------------------------------------------------------------ reconstructions
 // wenoz4_left / wenoz6_left (reconstruction.py:98-169)
 template <typename T, typename S>
@@ -193,9 +209,9 @@ __device__ __forceinline__ S wenoz4(const S& qmm, const S& qm, const S& qp, cons
     const S q2 = T(0.5) * (qm + qp);
     const S b1 = sq(qm - qmm), b2 = sq(qp - qm);
     const S tau = dsqrt(sq(b2 - b1) + T(WENO_EPS * WENO_EPS));
-    const S w1 = T(1.0 / 3.0) * (T(1) + tau / (b1 + T(WENO_EPS)));
-    const S w2 = T(2.0 / 3.0) * (T(1) + tau / (b2 + T(WENO_EPS)));
-    return (w1 * q1 + w2 * q2) / (w1 + w2);
+    const S w1 = T(1.0 / 3.0) * (T(1) + qdiv(tau, b1 + T(WENO_EPS)));
+    const S w2 = T(2.0 / 3.0) * (T(1) + qdiv(tau, b2 + T(WENO_EPS)));
+    return qdiv(w1 * q1 + w2 * q2, w1 + w2);
 }
 
 template <typename T, typename S>
@@ -210,10 +226,10 @@ __device__ __forceinline__ S wenoz6(const S& q0, const S& q1, const S& q2, const
     const S b2 = k1 * sq(q1 - T(2) * q2 + q3) + k2 * sq(q1 - q3);
     const S b3 = k1 * sq(q2 - T(2) * q3 + q4) + k2 * sq(T(3) * q2 - T(4) * q3 + q4);
     const S tau = dsqrt(sq(b1 - b3) + T(WENO_EPS * WENO_EPS));
-    const S w1 = T(0.1) * (T(1) + tau / (b1 + T(WENO_EPS)));
-    const S w2 = T(0.6) * (T(1) + tau / (b2 + T(WENO_EPS)));
-    const S w3 = T(0.3) * (T(1) + tau / (b3 + T(WENO_EPS)));
-    return (w1 * r1 + w2 * r2 + w3 * r3) / (w1 + w2 + w3);
+    const S w1 = T(0.1) * (T(1) + qdiv(tau, b1 + T(WENO_EPS)));
+    const S w2 = T(0.6) * (T(1) + qdiv(tau, b2 + T(WENO_EPS)));
+    const S w3 = T(0.3) * (T(1) + qdiv(tau, b3 + T(WENO_EPS)));
+    return qdiv(w1 * r1 + w2 * r2 + w3 * r3, w1 + w2 + w3);
 }
 
 // Mask bits of one face: 1 = 2-point, 2 = 4-point, 4 = 6-point term.
