@@ -269,29 +269,108 @@ __device__ __forceinline__ S weno_flux(const S* q, const S& vel, int bits, bool 
     return F;
 }
 
-// Local gradient of the face flux: F and dF/dq[0..5], dF/dvel.
+// Reverse-mode gradients of the reconstructions (the same quotients as the
+// forward): wenoz4 of (q[1..4]) and wenoz6 of (q[0..5]) accumulate dR/dq
+// into g and return R.
+template <typename T>
+__device__ __forceinline__ T wenoz4_grad(const T* q, T* g)
+{
+    const T qmm = q[1], qm = q[2], qp = q[3];
+    const T q1 = T(-0.5) * qmm + T(1.5) * qm;
+    const T q2 = T(0.5) * (qm + qp);
+    const T e1 = qm - qmm, e2 = qp - qm;
+    const T b1 = e1 * e1, b2 = e2 * e2;
+    const T dd = b2 - b1;
+    const T tau = sqrt(dd * dd + T(WENO_EPS * WENO_EPS));
+    const T s1 = qdiv(T(1), b1 + T(WENO_EPS)), s2 = qdiv(T(1), b2 + T(WENO_EPS));
+    const T w1 = T(1.0 / 3.0) * (T(1) + qdiv(tau, b1 + T(WENO_EPS)));
+    const T w2 = T(2.0 / 3.0) * (T(1) + qdiv(tau, b2 + T(WENO_EPS)));
+    const T W = w1 + w2;
+    const T R = qdiv(w1 * q1 + w2 * q2, W);
+    const T iW = qdiv(T(1), W);
+    const T aw1 = (q1 - R) * iW, aw2 = (q2 - R) * iW;       // dR/dw
+    const T ar1 = w1 * iW, ar2 = w2 * iW;                    // dR/dq1, dR/dq2
+    const T atau = aw1 * T(1.0 / 3.0) * s1 + aw2 * T(2.0 / 3.0) * s2;
+    const T dtau = qdiv(dd, tau);
+    const T ab1 = -aw1 * T(1.0 / 3.0) * tau * s1 * s1 - atau * dtau;
+    const T ab2 = -aw2 * T(2.0 / 3.0) * tau * s2 * s2 + atau * dtau;
+    // b1 = (qm - qmm)^2, b2 = (qp - qm)^2
+    g[1] += ar1 * T(-0.5) - ab1 * T(2) * e1;
+    g[2] += ar1 * T(1.5) + ar2 * T(0.5) + ab1 * T(2) * e1 - ab2 * T(2) * e2;
+    g[3] += ar2 * T(0.5) + ab2 * T(2) * e2;
+    return R;
+}
+
+template <typename T>
+__device__ __forceinline__ T wenoz6_grad(const T* q, T* g)
+{
+    const T k1 = T(13.0 / 12.0), k2 = T(0.25);
+    const T r1 = T(1.0 / 3.0) * q[0] - T(7.0 / 6.0) * q[1] + T(11.0 / 6.0) * q[2];
+    const T r2 = T(-1.0 / 6.0) * q[1] + T(5.0 / 6.0) * q[2] + T(1.0 / 3.0) * q[3];
+    const T r3 = T(1.0 / 3.0) * q[2] + T(5.0 / 6.0) * q[3] - T(1.0 / 6.0) * q[4];
+    const T d1 = q[0] - T(2) * q[1] + q[2], f1 = q[0] - T(4) * q[1] + T(3) * q[2];
+    const T d2 = q[1] - T(2) * q[2] + q[3], f2 = q[1] - q[3];
+    const T d3 = q[2] - T(2) * q[3] + q[4], f3 = T(3) * q[2] - T(4) * q[3] + q[4];
+    const T b1 = k1 * (d1 * d1) + k2 * (f1 * f1);
+    const T b2 = k1 * (d2 * d2) + k2 * (f2 * f2);
+    const T b3 = k1 * (d3 * d3) + k2 * (f3 * f3);
+    const T dd = b1 - b3;
+    const T tau = sqrt(dd * dd + T(WENO_EPS * WENO_EPS));
+    const T s1 = qdiv(T(1), b1 + T(WENO_EPS)), s2 = qdiv(T(1), b2 + T(WENO_EPS)), s3 = qdiv(T(1), b3 + T(WENO_EPS));
+    const T w1 = T(0.1) * (T(1) + qdiv(tau, b1 + T(WENO_EPS)));
+    const T w2 = T(0.6) * (T(1) + qdiv(tau, b2 + T(WENO_EPS)));
+    const T w3 = T(0.3) * (T(1) + qdiv(tau, b3 + T(WENO_EPS)));
+    const T W = w1 + w2 + w3;
+    const T R = qdiv(w1 * r1 + w2 * r2 + w3 * r3, W);
+    const T iW = qdiv(T(1), W);
+    const T aw1 = (r1 - R) * iW, aw2 = (r2 - R) * iW, aw3 = (r3 - R) * iW;
+    const T ar1 = w1 * iW, ar2 = w2 * iW, ar3 = w3 * iW;
+    const T atau = aw1 * T(0.1) * s1 + aw2 * T(0.6) * s2 + aw3 * T(0.3) * s3;
+    const T dtau = qdiv(dd, tau);
+    const T ab1 = -aw1 * T(0.1) * tau * s1 * s1 + atau * dtau;
+    const T ab2 = -aw2 * T(0.6) * tau * s2 * s2;
+    const T ab3 = -aw3 * T(0.3) * tau * s3 * s3 - atau * dtau;
+    const T c1 = T(2) * k1 * d1 * ab1, h1 = T(2) * k2 * f1 * ab1;
+    const T c2 = T(2) * k1 * d2 * ab2, h2 = T(2) * k2 * f2 * ab2;
+    const T c3 = T(2) * k1 * d3 * ab3, h3 = T(2) * k2 * f3 * ab3;
+    g[0] += ar1 * T(1.0 / 3.0) + c1 + h1;
+    g[1] += ar1 * T(-7.0 / 6.0) + ar2 * T(-1.0 / 6.0) - T(2) * c1 - T(4) * h1 + c2 + h2;
+    g[2] += ar1 * T(11.0 / 6.0) + ar2 * T(5.0 / 6.0) + ar3 * T(1.0 / 3.0) + c1 + T(3) * h1 - T(2) * c2 + c3 +
+            T(3) * h3;
+    g[3] += ar2 * T(1.0 / 3.0) + ar3 * T(5.0 / 6.0) + c2 - h2 - T(2) * c3 - T(4) * h3;
+    g[4] += ar3 * T(-1.0 / 6.0) + c3 + h3;
+    return R;
+}
+
+// Local gradient of the face flux: dF/dq[0..5], dF/dvel.
 template <typename T>
 __device__ __forceinline__ void weno_flux_grad(const T* q, T vel, int bits, bool ok4, bool ok6, T* g, T& gv)
 {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) g[k] = T(0);
     if (vel == T(0)) {
         const T P = recon<T>(q, bits, ok4, ok6, false), M = recon<T>(q, bits, ok4, ok6, true);
-#pragma unroll
-        for (int k = 0; k < 6; ++k) g[k] = T(0);
         gv = T(0.5) * (P + M);
         return;
     }
     const bool rev = vel < T(0);
-    DN<T, 6> qd[6];
+    T qq[6], gg[6];
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
-        qd[k].v = rev ? q[5 - k] : q[k];
-#pragma unroll
-        for (int m = 0; m < 6; ++m) qd[k].d[m] = (k == m) ? T(1) : T(0);
+        qq[k] = rev ? q[5 - k] : q[k];
+        gg[k] = T(0);
     }
-    const DN<T, 6> R = recon<T>(qd, bits, ok4, ok6, false);
+    T R = T(0);
+    if (bits & 1) {
+        R = T(0.5) * (qq[2] + qq[3]);
+        gg[2] += T(0.5);
+        gg[3] += T(0.5);
+    }
+    if ((bits & 2) && ok4) R = R + wenoz4_grad(qq, gg);
+    if ((bits & 4) && ok6) R = R + wenoz6_grad(qq, gg);
 #pragma unroll
-    for (int k = 0; k < 6; ++k) g[k] = vel * (rev ? R.d[5 - k] : R.d[k]);
-    gv = R.v;
+    for (int k = 0; k < 6; ++k) g[k] = vel * (rev ? gg[5 - k] : gg[k]);
+    gv = R;
 }
 
 // ------------------------------------------------------------------ tables
