@@ -97,6 +97,21 @@ def test_batched_modes_against_oracle():
     assert rel(out, ref) < 1e-10
 
 
+@pytest.mark.parametrize("nx,ny", [(20, 8), (12, 15), (9, 48), (17, 100), (7, 768), (30, 131)])
+def test_transform_lengths_fp64(nx, ny):
+    """float64 solves through the FFT form of the transform (2 ny = 16, 30,
+    96, 200, 1536: radices 4, 2, 3, 5) and the dense form (2 x 131 = 262)."""
+    from vardyn_gb300.helmholtz_dst import HelmholtzDST
+    rng = np.random.default_rng(nx * ny)
+    shift = np.array([0.0, 0.3, 2.0])
+    s = HelmholtzDST(nx, ny, 1.1, 0.9, shift)
+    rhs = rng.standard_normal((2, 3, nx - 1, ny - 1))
+    helm = O.compute_laplace_dstI(nx, ny, 1.1, 0.9)[None] - shift.reshape(3, 1, 1)
+    out = s.solve(torch.as_tensor(rhs, device="cuda")).cpu().numpy()
+    for b in range(2):
+        assert rel(out[b], O.solve_helmholtz_dstI(rhs[b], helm)) < 1e-12
+
+
 def test_cmm_without_boundary_points_is_masked_solve(g):
     s = solver(g)
     rhs = torch.tensor(g["helm_rhs"], device="cuda")

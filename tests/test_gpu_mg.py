@@ -45,6 +45,25 @@ def test_mg_fp64_matches_oracle(niter_bottom):
     assert rel(f, fo) < 1e-11
 
 
+@pytest.mark.parametrize("niter_bottom", [-1, 20])
+@pytest.mark.parametrize("n0,n1", [(48, 32), (16, 24), (8, 8)])
+def test_mg_small_grids_fp64_match_oracle(n0, n1, niter_bottom):
+    """Grids whose every level runs in the one-block coarse kernel (from level
+    0, on the caller's buffers), and a single-level grid."""
+    from vardyn_gb300.helmholtz_mg import MG_Helmholtz
+    rng = np.random.default_rng(n0 * n1)
+    mask = np.ones((n0, n1))
+    mask[n0 // 3:n0 // 2, n1 // 4:n1 // 2] = 0
+    cu = 1.0 + 0.3 * rng.random((n0 + 1, n1))
+    cv = 1.0 + 0.3 * rng.random((n0, n1 + 1))
+    lam = np.array([1e-3, 4e-3, 0.5])
+    g = MG_Helmholtz(1.0, 1.3, n0, n1, cu, cv, lambd=lam, mask=mask, niter_bottom=niter_bottom, max_ite=5)
+    o = MGOracle(1.0, 1.3, n0, n1, cu, cv, lam, mask=mask, niter_bottom=niter_bottom, max_ite=5)
+    assert g.n_levels == o.n_levels
+    rhs = rng.standard_normal((3, n0, n1)) * mask
+    assert rel(g.solve(rhs), o.solve(rhs)) < 1e-11
+
+
 def test_mg_converges_to_direct_solve_and_fp32():
     from vardyn_gb300.helmholtz_mg import MG_Helmholtz
     rng, mask, cu, cv = case(128, 96, 4)

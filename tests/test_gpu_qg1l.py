@@ -100,9 +100,11 @@ def _rand_case(scheme, ny=22, nx=27, seed=0, land=True):
     return kw, np.nan_to_num(ssh), 0.01 * rng.standard_normal((ny, nx)), rng
 
 
+# nx = 27: dense transform (26 = 2 x 13); nx = 31: FFT transform (L = 60)
+@pytest.mark.parametrize("nx", [27, 31])
 @pytest.mark.parametrize("scheme", ["Euler", "rk2", "rk3", "rk4"])
-def test_tangent_fp64_matches_oracle(scheme):
-    kw, h0, hb, rng = _rand_case(scheme)
+def test_tangent_fp64_matches_oracle(scheme, nx):
+    kw, h0, hb, rng = _rand_case(scheme, nx=nx)
     ref = QgmOracle(**kw)
     m = Qgm(dtype="float64", **kw)
     dh = 0.01 * rng.standard_normal(h0.shape)
@@ -111,19 +113,20 @@ def test_tangent_fp64_matches_oracle(scheme):
     assert rel(m.step_tgl(dh, h0, hb, 4), exp) < 1e-10
 
 
+@pytest.mark.parametrize("nx", [27, 31])
 @pytest.mark.parametrize("scheme", ["Euler", "rk2", "rk3", "rk4"])
-def test_adjoint_fp64_matches_oracle(scheme):
-    kw, h0, hb, rng = _rand_case(scheme, seed=4)
+def test_adjoint_fp64_matches_oracle(scheme, nx):
+    kw, h0, hb, rng = _rand_case(scheme, seed=4, nx=nx)
     ref = QgmOracle(**kw)
     m = Qgm(dtype="float64", **kw)
     ad = rng.standard_normal(h0.shape)
     assert rel(m.step_adj(ad, h0, hb, 4), ref.step_adj(ad, h0, hb, 4)) < 1e-10
 
 
-@pytest.mark.parametrize("dtype,tol", [("float64", 1e-12), ("float32", 2e-4)])
-def test_dot_product_on_gpu(dtype, tol):
+@pytest.mark.parametrize("dtype,tol,nx", [("float64", 1e-12, 48), ("float64", 1e-12, 49), ("float32", 2e-4, 48)])
+def test_dot_product_on_gpu(dtype, tol, nx):
     """<M dx, y> = <dx, M^T y> (mod.py:5367-5446 form), inner products in FP64."""
-    kw, h0, hb, rng = _rand_case("rk2", ny=40, nx=48, seed=7)
+    kw, h0, hb, rng = _rand_case("rk2", ny=40, nx=nx, seed=7)
     m = Qgm(dtype=dtype, **kw)
     dx_ = rng.standard_normal(h0.shape)
     y = rng.standard_normal(h0.shape)
@@ -146,10 +149,13 @@ def test_batched_equals_single():
         assert rel(batched[b], m.step(hs[b], hb, 5)) < 1e-14
 
 
-@pytest.mark.parametrize("ny,nx", [(37, 45), (64, 130), (130, 64), (200, 262)])
+@pytest.mark.parametrize("ny,nx", [(37, 45), (64, 130), (130, 64), (200, 262), (37, 61), (50, 16), (24, 769),
+                                   (33, 9)])
 def test_odd_and_ragged_grids_fp64(ny, nx):
     """Odd transform lengths (middle element of the even/odd split), ragged
-    CTA tiles, more than one column tile."""
+    CTA tiles, more than one column tile; nx - 1 = 60, 15, 768 and 8 take the
+    FFT form of the float64 transform (radices 4/2/3/5), the others the dense
+    one."""
     rng = np.random.default_rng(ny * nx)
     dx = np.full((ny, nx), 5.0e3)
     kw = dict(dx=dx, dy=dx, dt=600.0, c=2.7, f=1e-4, time_scheme="rk2")

@@ -365,6 +365,209 @@ tridiag_global_kernel(T* __restrict__ spec, const T* __restrict__ trim, int my, 
 }
 
 // ---------------------------------------------------------------------------
+// Float64 DST-I by FFT
+//
+// The FP64 rate of this part is a small fraction of its FP32 / tensor rate, so
+// the O(n^2) dense transform above costs ~3 ms a field at n ~ 1000 even at
+// the FP64 peak; an FFT does the same transform in O(n log n). Two real rows
+// a, b are packed as z = a + i b into their odd extension of length
+// L = 2(n+1): z_0 = z_{n+1} = 0, z_{p+1} = a_p + i b_p, z_{L-1-p} = -z_{p+1}.
+// The DFT of a real odd sequence is purely imaginary,
+//   A_m = -2i sum_p a_p sin(pi (p+1) m / (n+1)),
+// so Z = A + i B gives both rows at once: DST_a(m) = -Im Z_m / 2 and
+// DST_b(m) = Re Z_m / 2, times sqrt(2/(n+1)) for the orthonormal form. The
+// FFT is a Stockham autosort (each stage reads v_r = x[j + r L/R], applies the
+// twiddles e^{-2 pi i k r / (Ns R)} with k = j mod Ns, takes the length-R DFT
+// and writes y[(j/Ns) Ns R + k + r Ns]; the output is in natural order) with
+// radix 4, 2, 3 and 5 stages, ping-ponging between two shared-memory buffers.
+// The orthonormal DST-I is its own inverse, so the inverse pass is the same
+// transform from the parity-split spectral rows to the field.
+// ---------------------------------------------------------------------------
+struct FftGeom {
+    int L, N, n, ne, my, nx, R, lds, nst, pp;
+    long long fs;
+    double scale;        // sqrt(2/N) / 2
+    int rad[24];
+};
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b)
+{
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+// -i * a
+__device__ __forceinline__ double2 cmi(double2 a) { return make_double2(a.y, -a.x); }
+
+template <int R> struct Dft;
+template <> struct Dft<2> {
+    static __device__ __forceinline__ void run(double2 (&v)[2])
+    {
+        const double2 a = v[0], b = v[1];
+        v[0] = cadd(a, b);
+        v[1] = csub(a, b);
+    }
+};
+template <> struct Dft<4> {
+    static __device__ __forceinline__ void run(double2 (&v)[4])
+    {
+        const double2 a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
+        const double2 c = cadd(v[1], v[3]), d = cmi(csub(v[1], v[3]));
+        v[0] = cadd(a, c);
+        v[2] = csub(a, c);
+        v[1] = cadd(b, d);
+        v[3] = csub(b, d);
+    }
+};
+template <> struct Dft<3> {
+    // y1,2 = v0 - (v1+v2)/2 -/+ i (sqrt(3)/2) (v1 - v2)
+    static __device__ __forceinline__ void run(double2 (&v)[3])
+    {
+        constexpr double S3 = 0.86602540378443864676;   // sqrt(3)/2
+        const double2 t = cadd(v[1], v[2]);
+        const double2 m = make_double2(v[0].x - 0.5 * t.x, v[0].y - 0.5 * t.y);
+        const double2 d = cmi(csub(v[1], v[2]));
+        const double2 e = make_double2(S3 * d.x, S3 * d.y);
+        v[0] = cadd(v[0], t);
+        v[1] = cadd(m, e);
+        v[2] = csub(m, e);
+    }
+};
+template <> struct Dft<5> {
+    // pairs r, 5-r: t1 = v1+v4, t2 = v2+v3, d1 = v1-v4, d2 = v2-v3;
+    // y1,4 = v0 + c1 t1 + c2 t2 -/+ i (s1 d1 + s2 d2)
+    // y2,3 = v0 + c2 t1 + c1 t2 -/+ i (s2 d1 - s1 d2)
+    static __device__ __forceinline__ void run(double2 (&v)[5])
+    {
+        constexpr double C1 = 0.30901699437494742410;    // cos(2 pi / 5)
+        constexpr double C2 = -0.80901699437494742410;   // cos(4 pi / 5)
+        constexpr double S1 = 0.95105651629515357212;    // sin(2 pi / 5)
+        constexpr double S2 = 0.58778525229247312917;    // sin(4 pi / 5)
+        const double2 t1 = cadd(v[1], v[4]), t2 = cadd(v[2], v[3]);
+        const double2 d1 = cmi(csub(v[1], v[4])), d2 = cmi(csub(v[2], v[3]));
+        const double2 a1 = make_double2(v[0].x + C1 * t1.x + C2 * t2.x, v[0].y + C1 * t1.y + C2 * t2.y);
+        const double2 a2 = make_double2(v[0].x + C2 * t1.x + C1 * t2.x, v[0].y + C2 * t1.y + C1 * t2.y);
+        const double2 b1 = make_double2(S1 * d1.x + S2 * d2.x, S1 * d1.y + S2 * d2.y);
+        const double2 b2 = make_double2(S2 * d1.x - S1 * d2.x, S2 * d1.y - S1 * d2.y);
+        v[0] = cadd(v[0], cadd(t1, t2));
+        v[1] = cadd(a1, b1);
+        v[4] = csub(a1, b1);
+        v[2] = cadd(a2, b2);
+        v[3] = csub(a2, b2);
+    }
+};
+
+template <int R>
+__device__ __forceinline__ void fft_stage(const double2* __restrict__ in, double2* __restrict__ out,
+                                          const double2* __restrict__ tw, int L, int Ns, int pp)
+{
+    const int T = L / R;
+    const int tstep = L / (Ns * R);
+    for (int idx = threadIdx.x; idx < pp * T; idx += blockDim.x) {
+        const int q = idx / T;
+        const int j = idx - q * T;
+        const int k = j % Ns;
+        const double2* I = in + (long long)q * L;
+        double2* O = out + (long long)q * L;
+        double2 v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[r] = I[j + r * T];
+        if (Ns > 1) {
+#pragma unroll
+            for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(tw + (long long)k * r * tstep));
+        }
+        Dft<R>::run(v);
+        const int base = (j / Ns) * Ns * R + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) O[base + r * Ns] = v[r];
+    }
+}
+
+// One CTA: g.pp pairs of rows (2 g.pp consecutive rows of the R row list).
+template <int MODE, int EPI>
+__global__ void __launch_bounds__(256)
+dst_fft_kernel(FftGeom g, const double2* __restrict__ tw, const double* __restrict__ src,
+               const double* __restrict__ sub, int sub_batches, double* __restrict__ spec,
+               double* __restrict__ out, const double* __restrict__ add, int add_batches,
+               const int8_t* __restrict__ mask)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double2* b0 = reinterpret_cast<double2*>(smem_raw);
+    double2* b1 = b0 + (size_t)g.pp * g.L;
+    const int L = g.L, N = g.N, n = g.n;
+    const int row_base = 2 * blockIdx.x * g.pp;
+
+    auto load = [&](int row, int p) -> double {
+        if (row >= g.R) return 0.0;
+        if (MODE == MODE_FWD) {
+            const int f = row / g.my;
+            const int j = row - f * g.my + 1;
+            const long long o = f * g.fs + (long long)j * g.nx + 1 + p;
+            double x = src[o];
+            if (sub != nullptr && f < sub_batches) x -= sub[o];
+            return x;
+        } else {
+            const int t = (p & 1) ? g.ne + (p >> 1) : (p >> 1);
+            return spec[(long long)row * g.lds + t];
+        }
+    };
+    for (int idx = threadIdx.x; idx < g.pp * n; idx += blockDim.x) {
+        const int q = idx / n;
+        const int p = idx - q * n;
+        const int ra = row_base + 2 * q;
+        const double xa = load(ra, p), xb = load(ra + 1, p);
+        double2* Z = b0 + (size_t)q * L;
+        Z[p + 1] = make_double2(xa, xb);
+        Z[L - 1 - p] = make_double2(-xa, -xb);
+    }
+    for (int q = threadIdx.x; q < g.pp; q += blockDim.x) {
+        b0[(size_t)q * L] = make_double2(0.0, 0.0);
+        b0[(size_t)q * L + N] = make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+    int Ns = 1;
+    for (int s = 0; s < g.nst; ++s) {
+        const int R = g.rad[s];
+        switch (R) {
+            case 4: fft_stage<4>(b0, b1, tw, L, Ns, g.pp); break;
+            case 2: fft_stage<2>(b0, b1, tw, L, Ns, g.pp); break;
+            case 3: fft_stage<3>(b0, b1, tw, L, Ns, g.pp); break;
+            default: fft_stage<5>(b0, b1, tw, L, Ns, g.pp); break;
+        }
+        __syncthreads();
+        double2* t = b0; b0 = b1; b1 = t;
+        Ns *= R;
+    }
+    for (int idx = threadIdx.x; idx < g.pp * n; idx += blockDim.x) {
+        const int q = idx / n;
+        const int k = idx - q * n;
+        const double2 Zm = b0[(size_t)q * L + k + 1];
+        const double ys[2] = {-Zm.y * g.scale, Zm.x * g.scale};
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int row = row_base + 2 * q + u;
+            if (row >= g.R) continue;
+            if (MODE == MODE_FWD) {
+                const int t = (k & 1) ? g.ne + (k >> 1) : (k >> 1);
+                spec[(long long)row * g.lds + t] = ys[u];
+            } else {
+                const int f = row / g.my;
+                const int j = row - f * g.my + 1;
+                const long long o = f * g.fs + (long long)j * g.nx + 1 + k;
+                if (EPI == EPI_H) {
+                    double y = ys[u];
+                    if (add != nullptr && f < add_batches) y += add[o];
+                    out[o] = y;
+                } else {
+                    const int mi = j * g.nx + 1 + k;
+                    out[o] = (mask[mi] == 3) ? ys[u] + add[o] : 0.0;
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
 size_t spec_bytes(const vd_qg1l_plan* p, int nf)
@@ -378,6 +581,40 @@ static int upload(const std::vector<double>& h, void** d)
     std::vector<T> tmp(h.begin(), h.end());
     VD_CUDA_TRY(cudaMalloc(d, tmp.size() * sizeof(T)));
     VD_CUDA_TRY(cudaMemcpy(*d, tmp.data(), tmp.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return VD_OK;
+}
+
+// FFT radices for L = 2(n+1) (radix 4 first, then 2, 3, 5); false when L has
+// another prime factor or its buffers do not fit shared memory.
+static bool fft_factor(int L, std::vector<int>& rad)
+{
+    rad.clear();
+    if (L < 4 || size_t(2) * L * sizeof(double2) > 200 * 1024) return false;
+    int m = L;
+    while (m % 4 == 0) { rad.push_back(4); m /= 4; }
+    while (m % 2 == 0) { rad.push_back(2); m /= 2; }
+    while (m % 3 == 0) { rad.push_back(3); m /= 3; }
+    while (m % 5 == 0) { rad.push_back(5); m /= 5; }
+    return m == 1 && rad.size() <= 24;
+}
+
+static int build_fft_tables(DSTTables& t)
+{
+    const int L = 2 * (t.n + 1);
+    std::vector<int> rad;
+    if (!fft_factor(L, rad)) return VD_OK;
+    std::vector<double> tw(size_t(2) * L);
+    for (int m = 0; m < L; ++m) {
+        // e^{-2 pi i m / L} in float64 on the host
+        const double a = 2.0 * M_PI * double(m) / double(L);
+        tw[2 * m] = std::cos(a);
+        tw[2 * m + 1] = -std::sin(a);
+    }
+    int rc;
+    if ((rc = upload<double>(tw, &t.fft_tw))) return rc;
+    t.fft_L = L;
+    t.fft_nst = (int)rad.size();
+    for (size_t i = 0; i < rad.size(); ++i) t.fft_rad[i] = rad[i];
     return VD_OK;
 }
 
@@ -432,6 +669,7 @@ int build_dst_tables(vd_qg1l_plan* p)
         }
     }
     int rc;
+    if (p->d.dtype == VD_F64 && (rc = build_fft_tables(t))) return rc;
     if (p->d.dtype == VD_F32) {
         if ((rc = upload<float>(wodd, &t.Wodd))) return rc;
         if ((rc = upload<float>(woddT, &t.WoddT))) return rc;
@@ -452,6 +690,7 @@ void free_dst_tables(vd_qg1l_plan* p)
     cudaFree(p->dst.WoddT);
     cudaFree(p->dst.Weven);
     cudaFree(p->dst.trim);
+    cudaFree(p->dst.fft_tw);
 }
 
 template <typename T, int TR>
@@ -508,6 +747,13 @@ static cudaError_t configure_kernels()
         if (!e) e = set_smem_attrs<float, 64>();
         if (!e) e = set_smem_attrs<double, 16>();
         if (!e) e = set_smem_attrs<double, 32>();
+        const int maxb = 227 * 1024;
+        if (!e) e = cudaFuncSetAttribute(dst_fft_kernel<MODE_FWD, EPI_H>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, maxb);
+        if (!e) e = cudaFuncSetAttribute(dst_fft_kernel<MODE_INV, EPI_H>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, maxb);
+        if (!e) e = cudaFuncSetAttribute(dst_fft_kernel<MODE_INV, EPI_ADJQ>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, maxb);
         g_attr_err = e;
     });
     return g_attr_err;
@@ -533,6 +779,41 @@ static int launch_pair(const vd_qg1l_plan* p, const GemmGeom& g, const SolveArgs
         dst_gemm_kernel<T, TR, MODE_INV, EPI_ADJQ><<<grid, NT, smem, st>>>(
             g, (const T*)t.WoddT, (const T*)t.Weven, nullptr, nullptr, 0, spec, (T*)a.out,
             (const T*)a.add, a.add_batches, p->d_mask);
+    }
+    VD_LAUNCH_CHECK();
+    return VD_OK;
+}
+
+// The float64 FFT pass over g.R rows: pairs of rows per CTA chosen for about
+// two CTAs per SM-wave slot and at most ~100 KB of shared memory per CTA.
+static int launch_fft(const vd_qg1l_plan* p, const GemmGeom& g, const SolveArgs& a, double* spec,
+                      cudaStream_t st, bool fwd)
+{
+    const DSTTables& t = p->dst;
+    FftGeom fg;
+    fg.L = t.fft_L; fg.N = t.n + 1; fg.n = t.n; fg.ne = t.ne; fg.my = t.my; fg.nx = g.nx;
+    fg.R = g.R; fg.lds = t.lds; fg.nst = t.fft_nst; fg.fs = g.fs;
+    fg.scale = 0.5 * std::sqrt(2.0 / double(t.n + 1));
+    for (int i = 0; i < 24; ++i) fg.rad[i] = t.fft_rad[i];
+    const int pairs = (g.R + 1) / 2;
+    const size_t per_pair = size_t(2) * t.fft_L * sizeof(double2);
+    int pp = std::max(1, std::min<int>(8, int((100 * 1024) / per_pair)));
+    pp = std::max(1, std::min(pp, pairs / (2 * 152)));
+    fg.pp = pp;
+    const size_t smem = per_pair * pp;
+    const dim3 grid((pairs + pp - 1) / pp);
+    const double2* tw = (const double2*)t.fft_tw;
+    if (fwd) {
+        dst_fft_kernel<MODE_FWD, EPI_H><<<grid, 256, smem, st>>>(fg, tw, (const double*)a.src,
+                                                                 (const double*)a.sub, a.sub_batches, spec,
+                                                                 nullptr, nullptr, 0, nullptr);
+    } else if (a.epi == EPI_H) {
+        dst_fft_kernel<MODE_INV, EPI_H><<<grid, 256, smem, st>>>(fg, tw, nullptr, nullptr, 0, spec, (double*)a.out,
+                                                                 (const double*)a.add, a.add_batches, p->d_mask);
+    } else {
+        dst_fft_kernel<MODE_INV, EPI_ADJQ><<<grid, 256, smem, st>>>(fg, tw, nullptr, nullptr, 0, spec,
+                                                                    (double*)a.out, (const double*)a.add,
+                                                                    a.add_batches, p->d_mask);
     }
     VD_LAUNCH_CHECK();
     return VD_OK;
@@ -571,6 +852,8 @@ int helmholtz_solve(const vd_qg1l_plan* p, int nf, const SolveArgs& a, T* spec, 
         if constexpr (sizeof(T) == 4) {
             if (p->dst.tc && tc_fits(p, nf)) return dst_pass_tc(p, nf, a, (float*)spec, fwd, st);
             if (tr == 64) return launch_pair<T, 64>(p, g, a, spec, st, fwd);
+        } else {
+            if (p->dst.fft_L) return launch_fft(p, g, a, (double*)spec, st, fwd);
         }
         if (tr == 32) return launch_pair<T, 32>(p, g, a, spec, st, fwd);
         return launch_pair<T, 16>(p, g, a, spec, st, fwd);
@@ -602,6 +885,8 @@ int dst_x_only(const vd_qg1l_plan* p, int nf, const T* field, T* spec, int inver
     if constexpr (sizeof(T) == 4) {
         if (p->dst.tc && tc_fits(p, nf)) return dst_pass_tc(p, nf, a, (float*)spec, !inverse, st);
         if (tr == 64) return launch_pair<T, 64>(p, g, a, spec, st, !inverse);
+    } else {
+        if (p->dst.fft_L) return launch_fft(p, g, a, (double*)spec, st, !inverse);
     }
     if (tr == 32) return launch_pair<T, 32>(p, g, a, spec, st, !inverse);
     return launch_pair<T, 16>(p, g, a, spec, st, !inverse);

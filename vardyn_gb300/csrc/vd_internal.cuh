@@ -60,6 +60,11 @@ struct DSTTables {
     void* trim;   // [my][lds] Thomas multipliers m_j per spectral column
     double tri_a; // off-diagonal g/f/dy^2
     void* tc;     // tensor-core images and tile table (float32 plans), or nullptr
+    // float64 plans whose odd extension 2(n+1) factors into 2, 3, 5: the
+    // FFT form of the transform (twiddles e^{-2 pi i m / L}, radix per stage)
+    void* fft_tw = nullptr;
+    int fft_L = 0, fft_nst = 0;
+    int fft_rad[24] = {};
 };
 
 constexpr int DST_NC = 128;   // output columns per CTA tile

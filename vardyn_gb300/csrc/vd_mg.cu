@@ -101,6 +101,7 @@ struct vd_mg_plan {
     std::vector<double> lambda;
     std::vector<HLevel> lv;
     int nb = 0;                          // bottom cells
+    int lc = 0;                          // first level run by the one-block coarse kernel (nlev: none)
     void* dev = nullptr;
     struct DLev {
         const void *mask = nullptr, *cu = nullptr, *cv = nullptr, *factor = nullptr, *divr = nullptr,
@@ -110,6 +111,15 @@ struct vd_mg_plan {
     const void* lam = nullptr;           // [nsys]
     const int32_t* bot_idx = nullptr;    // [nb] flat bottom cell index
     const void* bot_inv = nullptr;       // [nsys][nb][nb]
+    // the bottom level's 6 niter_bottom damped sweeps as one linear map,
+    // f = N rhs (+ M f on a one-level grid): [nsys][N, M][input k][output m]
+    const void* bot_sm = nullptr;
+    // the whole solve as one CUDA graph on plan-owned rhs / solution buffers
+    // (captured at the first solve with a given workspace, replayed after)
+    void* gbuf = nullptr;                // [2][nsys][n0][n1]: rhs, solution
+    cudaStream_t gstream = nullptr;      // capture stream
+    cudaGraphExec_t gexec = nullptr;
+    const void* gws = nullptr;           // workspace the graph was captured with
     std::vector<size_t> ws_off;          // per level: f, rhs, tmp offsets (elements)
     size_t ws_elems = 0;
 };
@@ -129,7 +139,59 @@ __device__ __forceinline__ T fat(const T* f, int n0, int n1, int i, int j)
     return (i < 0 || j < 0 || i >= n0 || j >= n1) ? T(0) : f[(long long)i * n1 + j];
 }
 
-// one damped Jacobi sweep (helmholtz_multigrid.py:86-98)
+// Per-point arithmetic, shared by the level-wide kernels and the one-block
+// coarse-level kernel so that both give the same bits.
+
+// one damped Jacobi update at (i, j) (helmholtz_multigrid.py:86-98)
+template <typename T>
+__device__ __forceinline__ T mg_sweep_pt(const MgLev<T>& L, const T* F, T rhs, T factor, int i, int j, T omega)
+{
+    const long long o = (long long)i * L.n1 + j;
+    const T cup = L.cu[(long long)(i + 1) * L.n1 + j], cui = L.cu[o];
+    const T cvp = L.cv[(long long)i * (L.n1 + 1) + j + 1], cvi = L.cv[(long long)i * (L.n1 + 1) + j];
+    const T s = L.dxm2 * (cup * fat(F, L.n0, L.n1, i + 1, j) + cui * fat(F, L.n0, L.n1, i - 1, j)) +
+                L.dym2 * (cvp * fat(F, L.n0, L.n1, i, j + 1) + cvi * fat(F, L.n0, L.n1, i, j - 1));
+    return omega * factor * (s - rhs) + (T(1) - omega) * F[o];
+}
+
+// rhs - mask (div(c grad f) - lambda f) at (i, j)  (helmholtz_multigrid.py:102-114)
+template <typename T>
+__device__ __forceinline__ T mg_residual_pt(const MgLev<T>& L, const T* F, T rhs, T lam, int i, int j)
+{
+    const long long o = (long long)i * L.n1 + j;
+    const T fc = F[o];
+    const T cup = L.cu[(long long)(i + 1) * L.n1 + j], cui = L.cu[o];
+    const T cvp = L.cv[(long long)i * (L.n1 + 1) + j + 1], cvi = L.cv[(long long)i * (L.n1 + 1) + j];
+    const T hx = cup * (fat(F, L.n0, L.n1, i + 1, j) - fc) - cui * (fc - fat(F, L.n0, L.n1, i - 1, j));
+    const T hy = cvp * (fat(F, L.n0, L.n1, i, j + 1) - fc) - cvi * (fc - fat(F, L.n0, L.n1, i, j - 1));
+    const T Hf = (hx * L.dxm2 + hy * L.dym2 - lam * fc) * L.mask[o];
+    return rhs - Hf;
+}
+
+// (sum of the 2x2 fine cells) / div * mask_coarse at coarse (I, J)  (147-151)
+template <typename T>
+__device__ __forceinline__ T mg_restrict_pt(const T* fine, int n1c, int I, int J, const T* divr, const T* maskc)
+{
+    const int n1f = 2 * n1c;
+    const T* F = fine + (long long)(2 * I) * n1f + 2 * J;
+    const long long o = (long long)I * n1c + J;
+    const T s = F[0] + F[n1f] + F[1] + F[n1f + 1];
+    return s / divr[o] * maskc[o];
+}
+
+// prolong(coarse) / div * mask_fine at fine (i, j)  (117-144)
+template <typename T>
+__device__ __forceinline__ T mg_prolong_pt(const T* V, int n0c, int n1c, int i_f, int jf, const T* divp,
+                                           const T* maskf)
+{
+    const int I = i_f >> 1, J = jf >> 1;
+    const int di = (i_f & 1) ? 1 : -1, dj = (jf & 1) ? 1 : -1;
+    const T q = T(9) * fat(V, n0c, n1c, I, J) + T(3) * (fat(V, n0c, n1c, I, J + dj) + fat(V, n0c, n1c, I + di, J)) +
+                fat(V, n0c, n1c, I + di, J + dj);
+    const long long o = (long long)i_f * (2 * n1c) + jf;
+    return q / divp[o] * maskf[o];
+}
+
 template <typename T>
 __global__ void k_mg_sweep(MgLev<T> L, const T* __restrict__ f, const T* __restrict__ rhs, T* __restrict__ out,
                            T omega)
@@ -138,15 +200,9 @@ __global__ void k_mg_sweep(MgLev<T> L, const T* __restrict__ f, const T* __restr
     const int i = blockIdx.y, b = blockIdx.z;
     if (j >= L.n1) return;
     const long long fs = (long long)L.n0 * L.n1, o = (long long)i * L.n1 + j;
-    const T* F = f + b * fs;
-    const T cup = L.cu[(long long)(i + 1) * L.n1 + j], cui = L.cu[o];
-    const T cvp = L.cv[(long long)i * (L.n1 + 1) + j + 1], cvi = L.cv[(long long)i * (L.n1 + 1) + j];
-    const T s = L.dxm2 * (cup * fat(F, L.n0, L.n1, i + 1, j) + cui * fat(F, L.n0, L.n1, i - 1, j)) +
-                L.dym2 * (cvp * fat(F, L.n0, L.n1, i, j + 1) + cvi * fat(F, L.n0, L.n1, i, j - 1));
-    out[b * fs + o] = omega * L.factor[b * fs + o] * (s - rhs[b * fs + o]) + (T(1) - omega) * F[o];
+    out[b * fs + o] = mg_sweep_pt(L, f + b * fs, rhs[b * fs + o], L.factor[b * fs + o], i, j, omega);
 }
 
-// res = rhs - mask (div(c grad f) - lambda f)  (helmholtz_multigrid.py:102-114)
 template <typename T>
 __global__ void k_mg_residual(MgLev<T> L, const T* __restrict__ f, const T* __restrict__ rhs, T* __restrict__ res)
 {
@@ -154,17 +210,9 @@ __global__ void k_mg_residual(MgLev<T> L, const T* __restrict__ f, const T* __re
     const int i = blockIdx.y, b = blockIdx.z;
     if (j >= L.n1) return;
     const long long fs = (long long)L.n0 * L.n1, o = (long long)i * L.n1 + j;
-    const T* F = f + b * fs;
-    const T fc = F[o];
-    const T cup = L.cu[(long long)(i + 1) * L.n1 + j], cui = L.cu[o];
-    const T cvp = L.cv[(long long)i * (L.n1 + 1) + j + 1], cvi = L.cv[(long long)i * (L.n1 + 1) + j];
-    const T hx = cup * (fat(F, L.n0, L.n1, i + 1, j) - fc) - cui * (fc - fat(F, L.n0, L.n1, i - 1, j));
-    const T hy = cvp * (fat(F, L.n0, L.n1, i, j + 1) - fc) - cvi * (fc - fat(F, L.n0, L.n1, i, j - 1));
-    const T Hf = (hx * L.dxm2 + hy * L.dym2 - L.lam[b] * fc) * L.mask[o];
-    res[b * fs + o] = rhs[b * fs + o] - Hf;
+    res[b * fs + o] = mg_residual_pt(L, f + b * fs, rhs[b * fs + o], L.lam[b], i, j);
 }
 
-// coarse = (sum of the 2x2 fine cells) / div * mask_coarse  (147-151)
 template <typename T>
 __global__ void k_mg_restrict(int n0c, int n1c, const T* __restrict__ fine, const T* __restrict__ divr,
                               const T* __restrict__ maskc, T* __restrict__ coarse)
@@ -172,15 +220,10 @@ __global__ void k_mg_restrict(int n0c, int n1c, const T* __restrict__ fine, cons
     const int J = blockIdx.x * blockDim.x + threadIdx.x;
     const int I = blockIdx.y, b = blockIdx.z;
     if (J >= n1c) return;
-    const int n1f = 2 * n1c;
-    const long long fsc = (long long)n0c * n1c, fsf = 4 * fsc;
-    const T* F = fine + b * fsf + (long long)(2 * I) * n1f + 2 * J;
-    const long long o = (long long)I * n1c + J;
-    const T s = F[0] + F[n1f] + F[1] + F[n1f + 1];
-    coarse[b * fsc + o] = s / divr[o] * maskc[o];
+    const long long fsc = (long long)n0c * n1c;
+    coarse[b * fsc + (long long)I * n1c + J] = mg_restrict_pt(fine + b * 4 * fsc, n1c, I, J, divr, maskc);
 }
 
-// fine (=, or +=) prolong(coarse) / div * mask_fine  (117-144)
 template <typename T>
 __global__ void k_mg_prolong(int n0c, int n1c, const T* __restrict__ coarse, const T* __restrict__ divp,
                              const T* __restrict__ maskf, T* __restrict__ fine, int add)
@@ -190,13 +233,8 @@ __global__ void k_mg_prolong(int n0c, int n1c, const T* __restrict__ coarse, con
     const int n1f = 2 * n1c;
     if (jf >= n1f) return;
     const long long fsc = (long long)n0c * n1c, fsf = 4 * fsc;
-    const T* V = coarse + b * fsc;
-    const int I = i_f >> 1, J = jf >> 1;
-    const int di = (i_f & 1) ? 1 : -1, dj = (jf & 1) ? 1 : -1;
-    const T q = T(9) * fat(V, n0c, n1c, I, J) + T(3) * (fat(V, n0c, n1c, I, J + dj) + fat(V, n0c, n1c, I + di, J)) +
-                fat(V, n0c, n1c, I + di, J + dj);
+    const T v = mg_prolong_pt(coarse + b * fsc, n0c, n1c, i_f, jf, divp, maskf);
     const long long o = (long long)i_f * n1f + jf;
-    const T v = q / divp[o] * maskf[o];
     fine[b * fsf + o] = add ? fine[b * fsf + o] + v : v;
 }
 
@@ -213,6 +251,191 @@ __global__ void k_mg_bottom(int nb, long long fs, const int32_t* __restrict__ id
     T s = T(0);
     for (int l = 0; l < nb; ++l) s += R[idx[l]] * P[(long long)l * nb + m];
     f[b * fs + idx[m]] = s;
+}
+
+// ---------------------------------------------------------------------------
+// Coarse levels in one block per system. Below a few thousand cells a level's
+// sweep is shorter than a kernel launch, and the bottom smoothing alone is
+// 6 x niter_bottom sweeps per V-cycle; this kernel runs everything from level
+// l0 down (the V-cycle, or the full-multigrid start) with the block's threads
+// striding over the level and __syncthreads() between phases. The solution,
+// right-hand side and scratch of every level from l0 down live in shared
+// memory (level l0's come in from, and its solution goes back to, global
+// memory); the coefficients are read-only global tables; the arithmetic is
+// the per-point functions above.
+// ---------------------------------------------------------------------------
+constexpr int MG_MAXLEV = 16;
+
+template <typename T>
+struct MgCoarseArgs {
+    int l0, nlev, niter_bottom, nb, fmg;
+    T omega;
+    MgLev<T> L[MG_MAXLEV];
+    const T* divr[MG_MAXLEV];   // restriction divisor of coarse level l
+    const T* divp[MG_MAXLEV];   // prolongation divisor of fine level l
+    int soff[MG_MAXLEV];        // shared-memory offset of level l: f, rhs, scratch (n0 n1 each)
+    T* f0;                      // level l0 solution (system-0 base): in (V-cycle) and out
+    const T* rhs0;              // level l0 right-hand side (system-0 base)
+    const int32_t* bot_idx;
+    const T* bot_inv;
+    const T* bot_sm;            // bottom smoothing as matrices, or nullptr
+};
+
+template <typename T>
+struct MgcLevel {
+    T *f, *rhs, *tmp;
+    int n;
+};
+
+template <typename T>
+__device__ __forceinline__ MgcLevel<T> mgc_level(const MgCoarseArgs<T>& A, T* sm, int l)
+{
+    MgcLevel<T> v;
+    v.n = A.L[l].n0 * A.L[l].n1;
+    v.f = sm + A.soff[l];
+    v.rhs = v.f + v.n;
+    v.tmp = v.rhs + v.n;
+    return v;
+}
+
+template <typename T>
+__device__ void mgc_smooth(const MgCoarseArgs<T>& A, T* sm, int l, int b, int times)
+{
+    const MgLev<T>& L = A.L[l];
+    const MgcLevel<T> v = mgc_level(A, sm, l);
+    const T* fac = L.factor + (long long)b * v.n;
+    for (int t = 0; t < times; ++t)
+        for (int s = 0; s < 6; ++s) {
+            const T* src = (s % 2 == 0) ? v.f : v.tmp;
+            T* dst = (s % 2 == 0) ? v.tmp : v.f;
+            for (int o = threadIdx.x; o < v.n; o += blockDim.x) {
+                const int i = o / L.n1, j = o - i * L.n1;
+                dst[o] = mg_sweep_pt(L, src, v.rhs[o], __ldg(fac + o), i, j, A.omega);
+            }
+            __syncthreads();
+        }
+}
+
+template <typename T>
+__device__ void mgc_bottom(const MgCoarseArgs<T>& A, T* sm, int b)
+{
+    const int l = A.nlev - 1;
+    if (A.niter_bottom > 0 && A.bot_sm != nullptr) {
+        // f = N rhs (+ M f when the grid has one level; below it f is zero here)
+        const MgcLevel<T> v = mgc_level(A, sm, l);
+        const long long n2 = (long long)v.n * v.n;
+        const T* Nm = A.bot_sm + (long long)b * 2 * n2;
+        const T* Mm = Nm + n2;
+        for (int m = threadIdx.x; m < v.n; m += blockDim.x) {
+            T s = T(0);
+            for (int k = 0; k < v.n; ++k) s += __ldg(Nm + (long long)k * v.n + m) * v.rhs[k];
+            if (A.nlev == 1)
+                for (int k = 0; k < v.n; ++k) s += __ldg(Mm + (long long)k * v.n + m) * v.f[k];
+            v.tmp[m] = s;
+        }
+        __syncthreads();
+        for (int m = threadIdx.x; m < v.n; m += blockDim.x) v.f[m] = v.tmp[m];
+        __syncthreads();
+        return;
+    }
+    if (A.niter_bottom > 0) {
+        mgc_smooth(A, sm, l, b, A.niter_bottom);
+        return;
+    }
+    const MgcLevel<T> v = mgc_level(A, sm, l);
+    for (int o = threadIdx.x; o < v.n; o += blockDim.x) v.f[o] = T(0);
+    __syncthreads();
+    const T* P = A.bot_inv + (long long)b * A.nb * A.nb;
+    for (int m = threadIdx.x; m < A.nb; m += blockDim.x) {
+        T s = T(0);
+        for (int k = 0; k < A.nb; ++k) s += v.rhs[__ldg(A.bot_idx + k)] * __ldg(P + (long long)k * A.nb + m);
+        v.f[__ldg(A.bot_idx + m)] = s;
+    }
+    __syncthreads();
+}
+
+// rhs of level lc from a fine-level field (shared memory)
+template <typename T>
+__device__ void mgc_restrict(const MgCoarseArgs<T>& A, T* sm, const T* fine, int lc)
+{
+    const MgLev<T>& C = A.L[lc];
+    const MgcLevel<T> v = mgc_level(A, sm, lc);
+    for (int o = threadIdx.x; o < v.n; o += blockDim.x) {
+        const int I = o / C.n1, J = o - I * C.n1;
+        v.rhs[o] = mg_restrict_pt(fine, C.n1, I, J, A.divr[lc], C.mask);
+    }
+}
+
+template <typename T>
+__device__ void mgc_prolong(const MgCoarseArgs<T>& A, T* sm, int l, bool add)
+{
+    const MgLev<T>& Fl = A.L[l];
+    const MgLev<T>& C = A.L[l + 1];
+    const MgcLevel<T> vf = mgc_level(A, sm, l), vc = mgc_level(A, sm, l + 1);
+    for (int o = threadIdx.x; o < vf.n; o += blockDim.x) {
+        const int i = o / Fl.n1, j = o - i * Fl.n1;
+        const T x = mg_prolong_pt(vc.f, C.n0, C.n1, i, j, A.divp[l], Fl.mask);
+        vf.f[o] = add ? vf.f[o] + x : x;
+    }
+    __syncthreads();
+}
+
+template <typename T>
+__device__ void mgc_vcycle(const MgCoarseArgs<T>& A, T* sm, int l0, int b)
+{
+    const int last = A.nlev - 1;
+    for (int l = l0; l < last; ++l) {
+        mgc_smooth(A, sm, l, b, 1);
+        const MgLev<T>& L = A.L[l];
+        const MgcLevel<T> v = mgc_level(A, sm, l);
+        for (int o = threadIdx.x; o < v.n; o += blockDim.x) {
+            const int i = o / L.n1, j = o - i * L.n1;
+            v.tmp[o] = mg_residual_pt(L, v.f, v.rhs[o], L.lam[b], i, j);
+        }
+        __syncthreads();
+        mgc_restrict(A, sm, v.tmp, l + 1);
+        const MgcLevel<T> c = mgc_level(A, sm, l + 1);
+        for (int o = threadIdx.x; o < c.n; o += blockDim.x) c.f[o] = T(0);
+        __syncthreads();
+    }
+    mgc_bottom(A, sm, b);
+    for (int l = last - 1; l >= l0; --l) {
+        mgc_prolong(A, sm, l, true);
+        mgc_smooth(A, sm, l, b, 1);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024) k_mg_coarse(MgCoarseArgs<T> A)
+{
+    extern __shared__ __align__(16) unsigned char mg_smem[];
+    T* sm = reinterpret_cast<T*>(mg_smem);
+    const int b = blockIdx.x;
+    const MgcLevel<T> v0 = mgc_level(A, sm, A.l0);
+    const long long g0 = (long long)b * v0.n;
+    for (int o = threadIdx.x; o < v0.n; o += blockDim.x) {
+        v0.rhs[o] = A.rhs0[g0 + o];
+        if (!A.fmg) v0.f[o] = A.f0[g0 + o];
+    }
+    __syncthreads();
+    if (!A.fmg) {
+        mgc_vcycle(A, sm, A.l0, b);
+    } else {
+        const int last = A.nlev - 1;
+        for (int l = A.l0 + 1; l <= last; ++l) {
+            mgc_restrict(A, sm, mgc_level(A, sm, l - 1).rhs, l);
+            __syncthreads();
+        }
+        const MgcLevel<T> vb = mgc_level(A, sm, last);
+        for (int o = threadIdx.x; o < vb.n; o += blockDim.x) vb.f[o] = T(0);
+        __syncthreads();
+        mgc_bottom(A, sm, b);
+        for (int l = last - 1; l >= A.l0; --l) {
+            mgc_prolong(A, sm, l, false);
+            mgc_vcycle(A, sm, l, b);
+        }
+    }
+    for (int o = threadIdx.x; o < v0.n; o += blockDim.x) A.f0[g0 + o] = v0.f[o];
 }
 
 template <typename T>
@@ -288,8 +511,33 @@ struct MgRun {
         }
         return smooth(l, f, rhs, p->niter_bottom);
     }
+    // levels >= l0 in one block per system (p->lc <= l0): a V-cycle on (f, rhs)
+    // at l0, or (fmg) the full-multigrid start from the restricted rhs at l0
+    int coarse(T* f, const T* rhs, int l0, bool fmg) const
+    {
+        vd::MgCoarseArgs<T> A;
+        A.l0 = l0; A.nlev = p->nlev; A.niter_bottom = p->niter_bottom; A.nb = p->nb; A.fmg = fmg ? 1 : 0;
+        A.omega = T(p->omega);
+        int off = 0;
+        for (int l = 0; l < p->nlev; ++l) {
+            A.L[l] = lev(l);
+            A.divr[l] = (const T*)p->dl[l].divr;
+            A.divp[l] = (const T*)p->dl[l].divp;
+            A.soff[l] = off;
+            if (l >= l0) off += 3 * p->lv[l].n0 * p->lv[l].n1;
+        }
+        A.f0 = f;
+        A.rhs0 = rhs;
+        A.bot_idx = p->bot_idx;
+        A.bot_inv = (const T*)p->bot_inv;
+        A.bot_sm = (const T*)p->bot_sm;
+        vd::k_mg_coarse<T><<<(unsigned)p->nsys, 1024, (size_t)off * sizeof(T), st>>>(A);
+        VD_LAUNCH_CHECK();
+        return VD_OK;
+    }
     int vcycle(T* f, const T* rhs, int l) const
     {
+        if (l >= p->lc) return coarse(f, rhs, l, false);
         if (l == p->nlev - 1) return bottom(f, rhs);
         int rc;
         if ((rc = smooth(l, f, rhs, 1))) return rc;
@@ -318,6 +566,25 @@ struct MgRun {
         if (n == 1) {
             if ((rc = zero(out, nel(0)))) return rc;
             if ((rc = bottom(out, rhs))) return rc;
+        } else if (p->lc < n) {
+            // host levels down to lc, then the coarse kernel's full-multigrid start
+            const int lc = p->lc;
+            for (int i = 1; i <= lc; ++i) {
+                const T* src = (i == 1) ? rhs : buf(i - 1, 1);
+                vd::k_mg_restrict<T><<<grid(p->lv[i].n0, p->lv[i].n1), 128, 0, st>>>(
+                    p->lv[i].n0, p->lv[i].n1, src, (const T*)p->dl[i].divr, (const T*)p->dl[i].mask, buf(i, 1));
+                VD_LAUNCH_CHECK();
+            }
+            if ((rc = coarse(lc == 0 ? out : buf(lc, 0), lc == 0 ? rhs : buf(lc, 1), lc, true))) return rc;
+            for (int L = lc - 1; L >= 0; --L) {
+                T* fL = (L == 0) ? out : buf(L, 0);
+                const T* rL = (L == 0) ? rhs : buf(L, 1);
+                vd::k_mg_prolong<T><<<grid(p->lv[L].n0, p->lv[L].n1), 128, 0, st>>>(
+                    p->lv[L + 1].n0, p->lv[L + 1].n1, buf(L + 1, 0), (const T*)p->dl[L].divp,
+                    (const T*)p->dl[L].mask, fL, 0);
+                VD_LAUNCH_CHECK();
+                if ((rc = vcycle(fL, rL, L))) return rc;
+            }
         } else {
             for (int i = 1; i < n; ++i) {
                 const T* src = (i == 1) ? rhs : buf(i - 1, 1);
@@ -399,6 +666,43 @@ void helm_apply(const HLevel& L, double lam, const std::vector<double>& f, std::
         }
 }
 
+// The bottom level's K damped Jacobi sweeps (the device formula, in float64)
+// as f_K = M f_0 + N rhs, by sweeping unit vectors; appended to `out` as
+// N then M (zeros when !with_m), each [input k][output m].
+void bottom_sweep_matrices(const HLevel& L, const double* factor, double omega, int K, bool with_m,
+                           std::vector<double>& out)
+{
+    const int n0 = L.n0, n1 = L.n1, n = n0 * n1;
+    const double dxm2 = 1.0 / (L.d0 * L.d0), dym2 = 1.0 / (L.d1 * L.d1);
+    std::vector<double> f(n), g(n), r(n);
+    auto sweep = [&](const std::vector<double>& src, std::vector<double>& dst) {
+        for (int i = 0; i < n0; ++i)
+            for (int j = 0; j < n1; ++j) {
+                const size_t o = (size_t)i * n1 + j;
+                const double sx = L.cu[(size_t)(i + 1) * n1 + j] * at(src, n0, n1, i + 1, j) +
+                                  L.cu[o] * at(src, n0, n1, i - 1, j);
+                const double sy = L.cv[(size_t)i * (n1 + 1) + j + 1] * at(src, n0, n1, i, j + 1) +
+                                  L.cv[(size_t)i * (n1 + 1) + j] * at(src, n0, n1, i, j - 1);
+                const double s = dxm2 * sx + dym2 * sy;
+                dst[o] = omega * factor[o] * (s - r[o]) + (1.0 - omega) * src[o];
+            }
+    };
+    const size_t base = out.size();
+    out.resize(base + 2 * (size_t)n * n, 0.0);
+    for (int pass = 0; pass < (with_m ? 2 : 1); ++pass)
+        for (int k = 0; k < n; ++k) {
+            std::fill(f.begin(), f.end(), 0.0);
+            std::fill(r.begin(), r.end(), 0.0);
+            (pass == 0 ? r : f)[k] = 1.0;
+            for (int t = 0; t < K; ++t) {
+                sweep(f, g);
+                f.swap(g);
+            }
+            double* dst = out.data() + base + (size_t)pass * n * n + (size_t)k * n;
+            std::copy(f.begin(), f.end(), dst);
+        }
+}
+
 struct Blob {
     std::vector<unsigned char> b;
     size_t add(const void* p, size_t n)
@@ -417,7 +721,8 @@ struct Blob {
 };
 
 template <typename T>
-int mg_upload(vd_mg_plan* p, const std::vector<int32_t>& idx, const std::vector<double>& inv)
+int mg_upload(vd_mg_plan* p, const std::vector<int32_t>& idx, const std::vector<double>& inv,
+              const std::vector<double>& bsm)
 {
     Blob bl;
     struct Off { size_t mask, cu, cv, factor, divr, divp; };
@@ -434,6 +739,7 @@ int mg_upload(vd_mg_plan* p, const std::vector<int32_t>& idx, const std::vector<
     const size_t o_lam = bl.addv<T>(p->lambda);
     const size_t o_idx = bl.add(idx.data(), idx.size() * sizeof(int32_t));
     const size_t o_inv = bl.addv<T>(inv);
+    const size_t o_bsm = bl.addv<T>(bsm);
     VD_CUDA_TRY(cudaMalloc(&p->dev, bl.b.size()));
     VD_CUDA_TRY(cudaMemcpy(p->dev, bl.b.data(), bl.b.size(), cudaMemcpyHostToDevice));
     unsigned char* b = (unsigned char*)p->dev;
@@ -449,6 +755,7 @@ int mg_upload(vd_mg_plan* p, const std::vector<int32_t>& idx, const std::vector<
     p->lam = b + o_lam;
     p->bot_idx = (const int32_t*)(b + o_idx);
     p->bot_inv = b + o_inv;
+    p->bot_sm = bsm.empty() ? nullptr : b + o_bsm;
     return VD_OK;
 }
 
@@ -566,7 +873,41 @@ extern "C" vd_status vd_mg_plan_create(vd_mg_plan** out, const vd_mg_desc* d)
             offw = (offw + 63) & ~size_t(63);
         }
     p->ws_elems = offw;
-    const int st = p->dtype == VD_F64 ? mg_upload<double>(p, idx, inv) : mg_upload<float>(p, idx, inv);
+    // the one-block coarse kernel takes the levels of at most 4096 cells (1024
+    // in float64: one SM's FP64 rate is ~1/64 of its FP32 rate, so a float64
+    // level of 3072 cells runs faster spread over the GPU) whose solution, rhs
+    // and scratch fit 200 KB of shared memory
+    p->lc = nlev;
+    const size_t esz = p->dtype == VD_F64 ? 8 : 4;
+    const long long max_cells = p->dtype == VD_F64 ? 1024 : 4096;
+    for (int l = 0; l < nlev; ++l) {
+        size_t sm = 0;
+        for (int k = l; k < nlev; ++k) sm += 3 * (size_t)p->lv[k].n0 * p->lv[k].n1 * esz;
+        if ((long long)p->lv[l].n0 * p->lv[l].n1 <= max_cells && sm <= 200 * 1024) {
+            p->lc = l;
+            break;
+        }
+    }
+    if (nlev > vd::MG_MAXLEV) p->lc = nlev;
+    if (p->lc < nlev) {
+        const cudaError_t e = p->dtype == VD_F64
+            ? cudaFuncSetAttribute(vd::k_mg_coarse<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024)
+            : cudaFuncSetAttribute(vd::k_mg_coarse<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        if (e != cudaSuccess) {
+            if (p->dev) cudaFree(p->dev);
+            delete p;
+            return VD_ERR_CUDA;
+        }
+    }
+    // bottom smoothing of the coarse kernel as matrices (bottom levels of at
+    // most 512 cells: 2 x 512^2 entries a system, built in well under a second)
+    std::vector<double> bsm;
+    if (p->niter_bottom > 0 && p->lc < nlev && (long long)Bt.n0 * Bt.n1 <= 512) {
+        const size_t nbc = (size_t)Bt.n0 * Bt.n1;
+        for (int b = 0; b < p->nsys; ++b)
+            bottom_sweep_matrices(Bt, Bt.factor.data() + b * nbc, p->omega, 6 * p->niter_bottom, nlev == 1, bsm);
+    }
+    const int st = p->dtype == VD_F64 ? mg_upload<double>(p, idx, inv, bsm) : mg_upload<float>(p, idx, inv, bsm);
     if (st != VD_OK) {
         if (p->dev) cudaFree(p->dev);
         delete p;
@@ -579,6 +920,9 @@ extern "C" vd_status vd_mg_plan_create(vd_mg_plan** out, const vd_mg_desc* d)
 extern "C" vd_status vd_mg_plan_destroy(vd_mg_plan* p)
 {
     if (!p) return VD_ERR_ARG;
+    if (p->gexec) cudaGraphExecDestroy(p->gexec);
+    if (p->gstream) cudaStreamDestroy(p->gstream);
+    if (p->gbuf) cudaFree(p->gbuf);
     if (p->dev) cudaFree(p->dev);
     delete p;
     return VD_OK;
@@ -591,16 +935,65 @@ extern "C" size_t vd_mg_workspace_bytes(const vd_mg_plan* p)
     return p ? p->ws_elems * (p->dtype == VD_F64 ? 8 : 4) : 0;
 }
 
+static int mg_run(const vd_mg_plan* p, const void* rhs, void* f, void* ws, cudaStream_t st)
+{
+    if (p->dtype == VD_F64) {
+        MgRun<double> r{p, (double*)ws, st};
+        return r.solve((const double*)rhs, (double*)f);
+    }
+    MgRun<float> r{p, (float*)ws, st};
+    return r.solve((const float*)rhs, (float*)f);
+}
+
+// (Re)capture the solve on the plan's buffers with workspace ws.
+static int mg_capture(vd_mg_plan* p, void* ws)
+{
+    const size_t bytes = (size_t)p->nsys * p->n0 * p->n1 * (p->dtype == VD_F64 ? 8 : 4);
+    if (!p->gbuf) VD_CUDA_TRY(cudaMalloc(&p->gbuf, 2 * bytes));
+    if (!p->gstream) VD_CUDA_TRY(cudaStreamCreateWithFlags(&p->gstream, cudaStreamNonBlocking));
+    if (p->gexec) {
+        cudaGraphExecDestroy(p->gexec);
+        p->gexec = nullptr;
+    }
+    char* g = (char*)p->gbuf;
+    VD_CUDA_TRY(cudaStreamBeginCapture(p->gstream, cudaStreamCaptureModeRelaxed));
+    const int rc = mg_run(p, g, g + bytes, ws, p->gstream);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(p->gstream, &graph);
+    if (rc != VD_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    VD_CUDA_TRY(ec);
+    const cudaError_t ei = cudaGraphInstantiate(&p->gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    VD_CUDA_TRY(ei);
+    p->gws = ws;
+    return VD_OK;
+}
+
 extern "C" vd_status vd_mg_solve(const vd_mg_plan* p, const void* rhs, void* f, void* ws, size_t wsb, void* stream)
 {
     if (!p || !rhs || !f || !ws) return VD_ERR_ARG;
     if (wsb < vd_mg_workspace_bytes(p)) return VD_ERR_WORKSPACE;
-    if (p->dtype == VD_F64) {
-        MgRun<double> r{p, (double*)ws, (cudaStream_t)stream};
-        return r.solve((const double*)rhs, (double*)f);
+    cudaStream_t st = (cudaStream_t)stream;
+    // a caller that is itself capturing records the launches directly
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    VD_CUDA_TRY(cudaStreamIsCapturing(st, &cs));
+    if (cs != cudaStreamCaptureStatusNone) return mg_run(p, rhs, f, ws, st);
+    // a solve is ~25 kernel launches per level per V-cycle; replaying them as
+    // one graph removes their host launch cost
+    vd_mg_plan* q = const_cast<vd_mg_plan*>(p);
+    if (!q->gexec || q->gws != ws) {
+        const int rc = mg_capture(q, ws);
+        if (rc != VD_OK) return rc;
     }
-    MgRun<float> r{p, (float*)ws, (cudaStream_t)stream};
-    return r.solve((const float*)rhs, (float*)f);
+    const size_t bytes = (size_t)p->nsys * p->n0 * p->n1 * (p->dtype == VD_F64 ? 8 : 4);
+    char* g = (char*)q->gbuf;
+    VD_CUDA_TRY(cudaMemcpyAsync(g, rhs, bytes, cudaMemcpyDeviceToDevice, st));
+    VD_CUDA_TRY(cudaGraphLaunch(q->gexec, st));
+    VD_CUDA_TRY(cudaMemcpyAsync(f, g + bytes, bytes, cudaMemcpyDeviceToDevice, st));
+    return VD_OK;
 }
 
 extern "C" vd_status vd_mg_residual(const vd_mg_plan* p, const void* f, const void* rhs, void* res, void* stream)
