@@ -973,6 +973,23 @@ def gpu_arm_aux(args):
     rows = {}
     nx, ny = S5_NX, S5_NY
     rng = np.random.default_rng(6000)
+    if args.profile_small:
+        # one multigrid solve, then one float64 spectral solve: the launches an
+        # ncu capture of k_mg_coarse / dst_fft_kernel selects (not a bench value)
+        from vardyn_gb300.helmholtz_mg import MG_Helmholtz
+        from vardyn_gb300.helmholtz_dst import HelmholtzDST
+        from vardyn_gb300.sw import SWMasks
+        msw = SWMasks(nx, ny, s5_land(nx, ny))
+        h_tot, dt_sw = float(sum(S5_H)), 12.0
+        mg = MG_Helmholtz(S5_DX, S5_DX, nx, ny, h_tot * msw.u, h_tot * msw.v,
+                          lambd=np.array([1.0 / (9.81 * dt_sw * 2 * dt_sw)]), mask=msw.h, niter_bottom=20,
+                          dtype=torch.float64)
+        mg.solve(torch.as_tensor(rng.standard_normal((1, nx, ny)) * msw.h, device="cuda"))
+        hs = HelmholtzDST(nx, ny, S5_DX, S5_DX, [2e-9, 7e-10, 2.5e-13], dtype=torch.float64)
+        hs.solve(torch.as_tensor(rng.standard_normal((3, nx - 1, ny - 1)), device="cuda"))
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_small": "aux", "note": "one multigrid and one spectral solve; not a bench value"}))
+        return
     # --- masked multigrid: the shallow-water barotropic filter's solve (coefficients
     # H_tot on the ocean faces, lambda = 1 / (g dt tau) with tau = 2 dt, 20 bottom
     # smooths), float64 as the reference

@@ -477,6 +477,9 @@ typedef struct vd_sw_desc {
     const double* sponge_u_host;  /* [nx+1][ny] or NULL */
     const double* sponge_v_host;  /* [nx][ny+1] or NULL */
     const double* sponge_h_host;  /* [nx][ny] or NULL */
+    const double* Hwind_host;     /* h_wind_mode 0: the layer-0 thickness [nx][ny] the wind
+                                     depth is taken from (sw.py:622-630 read the model's
+                                     own H, not a perturbed one); NULL = this plan's H */
 } vd_sw_desc;
 
 /* Host-only: the flag bytes of the staggered masks (masks.py:57-158).
@@ -490,6 +493,21 @@ vd_status vd_sw_masks(int nx, int ny, const double* mask, uint8_t* fh, uint8_t* 
 vd_status vd_sw_plan_create(vd_sw_plan** out, const vd_sw_desc* desc);
 void vd_sw_plan_destroy(vd_sw_plan* plan);
 size_t vd_sw_workspace_bytes(const vd_sw_plan* plan, int batch, int nstep);
+/* Cotangents of H and h_wind (the H / h_wind entries of jax.vjp in
+ * sw.py:924-938 and mod.py:3255-3290). While a zeroed buffer of
+ * vd_sw_ref_adj_bytes is registered with vd_sw_set_ref_adj, every adjoint
+ * call on the plan accumulates into it the cotangents of the tables built
+ * from H and h_wind (reference thickness on h / u / v points, reference
+ * pressure gradients, wind factors), summed over batch, stages and steps;
+ * register NULL to stop. vd_sw_ref_pullback maps the buffer to adH
+ * [nl][nx][ny] (the cotangent of every layer's thickness H, sw.py:386-406)
+ * and, when adhw is not NULL, to the cotangent of a field h_wind [nx][ny]
+ * (zero unless the plan's h_wind is a field, sw.py:608-640). Registration is
+ * plan state: one adjoint at a time per plan. */
+size_t vd_sw_ref_adj_bytes(const vd_sw_plan* plan);
+vd_status vd_sw_set_ref_adj(vd_sw_plan* plan, void* buf);
+vd_status vd_sw_ref_pullback(const vd_sw_plan* plan, const void* buf, void* adH, void* adhw,
+                             void* stream);
 /* nstep RK3-SSP steps. ub/vb/hb (sponge targets) default to the initial
  * state, Fu/Fv/Fh (forcing) to zero, taux [nx-1][ny] / tauy [nx][ny-1] to
  * the plan's wind stress; all are physical, all nullable (in groups of

@@ -244,7 +244,10 @@ class SWOracle:
             else:
                 Hu = Hv = np.maximum(hw, self.h_min)
         else:
-            H0u, H0v = refv[1][0], refv[2][0]
+            # the model's own reference thickness, not the one of a perturbed H
+            # passed to step (sw.py:622-630 read self.h_ref_ugrid / _vgrid)
+            base = self.ref_values(self.H)
+            H0u, H0v = base[1][0], base[2][0]
             if H0u.shape[0] > 1:
                 H0u = H0u[1:-1, :]
             if H0v.shape[1] > 1:

@@ -99,7 +99,7 @@ class VdSwDesc(ctypes.Structure):
         ("h_wind_scalar", ctypes.c_double), ("h_wind_host", _DP),
         ("taux_scalar", ctypes.c_double), ("tauy_scalar", ctypes.c_double),
         ("taux_host", _DP), ("tauy_host", _DP),
-        ("sponge_u_host", _DP), ("sponge_v_host", _DP), ("sponge_h_host", _DP),
+        ("sponge_u_host", _DP), ("sponge_v_host", _DP), ("sponge_h_host", _DP), ("Hwind_host", _DP),
     ]
 
 
@@ -178,6 +178,9 @@ SIGNATURES = {
     "vd_sw_plan_create": (I, [ctypes.POINTER(P), ctypes.POINTER(VdSwDesc)]),
     "vd_sw_plan_destroy": (None, [P]),
     "vd_sw_workspace_bytes": (SZ, [P, I, I]),
+    "vd_sw_ref_adj_bytes": (SZ, [P]),
+    "vd_sw_set_ref_adj": (I, [P, P]),
+    "vd_sw_ref_pullback": (I, [P, P, P, P, P]),
     "vd_sw_step": (I, [P, I, P, P, P, I, P, P, P, P, P, P, P, P, P, P, P, P, SZ, P]),
     "vd_sw_step_tgl": (I, [P, I, P, P, P, P, P, P, I, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P,
                            P, SZ, P]),

@@ -390,6 +390,11 @@ struct Tab {
     const T *idyv2, *idyv, *idxv2;   // on the v grid: 1/dy^2, 1/dy, 1/dx^2
     const T *iarea, *idx2h, *idy2h;  // on the h grid: 1/area, 1/dx^2, 1/dy^2
     const uint8_t *fh, *fu, *fv;  // flag bytes
+    const T *dwu, *dwv;           // d(wind factor)/d(face H_ref) on interior faces, masked
+    // cotangent accumulators of the H / h_wind dependent tables, summed over
+    // batch, stages and steps by the adjoint kernels (null: not accumulated)
+    T *ad_href, *ad_hrefu, *ad_hrefv, *ad_dxp, *ad_dyp, *ad_wfu, *ad_wfv;
+    int wind_mode;                // h_wind: 0 from H (layer 0), 1 scalar, 2 field
     T G[MAXL];                    // G[l] = sum_{k<=l} g'_k
     T gp[MAXL];
     T drag, visc, diff, hmin, sharp, dt;
@@ -747,6 +752,79 @@ __global__ void k_sw_force_mc(Tab<T> t, Tri<R> x, Tri<R> F, Tri<W> out)
     }
 }
 
+// ------------------------------------------------------------------ H / h_wind cotangents
+// Pull the accumulated table cotangents back to H (every layer's thickness,
+// [nl][nx][ny]) and to a field h_wind ([nx][ny]), transposing the plan's
+// table construction (sw.py:386-406 reference values, 567-640 wind depth):
+//   h_ref = H area; h_ref on u / v faces = edge-padded averages;
+//   eta_l = -sum_{m<l} H_m, p_l = sum_{k<=l} g'_k eta_k, dxp / dyp = diffs of p;
+//   wind factor = dx / (rho max(H_face, h_min)), H_face from h_wind (average
+//   of the two cells); without h_wind it comes from the model's own H, which
+//   the H argument does not reach (sw.py:622-630), so it adds nothing to adH.
+template <typename T>
+__global__ void k_sw_ref_pullback(Tab<T> t, const T* a_href, const T* a_hrefu, const T* a_hrefv, const T* a_dxp,
+                                  const T* a_dyp, const T* a_wfu, const T* a_wfv, T* adH, T* adhw)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    const int nx = t.nx, ny = t.ny, nl = t.nl;
+    if (i >= nx || j >= ny) return;
+    const long long hi = (long long)i * ny + j;
+    auto Au = [&](int l, int f) { return a_hrefu[(long long)l * t.su + (long long)f * ny + j]; };
+    auto Av = [&](int l, int c) { return a_hrefv[(long long)l * t.sv + (long long)i * (ny + 1) + c]; };
+    T aH[MAXL];
+    for (int l = 0; l < nl; ++l) {
+        T a = a_href[(long long)l * t.sh + hi];
+        a += T(0.5) * (Au(l, i) + Au(l, i + 1));
+        if (i == 0) a += T(0.5) * Au(l, 0);
+        if (i == nx - 1) a += T(0.5) * Au(l, nx);
+        a += T(0.5) * (Av(l, j) + Av(l, j + 1));
+        if (j == 0) a += T(0.5) * Av(l, 0);
+        if (j == ny - 1) a += T(0.5) * Av(l, ny);
+        aH[l] = a * t.area[hi];
+    }
+    if (t.hxy_dxp) {
+        T ap[MAXL], aeta[MAXL];
+        for (int l = 0; l < nl; ++l) {
+            const long long bx = (long long)l * (nx - 1) * ny, by = (long long)l * nx * (ny - 1);
+            T a = T(0);
+            if (i >= 1) a += a_dxp[bx + (long long)(i - 1) * ny + j];
+            if (i <= nx - 2) a -= a_dxp[bx + (long long)i * ny + j];
+            if (j >= 1) a += a_dyp[by + (long long)i * (ny - 1) + j - 1];
+            if (j <= ny - 2) a -= a_dyp[by + (long long)i * (ny - 1) + j];
+            ap[l] = a;
+        }
+        T suf = T(0);
+        for (int l = nl - 1; l >= 0; --l) {
+            suf += ap[l];
+            aeta[l] = t.gp[l] * suf;
+        }
+        T above = T(0);
+        for (int m = nl - 1; m >= 0; --m) {
+            aH[m] -= above;
+            above += aeta[m];
+        }
+    }
+    for (int l = 0; l < nl; ++l) adH[(long long)l * t.sh + hi] = aH[l];
+    if (adhw) {
+        T a = T(0);
+        if (t.wind_mode == 2) {
+            auto Gu = [&](int f) -> T {
+                if (f < 1 || f > nx - 1) return T(0);
+                const long long k = (long long)f * ny + j;
+                return a_wfu[k] * t.dwu[k];
+            };
+            auto Gv = [&](int c) -> T {
+                if (c < 1 || c > ny - 1) return T(0);
+                const long long k = (long long)i * (ny + 1) + c;
+                return a_wfv[k] * t.dwv[k];
+            };
+            a = T(0.5) * (Gu(i) + Gu(i + 1) + Gv(j) + Gv(j + 1));
+        }
+        adhw[hi] = a;
+    }
+}
+
 // ------------------------------------------------------------------ conversions
 // set_input_uvh (sw.py:432-450) and get_physical_uvh (421-427); the adjoint
 // of either is the same diagonal scaling.
@@ -830,7 +908,7 @@ template <typename T> __device__ __forceinline__ void aadd(T* p, T v) { atomicAd
 template <typename T>
 __global__ void k_sw_tend_adj(Tab<T> t, const T* u, const T* v, const T* h, const T* om, const T* ht,
                               const T* adk_u, const T* adk_v, const T* adk_h, T* adom, T* adkp, T* adht, T* adu,
-                              T* adv, T* adh)
+                              T* adv, T* adh, const T* taux, const T* tauy)
 {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = blockIdx.y * blockDim.y + threadIdx.y;
@@ -877,6 +955,9 @@ __global__ void k_sw_tend_adj(Tab<T> t, const T* u, const T* v, const T* h, cons
             addV(i - 1, j);
             aadd(&adkp[ob * t.sh + ui], -a);
             aadd(&adkp[ob * t.sh + ui - ny], a);
+            // reference pressure gradient and wind factor (H / h_wind cotangents)
+            if (t.ad_dxp && t.hxy_dxp) aadd(&t.ad_dxp[(long long)l * (nx - 1) * ny + (long long)(i - 1) * ny + j], -a);
+            if (t.ad_wfu && l == 0) aadd(&t.ad_wfu[ui], a * (taux ? taux : t.taux)[(long long)(i - 1) * ny + j]);
             const long long ub = ob * t.su;
             if (l == nl - 1) aadd(&adu[ub + ui], -t.drag * a);
             if (t.visc > T(0)) {
@@ -954,6 +1035,8 @@ __global__ void k_sw_tend_adj(Tab<T> t, const T* u, const T* v, const T* h, cons
             const long long hi = (long long)i * ny + j;
             aadd(&adkp[ob * t.sh + hi], -a);
             aadd(&adkp[ob * t.sh + hi - 1], a);
+            if (t.ad_dyp && t.hxy_dyp) aadd(&t.ad_dyp[(long long)l * nx * (ny - 1) + (long long)i * (ny - 1) + j - 1], -a);
+            if (t.ad_wfv && l == 0) aadd(&t.ad_wfv[vi], a * (tauy ? tauy : t.tauy)[(long long)i * (ny - 1) + j - 1]);
             const long long vb = ob * t.sv;
             if (l == nl - 1) aadd(&adv[vb + vi], -t.drag * a);
             if (t.visc > T(0)) {
@@ -1062,11 +1145,14 @@ __global__ void k_sw_diag_adj(Tab<T> t, const T* u, const T* v, const T* h, cons
             T a = T(0);
             for (int l = 0; l < nl; ++l) a += ap[l] * t.G[l < m ? l : m];
             a = a * t.iarea[hi];
+            T aref = adht[o];   // d h_tot / d h_ref (linear: h_tot = h_ref)
             if (!t.linear) {
                 const T z = (t.href[(long long)m * t.sh + hi] + h[o] - t.hmin * ar) * t.sharp;
-                a += adht[o] * sigmoid_v(z);
+                aref = adht[o] * sigmoid_v(z);
+                a += aref;
             }
             adh[o] += a;
+            if (t.ad_href) aadd(&t.ad_href[(long long)m * t.sh + hi], aref);
         }
     }
 }
@@ -1122,6 +1208,7 @@ __global__ void k_sw_force_mc_adj(Tab<T> t, const T* u, const T* v, const T* h, 
         adu[idx] = a * (T(1) - dt * fu / htu);
         const T aht = a * dt * uu * fu / (htu * htu) * sigmoid_v(zz);
         const T afu = -a * dt * uu / htu;
+        if (t.ad_hrefu) aadd(&t.ad_hrefu[(long long)l * t.su + ui], aht);
         rep_pad_adj(t, adh_acc, hb, i + 1, j + 1, T(0.5) * aht);
         rep_pad_adj(t, adh_acc, hb, i, j + 1, T(0.5) * aht);
         if (adFh) {
@@ -1141,6 +1228,7 @@ __global__ void k_sw_force_mc_adj(Tab<T> t, const T* u, const T* v, const T* h, 
         adv[idx] = a * (T(1) - dt * fv / htv);
         const T aht = a * dt * vv * fv / (htv * htv) * sigmoid_v(zz);
         const T afv = -a * dt * vv / htv;
+        if (t.ad_hrefv) aadd(&t.ad_hrefv[(long long)l * t.sv + vi], aht);
         rep_pad_adj(t, adh_acc, hb, i + 1, j + 1, T(0.5) * aht);
         rep_pad_adj(t, adh_acc, hb, i + 1, j, T(0.5) * aht);
         if (adFh) {
@@ -1302,6 +1390,8 @@ static void fill_tab(Tab<T>& t, vd_sw_plan* p, const std::vector<size_t>& off)
     t.gu = P(); t.gv = P(); t.gh = P();
     t.idxu2 = P(); t.idxu = P(); t.idyu2 = P(); t.idyv2 = P(); t.idyv = P(); t.idxv2 = P();
     t.iarea = P(); t.idx2h = P(); t.idy2h = P();
+    t.dwu = P(); t.dwv = P();
+    t.ad_href = t.ad_hrefu = t.ad_hrefv = t.ad_dxp = t.ad_dyp = t.ad_wfu = t.ad_wfv = nullptr;
     t.fh = (const uint8_t*)(base + off[k++]);
     t.fu = (const uint8_t*)(base + off[k++]);
     t.fv = (const uint8_t*)(base + off[k++]);
@@ -1413,8 +1503,17 @@ extern "C" vd_status vd_sw_plan_create(vd_sw_plan** out, const vd_sw_desc* d)
                         pref[(size_t)l * sh + (size_t)i * ny + j + 1] - pref[(size_t)l * sh + (size_t)i * ny + j];
         }
     }
-    // wind factors (sw.py:570-669): dx_u / (rho H_ref_u) on interior u faces, masked
+    // wind factors (sw.py:570-669): dx_u / (rho H_ref_u) on interior u faces, masked;
+    // without h_wind the depth is the layer-0 reference thickness of the
+    // model's own H (Hwind_host when given)
     const double rho = d->rho_water > 0 ? d->rho_water : 1025.0, hmin = d->h_min;
+    std::vector<double> hwu(hrefu.begin(), hrefu.begin() + su), hwv(hrefv.begin(), hrefv.begin() + sv);
+    if (d->h_wind_mode == 0 && d->Hwind_host) {
+        std::vector<double> hr(sh);
+        for (size_t k = 0; k < sh; ++k) hr[k] = d->Hwind_host[k] * area[k];
+        edge_avg0(hr, nx, ny, hwu);
+        edge_avg1(hr, nx, ny, hwv);
+    }
     std::vector<double> wfu(su, 0.0), wfv(sv, 0.0);
     for (int i = 1; i < nx; ++i)
         for (int j = 0; j < ny; ++j) {
@@ -1423,7 +1522,7 @@ extern "C" vd_status vd_sw_plan_create(vd_sw_plan** out, const vd_sw_desc* d)
             double Hu;
             if (d->h_wind_mode == 1) Hu = d->h_wind_scalar;
             else if (d->h_wind_mode == 2) Hu = 0.5 * (d->h_wind_host[(size_t)(i - 1) * ny + j] + d->h_wind_host[(size_t)i * ny + j]);
-            else Hu = hrefu[k] / areau[k];
+            else Hu = hwu[k] / areau[k];
             Hu = Hu > hmin ? Hu : hmin;
             wfu[k] = dxu[k] / (rho * Hu);
         }
@@ -1434,9 +1533,35 @@ extern "C" vd_status vd_sw_plan_create(vd_sw_plan** out, const vd_sw_desc* d)
             double Hv;
             if (d->h_wind_mode == 1) Hv = d->h_wind_scalar;
             else if (d->h_wind_mode == 2) Hv = 0.5 * (d->h_wind_host[(size_t)i * ny + j - 1] + d->h_wind_host[(size_t)i * ny + j]);
-            else Hv = hrefv[k] / areav[k];
+            else Hv = hwv[k] / areav[k];
             Hv = Hv > hmin ? Hv : hmin;
             wfv[k] = dyv[k] / (rho * Hv);
+        }
+    // d(wind factor)/d(face H_ref) with jnp.maximum's rule (1 above h_min,
+    // 1/2 at a tie, 0 below), for the cotangents of H and h_wind
+    std::vector<double> dwu(su, 0.0), dwv(sv, 0.0);
+    auto dclamp = [&](double x) { return x > hmin ? 1.0 : (x == hmin ? 0.5 : 0.0); };
+    for (int i = 1; i < nx; ++i)
+        for (int j = 0; j < ny; ++j) {
+            const size_t k = (size_t)i * ny + j;
+            if (!(M.fu[k] & 1)) continue;
+            double Hu;
+            if (d->h_wind_mode == 1) Hu = d->h_wind_scalar;
+            else if (d->h_wind_mode == 2) Hu = 0.5 * (d->h_wind_host[(size_t)(i - 1) * ny + j] + d->h_wind_host[(size_t)i * ny + j]);
+            else Hu = hwu[k] / areau[k];
+            const double Hc = Hu > hmin ? Hu : hmin;
+            dwu[k] = -dxu[k] / (rho * Hc * Hc) * dclamp(Hu);
+        }
+    for (int i = 0; i < nx; ++i)
+        for (int j = 1; j < ny; ++j) {
+            const size_t k = (size_t)i * (ny + 1) + j;
+            if (!(M.fv[k] & 1)) continue;
+            double Hv;
+            if (d->h_wind_mode == 1) Hv = d->h_wind_scalar;
+            else if (d->h_wind_mode == 2) Hv = 0.5 * (d->h_wind_host[(size_t)i * ny + j - 1] + d->h_wind_host[(size_t)i * ny + j]);
+            else Hv = hwv[k] / areav[k];
+            const double Hc = Hv > hmin ? Hv : hmin;
+            dwv[k] = -dyv[k] / (rho * Hc * Hc) * dclamp(Hv);
         }
     // default wind stress
     std::vector<double> taux((size_t)(nx - 1) * ny), tauy((size_t)nx * (ny - 1));
@@ -1466,7 +1591,7 @@ extern "C" vd_status vd_sw_plan_create(vd_sw_plan** out, const vd_sw_desc* d)
                                                    &fsu, &fsv, &wa, &wb, &wfu, &wfv, &href, &hrefu, &hrefv,
                                                    &dxp, &dyp, &taux, &tauy, &gu, &gv, &gh,
                                                    &idxu2, &idxu, &idyu2, &idyv2, &idyv, &idxv2,
-                                                   &iarea, &idx2h, &idy2h};
+                                                   &iarea, &idx2h, &idy2h, &dwu, &dwv};
     std::vector<size_t> off;
     size_t tot = 0;
     for (auto* a : arrs) {
@@ -1494,6 +1619,7 @@ extern "C" vd_status vd_sw_plan_create(vd_sw_plan** out, const vd_sw_desc* d)
     p->d.mask_host = nullptr; p->d.dx_host = p->d.dy_host = p->d.f_host = p->d.H_host = p->d.g_prime_host = nullptr;
     p->d.h_wind_host = p->d.taux_host = p->d.tauy_host = nullptr;
     p->d.sponge_u_host = p->d.sponge_v_host = p->d.sponge_h_host = nullptr;
+    p->d.Hwind_host = nullptr;
     p->nx = nx; p->ny = ny; p->nl = nl; p->esz = esz;
     if (cudaMalloc(&p->dev, tot) != cudaSuccess) {
         delete p;
@@ -1520,12 +1646,69 @@ extern "C" vd_status vd_sw_plan_create(vd_sw_plan** out, const vd_sw_desc* d)
         t.diff = (TT)(d->diff_coef > 0 ? d->diff_coef : 0); t.hmin = (TT)hmin;
         t.sharp = (TT)(d->h_min_sharpness > 0 ? d->h_min_sharpness : 10.0); t.dt = (TT)d->dt;
         t.linear = d->flag_linear ? 1 : 0; t.has_sponge = has_sponge; t.hxy_dxp = Hs; t.hxy_dyp = Hs;
+        t.wind_mode = d->h_wind_mode;
         fill_tab(t, p, off);
         if (!Hs) { t.dxp = nullptr; t.dyp = nullptr; }
     };
     if (esz == 8) common(p->td);
     else common(p->tf);
     *out = p;
+    return VD_OK;
+}
+
+// Cotangent accumulators of the H / h_wind dependent tables: one buffer of
+// nl*(sh + su + sv) + nl*((nx-1)*ny + nx*(ny-1)) + su + sv elements.
+static size_t ref_adj_elems(const vd_sw_plan* p)
+{
+    const size_t nx = p->nx, ny = p->ny, nl = p->nl;
+    const size_t sh = nx * ny, su = (nx + 1) * ny, sv = nx * (ny + 1);
+    return nl * (sh + su + sv) + nl * ((nx - 1) * ny + nx * (ny - 1)) + su + sv;
+}
+
+template <typename T>
+static void set_ref_adj(vd_sw_plan* p, Tab<T>& t, void* buf)
+{
+    if (!buf) {
+        t.ad_href = t.ad_hrefu = t.ad_hrefv = t.ad_dxp = t.ad_dyp = t.ad_wfu = t.ad_wfv = nullptr;
+        return;
+    }
+    const long long nx = p->nx, ny = p->ny, nl = p->nl;
+    T* b = (T*)buf;
+    t.ad_href = b; b += nl * t.sh;
+    t.ad_hrefu = b; b += nl * t.su;
+    t.ad_hrefv = b; b += nl * t.sv;
+    t.ad_dxp = b; b += nl * (nx - 1) * ny;
+    t.ad_dyp = b; b += nl * nx * (ny - 1);
+    t.ad_wfu = b; b += t.su;
+    t.ad_wfv = b;
+}
+
+extern "C" size_t vd_sw_ref_adj_bytes(const vd_sw_plan* p) { return p ? ref_adj_elems(p) * p->esz : 0; }
+
+extern "C" vd_status vd_sw_set_ref_adj(vd_sw_plan* p, void* buf)
+{
+    if (!p) return VD_ERR_ARG;
+    if (p->esz == 8) set_ref_adj(p, p->td, buf);
+    else set_ref_adj(p, p->tf, buf);
+    return VD_OK;
+}
+
+extern "C" vd_status vd_sw_ref_pullback(const vd_sw_plan* p, const void* buf, void* adH, void* adhw, void* stream)
+{
+    if (!p || !buf || !adH) return VD_ERR_ARG;
+    const dim3 block(32, 8), grid((unsigned)((p->ny + 31) / 32), (unsigned)((p->nx + 7) / 8));
+    cudaStream_t st = (cudaStream_t)stream;
+    auto go = [&](auto tab) {
+        using T = std::remove_reference_t<decltype(*tab.area)>;
+        using TT = std::remove_const_t<T>;
+        Tab<TT> t = tab;
+        set_ref_adj(const_cast<vd_sw_plan*>(p), t, const_cast<void*>(buf));
+        k_sw_ref_pullback<TT><<<grid, block, 0, st>>>(t, t.ad_href, t.ad_hrefu, t.ad_hrefv, t.ad_dxp, t.ad_dyp,
+                                                      t.ad_wfu, t.ad_wfv, (TT*)adH, (TT*)adhw);
+    };
+    if (p->esz == 8) go(p->td);
+    else go(p->tf);
+    VD_LAUNCH_CHECK();
     return VD_OK;
 }
 
@@ -1830,7 +2013,7 @@ static int sw_tgl_t(vd_sw_plan* p, int B, const void* u0, const void* v0, const 
 // adjoint of one right-hand side at state x (model space): adk -> adx (+=)
 template <typename T>
 static int rhs_adj(vd_sw_plan* p, int B, Fields<T> x, Fields<T> adk, Fields<T> adx, Work<T>& wk, T* adom, T* adkp,
-                   T* adht, cudaStream_t st)
+                   T* adht, const T* taux, const T* tauy, cudaStream_t st)
 {
     Tab<T>& t = tab<T>(p);
     const Sizes s = sizes(p);
@@ -1841,7 +2024,7 @@ static int rhs_adj(vd_sw_plan* p, int B, Fields<T> x, Fields<T> adk, Fields<T> a
     VD_CUDA_TRY(cudaMemsetAsync(adkp, 0, sizeof(T) * s.sh * B, st));
     VD_CUDA_TRY(cudaMemsetAsync(adht, 0, sizeof(T) * s.sh * B, st));
     k_sw_tend_adj<T><<<Ll.grid, Ll.block, 0, st>>>(t, x.u, x.v, x.h, wk.om, wk.ht, adk.u, adk.v, adk.h, adom, adkp,
-                                                    adht, adx.u, adx.v, adx.h);
+                                                    adht, adx.u, adx.v, adx.h, taux, tauy);
     VD_LAUNCH_CHECK();
     k_sw_diag_adj<T><<<Ld.grid, Ld.block, 0, st>>>(t, x.u, x.v, x.h, adom, adkp, adht, adx.u, adx.v, adx.h);
     VD_LAUNCH_CHECK();
@@ -1938,7 +2121,9 @@ static int sw_adj_t(vd_sw_plan* p, int B, const void* u0, const void* v0, const 
             k_sw_update_adj<T><<<Ll.grid, Ll.block, 0, st>>>(t, stg, B * p->nl, ad.u, ad.v, ad.h, adk.u, adk.v, adk.h,
                                                              a0.u, a0.v, a0.h, a1.u, a1.v, a1.h, adb.u, adb.v, adb.h);
             VD_LAUNCH_CHECK();
-            if ((rc = rhs_adj<T>(p, B, stages[stg], adk, ad, wk, adom, adkp, adht, st))) return rc;
+            if ((rc = rhs_adj<T>(p, B, stages[stg], adk, ad, wk, adom, adkp, adht, (const T*)taux, (const T*)tauy,
+                                 st)))
+                return rc;
         }
     }
     // boundary fields that default to the initial state feed its adjoint
@@ -2099,7 +2284,7 @@ static int sw_rhs_adj_t(vd_sw_plan* p, int B, const void* u, const void* v, cons
     T* adht = (T*)ws.take(sizeof(T) * s.sh * B);
     if (!adom || !adkp || !adht) return VD_ERR_WORKSPACE;
     Fields<T> x{(T*)u, (T*)v, (T*)h}, ak{(T*)aku, (T*)akv, (T*)akh}, ad{(T*)adu, (T*)adv, (T*)adh};
-    return rhs_adj<T>(p, B, x, ak, ad, wk, adom, adkp, adht, st);
+    return rhs_adj<T>(p, B, x, ak, ad, wk, adom, adkp, adht, nullptr, nullptr, st);
 }
 
 // elementwise stage combination: k = rhs + sponge; stage 0/1 store k

@@ -150,9 +150,12 @@ class Model_qgsw:
         self.model.sponge_h = self.sponge_h.T
         self.max_nstep = getattr(MOD, "max_nstep", 240)
         self.name_params = list(getattr(MOD, "name_params", None) or [])
-        for p in ("H", "h_wind"):
-            if p in self.name_params:
-                raise NotImplementedError(f"{p} as a control parameter")
+        # bathymetry / layer-thickness and mixed-layer-depth controls start at
+        # zero perturbation (mod.py:2829-2842; a file's H is passed as an array)
+        if "H" in self.name_params and "H" not in State.params:
+            State.params["H"] = np.zeros((ny, nx))
+        if "h_wind" in self.name_params:
+            State.params["h_wind"] = np.zeros((ny, nx))
         if "bc" in self.name_params:
             State.params["u_b"] = np.zeros((ny, nx + 1))
             State.params["v_b"] = np.zeros((ny + 1, nx))
@@ -281,8 +284,17 @@ class Model_qgsw:
             done += n
         return out
 
-    def _plan(self):
-        return self.model._base
+    def _ref_params(self, S):
+        """The H (1, nx, ny) and h_wind (nx, ny) perturbations of State S
+        (mod.py:3311-3320), or None."""
+        H = np.asarray(_np(S.params["H"]), dtype=np.float64).T[None] if "H" in self.name_params else None
+        hw = np.asarray(_np(S.params["h_wind"]), dtype=np.float64).T if "h_wind" in self.name_params else None
+        return H, hw
+
+    def _plan(self, S=None):
+        if S is None:
+            return self.model._base
+        return self.model._plan(*self._ref_params(S))
 
     def _mdt(self, x, sign):
         if self.mdt is None:
@@ -308,7 +320,7 @@ class Model_qgsw:
 
     # ---------------- model ----------------
     def _fwd(self, x, S, t_chunk, n_chunk, F):
-        pl = self._plan()
+        pl = self._plan(S)
         ub, vb, hb = self._bc(S, t_chunk, n_chunk)
         tx, ty = self._wind(t_chunk)
         x = self._mdt(x, +1)
@@ -325,7 +337,10 @@ class Model_qgsw:
 
     def step_tgl(self, dState, State, nstep=1, t=0):
         """mod.py:3348-3453 (tangent of state, forcing and bc parameters)."""
-        pl = self._plan()
+        for k in ("H", "h_wind"):
+            if k in self.name_params and np.any(np.asarray(_np(dState.params.get(k, 0.0))) != 0):
+                raise NotImplementedError(f"tangent with respect to {k}")
+        pl = self._plan(State)
         x = self._state_in(State)
         dx = self._state_in(dState)
         F, dF = self._forcing(State), self._forcing(dState)
@@ -355,8 +370,11 @@ class Model_qgsw:
 
     def step_adj(self, adState, State, nstep=1, t=0):
         """mod.py:3455-3617: overwrites the state adjoint, accumulates the
-        forcing (and bc) parameter adjoints."""
-        pl = self._plan()
+        forcing (and bc, H, h_wind) parameter adjoints."""
+        pl = self._plan(State)
+        want_ref = "H" in self.name_params or "h_wind" in self.name_params
+        adref = {k: np.array(_np(adState.params.get(k, np.zeros((self.ny, self.nx)))), dtype=np.float64)
+                 for k in ("H", "h_wind") if k in self.name_params}
         ny, nx, nl = self.ny, self.nx, self.nl
         if nl > 1:
             ahs = _np(adState.getvar(name_var=self.name_var["SSH"]))
@@ -386,7 +404,12 @@ class Model_qgsw:
             tx, ty = self._wind(t_chunk)
             xm = self._mdt(states[i], +1)
             a = pl.step_adj(*xm, *ad, nstep=n_chunk, ub=ub, vb=vb, hb=hb, Fu=F[0], Fv=F[1], Fh=F[2], taux=tx,
-                            tauy=ty, want_bc=True, want_forcing=True)
+                            tauy=ty, want_bc=True, want_forcing=True, **({"want_ref": True} if want_ref else {}))
+            # H enters every layer as the same (1, nx, ny) perturbation
+            if "H" in adref:
+                adref["H"] += a["H"].sum(0).cpu().numpy().T
+            if "h_wind" in adref:
+                adref["h_wind"] += a["h_wind"].cpu().numpy().T
             ad = (a["u0"], a["v0"], a["h0"])
             for k, key in enumerate(("Fu", "Fv", "Fh")):
                 adF[k] += a[key][0, 0].cpu().numpy().T / (3600 * 24)
@@ -409,3 +432,5 @@ class Model_qgsw:
             adState.params["u_b"], adState.params["v_b"], adState.params["h_b"] = adb
         for k, key in enumerate(("U", "V", "SSH")):
             adState.params[self.name_var[key]] = adF[k]
+        for k, val in adref.items():
+            adState.params[k] = val

@@ -21,9 +21,11 @@ from vardyn_gb300.qg_ml import QGPlan
 class QG(SW):
     """QG(param) of qg.py:22-43."""
 
-    def _make_plan(self, H):
+    def _make_plan(self, H, h_wind=None):
         if H is not None:
             raise NotImplementedError("QG needs H constant in space; a per-call H perturbation is not supported")
+        if h_wind is not None:
+            raise NotImplementedError("h_wind: the QG wind forcing divides by the top layer's H (qg.py:190-193)")
         p = self.param
         kw = self._plan_kwargs()
         kw.pop("rho_water")
@@ -58,6 +60,7 @@ class QG(SW):
         """qg.py:335-345: projected shallow-water tendencies."""
         if ref_vals is not None:
             raise NotImplementedError("ref_vals")
-        self._check_h_wind(h_wind)
+        if h_wind is not None:
+            raise NotImplementedError("h_wind: the QG wind forcing divides by the top layer's H (qg.py:190-193)")
         r = self._base.rhs(self._in(u), self._in(v), self._in(h), *self._tau(taux, tauy))
         return tuple(self._out(u, a) for a in r)

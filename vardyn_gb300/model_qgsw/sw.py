@@ -10,10 +10,14 @@ construction, as mod.py:2803-2806 does). Arrays may be NumPy (returned as
 NumPy) or CUDA torch tensors (returned as tensors) of shape
 ``(n_ens, nl, x, y)``.
 
+``step`` / ``step_adj`` take the reference's ``H`` (a perturbation added to
+every layer's thickness) and ``h_wind`` (added to the model's mixed-layer
+depth); ``step_adj`` returns their cotangents, summed to the shapes they were
+given in.
+
 Not supported (they raise): the barotropic filter (``SW`` only; its
 multigrid coefficients change every call, sw.py:335-356), open boundary
-conditions, the tangent linear and adjoint with respect to ``H`` and
-``h_wind``.
+conditions, the tangent linear with respect to ``H`` and ``h_wind``.
 """
 import numpy as np
 import torch
@@ -89,22 +93,44 @@ class SW:
                     sponge_u=self._sponge["u"], sponge_v=self._sponge["v"], sponge_h=self._sponge["h"],
                     dtype=self.dtype)
 
-    def _make_plan(self, H):
+    def _make_plan(self, H, h_wind=None):
         p = self.param
+        kw = self._plan_kwargs()
+        if H is not None:
+            # the wind depth stays the model's own (sw.py:622-630)
+            kw["H_wind"] = self.H
+        if h_wind is not None:
+            base = kw["h_wind"]
+            kw["h_wind"] = np.asarray(h_wind, dtype=np.float64) + (0.0 if base is None else np.asarray(base))
         Ht = self.H if H is None else self.H + np.asarray(H, dtype=np.float64)
-        return self._plan_cls(self.nx, self.ny, self.nl, p["dx"], p["dy"], p["f"], Ht, p["g_prime"], p["dt"],
-                              **self._plan_kwargs())
+        return self._plan_cls(self.nx, self.ny, self.nl, p["dx"], p["dy"], p["f"], Ht, p["g_prime"], p["dt"], **kw)
 
-    def _plan(self, H=None):
-        if H is None:
+    def _plan(self, H=None, h_wind=None):
+        if H is None and h_wind is None:
             return self._base
-        key = np.asarray(H, dtype=np.float64).tobytes()
+        key = tuple(None if a is None else (np.shape(a), np.asarray(a, dtype=np.float64).tobytes())
+                    for a in (H, h_wind))
         pl = self._plans.get(key)
         if pl is None:
             if len(self._plans) > 4:
                 self._plans.clear()
-            pl = self._plans[key] = self._make_plan(H)
+            pl = self._plans[key] = self._make_plan(H, h_wind)
         return pl
+
+    @staticmethod
+    def _host(a):
+        return None if a is None else (a.detach().cpu().numpy() if torch.is_tensor(a) else np.asarray(a))
+
+    @staticmethod
+    def _sum_to(a, shape):
+        """Sum a [nl, nx, ny] cotangent down to the broadcast shape of its input."""
+        shape = tuple(shape)
+        while a.dim() > len(shape):
+            a = a.sum(0)
+        for d in range(a.dim()):
+            if shape[d] == 1 and a.shape[d] != 1:
+                a = a.sum(d, keepdim=True)
+        return a.reshape(shape)
 
     def _rebuild(self):
         self._plans.clear()
@@ -145,9 +171,6 @@ class SW:
     def _tau(self, taux, tauy):
         return self._in(taux) if taux is not None else None, self._in(tauy) if tauy is not None else None
 
-    def _check_h_wind(self, h_wind):
-        if h_wind is not None:
-            raise NotImplementedError("h_wind passed per call (differentiable mixed-layer depth)")
 
     # ---------------- API ----------------
     def set_input_uvh(self, u_phys, v_phys, h_phys):
@@ -175,16 +198,14 @@ class SW:
         are not supported (pass H to :meth:`step` instead)."""
         if ref_vals is not None:
             raise NotImplementedError("ref_vals: pass the H perturbation to step()")
-        self._check_h_wind(h_wind)
-        pl = self._base
+        pl = self._plan(None, self._host(h_wind))
         r = pl.rhs(self._in(u), self._in(v), self._in(h), *self._tau(taux, tauy))
         return tuple(self._out(u, a) for a in r)
 
     def step(self, u0, v0, h0, H=None, nstep=1, u_b=None, v_b=None, h_b=None, Fu=None, Fv=None, Fh=None, taux=None,
              tauy=None, h_wind=None):
         """sw.py:752-904."""
-        self._check_h_wind(h_wind)
-        pl = self._plan(H)
+        pl = self._plan(self._host(H), self._host(h_wind))
         if (u_b is None) != (v_b is None) or (u_b is None) != (h_b is None):
             # a missing boundary field defaults to the initial state (sw.py:787-791)
             u_b = u0 if u_b is None else u_b
@@ -200,25 +221,25 @@ class SW:
         """jax.jvp of step in (u0, v0, h0) (sw.py:906-922)."""
         if dH is not None or dh_wind is not None:
             raise NotImplementedError("tangent with respect to H or h_wind")
-        self._check_h_wind(h_wind)
-        pl = self._plan(H)
+        pl = self._plan(self._host(H), self._host(h_wind))
         tx, ty = self._tau(taux, tauy)
         r = pl.step_tgl(self._in(u0), self._in(v0), self._in(h0), self._in(du0), self._in(dv0), self._in(dh0),
                         nstep=nstep, taux=tx, tauy=ty)
         return tuple(self._out(du0, a) for a in r)
 
     def step_adj(self, u0, v0, h0, wuT, wvT, whT, H=None, nstep=1, taux=None, tauy=None, h_wind=None):
-        """jax.vjp of step (sw.py:924-938): ((adu0, adv0, adh0, adH, adh_wind),)
-        with adH and adh_wind None (no cotangent for absent inputs; the adjoint
-        with respect to a given H or h_wind is not supported)."""
-        if H is not None:
-            raise NotImplementedError("adjoint with respect to H")
-        self._check_h_wind(h_wind)
-        pl = self._plan(None)
+        """jax.vjp of step (sw.py:924-938): ((adu0, adv0, adh0, adH, adh_wind),),
+        adH / adh_wind None when H / h_wind is None (no cotangent for an
+        absent input), else summed to the shape they were given in."""
+        Hh, hw = self._host(H), self._host(h_wind)
+        pl = self._plan(Hh, hw)
         tx, ty = self._tau(taux, tauy)
+        want = Hh is not None or hw is not None
         a = pl.step_adj(self._in(u0), self._in(v0), self._in(h0), self._in(wuT), self._in(wvT), self._in(whT),
-                        nstep=nstep, taux=tx, tauy=ty)
-        return ((self._out(wuT, a["u0"]), self._out(wvT, a["v0"]), self._out(whT, a["h0"]), None, None),)
+                        nstep=nstep, taux=tx, tauy=ty, **({"want_ref": True} if want else {}))
+        adH = None if Hh is None else self._out(H, self._sum_to(a["H"], np.shape(Hh)))
+        adhw = None if hw is None else self._out(h_wind, self._sum_to(a["h_wind"], np.shape(hw)))
+        return ((self._out(wuT, a["u0"]), self._out(wvT, a["v0"]), self._out(whT, a["h0"]), adH, adhw),)
 
     def adjoint_test_sw(self, nstep=1, seed=42):
         """<M dx, y> / <dx, M* y> in float64 sums (sw.py:940-1035), with

@@ -67,7 +67,10 @@ class SWPlan:
     def __init__(self, nx, ny, nl, dx, dy, f, H, g_prime, dt, mask=None, slip_coef=1.0, bottom_drag_coef=0.0,
                  rho_water=1025.0, h_min=0.1, h_min_sharpness=10.0, visc_coef=0.0, diff_coef=0.0, sponge_coef=0.0,
                  flag_linear=False, forcing_momentum="direct", h_wind=None, taux=0.0, tauy=0.0, sponge_u=None,
-                 sponge_v=None, sponge_h=None, dtype=torch.float64, device=None):
+                 sponge_v=None, sponge_h=None, dtype=torch.float64, device=None, H_wind=None):
+        """``H_wind`` (without ``h_wind``): the layer thicknesses the wind
+        depth is taken from, when they differ from ``H`` (a model stepped
+        with a perturbed H keeps its own H there, sw.py:622-630)."""
         if not torch.cuda.is_available():
             raise RuntimeError("vardyn_gb300 needs a CUDA device (no CPU path)")
         self.device = torch.device(device if device is not None else "cuda")
@@ -111,6 +114,10 @@ class SWPlan:
         d.forcing_momentum = _FORCING[forcing_momentum]
         if h_wind is None:
             d.h_wind_mode = 0
+            if H_wind is not None:
+                Hw = _f64(H_wind)
+                Hw0 = Hw.reshape(-1)[0] if Hw.size == nl else Hw.reshape((nl,) + Hw.shape[-2:])[0]
+                d.Hwind_host = _dp(k(np.ascontiguousarray(np.broadcast_to(Hw0, (nx, ny)))))
         elif np.ndim(h_wind) == 0:
             d.h_wind_mode, d.h_wind_scalar = 1, float(h_wind)
         else:
@@ -227,9 +234,25 @@ class SWPlan:
         return du1, dv1, dh1
 
     def step_adj(self, u0, v0, h0, adu1, adv1, adh1, nstep=1, ub=None, vb=None, hb=None, Fu=None, Fv=None, Fh=None,
-                 taux=None, tauy=None, want_bc=False, want_forcing=False):
+                 taux=None, tauy=None, want_bc=False, want_forcing=False, want_ref=False):
         """Adjoint of :meth:`step`; returns a dict with ``u0``, ``v0``, ``h0``
-        and, when asked, ``ub``, ``vb``, ``hb`` / ``Fu``, ``Fv``, ``Fh``."""
+        and, when asked, ``ub``, ``vb``, ``hb`` / ``Fu``, ``Fv``, ``Fh`` /
+        ``H`` (the cotangent of every layer's thickness, [nl, nx, ny]) and
+        ``h_wind`` ([nx, ny]; zero unless the plan's h_wind is a field)."""
+        if want_ref:
+            esz = 8 if self.dtype == torch.float64 else 4
+            buf = torch.zeros(self._lib.vd_sw_ref_adj_bytes(self._h) // esz, dtype=self.dtype,
+                              device=self.device)
+            _lib.call("vd_sw_set_ref_adj", self._h, _ptr(buf))
+            try:
+                out = self.step_adj(u0, v0, h0, adu1, adv1, adh1, nstep=nstep, ub=ub, vb=vb, hb=hb, Fu=Fu, Fv=Fv,
+                                    Fh=Fh, taux=taux, tauy=tauy, want_bc=want_bc, want_forcing=want_forcing)
+            finally:
+                _lib.call("vd_sw_set_ref_adj", self._h, None)
+            out["H"] = torch.empty((self.nl, self.nx, self.ny), dtype=self.dtype, device=self.device)
+            out["h_wind"] = torch.empty((self.nx, self.ny), dtype=self.dtype, device=self.device)
+            _lib.call("vd_sw_ref_pullback", self._h, _ptr(buf), _ptr(out["H"]), _ptr(out["h_wind"]), _stream())
+            return out
         B = self._batch(u0)
         u0, v0, h0 = self._uvh(u0, v0, h0, B)
         a1 = self._uvh(adu1, adv1, adh1, B, "ad")
