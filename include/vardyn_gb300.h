@@ -406,7 +406,12 @@ vd_status vd_mg_plan_create(vd_mg_plan** out, const vd_mg_desc* desc);
 vd_status vd_mg_plan_destroy(vd_mg_plan* plan);
 int vd_mg_levels(const vd_mg_plan* plan);
 size_t vd_mg_workspace_bytes(const vd_mg_plan* plan);
-/* f = FMG_Helmholtz(rhs) (helmholtz_multigrid.py:380-419). */
+/* f = FMG_Helmholtz(rhs) (helmholtz_multigrid.py:380-419). The first solve
+ * with a given workspace captures the whole solve as a CUDA graph on
+ * plan-owned rhs / solution buffers; later solves copy rhs in, replay it and
+ * copy f out, so solves on one plan must not run concurrently (one stream at
+ * a time). Called while the caller's stream is capturing, it launches the
+ * kernels directly into the caller's graph. */
 vd_status vd_mg_solve(const vd_mg_plan* plan, const void* rhs, void* f, void* workspace,
                       size_t workspace_bytes, void* stream);
 /* res = rhs - H f on the finest level (helmholtz_multigrid.py:102-114). */
