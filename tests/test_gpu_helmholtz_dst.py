@@ -97,10 +97,12 @@ def test_batched_modes_against_oracle():
     assert rel(out, ref) < 1e-10
 
 
-@pytest.mark.parametrize("nx,ny", [(20, 8), (12, 15), (9, 48), (17, 100), (7, 768), (30, 131)])
+@pytest.mark.parametrize("nx,ny", [(20, 8), (12, 15), (9, 48), (17, 100), (7, 768), (30, 131), (9, 1500),
+                                   (9, 2048)])
 def test_transform_lengths_fp64(nx, ny):
     """float64 solves through the FFT form of the transform (2 ny = 16, 30,
-    96, 200, 1536: radices 4, 2, 3, 5) and the dense form (2 x 131 = 262)."""
+    96, 200, 1536, 3000: radices 4, 2, 3, 5; 4096: one row pair fills 131 KB
+    of shared memory) and the dense form (2 x 131 = 262)."""
     from vardyn_gb300.helmholtz_dst import HelmholtzDST
     rng = np.random.default_rng(nx * ny)
     shift = np.array([0.0, 0.3, 2.0])
