@@ -1053,12 +1053,13 @@ def gpu_arm_aux(args):
     capn = cap.cpu().numpy()
     r2n = r2.cpu().numpy()
     t_cpu = _cpu_s(lambda: OH.solve_helmholtz_dstI_cmm(r2n, helm, capn, bx, by, mk))
+    t_cpu_dst = _cpu_s(lambda: OH.solve_helmholtz_dstI(r2n, helm))
     dst_bytes = 3 * (nx - 1) * (ny - 1) * 8 * 6      # x-DST in/out, tridiagonal in/out, x-DST in/out
     rows["a16_helmholtz_dst"] = {
         "case": f"{nx}x{ny} interior, 3 modes, float64, one island ({bx.size} boundary points)",
         "gpu_ms_per_dst_solve": ms_dst, "gpu_ms_per_cmm_solve": ms_cmm,
         "dst_solve_GBps": dst_bytes / (ms_dst * 1e-3) / 1e9,
-        "cpu_s_per_cmm_solve": t_cpu, "cpu_note": "oracle (scipy.fft.dstn) on the host"}
+        "cpu_s_per_cmm_solve": t_cpu, "cpu_s_per_dst_solve": t_cpu_dst, "cpu_note": "oracle (scipy.fft.dstn) on the host"}
     # --- QG projector (3 layers, one island), float32
     from vardyn_gb300.qg_ml import QGPlan
     yw = np.arange(ny + 1)[None, :] * S5_DX + np.zeros((nx + 1, 1))
