@@ -41,16 +41,18 @@ struct Cross {
 template <typename T>
 struct Vel {
     T u0, u1, v0, v1;
-    __device__ __forceinline__ void load(const QGGeom& G, const T* __restrict__ hc) {
-        const int nx = G.nx;
-        const T hn_w = hc[nx - 1], hn_c = hc[nx], hn_e = hc[nx + 1];
-        const T hs_w = hc[-nx - 1], hs_c = hc[-nx], hs_e = hc[-nx + 1];
-        const T h_w = hc[-1], h_e = hc[1];
+    // from the SSH at rows j-1 (s), j, j+1 (n) and columns i-1 (w), i, i+1 (e)
+    __device__ __forceinline__ void set(const QGGeom& G, T hs_w, T hs_c, T hs_e, T h_w, T h_e, T hn_w, T hn_c,
+                                        T hn_e) {
         const T cu = T(G.cu), cv = T(G.cv);
         u0 = cu * (hn_w + hn_c - hs_c - hs_w);
         u1 = cu * (hn_c + hn_e - hs_e - hs_c);
         v0 = cv * (h_e + hs_e - hs_w - h_w);
         v1 = cv * (hn_e + h_e - h_w - hn_w);
+    }
+    __device__ __forceinline__ void load(const QGGeom& G, const T* __restrict__ hc) {
+        const int nx = G.nx;
+        set(G, hc[-nx - 1], hc[-nx], hc[-nx + 1], hc[-1], hc[1], hc[nx - 1], hc[nx], hc[nx + 1]);
     }
 };
 
@@ -148,36 +150,96 @@ struct StageIn {
     int nk;
 };
 
+// One point's PV tendency, loading its own stencil (M3 points only).
+template <typename T>
+__device__ __forceinline__ T stage_point(const QGGeom& G, const T* __restrict__ hs, const T* __restrict__ qs,
+                                         long long o, long long go)
+{
+    Vel<T> V;
+    V.load(G, hs + o);
+    V.u0 = guard0(V.u0); V.u1 = guard0(V.u1); V.v0 = guard0(V.v0); V.v1 = guard0(V.v1);
+    Cross<T> q;
+    q.load(qs + o, G.nx);
+    Cross<T> qa = q;
+    if (G.fB) { Cross<T> b; b.load((const T*)G.fB + go, G.nx); qa.add(b); }
+    const T beta = G.beta ? ((const T*)G.beta)[go] : T(0);
+    return guard0(tendency<T>(G, V, qa, q, beta));
+}
+
+// The PV crosses of the points (j, i) and (j+1, i) from one column of six
+// rows (j-2 .. j+3) and the four x-neighbours of rows j and j+1.
+template <typename T>
+__device__ __forceinline__ void cross_pair(const T* __restrict__ p, int nx, Cross<T>& a, Cross<T>& b)
+{
+    const T c_2 = p[-2 * nx], c_1 = p[-nx], c0 = p[0], c1 = p[nx], c2 = p[2 * nx], c3 = p[3 * nx];
+    a.c = c0; a.e1 = p[1]; a.e2 = p[2]; a.w1 = p[-1]; a.w2 = p[-2];
+    a.n1 = c1; a.n2 = c2; a.s1 = c_1; a.s2 = c_2;
+    const T* r = p + nx;
+    b.c = c1; b.e1 = r[1]; b.e2 = r[2]; b.w1 = r[-1]; b.w2 = r[-2];
+    b.n1 = c2; b.n2 = c3; b.s1 = c0; b.s2 = c_1;
+}
+
+// Forward stage: k = rhs(h2uv(hs), qs); qout = qbase + sum_i cin[i] k_i + cself k.
+// Each thread takes the points (j, i) and (j+1, i) (blocks of 32 x 4 threads
+// cover 32 x 8 points): when both are M3 points their SSH and PV stencils
+// overlap, so the pair is loaded once (12 + 14 values instead of 16 + 18) and
+// each point then runs the same arithmetic as a single point.
 template <typename T>
 __global__ void k_stage_fwd(QGGeom G, int nf, const T* __restrict__ hs, const T* __restrict__ qs,
                             const T* __restrict__ qbase, StageIn<T> kin, T cself,
                             T* __restrict__ kout, T* __restrict__ qout)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int j = blockIdx.y * (2 * blockDim.y) + 2 * threadIdx.y;
     const int f = blockIdx.z;
     if (i >= G.nx || j >= G.ny || f >= nf) return;
-    const long long o = f * G.fs + (long long)j * G.nx + i;
-    const long long go = (long long)j * G.nx + i;
-    T r = T(0);
-    if (G.mask[go] == 3) {
-        Vel<T> V;
-        V.load(G, hs + o);
-        V.u0 = guard0(V.u0); V.u1 = guard0(V.u1); V.v0 = guard0(V.v0); V.v1 = guard0(V.v1);
-        Cross<T> q;
-        q.load(qs + o, G.nx);
-        Cross<T> qa = q;
-        if (G.fB) { Cross<T> b; b.load((const T*)G.fB + go, G.nx); qa.add(b); }
-        const T beta = G.beta ? ((const T*)G.beta)[go] : T(0);
-        r = guard0(tendency<T>(G, V, qa, q, beta));
-    }
-    T acc = qbase[o];
+    const bool two = j + 1 < G.ny;
+    const int nx = G.nx;
+    const long long go = (long long)j * nx + i, o = f * G.fs + go;
+    const int m0 = G.mask[go], m1 = two ? G.mask[go + nx] : 0;
+    T r[2] = {T(0), T(0)};
+    if (m0 == 3 && m1 == 3) {
+        const T* h = hs + o;
+        const T s_w = h[-nx - 1], s_c = h[-nx], s_e = h[-nx + 1];
+        const T m_w = h[-1], m_c = h[0], m_e = h[1];
+        const T n_w = h[nx - 1], n_c = h[nx], n_e = h[nx + 1];
+        const T t_w = h[2 * nx - 1], t_c = h[2 * nx], t_e = h[2 * nx + 1];
+        Vel<T> V[2];
+        V[0].set(G, s_w, s_c, s_e, m_w, m_e, n_w, n_c, n_e);
+        V[1].set(G, m_w, m_c, m_e, n_w, n_e, t_w, t_c, t_e);
+        Cross<T> q[2], qa[2];
+        cross_pair(qs + o, nx, q[0], q[1]);
+        qa[0] = q[0];
+        qa[1] = q[1];
+        if (G.fB) {
+            Cross<T> b[2];
+            cross_pair((const T*)G.fB + go, nx, b[0], b[1]);
+            qa[0].add(b[0]);
+            qa[1].add(b[1]);
+        }
 #pragma unroll
-    for (int t = 0; t < 4; ++t)
-        if (t < kin.nk) acc += kin.c[t] * kin.k[t][o];
-    acc += cself * r;
-    qout[o] = acc;
-    if (kout) kout[o] = r;
+        for (int u = 0; u < 2; ++u) {
+            V[u].u0 = guard0(V[u].u0); V[u].u1 = guard0(V[u].u1);
+            V[u].v0 = guard0(V[u].v0); V[u].v1 = guard0(V[u].v1);
+            const T beta = G.beta ? ((const T*)G.beta)[go + u * nx] : T(0);
+            r[u] = guard0(tendency<T>(G, V[u], qa[u], q[u], beta));
+        }
+    } else {
+        if (m0 == 3) r[0] = stage_point(G, hs, qs, o, go);
+        if (m1 == 3) r[1] = stage_point(G, hs, qs, o + nx, go + nx);
+    }
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        if (u == 1 && !two) break;
+        const long long ou = o + u * nx;
+        T acc = qbase[ou];
+#pragma unroll
+        for (int t = 0; t < 4; ++t)
+            if (t < kin.nk) acc += kin.c[t] * kin.k[t][ou];
+        acc += cself * r[u];
+        qout[ou] = acc;
+        if (kout) kout[ou] = r[u];
+    }
 }
 
 // Tangent stage on dual arrays: fields [0, B) primal, [B, 2B) tangent.
@@ -590,7 +652,8 @@ static int step_once(const vd_qg1l_plan* p, int nf, T* const* hsv, T* const* qsv
         if (tangent)
             k_stage_tl<T><<<pgrid(p, B), kBlock, 0, st>>>(p->geom, B, hsv[s], qsv[s], qsv[0], kin, cself, kout, qo);
         else
-            k_stage_fwd<T><<<pgrid(p, nf), kBlock, 0, st>>>(p->geom, nf, hsv[s], qsv[s], qsv[0], kin, cself, kout, qo);
+            k_stage_fwd<T><<<pgrid(p, nf), dim3(32, 4), 0, st>>>(p->geom, nf, hsv[s], qsv[s], qsv[0], kin, cself, kout,
+                                                                 qo);
         VD_LAUNCH_CHECK();
         SolveArgs a;
         a.src = qo; a.sub = qb; a.sub_batches = B;
