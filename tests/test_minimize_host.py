@@ -60,3 +60,4 @@ def test_line_search_matches_scipy(name, stp0, tols):
     else:
         assert stp == sstp
         assert task.startswith("CONV") == (stask[:4] == b"CONV" or str(stask).startswith("CONV"))
+
