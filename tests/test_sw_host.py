@@ -1,4 +1,6 @@
 """Host logic of the shallow-water drop-in (no GPU)."""
+
+
 def test_sw_cotangent_sum_to_broadcast_shape():
     """SW.step_adj returns the H / h_wind cotangents summed down to the shapes
     the inputs were given in (jax.vjp of a broadcast input)."""
