@@ -16,7 +16,10 @@ Semantics kept from jax.numpy:
 - ``lax.scan`` is a Python loop, ``checkpoint`` the identity (it only changes
   what reverse mode stores), ``lax.reduce_window`` a sliding-window reduction,
   ``nn.softplus`` is log(1 + e^x) by ``logaddexp``;
-- ``jnp.clip(x, a_min=...)`` accepts a missing bound, as jax's does.
+- ``jnp.clip(x, a_min=...)`` accepts a missing bound, as jax's does;
+- ``vmap`` over axis 0 is a loop with stacked outputs; ``lax.dynamic_slice``
+  and ``lax.dynamic_update_slice`` clamp their start indices into the operand,
+  as XLA's do.
 ``jvp``/``vjp`` are not provided: the tangent/adjoint golden checks use finite
 differences of this forward instead.
 """
@@ -122,6 +125,39 @@ def _unavailable(*args, **kwargs):
     raise NotImplementedError("not available in the NumPy stand-in")
 
 
+def _vmap(fun, in_axes=0, out_axes=0):
+    """jax.vmap over axis 0 of every argument (the form QgmWithTiles.step uses):
+    a Python loop whose outputs are stacked along axis 0."""
+    if in_axes != 0 or out_axes != 0:
+        raise NotImplementedError("vmap stand-in: axis 0 only")
+
+    def mapped(*args):
+        n = np.shape(args[0])[0]
+        outs = [fun(*(np.asarray(a)[k].view(JArray) for a in args)) for k in range(n)]
+        return np.stack([np.asarray(o) for o in outs]).view(JArray)
+    return mapped
+
+
+def _clamped_starts(shape, starts, sizes):
+    # jax.lax.dynamic_slice / dynamic_update_slice clamp every start index so
+    # that the window lies inside the operand
+    return [int(min(max(int(s), 0), d - z)) for s, d, z in zip(starts, shape, sizes)]
+
+
+def _dynamic_slice(operand, start_indices, slice_sizes):
+    x = np.asarray(operand)
+    st = _clamped_starts(x.shape, start_indices, slice_sizes)
+    return np.array(x[tuple(slice(a, a + z) for a, z in zip(st, slice_sizes))]).view(JArray)
+
+
+def _dynamic_update_slice(operand, update, start_indices):
+    x = np.array(np.asarray(operand))
+    u = np.asarray(update)
+    st = _clamped_starts(x.shape, start_indices, u.shape)
+    x[tuple(slice(a, a + z) for a, z in zip(st, u.shape))] = u
+    return x.view(JArray)
+
+
 def install(enable_x64=True):
     """Register fake ``jax``, ``matplotlib`` and ``src.config`` modules."""
     jax = types.ModuleType("jax")
@@ -137,12 +173,13 @@ def install(enable_x64=True):
     jax.nn = nn
     jax.jvp = _unavailable
     jax.vjp = _unavailable
-    jax.vmap = _unavailable
+    jax.vmap = _vmap
     cfg = types.SimpleNamespace(update=lambda *a, **k: None)
     jax.config = cfg
     lax = types.ModuleType("jax.lax")
-    for name in ("fori_loop", "dynamic_slice", "dynamic_update_slice"):
-        setattr(lax, name, _unavailable)
+    lax.fori_loop = _unavailable
+    lax.dynamic_slice = _dynamic_slice
+    lax.dynamic_update_slice = _dynamic_update_slice
     lax.scan = _scan
     lax.reduce_window = _reduce_window
     lax.add = np.add
