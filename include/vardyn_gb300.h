@@ -72,6 +72,41 @@ typedef struct vd_qg1l_desc {
 #define VD_DST_AUTO 0
 #define VD_DST_FMA 1
 
+/* ------------------------------------------------------------------------
+ * Overlapping-tile QG 1.5-layer model, forward (QgmWithTiles.step,
+ * mapping/models/model_qg1l/jqgm.py:1033-1376). Every tile runs its own
+ * QG1.5L model (tile-mean f and c, no beta or bathymetry, Dirichlet hb on
+ * the tile edge) for nstep steps; the weighted tiles are blended. The tables
+ * are device arrays the caller builds (the drop-in class does):
+ * ------------------------------------------------------------------------ */
+typedef struct vd_qgt_desc {
+    int ny, nx;                 /* domain */
+    int tile;                   /* tile side T (>= 8) */
+    int ntiles;
+    int dtype;                  /* VD_F32 | VD_F64 */
+    int time_scheme;            /* VD_EULER | VD_RK2 */
+    int has_Kdiffus;
+    double dx, dy, dt, g, Kdiffus;  /* centre spacings of the domain (jqgm.py:126-128) */
+    const int32_t* origins;     /* [ntiles][2] (row, column) of each tile, inside the domain */
+    const double* f_tile;       /* [ntiles] tile means of f (jqgm.py:1313) */
+    const double* c_tile;       /* [ntiles] tile means of c (jqgm.py:1314) */
+    const int8_t* mask;         /* [ny][nx] classes of the domain mask (0 land, 1/2 rings, 3) */
+    const void* S;              /* [T-2][T-2] orthonormal DST-I matrix */
+    const void* lap;            /* [T-2][T-2] Laplacian eigenvalues of the tile (jqgm.py:1065-1067) */
+    const void* weights;        /* [T][T] tile taper (jqgm.py:1069-1073) */
+    const void* wsum;           /* [ny][nx] summed tapers */
+    const void* mdt;            /* [ny][nx] or NULL */
+} vd_qgt_desc;
+
+/* Shared memory one tile needs (the tile kernel holds a whole tile); a step
+ * is VD_ERR_UNSUPPORTED above 227 KiB (e.g. T = 64 fits in float32, T <= 48
+ * in float64). */
+size_t vd_qgt_shared_bytes(int tile, int dtype);
+size_t vd_qgt_workspace_bytes(const vd_qgt_desc* desc);
+/* h1 = QgmWithTiles.step(h0, hb, nstep), fields [ny][nx] in desc->dtype. */
+vd_status vd_qgt_step(const vd_qgt_desc* desc, const void* h0, const void* hb, int nstep, void* h1,
+                      void* work, size_t work_bytes, void* stream);
+
 /* Build a plan: DST-I half matrices, tridiagonal multipliers, mask, beta and
  * bathymetry tables on the current device. Replaces the constant set-up of
  * Qgm.__init__ (jqgm.py:113-236). */

@@ -87,6 +87,19 @@ class VdMgDesc(ctypes.Structure):
 _DP = ctypes.POINTER(ctypes.c_double)
 
 
+class VdQgtDesc(ctypes.Structure):
+    """vd_qgt_desc: tables are device pointers (c_void_p)."""
+    _fields_ = [
+        ("ny", ctypes.c_int), ("nx", ctypes.c_int), ("tile", ctypes.c_int), ("ntiles", ctypes.c_int),
+        ("dtype", ctypes.c_int), ("time_scheme", ctypes.c_int), ("has_Kdiffus", ctypes.c_int),
+        ("dx", ctypes.c_double), ("dy", ctypes.c_double), ("dt", ctypes.c_double), ("g", ctypes.c_double),
+        ("Kdiffus", ctypes.c_double),
+        ("origins", ctypes.c_void_p), ("f_tile", ctypes.c_void_p), ("c_tile", ctypes.c_void_p),
+        ("mask", ctypes.c_void_p), ("S", ctypes.c_void_p), ("lap", ctypes.c_void_p),
+        ("weights", ctypes.c_void_p), ("wsum", ctypes.c_void_p), ("mdt", ctypes.c_void_p),
+    ]
+
+
 class VdSwDesc(ctypes.Structure):
     _fields_ = [
         ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nl", ctypes.c_int), ("dtype", ctypes.c_int),
@@ -129,6 +142,9 @@ SIGNATURES = {
     "vd_launch_count": (LL, []),
     "vd_device_error": (I, [ctypes.POINTER(ctypes.c_int), I]),
     "vd_qg1l_plan_create": (I, [ctypes.POINTER(P), ctypes.POINTER(VdDesc)]),
+    "vd_qgt_shared_bytes": (SZ, [I, I]),
+    "vd_qgt_workspace_bytes": (SZ, [ctypes.POINTER(VdQgtDesc)]),
+    "vd_qgt_step": (I, [ctypes.POINTER(VdQgtDesc), P, P, I, P, P, SZ, P]),
     "vd_qg1l_plan_destroy": (I, [P]),
     "vd_qg1l_workspace_bytes": (SZ, [P, I]),
     "vd_qg1l_traj_bytes": (SZ, [P, I, I]),

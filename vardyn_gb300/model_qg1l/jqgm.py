@@ -12,6 +12,7 @@ NumPy (returned as NumPy) or CUDA torch tensors (returned as tensors).
 Precision follows the reference's global flag: float32 unless
 ``VARDYN_GB300_FLOAT64=1`` is set or ``dtype='float64'`` is passed.
 """
+import ctypes
 import os
 
 import numpy as np
@@ -191,3 +192,131 @@ class Qgm_sf(Qgm):
         P0, PB = self._phi_in(h0, hb)
         adP = self.plan.scale(self._to_dev(adh0), self._sinv)
         return self._wrap(h0, self.plan.scale(self.plan.step_adj(adP, P0, PB, int(nstep)), self._s))
+
+
+def _gaspari_cohn(r, c):
+    """Gaspari-Cohn taper (jqgm.py:22-53): 1 at 0, zero beyond distance c."""
+    ra = 2 * np.abs(np.asarray(r, dtype=np.float64)) / c
+    gp = np.zeros_like(ra)
+    i = ra <= 1.0
+    gp[i] = -0.25 * ra[i] ** 5 + 0.5 * ra[i] ** 4 + 0.625 * ra[i] ** 3 - 5.0 / 3.0 * ra[i] ** 2 + 1.0
+    i = (ra > 1.0) & (ra <= 2.0)
+    gp[i] = (ra[i] ** 5 / 12.0 - 0.5 * ra[i] ** 4 + 0.625 * ra[i] ** 3 + 5.0 / 3.0 * ra[i] ** 2 - 5.0 * ra[i]
+             + 4.0 - 2.0 / 3.0 / ra[i])
+    return gp
+
+
+class QgmWithTiles:
+    """Overlapping-tile QG 1.5-layer model with the constructor of
+    jqgm.py:1035-1085. ``step`` runs on the GPU (vd_qgt_step): every tile of
+    ``tile_size`` (overlap ``tile_overlap``) is an independent QG1.5L model
+    with the tile means of f and c and Dirichlet hb on its edge, the tiles are
+    blended with Gaspari-Cohn tapers. ``time_scheme`` is 'Euler' or 'rk2' (the
+    reference's tile model knows only these). The tangent linear and adjoint
+    (jax.jvp / vjp of the blended step) are not built: they raise."""
+
+    def __init__(self, dx=None, dy=None, dt=None, SSH=None, c=None, Kdiffus=None, upwind=3, g=9.81, f=1e-4,
+                 time_scheme="Euler", mdt=None, tile_size=64, tile_overlap=8, dtype=None, device=None, **kwargs):
+        from vardyn_gb300 import _lib
+        if time_scheme not in ("Euler", "rk2"):
+            raise ValueError("QgmWithTiles steps with 'Euler' or 'rk2' (jqgm.py:1269-1276)")
+        if dtype is None:
+            dtype = _default_dtype()
+        elif isinstance(dtype, str):
+            dtype = torch.float64 if dtype == "float64" else torch.float32
+        self.dtype = dtype
+        self.device = torch.device(device if device is not None else "cuda")
+        self._lib = _lib
+        ny, nx = np.shape(dx)
+        self.ny, self.nx = ny, nx
+        self.dx = float(np.asarray(dx)[int(ny / 2), int(nx / 2)])       # jqgm.py:126-131
+        self.dy = float(np.asarray(dy)[int(ny / 2), int(nx / 2)])
+        self.dt, self.g = float(dt), float(g)
+        self.time_scheme, self.Kdiffus = time_scheme, Kdiffus
+        T, ov = int(tile_size), int(tile_overlap)
+        if not (8 <= T <= min(ny, nx)) or not (0 < ov < T):
+            raise ValueError("tile_size must lie in [8, min(ny, nx)] and 0 < tile_overlap < tile_size")
+        esz = 8 if dtype == torch.float64 else 4
+        need = _lib.load().vd_qgt_shared_bytes(T, _lib.VD_F64 if esz == 8 else _lib.VD_F32)
+        if need > 227 * 1024:
+            raise ValueError(f"tile_size {T} needs {need} B of shared memory per tile (more than 227 KiB)")
+        self.tile_size, self.tile_overlap = T, ov
+        self.mask = build_mask(ny, nx, None if SSH is None else np.asarray(SSH))
+        fa = np.broadcast_to(np.asarray(f, dtype=np.float64), (ny, nx))
+        ca = np.broadcast_to(np.asarray(c, dtype=np.float64), (ny, nx))
+        # tiles (jqgm.py:1087-1101): the last tile of a row / column moved back inside
+        tiles = []
+        for y in range(0, ny, T - ov):
+            for x in range(0, nx, T - ov):
+                tiles.append((ny - T if y + T > ny else y, nx - T if x + T > nx else x))
+        self.tiles = tiles
+        org = np.asarray(tiles, dtype=np.int32)
+        assert org.min() >= 0 and (org[:, 0] <= ny - T).all() and (org[:, 1] <= nx - T).all()
+        ftile = np.array([np.nanmean(fa[a:a + T, b:b + T]) for a, b in tiles])       # jqgm.py:1313-1314
+        ctile = np.array([np.nanmean(ca[a:a + T, b:b + T]) for a, b in tiles])
+        # tile taper (jqgm.py:1069-1079)
+        w = np.ones(T)
+        gc = _gaspari_cohn(np.arange(0, T), ov)[:ov]
+        w[:ov] = gc[::-1]
+        w[-ov:] = gc
+        wt = w[:, None] * w[None, :]
+        wsum = np.zeros((ny, nx))
+        for a, b in tiles:
+            wsum[a:a + T, b:b + T] += wt
+        # orthonormal DST-I of the tile interior and its Laplacian eigenvalues (jqgm.py:1063-1067)
+        n = T - 2
+        k = np.arange(1, n + 1)
+        S = np.sqrt(2.0 / (n + 1)) * np.sin(np.pi * np.outer(k, k) / (n + 1))
+        xg, yg = np.meshgrid(np.arange(1, T - 1, dtype=np.float64), np.arange(1, T - 1, dtype=np.float64))
+        lap = 2 * (np.cos(np.pi / (T - 1) * xg) - 1) / self.dx ** 2 + 2 * (np.cos(np.pi / (T - 1) * yg) - 1) / \
+            self.dy ** 2
+        dev, R = self.device, dtype
+        self._t = {
+            "origins": torch.as_tensor(org.reshape(-1), device=dev),
+            "f_tile": torch.as_tensor(ftile, dtype=torch.float64, device=dev),
+            "c_tile": torch.as_tensor(ctile, dtype=torch.float64, device=dev),
+            "mask": torch.as_tensor(self.mask.astype(np.int8), device=dev),
+            "S": torch.as_tensor(S, device=dev).to(R).contiguous(),
+            "lap": torch.as_tensor(lap, device=dev).to(R).contiguous(),
+            "weights": torch.as_tensor(wt, device=dev).to(R).contiguous(),
+            "wsum": torch.as_tensor(wsum, device=dev).to(R).contiguous(),
+        }
+        self._mdt = None if mdt is None else torch.as_tensor(np.asarray(mdt, dtype=np.float64),
+                                                               device=dev).to(R).contiguous()
+        d = _lib.VdQgtDesc()
+        d.ny, d.nx, d.tile, d.ntiles = ny, nx, T, len(tiles)
+        d.dtype = _lib.VD_F64 if esz == 8 else _lib.VD_F32
+        d.time_scheme = 0 if time_scheme == "Euler" else 1
+        d.has_Kdiffus = 0 if Kdiffus is None else 1
+        d.dx, d.dy, d.dt, d.g = self.dx, self.dy, self.dt, self.g
+        d.Kdiffus = 0.0 if Kdiffus is None else float(Kdiffus)
+        for key, val in self._t.items():
+            setattr(d, key, val.data_ptr())
+        d.mdt = None if self._mdt is None else self._mdt.data_ptr()
+        self._desc = d
+        self._work = torch.empty(_lib.load().vd_qgt_workspace_bytes(ctypes.byref(d)) // esz, dtype=R, device=dev)
+        self.step_jit = self.step
+        self.step_tgl_jit = self.step_tgl
+        self.step_adj_jit = self.step_adj
+
+    def step(self, h0, hb, nstep=1):
+        """QgmWithTiles.step (jqgm.py:1333-1356)."""
+        as_np = not isinstance(h0, torch.Tensor)
+        H0 = (h0 if not as_np else torch.as_tensor(np.asarray(h0, dtype=np.float64))).to(
+            device=self.device, dtype=self.dtype).contiguous()
+        HB = (hb if isinstance(hb, torch.Tensor) else torch.as_tensor(np.asarray(hb, dtype=np.float64))).to(
+            device=self.device, dtype=self.dtype).contiguous()
+        if tuple(H0.shape) != (self.ny, self.nx) or tuple(HB.shape) != (self.ny, self.nx):
+            raise ValueError(f"h0 and hb must be ({self.ny}, {self.nx})")
+        out = torch.empty_like(H0)
+        self._lib.call("vd_qgt_step", ctypes.byref(self._desc), ctypes.c_void_p(H0.data_ptr()),
+                       ctypes.c_void_p(HB.data_ptr()), int(nstep), ctypes.c_void_p(out.data_ptr()),
+                       ctypes.c_void_p(self._work.data_ptr()), self._work.numel() * self._work.element_size(),
+                       ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream))
+        return out.cpu().numpy() if as_np else out
+
+    def step_tgl(self, dh0, h0, hb, nstep=1):
+        raise NotImplementedError("tangent linear of QgmWithTiles (jax.jvp of the blended step) is not built")
+
+    def step_adj(self, adh0, h0, hb, nstep=1):
+        raise NotImplementedError("adjoint of QgmWithTiles (jax.vjp of the blended step) is not built")
