@@ -7,7 +7,11 @@ this module; the product never imports it.
 
 Pinning: ``step`` reproduces golden vectors generated by the reference's own
 ``jqgm.py`` source (``tests/golden/gen_golden_tiles.py``, checked in
-``tests/test_oracle_qg1l_tiles.py``).
+``tests/test_oracle_qg1l_tiles.py``). ``step_tgl`` / ``step_adj`` (jax.jvp /
+vjp of the blended step, jqgm.py:1358-1376) are hand-derived: every tile is
+the full-domain oracle's model with the tile's f, c and masks, so the tile
+Jacobians are that oracle's tangent and adjoint; they are checked against
+central differences of ``step`` and by a dot-product test.
 
 The model (all line numbers in jqgm.py):
 - the domain's masks are the full-domain model's (178-217): classes 1/2 on
@@ -26,7 +30,7 @@ The model (all line numbers in jqgm.py):
 """
 import numpy as np
 
-from oracle.qg1l import build_mask, inverse_elliptic_dst
+from oracle.qg1l import QgmOracle, build_mask, inverse_elliptic_dst
 
 
 def gaspari_cohn(r, c):
@@ -63,6 +67,46 @@ def tile_weights(size, overlap):
     w[:overlap] = gc[::-1]
     w[-overlap:] = gc
     return w[:, None] * w[None, :]
+
+
+class _TileModel(QgmOracle):
+    """One tile as the full-domain oracle's model: the tile's f and c, no beta
+    or bathymetry, the domain's mask classes sliced to the tile. Two point
+    sets replace the full domain's single interior set: PV is a function of h
+    on the tile interior [1:-1] (``ind_pv``), the tendency acts on [2:-2]
+    (``ind3``); both exclude the domain's ring classes and land."""
+
+    def __init__(self, T, dx, dy, dt, g, f, c, Kdiffus, scheme, ind12, ind0):
+        super().__init__(dx=np.full((T, T), dx), dy=np.full((T, T), dy), dt=dt, SSH=None, c=c, Kdiffus=Kdiffus,
+                         g=g, f=f, time_scheme=scheme)
+        self.ind0 = ind0
+        self.ind12 = ind12
+        self.ind1 = ind12
+        self.ind2 = np.zeros_like(ind12)
+        free = ~(ind12 | ind0)
+        core = np.zeros((T, T), bool)
+        core[2:-2, 2:-2] = True
+        inner = np.zeros((T, T), bool)
+        inner[1:-1, 1:-1] = True
+        self.ind3 = free & core
+        self.ind_pv = free & inner
+
+    def h2pv_tl(self, dh, h):
+        dq = np.zeros((self.ny, self.nx))
+        dq[1:-1, 1:-1] = self._h2pv_interior(dh)
+        qraw = np.zeros((self.ny, self.nx))
+        qraw[1:-1, 1:-1] = self._h2pv_interior(h)
+        dq[np.isnan(qraw)] = 0
+        dq[~self.ind_pv] = 0
+        return dq
+
+    def h2pv_adj(self, adq, h):
+        ind3 = self.ind3
+        self.ind3 = self.ind_pv
+        try:
+            return super().h2pv_adj(adq, h)
+        finally:
+            self.ind3 = ind3
 
 
 class QgmTilesOracle:
@@ -167,6 +211,40 @@ class QgmTilesOracle:
         for _ in range(int(nstep)):
             h1, q = self._one_step(h1, q, hbt, qb, f, c, i12, i0)
         return np.where(i0, np.nan, h1)
+
+    def _tile_model(self, k):
+        ys, xs = self.tiles[k]
+        s = (slice(ys, ys + self.T), slice(xs, xs + self.T))
+        return _TileModel(self.T, self.dx, self.dy, self.dt, self.g, float(np.nanmean(self.f[s])),
+                          float(np.nanmean(self.c[s])), self.K, self.scheme, self.ind12[s], self.ind0[s]), s
+
+    def _with_mdt(self, h, hb):
+        h = np.asarray(h, dtype=np.float64)
+        hb = np.asarray(hb, dtype=np.float64)
+        if self.mdt is not None:
+            return h + self.mdt, hb + self.mdt
+        return h, hb
+
+    def step_tgl(self, dh0, h0, hb, nstep=1):
+        """jax.jvp of the blended step with respect to h0 (jqgm.py:1358-1362);
+        zero on land, as the derivative of where(ind0, nan, h)."""
+        h, hbm = self._with_mdt(h0, hb)
+        dh0 = np.asarray(dh0, dtype=np.float64)
+        acc = np.zeros((self.ny, self.nx))
+        for k in range(len(self.tiles)):
+            m, s = self._tile_model(k)
+            acc[s] += self.w * m.step_tgl(dh0[s], h[s], hbm[s], nstep)
+        return acc / self.wsum
+
+    def step_adj(self, adh1, h0, hb, nstep=1):
+        """jax.vjp of the blended step with respect to h0 (jqgm.py:1364-1376)."""
+        h, hbm = self._with_mdt(h0, hb)
+        a = np.asarray(adh1, dtype=np.float64) / self.wsum
+        out = np.zeros((self.ny, self.nx))
+        for k in range(len(self.tiles)):
+            m, s = self._tile_model(k)
+            out[s] += m.step_adj(self.w * a[s], h[s], hbm[s], nstep)
+        return out
 
     # ---------------- the blended step (jqgm.py:1333-1376) ----------------
     def step(self, h, hb, nstep=1):

@@ -45,3 +45,39 @@ def test_tile_origins_cover_the_domain():
             assert 0 <= ys <= ny - T and 0 <= xs <= nx - T
             cov[ys:ys + T, xs:xs + T] += 1
         assert cov.min() >= 1
+
+
+def _tl_case(scheme, seed):
+    rng = np.random.default_rng(seed)
+    ny, nx = 30, 38
+    dx = np.full((ny, nx), 1.0e4)
+    ssh = 0.1 * rng.standard_normal((ny, nx))
+    ssh[12:15, 17:20] = np.nan
+    hb = 0.01 * rng.standard_normal((ny, nx))
+    hb[np.isnan(ssh)] = 0.0
+    o = QgmTilesOracle(dx=dx, dy=dx, dt=600.0, SSH=ssh, c=2.7, Kdiffus=20.0, f=1.0e-4, time_scheme=scheme,
+                       tile_size=16, tile_overlap=4, mdt=0.02 * rng.standard_normal((ny, nx)))
+    return o, np.nan_to_num(ssh), hb, rng
+
+
+@pytest.mark.parametrize("scheme", ["Euler", "rk2"])
+def test_tangent_matches_central_differences(scheme):
+    o, h0, hb, rng = _tl_case(scheme, 3)
+    d = 1e-3 * rng.standard_normal(h0.shape)
+    tl = o.step_tgl(d, h0, hb, 3)
+    eps = 1e-4     # the upwind switch makes larger steps cross kinks (1e-4 relative at 1e-3 for rk2)
+    fd = (o.step(h0 + eps * d, hb, 3) - o.step(h0 - eps * d, hb, 3)) / (2 * eps)
+    m = ~np.isnan(fd)
+    assert np.all(tl[~m] == 0)
+    assert np.abs(fd[m] - tl[m]).max() <= 1e-8 * np.abs(tl[m]).max()
+
+
+@pytest.mark.parametrize("scheme", ["Euler", "rk2"])
+def test_adjoint_dot_product(scheme):
+    o, h0, hb, rng = _tl_case(scheme, 4)
+    d = rng.standard_normal(h0.shape)
+    y = rng.standard_normal(h0.shape)
+    tl = o.step_tgl(d, h0, hb, 3)
+    ad = o.step_adj(y, h0, hb, 3)
+    lhs, rhs = float(np.sum(tl * y)), float(np.sum(d * ad))
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
