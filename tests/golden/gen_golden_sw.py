@@ -180,6 +180,34 @@ def qg_case(M, out, rng, island):
     out[p + "pqg"], out[p + "pqgi"] = np.asarray(pq), np.asarray(pqi)
 
 
+def sw_case_h(M, out, rng):
+    """Steps with the per-call H and h_wind arguments (sw.py:752-817): H
+    enters the reference values, the wind depth stays the model's own H
+    (sw.py:622-630); h_wind adds to the model's mixed-layer depth."""
+    nx, ny, nl = 26, 20, 2
+    dx, dy, f = grid(nx, ny, rng)
+    mask = land_mask(nx, ny)[:nx, :ny]
+    H = np.array([150.0, 600.0]).reshape(2, 1, 1)
+    gp = np.array([9.81, 0.03])
+    base = dict(nx=nx, ny=ny, nl=nl, dx=dx, dy=dy, H=H, g_prime=gp, f=f, taux=0.08, tauy=-0.05,
+                bottom_drag_coef=1e-6, dt=20.0, mask=mask, slip_coef=0.5, visc_coef=20.0, diff_coef=10.0,
+                compile=False, dtype=np.float64)
+    u0 = 0.05 * rng.standard_normal((1, nl, nx + 1, ny))
+    v0 = 0.05 * rng.standard_normal((1, nl, nx, ny + 1))
+    h0 = 0.3 * rng.standard_normal((1, nl, nx, ny))
+    dH = 4.0 * rng.standard_normal((1, nx, ny))
+    hw = 8.0 * rng.standard_normal((nx, ny))
+    p = "swh_"
+    for k, val in dict(dx=dx, dy=dy, f=f, mask=mask, H=H, gp=gp, u0=u0, v0=v0, h0=h0, dH=dH, hw=hw).items():
+        out[p + k] = np.asarray(val)
+    sw = M["sw"].SW(dict(base))
+    u1, v1, h1 = sw.step(J(u0), J(v0), J(h0), H=J(dH), nstep=3)
+    out[p + "uH"], out[p + "vH"], out[p + "hH"] = np.asarray(u1), np.asarray(v1), np.asarray(h1)
+    sw = M["sw"].SW(dict(base, h_wind=50.0))
+    u1, v1, h1 = sw.step(J(u0), J(v0), J(h0), nstep=3, h_wind=J(hw))
+    out[p + "uW"], out[p + "vW"], out[p + "hW"] = np.asarray(u1), np.asarray(v1), np.asarray(h1)
+
+
 def main():
     ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     M = load(ref_root)
@@ -189,6 +217,7 @@ def main():
     sw_case_b(M, out, rng)
     qg_case(M, out, rng, island=False)
     qg_case(M, out, rng, island=True)
+    sw_case_h(M, out, rng)
     np.savez_compressed(os.path.join(HERE, "sw_golden.npz"), **out)
     print("wrote", len(out), "arrays,", os.path.getsize(os.path.join(HERE, "sw_golden.npz")), "bytes")
 

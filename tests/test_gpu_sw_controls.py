@@ -156,3 +156,21 @@ def test_forward_with_perturbed_H_matches_oracle():
     exp = o.step(*x, H=dH, nstep=3)
     for a, b in zip(got, exp):
         assert np.abs(a - b).max() <= 1e-11 * np.abs(b).max()
+
+
+def test_dropin_H_and_h_wind_steps_match_reference():
+    """The drop-in SW.step with the per-call H and h_wind arguments against
+    the reference's own sw.py outputs (non-uniform metrics, land)."""
+    import os
+    from vardyn_gb300.model_qgsw.sw import SW
+    g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "sw_golden.npz")))
+    p = "swh_"
+    base = dict(nx=26, ny=20, nl=2, dx=g[p + "dx"], dy=g[p + "dy"], H=g[p + "H"], g_prime=g[p + "gp"], f=g[p + "f"],
+                taux=0.08, tauy=-0.05, bottom_drag_coef=1e-6, dt=20.0, mask=g[p + "mask"], slip_coef=0.5,
+                visc_coef=20.0, diff_coef=10.0, dtype="float64")
+    r = SW(dict(base)).step(g[p + "u0"], g[p + "v0"], g[p + "h0"], H=g[p + "dH"], nstep=3)
+    for a, k in zip(r, ("uH", "vH", "hH")):
+        assert np.abs(a - g[p + k]).max() <= 1e-11 * np.abs(g[p + k]).max(), k
+    r = SW(dict(base, h_wind=50.0)).step(g[p + "u0"], g[p + "v0"], g[p + "h0"], nstep=3, h_wind=g[p + "hw"])
+    for a, k in zip(r, ("uW", "vW", "hW")):
+        assert np.abs(a - g[p + k]).max() <= 1e-11 * np.abs(g[p + k]).max(), k

@@ -88,3 +88,27 @@ def test_oracle_steps(g):
     r = o.step(g[p + "u0"], g[p + "v0"], g[p + "h0"], nstep=5, Fh=g[p + "Fh"], taux=g[p + "taux"], tauy=g[p + "tauy"])
     for a, k in zip(r, ["u5", "v5", "h5"]):
         assert rel(a, g[p + k]) < 1e-13
+
+
+def param_h(g, **over):
+    p = "swh_"
+    d = dict(nx=26, ny=20, nl=2, dx=g[p + "dx"], dy=g[p + "dy"], H=g[p + "H"], g_prime=g[p + "gp"], f=g[p + "f"],
+             taux=0.08, tauy=-0.05, bottom_drag_coef=1e-6, dt=20.0, mask=g[p + "mask"], slip_coef=0.5,
+             visc_coef=20.0, diff_coef=10.0)
+    d.update(over)
+    return d
+
+
+def test_oracle_step_with_H_and_h_wind_arguments(g):
+    """SW.step(H=dH) (the wind depth stays the model's own H, sw.py:622-630)
+    and SW.step(h_wind=field) on a model whose h_wind is a scalar (the two
+    add, sw.py:810-817), on non-uniform metrics."""
+    p = "swh_"
+    o = SWOracle(param_h(g))
+    r = o.step(g[p + "u0"], g[p + "v0"], g[p + "h0"], H=g[p + "dH"], nstep=3)
+    for a, k in zip(r, ("uH", "vH", "hH")):
+        assert rel(a, g[p + k]) < 1e-12, k
+    o = SWOracle(param_h(g, h_wind=50.0 + g[p + "hw"]))
+    r = o.step(g[p + "u0"], g[p + "v0"], g[p + "h0"], nstep=3)
+    for a, k in zip(r, ("uW", "vW", "hW")):
+        assert rel(a, g[p + k]) < 1e-12, k
