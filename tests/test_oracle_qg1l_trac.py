@@ -1,0 +1,55 @@
+"""The QG 1.5-layer model with tracers (Qgm_trac, jqgm.py:1551-2151) restated
+in oracle/qg1l_trac.py against golden vectors produced by the reference's own
+jqgm.py source (tests/golden/gen_golden_trac.py)."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle.qg1l_trac import QgmTracOracle
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden", "qgtrac_golden.npz")
+
+
+@pytest.fixture(scope="module")
+def g():
+    return dict(np.load(GOLD))
+
+
+def _rel(a, b):
+    assert np.array_equal(np.isnan(a), np.isnan(b))
+    m = ~np.isnan(b)
+    return float(np.abs(a[m] - b[m]).max() / np.abs(b[m]).max())
+
+
+def test_euler_two_tracers_open_boundaries(g):
+    o = QgmTracOracle(dx=g["a_dx"], dy=g["a_dy"], dt=900.0, SSH=g["a_ssh"], c=2.7, g=9.81, f=g["a_f"],
+                      time_scheme="Euler", Kdiffus=30.0, Kdiffus_trac=10.0, bc_trac="OBC", mdt=g["a_mdt"])
+    assert _rel(o.step(g["a_X0"], g["a_Xb"], nstep=4), g["a_X1"]) < 1e-12
+
+
+def test_rk2_dirichlet_relaxation_no_pv_advection(g):
+    o = QgmTracOracle(dx=g["b_dx"], dy=g["b_dx"], dt=600.0, SSH=g["b_ssh"], c=2.5, g=9.81, f=1.0e-4,
+                      time_scheme="rk2", Wbc=g["b_wbc"], Kdiffus=None, Kdiffus_trac=5.0, bc_trac="dirichlet",
+                      advect_pv=False)
+    assert _rel(o.step(g["b_X0"], g["b_Xb"], nstep=3), g["b_X1"]) < 1e-12
+
+
+def test_rk2_without_tracers(g):
+    o = QgmTracOracle(dx=g["c_dx"], dy=g["c_dx"], dt=900.0, SSH=g["c_ssh"], c=2.7, g=9.81, f=1.0e-4,
+                      time_scheme="rk2", Kdiffus=15.0)
+    assert _rel(o.step(g["c_ssh"], g["c_hb"], nstep=3), g["c_h1"]) < 1e-12
+
+
+@pytest.mark.parametrize("change", [dict(bc_trac="OBC"), dict(Wbc=None), dict(Kdiffus_trac=None)])
+def test_fixtures_tell_the_options_apart(g, change):
+    kw = dict(dx=g["b_dx"], dy=g["b_dx"], dt=600.0, SSH=g["b_ssh"], c=2.5, g=9.81, f=1.0e-4, time_scheme="rk2",
+              Wbc=g["b_wbc"], Kdiffus_trac=5.0, bc_trac="dirichlet", advect_pv=False)
+    kw.update(change)
+    assert _rel(QgmTracOracle(**kw).step(g["b_X0"], g["b_Xb"], nstep=3), g["b_X1"]) > 1e-6
+
+
+def test_rk4_is_refused():
+    with pytest.raises(ValueError):
+        QgmTracOracle(dx=np.full((8, 8), 1e4), dy=np.full((8, 8), 1e4), dt=900.0, SSH=np.zeros((8, 8)), c=2.7,
+                      time_scheme="rk4")
