@@ -662,6 +662,15 @@ vd_status vd_qgp_op(const vd_qgp_plan* plan, int op, int batch, const void* cons
 vd_status vd_obs_knn(long long nobs, const double* x_km, const double* y_km, int ny, int nx,
                      double dx_km, double dy_km, int npix, double dmax_km, long long* idx,
                      double* w, void* stream);
+/* vd_obs_knn with the neighbour rules of the scipy operator Obsop_interp_l3
+ * (obsop.py:197-219): exclude [ny * nx] bytes (device, nullable), nonzero
+ * for grid points that may not carry a weight (its ind_borders and ind_mask,
+ * obsop.py:118-134). An excluded point keeps its place among the npix
+ * nearest and gets index -1, weight 0; the kept weights are normalised over
+ * the kept points. exclude = NULL is vd_obs_knn. */
+vd_status vd_obs_knn_excl(long long nobs, const double* x_km, const double* y_km, int ny, int nx,
+                          double dx_km, double dy_km, int npix, double dmax_km,
+                          const unsigned char* exclude, long long* idx, double* w, void* stream);
 
 /* ------------------------------------------------------------------------
  * Batched float64 vector kernels of the outer minimisation (L-BFGS without

@@ -1,5 +1,6 @@
 """Restatement of the along-track observation operator of the reference
-(mapping/src/obsop.py, Obsop_interp_l3_jax) in float64 NumPy. Test
+(mapping/src/obsop.py, Obsop_interp_l3_jax, and the neighbour rules of the
+scipy Obsop_interp_l3) in float64 NumPy. Test
 infrastructure only.
 
 Planar coordinates: the reference maps lon/lat to 3-D Cartesian km
@@ -61,3 +62,55 @@ def misfit_adj(cot, data, rows, cols, err, size, x_flat=None, yobs=None):
     ad = np.zeros(size)
     np.add.at(ad, cols, data * g[rows])
     return ad
+
+
+def l3_excluded(ny, nx, dx, dy, mask=None, mask_borders=False):
+    """Flat grid indices the scipy operator ``Obsop_interp_l3`` skips when it
+    picks neighbours (obsop.py:118-134), on the planar grid of this module.
+
+    ``ind_mask`` is ``np.where(State.mask)[1]`` (obsop.py:120): for a 2-D mask
+    that is the COLUMN number of every masked point, compared later with flat
+    indices, so the points it removes are those of row 0 whose column holds a
+    masked point. ``ind_borders`` is every point whose coordinates are close
+    (np.isclose) to those of a point on the outer ring (obsop.py:126-134)."""
+    out = set()
+    if mask is not None:
+        out.update(int(j) for j in np.where(np.asarray(mask))[1])
+    if mask_borders:
+        gx, gy = np.meshgrid(np.arange(nx) * dx / 1e3, np.arange(ny) * dy / 1e3)
+        ring = np.column_stack((np.concatenate((gx[0, :], gx[1:-1, -1], gx[-1, :], gx[:, 0])),
+                                np.concatenate((gy[0, :], gy[1:-1, -1], gy[-1, :], gy[:, 0]))))
+        pts = np.column_stack((gx.ravel(), gy.ravel()))
+        for i in range(pts.shape[0]):
+            if np.any(np.all(np.isclose(ring, pts[i]), axis=1)):
+                out.add(i)
+    return out
+
+
+def sparse_op_l3(x_obs_km, y_obs_km, ny, nx, dx, dy, npix=4, excluded=()):
+    """(data, rows, cols) of the scipy operator's H (``_sparse_op``,
+    obsop.py:197-219): per observation, all grid distances, the ``npix``
+    nearest in order; a neighbour is kept if it is not excluded and lies
+    within ``dmax``; kept weights exp(-d^2/(2(dmax/2)^2)) normalised over the
+    kept ones. Excluded neighbours keep their place among the ``npix``
+    nearest (they are not replaced by the next one). Equal distances are
+    ordered by grid index (the reference's argsort leaves them unordered;
+    they do not occur at seeded random positions)."""
+    gx, gy = np.meshgrid(np.arange(nx) * dx / 1e3, np.arange(ny) * dy / 1e3)
+    grid = np.column_stack((gx.ravel(), gy.ravel()))
+    dmax = dmax_km(dx, dy, npix)
+    excluded = set(excluded)
+    data, rows, cols = [], [], []
+    for o in range(len(x_obs_km)):
+        dist = np.sqrt(((grid - np.array([x_obs_km[o], y_obs_km[o]])) ** 2).sum(axis=1))
+        order = np.argsort(dist, kind="stable")
+        ws = []
+        for p in range(npix):
+            k = int(order[p])
+            if k not in excluded and dist[k] <= dmax:
+                ws.append(np.exp(-(dist[k] ** 2 / (2 * (0.5 * dmax) ** 2))))
+                rows.append(o)
+                cols.append(k)
+        s = np.sum(ws)
+        data.extend(w / s for w in ws)
+    return np.asarray(data, dtype=np.float64), np.asarray(rows, dtype=np.int64), np.asarray(cols, dtype=np.int64)

@@ -49,6 +49,26 @@ def test_obs_operator_same_either_build():
     assert (a.d_w4 - b.d_w4).abs().max().item() <= 1e-14
 
 
+@pytest.mark.parametrize("npix", [1, 4])
+def test_knn_with_exclusion_matches_host(npix):
+    """The scipy operator's rules (Obsop_interp_l3, obsop.py:197-219): ring
+    and row-0 mask columns excluded, on the device and on the host."""
+    from vardyn_gb300.obsop import interp_rows, interp_rows_gpu, l3_exclusion
+    ny, nx, dx, dy = 60, 70, 4.0e3, 7.0e3
+    mask = np.zeros((ny, nx), dtype=bool)
+    mask[20:30, 25:40] = True
+    ex = l3_exclusion(ny, nx, mask, mask_borders=True)
+    rng = np.random.default_rng(77 + npix)
+    n = 20000
+    x = rng.uniform(-30.0, nx * dx / 1e3 + 30.0, n)
+    y = rng.uniform(-30.0, ny * dy / 1e3 + 30.0, n)
+    i_h, w_h = interp_rows(x, y, ny, nx, dx, dy, npix, exclude=ex)
+    i_g, w_g = interp_rows_gpu(x, y, ny, nx, dx, dy, npix, exclude=ex)
+    assert np.array_equal(i_h, i_g)
+    assert np.abs(w_h - w_g).max() <= 1e-14
+    assert np.all(ex[i_g[i_g >= 0]] == 0)
+
+
 def test_knn_large_set_timing():
     """One million observations: the device construction against the host
     KDTree (printed, not asserted)."""

@@ -215,6 +215,7 @@ SIGNATURES = {
     "vd_qgp_op": (I, [P, I, I, P, P]),
     "vd_edge_pad_adj": (I, [I, I, I, I, P, P, P, P]),
     "vd_obs_knn": (I, [LL, P, P, I, I, D, D, I, D, P, P, P]),
+    "vd_obs_knn_excl": (I, [LL, P, P, I, I, D, D, I, D, P, P, P, P]),
     "vd_bdot_workspace_bytes": (SZ, [I, LL]),
     "vd_bdot_f64": (I, [I, LL, P, P, P, P, P, P, SZ, P]),
     "vd_baxpy_f64": (I, [I, LL, D, P, P, D, P, P]),

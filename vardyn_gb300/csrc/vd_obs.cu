@@ -320,8 +320,8 @@ extern "C" vd_status vd_diag_axpy(int dtype, long long n, long long period, cons
 // ---------------------------------------------------------------------------
 namespace vd {
 __global__ void k_obs_knn(long long nobs, const double* __restrict__ x, const double* __restrict__ y, int ny, int nx,
-                          double dx, double dy, int npix, double dmax, long long* __restrict__ idx,
-                          double* __restrict__ w)
+                          double dx, double dy, int npix, double dmax, const unsigned char* __restrict__ excl,
+                          long long* __restrict__ idx, double* __restrict__ w)
 {
     const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= nobs) return;
@@ -364,7 +364,8 @@ __global__ void k_obs_knn(long long nobs, const double* __restrict__ x, const do
     const double c = 2.0 * (0.5 * dmax) * (0.5 * dmax);
     for (int k = 0; k < npix; ++k) {
         D[k] = sqrt(bd[k]);
-        const bool valid = bi[k] >= 0 && D[k] <= dmax;
+        // an excluded point keeps its place among the npix nearest but gets no weight
+        const bool valid = bi[k] >= 0 && D[k] <= dmax && !(excl && excl[bi[k]]);
         ww[k] = npix > 1 ? (valid ? exp(-D[k] * D[k] / c) : 0.0) : (valid ? 1.0 : 0.0);
         if (!valid) bi[k] = -1;
     }
@@ -376,15 +377,22 @@ __global__ void k_obs_knn(long long nobs, const double* __restrict__ x, const do
 }
 }  // namespace vd
 
-extern "C" vd_status vd_obs_knn(long long nobs, const double* x_km, const double* y_km, int ny, int nx, double dx_km,
-                                double dy_km, int npix, double dmax_km, long long* idx, double* w, void* stream)
+extern "C" vd_status vd_obs_knn_excl(long long nobs, const double* x_km, const double* y_km, int ny, int nx,
+                                     double dx_km, double dy_km, int npix, double dmax_km, const unsigned char* exclude,
+                                     long long* idx, double* w, void* stream)
 {
     if (nobs < 0 || ny < 1 || nx < 1 || npix < 1 || npix > 4 || !(dx_km > 0) || !(dy_km > 0) || !(dmax_km > 0))
         return VD_ERR_ARG;
     if (nobs == 0) return VD_OK;
     if (!x_km || !y_km || !idx || !w) return VD_ERR_ARG;
     vd::k_obs_knn<<<(unsigned)((nobs + 127) / 128), 128, 0, (cudaStream_t)stream>>>(
-        nobs, x_km, y_km, ny, nx, dx_km, dy_km, npix, dmax_km, idx, w);
+        nobs, x_km, y_km, ny, nx, dx_km, dy_km, npix, dmax_km, exclude, idx, w);
     VD_LAUNCH_CHECK();
     return VD_OK;
+}
+
+extern "C" vd_status vd_obs_knn(long long nobs, const double* x_km, const double* y_km, int ny, int nx, double dx_km,
+                                double dy_km, int npix, double dmax_km, long long* idx, double* w, void* stream)
+{
+    return vd_obs_knn_excl(nobs, x_km, y_km, ny, nx, dx_km, dy_km, npix, dmax_km, nullptr, idx, w, stream);
 }

@@ -33,9 +33,33 @@ def dmax_km(dx, dy, npix):
     return npix * np.sqrt(dx ** 2 + dy ** 2) * 1e-3 * np.sqrt(2) / 2
 
 
-def interp_rows(x_km, y_km, ny, nx, dx, dy, npix=4):
+def l3_exclusion(ny, nx, mask=None, mask_borders=False):
+    """[ny * nx] uint8 table of the grid points the scipy operator
+    ``Obsop_interp_l3`` never weights (obsop.py:118-134, used at 207-211).
+
+    - ``mask_borders``: the outer ring of the grid (obsop.py:126-134 match
+      coordinates against the ring's; on a uniform grid that is the ring).
+    - ``mask`` (True on land): the reference stores ``np.where(mask)[1]``,
+      the column numbers of the masked points, and compares them with flat
+      grid indices, so what it removes is the points of row 0 whose column
+      holds a masked point. That rule is kept here as the reference applies
+      it."""
+    ex = np.zeros((ny, nx), dtype=np.uint8)
+    if mask_borders:
+        ex[0, :] = ex[-1, :] = 1
+        ex[:, 0] = ex[:, -1] = 1
+    flat = ex.reshape(-1)
+    if mask is not None:
+        cols = np.unique(np.where(np.asarray(mask, dtype=bool))[1])
+        flat[cols] = 1
+    return flat
+
+
+def interp_rows(x_km, y_km, ny, nx, dx, dy, npix=4, exclude=None):
     """(idx [n, npix] with -1 for dropped neighbours, w [n, npix]) on a
-    uniform grid whose point (0, 0) sits at (0 km, 0 km)."""
+    uniform grid whose point (0, 0) sits at (0 km, 0 km). ``exclude`` (an
+    :func:`l3_exclusion` table) applies the scipy operator's rule: an excluded
+    point keeps its place among the ``npix`` nearest and gets no weight."""
     gx, gy = np.meshgrid(np.arange(nx) * dx / 1e3, np.arange(ny) * dy / 1e3)
     tree = cKDTree(np.column_stack((gx.ravel(), gy.ravel())))
     D, ind = tree.query(np.column_stack((x_km, y_km)), k=npix)
@@ -43,6 +67,8 @@ def interp_rows(x_km, y_km, ny, nx, dx, dy, npix=4):
         D, ind = D[:, None], ind[:, None]
     dmax = dmax_km(dx, dy, npix)
     valid = D <= dmax
+    if exclude is not None:
+        valid &= np.asarray(exclude, dtype=bool)[np.minimum(ind, ny * nx - 1)] == 0
     if npix > 1:
         w = np.exp(-D ** 2 / (2 * (0.5 * dmax) ** 2)) * valid
         s = w.sum(axis=1, keepdims=True)
@@ -54,16 +80,25 @@ def interp_rows(x_km, y_km, ny, nx, dx, dy, npix=4):
     return idx, w
 
 
-def interp_rows_gpu(x_km, y_km, ny, nx, dx, dy, npix=4, device="cuda"):
-    """interp_rows on the GPU (vd_obs_knn); returns host arrays (idx with
-    -1 for dropped neighbours, w), shapes [n, npix]."""
+def interp_rows_gpu(x_km, y_km, ny, nx, dx, dy, npix=4, device="cuda", exclude=None):
+    """interp_rows on the GPU (vd_obs_knn, or vd_obs_knn_excl with an
+    ``exclude`` table); returns host arrays (idx with -1 for dropped
+    neighbours, w), shapes [n, npix]."""
     x = torch.as_tensor(np.ascontiguousarray(x_km, dtype=np.float64), device=device)
     y = torch.as_tensor(np.ascontiguousarray(y_km, dtype=np.float64), device=device)
     n = x.numel()
     idx = torch.empty((max(n, 1), 4), dtype=torch.int64, device=device)
     w = torch.empty((max(n, 1), 4), dtype=torch.float64, device=device)
-    _lib.call("vd_obs_knn", n, _p(x), _p(y), ny, nx, dx / 1e3, dy / 1e3, npix, dmax_km(dx, dy, npix), _p(idx), _p(w),
-              _stream())
+    if exclude is None:
+        _lib.call("vd_obs_knn", n, _p(x), _p(y), ny, nx, dx / 1e3, dy / 1e3, npix, dmax_km(dx, dy, npix), _p(idx),
+                  _p(w), _stream())
+    else:
+        ex = np.ascontiguousarray(exclude, dtype=np.uint8).reshape(-1)
+        if ex.size != ny * nx:
+            raise ValueError("exclude holds one byte per grid point")
+        ex = torch.as_tensor(ex, device=device)
+        _lib.call("vd_obs_knn_excl", n, _p(x), _p(y), ny, nx, dx / 1e3, dy / 1e3, npix, dmax_km(dx, dy, npix),
+                  _p(ex), _p(idx), _p(w), _stream())
     return idx[:n, :npix].cpu().numpy(), w[:n, :npix].cpu().numpy()
 
 
@@ -80,9 +115,13 @@ class AlongTrackObs:
 
     ``windows[b]`` is a dict with arrays ``x_km``, ``y_km`` (planar position),
     ``step`` (model step index at which the point is observed), ``yobs`` and
-    ``err`` (observation error, the reference's ``errobs``)."""
+    ``err`` (observation error, the reference's ``errobs``). ``exclude`` (an
+    :func:`l3_exclusion` table) builds the scipy operator ``Obsop_interp_l3``
+    instead (obsop.py:161-373): same misfit, same gradient of the cost, and
+    neighbours on excluded grid points dropped."""
 
-    def __init__(self, windows, ny, nx, dx, dy, dtype=torch.float32, device="cuda", npix=4, build="gpu"):
+    def __init__(self, windows, ny, nx, dx, dy, dtype=torch.float32, device="cuda", npix=4, build="gpu",
+                 exclude=None):
         if npix > 4:
             raise ValueError("at most 4 neighbours per observation")
         if build not in ("gpu", "host"):
@@ -96,7 +135,7 @@ class AlongTrackObs:
         fields, steps, idxs, ws, ys, errs = [], [], [], [], [], []
         for b, win in enumerate(windows):
             x = np.asarray(win["x_km"], dtype=np.float64)
-            idx, w = rows(x, np.asarray(win["y_km"], dtype=np.float64), ny, nx, dx, dy, npix)
+            idx, w = rows(x, np.asarray(win["y_km"], dtype=np.float64), ny, nx, dx, dy, npix, exclude=exclude)
             pad = 4 - npix
             if pad:
                 idx = np.pad(idx, ((0, 0), (0, pad)), constant_values=-1)
