@@ -107,6 +107,37 @@ size_t vd_qgt_workspace_bytes(const vd_qgt_desc* desc);
 vd_status vd_qgt_step(const vd_qgt_desc* desc, const void* h0, const void* hb, int nstep, void* h1,
                       void* work, size_t work_bytes, void* stream);
 
+/* ------------------------------------------------------------------------
+ * QG 1.5-layer model with passive tracers, forward (Qgm_trac.step,
+ * mapping/models/model_qg1l/jqgm.py:1551-2151). The SSH/PV part runs on a
+ * vd_qg1l plan built without bathymetry (its dx, dy, dt, g, f, c, Kdiffus,
+ * mask and beta); ntrac tracers per window are advected by the same
+ * third-order upwind scheme, diffused with Kdiffus_trac, zeroed on land, and
+ * after every step get boundary values (open boundaries of Mellor 1996 on
+ * the edge, or the boundary field on the ring classes) and a relaxation to
+ * the boundary field with weights wbc on rows/columns 1..n-2.
+ * ------------------------------------------------------------------------ */
+typedef struct vd_qgtrac_desc {
+    int ntrac;              /* tracers per window (0: the SSH alone) */
+    int time_scheme;        /* VD_EULER | VD_RK2 | VD_RK4 (classical Runge-Kutta 4:
+                               the reference's rk4 for this class cannot run) */
+    int advect_pv;          /* 0: the PV is only diffused (jqgm.py:1806-1815) */
+    int bc_obc;             /* 1: open boundaries ('OBC'); 0: boundary values on the rings */
+    int has_Kdiffus_trac;
+    double Kdiffus_trac;
+    const void* wbc;        /* [ny][nx] relaxation weights (plan dtype, device); needed when ntrac > 0 */
+    const void* mdt;        /* [ny][nx] mean dynamic topography (plan dtype, device) or NULL */
+} vd_qgtrac_desc;
+
+size_t vd_qgtrac_workspace_bytes(const vd_qg1l_plan* plan, const vd_qgtrac_desc* desc, int batch);
+/* nstep steps from SSH h0 [batch][ny][nx] and tracers c0 [batch][ntrac][ny][nx]
+ * with boundary fields hb, cb of the same shapes (jqgm.py:2057-2139): h1 and
+ * c1 are NaN on land, the MDT is added before and removed after. c0, cb, c1
+ * may be NULL when ntrac = 0. */
+vd_status vd_qgtrac_step(const vd_qg1l_plan* plan, const vd_qgtrac_desc* desc, int batch, const void* h0,
+                         const void* c0, const void* hb, const void* cb, int nstep, void* h1, void* c1,
+                         void* work, size_t work_bytes, void* stream);
+
 /* Build a plan: DST-I half matrices, tridiagonal multipliers, mask, beta and
  * bathymetry tables on the current device. Replaces the constant set-up of
  * Qgm.__init__ (jqgm.py:113-236). */

@@ -21,8 +21,14 @@ The model (line numbers in jqgm.py):
   or, with any other ``bc_trac``, their boundary values on the ring classes,
   then a relaxation to the boundary field with weights ``Wbc`` on the
   interior (2002-2003; ``Wbc`` defaults to 1 on class-1 points, 1657-1661);
-- Euler and rk2 time schemes (1897-1922); the reference's rk4 calls methods
-  the class does not define (1924-1955) and is not restated.
+- Euler and rk2 time schemes (1897-1922). The reference's rk4 (1924-1955)
+  cannot run: it calls ``qrhs_jit``, which the class does not define, and
+  names undefined variables. ``time_scheme='rk4'`` here is the classical
+  Runge-Kutta 4 that method sets out to be, on the stacked state [q,
+  tracers...]: k_s = dt * rhs(velocities of pv2h(q_s), state_s) with states
+  var0, var0 + k1/2, var0 + k2/2, var0 + k3 (the reference's text has var0 +
+  k2 for the last one, which is not RK4), var1 = var0 + (k1 + 2 k2 + 2 k3 +
+  k4) / 6. It is an extension, checked by its order of convergence.
 
 ``ageo_velocities`` is restated but not pinned: with it the reference's
 boundary stack holds the ageostrophic fields too (``cb = Xb[1:]``, 2079),
@@ -40,8 +46,8 @@ class QgmTracOracle(QgmOracle):
     def __init__(self, dx=None, dy=None, dt=None, SSH=None, c=None, upwind=3, g=9.81, f=1e-4,
                  time_scheme="Euler", Wbc=None, Kdiffus=None, Kdiffus_trac=None, bc_trac="OBC", mdt=None,
                  ageo_velocities=False, advect_pv=True, **kwargs):
-        if time_scheme not in ("Euler", "rk2"):
-            raise ValueError("Qgm_trac steps with 'Euler' or 'rk2' (its rk4 cannot run, jqgm.py:1924-1955)")
+        if time_scheme not in ("Euler", "rk2", "rk4"):
+            raise ValueError("Qgm_trac steps with 'Euler', 'rk2' or 'rk4' (classical, an extension)")
         super().__init__(dx=dx, dy=dy, dt=dt, SSH=SSH, c=c, Kdiffus=Kdiffus, upwind=upwind, g=g, f=f,
                          time_scheme=time_scheme, mdt=mdt)
         if Wbc is None or np.all(np.asarray(Wbc) == 0.0):
@@ -131,10 +137,17 @@ class QgmTracOracle(QgmOracle):
         incr = self.rhs_state(u, v, ua, va, var0)
         if self.time_scheme == "Euler":
             var1 = var0 + self.dt * incr
-        else:
+        elif self.time_scheme == "rk2":
             var12 = var0 + 0.5 * incr * self.dt
             u12, v12 = self.h2uv(self.pv2h(var12[0], hb, qb))
             var1 = var0 + self.dt * self.rhs_state(u12, v12, ua, va, var12)
+        else:
+            k = [incr * self.dt]
+            for a in (0.5, 0.5, 1.0):
+                vs = var0 + a * k[-1]
+                us, ws = self.h2uv(self.pv2h(vs[0], hb, qb))
+                k.append(self.rhs_state(us, ws, ua, va, vs) * self.dt)
+            var1 = var0 + (k[0] + 2 * k[1] + 2 * k[2] + k[3]) / 6.0
         h1 = self.pv2h(var1[0], hb, qb)
         ubc, vbc = (u + ua, v + va) if ua is not None else (u, v)
         return h1, self.bc(var1, var0, ubc, vbc, varb)

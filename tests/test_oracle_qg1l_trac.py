@@ -49,7 +49,28 @@ def test_fixtures_tell_the_options_apart(g, change):
     assert _rel(QgmTracOracle(**kw).step(g["b_X0"], g["b_Xb"], nstep=3), g["b_X1"]) > 1e-6
 
 
-def test_rk4_is_refused():
+def test_unknown_scheme_is_refused():
     with pytest.raises(ValueError):
         QgmTracOracle(dx=np.full((8, 8), 1e4), dy=np.full((8, 8), 1e4), dt=900.0, SSH=np.zeros((8, 8)), c=2.7,
-                      time_scheme="rk4")
+                      time_scheme="rk3")
+
+
+def test_rk4_extension_is_fourth_order():
+    """The classical RK4 extension converges at fourth order in dt (error
+    ratio 16 per halving), rk2 at second order (ratio 4). The flow is an
+    eddy on a uniform current, so that no velocity changes sign: the upwind
+    split max(u, 0) has a kink at u = 0 that lowers the order of any
+    Runge-Kutta scheme."""
+    ny, nx, d = 30, 34, 1.0e4
+    jj, ii = np.mgrid[0:ny, 0:nx]
+    ssh = 0.5e-6 * d * (ii - jj) + 0.01 * np.exp(-(((ii - 17) / 5.0) ** 2 + ((jj - 15) / 5.0) ** 2))
+
+    def run(scheme, dt, T=43200.0):
+        o = QgmTracOracle(dx=np.full((ny, nx), d), dy=np.full((ny, nx), d), dt=dt, SSH=ssh, c=2.7, g=9.81,
+                          f=1.0e-4, time_scheme=scheme)
+        return o.step(ssh, ssh, nstep=int(round(T / dt)))
+    fine = run("rk4", 675.0)
+    e4 = [np.abs(run("rk4", dt) - fine).max() for dt in (10800.0, 5400.0, 2700.0)]
+    assert all(14.0 < e4[k] / e4[k + 1] < 18.0 for k in range(2))
+    e2 = [np.abs(run("rk2", dt) - fine).max() for dt in (2700.0, 1350.0)]
+    assert 3.5 < e2[0] / e2[1] < 4.5

@@ -100,6 +100,15 @@ class VdQgtDesc(ctypes.Structure):
     ]
 
 
+class VdQgtracDesc(ctypes.Structure):
+    """vd_qgtrac_desc: wbc and mdt are device pointers (c_void_p)."""
+    _fields_ = [
+        ("ntrac", ctypes.c_int), ("time_scheme", ctypes.c_int), ("advect_pv", ctypes.c_int),
+        ("bc_obc", ctypes.c_int), ("has_Kdiffus_trac", ctypes.c_int), ("Kdiffus_trac", ctypes.c_double),
+        ("wbc", ctypes.c_void_p), ("mdt", ctypes.c_void_p),
+    ]
+
+
 class VdSwDesc(ctypes.Structure):
     _fields_ = [
         ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nl", ctypes.c_int), ("dtype", ctypes.c_int),
@@ -145,6 +154,8 @@ SIGNATURES = {
     "vd_qgt_shared_bytes": (SZ, [I, I]),
     "vd_qgt_workspace_bytes": (SZ, [ctypes.POINTER(VdQgtDesc)]),
     "vd_qgt_step": (I, [ctypes.POINTER(VdQgtDesc), P, P, I, P, P, SZ, P]),
+    "vd_qgtrac_workspace_bytes": (SZ, [P, ctypes.POINTER(VdQgtracDesc), I]),
+    "vd_qgtrac_step": (I, [P, ctypes.POINTER(VdQgtracDesc), I, P, P, P, P, I, P, P, P, SZ, P]),
     "vd_qg1l_plan_destroy": (I, [P]),
     "vd_qg1l_workspace_bytes": (SZ, [P, I]),
     "vd_qg1l_traj_bytes": (SZ, [P, I, I]),

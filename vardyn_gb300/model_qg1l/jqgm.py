@@ -320,3 +320,113 @@ class QgmWithTiles:
 
     def step_adj(self, adh0, h0, hb, nstep=1):
         raise NotImplementedError("adjoint of QgmWithTiles (jax.vjp of the blended step) is not built")
+
+
+class Qgm_trac(Qgm):
+    """QG 1.5-layer model with passive tracers, with the constructor of
+    jqgm.py:1553-1697. ``step(X0, Xb, nstep)`` runs on the GPU
+    (vd_qgtrac_step): X0 is the SSH [ny, nx], or [SSH, tracers...] stacked
+    [1 + ntrac, ny, nx], Xb the boundary fields of the same shape; the result
+    has the shape of X0, NaN on land (jqgm.py:2057-2139).
+
+    - ``Wbc``: relaxation weights on rows/columns 1..n-2 (None or all zero: 1
+      on the outer ring class, jqgm.py:1657-1661);
+    - ``bc_trac``: 'OBC' for the open boundaries of Mellor (1996) on the
+      edge, anything else for the boundary values on the ring classes;
+    - ``advect_pv``: False leaves the PV only diffused;
+    - ``time_scheme``: 'Euler', 'rk2', or 'rk4', the classical Runge-Kutta 4
+      that the reference's rk4 for this class sets out to be (that one
+      cannot run, jqgm.py:1924-1955).
+
+    Not built: ``ageo_velocities`` (the reference's boundary stack then holds
+    the ageostrophic fields, jqgm.py:2079, and its boundary loop indexes past
+    the tracers), and the tangent linear and adjoint: they raise."""
+
+    def __init__(self, dx=None, dy=None, dt=None, SSH=None, c=None, upwind=3, g=9.81, f=1e-4,
+                 time_scheme="Euler", Wbc=None, Kdiffus=None, Kdiffus_trac=None, bc_trac="OBC", mdt=None,
+                 ageo_velocities=False, advect_pv=True, dtype=None, device=None, **kwargs):
+        from vardyn_gb300 import _lib
+        if time_scheme not in ("Euler", "rk2", "rk4"):
+            raise ValueError("Qgm_trac steps with 'Euler', 'rk2' or 'rk4'")
+        if ageo_velocities:
+            raise NotImplementedError("Qgm_trac with ageo_velocities is not built")
+        super().__init__(dx=dx, dy=dy, dt=dt, SSH=SSH, c=c, Kdiffus=Kdiffus, upwind=upwind, g=g, f=f,
+                         time_scheme=time_scheme, mdt=mdt, dtype=dtype, device=device)
+        self._lib = _lib
+        ny, nx = self.ny, self.nx
+        if Wbc is None or np.all(np.asarray(Wbc) == 0.0):
+            w = np.zeros((ny, nx))
+            w[self.mask == 1] = 1.0
+        else:
+            w = np.asarray(Wbc, dtype=np.float64)
+        self.Wbc = self._to_dev(w)
+        self.Kdiffus_trac = Kdiffus_trac
+        self.bc_trac = bc_trac
+        self.advect_pv = bool(advect_pv)
+        self.ageo_velocities = False
+        self._ws = {}
+
+    def _desc(self, ntrac):
+        d = self._lib.VdQgtracDesc()
+        d.ntrac = int(ntrac)
+        d.time_scheme = self._lib.SCHEMES[self.time_scheme]
+        d.advect_pv = 1 if self.advect_pv else 0
+        d.bc_obc = 1 if self.bc_trac == "OBC" else 0
+        d.has_Kdiffus_trac = 0 if self.Kdiffus_trac is None else 1
+        d.Kdiffus_trac = 0.0 if self.Kdiffus_trac is None else float(self.Kdiffus_trac)
+        d.wbc = self.Wbc.data_ptr()
+        d.mdt = None if self._mdt is None else self._mdt.data_ptr()
+        return d
+
+    def step_windows(self, h0, c0, hb, cb, nstep=1):
+        """Batched step on device tensors: h0, hb [B, ny, nx]; c0, cb
+        [B, ntrac, ny, nx] (ntrac may be 0). Returns (h1, c1)."""
+        h0, hb = self._to_dev(h0), self._to_dev(hb)
+        c0, cb = self._to_dev(c0), self._to_dev(cb)
+        B = h0.shape[0]
+        if h0.dim() != 3 or hb.shape != h0.shape or h0.shape[1:] != (self.ny, self.nx):
+            raise ValueError("h0 and hb must be [B, ny, nx] on the model grid")
+        if c0.dim() != 4 or cb.shape != c0.shape or c0.shape[0] != B or c0.shape[2:] != (self.ny, self.nx):
+            raise ValueError("c0 and cb must be [B, ntrac, ny, nx] with the batch of h0")
+        nt = c0.shape[1]
+        d = self._desc(nt)
+        key = (B, nt)
+        ws = self._ws.get(key)
+        if ws is None:
+            nbytes = self._lib.load().vd_qgtrac_workspace_bytes(self.plan.handle, ctypes.byref(d), B)
+            if nbytes == 0:
+                raise ValueError("vd_qgtrac_workspace_bytes rejected the configuration")
+            ws = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+            self._ws[key] = ws
+        h1 = torch.empty_like(h0)
+        c1 = torch.empty_like(c0)
+        p = (lambda t: ctypes.c_void_p(t.data_ptr() if t.numel() else None))
+        self._lib.call("vd_qgtrac_step", self.plan.handle, ctypes.byref(d), B, p(h0), p(c0), p(hb), p(cb),
+                       int(nstep), p(h1), p(c1), p(ws), ws.numel(),
+                       ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream))
+        return h1, c1
+
+    def step(self, X0, Xb, nstep=1):
+        """nstep steps from X0 with boundary fields Xb (jqgm.py:2057-2139)."""
+        X, XB = self._to_dev(X0), self._to_dev(Xb)
+        if X.shape != XB.shape:
+            raise ValueError("X0 and Xb must have the same shape")
+        if X.dim() == 2:
+            h1, _ = self.step_windows(X[None], X.new_empty((1, 0) + X.shape), XB[None],
+                                      XB.new_empty((1, 0) + XB.shape), nstep)
+            out = h1[0]
+        elif X.dim() == 3:
+            h1, c1 = self.step_windows(X[:1], X[None, 1:], XB[:1], XB[None, 1:], nstep)
+            out = torch.cat([h1, c1[0]], dim=0)
+        else:
+            raise ValueError("X0 is [ny, nx] or [1 + ntrac, ny, nx]")
+        return out if isinstance(X0, torch.Tensor) else out.cpu().numpy()
+
+    def rhs(self, *args, **kwargs):
+        raise NotImplementedError("Qgm_trac.rhs takes the stacked state; the GPU step fuses it")
+
+    def step_tgl(self, *args, **kwargs):
+        raise NotImplementedError("Qgm_trac tangent linear is not built")
+
+    def step_adj(self, *args, **kwargs):
+        raise NotImplementedError("Qgm_trac adjoint is not built")
