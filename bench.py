@@ -286,6 +286,7 @@ def gpu_arm(args):
         rank, world = tdist.get_rank(), tdist.get_world_size()
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", rank)))
     from vardyn_gb300 import build, _lib
+    from vardyn_gb300.shard import max_over_ranks
     build.build()
     L = _lib.load()
     n = args.size
@@ -309,9 +310,7 @@ def gpu_arm(args):
     sampler = ClockSampler() if rank == 0 else None
     ms, clocks = time_graph(eng, x, args.warmup, args.steps, sampler)
     if dist:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t)
+        ms = max_over_ranks(ms, device="cuda")
     value = world * B / (ms / 1e3)
 
     # e2e through the public API: pinned host h0 -> device, evaluation,
@@ -331,6 +330,8 @@ def gpu_arm(args):
     for _ in range(max(1, args.warmup // 2)):
         e2e_step()
     torch.cuda.synchronize()
+    if dist:
+        torch.distributed.barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(st)
     ke = max(2, args.steps // 2)
@@ -339,6 +340,8 @@ def gpu_arm(args):
     e1.record(st)
     torch.cuda.synchronize()
     ms_e2e = e0.elapsed_time(e1) / ke
+    if dist:
+        ms_e2e = max_over_ranks(ms_e2e, device="cuda")
     e2e = {"value": world * B / (ms_e2e / 1e3), "unit": UNIT, "h2d_bytes_per_step": B * F,
            "d2h_bytes_per_step": B * F + B * 8,
            "path": "QGWindows4DVar.cost_and_grad (ctypes -> libvardyn_gb300 C ABI), pinned host buffers"}
@@ -579,15 +582,32 @@ M4_WINDOWS, M4_NSTEP, M4_NOBS, M4_SEED = 64, 960, 5000, 4000
 M4_METRIC = "4D-Var cost+grad evals/sec, QG1.5L 64 windows of sides 128..768, 10-day windows"
 
 
-def setup_mixed(nstep, windows=M4_WINDOWS):
+def mixed_windows(nstep, rank=0, world=1, windows=M4_WINDOWS):
+    """The windows of the mixed workload that rank ``rank`` of ``world``
+    runs: {side: [ordinal of the window among the windows of that side]}.
+    Sides are drawn once for the whole set, so a window (side, ordinal) and
+    its seeds are the same at any number of ranks; windows go to ranks by
+    greedy bin-packing of side^2 * nstep (vardyn_gb300.shard.assign)."""
+    from vardyn_gb300.shard import assign, window_cost
+    sides = [int(n) for n in np.random.default_rng(M4_SEED).choice(M4_SIDES, size=windows)]
+    owner, _ = assign([window_cost(n, n, nstep) for n in sides], world)
+    seen, mine = {}, {}
+    for n, r in zip(sides, owner):
+        k = seen.get(n, 0)
+        seen[n] = k + 1
+        if r == rank:
+            mine.setdefault(n, []).append(k)
+    return {n: mine[n] for n in M4_SIDES if n in mine}
+
+
+def setup_mixed(nstep, windows=M4_WINDOWS, rank=0, world=1):
     import torch
     from vardyn_gb300.fourdvar import MixedWindows4DVar, QGWindows4DVar
     from vardyn_gb300.obsop import AlongTrackObs
     from vardyn_gb300.qg1l import QG1LPlan
     from vardyn_gb300.synthetic import kminus3_ssh, satellite_tracks
-    rng = np.random.default_rng(M4_SEED)
-    sides = rng.choice(M4_SIDES, size=windows)
-    counts = {int(n): int((sides == n).sum()) for n in M4_SIDES if (sides == n).any()}
+    ordinals = mixed_windows(nstep, rank, world, windows)
+    counts = {n: len(k) for n, k in ordinals.items()}
     free, _ = torch.cuda.mem_get_info()
     # full trajectories where they fit in 60 % of the free memory, else
     # checkpoints for the largest classes first
@@ -603,7 +623,7 @@ def setup_mixed(nstep, windows=M4_WINDOWS):
     engines, guesses, win_sets = [], [], []
     for n, B in counts.items():
         truths, g0, wins = [], [], []
-        for b in range(B):
+        for b in ordinals[n]:
             r = np.random.default_rng(M4_SEED + 1000 * n + b)
             truths.append(kminus3_ssh(n, n, DX, DX, r, rms=0.1, cutoff_km=50.0))
             g0.append(kminus3_ssh(n, n, DX, DX, r, rms=0.1, cutoff_km=50.0))
@@ -638,6 +658,14 @@ def gpu_arm_mixed(args):
     import torch
     from vardyn_gb300 import build, _lib
     from vardyn_gb300.fourdvar import QGWindows4DVar
+    from vardyn_gb300.shard import max_over_ranks
+    dist = args.gpus > 1 or "RANK" in os.environ
+    rank, world = 0, 1
+    if dist:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl")
+        rank, world = tdist.get_rank(), tdist.get_world_size()
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", rank)))
     build.build()
     L = _lib.load()
     nstep = 64 if args.profile_small else (M4_NSTEP if args.nstep == NSTEP else args.nstep)
@@ -646,7 +674,7 @@ def gpu_arm_mixed(args):
     if os.path.exists(pk):
         peaks = json.load(open(pk))
     from vardyn_gb300.obsop import AlongTrackObs
-    mixed, guesses, counts, ckpt, win_sets = setup_mixed(nstep)
+    mixed, guesses, counts, ckpt, win_sets = setup_mixed(nstep, rank=rank, world=world)
     xs = [torch.as_tensor(g, dtype=torch.float32, device="cuda") for g in guesses]
     c0 = L.vd_launch_count()
     mixed.capture()
@@ -654,18 +682,23 @@ def gpu_arm_mixed(args):
     for _ in range(args.warmup):
         mixed.cost_and_grad(xs)
     torch.cuda.synchronize()
+    if dist:
+        torch.distributed.barrier()
     st = torch.cuda.current_stream()
-    sampler = ClockSampler()
+    sampler = ClockSampler() if rank == 0 else None
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    sampler.start()
+    if sampler:
+        sampler.start()
     e0.record(st)
     for _ in range(args.steps):
         mixed.cost_and_grad(xs)
     e1.record(st)
     torch.cuda.synchronize()
-    clocks = sampler.stop()
+    clocks = sampler.stop() if sampler else None
     ms = e0.elapsed_time(e1) / args.steps
-    nwin = sum(counts.values())
+    if dist:
+        ms = max_over_ranks(ms, device="cuda")
+    nwin = M4_WINDOWS                      # all ranks together run the whole set
     value = nwin / (ms / 1e3)
     # e2e: pinned host controls in, J and gradients out, every step
     hx = [torch.as_tensor(g, dtype=torch.float32).pin_memory() for g in guesses]
@@ -682,6 +715,8 @@ def gpu_arm_mixed(args):
             j.copy_(J, non_blocking=True)
     e2e_step()
     torch.cuda.synchronize()
+    if dist:
+        torch.distributed.barrier()
     ke = max(2, args.steps // 2)
     e0.record(st)
     for _ in range(ke):
@@ -689,11 +724,14 @@ def gpu_arm_mixed(args):
     e1.record(st)
     torch.cuda.synchronize()
     ms_e2e = e0.elapsed_time(e1) / ke
+    if dist:
+        ms_e2e = max_over_ranks(ms_e2e, device="cuda")
     bytes_io = sum(h.numel() * 4 for h in hx)
     # plain form: one window of each size alone, no graph, scaled by the counts
+    # (on one GPU only: under torchrun each rank holds a part of the set)
     plain_s = 0.0
     plain_detail = {}
-    if not args.no_plain:
+    if not args.no_plain and world == 1:
         for eng, g, wins in zip(mixed.engines, guesses, win_sets):
             n = eng.plan.nx
             o1 = AlongTrackObs(wins[:1], n, n, DX, DX, dtype=torch.float32)
@@ -710,18 +748,20 @@ def gpu_arm_mixed(args):
             plain_s += dt1 * counts[n]
             del e1w
     line = {
-        "metric": M4_METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "metric": M4_METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "strong",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"QG1.5L, {nwin} windows with sides drawn from {M4_SIDES} (seed {M4_SEED}), "
                                f"dx=5km dt=900s rk2, {nstep}-step windows, {M4_NOBS} obs each, control h0; "
                                f"one batched engine per size on its own stream, all captured as one CUDA graph",
-                   "windows_per_side": counts,
+                   "windows_per_side": {n: len(k) for n, k in mixed_windows(nstep).items()},
+                   "parallelism": (f"replicas x{world}: windows split over ranks by greedy bin-packing of "
+                                   f"side^2*nstep, rank 0 runs {counts}") if world > 1 else "one GPU",
                    "trajectory": {str(n): ("full" if ckpt[n] is None else f"checkpoint every {ckpt[n]} steps")
                                   for n in counts},
                    "l2": f"inputs larger than L2: {mixed.memory_bytes() / 1e9:.1f} GB of trajectories"},
         "e2e": {"value": nwin / (ms_e2e / 1e3), "unit": UNIT, "h2d_bytes_per_step": bytes_io,
-                "d2h_bytes_per_step": bytes_io + 8 * nwin,
+                "d2h_bytes_per_step": bytes_io + 8 * sum(counts.values()),
                 "path": "MixedWindows4DVar.cost_and_grad (ctypes -> libvardyn_gb300 C ABI), pinned host buffers"},
         "gpu_launches": int(launches_per_eval * args.steps),
         "clocks": clocks,
@@ -729,7 +769,10 @@ def gpu_arm_mixed(args):
         "batched_over_plain": (value * plain_s / nwin) if plain_s else None,
         "plain_seconds_per_window": {str(k): v for k, v in plain_detail.items()},
     }
-    print(json.dumps(line))
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        torch.distributed.destroy_process_group()
 
 
 # ----------------------------------------------------------------------------
