@@ -17,9 +17,10 @@ systems shares the grid and the coefficient; system b uses lambda[b]
   hierarchies                248-293
   V_cycle / FMG_Helmholtz    322-419
 
-Parity status: unpinned by reference data (jax is not importable); pinned by
-the solution of the assembled operator (scipy spsolve) after convergence and
-by the GPU kernels' agreement with this restatement.
+Parity status: pinned to solutions of the reference's own
+helmholtz_multigrid.py run with a NumPy stand-in for jax
+(tests/golden/gen_golden_mg.py, ≤1e-12), and to the solution of the
+assembled operator (scipy spsolve) after convergence.
 """
 import numpy as np
 

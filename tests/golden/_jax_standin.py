@@ -121,6 +121,14 @@ def _softplus(x):
     return np.logaddexp(np.asarray(x), 0.0).view(JArray)
 
 
+def _fori_loop(lower, upper, body, init):
+    """jax.lax.fori_loop as the plain loop it denotes."""
+    val = init
+    for i in range(int(lower), int(upper)):
+        val = body(i, val)
+    return val
+
+
 def _unavailable(*args, **kwargs):
     raise NotImplementedError("not available in the NumPy stand-in")
 
@@ -177,7 +185,7 @@ def install(enable_x64=True):
     cfg = types.SimpleNamespace(update=lambda *a, **k: None)
     jax.config = cfg
     lax = types.ModuleType("jax.lax")
-    lax.fori_loop = _unavailable
+    lax.fori_loop = _fori_loop
     lax.dynamic_slice = _dynamic_slice
     lax.dynamic_update_slice = _dynamic_update_slice
     lax.scan = _scan
