@@ -52,3 +52,20 @@ def test_wave_packet_projection_and_transpose_match_reference():
         plan.project_T(int(k), torch.as_tensor(g[f"t{k}_ad"], device="cuda")[None].contiguous(), adX)
         want_ad = g[f"t{k}_adX"]
         assert np.abs(adX[0].cpu().numpy() - want_ad).max() <= 1e-12 * np.abs(want_ad).max()
+
+
+def test_wavelet_projection_and_transpose_match_reference():
+    from test_oracle_wavelet_golden import WAV
+    from vardyn_gb300.basis import WaveletParams, WaveletPlan
+    g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "wavelet_golden.npz")))
+    plan = WaveletPlan(g["lon"], g["lat"], g["time"], WaveletParams(**WAV), land=g["mask"], geographic=True,
+                       dtype=torch.float64)
+    X = torch.as_tensor(g["X"], device="cuda")[None].contiguous()
+    for k in g["times_k"]:
+        phi = plan.project(int(k), X)[0].cpu().numpy()
+        want = g[f"t{k}_phi"]
+        assert np.abs(phi - want).max() <= 1e-12 * np.abs(want).max()
+        adX = torch.zeros_like(X)
+        plan.project_T(int(k), torch.as_tensor(g[f"t{k}_ad"], device="cuda")[None].contiguous(), adX)
+        want_ad = g[f"t{k}_adX"]
+        assert np.abs(adX[0].cpu().numpy() - want_ad).max() <= 1e-12 * np.abs(want_ad).max()
