@@ -6,6 +6,8 @@ import re
 
 import pytest
 
+from vardyn_gb300 import _lib
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "vardyn_gb300.h")
 
@@ -49,4 +51,13 @@ def test_null_arguments_are_rejected_without_gpu(lib):
     # argument validation happens before any CUDA call
     assert lib.vd_qg1l_plan_create(None, None) == 1
     assert lib.vd_obs_misfit(7, 1, None, 0, None, None, None, None, None, None, None) == 1
+    d = _lib.VdQgtracDesc()
+    d.ntrac, d.time_scheme = 1, _lib.VD_RK2
+    # no plan, an unknown scheme, a tracer model without relaxation weights
+    assert lib.vd_qgtrac_workspace_bytes(None, ctypes.byref(d), 1) == 0
+    assert lib.vd_qgtrac_step(None, ctypes.byref(d), 1, None, None, None, None, 1, None, None, None, 0, None) == 1
+    # npix out of range, non-positive spacing
+    assert lib.vd_obs_knn_excl(1, None, None, 4, 4, 1.0, 1.0, 5, 2.0, None, None, None, None) == 1
+    assert lib.vd_obs_knn_excl(1, None, None, 4, 4, 0.0, 1.0, 4, 2.0, None, None, None, None) == 1
+    assert lib.vd_obs_knn_excl(0, None, None, 4, 4, 1.0, 1.0, 4, 2.0, None, None, None, None) == 0
     assert lib.vd_qg1l_workspace_bytes(None, 4) == 0
