@@ -359,6 +359,10 @@ class Qgm_trac(Qgm):
             w[self.mask == 1] = 1.0
         else:
             w = np.asarray(Wbc, dtype=np.float64)
+        if w.shape != (ny, nx):
+            raise ValueError(f"Wbc must be [ny, nx] = {(ny, nx)}, got {w.shape}")
+        if self._mdt is not None and tuple(self._mdt.shape) != (ny, nx):
+            raise ValueError(f"mdt must be [ny, nx] = {(ny, nx)}, got {tuple(self._mdt.shape)}")
         self.Wbc = self._to_dev(w)
         self.Kdiffus_trac = Kdiffus_trac
         self.bc_trac = bc_trac
