@@ -6,6 +6,7 @@
 // adjoint through jax.vjp (630-678); cost terms of
 // mapping/src/tools_4Dvar.py:252-400 (Jo = misfit.R^-1.misfit, Jb = X0.X0).
 #include "vd_internal.cuh"
+#include "vd_obs_knn.cuh"
 
 namespace vd {
 
@@ -309,14 +310,8 @@ extern "C" vd_status vd_diag_axpy(int dtype, long long n, long long period, cons
 }
 
 // ---------------------------------------------------------------------------
-// Observation-operator construction (obsop.py:417-460, _sparse_op): the npix
-// nearest grid points of each observation and their normalised Gaussian
-// weights exp(-D^2 / (2 (dmax/2)^2)), neighbours beyond dmax dropped. On a
-// uniform planar grid (point (i, j) at (i dx, j dy) km) every neighbour that
-// survives the dmax test lies within dmax of the observation, so scanning the
-// grid points of that disc and keeping the npix nearest gives exactly the
-// valid neighbours of a k-nearest search. Ties in distance go to the smaller
-// flat index.
+// Observation-operator construction: one thread per observation runs the
+// neighbour search of vd_obs_knn.cuh.
 // ---------------------------------------------------------------------------
 namespace vd {
 __global__ void k_obs_knn(long long nobs, const double* __restrict__ x, const double* __restrict__ y, int ny, int nx,
@@ -325,55 +320,7 @@ __global__ void k_obs_knn(long long nobs, const double* __restrict__ x, const do
 {
     const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= nobs) return;
-    const double xo = x[o], yo = y[o];
-    double bd[4];
-    long long bi[4];
-    for (int k = 0; k < 4; ++k) {
-        bd[k] = INFINITY;
-        bi[k] = -1;
-    }
-    const double d2max = dmax * dmax;
-    const int rx = (int)ceil(dmax / dx) + 1, ry = (int)ceil(dmax / dy) + 1;
-    const double fx = floor(xo / dx), fy = floor(yo / dy);
-    // the disc may lie outside the grid: clamp the scan box in double first
-    const double i0d = fmax(fx - rx, 0.0), i1d = fmin(fx + rx + 1, (double)(nx - 1));
-    const double j0d = fmax(fy - ry, 0.0), j1d = fmin(fy + ry + 1, (double)(ny - 1));
-    if (i0d <= i1d && j0d <= j1d) {
-        const int i0 = (int)i0d, i1 = (int)i1d, j0 = (int)j0d, j1 = (int)j1d;
-        for (int j = j0; j <= j1; ++j) {
-            const double ey = (double)j * dy - yo;
-            for (int i = i0; i <= i1; ++i) {
-                const double ex = (double)i * dx - xo;
-                const double d2 = ex * ex + ey * ey;
-                if (d2 > d2max) continue;
-                const long long fi = (long long)j * nx + i;
-                // insertion into the sorted npix-best list (distance, then index)
-                int p = npix;
-                while (p > 0 && (d2 < bd[p - 1] || (d2 == bd[p - 1] && fi < bi[p - 1]))) --p;
-                if (p >= npix) continue;
-                for (int k = npix - 1; k > p; --k) {
-                    bd[k] = bd[k - 1];
-                    bi[k] = bi[k - 1];
-                }
-                bd[p] = d2;
-                bi[p] = fi;
-            }
-        }
-    }
-    double D[4], ww[4], s = 0.0;
-    const double c = 2.0 * (0.5 * dmax) * (0.5 * dmax);
-    for (int k = 0; k < npix; ++k) {
-        D[k] = sqrt(bd[k]);
-        // an excluded point keeps its place among the npix nearest but gets no weight
-        const bool valid = bi[k] >= 0 && D[k] <= dmax && !(excl && excl[bi[k]]);
-        ww[k] = npix > 1 ? (valid ? exp(-D[k] * D[k] / c) : 0.0) : (valid ? 1.0 : 0.0);
-        if (!valid) bi[k] = -1;
-    }
-    for (int k = 0; k < npix; ++k) s += ww[k];
-    for (int k = 0; k < 4; ++k) {
-        idx[o * 4 + k] = k < npix ? bi[k] : -1;
-        w[o * 4 + k] = k < npix ? (npix > 1 ? (s > 0 ? ww[k] / s : 0.0) : ww[k]) : 0.0;
-    }
+    obs_knn_point(x[o], y[o], ny, nx, dx, dy, npix, dmax, excl, idx + o * 4, w + o * 4);
 }
 }  // namespace vd
 
