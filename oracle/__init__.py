@@ -5,11 +5,18 @@ This package is the checker, never the product: only ``tests/``,
 import it. It is a float64 NumPy/SciPy restatement of the reference's algorithms,
 with every function citing the reference file:line it follows.
 
-Parity pin: the QG 1.5-layer forward restatement (``oracle.qg1l``) is pinned
-against golden vectors produced by the reference's own ``jqgm.py`` source
-executed with a NumPy stand-in for ``jax`` (``tests/golden/gen_golden.py``).
-The tangent/adjoint restatements are pinned by finite differences of that
-pinned forward and by dot-product tests. The observation operator and the
-4D-Var cost/gradient are restatements pinned by properties only (the reference
-ships no golden values and jax is not importable): parity there is unpinned.
+Parity pins: restatements checked against golden vectors produced by the
+reference's own source files, loaded unmodified and executed with a NumPy
+stand-in for ``jax`` (``tests/golden/gen_golden*.py``):
+- the QG 1.5-layer family (``qg1l``, ``qg1l_tiles``, ``qg1l_trac``);
+- the spectral and multigrid Helmholtz solvers (``helmholtz_dst``,
+  ``helmholtz_mg``);
+- the shallow-water model and the QG projector (``sw``, ``qg_ml``);
+- both observation operators (``obsop``);
+- the Gaussian, wave-packet and wavelet bases (``basis``).
+
+The tangent/adjoint restatements are pinned by finite differences of the
+pinned forwards and by dot-product tests. The 4D-Var cost/gradient assembly
+(``fourdvar``) is pinned by properties only: producing the reference's needs
+jax's vjp.
 """
