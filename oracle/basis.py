@@ -17,10 +17,11 @@ Two coordinate forms:
   geo=False  planar x/y in km for the Cartesian synthetic grids: the same
              formulas with km2deg = 1, cos(lat) = 1 and no wrap.
 
-Parity status: unpinned by reference data (the reference needs jax, xarray
-and netCDF inputs, none importable here); pinned by the transpose
-(dot-product) identity, by the analytic footprint values and by the GPU
-kernels' agreement with this restatement.
+Parity status: pinned to golden vectors produced by the reference's own
+Basis_gauss3d, Basis_bm and Basis_wavelet3d on a lon/lat grid with land
+(tests/golden/gen_golden_basis.py, gen_golden_bm.py, gen_golden_wavelet.py;
+G and G^T <= 1e-13), and checked by the transpose (dot-product) identity and
+the analytic footprint values.
 """
 import numpy as np
 from scipy.sparse import csc_matrix

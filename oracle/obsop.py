@@ -7,9 +7,12 @@ Planar coordinates: the reference maps lon/lat to 3-D Cartesian km
 (grid.geo2cart, obsop.py:421-422) before its KDTree query; the synthetic
 Cartesian grids here use planar x/y in km directly, with the same
 Npix-nearest search, distance cut ``dmax`` (obsop.py:406) and Gaussian weights
-(obsop.py:433-445). Parity: unpinned (the reference ships no golden values for
-this operator and jax is not importable); checked by transposition and
-finite-difference tests.
+(obsop.py:433-445). The ``*_points`` forms take any Cartesian coordinates,
+and ``geo2cart`` restates grid.py:61-98. Parity: the neighbours, weights,
+dmax, exclusions and ``geo2cart`` are pinned to golden vectors produced by the
+reference's own obsop.py and grid.py on a lon/lat grid
+(tests/golden/gen_golden_obs.py); the misfit and its adjoint are checked by
+transposition and finite differences.
 """
 import numpy as np
 from scipy.spatial import cKDTree
