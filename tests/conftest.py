@@ -10,12 +10,6 @@ if ROOT not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
-    config.addinivalue_line("markers", "last: runs after every other test (GPU paths not yet run on a GB300, "
-                                       "so that a failure under -x does not stop the established suites)")
-
-
-def pytest_collection_modifyitems(config, items):
-    items.sort(key=lambda it: it.get_closest_marker("last") is not None)   # stable: order kept within groups
 
 
 @pytest.fixture(scope="session")

@@ -10,7 +10,7 @@ from test_gpu_basis import make as basis_case
 from test_gpu_fourdvar import engine_case
 from test_gpu_sw import GOLD as SW_GOLD, plan_a as sw_plan_a
 
-pytestmark = [pytest.mark.gpu, pytest.mark.last]
+pytestmark = pytest.mark.gpu
 
 
 def close(a, b, tol):
@@ -51,7 +51,7 @@ def test_fourdvar_cost_backward_and_torch_optimiser():
     (2.0 * J).sum().backward()
     _, G = eng.cost_and_grad(x.detach())
     assert close(x.grad, 2.0 * G, 1e-12)
-    J0 = float(J.sum())
+    J0 = float(J.detach().sum())
     x2 = torch.as_tensor(h0, device="cuda").requires_grad_()
     opt = torch.optim.LBFGS([x2], max_iter=8, line_search_fn="strong_wolfe")
 

@@ -10,7 +10,7 @@ import torch
 
 from test_oracle_basis_golden import COMPS
 
-pytestmark = [pytest.mark.gpu, pytest.mark.last]
+pytestmark = pytest.mark.gpu
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden", "basis_golden.npz")
 

@@ -6,7 +6,7 @@ import os
 import numpy as np
 import pytest
 
-pytestmark = [pytest.mark.gpu, pytest.mark.last]
+pytestmark = pytest.mark.gpu
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden", "mg_golden.npz")
 

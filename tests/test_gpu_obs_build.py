@@ -49,7 +49,6 @@ def test_obs_operator_same_either_build():
     assert (a.d_w4 - b.d_w4).abs().max().item() <= 1e-14
 
 
-@pytest.mark.last
 @pytest.mark.parametrize("npix", [1, 4])
 def test_knn_with_exclusion_matches_host(npix):
     """The scipy operator's rules (Obsop_interp_l3, obsop.py:197-219): ring
