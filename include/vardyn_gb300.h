@@ -179,7 +179,9 @@ vd_status vd_qg1l_pv2h(const vd_qg1l_plan* plan, int batch, const void* q,
  * return VD_ERR_SIZE. The first call on a device looks up that array's
  * device address, so make it before capturing a stream. All calls share the
  * array: calls that may overlap on the GPU (other streams, other threads)
- * race on it and must be serialised by the caller. */
+ * race on it and must be serialised by the caller. The device address is
+ * cached per device ordinal for the life of the process, so a device reset
+ * (cudaDeviceReset) while the library is loaded is not supported. */
 size_t vd_qg1l_pv2h_noalloc_max_bytes(void);
 vd_status vd_qg1l_pv2h_noalloc(const vd_qg1l_plan* plan, int batch, const void* q,
                                const void* hb, const void* qb, void* h,
@@ -222,16 +224,26 @@ vd_status vd_qg1l_step_adj(const vd_qg1l_plan* plan, int batch, const void* adh1
 
 /* Lower-level state API used by the 4D-Var window engine: the state is the
  * pair (h, q) of Qgm.one_step (jqgm.py:480-503). */
-/* q = h2pv(h, hb) and qb = h2pv(hb, hb) (jqgm.py:536-537). */
+/* q = h2pv(h, hb) and qb = h2pv(hb, hb) (jqgm.py:536-537). qlo (nullable,
+ * [batch][ny][nx]): for float32 plans, the PV is evaluated in float64 and
+ * returned as the unevaluated pair q + qlo, the start of a compensated state
+ * (see vd_qg1l_advance). */
 vd_status vd_qg1l_init_state(const vd_qg1l_plan* plan, int batch, const void* h,
-                             const void* hb, void* q, void* qb, void* stream);
+                             const void* hb, void* q, void* qb, void* qlo,
+                             void* stream);
 /* nstep steps from traj slot (first_step*nstage) onwards; the starting state
  * must already be in that slot. Writes every stage slot and the slot of the
  * state after the last step. hb and qb may be NULL when the background SSH
- * is zero (then qb == 0 too); the solves then skip them. */
+ * is zero (then qb == 0 too); the solves then skip them.
+ * qlo (nullable, [batch][ny][nx], updated in place): the low part of a
+ * compensated PV state. The last stage of every step adds its increment to
+ * the pair q + qlo with an error-free sum, so the roundings of a long window
+ * do not accumulate in the trajectory (float32 plans; the library's own
+ * steps always use it for float32 and never for float64, whose arithmetic
+ * follows the reference's). NULL steps with plain arithmetic. */
 vd_status vd_qg1l_advance(const vd_qg1l_plan* plan, int batch, void* traj,
                           int traj_steps, int first_step, int nstep,
-                          const void* hb, const void* qb, void* work,
+                          const void* hb, const void* qb, void* qlo, void* work,
                           size_t work_bytes, void* stream);
 /* Reverse of vd_qg1l_advance over the same steps: (adh, adq) holds the
  * adjoint of the state after step first_step+nstep-1 on entry and of the

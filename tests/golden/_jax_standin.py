@@ -166,6 +166,18 @@ def _dynamic_update_slice(operand, update, start_indices):
     return x.view(JArray)
 
 
+def reference_root():
+    """Path of the VarDyn checkout whose files a generator loads: the first
+    command-line argument, else the VARDYN_REFERENCE environment variable."""
+    import os
+    if len(sys.argv) > 1:
+        return sys.argv[1]
+    root = os.environ.get("VARDYN_REFERENCE")
+    if not root:
+        raise SystemExit("usage: python %s <VarDyn checkout>  (or set VARDYN_REFERENCE)" % sys.argv[0])
+    return root
+
+
 def install(enable_x64=True):
     """Register fake ``jax``, ``matplotlib`` and ``src.config`` modules."""
     jax = types.ModuleType("jax")

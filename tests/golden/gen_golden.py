@@ -9,7 +9,7 @@ and records the outputs of ``Qgm``'s forward functions on seeded inputs in
 float64 (``USE_FLOAT64 = True``).
 
 Usage (only where the reference checkout exists):
-    python tests/golden/gen_golden.py [/root/reference]
+    python tests/golden/gen_golden.py <VarDyn checkout>
 Writes ``tests/golden/qg1l_golden.npz``.
 """
 import os
@@ -144,7 +144,7 @@ def c1_case(ref, out):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_root = _jax_standin.reference_root()
     ref = load_reference(ref_root)
     out = {}
     small_case(ref, out)

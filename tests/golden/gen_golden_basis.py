@@ -11,7 +11,7 @@ paths import but never call (xarray, pyinterp, netCDF4,
 jax.experimental.sparse) are empty modules.
 
 Usage (only where the reference checkout exists):
-    python tests/golden/gen_golden_basis.py [/root/reference]
+    python tests/golden/gen_golden_basis.py <VarDyn checkout>
 Writes ``tests/golden/basis_golden.npz``.
 """
 import importlib.util
@@ -23,6 +23,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
+
+import _jax_standin  # noqa: E402
 
 from gen_golden_obs import _empty, load_obsop  # noqa: E402
 
@@ -50,7 +52,7 @@ def load_basis(ref_root):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_root = _jax_standin.reference_root()
     basis = load_basis(ref_root)
     lon1d = -65.0 + 0.1 * np.arange(40)
     lat1d = 33.0 + 0.1 * np.arange(30)

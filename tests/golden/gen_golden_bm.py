@@ -9,7 +9,7 @@ The numpy form keeps a time centre while |dt| < tdec; the jax form
 cos^2(pi/2) is below 1e-32: the two give the same fields to rounding.
 
 Usage (only where the reference checkout exists):
-    python tests/golden/gen_golden_bm.py [/root/reference]
+    python tests/golden/gen_golden_bm.py <VarDyn checkout>
 Writes ``tests/golden/bm_golden.npz``.
 """
 import datetime
@@ -22,6 +22,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
+import _jax_standin  # noqa: E402
+
 from gen_golden_basis import load_basis  # noqa: E402
 
 BM = dict(lmin=60., lmax=300., npsp=3.5, facpsp=1.5, lmeso=150., tmeso=10., facns=1.2, facnlt=2.0, tdecmin=2.,
@@ -31,7 +33,7 @@ TIMES_K = (0, 9, 22, 40)
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_root = _jax_standin.reference_root()
     basis = load_basis(ref_root)
     lon1d = -65.0 + 0.1 * np.arange(40)
     lat1d = 33.0 + 0.1 * np.arange(30)

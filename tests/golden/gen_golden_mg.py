@@ -9,7 +9,7 @@ jax is the NumPy stand-in of ``_jax_standin.py`` (jit is the identity,
 fori_loop the plain loop).
 
 Usage (only where the reference checkout exists):
-    python tests/golden/gen_golden_mg.py [/root/reference]
+    python tests/golden/gen_golden_mg.py <VarDyn checkout>
 Writes ``tests/golden/mg_golden.npz``.
 """
 import importlib.util
@@ -40,7 +40,7 @@ def load_mg(ref_root):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_root = _jax_standin.reference_root()
     mg = load_mg(ref_root)
     out = {}
     for tag, (nx, ny, nb, lam, ite) in CASES.items():

@@ -12,7 +12,7 @@ the modules these code paths import but never call (xarray, pandas,
 pyinterp, matplotlib, jax.experimental.sparse) are empty modules.
 
 Usage (only where the reference checkout exists):
-    python tests/golden/gen_golden_obs.py [/root/reference]
+    python tests/golden/gen_golden_obs.py <VarDyn checkout>
 Writes ``tests/golden/obs_golden.npz``.
 """
 import datetime
@@ -105,7 +105,7 @@ def run_case(obsop, tag, out, mask_borders, seed):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_root = _jax_standin.reference_root()
     obsop, grid = load_obsop(ref_root)
     out = {}
     run_case(obsop, "a", out, mask_borders=False, seed=31)

@@ -18,7 +18,7 @@ and records in float64:
 ``QG.add_wind_forcing`` do not accept, so only its operators are recorded.
 
 Usage (only where the reference checkout exists):
-    python tests/golden/gen_golden_sw.py [/root/reference]
+    python tests/golden/gen_golden_sw.py <VarDyn checkout>
 Writes ``tests/golden/sw_golden.npz``.
 """
 import os
@@ -209,7 +209,7 @@ def sw_case_h(M, out, rng):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_root = _jax_standin.reference_root()
     M = load(ref_root)
     out = {}
     rng = np.random.default_rng(4242)

@@ -8,7 +8,7 @@ loads ``jqgm.py`` unmodified from the reference checkout and records
 ``QgmWithTiles.step`` on seeded inputs in float64.
 
 Usage (only where the reference checkout exists):
-    python tests/golden/gen_golden_tiles.py [/root/reference]
+    python tests/golden/gen_golden_tiles.py <VarDyn checkout>
 Writes ``tests/golden/qgt_golden.npz``.
 """
 import os
@@ -18,6 +18,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
+
+import _jax_standin  # noqa: E402
 
 from gen_golden import J, load_reference  # noqa: E402
 
@@ -64,7 +66,7 @@ def case_b(ref, out):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_root = _jax_standin.reference_root()
     ref = load_reference(ref_root)
     out = {}
     case_a(ref, out)

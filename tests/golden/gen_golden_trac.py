@@ -4,7 +4,7 @@ reference's own source code, through the NumPy stand-in for jax
 (``_jax_standin.py``), in float64.
 
 Usage (only where the reference checkout exists):
-    python tests/golden/gen_golden_trac.py [/root/reference]
+    python tests/golden/gen_golden_trac.py <VarDyn checkout>
 Writes ``tests/golden/qgtrac_golden.npz``.
 """
 import os
@@ -14,6 +14,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
+
+import _jax_standin  # noqa: E402
 
 from gen_golden import J, load_reference  # noqa: E402
 
@@ -79,7 +81,7 @@ def case_c(ref, out):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_root = _jax_standin.reference_root()
     ref = load_reference(ref_root)
     out = {}
     case_a(ref, out)

@@ -10,7 +10,7 @@ of an array (numpy 1 stored its single value). The loaded module's
 0-d array for scalar arguments; the reference files are not modified.
 
 Usage (only where the reference checkout exists):
-    python tests/golden/gen_golden_wavelet.py [/root/reference]
+    python tests/golden/gen_golden_wavelet.py <VarDyn checkout>
 Writes ``tests/golden/wavelet_golden.npz``.
 """
 import os
@@ -22,6 +22,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
+import _jax_standin  # noqa: E402
+
 from gen_golden_basis import load_basis  # noqa: E402
 
 WAV = dict(facnst=1.0, npsp=3.5, facpsp=1.5, lmin=60., lmax=250., tmin=3., tmax=15., sigma_Q=0.02)
@@ -29,7 +31,7 @@ TIMES_K = (0, 7, 21, 40)
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref_root = _jax_standin.reference_root()
     basis = load_basis(ref_root)
     gc = basis.gaspari_cohn
 

@@ -172,8 +172,8 @@ SIGNATURES = {
     "vd_qg1l_step": (I, [P, I, P, P, I, P, P, P, SZ, P]),
     "vd_qg1l_step_tgl": (I, [P, I, P, P, P, I, P, P, SZ, P]),
     "vd_qg1l_step_adj": (I, [P, I, P, P, P, I, P, P, I, P, SZ, P]),
-    "vd_qg1l_init_state": (I, [P, I, P, P, P, P, P]),
-    "vd_qg1l_advance": (I, [P, I, P, I, I, I, P, P, P, SZ, P]),
+    "vd_qg1l_init_state": (I, [P, I, P, P, P, P, P, P]),
+    "vd_qg1l_advance": (I, [P, I, P, I, I, I, P, P, P, P, SZ, P]),
     "vd_qg1l_advance_adj": (I, [P, I, P, I, I, I, P, P, P, SZ, P]),
     "vd_qg1l_init_state_adj": (I, [P, I, P, P, P, P]),
     "vd_qg1l_finalize": (I, [P, I, P, P, P, D, P, P]),

@@ -61,6 +61,8 @@ class SWStep(torch.autograd.Function):
 class BasisProjection(torch.autograd.Function):
     @staticmethod
     def forward(ctx, X, plan, k):
+        if X.dtype != plan.dtype:
+            raise TypeError(f"control dtype {X.dtype} differs from the basis plan's {plan.dtype}")
         ctx.plan, ctx.k, ctx.shape = plan, int(k), X.shape
         phi = plan.project(int(k), X.reshape(-1, plan.nbasis).contiguous())
         return phi[0] if X.dim() == 1 else phi

@@ -14,6 +14,7 @@ the coefficient adjoint and zeroes the parameter adjoint. ``t`` is looked up
 among the basis times by exact equality, as the reference does
 (basis.py:1636-1640).
 """
+import contextlib
 import ctypes
 
 import numpy as np
@@ -71,7 +72,6 @@ class _SeparablePlan:
                 raise RuntimeError("vardyn_gb300 needs a CUDA device (no CPU path)")
             dev = torch.device(device or "cuda")
             self.device = torch.device("cuda", dev.index if dev.index is not None else torch.cuda.current_device())
-            torch.cuda.set_device(self.device)
         self._land = None
         if land is not None:
             land = np.asarray(land, dtype=bool)
@@ -86,6 +86,11 @@ class _SeparablePlan:
             self.times.size, self.times.ctypes.data_as(dptr), int(host_only))
         self.lib = _lib.load()
         self._ws = None
+
+    def _on_device(self):
+        """Context that makes the plan's device current for a C call (the
+        caller's current device is restored afterwards)."""
+        return contextlib.nullcontext() if self.host_only else torch.cuda.device(self.device)
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -126,9 +131,10 @@ class _SeparablePlan:
             out = torch.empty(B, self.ny, self.nx, dtype=self.dtype, device=self.device)
             accumulate = False
         ws = self.workspace(B)
-        _lib.check(getattr(self.lib, self._prefix + "_project")(
-            self._h, B, int(k), _ptr(X), X.stride(0), _ptr(out), int(bool(accumulate)), _ptr(ws), ws.numel(),
-            _stream()), self._prefix + "_project")
+        with self._on_device():
+            _lib.check(getattr(self.lib, self._prefix + "_project")(
+                self._h, B, int(k), _ptr(X), X.stride(0), _ptr(out), int(bool(accumulate)), _ptr(ws), ws.numel(),
+                _stream()), self._prefix + "_project")
         return out
 
     def project_T(self, k, adphi, adX):
@@ -139,9 +145,10 @@ class _SeparablePlan:
         if not adphi.is_contiguous():
             raise ValueError("adphi must be contiguous")
         ws = self.workspace(B)
-        _lib.check(getattr(self.lib, self._prefix + "_project_T")(
-            self._h, B, int(k), _ptr(adphi), _ptr(adX), adX.stride(0), _ptr(ws), ws.numel(), _stream()),
-            self._prefix + "_project_T")
+        with self._on_device():
+            _lib.check(getattr(self.lib, self._prefix + "_project_T")(
+                self._h, B, int(k), _ptr(adphi), _ptr(adX), adX.stride(0), _ptr(ws), ws.numel(), _stream()),
+                self._prefix + "_project_T")
         return adX
 
     def q(self):
@@ -167,8 +174,9 @@ class BasisPlan(_SeparablePlan):
         self.comps = list(comps)
         params = (_lib.VdGauss3dParams * len(self.comps))(*[c.to_c() for c in self.comps])
         h = ctypes.c_void_p()
-        _lib.check(self.lib.vd_basis_plan_create(ctypes.byref(h), ctypes.byref(self._gridc), len(self.comps),
-                                                 params), "vd_basis_plan_create")
+        with self._on_device():
+            _lib.check(self.lib.vd_basis_plan_create(ctypes.byref(h), ctypes.byref(self._gridc), len(self.comps),
+                                                     params), "vd_basis_plan_create")
         self._h = h
         self.nbasis = int(self.lib.vd_basis_nbasis(h))
 
@@ -228,8 +236,9 @@ class BMPlan(_SeparablePlan):
         self.params = params
         h = ctypes.c_void_p()
         pc = params.to_c()
-        _lib.check(self.lib.vd_bm_plan_create(ctypes.byref(h), ctypes.byref(self._gridc), ctypes.byref(pc)),
-                   "vd_bm_plan_create")
+        with self._on_device():
+            _lib.check(self.lib.vd_bm_plan_create(ctypes.byref(h), ctypes.byref(self._gridc), ctypes.byref(pc)),
+                       "vd_bm_plan_create")
         self._h = h
         self.nbasis = int(self.lib.vd_bm_nbasis(h))
         nf, nth = ctypes.c_int(), ctypes.c_int()
@@ -288,8 +297,9 @@ class WaveletPlan(BMPlan):
         self.params = params
         h = ctypes.c_void_p()
         pc = params.to_c()
-        _lib.check(self.lib.vd_wavelet_plan_create(ctypes.byref(h), ctypes.byref(self._gridc), ctypes.byref(pc)),
-                   "vd_wavelet_plan_create")
+        with self._on_device():
+            _lib.check(self.lib.vd_wavelet_plan_create(ctypes.byref(h), ctypes.byref(self._gridc), ctypes.byref(pc)),
+                       "vd_wavelet_plan_create")
         self._h = h
         self.nbasis = int(self.lib.vd_bm_nbasis(h))
         nf, nth = ctypes.c_int(), ctypes.c_int()

@@ -14,13 +14,13 @@ void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 size_t elem_size(int dtype) { return dtype == VD_F64 ? 8 : 4; }
 
 template <typename T>
-int advance_impl(const vd_qg1l_plan*, int, T*, int, int, int, const T*, const T*, Arena&, cudaStream_t);
+int advance_impl(const vd_qg1l_plan*, int, T*, int, int, int, const T*, const T*, T*, Arena&, cudaStream_t);
 template <typename T>
-int forward_nostore(const vd_qg1l_plan*, int, T*, T*, int, const T*, const T*, Arena&, cudaStream_t, bool);
+int forward_nostore(const vd_qg1l_plan*, int, T*, T*, int, const T*, const T*, T*, Arena&, cudaStream_t, bool);
 template <typename T>
 int advance_adj_impl(const vd_qg1l_plan*, int, const T*, int, int, int, T*, T*, Arena&, cudaStream_t);
 template <typename T>
-int init_state_impl(const vd_qg1l_plan*, int, int, const T*, const T*, T*, T*, cudaStream_t);
+int init_state_impl(const vd_qg1l_plan*, int, int, const T*, const T*, T*, T*, T*, cudaStream_t);
 template <typename T>
 int init_state_adj_impl(const vd_qg1l_plan*, int, const T*, const T*, T*, cudaStream_t);
 template <typename T>
@@ -232,12 +232,14 @@ extern "C" size_t vd_qg1l_workspace_bytes(const vd_qg1l_plan* p, int B)
     if (!p || B <= 0) return 0;
     const size_t F = size_t(p->geom.fs) * elem_size(p->d.dtype);
     const int S = p->nstage, nk = nk_count(p);
-    auto fwd = [&](int nf) { return (nk + 2 * (S - 1) + 2) * nf * F + spec_bytes(p, nf); };
+    // the low part of the compensated PV state (float32 plans): one field
+    // per forward field
+    auto fwd = [&](int nf) { return (nk + 2 * (S - 1) + 3) * nf * F + spec_bytes(p, nf); };
     const size_t step = 3 * B * F + fwd(B);
     const size_t tgl = 5 * B * F + fwd(2 * B);
     const size_t adv_part = nk * B * F + spec_bytes(p, B);
     const size_t adj_part = (2 + S + 7) * B * F + spec_bytes(p, B);
-    const size_t adj = B * F + (adv_part > adj_part ? adv_part : adj_part) + 2 * B * F;
+    const size_t adj = 2 * B * F + (adv_part > adj_part ? adv_part : adj_part) + 2 * B * F;
     size_t m = step > tgl ? step : tgl;
     m = m > adj ? m : adj;
     return m + 64 * 256;
@@ -250,8 +252,9 @@ extern "C" vd_status vd_qg1l_h2pv(const vd_qg1l_plan* p, int B, const void* h, c
     if (!p || B <= 0 || !h || !hb || !q) return VD_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     return p->d.dtype == VD_F32
-               ? init_state_impl<float>(p, B, B, (const float*)h, (const float*)hb, (float*)q, nullptr, st)
-               : init_state_impl<double>(p, B, B, (const double*)h, (const double*)hb, (double*)q, nullptr, st);
+               ? init_state_impl<float>(p, B, B, (const float*)h, (const float*)hb, (float*)q, nullptr, nullptr, st)
+               : init_state_impl<double>(p, B, B, (const double*)h, (const double*)hb, (double*)q, nullptr, nullptr,
+                                         st);
 }
 
 extern "C" vd_status vd_qg1l_h2uv(const vd_qg1l_plan* p, int B, const void* h, void* u, void* v, void* stream)
@@ -297,6 +300,17 @@ extern "C" vd_status vd_qg1l_pv2h(const vd_qg1l_plan* p, int B, const void* q, c
                : pv2h_t<double>(p, B, (const double*)q, (const double*)hb, (const double*)qb, (double*)h, ws, st);
 }
 
+// Low part of the compensated PV state: float32 plans carry one, float64
+// plans step with the reference's plain arithmetic.
+template <typename T>
+static int take_qlo(const vd_qg1l_plan* p, long long n, Arena& ws, T** qlo)
+{
+    *qlo = nullptr;
+    if (p->d.dtype != VD_F32) return VD_OK;
+    *qlo = (T*)ws.take(n * sizeof(T));
+    return *qlo ? VD_OK : VD_ERR_WORKSPACE;
+}
+
 template <typename T>
 static int step_t(const vd_qg1l_plan* p, int B, const T* h0, const T* hb, int nstep, T* hout, T* traj, Arena& ws,
                   cudaStream_t st)
@@ -304,13 +318,15 @@ static int step_t(const vd_qg1l_plan* p, int B, const T* h0, const T* hb, int ns
     const long long fb = fb_elems(p, B);
     T* qb = (T*)ws.take(fb * sizeof(T));
     if (!qb) return VD_ERR_WORKSPACE;
+    T* qlo;
     int rc;
+    if ((rc = take_qlo<T>(p, fb, ws, &qlo))) return rc;
     if (traj) {
         T* h = traj;
         T* q = traj + fb;
         VD_CUDA_TRY(cudaMemcpyAsync(h, h0, fb * sizeof(T), cudaMemcpyDeviceToDevice, st));
-        if ((rc = init_state_impl<T>(p, B, B, h, hb, q, qb, st))) return rc;
-        if ((rc = advance_impl<T>(p, B, traj, nstep, 0, nstep, hb, qb, ws, st))) return rc;
+        if ((rc = init_state_impl<T>(p, B, B, h, hb, q, qb, qlo, st))) return rc;
+        if ((rc = advance_impl<T>(p, B, traj, nstep, 0, nstep, hb, qb, qlo, ws, st))) return rc;
         const T* hN = traj + (long long)nstep * p->nstage * 2 * fb;
         return finalize_impl<T>(p, B, hN, hb, nullptr, 0.0, nullptr, 1, hout, st);
     }
@@ -318,8 +334,8 @@ static int step_t(const vd_qg1l_plan* p, int B, const T* h0, const T* hb, int ns
     T* q = (T*)ws.take(fb * sizeof(T));
     if (!h || !q) return VD_ERR_WORKSPACE;
     VD_CUDA_TRY(cudaMemcpyAsync(h, h0, fb * sizeof(T), cudaMemcpyDeviceToDevice, st));
-    if ((rc = init_state_impl<T>(p, B, B, h, hb, q, qb, st))) return rc;
-    if ((rc = forward_nostore<T>(p, B, h, q, nstep, hb, qb, ws, st, false))) return rc;
+    if ((rc = init_state_impl<T>(p, B, B, h, hb, q, qb, qlo, st))) return rc;
+    if ((rc = forward_nostore<T>(p, B, h, q, nstep, hb, qb, qlo, ws, st, false))) return rc;
     return finalize_impl<T>(p, B, h, hb, nullptr, 0.0, nullptr, 1, hout, st);
 }
 
@@ -345,11 +361,13 @@ static int step_tgl_t(const vd_qg1l_plan* p, int B, const T* dh0, const T* h0, c
     T* q = (T*)ws.take(2 * fb * sizeof(T));
     T* qb = (T*)ws.take(fb * sizeof(T));
     if (!h || !q || !qb) return VD_ERR_WORKSPACE;
+    T* qlo;
+    int rc;
+    if ((rc = take_qlo<T>(p, 2 * fb, ws, &qlo))) return rc;
     VD_CUDA_TRY(cudaMemcpyAsync(h, h0, fb * sizeof(T), cudaMemcpyDeviceToDevice, st));
     VD_CUDA_TRY(cudaMemcpyAsync(h + fb, dh0, fb * sizeof(T), cudaMemcpyDeviceToDevice, st));
-    int rc;
-    if ((rc = init_state_impl<T>(p, 2 * B, B, h, hb, q, qb, st))) return rc;
-    if ((rc = forward_nostore<T>(p, 2 * B, h, q, nstep, hb, qb, ws, st, true))) return rc;
+    if ((rc = init_state_impl<T>(p, 2 * B, B, h, hb, q, qb, qlo, st))) return rc;
+    if ((rc = forward_nostore<T>(p, 2 * B, h, q, nstep, hb, qb, qlo, ws, st, true))) return rc;
     return finalize_impl<T>(p, B, h + fb, nullptr, nullptr, 0.0, nullptr, 2, dhout, st);
 }
 
@@ -380,10 +398,12 @@ static int step_adj_t(const vd_qg1l_plan* p, int B, const T* adh1, const T* h0, 
     if (!traj_ready) {
         T* qb = (T*)ws.take(fb * sizeof(T));
         if (!qb) return VD_ERR_WORKSPACE;
+        T* qlo;
+        if ((rc = take_qlo<T>(p, fb, ws, &qlo))) return rc;
         VD_CUDA_TRY(cudaMemcpyAsync(traj, h0, fb * sizeof(T), cudaMemcpyDeviceToDevice, st));
-        if ((rc = init_state_impl<T>(p, B, B, traj, hb, traj + fb, qb, st))) return rc;
+        if ((rc = init_state_impl<T>(p, B, B, traj, hb, traj + fb, qb, qlo, st))) return rc;
         Arena sub = ws;
-        if ((rc = advance_impl<T>(p, B, traj, nstep, 0, nstep, hb, qb, sub, st))) return rc;
+        if ((rc = advance_impl<T>(p, B, traj, nstep, 0, nstep, hb, qb, qlo, sub, st))) return rc;
     }
     if ((rc = copy_impl<T>(p, B, adh1, adh, 1, st))) return rc;
     if ((rc = zero_impl<T>(fb, adq, st))) return rc;
@@ -409,29 +429,31 @@ extern "C" vd_status vd_qg1l_step_adj(const vd_qg1l_plan* p, int B, const void* 
 }
 
 extern "C" vd_status vd_qg1l_init_state(const vd_qg1l_plan* p, int B, const void* h, const void* hb, void* q,
-                                        void* qb, void* stream)
+                                        void* qb, void* qlo, void* stream)
 {
     if (!p || B <= 0 || !h || !hb || !q) return VD_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     return p->d.dtype == VD_F32
-               ? init_state_impl<float>(p, B, B, (const float*)h, (const float*)hb, (float*)q, (float*)qb, st)
-               : init_state_impl<double>(p, B, B, (const double*)h, (const double*)hb, (double*)q, (double*)qb, st);
+               ? init_state_impl<float>(p, B, B, (const float*)h, (const float*)hb, (float*)q, (float*)qb,
+                                        (float*)qlo, st)
+               : init_state_impl<double>(p, B, B, (const double*)h, (const double*)hb, (double*)q, (double*)qb,
+                                         (double*)qlo, st);
 }
 
 extern "C" vd_status vd_qg1l_advance(const vd_qg1l_plan* p, int B, void* traj, int traj_steps, int first_step,
-                                     int nstep, const void* hb, const void* qb, void* work, size_t work_bytes,
-                                     void* stream)
+                                     int nstep, const void* hb, const void* qb, void* qlo, void* work,
+                                     size_t work_bytes, void* stream)
 {
     // hb == NULL / qb == NULL mean a zero background SSH / PV: the solves then
-    // skip the addition / subtraction.
+    // skip the addition / subtraction. qlo == NULL steps with plain arithmetic.
     if (!p || B <= 0 || !traj || !work) return VD_ERR_ARG;
     Arena ws{(char*)work, work_bytes, 0};
     cudaStream_t st = (cudaStream_t)stream;
     return p->d.dtype == VD_F32
                ? advance_impl<float>(p, B, (float*)traj, traj_steps, first_step, nstep, (const float*)hb,
-                                     (const float*)qb, ws, st)
+                                     (const float*)qb, (float*)qlo, ws, st)
                : advance_impl<double>(p, B, (double*)traj, traj_steps, first_step, nstep, (const double*)hb,
-                                      (const double*)qb, ws, st);
+                                      (const double*)qb, (double*)qlo, ws, st);
 }
 
 extern "C" vd_status vd_qg1l_advance_adj(const vd_qg1l_plan* p, int B, const void* traj, int traj_steps,

@@ -735,12 +735,11 @@ static int launch_tridiag(const vd_qg1l_plan* p, int nf, T* spec, cudaStream_t s
     return VD_OK;
 }
 
-static std::once_flag g_attr_once;
-static cudaError_t g_attr_err = cudaSuccess;
+static PerDeviceOnce g_attr_once;
 
 static cudaError_t configure_kernels()
 {
-    std::call_once(g_attr_once, [] {
+    return g_attr_once.run([]() -> cudaError_t {
         cudaError_t e = cudaSuccess;
         if (!e) e = set_smem_attrs<float, 16>();
         if (!e) e = set_smem_attrs<float, 32>();
@@ -754,9 +753,8 @@ static cudaError_t configure_kernels()
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, maxb);
         if (!e) e = cudaFuncSetAttribute(dst_fft_kernel<MODE_INV, EPI_ADJQ>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, maxb);
-        g_attr_err = e;
+        return e;
     });
-    return g_attr_err;
 }
 
 template <typename T, int TR>

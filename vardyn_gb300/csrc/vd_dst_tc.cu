@@ -659,21 +659,19 @@ void free_tc_images(vd_qg1l_plan* p)
     p->dst.tc = nullptr;
 }
 
-static std::once_flag g_tc_once;
-static cudaError_t g_tc_err = cudaSuccess;
+static PerDeviceOnce g_tc_once;
 
 static cudaError_t tc_configure()
 {
-    std::call_once(g_tc_once, [] {
+    return g_tc_once.run([]() -> cudaError_t {
         cudaError_t e = cudaFuncSetAttribute(dst_tc_kernel<0, EPI_H>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)SMEM_MAX);
         if (!e) e = cudaFuncSetAttribute(dst_tc_kernel<1, EPI_H>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)SMEM_MAX);
         if (!e) e = cudaFuncSetAttribute(dst_tc_kernel<1, EPI_ADJQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)SMEM_MAX);
-        g_tc_err = e;
+        return e;
     });
-    return g_tc_err;
 }
 
 // The producers address rows with 32-bit element offsets.

@@ -4,6 +4,7 @@
 #include <stdint.h>
 #include <stddef.h>
 #include <math.h>
+#include <mutex>
 #include "../../include/vardyn_gb300.h"
 
 #define VD_CUDA_TRY(expr)                                  \
@@ -117,6 +118,30 @@ void free_tc_images(vd_qg1l_plan* p);
 // Whether a batch of nf fields fits the tensor-core pass (32-bit row offsets).
 bool tc_fits(const vd_qg1l_plan* p, int nf);
 int dst_pass_tc(const vd_qg1l_plan* p, int nf, const SolveArgs& a, float* spec, bool fwd, cudaStream_t st);
+
+// Kernel attributes (cudaFuncSetAttribute) apply to the device that is
+// current when they are set. PerDeviceOnce runs a configuration function once
+// for each device ordinal, on that device, and keeps its result, so plans on
+// several GPUs of one process each launch with their attributes in place.
+struct PerDeviceOnce {
+    static constexpr int kMaxDevices = 64;
+    std::mutex mu;
+    bool done[kMaxDevices] = {};
+    cudaError_t err[kMaxDevices] = {};
+    template <typename F>
+    cudaError_t run(F&& fn) {
+        int dev = -1;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e != cudaSuccess) return e;
+        if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+        std::lock_guard<std::mutex> lock(mu);
+        if (!done[dev]) {
+            err[dev] = fn();
+            done[dev] = true;
+        }
+        return err[dev];
+    }
+};
 
 // Bump allocator over a caller workspace.
 struct Arena {

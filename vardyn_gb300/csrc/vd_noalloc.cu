@@ -34,7 +34,8 @@ std::mutex g_mu;
 void* g_scratch_ptr[kMaxDevices] = {nullptr};
 
 // Device address of the scratch array on the current device, looked up on
-// the first call for that device.
+// the first call for that device and cached until the process exits (a
+// cudaDeviceReset while the library is loaded is not supported).
 int scratch_for_current_device(void** out)
 {
     int dev = -1;

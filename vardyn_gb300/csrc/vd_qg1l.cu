@@ -20,6 +20,32 @@ namespace vd {
 
 template <typename T> __device__ __forceinline__ T guard0(T x) { return isnan(x) ? T(0) : x; }
 
+// Round-to-nearest add / subtract that the compiler neither contracts nor
+// reassociates (the error-free transformations below rely on it).
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+
+// Compensated state update of float32 plans. The prognostic PV of a step is
+// held as an unevaluated pair q + q_lo (q_lo a few ulps of q at most). The
+// last stage of a step adds its increment with TwoSum (Knuth), folds the
+// rounding error into q_lo and renormalises with Fast2Sum, so the 2880
+// roundings of a 30-day window do not accumulate in the trajectory. Earlier
+// stages evaluate q_n + (increment + q_lo) in plain arithmetic: their values
+// only feed the tendency of the next stage.
+template <typename T>
+__device__ __forceinline__ void comp_update(T base, T inc, T& q_out, T& lo)
+{
+    const T s = add_rn(base, inc);
+    const T bb = sub_rn(s, base);
+    const T e = add_rn(sub_rn(base, sub_rn(s, bb)), sub_rn(inc, bb));
+    const T l2 = add_rn(lo, e);
+    const T hi = add_rn(s, l2);
+    lo = sub_rn(l2, sub_rn(hi, s));
+    q_out = hi;
+}
+
 template <typename T>
 struct Cross {
     T c, e1, e2, w1, w2, n1, n2, s1, s2;   // (j,i), (j,i+1), (j,i+2), (j,i-1), ... (j-1,i), (j-2,i)
@@ -89,8 +115,19 @@ __device__ __forceinline__ T lap_helm(const QGGeom& G, const T* __restrict__ hc)
 }
 
 template <typename T>
+__device__ __forceinline__ double lap_helm_f64(const QGGeom& G, const T* __restrict__ hc)
+{
+    const int nx = G.nx;
+    const double c = hc[0];
+    return G.gf * (((double)hc[nx] + (double)hc[-nx] - 2.0 * c) * G.idy2 +
+                   ((double)hc[1] + (double)hc[-1] - 2.0 * c) * G.idx2) - G.gfc2 * c;
+}
+
+// With qlo != nullptr (float32 plans) the PV is evaluated in float64 from
+// the float32 SSH and returned as the pair q + qlo of the compensated state.
+template <typename T>
 __global__ void k_h2pv(QGGeom G, int nf, int ntan0, const T* __restrict__ h,
-                       const T* __restrict__ hb, T* __restrict__ q)
+                       const T* __restrict__ hb, T* __restrict__ q, T* __restrict__ qlo)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -98,6 +135,20 @@ __global__ void k_h2pv(QGGeom G, int nf, int ntan0, const T* __restrict__ h,
     if (i >= G.nx || j >= G.ny || f >= nf) return;
     const long long o = f * G.fs + (long long)j * G.nx + i;
     const int m = G.mask[j * G.nx + i];
+    if (qlo) {
+        double val = 0.0;
+        if (m == 3) {
+            val = lap_helm_f64<T>(G, h + o);
+            const double prim = f >= ntan0 ? lap_helm_f64<T>(G, h + o - ntan0 * G.fs) : val;
+            if (isnan(prim)) val = 0.0;
+        } else if (m != 0 && f < ntan0) {
+            val = -G.gfc2 * (double)hb[o];
+        }
+        const T hi = (T)val;
+        q[o] = hi;
+        qlo[o] = (T)(val - (double)hi);
+        return;
+    }
     T val = T(0);
     if (m == 3) {
         val = lap_helm<T>(G, h + o);
@@ -187,7 +238,7 @@ __device__ __forceinline__ void cross_pair(const T* __restrict__ p, int nx, Cros
 template <typename T>
 __global__ void k_stage_fwd(QGGeom G, int nf, const T* __restrict__ hs, const T* __restrict__ qs,
                             const T* __restrict__ qbase, StageIn<T> kin, T cself,
-                            T* __restrict__ kout, T* __restrict__ qout)
+                            T* __restrict__ kout, T* __restrict__ qout, T* __restrict__ qlo, int last)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * (2 * blockDim.y) + 2 * threadIdx.y;
@@ -232,12 +283,28 @@ __global__ void k_stage_fwd(QGGeom G, int nf, const T* __restrict__ hs, const T*
     for (int u = 0; u < 2; ++u) {
         if (u == 1 && !two) break;
         const long long ou = o + u * nx;
-        T acc = qbase[ou];
+        if (qlo) {
+            T inc = cself * r[u];
 #pragma unroll
-        for (int t = 0; t < 4; ++t)
-            if (t < kin.nk) acc += kin.c[t] * kin.k[t][ou];
-        acc += cself * r[u];
-        qout[ou] = acc;
+            for (int t = 0; t < 4; ++t)
+                if (t < kin.nk) inc += kin.c[t] * kin.k[t][ou];
+            T lo = qlo[ou];
+            if (last) {
+                T qo;
+                comp_update(qbase[ou], inc, qo, lo);
+                qout[ou] = qo;
+                qlo[ou] = lo;
+            } else {
+                qout[ou] = qbase[ou] + (inc + lo);
+            }
+        } else {
+            T acc = qbase[ou];
+#pragma unroll
+            for (int t = 0; t < 4; ++t)
+                if (t < kin.nk) acc += kin.c[t] * kin.k[t][ou];
+            acc += cself * r[u];
+            qout[ou] = acc;
+        }
         if (kout) kout[ou] = r[u];
     }
 }
@@ -246,7 +313,7 @@ __global__ void k_stage_fwd(QGGeom G, int nf, const T* __restrict__ hs, const T*
 template <typename T>
 __global__ void k_stage_tl(QGGeom G, int B, const T* __restrict__ hs, const T* __restrict__ qs,
                            const T* __restrict__ qbase, StageIn<T> kin, T cself,
-                           T* __restrict__ kout, T* __restrict__ qout)
+                           T* __restrict__ kout, T* __restrict__ qout, T* __restrict__ qlo, int last)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y * blockDim.y + threadIdx.y;
@@ -287,15 +354,36 @@ __global__ void k_stage_tl(QGGeom G, int B, const T* __restrict__ hs, const T* _
                 dr += T(G.Kx) * (dq.e1 + dq.w1 - T(2) * dq.c) + T(G.Ky) * (dq.n1 + dq.s1 - T(2) * dq.c);
         }
     }
-    T acc = qbase[o], dacc = qbase[od];
+    if (qlo) {
+        T inc = cself * r, dinc = cself * dr;
 #pragma unroll
-    for (int t = 0; t < 4; ++t) {
-        if (t >= kin.nk) break;
-        acc += kin.c[t] * kin.k[t][o];
-        dacc += kin.c[t] * kin.k[t][od];
+        for (int t = 0; t < 4; ++t) {
+            if (t >= kin.nk) break;
+            inc += kin.c[t] * kin.k[t][o];
+            dinc += kin.c[t] * kin.k[t][od];
+        }
+        T lo = qlo[o], dlo = qlo[od];
+        if (last) {
+            T qo, dqo;
+            comp_update(qbase[o], inc, qo, lo);
+            comp_update(qbase[od], dinc, dqo, dlo);
+            qout[o] = qo; qout[od] = dqo;
+            qlo[o] = lo; qlo[od] = dlo;
+        } else {
+            qout[o] = qbase[o] + (inc + lo);
+            qout[od] = qbase[od] + (dinc + dlo);
+        }
+    } else {
+        T acc = qbase[o], dacc = qbase[od];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            if (t >= kin.nk) break;
+            acc += kin.c[t] * kin.k[t][o];
+            dacc += kin.c[t] * kin.k[t][od];
+        }
+        qout[o] = acc + cself * r;
+        qout[od] = dacc + cself * dr;
     }
-    qout[o] = acc + cself * r;
-    qout[od] = dacc + cself * dr;
     if (kout) { kout[o] = r; kout[od] = dr; }
 }
 
@@ -633,7 +721,7 @@ struct TrajView {
 // One forward step (stage loop) between explicit buffers.
 template <typename T>
 static int step_once(const vd_qg1l_plan* p, int nf, T* const* hsv, T* const* qsv, T* hnew, T* qnew,
-                     T* const* kbuf, const T* hb, const T* qb, T* spec, cudaStream_t st, bool tangent)
+                     T* const* kbuf, const T* hb, const T* qb, T* spec, cudaStream_t st, bool tangent, T* qlo)
 {
     const int S = p->nstage;
     const int B = tangent ? nf / 2 : nf;
@@ -650,10 +738,11 @@ static int step_once(const vd_qg1l_plan* p, int nf, T* const* hsv, T* const* qsv
         T* qo = last ? qnew : qsv[s + 1];
         T* ho = last ? hnew : hsv[s + 1];
         if (tangent)
-            k_stage_tl<T><<<pgrid(p, B), kBlock, 0, st>>>(p->geom, B, hsv[s], qsv[s], qsv[0], kin, cself, kout, qo);
+            k_stage_tl<T><<<pgrid(p, B), kBlock, 0, st>>>(p->geom, B, hsv[s], qsv[s], qsv[0], kin, cself, kout, qo,
+                                                          qlo, last ? 1 : 0);
         else
             k_stage_fwd<T><<<pgrid(p, nf), dim3(32, 4), 0, st>>>(p->geom, nf, hsv[s], qsv[s], qsv[0], kin, cself, kout,
-                                                                 qo);
+                                                                 qo, qlo, last ? 1 : 0);
         VD_LAUNCH_CHECK();
         SolveArgs a;
         a.src = qo; a.sub = qb; a.sub_batches = B;
@@ -666,7 +755,7 @@ static int step_once(const vd_qg1l_plan* p, int nf, T* const* hsv, T* const* qsv
 
 template <typename T>
 int advance_impl(const vd_qg1l_plan* p, int nf, T* traj, int traj_steps, int first, int nstep,
-                 const T* hb, const T* qb, Arena& ws, cudaStream_t st)
+                 const T* hb, const T* qb, T* qlo, Arena& ws, cudaStream_t st)
 {
     if (first < 0 || nstep < 0 || first + nstep > traj_steps) return VD_ERR_ARG;
     const int S = p->nstage;
@@ -680,7 +769,7 @@ int advance_impl(const vd_qg1l_plan* p, int nf, T* traj, int traj_steps, int fir
     for (int n = first; n < first + nstep; ++n) {
         T* hs[4]; T* qs[4];
         for (int s = 0; s < S; ++s) { hs[s] = tv.h(n, s); qs[s] = tv.q(n, s); }
-        int rc = step_once<T>(p, nf, hs, qs, tv.h(n + 1, 0), tv.q(n + 1, 0), kbuf, hb, qb, spec, st, false);
+        int rc = step_once<T>(p, nf, hs, qs, tv.h(n + 1, 0), tv.q(n + 1, 0), kbuf, hb, qb, spec, st, false, qlo);
         if (rc) return rc;
     }
     return VD_OK;
@@ -689,7 +778,7 @@ int advance_impl(const vd_qg1l_plan* p, int nf, T* traj, int traj_steps, int fir
 // Forward without trajectory: ping-pong states in the workspace.
 template <typename T>
 int forward_nostore(const vd_qg1l_plan* p, int nf, T* h, T* q, int nstep, const T* hb, const T* qb,
-                    Arena& ws, cudaStream_t st, bool tangent)
+                    T* qlo, Arena& ws, cudaStream_t st, bool tangent)
 {
     const int S = p->nstage;
     const long long fb = (long long)nf * p->geom.fs;
@@ -710,7 +799,7 @@ int forward_nostore(const vd_qg1l_plan* p, int nf, T* h, T* q, int nstep, const 
     T* cur_h = h; T* cur_q = q; T* nxt_h = h2; T* nxt_q = q2;
     for (int n = 0; n < nstep; ++n) {
         hs[0] = cur_h; qs[0] = cur_q;
-        int rc = step_once<T>(p, nf, hs, qs, nxt_h, nxt_q, kbuf, hb, qb, spec, st, tangent);
+        int rc = step_once<T>(p, nf, hs, qs, nxt_h, nxt_q, kbuf, hb, qb, spec, st, tangent, qlo);
         if (rc) return rc;
         T* t1 = cur_h; cur_h = nxt_h; nxt_h = t1;
         T* t2 = cur_q; cur_q = nxt_q; nxt_q = t2;
@@ -737,14 +826,14 @@ int advance_adj_impl(const vd_qg1l_plan* p, int nf, const T* traj, int traj_step
     T* adhs = (T*)ws.take(fb * sizeof(T));
     T* spec = (T*)ws.take(spec_bytes(p, nf));
     if (!adql || !adhs || !spec) return VD_ERR_WORKSPACE;
-    static std::once_flag attr_once;
-    static cudaError_t attr_err = cudaSuccess;
-    std::call_once(attr_once, [] {
-        attr_err = cudaFuncSetAttribute(k_adj_stage_fused<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)sizeof(AdjTile<float>));
-        if (!attr_err)
-            attr_err = cudaFuncSetAttribute(k_adj_stage_fused<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)sizeof(AdjTile<double>));
+    static PerDeviceOnce attr_once;
+    const cudaError_t attr_err = attr_once.run([]() -> cudaError_t {
+        cudaError_t e = cudaFuncSetAttribute(k_adj_stage_fused<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)sizeof(AdjTile<float>));
+        if (!e)
+            e = cudaFuncSetAttribute(k_adj_stage_fused<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)sizeof(AdjTile<double>));
+        return e;
     });
     if (attr_err != cudaSuccess) return VD_ERR_CUDA;
 
@@ -788,12 +877,12 @@ int advance_adj_impl(const vd_qg1l_plan* p, int nf, const T* traj, int traj_step
 
 template <typename T>
 int init_state_impl(const vd_qg1l_plan* p, int nf, int ntan0, const T* h, const T* hb, T* q, T* qb,
-                    cudaStream_t st)
+                    T* qlo, cudaStream_t st)
 {
-    k_h2pv<T><<<pgrid(p, nf), kBlock, 0, st>>>(p->geom, nf, ntan0, h, hb, q);
+    k_h2pv<T><<<pgrid(p, nf), kBlock, 0, st>>>(p->geom, nf, ntan0, h, hb, q, qlo);
     VD_LAUNCH_CHECK();
     if (qb) {
-        k_h2pv<T><<<pgrid(p, ntan0), kBlock, 0, st>>>(p->geom, ntan0, ntan0, hb, hb, qb);
+        k_h2pv<T><<<pgrid(p, ntan0), kBlock, 0, st>>>(p->geom, ntan0, ntan0, hb, hb, qb, (T*)nullptr);
         VD_LAUNCH_CHECK();
     }
     return VD_OK;
@@ -859,13 +948,13 @@ int rhs_impl(const vd_qg1l_plan* p, int nf, const T* u, const T* v, const T* q, 
 }
 
 #define VD_INST(T)                                                                                        \
-    template int advance_impl<T>(const vd_qg1l_plan*, int, T*, int, int, int, const T*, const T*, Arena&, \
-                                 cudaStream_t);                                                           \
-    template int forward_nostore<T>(const vd_qg1l_plan*, int, T*, T*, int, const T*, const T*, Arena&,    \
-                                    cudaStream_t, bool);                                                  \
+    template int advance_impl<T>(const vd_qg1l_plan*, int, T*, int, int, int, const T*, const T*, T*,     \
+                                 Arena&, cudaStream_t);                                                   \
+    template int forward_nostore<T>(const vd_qg1l_plan*, int, T*, T*, int, const T*, const T*, T*,        \
+                                    Arena&, cudaStream_t, bool);                                          \
     template int advance_adj_impl<T>(const vd_qg1l_plan*, int, const T*, int, int, int, T*, T*, Arena&,   \
                                      cudaStream_t);                                                       \
-    template int init_state_impl<T>(const vd_qg1l_plan*, int, int, const T*, const T*, T*, T*,            \
+    template int init_state_impl<T>(const vd_qg1l_plan*, int, int, const T*, const T*, T*, T*, T*,        \
                                     cudaStream_t);                                                        \
     template int init_state_adj_impl<T>(const vd_qg1l_plan*, int, const T*, const T*, T*, cudaStream_t);  \
     template int finalize_impl<T>(const vd_qg1l_plan*, int, const T*, const T*, const T*, double,         \

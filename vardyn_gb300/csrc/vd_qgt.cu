@@ -243,10 +243,9 @@ template <typename R>
 static int qgt_run(const vd_qgt_desc* d, const void* h0, const void* hb, int nstep, void* h1, void* work,
                    cudaStream_t st)
 {
-    static std::once_flag once;
-    static cudaError_t attr = cudaSuccess;
-    std::call_once(once, [] {
-        attr = cudaFuncSetAttribute(k_qgt_tile<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    static PerDeviceOnce once;
+    const cudaError_t attr = once.run([]() -> cudaError_t {
+        return cudaFuncSetAttribute(k_qgt_tile<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     });
     if (attr != cudaSuccess) return VD_ERR_CUDA;
     QgtGeom<R> G;

@@ -23,6 +23,10 @@ Trajectory storage: ``full`` keeps every stage state of every step (the
 "plain" form, memory 2*nstage fields per step); ``checkpoint=K`` keeps the
 state every K steps and recomputes each K-step segment during the reverse
 sweep (one extra forward, memory (nstep/K)*2 + 2*nstage*K fields).
+
+Float32 plans carry the prognostic PV as a compensated pair (q, q_lo): the
+low part is one running field, saved with every snapshot so that a
+recomputed segment repeats the forward sweep bit for bit.
 """
 import ctypes
 import math
@@ -59,6 +63,7 @@ class QGWindows4DVar:
         self.vd_dtype = _lib.VD_F64 if plan.dtype == torch.float64 else _lib.VD_F32
         dev, dt = plan.device, plan.dtype
         self.qb = torch.zeros(B, ny, nx, dtype=dt, device=dev)
+        self.qlo = plan.new_qlo(B)
         self.tmp = torch.zeros(B, ny, nx, dtype=dt, device=dev)
         self.adh = torch.zeros(B, ny, nx, dtype=dt, device=dev)
         self.adq = torch.zeros(B, ny, nx, dtype=dt, device=dev)
@@ -83,7 +88,7 @@ class QGWindows4DVar:
             # segment trajectory (K steps) + snapshots of (h, q) at segment starts
             self.traj = plan.new_traj(B, K)
             self.traj_steps = K
-            self.snap = torch.zeros(self.nseg, 2, B, ny, nx, dtype=dt, device=dev)
+            self.snap = torch.zeros(self.nseg, 2 if self.qlo is None else 3, B, ny, nx, dtype=dt, device=dev)
         self.tv = self.traj.view(-1, 2, B, ny, nx)
         self.S = S
         self.graph = None
@@ -118,7 +123,7 @@ class QGWindows4DVar:
         for s in self.obs_steps + [self.nstep]:
             if s <= prev:
                 continue
-            p.advance(B, self.traj, self.traj_steps, prev, s - prev, self.hb_arg, self.qb_arg)
+            p.advance(B, self.traj, self.traj_steps, prev, s - prev, self.hb_arg, self.qb_arg, self.qlo)
             prev = s
             self._obs_forward(s, self.tv[s * self.S, 0])
 
@@ -142,7 +147,9 @@ class QGWindows4DVar:
         for g in range(self.nseg):
             a = g * K
             n = min(K, self.nstep - a)
-            self._copy(self.tv[0], self.snap[g])
+            self._copy(self.tv[0], self.snap[g, :2])
+            if self.qlo is not None:
+                self._copy(self.qlo, self.snap[g, 2])
             self._advance_segment(a, n, with_obs=True)
             self._copy(self.tv[n * self.S], self.tv[0])
 
@@ -153,7 +160,7 @@ class QGWindows4DVar:
         for ls in local + [n]:
             if ls <= prev:
                 continue
-            p.advance(B, self.traj, self.traj_steps, prev, ls - prev, self.hb_arg, self.qb_arg)
+            p.advance(B, self.traj, self.traj_steps, prev, ls - prev, self.hb_arg, self.qb_arg, self.qlo)
             prev = ls
             if with_obs:
                 self._obs_forward(a + ls, self.tv[ls * self.S, 0])
@@ -165,7 +172,9 @@ class QGWindows4DVar:
         for g in reversed(range(self.nseg)):
             a = g * K
             n = min(K, self.nstep - a)
-            self._copy(self.snap[g], self.tv[0])
+            self._copy(self.snap[g, :2], self.tv[0])
+            if self.qlo is not None:
+                self._copy(self.snap[g, 2], self.qlo)
             self._advance_segment(a, n, with_obs=False)
             prev = n
             local = sorted([s - a for s in self.obs_steps if a <= s < a + n] + [0], reverse=True)
@@ -182,7 +191,7 @@ class QGWindows4DVar:
         """Enqueue one cost+gradient evaluation for the control ``h0`` [B, ny, nx]."""
         p, B = self.plan, self.B
         self._copy(h0, self.tv[0, 0])
-        p.init_state(self.tv[0, 0], self.hb, self.tv[0, 1], self.qb)
+        p.init_state(self.tv[0, 0], self.hb, self.tv[0, 1], self.qb, self.qlo)
         if self.snap is None:
             self._forward_full()
         else:
@@ -195,7 +204,7 @@ class QGWindows4DVar:
             h0_state = self.tv[0, 0]
         else:
             self._reverse_ckpt()
-            self._copy(self.snap[0], self.tv[0])
+            self._copy(self.snap[0, :2], self.tv[0])
             h0_state = self.tv[0, 0]
         p.init_state_adj(B, h0_state, self.adq, self.adh)
         self._copy(self.adh, self.grad)
@@ -338,6 +347,9 @@ class QGBasis4DVar:
         self.snap = torch.zeros(self.nint, B, ny, nx, dtype=dt, device=dev)
         z = lambda: torch.zeros(B, ny, nx, dtype=dt, device=dev)  # noqa: E731
         self.h, self.F, self.adh, self.adq, self.adF = z(), z(), z(), z(), z()
+        # low part of the compensated PV state, re-derived with q at every
+        # interval start (float32 plans)
+        self.qlo = plan.new_qlo(B)
         self.X = torch.zeros(B, self.nb, dtype=dt, device=dev)
         self.adX = torch.zeros(B, self.nb, dtype=dt, device=dev)
         self.gb = torch.zeros(B, self.nb, dtype=dt, device=dev)
@@ -364,8 +376,8 @@ class QGBasis4DVar:
         p, B = self.plan, self.B
         n = self.cps[i + 1] - self.cps[i]
         self._copy(self.snap[i], self.tv[0, 0])
-        p.init_state(self.tv[0, 0], self.hb, self.tv[0, 1], self.qb)
-        p.advance(B, self.traj, self.K, 0, n, self.hb_arg, self.qb_arg)
+        p.init_state(self.tv[0, 0], self.hb, self.tv[0, 1], self.qb, self.qlo)
+        p.advance(B, self.traj, self.K, 0, n, self.hb_arg, self.qb_arg, self.qlo)
         return n
 
     def _run(self, X0):
@@ -395,9 +407,9 @@ class QGBasis4DVar:
                 self.basis.project(c // self.nstep_check, self.X, out=self.F)
             self._copy(self.h, self.snap[i])
             self._copy(self.h, self.tv[0, 0])
-            p.init_state(self.tv[0, 0], self.hb, self.tv[0, 1], self.qb)
+            p.init_state(self.tv[0, 0], self.hb, self.tv[0, 1], self.qb, self.qlo)
             n = self.cps[i + 1] - c
-            p.advance(B, self.traj, self.K, 0, n, self.hb_arg, self.qb_arg)
+            p.advance(B, self.traj, self.K, 0, n, self.hb_arg, self.qb_arg, self.qlo)
             _lib.call("vd_qg1l_force", p._h, B, _p(self.tv[n * self.S, 0]), _p(self.hb), _p(self.F),
                       _p(self.coef[i]), _p(self.h), _stream())
         if self.nstep in obs.step_range:

@@ -114,6 +114,8 @@ class QG1LPlan:
         self._h = handle
         self._lib = _lib.load()
         self.nstage = self._lib.vd_qg1l_nstage(self._h)
+        # float32 plans carry the PV state as a compensated pair (q, q_lo)
+        self.compensated = dtype == torch.float32
         self._ws = {}
 
     def __del__(self):
@@ -220,14 +222,20 @@ class QG1LPlan:
         return out
 
     # ---------------- state-level API (window engine) ----------------
-    def init_state(self, h, hb, q, qb):
-        _lib.call("vd_qg1l_init_state", self._h, h.shape[0] if h.dim() == 3 else 1, _ptr(h),
-                  _ptr(hb), _ptr(q), _ptr(qb), _stream())
+    def new_qlo(self, batch):
+        """Low-part buffer of the compensated PV state ([batch, ny, nx]), or
+        None for float64 plans, which step with the reference's plain
+        arithmetic."""
+        return self.field(batch) if self.compensated else None
 
-    def advance(self, batch, traj, traj_steps, first, nstep, hb, qb):
+    def init_state(self, h, hb, q, qb, qlo=None):
+        _lib.call("vd_qg1l_init_state", self._h, h.shape[0] if h.dim() == 3 else 1, _ptr(h),
+                  _ptr(hb), _ptr(q), _ptr(qb), _ptr(qlo), _stream())
+
+    def advance(self, batch, traj, traj_steps, first, nstep, hb, qb, qlo=None):
         ws = self.workspace(batch)
         _lib.call("vd_qg1l_advance", self._h, batch, _ptr(traj), int(traj_steps), int(first),
-                  int(nstep), _ptr(hb), _ptr(qb), _ptr(ws), ws.numel(), _stream())
+                  int(nstep), _ptr(hb), _ptr(qb), _ptr(qlo), _ptr(ws), ws.numel(), _stream())
 
     def advance_adj(self, batch, traj, traj_steps, first, nstep, adh, adq):
         ws = self.workspace(batch)
