@@ -17,6 +17,8 @@ Semantics kept from jax.numpy:
   what reverse mode stores), ``lax.reduce_window`` a sliding-window reduction,
   ``nn.softplus`` is log(1 + e^x) by ``logaddexp``;
 - ``jnp.clip(x, a_min=...)`` accepts a missing bound, as jax's does;
+- ``jnp.where(cond, size=n)`` pads / truncates the index arrays to n, and
+  ``jnp.add.at(a, idx, v, inplace=False)`` returns an updated copy;
 - ``vmap`` over axis 0 is a loop with stacked outputs; ``lax.dynamic_slice``
   and ``lax.dynamic_update_slice`` clamp their start indices into the operand,
   as XLA's do.
@@ -129,6 +131,42 @@ def _fori_loop(lower, upper, body, init):
     return val
 
 
+def _where(cond, x=None, y=None, size=None, fill_value=None):
+    """jnp.where, with jax's ``size`` form of the one-argument call: the first
+    ``size`` indices of each axis, padded with ``fill_value`` (0 by default)."""
+    if x is not None or y is not None:
+        return np.where(cond, x, y).view(JArray)
+    idx = np.nonzero(np.asarray(cond))
+    if size is None:
+        return tuple(i.view(JArray) for i in idx)
+    fill = 0 if fill_value is None else fill_value
+    out = []
+    for i in idx:
+        o = np.full(size, fill, dtype=i.dtype)
+        o[:min(size, i.size)] = i[:size]
+        out.append(o.view(JArray))
+    return tuple(out)
+
+
+class _UfuncAt:
+    """jnp.add / jnp.multiply with jax's functional ``.at(a, idx, v,
+    inplace=False)``: the update applied to a copy."""
+
+    def __init__(self, ufunc):
+        self._u = ufunc
+
+    def __call__(self, *args, **kwargs):
+        return _wrap(self._u)(*args, **kwargs)
+
+    def at(self, a, indices, values=None, inplace=True):
+        out = np.array(np.asarray(a), copy=True)
+        if values is None:
+            self._u.at(out, indices)
+        else:
+            self._u.at(out, indices, np.asarray(values))
+        return out.view(JArray)
+
+
 def _unavailable(*args, **kwargs):
     raise NotImplementedError("not available in the NumPy stand-in")
 
@@ -185,6 +223,8 @@ def install(enable_x64=True):
     jnp.fft = _NumpyNamespace("jax.numpy.fft", np.fft)
     jnp.linalg = _NumpyNamespace("jax.numpy.linalg", np.linalg)
     jnp.clip = _clip
+    jnp.where = _where
+    jnp.add = _UfuncAt(np.add)
     jax.numpy = jnp
     jax.jit = _jit
     jax.checkpoint = lambda f, **kw: f

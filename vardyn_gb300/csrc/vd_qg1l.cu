@@ -727,7 +727,7 @@ static int step_once(const vd_qg1l_plan* p, int nf, T* const* hsv, T* const* qsv
     const int B = tangent ? nf / 2 : nf;
     for (int s = 0; s < S; ++s) {
         const bool last = (s == S - 1);
-        StageIn<T> kin;
+        StageIn<T> kin{};
         kin.nk = 0;
         for (int i = 0; i < s; ++i) {
             const double c = last ? p->b[i] : p->A[s + 1][i];
@@ -845,14 +845,14 @@ int advance_adj_impl(const vd_qg1l_plan* p, int nf, const T* traj, int traj_step
         int rc = helmholtz_solve<T>(p, nf, a0, spec, st);
         if (rc) return rc;
         for (int s = S - 1; s >= 0; --s) {
-            StageIn<T> gin;
+            StageIn<T> gin{};
             gin.nk = 0;
             if (p->b[s] != 0.0) { gin.k[gin.nk] = Gb[0]; gin.c[gin.nk] = (T)p->b[s]; ++gin.nk; }
             for (int t = s + 1; t < S; ++t)
                 if (p->A[t][s] != 0.0) { gin.k[gin.nk] = Gb[t]; gin.c[gin.nk] = (T)p->A[t][s]; ++gin.nk; }
             const dim3 agrid((p->d.nx + AT_X - 1) / AT_X, (p->d.ny + AT_Y - 1) / AT_Y, nf);
             if (s >= 1) {
-                StageIn<T> none;
+                StageIn<T> none{};
                 none.nk = 0;
                 k_adj_stage_fused<T><<<agrid, kBlock, sizeof(AdjTile<T>), st>>>(p->geom, nf, tv.h(n, s),
                                                                                  tv.q(n, s), gin, none, adql, adhs);
@@ -863,7 +863,7 @@ int advance_adj_impl(const vd_qg1l_plan* p, int nf, const T* traj, int traj_step
                 rc = helmholtz_solve<T>(p, nf, a, spec, st);
                 if (rc) return rc;
             } else {
-                StageIn<T> acc;
+                StageIn<T> acc{};
                 acc.nk = 0;
                 for (int t = 0; t < S; ++t) { acc.k[acc.nk] = Gb[t]; acc.c[acc.nk] = T(1); ++acc.nk; }
                 k_adj_stage_fused<T><<<agrid, kBlock, sizeof(AdjTile<T>), st>>>(p->geom, nf, tv.h(n, s),

@@ -121,11 +121,17 @@ class AlongTrackObs:
     neighbours on excluded grid points dropped."""
 
     def __init__(self, windows, ny, nx, dx, dy, dtype=torch.float32, device="cuda", npix=4, build="gpu",
-                 exclude=None):
+                 exclude=None, operator=None):
+        """``operator`` (optional): one ``(idx, w)`` pair per window, arrays
+        [n, npix] of grid indices (-1 for no neighbour) and weights, for
+        operators built elsewhere (e.g. the reference's 3-D Cartesian
+        distances on a lon/lat grid); ``x_km`` / ``y_km`` are then unused."""
         if npix > 4:
             raise ValueError("at most 4 neighbours per observation")
         if build not in ("gpu", "host"):
             raise ValueError("build is 'gpu' or 'host'")
+        if operator is not None and len(operator) != len(windows):
+            raise ValueError("one (idx, w) operator per window")
         rows = interp_rows_gpu if build == "gpu" else interp_rows
         self.B = len(windows)
         self.ny, self.nx = ny, nx
@@ -134,8 +140,15 @@ class AlongTrackObs:
         self.device = torch.device(device)
         fields, steps, idxs, ws, ys, errs = [], [], [], [], [], []
         for b, win in enumerate(windows):
-            x = np.asarray(win["x_km"], dtype=np.float64)
-            idx, w = rows(x, np.asarray(win["y_km"], dtype=np.float64), ny, nx, dx, dy, npix, exclude=exclude)
+            if operator is not None:
+                idx = np.asarray(operator[b][0], dtype=np.int64).reshape(len(win["step"]), -1)
+                w = np.asarray(operator[b][1], dtype=np.float64).reshape(idx.shape)
+                if idx.shape[1] != npix:
+                    raise ValueError(f"operator rows of window {b} have {idx.shape[1]} entries, npix is {npix}")
+                x = idx[:, 0]
+            else:
+                x = np.asarray(win["x_km"], dtype=np.float64)
+                idx, w = rows(x, np.asarray(win["y_km"], dtype=np.float64), ny, nx, dx, dy, npix, exclude=exclude)
             pad = 4 - npix
             if pad:
                 idx = np.pad(idx, ((0, 0), (0, pad)), constant_values=-1)
