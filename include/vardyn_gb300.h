@@ -199,8 +199,33 @@ size_t vd_qg1l_spec_bytes(const vd_qg1l_plan* plan, int batch);
  * with X = 0 beyond the walls (equal to the y-DST / eigenvalue division /
  * y-DST of inverse_elliptic_dst, jqgm.py:83-91). */
 vd_status vd_qg1l_tridiag_y(const vd_qg1l_plan* plan, int batch, void* spec, void* stream);
+/* inverse == 2 runs the inverse pass with the adjoint epilogue of the
+ * solve: out = (mask == 3) ? x + field : 0 (field is the addend). */
 vd_status vd_qg1l_dst_x(const vd_qg1l_plan* plan, int batch, const void* field,
                         void* spec, int inverse, void* out, void* stream);
+
+/* One forward Runge-Kutta stage of Qgm.one_step (jqgm.py:480-503 with the
+ * scheme bodies of 398-477): k = rhs(h2uv(hs), qs) (jqgm.py:238-262,
+ * 321-396; 0 off the tendency points) and
+ * q_out = q_base + sum_t c[t] * k_in[t] + c_self * k. k_in is a host array of
+ * nk <= 4 device fields, c its host coefficients; k_out (nullable) receives
+ * k. The kernel of the library's own steps, launched alone. */
+vd_status vd_qg1l_rk_stage(const vd_qg1l_plan* plan, int batch, const void* hs,
+                           const void* qs, const void* q_base, int nk,
+                           const void* const* k_in, const double* c,
+                           double c_self, void* k_out, void* q_out,
+                           void* stream);
+/* Adjoint of the tendency of one stage (the vjp of jqgm.py:238-262, 321-396
+ * that step_adj takes through jax.vjp, jqgm.py:565-569): with the stage
+ * cotangent lk = sum_t c[t] * g[t] on the tendency points, adh_out = the
+ * SSH adjoint through h2uv, adq_out = (mask == 3) * (PV adjoint +
+ * sum_t acc[t]). g (ng <= 4) and acc (nacc <= 4) are host arrays of device
+ * fields, c host coefficients. */
+vd_status vd_qg1l_rk_stage_adj(const vd_qg1l_plan* plan, int batch,
+                               const void* hs, const void* qs, int ng,
+                               const void* const* g, const double* c, int nacc,
+                               const void* const* acc, void* adq_out,
+                               void* adh_out, void* stream);
 
 /* Forward model: Qgm.step (jqgm.py:517-557). h_out = M^nstep(h0) with
  * q0 = h2pv(h0, hb), land set to NaN. If traj != NULL (sized by

@@ -169,6 +169,8 @@ SIGNATURES = {
     "vd_qg1l_spec_bytes": (SZ, [P, I]),
     "vd_qg1l_tridiag_y": (I, [P, I, P, P]),
     "vd_qg1l_dst_x": (I, [P, I, P, P, I, P, P]),
+    "vd_qg1l_rk_stage": (I, [P, I, P, P, P, I, P, P, D, P, P, P]),
+    "vd_qg1l_rk_stage_adj": (I, [P, I, P, P, I, P, P, I, P, P, P, P]),
     "vd_qg1l_step": (I, [P, I, P, P, I, P, P, P, SZ, P]),
     "vd_qg1l_step_tgl": (I, [P, I, P, P, P, I, P, P, SZ, P]),
     "vd_qg1l_step_adj": (I, [P, I, P, P, P, I, P, P, I, P, SZ, P]),

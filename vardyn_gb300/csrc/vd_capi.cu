@@ -123,7 +123,8 @@ extern "C" size_t vd_qg1l_spec_bytes(const vd_qg1l_plan* p, int batch)
 extern "C" vd_status vd_qg1l_dst_x(const vd_qg1l_plan* p, int B, const void* field, void* spec, int inverse,
                                    void* out, void* stream)
 {
-    if (!p || B <= 0 || !spec || (!inverse && !field) || (inverse && !out)) return VD_ERR_ARG;
+    if (!p || B <= 0 || !spec || inverse < 0 || inverse > 2 || (inverse != 1 && !field) || (inverse && !out))
+        return VD_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     return p->d.dtype == VD_F32
                ? dst_x_only<float>(p, B, (const float*)field, (float*)spec, inverse, (float*)out, st)
@@ -426,6 +427,50 @@ extern "C" vd_status vd_qg1l_step_adj(const vd_qg1l_plan* p, int B, const void* 
                                    (float*)adh_out, (float*)traj, traj_ready, ws, st)
                : step_adj_t<double>(p, B, (const double*)adh1, (const double*)h0, (const double*)hb, nstep,
                                     (double*)adh_out, (double*)traj, traj_ready, ws, st);
+}
+
+namespace vd {
+template <typename T>
+int rk_stage_impl(const vd_qg1l_plan*, int, const T*, const T*, const T*, int, const T* const*, const double*,
+                  double, T*, T*, cudaStream_t);
+template <typename T>
+int rk_stage_adj_impl(const vd_qg1l_plan*, int, const T*, const T*, int, const T* const*, const double*, int,
+                      const T* const*, T*, T*, cudaStream_t);
+}
+
+extern "C" vd_status vd_qg1l_rk_stage(const vd_qg1l_plan* p, int B, const void* hs, const void* qs, const void* qbase,
+                                      int nk, const void* const* k, const double* c, double cself, void* k_out,
+                                      void* q_out, void* stream)
+{
+    if (!p || B <= 0 || !hs || !qs || !qbase || !q_out || nk < 0 || nk > 4 || (nk && (!k || !c))) return VD_ERR_ARG;
+    for (int t = 0; t < nk; ++t)
+        if (!k[t]) return VD_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    return p->d.dtype == VD_F32
+               ? rk_stage_impl<float>(p, B, (const float*)hs, (const float*)qs, (const float*)qbase, nk,
+                                      (const float* const*)k, c, cself, (float*)k_out, (float*)q_out, st)
+               : rk_stage_impl<double>(p, B, (const double*)hs, (const double*)qs, (const double*)qbase, nk,
+                                       (const double* const*)k, c, cself, (double*)k_out, (double*)q_out, st);
+}
+
+extern "C" vd_status vd_qg1l_rk_stage_adj(const vd_qg1l_plan* p, int B, const void* hs, const void* qs, int ng,
+                                          const void* const* g, const double* c, int nacc, const void* const* acc,
+                                          void* adq_out, void* adh_out, void* stream)
+{
+    if (!p || B <= 0 || !hs || !qs || !adq_out || !adh_out || ng < 0 || ng > 4 || nacc < 0 || nacc > 4 ||
+        (ng && (!g || !c)) || (nacc && !acc))
+        return VD_ERR_ARG;
+    for (int t = 0; t < ng; ++t)
+        if (!g[t]) return VD_ERR_ARG;
+    for (int t = 0; t < nacc; ++t)
+        if (!acc[t]) return VD_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    return p->d.dtype == VD_F32
+               ? rk_stage_adj_impl<float>(p, B, (const float*)hs, (const float*)qs, ng, (const float* const*)g, c,
+                                          nacc, (const float* const*)acc, (float*)adq_out, (float*)adh_out, st)
+               : rk_stage_adj_impl<double>(p, B, (const double*)hs, (const double*)qs, ng, (const double* const*)g,
+                                           c, nacc, (const double* const*)acc, (double*)adq_out, (double*)adh_out,
+                                           st);
 }
 
 extern "C" vd_status vd_qg1l_init_state(const vd_qg1l_plan* p, int B, const void* h, const void* hb, void* q,

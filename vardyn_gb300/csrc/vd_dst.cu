@@ -879,6 +879,10 @@ int dst_x_only(const vd_qg1l_plan* p, int nf, const T* field, T* spec, int inver
     SolveArgs a;
     a.src = field; a.sub = nullptr; a.sub_batches = 0;
     a.out = out; a.add = nullptr; a.add_batches = 0; a.epi = EPI_H;
+    if (inverse == 2) {            // adjoint epilogue: out = M3 * (x + field)
+        a.src = nullptr;
+        a.add = field; a.add_batches = nf; a.epi = EPI_ADJQ;
+    }
     const int tr = pick_tr<T>(p, g.R);
     if constexpr (sizeof(T) == 4) {
         if (p->dst.tc && tc_fits(p, nf)) return dst_pass_tc(p, nf, a, (float*)spec, !inverse, st);

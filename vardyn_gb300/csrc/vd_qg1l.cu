@@ -875,6 +875,48 @@ int advance_adj_impl(const vd_qg1l_plan* p, int nf, const T* traj, int traj_step
     return VD_OK;
 }
 
+// One forward stage and one adjoint stage on caller buffers: the kernels of
+// step_once / advance_adj_impl, launched alone (building blocks and kernel
+// timing).
+template <typename T>
+int rk_stage_impl(const vd_qg1l_plan* p, int nf, const T* hs, const T* qs, const T* qbase, int nk,
+                  const T* const* k, const double* c, double cself, T* kout, T* qout, cudaStream_t st)
+{
+    StageIn<T> kin{};
+    kin.nk = nk;
+    for (int t = 0; t < nk; ++t) { kin.k[t] = k[t]; kin.c[t] = (T)c[t]; }
+    k_stage_fwd<T><<<pgrid(p, nf), dim3(32, 4), 0, st>>>(p->geom, nf, hs, qs, qbase, kin, (T)cself, kout, qout,
+                                                         (T*)nullptr, 0);
+    VD_LAUNCH_CHECK();
+    return VD_OK;
+}
+
+template <typename T>
+int rk_stage_adj_impl(const vd_qg1l_plan* p, int nf, const T* hs, const T* qs, int ng, const T* const* g,
+                      const double* c, int nacc, const T* const* acc, T* adq_out, T* adh_out, cudaStream_t st)
+{
+    static PerDeviceOnce attr_once;
+    const cudaError_t attr_err = attr_once.run([]() -> cudaError_t {
+        cudaError_t e = cudaFuncSetAttribute(k_adj_stage_fused<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)sizeof(AdjTile<float>));
+        if (!e)
+            e = cudaFuncSetAttribute(k_adj_stage_fused<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)sizeof(AdjTile<double>));
+        return e;
+    });
+    if (attr_err != cudaSuccess) return VD_ERR_CUDA;
+    StageIn<T> gin{}, gac{};
+    gin.nk = ng;
+    for (int t = 0; t < ng; ++t) { gin.k[t] = g[t]; gin.c[t] = (T)c[t]; }
+    gac.nk = nacc;
+    for (int t = 0; t < nacc; ++t) { gac.k[t] = acc[t]; gac.c[t] = T(1); }
+    const dim3 agrid((p->d.nx + AT_X - 1) / AT_X, (p->d.ny + AT_Y - 1) / AT_Y, nf);
+    k_adj_stage_fused<T><<<agrid, kBlock, sizeof(AdjTile<T>), st>>>(p->geom, nf, hs, qs, gin, gac, adq_out,
+                                                                     adh_out);
+    VD_LAUNCH_CHECK();
+    return VD_OK;
+}
+
 template <typename T>
 int init_state_impl(const vd_qg1l_plan* p, int nf, int ntan0, const T* h, const T* hb, T* q, T* qb,
                     T* qlo, cudaStream_t st)
@@ -948,6 +990,10 @@ int rhs_impl(const vd_qg1l_plan* p, int nf, const T* u, const T* v, const T* q, 
 }
 
 #define VD_INST(T)                                                                                        \
+    template int rk_stage_impl<T>(const vd_qg1l_plan*, int, const T*, const T*, const T*, int, const T* const*, \
+                                  const double*, double, T*, T*, cudaStream_t);                           \
+    template int rk_stage_adj_impl<T>(const vd_qg1l_plan*, int, const T*, const T*, int, const T* const*,  \
+                                      const double*, int, const T* const*, T*, T*, cudaStream_t);         \
     template int advance_impl<T>(const vd_qg1l_plan*, int, T*, int, int, int, const T*, const T*, T*,     \
                                  Arena&, cudaStream_t);                                                   \
     template int forward_nostore<T>(const vd_qg1l_plan*, int, T*, T*, int, const T*, const T*, T*,        \

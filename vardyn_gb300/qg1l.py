@@ -221,6 +221,33 @@ class QG1LPlan:
                   _ptr(out), _ptr(traj), int(bool(traj_ready)), _ptr(ws), ws.numel(), _stream())
         return out
 
+    def rk_stage(self, hs, qs, qbase, k=(), c=(), cself=0.0, k_out=None):
+        """One forward Runge-Kutta stage (vd_qg1l_rk_stage): returns
+        q_out = qbase + sum c[t] k[t] + cself * rhs(h2uv(hs), qs)."""
+        hs, qs, qbase = self._as_batch(hs, "hs"), self._as_batch(qs, "qs"), self._as_batch(qbase, "qbase")
+        ks = [self._as_batch(x, "k") for x in k]
+        kp = (ctypes.c_void_p * max(1, len(ks)))(*[x.data_ptr() for x in ks])
+        cp = (ctypes.c_double * max(1, len(ks)))(*[float(x) for x in c])
+        q_out = torch.empty_like(qs)
+        _lib.call("vd_qg1l_rk_stage", self._h, qs.shape[0], _ptr(hs), _ptr(qs), _ptr(qbase), len(ks), kp, cp,
+                  float(cself), _ptr(k_out), _ptr(q_out), _stream())
+        return q_out
+
+    def rk_stage_adj(self, hs, qs, g=(), c=(), acc=()):
+        """Adjoint of one stage's tendency (vd_qg1l_rk_stage_adj): returns
+        (adq, adh) for the stage cotangent sum c[t] g[t] plus the addends acc
+        (on the tendency points)."""
+        hs, qs = self._as_batch(hs, "hs"), self._as_batch(qs, "qs")
+        gs = [self._as_batch(x, "g") for x in g]
+        ac = [self._as_batch(x, "acc") for x in acc]
+        gp = (ctypes.c_void_p * max(1, len(gs)))(*[x.data_ptr() for x in gs])
+        cp = (ctypes.c_double * max(1, len(gs)))(*[float(x) for x in c])
+        ap = (ctypes.c_void_p * max(1, len(ac)))(*[x.data_ptr() for x in ac])
+        adq, adh = torch.empty_like(qs), torch.empty_like(qs)
+        _lib.call("vd_qg1l_rk_stage_adj", self._h, qs.shape[0], _ptr(hs), _ptr(qs), len(gs), gp, cp, len(ac), ap,
+                  _ptr(adq), _ptr(adh), _stream())
+        return adq, adh
+
     # ---------------- state-level API (window engine) ----------------
     def new_qlo(self, batch):
         """Low-part buffer of the compensated PV state ([batch, ny, nx]), or
