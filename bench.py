@@ -474,8 +474,18 @@ def gpu_arm(args):
         ms_c, _ = time_graph(eng_c, x, 2, max(2, args.steps // 4))
         ckpt = {"evals_per_s": B / (ms_c / 1e3), "ms_per_eval_batch": ms_c,
                 "schedule": f"snapshot every {K} steps, one recompute of each segment in reverse",
-                "memory_gb": eng_c.memory_bytes() / 1e9}
+                "memory_gb": eng_c.memory_bytes() / 1e9, "recomputed_steps": eng_c.recomputed_steps()}
         del eng_c
+        torch.cuda.empty_cache()
+        # binomial (revolve) schedule: 40 snapshot slots over units of 4 steps
+        rv = ("revolve", 40, 4)
+        _, _, eng_r, _ = setup_engine(B, n, nstep, NOBS, checkpoint=rv)
+        eng_r.capture()
+        ms_r, _ = time_graph(eng_r, x, 2, max(2, args.steps // 4))
+        ckpt["revolve"] = {"evals_per_s": B / (ms_r / 1e3), "ms_per_eval_batch": ms_r,
+                           "schedule": f"binomial (revolve), {rv[1]} snapshot slots, units of {rv[2]} steps",
+                           "memory_gb": eng_r.memory_bytes() / 1e9, "recomputed_steps": eng_r.recomputed_steps()}
+        del eng_r
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",

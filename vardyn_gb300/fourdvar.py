@@ -24,6 +24,11 @@ Trajectory storage: ``full`` keeps every stage state of every step (the
 state every K steps and recomputes each K-step segment during the reverse
 sweep (one extra forward, memory (nstep/K)*2 + 2*nstage*K fields).
 
+``checkpoint=("revolve", slots, unit)`` keeps at most slots + 1 snapshots
+and one unit's trajectory and follows a binomial schedule
+(:func:`revolve_schedule`): the memory of a few fields for a bounded number
+of recomputations, for windows or batches whose snapshots would not fit.
+
 Float32 plans carry the prognostic PV as a compensated pair (q, q_lo): the
 low part is one running field, saved with every snapshot so that a
 recomputed segment repeats the forward sweep bit for bit.
@@ -44,6 +49,65 @@ def _p(t):
 
 def _stream():
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def binomial_reach(slots, reps):
+    """Units that a binomial schedule with ``slots`` free snapshot slots and
+    at most ``reps`` forward repetitions of any unit can reverse:
+    C(slots + reps, slots) (Griewank and Walther, Algorithm 799: revolve)."""
+    return math.comb(slots + reps, slots)
+
+
+def revolve_schedule(n_units, slots):
+    """Binomial checkpointing schedule for reversing ``n_units`` time units
+    with ``slots`` snapshot slots beyond the one holding the initial state.
+
+    Returns a list of actions, executed in order:
+      ("advance", a, b)  run units a .. b-1 forward from the current state
+                         (no trajectory kept), leaving the state at unit b;
+      ("save", b)        push the current state (at unit b) on the snapshot stack;
+      ("restore", a)     make the snapshot on top of the stack (at unit a) the
+                         current state (the snapshot stays);
+      ("drop", a)        pop the snapshot at unit a;
+      ("reverse", u)     run unit u forward keeping its trajectory, then its
+                         adjoint (the current state is at unit u).
+    The recursion splits [a, b) at m so that the right part, reversed with one
+    slot fewer, holds at most binomial_reach(slots - 1, r) units and the left
+    part, reversed after the right one frees its slot, at most
+    binomial_reach(slots, r - 1), with r the smallest repetition count that
+    reaches b - a; without free slots, every unit is recomputed from a."""
+    acts = []
+
+    def rev(a, b, free):
+        n = b - a
+        if n == 1:
+            acts.append(("reverse", a))
+            return
+        if free == 0:
+            for u in range(b - 1, a - 1, -1):
+                if u > a:
+                    acts.append(("advance", a, u))
+                acts.append(("reverse", u))
+                if u > a:
+                    acts.append(("restore", a))
+            return
+        r = 1
+        while binomial_reach(free, r) < n:
+            r += 1
+        right = max(1, min(n - 1, binomial_reach(free - 1, r)))
+        m = b - right
+        acts.append(("advance", a, m))
+        acts.append(("save", m))
+        rev(m, b, free - 1)
+        acts.append(("drop", m))
+        acts.append(("restore", a))
+        rev(a, m, free)
+
+    if n_units > 0:
+        acts.append(("save", 0))
+        rev(0, n_units, slots)
+        acts.append(("drop", 0))
+    return acts
 
 
 class QGWindows4DVar:
@@ -77,7 +141,21 @@ class QGWindows4DVar:
         self.hb_arg = None if zero_bg else self.hb
         self.checkpoint = checkpoint
         S = plan.nstage
-        if checkpoint is None:
+        self.revolve = isinstance(checkpoint, (tuple, list)) and len(checkpoint) == 3 and checkpoint[0] == "revolve"
+        if self.revolve:
+            # binomial schedule over units of `unit` steps with `slots`
+            # snapshot slots (plus the initial state)
+            _, slots, unit = checkpoint
+            self.unit, self.slots = int(unit), int(slots)
+            if self.unit < 1 or self.slots < 0:
+                raise ValueError("revolve needs unit >= 1 and slots >= 0")
+            self.nunit = math.ceil(self.nstep / self.unit)
+            self.schedule = revolve_schedule(self.nunit, self.slots)
+            self.traj = plan.new_traj(B, self.unit)
+            self.traj_steps = self.unit
+            self.stack = torch.zeros(self.slots + 1, 2 if self.qlo is None else 3, B, ny, nx, dtype=dt, device=dev)
+            self.snap = None
+        elif checkpoint is None:
             self.traj = plan.new_traj(B, self.nstep)
             self.traj_steps = self.nstep
             self.snap = None
@@ -98,7 +176,19 @@ class QGWindows4DVar:
         n = self.traj.numel() * self.traj.element_size()
         if self.snap is not None:
             n += self.snap.numel() * self.snap.element_size()
+        if self.revolve:
+            n += self.stack.numel() * self.stack.element_size()
         return n
+
+    def recomputed_steps(self):
+        """Forward steps the reverse sweep repeats (revolve: the schedule's
+        advances plus the taping run of every unit; two-level: one more
+        forward; full trajectory: none)."""
+        if self.revolve:
+            adv = sum(min(b * self.unit, self.nstep) - a * self.unit
+                      for act, *ab in self.schedule if act == "advance" for a, b in [ab])
+            return adv + self.nstep
+        return 0 if self.snap is None else self.nstep
 
     def _copy(self, src, dst):
         _lib.call("vd_copy", self.vd_dtype, ctypes.c_longlong(src.numel()), _p(src), _p(dst), _stream())
@@ -186,12 +276,79 @@ class QGWindows4DVar:
                 if (a + ls) in self.obs.step_range:
                     self.obs.apply_adjoint(a + ls, self.adh)
 
+    def _run_revolve(self):
+        """Execute the binomial schedule: the first pass over a step computes
+        its misfits (every step is first reached, in order, by the schedule's
+        initial descent); later passes only recompute the trajectory."""
+        p, B, L = self.plan, self.B, self.unit
+        frontier = 0                  # steps whose misfits exist
+        depth = 0
+
+        def span(u):
+            a = u * L
+            return a, min(L, self.nstep - a)
+
+        def copy_state(dst):
+            self._copy(self.tv[0], dst[:2])
+            if self.qlo is not None:
+                self._copy(self.qlo, dst[2])
+
+        def load_state(src):
+            self._copy(src[:2], self.tv[0])
+            if self.qlo is not None:
+                self._copy(src[2], self.qlo)
+
+        self._obs_forward(0, self.tv[0, 0])
+        for act in self.schedule:
+            kind = act[0]
+            if kind == "advance":
+                for u in range(act[1], act[2]):
+                    a, n = span(u)
+                    self._advance_segment(a, n, with_obs=a + n > frontier)
+                    frontier = max(frontier, a + n)
+                    self._copy(self.tv[n * self.S], self.tv[0])
+            elif kind == "save":
+                copy_state(self.stack[depth])
+                depth += 1
+            elif kind == "restore":
+                load_state(self.stack[depth - 1])
+            elif kind == "drop":
+                depth -= 1
+            else:                                     # reverse one unit
+                u = act[1]
+                a, n = span(u)
+                self._advance_segment(a, n, with_obs=a + n > frontier)
+                if a + n > frontier:
+                    frontier = a + n
+                    if a + n == self.nstep:
+                        # the window's last misfits exist now: the cost and
+                        # the final observation adjoint
+                        self.obs.sumsq_per_window(self.J, 0.5 / self.sigma_R ** 2)
+                        if self.nstep in self.obs.step_range:
+                            self.obs.apply_adjoint(self.nstep, self.adh)
+                prev = n
+                local = sorted([s - a for s in self.obs_steps if a <= s < a + n] + [0], reverse=True)
+                for ls in local:
+                    if ls >= prev:
+                        continue
+                    p.advance_adj(B, self.traj, self.traj_steps, ls, prev - ls, self.adh, self.adq)
+                    prev = ls
+                    if (a + ls) in self.obs.step_range:
+                        self.obs.apply_adjoint(a + ls, self.adh)
+
     # ------------------------------------------------------------------
     def _run(self, h0):
         """Enqueue one cost+gradient evaluation for the control ``h0`` [B, ny, nx]."""
         p, B = self.plan, self.B
         self._copy(h0, self.tv[0, 0])
         p.init_state(self.tv[0, 0], self.hb, self.tv[0, 1], self.qb, self.qlo)
+        if self.revolve:
+            self._fill0(self.adh)
+            self._fill0(self.adq)
+            self._run_revolve()
+            p.init_state_adj(B, self.tv[0, 0], self.adq, self.adh)
+            self._copy(self.adh, self.grad)
+            return
         if self.snap is None:
             self._forward_full()
         else:
