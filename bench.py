@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--profile-small", action="store_true",
                     help="short window for profiler captures (not a bench value)")
-    ap.add_argument("--workload", default="qg512", choices=["qg512", "basis1024", "mixed64", "sw3l", "aux"],
+    ap.add_argument("--workload", default="qg512", choices=["qg512", "basis1024", "mixed64", "sw3l", "qg3l", "aux"],
                     help="qg512: control = initial SSH, 512^2, batched windows (the headline); "
                          "basis1024: reduced-basis control forcing the SSH, 1024^2, one window; "
                          "mixed64: 64 windows of mixed sizes 128^2..768^2, 10 days; "
@@ -1064,6 +1064,93 @@ def gpu_arm_sw(args):
     print(json.dumps(line))
 
 
+Q5_METRIC = "QG 3-layer 1024x768 with 20% land, multigrid PV inversion: model steps/s (forward + adjoint)"
+
+
+def gpu_arm_qg(args):
+    """The config-5 case as specified: 3-layer QG (qg.py via projected SW) on
+    1024 x 768 at 5 km with ~20 % land, the PV inverted per vertical mode by
+    the masked Dirichlet multigrid in float64 (relative residual 1e-8) while
+    the model runs in float32. One bench step is the forward and the adjoint
+    of a 20-step window (dt = 600 s)."""
+    import scipy.sparse.linalg as spla
+    import torch
+    from vardyn_gb300 import build, _lib
+    from vardyn_gb300.qg_ml import QGPlan
+    build.build()
+    L = _lib.load()
+    nstep = S5_NSTEP if args.nstep == NSTEP else args.nstep
+    nx, ny, nl = S5_NX, S5_NY, S5_NL
+    yw = np.arange(ny + 1)[None, :] * S5_DX + np.zeros((nx + 1, 1))
+    f = 1.0e-4 + 1.6e-11 * (yw - yw.mean())
+    mask = s5_land(nx, ny)
+    dt = 600.0
+    plan = QGPlan(nx, ny, nl, S5_DX, S5_DX, f, np.array(S5_H), np.array(S5_GP), dt, mask=mask, slip_coef=1.0,
+                  bottom_drag_coef=1e-7, visc_coef=50.0, diff_coef=20.0, dtype=torch.float32,
+                  inversion="multigrid", mg_tol=1e-8, mg_max_cycles=24, mg_dtype=torch.float64)
+    rng = np.random.default_rng(5001)
+    m = plan.masks
+    x = [torch.as_tensor(a, dtype=torch.float32, device="cuda") for a in
+         (0.1 * rng.standard_normal((1, nl, nx + 1, ny)) * m.u, 0.1 * rng.standard_normal((1, nl, nx, ny + 1)) * m.v,
+          0.5 * rng.standard_normal((1, nl, nx, ny)) * m.h)]
+    w = [torch.as_tensor(rng.standard_normal(a.shape), dtype=torch.float32, device="cuda") for a in x]
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def step():
+        plan.step(*x, nstep=nstep)
+        plan.step_adj(*x, *w, nstep=nstep)
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    sampler = ClockSampler()
+    c0 = L.vd_launch_count()
+    sampler.start()
+    e0.record(st)
+    for _ in range(args.steps):
+        step()
+    e1.record(st)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    launches = L.vd_launch_count() - c0
+    ms = e0.elapsed_time(e1) / args.steps
+    # one inversion of the three modes (float64 multigrid to 1e-8)
+    X, Y = nx + 1, ny + 1
+    q = torch.as_tensor(rng.standard_normal((nl, 1, X, Y)) * 1e-9, dtype=torch.float64, device="cuda")
+    sol = torch.zeros_like(q)
+    plan.mg.solve_strided(1, q[:, :, 1:, 1:], Y, X * Y, sol[:, :, 1:, 1:], Y, X * Y)
+    torch.cuda.synchronize()
+    e0.record(st)
+    reps = 5
+    for _ in range(reps):
+        plan.mg.solve_strided(1, q[:, :, 1:, 1:], Y, X * Y, sol[:, :, 1:, 1:], Y, X * Y)
+    e1.record(st)
+    torch.cuda.synchronize()
+    mg_ms = e0.elapsed_time(e1) / reps
+    mg_rel = plan.mg.rel.cpu().numpy().tolist()
+    # CPU: one mode's masked Dirichlet system by a direct sparse solve (the
+    # oracle's check), float64
+    from oracle.helmholtz_masked import dirichlet_operator
+    A, oc = dirichlet_operator(nx - 1, ny - 1, S5_DX, S5_DX, plan.f0 ** 2 * plan.lambd[0],
+                               np.asarray(m.psi, dtype=np.float64)[1:-1, 1:-1])
+    rhs = q[0, 0, 1:-1, 1:-1].cpu().numpy()[oc[:, 0], oc[:, 1]]
+    t0 = time.perf_counter()
+    spla.spsolve(A.tocsc(), rhs)
+    cpu_s = time.perf_counter() - t0
+    line = {"metric": Q5_METRIC, "value": 2 * nstep / (ms / 1e3), "unit": "steps/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (multigrid f64)", "data": "synthetic",
+            "config": {"workload": f"QG {nl}-layer {nx}x{ny} dx=5km, H={S5_H}, g'={S5_GP}, beta plane, "
+                                   f"{100 * (1 - mask.mean()):.0f}% land (seeded smooth field), dt={dt:.0f}s, "
+                                   f"one step = forward + adjoint of a {nstep}-step window; PV inverted per mode "
+                                   f"by the masked Dirichlet multigrid (float64, relative residual 1e-8)",
+                       "mg_levels": plan.mg.levels, "mg_coarse_unknowns": plan.mg.coarse_unknowns},
+            "inversion": {"modes": nl, "gpu_ms_per_solve": mg_ms, "relative_residual": mg_rel,
+                          "cpu_spsolve_one_mode_s": cpu_s},
+            "e2e": None, "gpu_launches": int(launches), "clocks": clocks}
+    print(json.dumps(line))
+
+
 def cpu_sample_sw(nstep_sample=1):
     """The float64 NumPy restatement (oracle/sw.py) on the host cores: forward
     steps of the same 3-layer 1024 x 768 domain (the oracle has no adjoint;
@@ -1288,6 +1375,8 @@ def main():
         gpu_arm_basis(args)
     elif args.workload == "mixed64":
         gpu_arm_mixed(args)
+    elif args.workload == "qg3l":
+        gpu_arm_qg(args)
     elif args.workload == "sw3l":
         gpu_arm_sw(args)
     elif args.workload == "aux":

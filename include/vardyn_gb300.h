@@ -522,6 +522,43 @@ vd_status vd_mg_residual(const vd_mg_plan* plan, const void* f, const void* rhs,
                          void* stream);
 
 /* ------------------------------------------------------------------------
+ * Masked Dirichlet multigrid for the PV inversion of the multilayer QG
+ * model on a domain with land (mapping/models/model_qgsw/qg.py:222-298, the
+ * problem the reference solves with a DST and a capacitance-matrix
+ * correction, helmholtz.py:146-184): per mode m, on n0 x n1 interior psi
+ * nodes, (u_E + u_W - 2u)/d0^2 + (u_N + u_S - 2u)/d1^2 - lambda_m u = b at
+ * nodes with mask != 0, u = 0 at masked nodes and beyond the boundary.
+ * Node-centred geometric V-cycles (red-black Gauss-Seidel, full weighting,
+ * bilinear prolongation) preconditioning conjugate gradients, the coarsest
+ * level solved with a float64 inverse;
+ * a solve stops each system at ||b - A u|| <= tol ||b|| (float64 norms) or
+ * after max_cycles. No counterpart class in the reference.
+ * ------------------------------------------------------------------------ */
+typedef struct vd_mgd_plan vd_mgd_plan;
+typedef struct vd_mgd_desc {
+    int n0, n1;                 /* interior nodes; coarsening needs n+1 even */
+    int nmode;                  /* systems per batch entry (vertical modes) */
+    int dtype;                  /* VD_F32 | VD_F64 */
+    double d0, d1;              /* node spacings */
+    const double* lambda_host;  /* [nmode] */
+    const double* mask_host;    /* [n0][n1], 0 = land (Dirichlet 0); NULL: none */
+    int max_cycles;             /* conjugate-gradient iterations at most */
+    double tol;                 /* relative residual that stops a system */
+} vd_mgd_desc;
+vd_status vd_mgd_plan_create(vd_mgd_plan** out, const vd_mgd_desc* desc);
+vd_status vd_mgd_plan_destroy(vd_mgd_plan* plan);
+int vd_mgd_levels(const vd_mgd_plan* plan);
+int vd_mgd_coarse_unknowns(const vd_mgd_plan* plan);
+size_t vd_mgd_workspace_bytes(const vd_mgd_plan* plan, int batch);
+/* u = A^-1 b for batch * nmode systems, system s = m * batch + k using
+ * lambda_m; element (i, j) of system s at b[s * fsb + i * ldb + j] (and the
+ * same for u with ldu / fsu), so the interior of a padded field is solved in
+ * place. rel (device, nullable): [batch * nmode] relative residual reached. */
+vd_status vd_mgd_solve(const vd_mgd_plan* plan, int batch, const void* b, long long ldb,
+                       long long fsb, void* u, long long ldu, long long fsu, double* rel,
+                       void* workspace, size_t workspace_bytes, void* stream);
+
+/* ------------------------------------------------------------------------
  * Spectral Helmholtz helpers (mapping/models/model_qgsw/helmholtz.py). The
  * DST-I solve of one mode, div grad u - s u = rhs with Dirichlet walls
  * (solve_helmholtz_dstI, 138-143), is vd_qg1l_pv2h of a plan built with

@@ -13,10 +13,14 @@ stand-in for ``jax`` (``tests/golden/gen_golden*.py``):
   ``helmholtz_mg``);
 - the shallow-water model and the QG projector (``sw``, ``qg_ml``);
 - both observation operators (``obsop``);
-- the Gaussian, wave-packet and wavelet bases (``basis``).
+- the Gaussian, wave-packet and wavelet bases (``basis``);
+- the 4D-Var cost/gradient assembly (``fourdvar``): golden J and G from the
+  reference's own Variational.cost_and_grad with Model_qg1l_jax, the jax
+  observation operator and Basis_gauss3d, its two jax.vjp uses taking the
+  pinned adjoint restatements (``gen_golden_fourdvar.py``).
 
-The tangent/adjoint restatements are pinned by finite differences of the
-pinned forwards and by dot-product tests. The 4D-Var cost/gradient assembly
-(``fourdvar``) is pinned by properties only: producing the reference's needs
-jax's vjp.
+``helmholtz_masked`` (direct sparse solve of the masked Dirichlet problem the
+multigrid inversion solves) equals the reference's capacitance-matrix
+solutions on the ocean nodes. The tangent/adjoint restatements are pinned by
+finite differences of the pinned forwards and by dot-product tests.
 """

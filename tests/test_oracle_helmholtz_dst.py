@@ -81,3 +81,24 @@ def test_infer_rejects_other_operators(g):
         _infer(h)
     with pytest.raises(ValueError):
         _infer(compute_laplace_dstI(NX, NY, DX, DY) + 1e-6)   # negative shift
+
+
+def test_direct_masked_solve_equals_reference_capacitance_solve(g):
+    """The direct sparse solve of the masked Dirichlet problem
+    (oracle/helmholtz_masked.py, the checker of the multigrid) equals the
+    reference's capacitance-matrix solution (golden vectors of helmholtz.py)
+    on every ocean node: both solve the 5-point problem with u = 0 at the
+    land points next to the ocean."""
+    from oracle.helmholtz_masked import solve
+    helm = helm_of(g)
+    mask = g["helm_mask"]
+    nl = helm.shape[-3]
+    rhs = np.asarray(g["helm_rhs"])
+    want = np.asarray(g["helm_cmm_sol"])
+    inner = mask[..., 1:-1, 1:-1] if mask.ndim == 2 else mask.reshape(mask.shape[-2:])[1:-1, 1:-1]
+    nx, ny = NX, NY
+    shifts = [0.0] + [F0 ** 2 * float(g["helm_lam"][m]) for m in range(1, nl)]
+    for m in range(nl):
+        u = solve(nx - 1, ny - 1, DX, DY, shifts[m], inner, rhs.reshape((nl,) + rhs.shape[-2:])[m] * inner)
+        w = want.reshape((nl,) + want.shape[-2:])[m][1:-1, 1:-1]
+        assert np.abs(u - w * inner).max() <= 1e-11 * np.abs(w).max()

@@ -72,6 +72,16 @@ class VdBmParams(ctypes.Structure):
     ]
 
 
+class VdMgdDesc(ctypes.Structure):
+    _fields_ = [
+        ("n0", ctypes.c_int), ("n1", ctypes.c_int), ("nmode", ctypes.c_int), ("dtype", ctypes.c_int),
+        ("d0", ctypes.c_double), ("d1", ctypes.c_double),
+        ("lambda_host", ctypes.POINTER(ctypes.c_double)),
+        ("mask_host", ctypes.POINTER(ctypes.c_double)),
+        ("max_cycles", ctypes.c_int), ("tol", ctypes.c_double),
+    ]
+
+
 class VdMgDesc(ctypes.Structure):
     _fields_ = [
         ("n0", ctypes.c_int), ("n1", ctypes.c_int), ("nsys", ctypes.c_int), ("dtype", ctypes.c_int),
@@ -239,6 +249,12 @@ SIGNATURES = {
     "vd_mg_workspace_bytes": (SZ, [P]),
     "vd_mg_solve": (I, [P, P, P, P, SZ, P]),
     "vd_mg_residual": (I, [P, P, P, P, P]),
+    "vd_mgd_plan_create": (I, [ctypes.POINTER(P), ctypes.POINTER(VdMgdDesc)]),
+    "vd_mgd_plan_destroy": (I, [P]),
+    "vd_mgd_levels": (I, [P]),
+    "vd_mgd_coarse_unknowns": (I, [P]),
+    "vd_mgd_workspace_bytes": (SZ, [P, I]),
+    "vd_mgd_solve": (I, [P, I, P, LL, LL, P, LL, LL, P, P, SZ, P]),
     "vd_bm_plan_create": (I, [ctypes.POINTER(P), ctypes.POINTER(VdBasisGrid), ctypes.POINTER(VdBmParams)]),
     "vd_wavelet_plan_create": (I, [ctypes.POINTER(P), ctypes.POINTER(VdBasisGrid), ctypes.POINTER(VdWaveletParams)]),
     "vd_bm_plan_destroy": (I, [P]),

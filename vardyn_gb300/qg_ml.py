@@ -11,6 +11,12 @@ tendency and the adjoint applies P^T = Q^T (Q o G)^-T G^T: the DST solve is
 symmetric, edge padding and the capacitance correction are transposed
 explicitly.
 
+``inversion="multigrid"`` replaces the DST + capacitance inversion by a
+masked Dirichlet multigrid (vd_mgd_*) solving the same discrete problem per
+mode: on domains with many irregular boundary points (20 % land) the
+capacitance set-up, one DST solve per point and an M x M inverse, is out of
+reach.
+
 Deviations needed to run at all (``QG.step`` fails in the reference as
 shipped, see oracle/qg_ml.py): the SW step passes its reference values and
 wind arguments through QG's overrides, and QG's wind term
@@ -23,6 +29,7 @@ import torch
 
 from . import _lib
 from .helmholtz_dst import HelmholtzDST
+from .helmholtz_mg import MaskedDirichletMG
 from .qg1l import _ptr, _stream
 from .sw import SWPlan
 
@@ -69,7 +76,8 @@ class QGPlan:
     def __init__(self, nx, ny, nl, dx, dy, f, H, g_prime, dt, mask=None, slip_coef=1.0, bottom_drag_coef=0.0,
                  h_min=0.1, h_min_sharpness=10.0, visc_coef=0.0, diff_coef=0.0, sponge_coef=0.0, flag_linear=False,
                  forcing_momentum="direct", taux=0.0, tauy=0.0, sponge_u=None, sponge_v=None, sponge_h=None,
-                 dtype=torch.float64, device=None):
+                 dtype=torch.float64, device=None, inversion="spectral", mg_tol=1e-8, mg_max_cycles=24,
+                 mg_dtype=None):
         self.nx, self.ny, self.nl = int(nx), int(ny), int(nl)
         nx, ny, nl = self.nx, self.ny, self.nl
         Hc = np.asarray(H, dtype=np.float64)
@@ -94,7 +102,19 @@ class QGPlan:
         self.helm = HelmholtzDST(nx, ny, self.dx, self.dy, self.f0 ** 2 * self.lambd, dtype=dtype,
                                  device=self.device)
         m = self.masks
-        self.cmm = m.psi_irrbound_xids.size > 0
+        if inversion not in ("spectral", "multigrid"):
+            raise ValueError("inversion is 'spectral' (DST + capacitance matrices, the reference's) or 'multigrid'")
+        self.inversion = inversion
+        self.masked = m.psi_irrbound_xids.size > 0
+        # the capacitance branch only for the spectral inversion; the
+        # multigrid solves the masked Dirichlet problem directly
+        self.cmm = self.masked and inversion == "spectral"
+        self.mg = None
+        if inversion == "multigrid":
+            self.mg = MaskedDirichletMG(nx - 1, ny - 1, self.dx, self.dy, self.f0 ** 2 * self.lambd,
+                                        mask=np.asarray(m.psi, dtype=np.float64)[1:-1, 1:-1],
+                                        dtype=dtype if mg_dtype is None else mg_dtype, tol=mg_tol,
+                                        max_cycles=mg_max_cycles, device=self.device)
         self._dt = _lib.VD_F64 if dtype == torch.float64 else _lib.VD_F32
         X, Y = nx + 1, ny + 1
         self.psi = torch.as_tensor(m.psi, dtype=dtype, device=self.device).contiguous()
@@ -111,14 +131,14 @@ class QGPlan:
         d.dx, d.dy, d.f0 = self.dx, self.dy, self.f0
         d.H_host, d.A_host, d.Cl2m_host, d.Cm2l_host = (dp(a) for a in keep)
         d.mask_host = None if mk is None else dp(mk)
-        d.cmm = 1 if self.cmm else 0
+        d.cmm = 1 if self.masked else 0          # Q masks the modal rhs on land
         h = ctypes.c_void_p()
         _lib.call("vd_qgp_plan_create", ctypes.byref(h), ctypes.byref(d))
         self._q = h
         self._lib = _lib.load()
         # homogeneous solutions (qg.py:87-98)
         q = torch.zeros((nl, 1, X, Y), dtype=dtype, device=self.device)
-        q[..., 1:-1, 1:-1] = self.psi[1:-1, 1:-1] if self.cmm else 1.0
+        q[..., 1:-1, 1:-1] = self.psi[1:-1, 1:-1] if self.masked else 1.0
         sol = self._solve(q)[:, 0]
         shift = torch.as_tensor(self.f0 ** 2 * self.lambd, dtype=dtype, device=self.device).reshape(nl, 1, 1)
         self.homsol = (1.0 + sol * shift).contiguous()
@@ -143,10 +163,29 @@ class QGPlan:
         self.helm._solve_modes(q, out)
         return out
 
+    def _mg_interior(self, src, dst):
+        """dst interior = multigrid solve of src interior ([nl][B][X][Y], in
+        place on the padded fields: system m*B + b)."""
+        X, Y = self.nx + 1, self.ny + 1
+        if self.mg.dtype != src.dtype:
+            # float32 model, float64 inversion (a 1e-8 relative residual is
+            # below float32 resolution)
+            s64, d64 = src.to(self.mg.dtype), torch.zeros(dst.shape, dtype=self.mg.dtype, device=dst.device)
+            self.mg.solve_strided(src.shape[1], s64[:, :, 1:, 1:], Y, X * Y, d64[:, :, 1:, 1:], Y, X * Y)
+            return dst.copy_(d64)
+        self.mg.solve_strided(src.shape[1], src[:, :, 1:, 1:], Y, X * Y, dst[:, :, 1:, 1:], Y, X * Y)
+        return dst
+
     def _solve(self, q):
         """Modal solutions of QoG_inv (qg.py:272-280), [nl][B][nx+1][ny+1]
-        edge-padded (times psi in the capacitance branch)."""
+        edge-padded (times psi in the capacitance branch and, on a masked
+        domain, in the multigrid branch)."""
         nl, B = q.shape[0], q.shape[1]
+        if self.inversion == "multigrid":
+            s = self._mg_interior(q, torch.zeros_like(q))
+            out = torch.empty_like(s)
+            self.helm._edge_pad(s, out, self.psi if self.masked else None)
+            return out
         s = self._S(q)
         if not self.cmm:
             self.helm._edge_pad(s, s)
@@ -164,8 +203,12 @@ class QGPlan:
         nl, B = ad.shape[0], ad.shape[1]
         X, Y = self.nx + 1, self.ny + 1
         g0 = torch.empty_like(ad)
-        _lib.call("vd_edge_pad_adj", self._dt, nl * B, X, Y, _ptr(ad), _ptr(self.psi if self.cmm else None),
+        _lib.call("vd_edge_pad_adj", self._dt, nl * B, X, Y, _ptr(ad), _ptr(self.psi if self.masked else None),
                   _ptr(g0), _stream())
+        if self.inversion == "multigrid":
+            # the masked Dirichlet operator is symmetric: its inverse is its
+            # own transpose (to the solve's tolerance)
+            return self._mg_interior(g0, torch.zeros_like(g0))
         g = self._S(g0)
         if not self.cmm:
             return g
