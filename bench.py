@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--profile-small", action="store_true",
                     help="short window for profiler captures (not a bench value)")
-    ap.add_argument("--workload", default="qg512", choices=["qg512", "basis1024", "mixed64", "sw3l", "qg3l", "aux"],
+    ap.add_argument("--workload", default="qg512", choices=["qg512", "basis1024", "mixed64", "sw3l", "qg3l", "aux", "jqgm"],
                     help="qg512: control = initial SSH, 512^2, batched windows (the headline); "
                          "basis1024: reduced-basis control forcing the SSH, 1024^2, one window; "
                          "mixed64: 64 windows of mixed sizes 128^2..768^2, 10 days; "
@@ -1367,6 +1367,94 @@ def gpu_arm_aux(args):
     print(json.dumps(line))
 
 
+JQ_N, JQ_DX, JQ_DT, JQ_NSTEP = 512, 5.0e3, 900.0, 96
+
+
+def _jq_fields(n, seed):
+    """Smooth synthetic SSH (eddy scales of a few tens of km, 0.1 m), a
+    rectangular island, a small boundary SSH and two smooth tracers."""
+    rng = np.random.default_rng(seed)
+    k = np.fft.fftfreq(n)[:, None] ** 2 + np.fft.fftfreq(n)[None, :] ** 2
+
+    def smooth(scale):
+        f = np.real(np.fft.ifft2(np.exp(-k / 4e-4) * np.fft.fft2(rng.standard_normal((n, n)))))
+        return scale * f / np.abs(f).max()
+
+    ssh = smooth(0.1)
+    ssh[200:240, 300:330] = np.nan
+    hb = smooth(0.01)
+    hb[np.isnan(ssh)] = 0.0
+    return ssh, hb, smooth(1.0), smooth(1.0)
+
+
+def gpu_arm_jqgm(args):
+    """The jqgm variants at 512^2 (dx 5 km, dt 900 s, one day = 96 steps,
+    float32): QgmWithTiles (tiles 64, overlap 8: 100 tiles) forward, tangent
+    linear and adjoint; Qgm_trac (rk2, two tracers, open boundaries) forward.
+    Times are CUDA-event milliseconds per call of nstep steps; the CPU
+    figures time the float64 oracle on one step and scale by nstep."""
+    import torch
+    from vardyn_gb300 import build
+    build.build()
+    from vardyn_gb300.model_qg1l.jqgm import QgmWithTiles, Qgm_trac
+    n = JQ_N
+    nstep = 8 if args.profile_small else (JQ_NSTEP if args.nstep == NSTEP else args.nstep)
+    ssh, hb, c1, c2 = _jq_fields(n, 7100)
+    dx = np.full((n, n), JQ_DX)
+    h0 = np.nan_to_num(ssh)
+    dev = "cuda"
+    rows = {}
+    kw = dict(dx=dx, dy=dx, dt=JQ_DT, SSH=ssh, c=2.7, Kdiffus=None, g=9.81, f=1.0e-4, time_scheme="rk2",
+              tile_size=64, tile_overlap=8)
+    mt = QgmWithTiles(dtype="float32", **kw)
+    H0 = torch.as_tensor(h0, dtype=torch.float32, device=dev)
+    HB = torch.as_tensor(hb, dtype=torch.float32, device=dev)
+    rng = np.random.default_rng(7101)
+    D = torch.as_tensor(rng.standard_normal((n, n)) * 1e-3, dtype=torch.float32, device=dev)
+    nt = len(mt.tiles)
+    m = 62
+    # dense DST flops per interior inversion of one tile: 4 n x n products of
+    # 2 n^3 flops; rk2 forward 2 inversions per step, tangent 4, adjoint
+    # 2 (forward sweep) + 2 (reverse)
+    inv_flops = 4 * 2 * m ** 3
+    forms = {}
+    for name, fn, ninv in (("forward", lambda: mt.step(H0, HB, nstep), 2),
+                           ("tangent", lambda: mt.step_tgl(D, H0, HB, nstep), 4),
+                           ("adjoint", lambda: mt.step_adj(D, H0, HB, nstep), 4)):
+        ms = _gpu_ms(fn, reps=1 if args.profile_small else 3)
+        forms[name] = {"ms": ms, "tile_steps_per_s": nt * nstep / (ms * 1e-3),
+                       "dst_gflops": nt * nstep * ninv * inv_flops / (ms * 1e-3) / 1e9}
+    rows["qgm_with_tiles"] = {"case": f"{n}x{n}, {nt} tiles of 64 (overlap 8), rk2, {nstep} steps, float32",
+                              **forms}
+    if not args.no_cpu and not args.profile_small:
+        from oracle.qg1l_tiles import QgmTilesOracle
+        o = QgmTilesOracle(**kw)
+        t1 = _cpu_s(lambda: o.step(h0, hb, 1))
+        rows["qgm_with_tiles"]["cpu_oracle_forward_ms"] = t1 * nstep * 1e3
+        rows["qgm_with_tiles"]["cpu_note"] = "float64 NumPy oracle, 1 step timed, x nstep, one core"
+    mq = Qgm_trac(dx=dx, dy=dx, dt=JQ_DT, SSH=ssh, c=2.7, g=9.81, f=1.0e-4, time_scheme="rk2", Kdiffus_trac=10.0,
+                  bc_trac="OBC", dtype="float32")
+    X0 = torch.as_tensor(np.stack([h0, c1, c2]), dtype=torch.float32, device=dev)
+    XB = torch.as_tensor(np.stack([hb, 0 * c1, 0 * c2]), dtype=torch.float32, device=dev)
+    ms = _gpu_ms(lambda: mq.step(X0, XB, nstep), reps=1 if args.profile_small else 3)
+    F = n * n * 4
+    # modelled DRAM bytes per rk2 step: the QG1.5L SSH/PV part (two stages of
+    # stage + x-DST + tridiagonal + inverse x-DST, ~12F each, + the final
+    # inversion ~6F) and per tracer plane two stages (u, v, c in, base, out:
+    # 5F) + the boundary update (4F)
+    step_bytes = (30 + 2 * (2 * 5 + 4)) * F
+    rows["qgm_trac"] = {"case": f"{n}x{n}, rk2, 2 tracers, open boundaries, {nstep} steps, float32", "ms": ms,
+                        "steps_per_s": nstep / (ms * 1e-3), "modelled_GBps": nstep * step_bytes / (ms * 1e-3) / 1e9}
+    if not args.no_cpu and not args.profile_small:
+        from oracle.qg1l_trac import QgmTracOracle
+        oq = QgmTracOracle(dx=dx, dy=dx, dt=JQ_DT, SSH=ssh, c=2.7, g=9.81, f=1.0e-4, time_scheme="rk2",
+                           Kdiffus_trac=10.0, bc_trac="OBC")
+        X0n, XBn = np.stack([h0, c1, c2]), np.stack([hb, 0 * c1, 0 * c2])
+        rows["qgm_trac"]["cpu_oracle_ms"] = _cpu_s(lambda: oq.step(X0n, XBn, 1)) * nstep * 1e3
+    torch.cuda.synchronize()
+    print(json.dumps({"workload": "jqgm", "note": "builder-reported; not the headline metric", "rows": rows}))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -1381,6 +1469,8 @@ def main():
         gpu_arm_sw(args)
     elif args.workload == "aux":
         gpu_arm_aux(args)
+    elif args.workload == "jqgm":
+        gpu_arm_jqgm(args)
     else:
         gpu_arm(args)
 

@@ -106,6 +106,19 @@ size_t vd_qgt_workspace_bytes(const vd_qgt_desc* desc);
 /* h1 = QgmWithTiles.step(h0, hb, nstep), fields [ny][nx] in desc->dtype. */
 vd_status vd_qgt_step(const vd_qgt_desc* desc, const void* h0, const void* hb, int nstep, void* h1,
                       void* work, size_t work_bytes, void* stream);
+/* Tangent linear and adjoint of QgmWithTiles.step with respect to h0
+ * (QgmWithTiles.step_tgl / step_adj, jqgm.py:1358-1376: jax.jvp / jax.vjp of
+ * the blended step). dh1 = J dh0, adh0 = J^T adh1; land carries no
+ * derivative and NaN in adh1 reads as 0. The workspace holds a slab per tile
+ * and, for the adjoint, the stage inputs of every step of every tile (it grows
+ * with nstep; adjoint != 0 sizes the adjoint's). The tile kernels keep only
+ * the DST matrix, the eigenvalues and two work blocks in shared memory
+ * (4 (T-2)^2 elements + T^2 bytes): T = 64 fits in both dtypes. */
+size_t vd_qgt_ad_workspace_bytes(const vd_qgt_desc* desc, int nstep, int adjoint);
+vd_status vd_qgt_step_tgl(const vd_qgt_desc* desc, const void* dh0, const void* h0, const void* hb, int nstep,
+                          void* dh1, void* work, size_t work_bytes, void* stream);
+vd_status vd_qgt_step_adj(const vd_qgt_desc* desc, const void* adh1, const void* h0, const void* hb, int nstep,
+                          void* adh0, void* work, size_t work_bytes, void* stream);
 
 /* ------------------------------------------------------------------------
  * QG 1.5-layer model with passive tracers, forward (Qgm_trac.step,

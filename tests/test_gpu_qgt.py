@@ -1,6 +1,8 @@
 """Overlapping-tile QG 1.5-layer model on the GPU (vd_qgt_step, drop-in
 QgmWithTiles.step) against the reference's own QgmWithTiles outputs
-(tests/golden/gen_golden_tiles.py) and the float64 oracle."""
+(tests/golden/gen_golden_tiles.py) and the float64 oracle; its tangent
+linear and adjoint (vd_qgt_step_tgl / vd_qgt_step_adj) against the oracle's,
+by a dot-product test and by central differences of the GPU step."""
 import os
 
 import numpy as np
@@ -91,5 +93,97 @@ def test_guards():
     with pytest.raises(ValueError):
         QgmWithTiles(dx=dx, dy=dx, dt=600.0, SSH=ssh, c=2.7, f=1e-4, time_scheme="rk3", tile_size=32)
     m = QgmWithTiles(dx=dx, dy=dx, dt=600.0, SSH=ssh, c=2.7, f=1e-4, tile_size=32, tile_overlap=8)
-    with pytest.raises(NotImplementedError):
-        m.step_adj(hb, ssh, hb, 1)
+    with pytest.raises(ValueError):
+        m.step_adj(hb[:, :-1], ssh, hb, 1)
+
+
+# ---- tangent linear and adjoint (jqgm.py:1358-1376) against the oracle's,
+# which is itself checked against central differences of the reference-pinned
+# step and by a dot-product test
+
+def _ad_case(scheme, seed, ny=30, nx=38, T=16, ov=4):
+    from oracle.qg1l_tiles import QgmTilesOracle
+    from vardyn_gb300.model_qg1l.jqgm import QgmWithTiles
+    rng = np.random.default_rng(seed)
+    dx = np.full((ny, nx), 1.0e4)
+    ssh = 0.1 * rng.standard_normal((ny, nx))
+    ssh[12:15, 17:20] = np.nan
+    hb = 0.01 * rng.standard_normal((ny, nx))
+    hb[np.isnan(ssh)] = 0.0
+    kw = dict(dx=dx, dy=dx, dt=600.0, SSH=ssh, c=2.7, Kdiffus=20.0, f=1.0e-4, time_scheme=scheme,
+              tile_size=T, tile_overlap=ov, mdt=0.02 * rng.standard_normal((ny, nx)))
+    return QgmTilesOracle(**kw), QgmWithTiles(dtype="float64", **kw), np.nan_to_num(ssh), hb, rng
+
+
+def _relmax(a, b):
+    return float(np.abs(a - b).max() / np.abs(b).max())
+
+
+@pytest.mark.parametrize("scheme", ["Euler", "rk2"])
+def test_tangent_matches_oracle(scheme):
+    o, m, h0, hb, rng = _ad_case(scheme, 11)
+    d = 1e-3 * rng.standard_normal(h0.shape)
+    ref = o.step_tgl(d, h0, hb, 3)
+    got = m.step_tgl(d, h0, hb, 3)
+    e = _relmax(got, ref)
+    print(f"\nQgmWithTiles {scheme} tangent vs oracle: {e:.1e}")
+    assert e < 1e-11
+    assert np.all(got[m.mask == 0] == 0)
+
+
+@pytest.mark.parametrize("scheme", ["Euler", "rk2"])
+def test_adjoint_matches_oracle(scheme):
+    o, m, h0, hb, rng = _ad_case(scheme, 12)
+    y = rng.standard_normal(h0.shape)
+    y[m.mask == 0] = np.nan                  # NaN on land, as a blended step leaves it
+    ref = o.step_adj(y, h0, hb, 3)
+    got = m.step_adj(y, h0, hb, 3)
+    e = _relmax(got, ref)
+    print(f"\nQgmWithTiles {scheme} adjoint vs oracle: {e:.1e}")
+    assert e < 1e-11
+
+
+@pytest.mark.parametrize("scheme", ["Euler", "rk2"])
+def test_dot_product_and_central_differences_on_a_larger_domain(scheme):
+    """tile 32, overlap 8 on 70 x 90 with an island: <J d, y> = <d, J^T y> to
+    1e-12 and the tangent against central differences of the GPU step."""
+    from vardyn_gb300.model_qg1l.jqgm import QgmWithTiles
+    dx, ssh, hb = _case(70, 90, 13)
+    m = QgmWithTiles(dx=dx, dy=dx, dt=600.0, SSH=ssh, c=2.7, Kdiffus=20.0, g=9.81, f=1.0e-4, time_scheme=scheme,
+                     tile_size=32, tile_overlap=8, dtype="float64")
+    rng = np.random.default_rng(14)
+    h0 = np.nan_to_num(ssh)
+    d = rng.standard_normal(h0.shape) * (m.mask != 0)
+    y = rng.standard_normal(h0.shape) * (m.mask != 0)
+    tl = m.step_tgl(d, h0, hb, 4)
+    ad = m.step_adj(y, h0, hb, 4)
+    lhs, rhs = float(np.sum(tl * y)), float(np.sum(d * ad))
+    print(f"\n{scheme}: <J d, y> {lhs:.15e}  <d, J^T y> {rhs:.15e}")
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+    # an upwind switch of the rk2 trajectory lies within 1e-7 of this state:
+    # at eps = 1e-7 central differences cross it (0.9 % at some points, for the
+    # float64 oracle as well), at 1e-8 they do not
+    eps = 1e-8
+    fd = (m.step(h0 + eps * d, hb, 4) - m.step(h0 - eps * d, hb, 4)) / (2 * eps)
+    ok = ~np.isnan(fd)
+    assert np.abs(fd[ok] - tl[ok]).max() <= 1e-6 * np.abs(tl[ok]).max()
+
+
+def test_float32_default_tile_tangent_and_adjoint():
+    """The reference's default tiles (64, overlap 8) in float32 against the
+    float64 oracle."""
+    from oracle.qg1l_tiles import QgmTilesOracle
+    from vardyn_gb300.model_qg1l.jqgm import QgmWithTiles
+    dx, ssh, hb = _case(130, 150, 15)
+    kw = dict(dx=dx, dy=dx, dt=600.0, SSH=ssh, c=2.7, Kdiffus=None, g=9.81, f=1.0e-4, time_scheme="rk2",
+              tile_size=64, tile_overlap=8)
+    h0 = np.nan_to_num(ssh)
+    rng = np.random.default_rng(16)
+    d = 1e-2 * rng.standard_normal(h0.shape)
+    o = QgmTilesOracle(**kw)
+    m = QgmWithTiles(dtype="float32", **kw)
+    for got, ref in ((m.step_tgl(d, h0, hb, 2), o.step_tgl(d, h0, hb, 2)),
+                     (m.step_adj(d, h0, hb, 2), o.step_adj(d, h0, hb, 2))):
+        err = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+        print(f"\nfloat32 tile-64 rel-L2 vs float64 oracle: {err:.2e}")
+        assert err < 1e-5

@@ -74,3 +74,59 @@ def test_rk4_extension_is_fourth_order():
     assert all(14.0 < e4[k] / e4[k + 1] < 18.0 for k in range(2))
     e2 = [np.abs(run("rk2", dt) - fine).max() for dt in (2700.0, 1350.0)]
     assert 3.5 < e2[0] / e2[1] < 4.5
+
+
+# ---- tangent linear and adjoint (jax.jvp / vjp of step, jqgm.py:2141-2151)
+
+def _tl_case(g, key, seed):
+    from oracle.qg1l_trac import QgmTracTLAD
+    rng = np.random.default_rng(seed)
+    if key == "a":
+        o = QgmTracTLAD(dx=g["a_dx"], dy=g["a_dy"], dt=900.0, SSH=g["a_ssh"], c=2.7, g=9.81, f=g["a_f"],
+                        time_scheme="Euler", Kdiffus=30.0, Kdiffus_trac=10.0, bc_trac="OBC", mdt=g["a_mdt"])
+        X0, Xb = g["a_X0"], g["a_Xb"]
+    elif key == "b":
+        o = QgmTracTLAD(dx=g["b_dx"], dy=g["b_dx"], dt=600.0, SSH=g["b_ssh"], c=2.5, g=9.81, f=1.0e-4,
+                        time_scheme="rk2", Wbc=g["b_wbc"], Kdiffus_trac=5.0, bc_trac="dirichlet", advect_pv=False)
+        X0, Xb = g["b_X0"], g["b_Xb"]
+    elif key == "rk2obc":
+        o = QgmTracTLAD(dx=g["a_dx"], dy=g["a_dy"], dt=900.0, SSH=g["a_ssh"], c=2.7, g=9.81, f=g["a_f"],
+                        time_scheme="rk2", Kdiffus=30.0, Kdiffus_trac=10.0, bc_trac="OBC")
+        X0, Xb = g["a_X0"], g["a_Xb"]
+    elif key == "rk4":
+        o = QgmTracTLAD(dx=g["a_dx"], dy=g["a_dy"], dt=900.0, SSH=g["a_ssh"], c=2.7, g=9.81, f=g["a_f"],
+                        time_scheme="rk4", Kdiffus_trac=10.0, bc_trac="OBC", mdt=g["a_mdt"])
+        X0, Xb = g["a_X0"], g["a_Xb"]
+    else:
+        o = QgmTracTLAD(dx=g["c_dx"], dy=g["c_dx"], dt=900.0, SSH=g["c_ssh"], c=2.7, g=9.81, f=1.0e-4,
+                        time_scheme="rk2", Kdiffus=15.0)
+        X0, Xb = g["c_ssh"], g["c_hb"]
+    X0 = np.nan_to_num(np.asarray(X0, dtype=np.float64))
+    return o, X0, np.asarray(Xb, dtype=np.float64), rng
+
+
+CASES = ["a", "b", "rk2obc", "rk4", "c"]
+
+
+@pytest.mark.parametrize("key", CASES)
+def test_trac_tangent_matches_central_differences(g, key):
+    o, X0, Xb, rng = _tl_case(g, key, 31)
+    d = rng.standard_normal(X0.shape) * np.abs(X0).max() * 1e-3
+    tl = o.step_tgl(d, X0, Xb, 3)
+    eps = 1e-4
+    fd = (o.step(X0 + eps * d, Xb, 3) - o.step(X0 - eps * d, Xb, 3)) / (2 * eps)
+    m = ~np.isnan(fd)
+    assert np.all(tl[~m] == 0)
+    err = np.abs(fd[m] - tl[m]).max() / np.abs(tl[m]).max()
+    assert err <= 1e-7, err
+
+
+@pytest.mark.parametrize("key", CASES)
+def test_trac_adjoint_dot_product(g, key):
+    o, X0, Xb, rng = _tl_case(g, key, 32)
+    d = rng.standard_normal(X0.shape)
+    y = rng.standard_normal(X0.shape)
+    tl = o.step_tgl(d, X0, Xb, 3)
+    ad = o.step_adj(y, X0, Xb, 3)
+    lhs, rhs = float(np.sum(tl * y)), float(np.sum(d * ad))
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)

@@ -164,8 +164,14 @@ SIGNATURES = {
     "vd_qgt_shared_bytes": (SZ, [I, I]),
     "vd_qgt_workspace_bytes": (SZ, [ctypes.POINTER(VdQgtDesc)]),
     "vd_qgt_step": (I, [ctypes.POINTER(VdQgtDesc), P, P, I, P, P, SZ, P]),
+    "vd_qgt_ad_workspace_bytes": (SZ, [ctypes.POINTER(VdQgtDesc), I, I]),
+    "vd_qgt_step_tgl": (I, [ctypes.POINTER(VdQgtDesc), P, P, P, I, P, P, SZ, P]),
+    "vd_qgt_step_adj": (I, [ctypes.POINTER(VdQgtDesc), P, P, P, I, P, P, SZ, P]),
     "vd_qgtrac_workspace_bytes": (SZ, [P, ctypes.POINTER(VdQgtracDesc), I]),
     "vd_qgtrac_step": (I, [P, ctypes.POINTER(VdQgtracDesc), I, P, P, P, P, I, P, P, P, SZ, P]),
+    "vd_qgtrac_ad_workspace_bytes": (SZ, [P, ctypes.POINTER(VdQgtracDesc), I, I, I]),
+    "vd_qgtrac_step_tgl": (I, [P, ctypes.POINTER(VdQgtracDesc), I, P, P, P, P, P, P, I, P, P, P, SZ, P]),
+    "vd_qgtrac_step_adj": (I, [P, ctypes.POINTER(VdQgtracDesc), I, P, P, P, P, P, P, I, P, P, P, SZ, P]),
     "vd_qg1l_plan_destroy": (I, [P]),
     "vd_qg1l_workspace_bytes": (SZ, [P, I]),
     "vd_qg1l_traj_bytes": (SZ, [P, I, I]),

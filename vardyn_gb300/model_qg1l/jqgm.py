@@ -213,7 +213,8 @@ class QgmWithTiles:
     with the tile means of f and c and Dirichlet hb on its edge, the tiles are
     blended with Gaspari-Cohn tapers. ``time_scheme`` is 'Euler' or 'rk2' (the
     reference's tile model knows only these). The tangent linear and adjoint
-    (jax.jvp / vjp of the blended step) are not built: they raise."""
+    (jax.jvp / vjp of the blended step) run on the GPU too (vd_qgt_step_tgl /
+    vd_qgt_step_adj)."""
 
     def __init__(self, dx=None, dy=None, dt=None, SSH=None, c=None, Kdiffus=None, upwind=3, g=9.81, f=1e-4,
                  time_scheme="Euler", mdt=None, tile_size=64, tile_overlap=8, dtype=None, device=None, **kwargs):
@@ -295,6 +296,7 @@ class QgmWithTiles:
         d.mdt = None if self._mdt is None else self._mdt.data_ptr()
         self._desc = d
         self._work = torch.empty(_lib.load().vd_qgt_workspace_bytes(ctypes.byref(d)) // esz, dtype=R, device=dev)
+        self._ad_work = {}
         self.step_jit = self.step
         self.step_tgl_jit = self.step_tgl
         self.step_adj_jit = self.step_adj
@@ -315,11 +317,39 @@ class QgmWithTiles:
                        ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream))
         return out.cpu().numpy() if as_np else out
 
+    def _field(self, x):
+        t = x if isinstance(x, torch.Tensor) else torch.as_tensor(np.asarray(x, dtype=np.float64))
+        t = t.to(device=self.device, dtype=self.dtype).contiguous()
+        if tuple(t.shape) != (self.ny, self.nx):
+            raise ValueError(f"fields must be ({self.ny}, {self.nx})")
+        return t
+
+    def _ad(self, name, adjoint, x, h0, hb, nstep):
+        as_np = not isinstance(h0, torch.Tensor)
+        X, H0, HB = self._field(x), self._field(h0), self._field(hb)
+        nbytes = self._lib.load().vd_qgt_ad_workspace_bytes(ctypes.byref(self._desc), int(nstep), int(adjoint))
+        esz = X.element_size()
+        key = (adjoint, int(nstep))
+        if self._ad_work.get(key) is None:
+            self._ad_work = {key: torch.empty(nbytes // esz, dtype=self.dtype, device=self.device)}
+        work = self._ad_work[key]
+        out = torch.empty_like(H0)
+        self._lib.call(name, ctypes.byref(self._desc), ctypes.c_void_p(X.data_ptr()), ctypes.c_void_p(H0.data_ptr()),
+                       ctypes.c_void_p(HB.data_ptr()), int(nstep), ctypes.c_void_p(out.data_ptr()),
+                       ctypes.c_void_p(work.data_ptr()), work.numel() * esz,
+                       ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream))
+        return out.cpu().numpy() if as_np else out
+
     def step_tgl(self, dh0, h0, hb, nstep=1):
-        raise NotImplementedError("tangent linear of QgmWithTiles (jax.jvp of the blended step) is not built")
+        """jax.jvp of the blended step with respect to h0 (jqgm.py:1358-1362),
+        on the GPU (vd_qgt_step_tgl); zero on land."""
+        return self._ad("vd_qgt_step_tgl", 0, dh0, h0, hb, nstep)
 
     def step_adj(self, adh0, h0, hb, nstep=1):
-        raise NotImplementedError("adjoint of QgmWithTiles (jax.vjp of the blended step) is not built")
+        """jax.vjp of the blended step with respect to h0 (jqgm.py:1364-1376),
+        on the GPU (vd_qgt_step_adj): the adjoint keeps every tile's stage
+        inputs of every step in its workspace."""
+        return self._ad("vd_qgt_step_adj", 1, adh0, h0, hb, nstep)
 
 
 class Qgm_trac(Qgm):
@@ -338,9 +368,12 @@ class Qgm_trac(Qgm):
       that the reference's rk4 for this class sets out to be (that one
       cannot run, jqgm.py:1924-1955).
 
+    ``step_tgl`` / ``step_adj`` (jax.jvp / vjp of step, jqgm.py:2141-2151) run
+    on the GPU too (vd_qgtrac_step_tgl / vd_qgtrac_step_adj).
+
     Not built: ``ageo_velocities`` (the reference's boundary stack then holds
     the ageostrophic fields, jqgm.py:2079, and its boundary loop indexes past
-    the tracers), and the tangent linear and adjoint: they raise."""
+    the tracers)."""
 
     def __init__(self, dx=None, dy=None, dt=None, SSH=None, c=None, upwind=3, g=9.81, f=1e-4,
                  time_scheme="Euler", Wbc=None, Kdiffus=None, Kdiffus_trac=None, bc_trac="OBC", mdt=None,
@@ -429,8 +462,64 @@ class Qgm_trac(Qgm):
     def rhs(self, *args, **kwargs):
         raise NotImplementedError("Qgm_trac.rhs takes the stacked state; the GPU step fuses it")
 
-    def step_tgl(self, *args, **kwargs):
-        raise NotImplementedError("Qgm_trac tangent linear is not built")
+    def _ad_windows(self, name, adjoint, h0, c0, hb, cb, xh, xc, nstep):
+        h0, hb, xh = self._to_dev(h0), self._to_dev(hb), self._to_dev(xh)
+        c0, cb, xc = self._to_dev(c0), self._to_dev(cb), self._to_dev(xc)
+        B = h0.shape[0]
+        if h0.dim() != 3 or hb.shape != h0.shape or xh.shape != h0.shape or h0.shape[1:] != (self.ny, self.nx):
+            raise ValueError("h0, hb and the direction must be [B, ny, nx] on the model grid")
+        if c0.dim() != 4 or cb.shape != c0.shape or xc.shape != c0.shape or c0.shape[0] != B or \
+                c0.shape[2:] != (self.ny, self.nx):
+            raise ValueError("c0, cb and the tracer direction must be [B, ntrac, ny, nx] with the batch of h0")
+        nt = c0.shape[1]
+        d = self._desc(nt)
+        nbytes = self._lib.load().vd_qgtrac_ad_workspace_bytes(self.plan.handle, ctypes.byref(d), B, int(nstep),
+                                                                int(adjoint))
+        if nbytes == 0:
+            raise ValueError("vd_qgtrac_ad_workspace_bytes rejected the configuration")
+        key = ("ad", B, nt)
+        ws = self._ws.get(key)
+        if ws is None or ws.numel() < nbytes:
+            ws = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+            self._ws[key] = ws
+        oh = torch.empty_like(h0)
+        oc = torch.empty_like(c0)
+        p = (lambda t: ctypes.c_void_p(t.data_ptr() if t.numel() else None))
+        self._lib.call(name, self.plan.handle, ctypes.byref(d), B, p(h0), p(c0), p(hb), p(cb), p(xh), p(xc),
+                       int(nstep), p(oh), p(oc), p(ws), ws.numel(),
+                       ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream))
+        return oh, oc
 
-    def step_adj(self, *args, **kwargs):
-        raise NotImplementedError("Qgm_trac adjoint is not built")
+    def step_tgl_windows(self, dh0, dc0, h0, c0, hb, cb, nstep=1):
+        """Batched tangent linear on device tensors (shapes of step_windows)."""
+        return self._ad_windows("vd_qgtrac_step_tgl", 0, h0, c0, hb, cb, dh0, dc0, nstep)
+
+    def step_adj_windows(self, adh1, adc1, h0, c0, hb, cb, nstep=1):
+        """Batched adjoint on device tensors (shapes of step_windows)."""
+        return self._ad_windows("vd_qgtrac_step_adj", 1, h0, c0, hb, cb, adh1, adc1, nstep)
+
+    def _ad(self, adjoint, dX, X0, Xb, nstep):
+        X, XB, D = self._to_dev(X0), self._to_dev(Xb), self._to_dev(dX)
+        if X.shape != XB.shape or D.shape != X.shape:
+            raise ValueError("the direction, X0 and Xb must have the same shape")
+        f = self.step_adj_windows if adjoint else self.step_tgl_windows
+        if X.dim() == 2:
+            e = X.new_empty((1, 0) + tuple(X.shape))
+            oh, _ = f(D[None], e, X[None], e, XB[None], e, nstep)
+            out = oh[0]
+        elif X.dim() == 3:
+            oh, oc = f(D[:1], D[None, 1:], X[:1], X[None, 1:], XB[:1], XB[None, 1:], nstep)
+            out = torch.cat([oh, oc[0]], dim=0)
+        else:
+            raise ValueError("X0 is [ny, nx] or [1 + ntrac, ny, nx]")
+        return out if isinstance(X0, torch.Tensor) else out.cpu().numpy()
+
+    def step_tgl(self, dX0, X0, Xb, way=1, nstep=1):
+        """jax.jvp of step with respect to X0 (jqgm.py:2141-2145), on the GPU
+        (vd_qgtrac_step_tgl); zero on land."""
+        return self._ad(0, dX0, X0, Xb, nstep)
+
+    def step_adj(self, adX0, X0, Xb, way=1, nstep=1):
+        """jax.vjp of step with respect to X0 (jqgm.py:2147-2151), on the GPU
+        (vd_qgtrac_step_adj); NaN in adX0 reads as 0."""
+        return self._ad(1, adX0, X0, Xb, nstep)
