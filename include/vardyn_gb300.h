@@ -150,6 +150,21 @@ size_t vd_qgtrac_workspace_bytes(const vd_qg1l_plan* plan, const vd_qgtrac_desc*
 vd_status vd_qgtrac_step(const vd_qg1l_plan* plan, const vd_qgtrac_desc* desc, int batch, const void* h0,
                          const void* c0, const void* hb, const void* cb, int nstep, void* h1, void* c1,
                          void* work, size_t work_bytes, void* stream);
+/* Tangent linear and adjoint of vd_qgtrac_step with respect to (h0, c0)
+ * (Qgm_trac.step_tgl / step_adj, jqgm.py:2141-2151: jax.jvp / jax.vjp of
+ * step; hb, cb are not differentiated). Shapes of vd_qgtrac_step; the plan's
+ * time scheme must be desc->time_scheme. tgl: (dh1, dc1) = J (dh0, dc0), zero
+ * on land. adj: (adh0, adc0) = J^T (adh1, adc1), NaN in adh1 / adc1 read as 0.
+ * The adjoint's workspace holds every stage input of every step (it grows
+ * with nstep; adjoint != 0 sizes the adjoint's). */
+size_t vd_qgtrac_ad_workspace_bytes(const vd_qg1l_plan* plan, const vd_qgtrac_desc* desc, int batch, int nstep,
+                                    int adjoint);
+vd_status vd_qgtrac_step_tgl(const vd_qg1l_plan* plan, const vd_qgtrac_desc* desc, int batch, const void* h0,
+                             const void* c0, const void* hb, const void* cb, const void* dh0, const void* dc0,
+                             int nstep, void* dh1, void* dc1, void* work, size_t work_bytes, void* stream);
+vd_status vd_qgtrac_step_adj(const vd_qg1l_plan* plan, const vd_qgtrac_desc* desc, int batch, const void* h0,
+                             const void* c0, const void* hb, const void* cb, const void* adh1, const void* adc1,
+                             int nstep, void* adh0, void* adc0, void* work, size_t work_bytes, void* stream);
 
 /* Build a plan: DST-I half matrices, tridiagonal multipliers, mask, beta and
  * bathymetry tables on the current device. Replaces the constant set-up of

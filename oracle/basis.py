@@ -498,3 +498,206 @@ class WaveletOracle(BMOracle):
                 if fact != 0:
                     out.append((it, fact))
         return out
+
+
+def aux_interp_mean(fc, latc, lonc, data, f, elon, elat):
+    """np.nanmean of ``data.interp(f=f, lon=elon, lat=elat)`` for 1-D lon /
+    lat indexers (basis.py:2071, 2134): xarray interpolates orthogonally
+    (the outer product of the lon and lat values), multilinearly, NaN outside
+    the coordinates. data is [f][lat][lon] on ascending coordinates. Returns
+    NaN when every value is NaN."""
+    from scipy.interpolate import RegularGridInterpolator
+    rgi = RegularGridInterpolator((np.asarray(fc, float), np.asarray(latc, float), np.asarray(lonc, float)),
+                                  np.asarray(data, float), method="linear", bounds_error=False, fill_value=np.nan)
+    la, lo = np.meshgrid(np.asarray(elat, float), np.asarray(elon, float), indexing="ij")
+    pts = np.stack([np.full(la.size, float(f)), la.ravel(), lo.ravel()], axis=1)
+    v = rgi(pts)
+    return np.nan if np.all(np.isnan(v)) else float(np.nanmean(v))
+
+
+class BMauxOracle:
+    """Wave-packet basis with per-location decorrelation times and variances
+    of the reference (Basis_bmaux / Basis_bmaux_jax, mapping/src/basis.py
+    1741-2638), without depth tapering, facQ_aux file or C-grid variables.
+
+    The atoms are the wave packets of Basis_bm. What differs (basis.py):
+    - the lattice ends at LAT_MAX + DX and LON_MAX + DX/cos (1947-1954), not
+      1.5 DX;
+    - every space centre P of frequency f has its own decorrelation time
+      tdec = factdec * nanmean of Tdec(f, lon, lat) over a 10 x 10 grid of its
+      box of half-width DX, clipped to [tdecmin, tdecmax] (2004-2015), its own
+      window integral norm_fact (2017-2024) and its own time centres from
+      -time_ref mod tdec, spaced tdec / facnlt (2026-2027); the time axis of
+      a frequency is padded with NaN centres to its longest list (2029-2035);
+    - Q of (time centre, P) is facQ * nanmean of Std over the same box (1e-10
+      where every value is NaN), or 1e-10 * facQ on a padded centre
+      (2041-2100);
+    - G(t) phi = sum_f Gx_f sum_it Gt(t)[it, P] X[it, P, :] with Gt = window(
+      dt / tdec_P) / norm_fact_P for |dt| <= tdec_P, 0 otherwise or on a
+      padded centre (jax form, 2473-2530; the numpy operg of 2303-2340
+      accumulates into a variable it never returns).
+    aux = dict(f, lat, lon, Tdec, Std) with Tdec, Std [f][lat][lon] on
+    ascending coordinates (in the grid's longitude convention)."""
+
+    def __init__(self, lon, lat, aux, npsp=3.5, facpsp=1.5, lmin=80., lmax=900., facns=1., facnlt=2.,
+                 tdecmin=2., tdecmax=20., factdec=1., facQ=1., norm_time=True, flux=False, time_ref=0.0,
+                 mask=None, geo=True):
+        lon = np.asarray(lon, float)
+        lat = np.asarray(lat, float)
+        self.shape_phys = lon.shape
+        self.lon1d, self.lat1d = lon.ravel(), lat.ravel()
+        self.lon_min, self.lon_max = lon.min(), lon.max()
+        self.lat_min, self.lat_max = lat.min(), lat.max()
+        self.aux = aux
+        self.npsp, self.facpsp, self.lmin, self.lmax = float(npsp), float(facpsp), float(lmin), float(lmax)
+        self.facns, self.facnlt = float(facns), float(facnlt)
+        self.tdecmin, self.tdecmax, self.factdec, self.facQ = float(tdecmin), float(tdecmax), float(factdec), \
+            float(facQ)
+        self.norm_time = norm_time
+        self.window = mywindow_flux if flux else mywindow
+        self.time_ref = float(time_ref)
+        self.geo = geo
+        self.km2deg = KM2DEG if geo else 1.0
+        self.mask1d = None
+        if mask is not None and np.any(mask):
+            self.mask1d = np.asarray(mask, bool).ravel()
+
+    def _cos(self, lat_deg):
+        return np.cos(lat_deg * np.pi / 180.) if self.geo else 1.0
+
+    def _box_mean(self, name, iff, P):
+        k2 = self.km2deg
+        lo, la = self.ENSLON[iff][P], self.ENSLAT[iff][P]
+        dlon = self.DX[iff] * k2 / self._cos(la)
+        dlat = self.DX[iff] * k2
+        elon = np.linspace(lo - dlon, lo + dlon, 10)
+        elat = np.linspace(la - dlat, la + dlat, 10)
+        a = self.aux
+        return aux_interp_mean(a["f"], a["lat"], a["lon"], a[name], self.ff[iff], elon, elat)
+
+    def set_basis(self, time):
+        time = np.asarray(time, float)
+        TIME_MIN, TIME_MAX = time.min(), time.max()
+        LON_MIN, LON_MAX, LAT_MIN, LAT_MAX = self.lon_min, self.lon_max, self.lat_min, self.lat_max
+        if LON_MAX < LON_MIN:
+            LON_MAX = LON_MAX + 360.
+        k2 = self.km2deg
+        logff = np.arange(np.log(1. / self.lmin), np.log(1. / self.lmax) - np.log(1 + self.facpsp / self.npsp),
+                          -np.log(1 + self.facpsp / self.npsp))[::-1]
+        ff = np.exp(logff)
+        dff = ff[1:] - ff[:-1]
+        theta = np.linspace(0, np.pi, int(np.pi * ff[0] / dff[0] * self.facpsp))[:-1]
+        ntheta, nf = len(theta), len(ff)
+        deltat = TIME_MAX - TIME_MIN
+        DX = 1. / ff * self.npsp * 0.5
+        DXG = DX / self.facns
+        self.ff, self.DX = ff, DX
+        ENSLON, ENSLAT = [], []
+        NP = np.zeros(nf, dtype=int)
+        for iff in range(nf):
+            el, ea = [], []
+            dlat = DXG[iff] * k2
+            lat0 = LAT_MIN - LAT_MIN % dlat - DX[iff] * k2
+            lat1 = LAT_MAX + DX[iff] * k2
+            for la in np.arange(lat0, lat1, dlat):
+                cl = self._cos(la)
+                dlon = DXG[iff] / cl * k2
+                lon0 = LON_MIN - LON_MIN % dlon - DX[iff] / cl * k2
+                lon1 = LON_MAX + DX[iff] / cl * k2
+                for lo in np.arange(lon0, lon1, dlon):
+                    if self.mask1d is not None:
+                        ind = np.where((np.abs((self.lon1d - lo) / k2 * self._cos(la)) <= 1. / ff[iff]) &
+                                       (np.abs((self.lat1d - la) / k2) <= 1. / ff[iff]))[0]
+                        if np.all(self.mask1d[ind]):
+                            continue
+                    el.append(lo)
+                    ea.append(la)
+            ENSLON.append(np.array(el))
+            ENSLAT.append(np.array(ea))
+            NP[iff] = len(el)
+        self.ENSLON, self.ENSLAT, self.NP = ENSLON, ENSLAT, NP
+        tdec, norm_fact, enst, std = [], [], [], []
+        for iff in range(nf):
+            td_f, nf_f, en_f, sd_f = [], [], [], []
+            for P in range(NP[iff]):
+                m = self._box_mean("Tdec", iff, P)
+                td = 0.0 if np.isnan(m) else m
+                td *= self.factdec
+                td = min(max(td, self.tdecmin), self.tdecmax)
+                if self.norm_time:
+                    tt = np.linspace(-td, td)
+                    tmp = np.zeros_like(tt)
+                    for i in range(tt.size - 1):
+                        tmp[i + 1] = tmp[i] + self.window(tt[i] / td) * (tt[i + 1] - tt[i])
+                    nrm = tmp.max()
+                else:
+                    nrm = 1.0
+                t0 = -self.time_ref % td
+                td_f.append(td)
+                nf_f.append(nrm)
+                en_f.append(np.arange(t0 - td / self.facnlt, deltat + td / self.facnlt, td / self.facnlt))
+                s = self._box_mean("Std", iff, P)
+                sd_f.append(1e-10 if np.isnan(s) else s)
+            nit = max((e.size for e in en_f), default=0)
+            pad = np.full((NP[iff], nit), np.nan)
+            for P in range(NP[iff]):
+                pad[P, :en_f[P].size] = en_f[P]
+            tdec.append(np.array(td_f))
+            norm_fact.append(np.array(nf_f))
+            enst.append(pad)
+            std.append(np.array(sd_f))
+        Q, bounds, iw = [], [], 0
+        for iff in range(nf):
+            bounds.append(iw)
+            nit = enst[iff].shape[1]
+            for it in range(nit):
+                for P in range(NP[iff]):
+                    q = 1e-10 if np.isnan(enst[iff][P, it]) else std[iff][P]
+                    Q.append(np.full(2 * ntheta, q * self.facQ))
+            iw += 2 * ntheta * NP[iff] * nit
+        bounds.append(iw)
+        self.theta, self.ntheta, self.nf = theta, ntheta, nf
+        self.tdec, self.norm_fact, self.enst, self.std = tdec, norm_fact, enst, std
+        self.k = 2 * np.pi * ff
+        self.bounds = bounds
+        self.nbasis = iw
+        self.Q = np.concatenate(Q) if Q else np.zeros(0)
+        self.Gx = [BMOracle._space(self, iff) for iff in range(nf)]
+        self.times = time
+        return np.zeros_like(self.Q), self.Q
+
+    def time_weights(self, iff, t):
+        """Gt(t) of frequency iff as [time centre][space centre]."""
+        en = self.enst[iff]
+        g = np.zeros(en.shape)
+        for P in range(en.shape[0]):
+            td = self.tdec[iff][P]
+            for it in range(en.shape[1]):
+                dt = t - en[P, it]
+                if not (abs(dt) > td or np.isnan(en[P, it])):
+                    g[P, it] = self.window(dt / td) / self.norm_fact[iff][P]
+        return g.T
+
+    def operg(self, t, X):
+        phi = np.zeros(self.lon1d.size)
+        for iff in range(self.nf):
+            nx_ = 2 * self.ntheta * self.NP[iff]
+            if nx_ == 0:
+                continue
+            nit = self.enst[iff].shape[1]
+            Xf = X[self.bounds[iff]:self.bounds[iff + 1]].reshape(nit, self.NP[iff], 2 * self.ntheta)
+            z = (self.time_weights(iff, t)[:, :, None] * Xf).sum(axis=0).ravel()
+            phi += self.Gx[iff].dot(z)
+        return phi.reshape(self.shape_phys)
+
+    def operg_transpose(self, t, adphi):
+        adX = np.zeros(self.nbasis)
+        for iff in range(self.nf):
+            nx_ = 2 * self.ntheta * self.NP[iff]
+            if nx_ == 0:
+                continue
+            nit = self.enst[iff].shape[1]
+            ad = self.Gx[iff].T.dot(np.asarray(adphi).ravel()).reshape(self.NP[iff], 2 * self.ntheta)
+            blk = adX[self.bounds[iff]:self.bounds[iff + 1]].reshape(nit, self.NP[iff], 2 * self.ntheta)
+            blk += self.time_weights(iff, t)[:, :, None] * ad[None]
+        return adX
