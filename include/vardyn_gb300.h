@@ -485,6 +485,37 @@ typedef struct vd_wavelet_params {
 } vd_wavelet_params;
 vd_status vd_wavelet_plan_create(vd_bm_plan** out, const vd_basis_grid* grid,
                                  const vd_wavelet_params* params);
+/* Wave packets with per-location decorrelation times and variances
+ * (Basis_bmaux / Basis_bmaux_jax, basis.py:1741-2638): the atoms and the
+ * lattice of the wave packets (the lattice ends at LAT_MAX + DX, LON_MAX +
+ * DX/cos), but every space centre P of a frequency takes its decorrelation
+ * time (factdec * the mean of Tdec over a 10 x 10 grid of its box, clipped),
+ * window integral and time centres (from -time_ref mod tdec, spaced
+ * tdec / facnlt) of its own, and Q = facQ * the box mean of Std; a
+ * frequency's time axis is padded to its longest list (padded centres have
+ * weight 0 and Q = 1e-10 facQ). The auxiliary fields are host arrays
+ * [aux_nf][aux_nlat][aux_nlon] on ascending coordinates in the grid's
+ * longitude convention, interpolated as xarray's DataArray.interp with 1-D
+ * indexers does (orthogonal points, linear, NaN outside). Controls of one
+ * frequency are ordered [time centre][space centre][theta][cos, sin]. Every
+ * vd_bm_* query and projection applies, except vd_bm_time_weights (the time
+ * weights are per centre); vd_bm_frequency's tdec is 0 and its time-centre
+ * count the padded one; vd_bm_lattice's enst is [NP][padded count] (NaN
+ * padding). */
+typedef struct vd_bmaux_params {
+    double npsp, facpsp, lmin, lmax, facns, facnlt;
+    double tdecmin, tdecmax, factdec;   /* decorrelation time bounds and factor */
+    double facQ;                        /* factor of the prior std */
+    int norm_time, flux;
+    double time_ref;                    /* days from 1950-01-01 to the window start */
+    int aux_nf, aux_nlat, aux_nlon;     /* auxiliary grid (each >= 2) */
+    const double *aux_f, *aux_lat, *aux_lon;   /* ascending coordinates */
+    const double *aux_tdec, *aux_std;          /* [aux_nf][aux_nlat][aux_nlon], NaN allowed */
+} vd_bmaux_params;
+vd_status vd_bmaux_plan_create(vd_bm_plan** out, const vd_basis_grid* grid, const vd_bmaux_params* params);
+/* Per space centre of frequency iff: decorrelation time, window integral and
+ * number of time centres (any pointer may be NULL). */
+vd_status vd_bmaux_centres(const vd_bm_plan* plan, int iff, double* tdec_host, double* norm_host, int* nt_host);
 vd_status vd_bm_plan_destroy(vd_bm_plan* plan);
 long long vd_bm_nbasis(const vd_bm_plan* plan);
 /* Number of frequencies and directions; theta_host [ntheta] if non-NULL. */

@@ -64,3 +64,42 @@ def test_projection_and_transpose(g, o):
         e2 = np.abs(adX - g[f"t{k}_adX"]).max() / np.abs(g[f"t{k}_adX"]).max()
         # the time-centre offsets above bound the agreement near 1e-12
         assert e1 < 1e-11 and e2 < 1e-11, (k, e1, e2)
+
+
+def test_library_host_tables_match_reference(g):
+    """The plan's host tables (built by the library in C++, no device)
+    against the reference's own class."""
+    from vardyn_gb300.basis import BMauxParams, BMauxPlan
+    plan = BMauxPlan(g["lon"], g["lat"], g["time"], BMauxParams(aux_sorted(g), time_ref=float(g["time_ref"]), **PRM),
+                     land=g["mask"], geographic=True, host_only=True)
+    assert plan.nf == g["ff"].size and plan.ntheta == g["theta"].size
+    assert np.allclose(plan.theta, g["theta"], rtol=1e-15, atol=0)
+    assert plan.nbasis == g["bounds"][-1]
+    assert np.allclose(plan.q(), g["q"], rtol=1e-13, atol=0)
+    for iff in range(plan.nf):
+        ff, _, off, nt, ns = plan.frequency(iff)
+        assert abs(ff - g["ff"][iff]) <= 1e-15 * g["ff"][iff]
+        assert off == g["bounds"][iff] and ns == g["NP"][iff] and nt == g[f"f{iff}_enst"].shape[1]
+        enst, lat, lon = plan.lattice(iff)
+        assert np.allclose(lat, g[f"f{iff}_lat"], rtol=1e-14, atol=0)
+        assert np.allclose(lon, g[f"f{iff}_lon"], rtol=1e-14, atol=0)
+        ref = g[f"f{iff}_enst"]
+        assert np.array_equal(np.isnan(enst), np.isnan(ref))
+        assert np.allclose(enst[~np.isnan(ref)], ref[~np.isnan(ref)], rtol=0, atol=1e-10)
+        td, nrm, n = plan.centres(iff)
+        assert np.allclose(td, g[f"f{iff}_tdec"], rtol=1e-13, atol=0)
+        assert np.allclose(nrm, g[f"f{iff}_norm"], rtol=1e-13, atol=0)
+        assert np.array_equal(n, (~np.isnan(ref)).sum(axis=1))
+
+
+def test_drop_in_longitude_handling():
+    """prepare_aux converts the dataset's longitudes as basis.py:1944-1948
+    and sorts them."""
+    from vardyn_gb300.basis import Basis_bmaux
+    ds = dict(f=[1.0, 2.0], lat=[0.0, 1.0], lon=np.array([350.0, 10.0, 190.0]),
+              Tdec=np.arange(12.0).reshape(2, 2, 3), Std=np.ones((2, 2, 3)))
+    a = Basis_bmaux.prepare_aux(ds, "-180_180")
+    assert np.array_equal(a["lon"], [-170.0, -10.0, 10.0])
+    assert np.array_equal(a["Tdec"][0, 0], [2.0, 0.0, 1.0])
+    b = Basis_bmaux.prepare_aux(dict(ds, lon=np.array([-20.0, 5.0, 30.0])), "0_360")
+    assert np.array_equal(b["lon"], [5.0, 30.0, 340.0])

@@ -135,6 +135,15 @@ class VdSwDesc(ctypes.Structure):
     ]
 
 
+class VdBmauxParams(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_double) for k in ("npsp", "facpsp", "lmin", "lmax", "facns", "facnlt", "tdecmin",
+                                                "tdecmax", "factdec", "facQ")] + [
+        ("norm_time", ctypes.c_int), ("flux", ctypes.c_int), ("time_ref", ctypes.c_double),
+        ("aux_nf", ctypes.c_int), ("aux_nlat", ctypes.c_int), ("aux_nlon", ctypes.c_int),
+        ("aux_f", _DP), ("aux_lat", _DP), ("aux_lon", _DP), ("aux_tdec", _DP), ("aux_std", _DP),
+    ]
+
+
 class VdWaveletParams(ctypes.Structure):
     _fields_ = [(k, ctypes.c_double) for k in ("npsp", "facpsp", "facnst", "lmin", "lmax", "tmin", "tmax",
                                                 "sigma_Q")]
@@ -263,6 +272,8 @@ SIGNATURES = {
     "vd_mgd_solve": (I, [P, I, P, LL, LL, P, LL, LL, P, P, SZ, P]),
     "vd_bm_plan_create": (I, [ctypes.POINTER(P), ctypes.POINTER(VdBasisGrid), ctypes.POINTER(VdBmParams)]),
     "vd_wavelet_plan_create": (I, [ctypes.POINTER(P), ctypes.POINTER(VdBasisGrid), ctypes.POINTER(VdWaveletParams)]),
+    "vd_bmaux_plan_create": (I, [ctypes.POINTER(P), ctypes.POINTER(VdBasisGrid), ctypes.POINTER(VdBmauxParams)]),
+    "vd_bmaux_centres": (I, [P, I, P, P, P]),
     "vd_bm_plan_destroy": (I, [P]),
     "vd_bm_nbasis": (LL, [P]),
     "vd_bm_shape": (I, [P, ctypes.POINTER(I), ctypes.POINTER(I), P]),

@@ -309,6 +309,77 @@ class WaveletPlan(BMPlan):
         _lib.check(self.lib.vd_bm_shape(h, None, None, self.theta.ctypes.data), "vd_bm_shape")
 
 
+class BMauxParams:
+    """Parameters of the wave-packet basis with auxiliary fields (config.BASIS
+    fields of Basis_bmaux, basis.py:1748-1765) and the auxiliary fields
+    themselves: ``aux`` = dict(f, lat, lon, Tdec, Std), Tdec / Std
+    [f][lat][lon] on ascending coordinates in the grid's longitude
+    convention (Basis_bmaux.prepare_aux puts a dataset in that form)."""
+
+    def __init__(self, aux, npsp=3.5, facpsp=1.5, lmin=80., lmax=900., facns=1., facnlt=2., tdecmin=2.,
+                 tdecmax=20., factdec=1., facQ=1., norm_time=True, flux=False, time_ref=0.0):
+        self.__dict__.update(dict(npsp=npsp, facpsp=facpsp, lmin=lmin, lmax=lmax, facns=facns, facnlt=facnlt,
+                                  tdecmin=tdecmin, tdecmax=tdecmax, factdec=factdec, facQ=facQ,
+                                  norm_time=norm_time, flux=flux, time_ref=time_ref))
+        c = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        self.aux = {k: c(aux[k]) for k in ("f", "lat", "lon", "Tdec", "Std")}
+        shape = (self.aux["f"].size, self.aux["lat"].size, self.aux["lon"].size)
+        for k in ("Tdec", "Std"):
+            if self.aux[k].shape != shape:
+                raise ValueError(f"aux['{k}'] must be [f, lat, lon] = {shape}")
+
+    def to_c(self):
+        dp = ctypes.POINTER(ctypes.c_double)
+        a = self.aux
+        return _lib.VdBmauxParams(*[float(getattr(self, k)) for k in (
+            "npsp", "facpsp", "lmin", "lmax", "facns", "facnlt", "tdecmin", "tdecmax", "factdec", "facQ")],
+            int(bool(self.norm_time)), int(bool(self.flux)), float(self.time_ref),
+            a["f"].size, a["lat"].size, a["lon"].size, *[a[k].ctypes.data_as(dp) for k in (
+                "f", "lat", "lon", "Tdec", "Std")])
+
+
+class BMauxPlan(BMPlan):
+    """Wave-packet basis with per-location decorrelation times and variances
+    (Basis_bmaux, basis.py:1741-2638) on a rectilinear grid: the wave-packet
+    plan's atoms and passes, after a per-centre time reduction."""
+
+    def __init__(self, xc, yc, time, params, land=None, geographic=False, dtype=torch.float32, device=None,
+                 host_only=False):
+        self._grid(xc, yc, time, land, geographic, dtype, device, host_only)
+        self.params = params
+        h = ctypes.c_void_p()
+        pc = params.to_c()
+        with self._on_device():
+            _lib.check(self.lib.vd_bmaux_plan_create(ctypes.byref(h), ctypes.byref(self._gridc), ctypes.byref(pc)),
+                       "vd_bmaux_plan_create")
+        self._h = h
+        self.nbasis = int(self.lib.vd_bm_nbasis(h))
+        nf, nth = ctypes.c_int(), ctypes.c_int()
+        _lib.check(self.lib.vd_bm_shape(h, ctypes.byref(nf), ctypes.byref(nth), None), "vd_bm_shape")
+        self.nf, self.ntheta = nf.value, nth.value
+        self.theta = np.zeros(self.ntheta)
+        _lib.check(self.lib.vd_bm_shape(h, None, None, self.theta.ctypes.data), "vd_bm_shape")
+
+    def lattice(self, iff):
+        """(enst [NP][padded time centres], lat, lon) of frequency iff."""
+        _, _, _, nt, ns = self.frequency(iff)
+        enst, lat, lon = np.zeros((ns, nt)), np.zeros(ns), np.zeros(ns)
+        _lib.check(self.lib.vd_bm_lattice(self._h, iff, enst.ctypes.data, lat.ctypes.data, lon.ctypes.data),
+                   "vd_bm_lattice")
+        return enst, lat, lon
+
+    def centres(self, iff):
+        """(tdec, norm_fact, time-centre count) per space centre of frequency iff."""
+        ns = self.frequency(iff)[4]
+        td, nrm, nt = np.zeros(ns), np.zeros(ns), np.zeros(ns, dtype=np.int32)
+        _lib.check(self.lib.vd_bmaux_centres(self._h, iff, td.ctypes.data, nrm.ctypes.data, nt.ctypes.data),
+                   "vd_bmaux_centres")
+        return td, nrm, nt
+
+    def time_weights(self, k, iff):
+        raise NotImplementedError("the auxiliary-field basis weights time per space centre")
+
+
 # ---------------------------------------------------------------------------
 # Reference-facing classes
 # ---------------------------------------------------------------------------
@@ -516,3 +587,68 @@ class Basis_wavelet3d(Basis_gauss3d):
     def _make_plan(self, time):
         return WaveletPlan(self.lon, self.lat, time, self.params, land=self.mask, geographic=self.geographic,
                            dtype=self.dtype, device=self.device)
+
+
+class Basis_bmaux(Basis_gauss3d):
+    """Drop-in for Basis_bmaux / Basis_bmaux_jax (basis.py:1741-2638) with
+    the GPU projection: the jax class's operg / operg_transpose (the numpy
+    class's operg returns a field it never fills, 2303-2320).
+
+    ``config.BASIS.file_aux`` is the auxiliary dataset the reference opens
+    with xarray (1943-1950): here a mapping with 1-D ``lon``, ``lat``, ``f``
+    and 3-D ``Tdec``, ``Std`` [f][lat][lon] (no NetCDF reader ships with this
+    build); its longitudes are converted to the grid's convention and sorted
+    as the reference does. Not supported (they raise): depth tapering
+    (file_depth), a facQ_aux file, C-grid variables, geostrophic velocities
+    and background files."""
+
+    def __init__(self, config, State, multi_mode=False, dtype=torch.float32, device=None):
+        cb = config.BASIS
+        for name in ("file_depth", "file_facQaux", "c_grid_var"):
+            if getattr(cb, name, None) is not None:
+                raise NotImplementedError(f"config.BASIS.{name} is not supported by the GPU basis")
+        if getattr(cb, "compute_velocities", False):
+            raise NotImplementedError("config.BASIS.compute_velocities is not supported by the GPU basis")
+        pb = getattr(cb, "path_background", None)
+        if pb is not None:
+            import os
+            if os.path.exists(pb):
+                raise NotImplementedError("config.BASIS.path_background is not supported by the GPU basis")
+        import datetime
+        tref = (config.EXP.init_date - datetime.datetime(1950, 1, 1, 0)).total_seconds() / 24 / 3600
+        aux = self.prepare_aux(cb.file_aux, getattr(State, "lon_unit", "-180_180"))
+        self.params = BMauxParams(aux, npsp=cb.npsp, facpsp=cb.facpsp, lmin=cb.lmin, lmax=cb.lmax, facns=cb.facns,
+                                  facnlt=cb.facnlt, tdecmin=cb.tdecmin, tdecmax=cb.tdecmax, factdec=cb.factdec,
+                                  facQ=cb.facQ, norm_time=cb.norm_time, flux=getattr(cb, "flux", False),
+                                  time_ref=tref)
+        self.name_mod_var = cb.name_mod_var
+        self.multi_mode = multi_mode
+        self.lon, self.lat = _grid_axes(State)
+        self.geographic = True
+        self.ny, self.nx = State.ny, State.nx
+        self.mask = None
+        if getattr(State, "mask", None) is not None and np.any(State.mask):
+            self.mask = np.asarray(State.mask, dtype=bool)
+        self.dtype = dtype
+        self.device = torch.device(device or "cuda")
+        self.plan = None
+
+    @staticmethod
+    def prepare_aux(ds, lon_unit):
+        """The reference's longitude handling of the auxiliary dataset
+        (basis.py:1944-1948): to [0, 360) for a '0_360' grid when the
+        dataset has negative longitudes, to [-180, 180) for a '-180_180'
+        grid when it has none or some above 180; then sorted by longitude."""
+        lon = np.asarray(ds["lon"], dtype=np.float64)
+        if np.sign(lon.min()) == -1 and lon_unit == "0_360":
+            lon = lon % 360
+        elif (np.sign(lon.min()) >= 0 or lon.max() > 180) and lon_unit == "-180_180":
+            lon = (lon + 180) % 360 - 180
+        order = np.argsort(lon, kind="stable")
+        return dict(f=np.asarray(ds["f"], dtype=np.float64), lat=np.asarray(ds["lat"], dtype=np.float64),
+                    lon=lon[order], Tdec=np.asarray(ds["Tdec"], dtype=np.float64)[..., order],
+                    Std=np.asarray(ds["Std"], dtype=np.float64)[..., order])
+
+    def _make_plan(self, time):
+        return BMauxPlan(self.lon, self.lat, time, self.params, land=self.mask, geographic=self.geographic,
+                         dtype=self.dtype, device=self.device)

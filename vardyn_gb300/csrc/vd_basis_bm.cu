@@ -37,6 +37,13 @@ struct BmFreq {
     long long NP = 0;
     long long boff = 0;
     int rowoff = 0;
+    // auxiliary-field basis: per space centre the decorrelation time, window
+    // integral, time-centre axis (numpy arange: start, start + step, then
+    // start + i * delta) and count, prior std; the padded time-centre count
+    std::vector<double> c_tdec, c_norm, c_start, c_step, c_delta, c_std;
+    std::vector<int> c_n;
+    int nit = 0;
+    long long cboff = 0, cstart = 0;
 };
 
 }  // namespace
@@ -47,8 +54,16 @@ struct vd_bm_plan {
     long long nbasis = 0;
     int R = 0, KX = 1, KY = 1, NA = 1;
     vd_bm_params prm;
-    int kind = 0;                 // 0 wave packets (Basis_bm), 1 wavelets (Basis_wavelet3d)
+    int kind = 0;                 // 0 wave packets (Basis_bm), 1 wavelets (Basis_wavelet3d),
+                                  // 2 wave packets with auxiliary fields (Basis_bmaux)
     vd_wavelet_params wprm;
+    vd_bmaux_params aprm;
+    std::vector<double> ax_f, ax_lat, ax_lon, ax_td, ax_sd;
+    long long cbasis = 0;         // kind 2: time-reduced coefficients per window
+    long long ncentres = 0;
+    void* dev_aux = nullptr;
+    const double* d_ctab = nullptr;   // kind 2: [centre][5] tdec, norm, start, step, delta
+    const int32_t* d_cn = nullptr;    // kind 2: [centre] time-centre count
     std::vector<double> theta;
     std::vector<BmFreq> fr;
     std::vector<double> times;
@@ -209,6 +224,66 @@ k_bmT_xpass(BmDev<T> d, int k, const T* __restrict__ Uw, T* __restrict__ adX, lo
             A[o + 1] += g * zs;
         }
     }
+}
+
+// Auxiliary-field basis, time part at basis time t (days). For space centre
+// P of frequency f (global centre index cs + P) the active time centres are
+// those with |t - enst| <= tdec_P, weight window((t - enst) / tdec_P) /
+// norm_P (basis.py:2337-2352, jax form 2448-2461).
+__device__ __forceinline__ double bmaux_weight(const double* tab, int it, double t, int flux)
+{
+    const double tdec = tab[0], norm = tab[1], start = tab[2], step = tab[3], delta = tab[4];
+    const double c = it == 0 ? start : (it == 1 ? start + step : start + (double)it * delta);
+    const double dt = t - c;
+    if (fabs(dt) > tdec) return 0.0;
+    const double x = dt / tdec;
+    const double w = flux ? -M_PI * sin(x * 0.5 * M_PI) * cos(x * 0.5 * M_PI)
+                          : cos(x * 0.5 * M_PI) * cos(x * 0.5 * M_PI);
+    return w / norm;
+}
+
+// C[b][cboff + (P nth + th) 2 + c] = sum_it g(it, P) X[b][xboff + ((it NP + P) nth + th) 2 + c]
+// for one frequency: one thread per (P, th, c), window b on blockIdx.y
+template <typename T>
+__global__ void k_bmaux_reduce(const double* __restrict__ ctab, const int32_t* __restrict__ cn, long long cstart,
+                               long long np, int nth, long long xboff, long long cboff, double t, int flux,
+                               const T* __restrict__ X, long long ldX, T* __restrict__ C, long long ldC)
+{
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.y;
+    if (q >= np * 2 * nth) return;
+    const long long P = q / (2 * nth);
+    const double* tab = ctab + (cstart + P) * 5;
+    const int n = cn[cstart + P];
+    const T* x = X + (long long)b * ldX + xboff + q;
+    const long long stride = np * 2 * nth;
+    double acc = 0.0;
+    for (int it = 0; it < n; ++it) {
+        const double g = bmaux_weight(tab, it, t, flux);
+        if (g != 0.0) acc += g * (double)x[it * stride];
+    }
+    C[(long long)b * ldC + cboff + q] = (T)acc;
+}
+
+// adX[b][xboff + ((it NP + P) nth + th) 2 + c] += g(it, P) adC[b][cboff + (P nth + th) 2 + c]
+// for one frequency: one thread per coefficient of the frequency
+template <typename T>
+__global__ void k_bmaux_scatter(const double* __restrict__ ctab, const int32_t* __restrict__ cn, long long cstart,
+                                long long np, int nth, int nit, long long xboff, long long cboff, double t, int flux,
+                                const T* __restrict__ adC, long long ldC, T* __restrict__ adX, long long ldX)
+{
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.y;
+    const long long per = np * 2 * nth;
+    if (e >= per * nit) return;
+    const int it = (int)(e / per);
+    const long long q = e - (long long)it * per;
+    const long long P = q / (2 * nth);
+    if (it >= cn[cstart + P]) return;                 // padded time centre: weight 0
+    const double g = bmaux_weight(ctab + (cstart + P) * 5, it, t, flux);
+    if (g == 0.0) return;
+    T* a = adX + (long long)b * ldX + xboff + e;
+    *a = (T)((double)*a + g * (double)adC[(long long)b * ldC + cboff + q]);
 }
 
 }  // namespace vd
@@ -498,6 +573,184 @@ int bm_build(vd_bm_plan* p, const vd_basis_grid* g, BmTables& tb)
     return VD_OK;
 }
 
+// Orthogonal multilinear interpolation of an auxiliary field [f][lat][lon]
+// at (f, la, lo), NaN outside the coordinates (xarray's DataArray.interp with
+// 1-D indexers, linear); a NaN corner gives NaN.
+double aux_value(const vd_bm_plan* p, const std::vector<double>& fld, double f, double la, double lo)
+{
+    auto bracket = [](const std::vector<double>& c, double x, int& i0, double& w) {
+        const int n = (int)c.size();
+        if (!(x >= c[0] && x <= c[n - 1])) return false;
+        int i = (int)(std::upper_bound(c.begin(), c.end(), x) - c.begin()) - 1;
+        i = std::min(std::max(i, 0), n - 2);
+        i0 = i;
+        w = (x - c[i]) / (c[i + 1] - c[i]);
+        return true;
+    };
+    int a, b, c;
+    double wa, wb, wc;
+    if (!bracket(p->ax_f, f, a, wa) || !bracket(p->ax_lat, la, b, wb) || !bracket(p->ax_lon, lo, c, wc))
+        return std::nan("");
+    const size_t NL = p->ax_lat.size(), NO = p->ax_lon.size();
+    auto at = [&](int i, int j, int k) { return fld[((size_t)i * NL + j) * NO + k]; };
+    // along f, then lat, then lon, as the successive 1-D interpolations do
+    double v[2][2];
+    for (int j = 0; j < 2; ++j)
+        for (int k = 0; k < 2; ++k) v[j][k] = (1 - wa) * at(a, b + j, c + k) + wa * at(a + 1, b + j, c + k);
+    const double v0 = (1 - wb) * v[0][0] + wb * v[1][0], v1 = (1 - wb) * v[0][1] + wb * v[1][1];
+    return (1 - wc) * v0 + wc * v1;
+}
+
+// nanmean of a field over the 10 x 10 grid of a centre's box of half-width DX
+// (basis.py:2005-2009, 2066-2072); NaN when every value is NaN
+double aux_box_mean(const vd_bm_plan* p, const std::vector<double>& fld, double f, double la, double lo,
+                    double dlat, double dlon)
+{
+    const std::vector<double> elon = np_linspace(lo - dlon, lo + dlon, 10), elat = np_linspace(la - dlat, la + dlat, 10);
+    double sum = 0.0;
+    int cnt = 0;
+    for (double y : elat)
+        for (double x : elon) {
+            const double v = aux_value(p, fld, f, y, x);
+            if (!std::isnan(v)) {
+                sum += v;
+                ++cnt;
+            }
+        }
+    return cnt ? sum / cnt : std::nan("");
+}
+
+// Basis_bmaux (basis.py:1741-2393): the wave-packet lattice ending at
+// LAT_MAX + DX and LON_MAX + DX/cos (1947-1954), per-centre times and Q
+int bmaux_build(vd_bm_plan* p, const vd_basis_grid* g, BmTables& tb)
+{
+    const vd_bmaux_params& q = p->aprm;
+    const int ny = g->ny, nx = g->nx;
+    const bool geo = g->geographic != 0;
+    const double k2 = geo ? 1.0 / 110 : 1.0;
+    std::vector<double> xc(g->xc_host, g->xc_host + nx), yc(g->yc_host, g->yc_host + ny);
+    for (double v : xc) if (!std::isfinite(v)) return VD_ERR_ARG;
+    for (double v : yc) if (!std::isfinite(v)) return VD_ERR_ARG;
+    if (!(q.npsp > 0) || !(q.facpsp > 0) || !(q.lmin > 0) || !(q.lmax > q.lmin) || !(q.facns > 0) ||
+        !(q.facnlt > 0) || !(q.tdecmin > 0) || !(q.tdecmax >= q.tdecmin))
+        return VD_ERR_ARG;
+    const double LON_MIN = *std::min_element(xc.begin(), xc.end());
+    double LON_MAX = *std::max_element(xc.begin(), xc.end());
+    const double LAT_MIN = *std::min_element(yc.begin(), yc.end());
+    const double LAT_MAX = *std::max_element(yc.begin(), yc.end());
+    if (LON_MAX < LON_MIN) LON_MAX += 360.;
+    p->times.assign(g->time_host, g->time_host + g->ntime);
+    const double deltat = *std::max_element(p->times.begin(), p->times.end()) -
+                          *std::min_element(p->times.begin(), p->times.end());
+    auto cosd = [&](double lat) { return geo ? std::cos(lat * M_PI / 180.) : 1.0; };
+    auto window = [&](double x) { return q.flux ? mywindow_flux(x) : mywindow(x); };
+    std::vector<int8_t> land;
+    bool any_land = false;
+    if (g->land_host) {
+        land.assign(g->land_host, g->land_host + (size_t)ny * nx);
+        for (int8_t v : land) any_land |= (v != 0);
+    }
+    const double lstep = std::log(1 + q.facpsp / q.npsp);
+    std::vector<double> logff = np_arange(std::log(1. / q.lmin), std::log(1. / q.lmax) - lstep, -lstep);
+    std::reverse(logff.begin(), logff.end());
+    if (logff.size() < 2) return VD_ERR_ARG;
+    std::vector<double> ff(logff.size());
+    for (size_t i = 0; i < ff.size(); ++i) ff[i] = std::exp(logff[i]);
+    std::vector<double> th = np_linspace(0, M_PI, (int)(M_PI * ff[0] / (ff[1] - ff[0]) * q.facpsp));
+    if (th.size() < 2) return VD_ERR_ARG;
+    th.pop_back();
+    p->theta = th;
+    p->nth = (int)th.size();
+    p->nf = (int)ff.size();
+    p->fr.resize(ff.size());
+    PatState ps;
+    long long boff = 0, cboff = 0, cstart = 0;
+    int rowoff = 0;
+    for (int iff = 0; iff < p->nf; ++iff) {
+        BmFreq& F = p->fr[iff];
+        F.ff = ff[iff];
+        F.k = 2 * M_PI * ff[iff];
+        F.DX = 1. / ff[iff] * q.npsp * 0.5;
+        F.DXG = F.DX / q.facns;
+        const double dlat = F.DXG * k2;
+        const double lat0 = LAT_MIN - pymod(LAT_MIN, dlat) - F.DX * k2;
+        const double lat1 = LAT_MAX + F.DX * k2;
+        F.rows_lat = np_arange(lat0, lat1, dlat);
+        F.rowoff = rowoff;
+        long long cb = 0;
+        for (double la : F.rows_lat) {
+            const double cl = cosd(la);
+            const double dlon = F.DXG / cl * k2;
+            const double lon0 = LON_MIN - pymod(LON_MIN, dlon) - F.DX / cl * k2;
+            const double lon1 = LON_MAX + F.DX / cl * k2;
+            std::vector<double> lons0 = np_arange(lon0, lon1, dlon), lons;
+            for (double lo : lons0) {
+                if (any_land) {
+                    bool keep = false;
+                    for (int yy = 0; yy < ny && !keep; ++yy) {
+                        if (!(std::fabs((yc[yy] - la) / k2) <= 1. / ff[iff])) continue;
+                        for (int xx = 0; xx < nx; ++xx)
+                            if (std::fabs((xc[xx] - lo) / k2 * cl) <= 1. / ff[iff] && !land[(size_t)yy * nx + xx]) {
+                                keep = true;
+                                break;
+                            }
+                    }
+                    if (!keep) continue;
+                }
+                lons.push_back(lo);
+            }
+            add_row(p, tb, ps, iff, la, cl, lons, xc, k2, cb);
+        }
+        F.NP = cb;
+        // per-centre decorrelation time, window integral, time centres and std
+        int nit = 0;
+        for (long long P = 0; P < F.NP; ++P) {
+            const double la = F.enslat[P], lo = F.enslon[P];
+            const double bdlon = F.DX * k2 / cosd(la), bdlat = F.DX * k2;
+            const double m = aux_box_mean(p, p->ax_td, ff[iff], la, lo, bdlat, bdlon);
+            double td = std::isnan(m) ? 0.0 : m;
+            td *= q.factdec;
+            if (td < q.tdecmin) td = q.tdecmin;
+            if (td > q.tdecmax) td = q.tdecmax;
+            const double nrm = q.norm_time ? window_norm(td, window) : 1.0;
+            const double t0 = pymod(-q.time_ref, td);
+            const double step = td / q.facnlt, start = t0 - step;
+            const std::vector<double> en = np_arange(start, deltat + step, step);
+            const double sd = aux_box_mean(p, p->ax_sd, ff[iff], la, lo, bdlat, bdlon);
+            F.c_tdec.push_back(td);
+            F.c_norm.push_back(nrm);
+            F.c_start.push_back(start);
+            F.c_step.push_back(step);
+            F.c_delta.push_back((start + step) - start);
+            F.c_n.push_back((int)en.size());
+            F.c_std.push_back(std::isnan(sd) ? 1e-10 : sd);
+            nit = std::max(nit, (int)en.size());
+        }
+        F.nit = nit;
+        F.tdec = 0.0;
+        F.enst.assign((size_t)nit, std::nan(""));
+        F.boff = boff;
+        F.cboff = cboff;
+        F.cstart = cstart;
+        boff += (long long)nit * 2 * p->nth * F.NP;
+        cboff += 2LL * p->nth * F.NP;
+        cstart += F.NP;
+        rowoff += (int)F.rows_lat.size();
+        tb.freq_rowoff.push_back(F.rowoff);
+        tb.freq_boff.push_back(F.cboff);     // the passes read the time-reduced coefficients
+        tb.freq_np.push_back(F.NP);
+    }
+    p->nbasis = boff;
+    p->cbasis = cboff;
+    p->ncentres = cstart;
+    p->R = rowoff;
+    build_xy(p, tb, ps, yc, k2, ny, nx);
+    // the passes run on the time-reduced coefficients: one "time centre" of weight 1
+    std::vector<std::vector<std::pair<int, double>>> act((size_t)p->ntime * p->nf, {{0, 1.0}});
+    pack_time(p, act);
+    return VD_OK;
+}
+
 // Gaspari-Cohn function of mapping/src/tools.py:16-46 for one value
 double gaspari_cohn(double r, double c)
 {
@@ -706,12 +959,39 @@ int bm_upload(vd_bm_plan* p, const BmTables& tb, const int8_t* land_host)
     p->fy_s = b + o_fys;
     p->d_tact_g = b + o_tg;
     p->land = any_land ? (const int8_t*)(b + o_land) : nullptr;
+    if (p->kind == 2 && p->ncentres > 0) {
+        std::vector<double> tab;
+        std::vector<int32_t> cn;
+        tab.reserve((size_t)p->ncentres * 5);
+        for (const BmFreq& F : p->fr)
+            for (long long P = 0; P < F.NP; ++P) {
+                tab.insert(tab.end(), {F.c_tdec[P], F.c_norm[P], F.c_start[P], F.c_step[P], F.c_delta[P]});
+                cn.push_back(F.c_n[P]);
+            }
+        Packer pa;
+        const size_t o_tab = pa.add(tab), o_cn = pa.add(cn);
+        VD_CUDA_TRY(cudaMalloc(&p->dev_aux, pa.blob.size()));
+        VD_CUDA_TRY(cudaMemcpy(p->dev_aux, pa.blob.data(), pa.blob.size(), cudaMemcpyHostToDevice));
+        p->d_ctab = (const double*)((unsigned char*)p->dev_aux + o_tab);
+        p->d_cn = (const int32_t*)((unsigned char*)p->dev_aux + o_cn);
+    }
     return VD_OK;
 }
 
 size_t bm_ws_bytes(const vd_bm_plan* p, int batch)
 {
-    return (size_t)batch * p->R * p->nth * 2 * p->nx * (p->dtype == VD_F64 ? 8 : 4);
+    const size_t es = p->dtype == VD_F64 ? 8 : 4;
+    const size_t rows = (size_t)batch * p->R * p->nth * 2 * p->nx * es;
+    if (p->kind != 2) return rows;
+    return ((rows + 255) & ~size_t(255)) + (size_t)batch * p->cbasis * es;
+}
+
+// time-reduced coefficients of the auxiliary-field basis (behind the rows)
+template <typename T>
+T* bmaux_coeffs(const vd_bm_plan* p, int B, T* ws)
+{
+    const size_t rows = (size_t)B * p->R * p->nth * 2 * p->nx * sizeof(T);
+    return (T*)((char*)ws + ((rows + 255) & ~size_t(255)));
 }
 
 template <typename T>
@@ -720,6 +1000,20 @@ int bm_project(const vd_bm_plan* p, int B, int k, const T* X, long long ldX, T* 
 {
     const vd::BmDev<T> d = vd::bm_view<T>(p);
     const unsigned gx = (unsigned)((p->nx + 127) / 128);
+    if (p->kind == 2) {
+        T* C = bmaux_coeffs<T>(p, B, ws);
+        for (const BmFreq& F : p->fr) {
+            const long long n = F.NP * 2 * p->nth;
+            if (n == 0) continue;
+            vd::k_bmaux_reduce<T><<<dim3((unsigned)((n + 127) / 128), B), 128, 0, st>>>(
+                p->d_ctab, p->d_cn, F.cstart, F.NP, p->nth, F.boff, F.cboff, p->times[k], p->aprm.flux, X, ldX, C,
+                p->cbasis);
+            VD_LAUNCH_CHECK();
+        }
+        X = C;
+        ldX = p->cbasis;
+        k = 0;
+    }
     vd::k_bm_xpass<T><<<dim3(gx, p->R * p->nth, B), 128, 0, st>>>(d, k, X, ldX, ws);
     VD_LAUNCH_CHECK();
     vd::k_bm_ypass<T><<<dim3(gx, p->ny, B), 128, 0, st>>>(d, ws, phi, acc);
@@ -734,8 +1028,23 @@ int bm_project_T(const vd_bm_plan* p, int B, int k, const T* adphi, T* adX, long
     const unsigned gx = (unsigned)((p->nx + 127) / 128);
     vd::k_bmT_ypass<T><<<dim3(gx, p->R * p->nth, B), 128, 0, st>>>(d, adphi, ws);
     VD_LAUNCH_CHECK();
-    vd::k_bmT_xpass<T><<<dim3(p->R, B), 128, 0, st>>>(d, k, ws, adX, ldX);
+    if (p->kind != 2) {
+        vd::k_bmT_xpass<T><<<dim3(p->R, B), 128, 0, st>>>(d, k, ws, adX, ldX);
+        VD_LAUNCH_CHECK();
+        return VD_OK;
+    }
+    T* C = bmaux_coeffs<T>(p, B, ws);
+    VD_CUDA_TRY(cudaMemsetAsync(C, 0, (size_t)B * p->cbasis * sizeof(T), st));
+    vd::k_bmT_xpass<T><<<dim3(p->R, B), 128, 0, st>>>(d, 0, ws, C, p->cbasis);
     VD_LAUNCH_CHECK();
+    for (const BmFreq& F : p->fr) {
+        const long long n = (long long)F.nit * F.NP * 2 * p->nth;
+        if (n == 0) continue;
+        vd::k_bmaux_scatter<T><<<dim3((unsigned)((n + 127) / 128), B), 128, 0, st>>>(
+            p->d_ctab, p->d_cn, F.cstart, F.NP, p->nth, F.nit, F.boff, F.cboff, p->times[k], p->aprm.flux, C,
+            p->cbasis, adX, ldX);
+        VD_LAUNCH_CHECK();
+    }
     return VD_OK;
 }
 
@@ -751,9 +1060,9 @@ int bm_check(const vd_bm_plan* p, int B, int k, long long ldX, const void* a, co
 }  // namespace
 
 static vd_status bm_create(vd_bm_plan** out, const vd_basis_grid* g, const vd_bm_params* prm,
-                           const vd_wavelet_params* wprm)
+                           const vd_wavelet_params* wprm, const vd_bmaux_params* aprm = nullptr)
 {
-    if (!out || !g || (!prm && !wprm)) return VD_ERR_ARG;
+    if (!out || !g || (!prm && !wprm && !aprm)) return VD_ERR_ARG;
     *out = nullptr;
     if (g->ny < 1 || g->nx < 1 || !g->xc_host || !g->yc_host || g->ntime < 1 || !g->time_host) return VD_ERR_ARG;
     if (g->dtype != VD_F32 && g->dtype != VD_F64) return VD_ERR_ARG;
@@ -768,17 +1077,56 @@ static vd_status bm_create(vd_bm_plan** out, const vd_basis_grid* g, const vd_bm
         p->kind = 1;
         p->wprm = *wprm;
     }
+    if (aprm) {
+        p->kind = 2;
+        p->aprm = *aprm;
+        const vd_bmaux_params& a = *aprm;
+        if (a.aux_nf < 2 || a.aux_nlat < 2 || a.aux_nlon < 2 || !a.aux_f || !a.aux_lat || !a.aux_lon ||
+            !a.aux_tdec || !a.aux_std) {
+            delete p;
+            return VD_ERR_ARG;
+        }
+        const size_t n = (size_t)a.aux_nf * a.aux_nlat * a.aux_nlon;
+        p->ax_f.assign(a.aux_f, a.aux_f + a.aux_nf);
+        p->ax_lat.assign(a.aux_lat, a.aux_lat + a.aux_nlat);
+        p->ax_lon.assign(a.aux_lon, a.aux_lon + a.aux_nlon);
+        p->ax_td.assign(a.aux_tdec, a.aux_tdec + n);
+        p->ax_sd.assign(a.aux_std, a.aux_std + n);
+        p->aprm.aux_f = p->aprm.aux_lat = p->aprm.aux_lon = p->aprm.aux_tdec = p->aprm.aux_std = nullptr;
+        for (const std::vector<double>* c : {&p->ax_f, &p->ax_lat, &p->ax_lon})
+            for (size_t i = 1; i < c->size(); ++i)
+                if (!((*c)[i] > (*c)[i - 1])) {
+                    delete p;
+                    return VD_ERR_ARG;
+                }
+    }
     BmTables tb;
-    int st = p->kind == 1 ? wav_build(p, g, tb) : bm_build(p, g, tb);
+    int st = p->kind == 1 ? wav_build(p, g, tb) : (p->kind == 2 ? bmaux_build(p, g, tb) : bm_build(p, g, tb));
     if (st == VD_OK && ((long long)p->R * p->nth > 65535 || p->ny > 65535 || p->R > 65535)) st = VD_ERR_UNSUPPORTED;
     if (st == VD_OK && !p->host_only)
         st = p->dtype == VD_F64 ? bm_upload<double>(p, tb, g->land_host) : bm_upload<float>(p, tb, g->land_host);
     if (st != VD_OK) {
         if (p->dev) cudaFree(p->dev);
+        if (p->dev_aux) cudaFree(p->dev_aux);
         delete p;
         return st;
     }
     *out = p;
+    return VD_OK;
+}
+
+extern "C" vd_status vd_bmaux_plan_create(vd_bm_plan** out, const vd_basis_grid* g, const vd_bmaux_params* prm)
+{
+    return prm ? bm_create(out, g, nullptr, nullptr, prm) : VD_ERR_ARG;
+}
+
+extern "C" vd_status vd_bmaux_centres(const vd_bm_plan* p, int iff, double* tdec, double* norm, int* nt)
+{
+    if (!p || p->kind != 2 || iff < 0 || iff >= p->nf) return VD_ERR_ARG;
+    const BmFreq& F = p->fr[iff];
+    if (tdec) std::copy(F.c_tdec.begin(), F.c_tdec.end(), tdec);
+    if (norm) std::copy(F.c_norm.begin(), F.c_norm.end(), norm);
+    if (nt) std::copy(F.c_n.begin(), F.c_n.end(), nt);
     return VD_OK;
 }
 
@@ -796,6 +1144,7 @@ extern "C" vd_status vd_bm_plan_destroy(vd_bm_plan* p)
 {
     if (!p) return VD_ERR_ARG;
     if (p->dev) cudaFree(p->dev);
+    if (p->dev_aux) cudaFree(p->dev_aux);
     delete p;
     return VD_OK;
 }
@@ -828,7 +1177,17 @@ extern "C" vd_status vd_bm_lattice(const vd_bm_plan* p, int iff, double* enst, d
 {
     if (!p || iff < 0 || iff >= p->nf) return VD_ERR_ARG;
     const BmFreq& F = p->fr[iff];
-    if (enst) std::copy(F.enst.begin(), F.enst.end(), enst);
+    if (enst && p->kind == 2) {
+        // [NP][nit], NaN beyond a centre's own count (basis.py:2029-2035)
+        for (long long P = 0; P < F.NP; ++P)
+            for (int it = 0; it < F.nit; ++it)
+                enst[P * F.nit + it] = it >= F.c_n[P] ? std::nan("")
+                                       : it == 0 ? F.c_start[P]
+                                       : it == 1 ? F.c_start[P] + F.c_step[P]
+                                                 : F.c_start[P] + (double)it * F.c_delta[P];
+    } else if (enst) {
+        std::copy(F.enst.begin(), F.enst.end(), enst);
+    }
     if (enslat) std::copy(F.enslat.begin(), F.enslat.end(), enslat);
     if (enslon) std::copy(F.enslon.begin(), F.enslon.end(), enslon);
     return VD_OK;
@@ -837,6 +1196,16 @@ extern "C" vd_status vd_bm_lattice(const vd_bm_plan* p, int iff, double* enst, d
 extern "C" vd_status vd_bm_q(const vd_bm_plan* p, double* q)
 {
     if (!p || !q) return VD_ERR_ARG;
+    if (p->kind == 2) {
+        for (const BmFreq& F : p->fr)
+            for (int it = 0; it < F.nit; ++it)
+                for (long long P = 0; P < F.NP; ++P) {
+                    const double v = (it < F.c_n[P] ? F.c_std[P] : 1e-10) * p->aprm.facQ;
+                    std::fill(q + F.boff + (it * F.NP + P) * 2 * p->nth,
+                              q + F.boff + (it * F.NP + P + 1) * 2 * p->nth, v);
+                }
+        return VD_OK;
+    }
     for (const BmFreq& F : p->fr) {
         const long long n = (long long)F.enst.size() * 2 * p->nth * F.NP;
         std::fill(q + F.boff, q + F.boff + n, F.Q);
@@ -847,6 +1216,7 @@ extern "C" vd_status vd_bm_q(const vd_bm_plan* p, double* q)
 extern "C" vd_status vd_bm_time_weights(const vd_bm_plan* p, int k, int iff, int* count, int* it, double* w)
 {
     if (!p || !count || k < 0 || k >= p->ntime || iff < 0 || iff >= p->nf) return VD_ERR_ARG;
+    if (p->kind == 2) return VD_ERR_UNSUPPORTED;      // per-centre time weights
     const size_t s = (size_t)k * p->nf + iff;
     *count = p->tact_n[s];
     for (int a = 0; a < p->tact_n[s]; ++a) {
