@@ -72,6 +72,26 @@ typedef struct vd_qg1l_desc {
 #define VD_DST_AUTO 0
 #define VD_DST_FMA 1
 
+/* Launch schedule of a plan's Helmholtz inversion (x-DST pass, y tridiagonal
+ * solve, inverse x-DST pass). Every field 0 keeps the built-in rule; the
+ * autotuner (vardyn_gb300.autotune) times candidates and sets the fastest.
+ * A schedule applies to launches issued after the call (a captured CUDA
+ * graph keeps the schedule it was captured with); results agree to rounding
+ * whatever the schedule. */
+typedef struct vd_qg1l_schedule {
+    int engine;          /* 0 rule (tensor cores for float32 plans built with
+                            VD_DST_AUTO, else CUDA-core FMA / float64 FFT);
+                            1 CUDA-core FMA; 2 tensor cores (float32 plans
+                            built with VD_DST_AUTO) */
+    int tc_group_fwd;    /* 32-column output tiles per CTA of the forward
+                            tensor-core pass: 0 rule, or 1, 2, 4, 8 */
+    int tc_group_inv;    /* the same for the inverse pass */
+    int fma_rows;        /* rows per CTA of the FMA pass: 0 rule, 16, 32 or
+                            64 (float32) */
+    int tridiag_rows;    /* rows per thread of the tridiagonal solve: 0 rule,
+                            16 or 32 (used when the field fits, else the rule) */
+} vd_qg1l_schedule;
+
 /* ------------------------------------------------------------------------
  * Overlapping-tile QG 1.5-layer model, forward (QgmWithTiles.step,
  * mapping/models/model_qg1l/jqgm.py:1033-1376). Every tile runs its own
@@ -171,6 +191,11 @@ vd_status vd_qgtrac_step_adj(const vd_qg1l_plan* plan, const vd_qgtrac_desc* des
  * Qgm.__init__ (jqgm.py:113-236). */
 vd_status vd_qg1l_plan_create(vd_qg1l_plan** plan, const vd_qg1l_desc* desc);
 vd_status vd_qg1l_plan_destroy(vd_qg1l_plan* plan);
+/* VD_ERR_ARG for an out-of-range field, VD_ERR_UNSUPPORTED for a choice the
+ * plan cannot run (tensor cores without its images, an FMA row tile above
+ * the shared-memory limit). */
+vd_status vd_qg1l_set_schedule(vd_qg1l_plan* plan, const vd_qg1l_schedule* schedule);
+vd_status vd_qg1l_get_schedule(const vd_qg1l_plan* plan, vd_qg1l_schedule* schedule);
 
 /* Workspace for one call of `batch` windows (forward, tangent, adjoint and
  * the solve all fit in it). */

@@ -135,6 +135,10 @@ class VdSwDesc(ctypes.Structure):
     ]
 
 
+class VdQg1lSchedule(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_int) for k in ("engine", "tc_group_fwd", "tc_group_inv", "fma_rows", "tridiag_rows")]
+
+
 class VdBmauxParams(ctypes.Structure):
     _fields_ = [(k, ctypes.c_double) for k in ("npsp", "facpsp", "lmin", "lmax", "facns", "facnlt", "tdecmin",
                                                 "tdecmax", "factdec", "facQ")] + [
@@ -182,6 +186,8 @@ SIGNATURES = {
     "vd_qgtrac_step_tgl": (I, [P, ctypes.POINTER(VdQgtracDesc), I, P, P, P, P, P, P, I, P, P, P, SZ, P]),
     "vd_qgtrac_step_adj": (I, [P, ctypes.POINTER(VdQgtracDesc), I, P, P, P, P, P, P, I, P, P, P, SZ, P]),
     "vd_qg1l_plan_destroy": (I, [P]),
+    "vd_qg1l_set_schedule": (I, [P, ctypes.POINTER(VdQg1lSchedule)]),
+    "vd_qg1l_get_schedule": (I, [P, ctypes.POINTER(VdQg1lSchedule)]),
     "vd_qg1l_workspace_bytes": (SZ, [P, I]),
     "vd_qg1l_traj_bytes": (SZ, [P, I, I]),
     "vd_qg1l_nstage": (I, [P]),

@@ -1,5 +1,6 @@
 // C ABI entry points of libvardyn_gb300 (declared in include/vardyn_gb300.h).
 #include "vd_internal.cuh"
+#include <algorithm>
 #include <vector>
 #include <new>
 #include <cstring>
@@ -217,6 +218,33 @@ extern "C" vd_status vd_qg1l_plan_destroy(vd_qg1l_plan* p)
     cudaFree(p->d_beta);
     cudaFree(p->d_fB);
     delete p;
+    return VD_OK;
+}
+
+extern "C" vd_status vd_qg1l_set_schedule(vd_qg1l_plan* p, const vd_qg1l_schedule* s)
+{
+    if (!p || !s) return VD_ERR_ARG;
+    if (s->engine < 0 || s->engine > 2) return VD_ERR_ARG;
+    for (int g : {s->tc_group_fwd, s->tc_group_inv})
+        if (g != 0 && g != 1 && g != 2 && g != 4 && g != 8) return VD_ERR_ARG;
+    if (s->fma_rows != 0 && s->fma_rows != 16 && s->fma_rows != 32 && s->fma_rows != 64) return VD_ERR_ARG;
+    if (s->tridiag_rows != 0 && s->tridiag_rows != 16 && s->tridiag_rows != 32) return VD_ERR_ARG;
+    if (s->engine == 2 && !p->dst.tc) return VD_ERR_UNSUPPORTED;
+    if (s->fma_rows) {
+        const size_t es = elem_size(p->d.dtype);
+        if (s->fma_rows == 64 && es == 8) return VD_ERR_UNSUPPORTED;
+        const size_t c = (size_t)s->fma_rows;
+        const size_t smem = (2 * (size_t)p->dst.kpad * c + std::max<size_t>(2 * DST_KC * DST_NC, c * DST_NC)) * es;
+        if (smem > 200 * 1024) return VD_ERR_UNSUPPORTED;
+    }
+    p->sched = *s;
+    return VD_OK;
+}
+
+extern "C" vd_status vd_qg1l_get_schedule(const vd_qg1l_plan* p, vd_qg1l_schedule* s)
+{
+    if (!p || !s) return VD_ERR_ARG;
+    *s = p->sched;
     return VD_OK;
 }
 

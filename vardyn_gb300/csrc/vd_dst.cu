@@ -721,7 +721,8 @@ static int launch_tridiag(const vd_qg1l_plan* p, int nf, T* spec, cudaStream_t s
     const dim3 grid((t.n + CW - 1) / CW, nf);
     const int nw16 = ((t.my + 15) / 16 + SUB - 1) / SUB;
     const int nw32 = ((t.my + 31) / 32 + SUB - 1) / SUB;
-    if (nw16 <= 16) {
+    const bool want32 = p->sched.tridiag_rows == 32 && nw32 <= 16;
+    if (nw16 <= 16 && !want32) {
         tridiag_chunked_kernel<T, CW, 16><<<grid, dim3(32, nw16), 2 * nw16 * SUB * CW * sizeof(T), st>>>(
             spec, (const T*)t.trim, t.my, t.n, t.lds, a);
     } else if (nw32 <= 16) {
@@ -823,6 +824,8 @@ template <typename T>
 static int pick_tr(const vd_qg1l_plan* p, int R)
 {
     const DSTTables& t = p->dst;
+    if (p->sched.fma_rows == 16 || p->sched.fma_rows == 32 || (p->sched.fma_rows == 64 && sizeof(T) == 4))
+        return p->sched.fma_rows;
     const int cand[3] = {64, 32, 16};
     for (int c : cand) {
         if (sizeof(T) == 8 && c == 64) continue;
@@ -848,7 +851,7 @@ int helmholtz_solve(const vd_qg1l_plan* p, int nf, const SolveArgs& a, T* spec, 
     int rc;
     auto run = [&](bool fwd) -> int {
         if constexpr (sizeof(T) == 4) {
-            if (p->dst.tc && tc_fits(p, nf)) return dst_pass_tc(p, nf, a, (float*)spec, fwd, st);
+            if (use_tc(p, nf)) return dst_pass_tc(p, nf, a, (float*)spec, fwd, st);
             if (tr == 64) return launch_pair<T, 64>(p, g, a, spec, st, fwd);
         } else {
             if (p->dst.fft_L) return launch_fft(p, g, a, (double*)spec, st, fwd);
@@ -885,7 +888,7 @@ int dst_x_only(const vd_qg1l_plan* p, int nf, const T* field, T* spec, int inver
     }
     const int tr = pick_tr<T>(p, g.R);
     if constexpr (sizeof(T) == 4) {
-        if (p->dst.tc && tc_fits(p, nf)) return dst_pass_tc(p, nf, a, (float*)spec, !inverse, st);
+        if (use_tc(p, nf)) return dst_pass_tc(p, nf, a, (float*)spec, !inverse, st);
         if (tr == 64) return launch_pair<T, 64>(p, g, a, spec, st, !inverse);
     } else {
         if (p->dst.fft_L) return launch_fft(p, g, a, (double*)spec, st, !inverse);

@@ -709,6 +709,8 @@ int dst_pass_tc(const vd_qg1l_plan* p, int nf, const SolveArgs& a, float* spec, 
     for (int gsz : {8, 4, 2}) {
         if (2LL * groups(gsz) * rows >= 120) { tab.gi = gsz; break; }
     }
+    if (p->sched.tc_group_fwd > 0) tab.gf = p->sched.tc_group_fwd;
+    if (p->sched.tc_group_inv > 0) tab.gi = p->sched.tc_group_inv;
     // as many stages as the B operand size of the launch allows
     const int gmax = fwd ? tab.gf : tab.gi;
     tab.b_tile = (uint32_t)gmax * TILE_BYTES;

@@ -99,6 +99,7 @@ struct vd_qg1l_plan {
     void* d_beta;
     void* d_fB;
     int device;
+    vd_qg1l_schedule sched{};   // launch schedule of the inversion (0 = rule)
 };
 
 namespace vd {
@@ -117,6 +118,8 @@ int build_tc_images(vd_qg1l_plan* p);
 void free_tc_images(vd_qg1l_plan* p);
 // Whether a batch of nf fields fits the tensor-core pass (32-bit row offsets).
 bool tc_fits(const vd_qg1l_plan* p, int nf);
+// Whether the tensor-core pass runs for nf fields under the plan's schedule.
+inline bool use_tc(const vd_qg1l_plan* p, int nf) { return p->dst.tc && tc_fits(p, nf) && p->sched.engine != 1; }
 int dst_pass_tc(const vd_qg1l_plan* p, int nf, const SolveArgs& a, float* spec, bool fwd, cudaStream_t st);
 
 // Kernel attributes (cudaFuncSetAttribute) apply to the device that is

@@ -678,6 +678,19 @@ class MixedWindows4DVar:
             self._run(xs)
         return [(eng.J, eng.grad) for eng in self.engines]
 
+    def tune(self, verbose=False):
+        """Autotune each size class's inversion schedule for its batch
+        (vardyn_gb300.autotune.tune); a captured graph is dropped, since it
+        keeps the schedule it was captured with. Returns {(ny, nx):
+        schedule}."""
+        from . import autotune
+        out = {}
+        for eng in self.engines:
+            sched, _ = autotune.tune(eng.plan, eng.B, verbose=verbose)
+            out[(eng.plan.ny, eng.plan.nx)] = sched
+        self.graph = None
+        return out
+
     def capture(self):
         self.x_static = [torch.zeros(eng.B, eng.plan.ny, eng.plan.nx, dtype=eng.plan.dtype,
                                      device=eng.plan.device) for eng in self.engines]

@@ -131,6 +131,27 @@ class QG1LPlan:
     def handle(self):
         return self._h
 
+    # ---------------- launch schedule of the inversion ----------------
+    SCHEDULE_KEYS = ("engine", "tc_group_fwd", "tc_group_inv", "fma_rows", "tridiag_rows")
+
+    def schedule(self):
+        """The inversion's launch schedule (vd_qg1l_schedule; 0 = built-in rule)."""
+        s = _lib.VdQg1lSchedule()
+        _lib.call("vd_qg1l_get_schedule", self._h, ctypes.byref(s))
+        return {k: int(getattr(s, k)) for k in self.SCHEDULE_KEYS}
+
+    def set_schedule(self, **kw):
+        """Set schedule fields (the others keep their values); see
+        vd_qg1l_set_schedule for the choices. Raises on a choice the plan
+        cannot run."""
+        cur = self.schedule()
+        for k, v in kw.items():
+            if k not in cur:
+                raise KeyError(k)
+            cur[k] = int(v)
+        _lib.call("vd_qg1l_set_schedule", self._h, ctypes.byref(_lib.VdQg1lSchedule(**cur)))
+        return cur
+
     # ---------------- buffers ----------------
     def workspace(self, batch):
         ws = self._ws.get(batch)
