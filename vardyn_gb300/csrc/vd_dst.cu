@@ -237,8 +237,12 @@ dst_gemm_kernel(GemmGeom g, const T* __restrict__ W1, const T* __restrict__ W2,
 // the pieces of their column through shared memory and every piece applies
 // the carry it receives. Eight columns per CTA: 1024 CTAs for 16 fields of
 // 512^2, 128 for one 1024^2 field.
-template <typename T, int CW, int CH>
-__global__ void __launch_bounds__(512)
+// LEAN caps the registers at 80 (16-row pieces in float32 otherwise take
+// ~124): three 256-thread CTAs fit an SM instead of two, which hides the
+// barrier of the carry chain better at some shapes (a schedule choice, picked
+// by timing).
+template <typename T, int CW, int CH, bool LEAN = false>
+__global__ void __maxnreg__(LEAN ? 80 : 128)
 tridiag_chunked_kernel(T* __restrict__ spec, const T* __restrict__ trim, int my, int n, int lds, T a)
 {
     constexpr int SUB = 32 / CW;
@@ -722,7 +726,10 @@ static int launch_tridiag(const vd_qg1l_plan* p, int nf, T* spec, cudaStream_t s
     const int nw16 = ((t.my + 15) / 16 + SUB - 1) / SUB;
     const int nw32 = ((t.my + 31) / 32 + SUB - 1) / SUB;
     const bool want32 = p->sched.tridiag_rows == 32 && nw32 <= 16;
-    if (nw16 <= 16 && !want32) {
+    if (nw16 <= 16 && !want32 && p->sched.tridiag_lean == 1 && sizeof(T) == 4) {
+        tridiag_chunked_kernel<T, CW, 16, true><<<grid, dim3(32, nw16), 2 * nw16 * SUB * CW * sizeof(T), st>>>(
+            spec, (const T*)t.trim, t.my, t.n, t.lds, a);
+    } else if (nw16 <= 16 && !want32) {
         tridiag_chunked_kernel<T, CW, 16><<<grid, dim3(32, nw16), 2 * nw16 * SUB * CW * sizeof(T), st>>>(
             spec, (const T*)t.trim, t.my, t.n, t.lds, a);
     } else if (nw32 <= 16) {

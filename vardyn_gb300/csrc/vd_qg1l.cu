@@ -399,7 +399,9 @@ __global__ void k_stage_tl(QGGeom G, int B, const T* __restrict__ hs, const T* _
 //     aut / avt). With gacc.nk > 0 the PV adjoint is returned as
 //     M3 * (sum of gacc + local), the final combination of a step.
 // h (halo 3) and q (halo 4) are staged in shared memory once; the phase-A
-// quantities never leave shared memory.
+// quantities never leave shared memory, and phase A stores lk times the split
+// T-point velocities (lk u+, lk u-, lk v+, lk v-) so phase B's upwind
+// transpose reads them without re-splitting.
 // ---------------------------------------------------------------------------
 constexpr int AT_Y = 32, AT_X = 32;                 // output tile
 constexpr int AH_Y = AT_Y + 6, AH_X = AT_X + 6;     // h tile (halo 3)
@@ -407,16 +409,59 @@ constexpr int AQ_Y = AT_Y + 8, AQ_X = AT_X + 8;     // q tile (halo 4)
 constexpr int AA_Y = AT_Y + 4, AA_X = AT_X + 4;     // phase-A region (halo 2)
 
 template <typename T>
-struct AdjTile {
-    T h[AH_Y][AH_X];
-    T q[AQ_Y][AQ_X];
-    T qa[AQ_Y][AQ_X];        // q + f*bathymetry (only when present)
-    T lk[AA_Y][AA_X];
-    T ut[AA_Y][AA_X];
-    T vt[AA_Y][AA_X];
-    T aut[AA_Y][AA_X];
-    T avt[AA_Y][AA_X];
+static size_t adj_bytes(const vd_qg1l_plan* p);
+
+// Shared layout of one CTA: h tile, q tile, the upwind products of the
+// stage-increment adjoint lk with the split T-point velocities (lk u+, lk u-,
+// lk v+, lk v-: phase B reads them directly), the velocity adjoints aut, avt;
+// then, only when present, lk itself (the diffusion transpose) and q + f *
+// bathymetry.
+template <typename T>
+struct AdjSmem {
+    T (*h)[AH_X];
+    T (*q)[AQ_X];
+    T (*lup)[AA_X];
+    T (*lum)[AA_X];
+    T (*lvp)[AA_X];
+    T (*lvm)[AA_X];
+    T (*aut)[AA_X];
+    T (*avt)[AA_X];
+    T (*lk)[AA_X];           // only when the plan has diffusion
+    T (*qa)[AQ_X];           // only with a bathymetry term
 };
+
+__host__ __device__ constexpr size_t adj_smem_elems(bool hasK, bool hasB)
+{
+    return (size_t)AH_Y * AH_X + (size_t)AQ_Y * AQ_X + 6 * (size_t)AA_Y * AA_X + (hasK ? (size_t)AA_Y * AA_X : 0) +
+           (hasB ? (size_t)AQ_Y * AQ_X : 0);
+}
+
+template <typename T>
+__device__ __forceinline__ AdjSmem<T> adj_smem(unsigned char* raw, bool hasK, bool hasB)
+{
+    T* b = reinterpret_cast<T*>(raw);
+    AdjSmem<T> S;
+    S.h = reinterpret_cast<T(*)[AH_X]>(b);
+    b += AH_Y * AH_X;
+    S.q = reinterpret_cast<T(*)[AQ_X]>(b);
+    b += AQ_Y * AQ_X;
+    S.lup = reinterpret_cast<T(*)[AA_X]>(b); b += AA_Y * AA_X;
+    S.lum = reinterpret_cast<T(*)[AA_X]>(b); b += AA_Y * AA_X;
+    S.lvp = reinterpret_cast<T(*)[AA_X]>(b); b += AA_Y * AA_X;
+    S.lvm = reinterpret_cast<T(*)[AA_X]>(b); b += AA_Y * AA_X;
+    S.aut = reinterpret_cast<T(*)[AA_X]>(b); b += AA_Y * AA_X;
+    S.avt = reinterpret_cast<T(*)[AA_X]>(b); b += AA_Y * AA_X;
+    S.lk = hasK ? reinterpret_cast<T(*)[AA_X]>(b) : nullptr;
+    if (hasK) b += AA_Y * AA_X;
+    S.qa = hasB ? reinterpret_cast<T(*)[AQ_X]>(b) : nullptr;
+    return S;
+}
+
+template <typename T>
+static size_t adj_bytes(const vd_qg1l_plan* p)
+{
+    return adj_smem_elems(p->geom.hasK != 0, p->geom.fB != nullptr) * sizeof(T);
+}
 
 template <typename T>
 __global__ void __launch_bounds__(256)
@@ -424,12 +469,13 @@ k_adj_stage_fused(QGGeom G, int nf, const T* __restrict__ hs, const T* __restric
                   StageIn<T> gacc, T* __restrict__ adq_out, T* __restrict__ adh_out)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    AdjTile<T>& S = *reinterpret_cast<AdjTile<T>*>(smem_raw);
+    const bool hasB = G.fB != nullptr;
+    const bool hasK = G.hasK != 0;
+    const AdjSmem<T> S = adj_smem<T>(smem_raw, hasK, hasB);
     const int f = blockIdx.z;
     const int j0 = blockIdx.y * AT_Y, i0 = blockIdx.x * AT_X;
     const int tid = threadIdx.y * 32 + threadIdx.x;
     const long long fo = f * G.fs;
-    const bool hasB = G.fB != nullptr;
     // ---- stage h and q: every load of the thread issued before any store ----
     {
         constexpr int NHL = (AH_Y * AH_X + 255) / 256, NQL = (AQ_Y * AQ_X + 255) / 256;
@@ -528,7 +574,13 @@ k_adj_stage_fused(QGGeom G, int nf, const T* __restrict__ hs, const T* __restric
             aut = lk * gu;
             avt = lk * gv - beta * lk;
         }
-        S.lk[a][b] = lk; S.ut[a][b] = uT; S.vt[a][b] = vT; S.aut[a][b] = aut; S.avt[a][b] = avt;
+        S.lup[a][b] = lk * (uT < T(0) ? T(0) : uT);
+        S.lum[a][b] = lk * (uT > T(0) ? T(0) : uT);
+        S.lvp[a][b] = lk * (vT < T(0) ? T(0) : vT);
+        S.lvm[a][b] = lk * (vT > T(0) ? T(0) : vT);
+        S.aut[a][b] = aut;
+        S.avt[a][b] = avt;
+        if (hasK) S.lk[a][b] = lk;
     }
     __syncthreads();
     // ---- phase B on the tile (accumulated adjoints and flags loaded first) ----
@@ -556,10 +608,10 @@ k_adj_stage_fused(QGGeom G, int nf, const T* __restrict__ hs, const T* __restric
         const int j = j0 + a, i = i0 + b;
         if (e >= AT_Y * AT_X || j >= G.ny || i >= G.nx) continue;
         const int A = a + 2, Bc = b + 2;    // phase-A index of X
-        auto UP = [&](int da, int db) { const T u = S.ut[A + da][Bc + db]; return S.lk[A + da][Bc + db] * (u < T(0) ? T(0) : u); };
-        auto UM = [&](int da, int db) { const T u = S.ut[A + da][Bc + db]; return S.lk[A + da][Bc + db] * (u > T(0) ? T(0) : u); };
-        auto VP = [&](int da, int db) { const T v = S.vt[A + da][Bc + db]; return S.lk[A + da][Bc + db] * (v < T(0) ? T(0) : v); };
-        auto VM = [&](int da, int db) { const T v = S.vt[A + da][Bc + db]; return S.lk[A + da][Bc + db] * (v > T(0) ? T(0) : v); };
+        auto UP = [&](int da, int db) { return S.lup[A + da][Bc + db]; };
+        auto UM = [&](int da, int db) { return S.lum[A + da][Bc + db]; };
+        auto VP = [&](int da, int db) { return S.lvp[A + da][Bc + db]; };
+        auto VM = [&](int da, int db) { return S.lvm[A + da][Bc + db]; };
         T aq = cx * (-T(2) * UP(0, -1) - T(6) * UM(0, -1)
                      - T(3) * UP(0, 0) + T(3) * UM(0, 0)
                      + T(6) * UP(0, 1) + T(2) * UM(0, 1)
@@ -568,7 +620,7 @@ k_adj_stage_fused(QGGeom G, int nf, const T* __restrict__ hs, const T* __restric
                      - T(3) * VP(0, 0) + T(3) * VM(0, 0)
                      + T(6) * VP(1, 0) + T(2) * VM(1, 0)
                      - VP(2, 0) + VM(-2, 0));
-        if (G.hasK) {
+        if (hasK) {
             const T lc = S.lk[A][Bc];
             aq += T(G.Kx) * (S.lk[A][Bc - 1] + S.lk[A][Bc + 1] - T(2) * lc)
                 + T(G.Ky) * (S.lk[A - 1][Bc] + S.lk[A + 1][Bc] - T(2) * lc);
@@ -829,10 +881,10 @@ int advance_adj_impl(const vd_qg1l_plan* p, int nf, const T* traj, int traj_step
     static PerDeviceOnce attr_once;
     const cudaError_t attr_err = attr_once.run([]() -> cudaError_t {
         cudaError_t e = cudaFuncSetAttribute(k_adj_stage_fused<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)sizeof(AdjTile<float>));
+                                             (int)(adj_smem_elems(true, true) * sizeof(float)));
         if (!e)
             e = cudaFuncSetAttribute(k_adj_stage_fused<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)sizeof(AdjTile<double>));
+                                     (int)(adj_smem_elems(true, true) * sizeof(double)));
         return e;
     });
     if (attr_err != cudaSuccess) return VD_ERR_CUDA;
@@ -854,7 +906,7 @@ int advance_adj_impl(const vd_qg1l_plan* p, int nf, const T* traj, int traj_step
             if (s >= 1) {
                 StageIn<T> none{};
                 none.nk = 0;
-                k_adj_stage_fused<T><<<agrid, kBlock, sizeof(AdjTile<T>), st>>>(p->geom, nf, tv.h(n, s),
+                k_adj_stage_fused<T><<<agrid, kBlock, adj_bytes<T>(p), st>>>(p->geom, nf, tv.h(n, s),
                                                                                  tv.q(n, s), gin, none, adql, adhs);
                 VD_LAUNCH_CHECK();
                 SolveArgs a;
@@ -866,7 +918,7 @@ int advance_adj_impl(const vd_qg1l_plan* p, int nf, const T* traj, int traj_step
                 StageIn<T> acc{};
                 acc.nk = 0;
                 for (int t = 0; t < S; ++t) { acc.k[acc.nk] = Gb[t]; acc.c[acc.nk] = T(1); ++acc.nk; }
-                k_adj_stage_fused<T><<<agrid, kBlock, sizeof(AdjTile<T>), st>>>(p->geom, nf, tv.h(n, s),
+                k_adj_stage_fused<T><<<agrid, kBlock, adj_bytes<T>(p), st>>>(p->geom, nf, tv.h(n, s),
                                                                                  tv.q(n, s), gin, acc, adq, adh);
                 VD_LAUNCH_CHECK();
             }
@@ -898,10 +950,10 @@ int rk_stage_adj_impl(const vd_qg1l_plan* p, int nf, const T* hs, const T* qs, i
     static PerDeviceOnce attr_once;
     const cudaError_t attr_err = attr_once.run([]() -> cudaError_t {
         cudaError_t e = cudaFuncSetAttribute(k_adj_stage_fused<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)sizeof(AdjTile<float>));
+                                             (int)(adj_smem_elems(true, true) * sizeof(float)));
         if (!e)
             e = cudaFuncSetAttribute(k_adj_stage_fused<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)sizeof(AdjTile<double>));
+                                     (int)(adj_smem_elems(true, true) * sizeof(double)));
         return e;
     });
     if (attr_err != cudaSuccess) return VD_ERR_CUDA;
@@ -911,7 +963,7 @@ int rk_stage_adj_impl(const vd_qg1l_plan* p, int nf, const T* hs, const T* qs, i
     gac.nk = nacc;
     for (int t = 0; t < nacc; ++t) { gac.k[t] = acc[t]; gac.c[t] = T(1); }
     const dim3 agrid((p->d.nx + AT_X - 1) / AT_X, (p->d.ny + AT_Y - 1) / AT_Y, nf);
-    k_adj_stage_fused<T><<<agrid, kBlock, sizeof(AdjTile<T>), st>>>(p->geom, nf, hs, qs, gin, gac, adq_out,
+    k_adj_stage_fused<T><<<agrid, kBlock, adj_bytes<T>(p), st>>>(p->geom, nf, hs, qs, gin, gac, adq_out,
                                                                      adh_out);
     VD_LAUNCH_CHECK();
     return VD_OK;
