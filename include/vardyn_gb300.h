@@ -740,6 +740,18 @@ size_t vd_sw_ref_adj_bytes(const vd_sw_plan* plan);
 vd_status vd_sw_set_ref_adj(vd_sw_plan* plan, void* buf);
 vd_status vd_sw_ref_pullback(const vd_sw_plan* plan, const void* buf, void* adH, void* adhw,
                              void* stream);
+/* Tangent with respect to H and h_wind (the dH / dh_wind inputs of the jvp
+ * of SW.step, sw.py:906-922, used by Model_qgsw.jstep_tgl, mod.py:3222-3253):
+ * computes the tangents of the H / h_wind dependent tables (reference
+ * thickness and its face averages, reference pressure gradients; the wind
+ * factors move only with h_wind, the wind depth of a perturbed H being the
+ * model's own) on the host and registers them for the following
+ * vd_sw_step_tgl / vd_sw_rhs_tgl calls. dH_host [nl][nx][ny] and
+ * dhwind_host [nx][ny] (a scalar h_wind plan reads dhwind_host[0]) may be
+ * NULL; buf is a device buffer of vd_sw_ref_adj_bytes(plan) bytes that stays
+ * alive while registered; buf NULL unregisters. Synchronous (one host to
+ * device copy). */
+vd_status vd_sw_set_ref_tangent(vd_sw_plan* plan, const double* dH_host, const double* dhwind_host, void* buf);
 /* nstep RK3-SSP steps. ub/vb/hb (sponge targets) default to the initial
  * state, Fu/Fv/Fh (forcing) to zero, taux [nx-1][ny] / tauy [nx][ny-1] to
  * the plan's wind stress; all are physical, all nullable (in groups of

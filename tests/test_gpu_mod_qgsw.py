@@ -207,3 +207,43 @@ def test_state_level_H_and_h_wind_controls():
         # settle at ~1e-6 to 1e-5 (measured), while the H / h_wind cotangents
         # themselves are pinned to 1e-6 by the plan-level tests
         assert abs(ad - fd) <= 1e-4 * abs(fd), (k, ad, fd)
+
+
+def test_state_level_tangent_with_H_and_h_wind_controls():
+    """The tangent with nonzero dState.params['H'] / ['h_wind'] (mod.py:
+    3348-3453) against the adjoint of the same State-level step: the dot
+    product holds to rounding."""
+    M, st = setup("SW", 2, True, name_params=("bc", "H", "h_wind"))
+    rng = np.random.default_rng(22)
+    ny, nx = M.ny, M.nx
+    ocean = ~st.mask
+    st.params["H"] = 3.0 * rng.standard_normal((ny, nx))
+    st.params["h_wind"] = 50.0 + 5.0 * rng.standard_normal((ny, nx))
+
+    def draw(seed):
+        r = np.random.default_rng(seed)
+        d = st.copy()
+        for k in list(d.var):
+            d.var[k] = r.standard_normal(d.var[k].shape) * (ocean if d.var[k].shape[-2:] == (ny, nx) else 1)
+        d.var["u"], d.var["v"] = d.var["u_layers"][0].copy(), d.var["v_layers"][0].copy()
+        d.var["ssh"] = d.var["h_layers"].sum(0)
+        for k in list(d.params):
+            d.params[k] = r.standard_normal(d.params[k].shape)
+        return d
+
+    d, d0 = draw(23), draw(23)
+    M.step_tgl(d, st, nstep=3, t=0)
+    w = st.copy()
+    for k in list(w.var):
+        w.var[k] = rng.standard_normal(w.var[k].shape)
+    for k in list(w.params):
+        w.params[k] = np.zeros_like(w.params[k])
+    a = w.copy()
+    M.step_adj(a, st, nstep=3, t=0)
+    keys = ["u_layers", "v_layers", "h_layers"]
+    lhs = sum(float((d.var[k] * w.var[k]).sum()) for k in keys)
+    lhs += float((d.var["ssh"] * w.var["ssh"]).sum() + (d.var["u"] * w.var["u"]).sum()
+                 + (d.var["v"] * w.var["v"]).sum())
+    rhs = sum(float((d0.var[k] * a.var[k]).sum()) for k in keys)
+    rhs += sum(float((d0.params[k] * a.params[k]).sum()) for k in a.params)
+    assert abs(lhs - rhs) <= 1e-9 * abs(lhs), (lhs, rhs)

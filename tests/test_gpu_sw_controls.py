@@ -174,3 +174,87 @@ def test_dropin_H_and_h_wind_steps_match_reference():
     r = SW(dict(base, h_wind=50.0)).step(g[p + "u0"], g[p + "v0"], g[p + "h0"], nstep=3, h_wind=g[p + "hw"])
     for a, k in zip(r, ("uW", "vW", "hW")):
         assert np.abs(a - g[p + k]).max() <= 1e-11 * np.abs(g[p + k]).max(), k
+
+
+def _tl_J(pl, x, dx, w, forcing, nstep=3, **d):
+    out = pl.step_tgl(*map(T, x), *map(T, dx), nstep=nstep, **forcing, **d)
+    return sum(float((a * T(b)).sum()) for a, b in zip(out, w))
+
+
+@pytest.mark.parametrize("forcing_momentum", ["direct", "mass_consistent"])
+def test_tangent_wrt_H_matches_finite_differences(forcing_momentum):
+    """The tangent of the step in a spatial, per-layer H (the H entry of
+    jax.jvp, sw.py:906-922) against central differences of the forward, with
+    the state tangent zero; wind depth from the model's H."""
+    rng = np.random.default_rng(31)
+    Hb = H0.reshape(NL, 1, 1)
+    Ht = Hb + 5.0 * rng.standard_normal((NL, NX, NY))
+    x, w = _state(8), _state(9)
+    F = _forcing(10)
+    mk = lambda H: _plan(H, H_wind=Hb, forcing_momentum=forcing_momentum)
+    dH = rng.standard_normal((NL, NX, NY))
+    zero = tuple(np.zeros_like(a) for a in x)
+    tl = _tl_J(mk(Ht), x, zero, w, F, dH=dH)
+    # strongly nonlinear in H: central differences reach ~3e-9 at eps = 1e-4
+    eps = 1e-4
+    fd = (_J(mk(Ht + eps * dH), x, w, F) - _J(mk(Ht - eps * dH), x, w, F)) / (2 * eps)
+    assert abs(tl - fd) <= 1e-6 * abs(fd), (tl, fd)
+
+
+@pytest.mark.parametrize("h_wind", ["field", "scalar"])
+def test_tangent_wrt_h_wind_matches_finite_differences(h_wind):
+    rng = np.random.default_rng(32)
+    hw = 60.0 + 10.0 * rng.standard_normal((NX, NY)) if h_wind == "field" else 55.0
+    d = rng.standard_normal((NX, NY)) if h_wind == "field" else 1.0
+    x, w = _state(11), _state(12)
+    mk = lambda h: _plan(H0.reshape(NL, 1, 1), h_wind=h)
+    zero = tuple(np.zeros_like(a) for a in x)
+    tl = _tl_J(mk(hw), x, zero, w, {}, dh_wind=d)
+    eps = 1e-2
+    fd = (_J(mk(hw + eps * d), x, w, {}) - _J(mk(hw - eps * d), x, w, {})) / (2 * eps)
+    assert abs(tl - fd) <= 1e-6 * abs(fd), (tl, fd)
+
+
+def test_tangent_and_adjoint_wrt_H_and_h_wind_are_transposes():
+    """<TL(dx, dH, dh_wind), w> = <dx, adj_x(w)> + <dH, adj_H(w)> +
+    <dh_wind, adj_h_wind(w)> to rounding, with forcing and mass-consistent
+    momentum forcing on."""
+    rng = np.random.default_rng(33)
+    Hb = H0.reshape(NL, 1, 1)
+    Ht = Hb + 5.0 * rng.standard_normal((NL, NX, NY))
+    hw = 60.0 + 10.0 * rng.standard_normal((NX, NY))
+    pl = _plan(Ht, H_wind=Hb, h_wind=hw, forcing_momentum="mass_consistent")
+    x, dx, w = _state(13), _state(14), _state(15)
+    F = _forcing(16)
+    dH = rng.standard_normal((NL, NX, NY))
+    dhw = rng.standard_normal((NX, NY))
+    lhs = _tl_J(pl, x, dx, w, F, dH=dH, dh_wind=dhw)
+    a = pl.step_adj(*map(T, x), *map(T, w), nstep=3, want_ref=True, **F)
+    rhs = sum(float((a[k] * T(b)).sum()) for k, b in zip(("u0", "v0", "h0"), dx))
+    rhs += float((a["H"] * T(dH)).sum()) + float((a["h_wind"] * T(dhw)).sum())
+    assert abs(lhs - rhs) <= 1e-11 * abs(lhs), (lhs, rhs)
+    # the tangent tables are unregistered after the call: a plain tangent
+    # again ignores H / h_wind
+    plain = _tl_J(pl, x, dx, w, F)
+    rhs0 = sum(float((a[k] * T(b)).sum()) for k, b in zip(("u0", "v0", "h0"), dx))
+    assert abs(plain - rhs0) <= 1e-11 * abs(plain), (plain, rhs0)
+
+
+def test_dropin_step_tgl_with_H_and_h_wind_tangents():
+    """SW.step_tgl with H / dH (1, nx, ny) and h_wind / dh_wind (nx, ny), as
+    Model_qgsw passes them, equals the plan's tangent at H + dH-base."""
+    rng = np.random.default_rng(34)
+    m = _sw(h_wind=40.0)
+    Hp = 3.0 * rng.standard_normal((1, NX, NY))
+    hwp = 5.0 * rng.standard_normal((NX, NY))
+    dH = rng.standard_normal((1, NX, NY))
+    dhw = rng.standard_normal((NX, NY))
+    x, dx = _state(17), _state(18)
+    r = m.step_tgl(*x, *dx, H=Hp, dH=dH, nstep=2, h_wind=hwp, dh_wind=dhw)
+    pl = _plan(H0.reshape(NL, 1, 1) + Hp, h_wind=40.0 + hwp, H_wind=H0.reshape(NL, 1, 1))
+    ref = pl.step_tgl(*map(T, x), *map(T, dx), nstep=2, dH=np.broadcast_to(dH, (NL, NX, NY)), dh_wind=dhw)
+    for a, b in zip(r, ref):
+        b = b.cpu().numpy()
+        assert np.abs(np.asarray(a) - b).max() <= 1e-13 * np.abs(b).max()
+    r0 = m.step_tgl(*x, *dx, H=Hp, nstep=2, h_wind=hwp)
+    assert max(float(np.abs(np.asarray(a) - b.cpu().numpy()).max()) for a, b in zip(r0, ref)) > 0.0

@@ -241,6 +241,7 @@ SIGNATURES = {
     "vd_sw_workspace_bytes": (SZ, [P, I, I]),
     "vd_sw_ref_adj_bytes": (SZ, [P]),
     "vd_sw_set_ref_adj": (I, [P, P]),
+    "vd_sw_set_ref_tangent": (I, [P, P, P, P]),
     "vd_sw_ref_pullback": (I, [P, P, P, P, P]),
     "vd_sw_step": (I, [P, I, P, P, P, I, P, P, P, P, P, P, P, P, P, P, P, P, SZ, P]),
     "vd_sw_step_tgl": (I, [P, I, P, P, P, P, P, P, I, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P, P,

@@ -394,6 +394,9 @@ struct Tab {
     // cotangent accumulators of the H / h_wind dependent tables, summed over
     // batch, stages and steps by the adjoint kernels (null: not accumulated)
     T *ad_href, *ad_hrefu, *ad_hrefv, *ad_dxp, *ad_dyp, *ad_wfu, *ad_wfv;
+    // tangents of the same tables (jvp with respect to H / h_wind), read by
+    // the dual-number kernels when registered (null: not perturbed)
+    const T *d_href, *d_hrefu, *d_hrefv, *d_dxp, *d_dyp, *d_wfu, *d_wfv;
     int wind_mode;                // h_wind: 0 from H (layer 0), 1 scalar, 2 field
     T G[MAXL];                    // G[l] = sum_{k<=l} g'_k
     T gp[MAXL];
@@ -440,6 +443,24 @@ struct WD {
 };
 
 template <typename R> struct Tri { R u, v, h; };
+
+// A table value as the kernel's arithmetic type: the plain value, or for the
+// dual-number (tangent) kernels the value with its registered tangent
+// (0 when none); p null reads as 0.
+template <typename T>
+__device__ __forceinline__ T tab_val(const T* p, const T*, long long i, T*)
+{
+    return p ? p[i] : T(0);
+}
+template <typename T>
+__device__ __forceinline__ DN<T, 1> tab_val(const T* p, const T* d, long long i, DN<T, 1>*)
+{
+    DN<T, 1> r;
+    r.v = p ? p[i] : T(0);
+    r.d[0] = d ? d[i] : T(0);
+    return r;
+}
+#define VD_TAB(S, p, d, i) tab_val((p), (d), (i), (S*)nullptr)
 
 // ------------------------------------------------------------------ k_sw_diag
 // One thread per (x, y) of the vorticity grid and batch member; loops over
@@ -495,7 +516,7 @@ __global__ void k_sw_diag(Tab<T> t, Tri<R> x, W om, W kp, W ht)
         const T iv1 = t.idyv2[(long long)i * (ny + 1) + j + 1], iv0 = t.idyv2[(long long)i * (ny + 1) + j];
         const S ke = T(0.25) * (a * (a * iu1) + c * (c * iu0) + d * (d * iv1) + e * (e * iv0)) * mh;
         kp(ob * t.sh + hi, ke + pacc);
-        const T hr = t.href[(long long)l * t.sh + hi];
+        const S hr = VD_TAB(S, t.href, t.d_href, (long long)l * t.sh + hi);
         if (t.linear) ht(ob * t.sh + hi, hr + T(0) * hl[l]);
         else ht(ob * t.sh + hi, sclamp(hr + hl[l], t.hmin * ar, t.sharp));
     }
@@ -539,8 +560,14 @@ __global__ void k_sw_tend(Tab<T> t, Tri<R> x, R om, R kp, R ht, const T* taux, c
             const S oVm = weno_flux<T>(q, Vm, bits, j >= 1 && j <= ny - 2, j >= 2 && j <= ny - 3);
             du = oVm + t.fsu[ui] * Vm;
             const S kpd = kp(ob * t.sh + ui) - kp(ob * t.sh + ui - ny);
-            du = du - (t.hxy_dxp ? kpd + t.dxp[(long long)l * (nx - 1) * ny + (long long)(i - 1) * ny + j] : kpd);
-            if (l == 0) du = du + (taux ? taux : t.taux)[(long long)(i - 1) * ny + j] * t.wfu[ui];
+            const long long pi = (long long)l * (nx - 1) * ny + (long long)(i - 1) * ny + j;
+            if constexpr (std::is_same<S, T>::value) {
+                du = du - (t.hxy_dxp ? kpd + t.dxp[pi] : kpd);
+                if (l == 0) du = du + (taux ? taux : t.taux)[(long long)(i - 1) * ny + j] * t.wfu[ui];
+            } else {
+                du = du - ((t.hxy_dxp || t.d_dxp) ? kpd + VD_TAB(S, t.hxy_dxp ? t.dxp : nullptr, t.d_dxp, pi) : kpd);
+                if (l == 0) du = du + (taux ? taux : t.taux)[(long long)(i - 1) * ny + j] * VD_TAB(S, t.wfu, t.d_wfu, ui);
+            }
             if (l == nl - 1) du = du - t.drag * x.u(ob * t.su + ui);
             if (t.visc > T(0)) {
                 const long long ub = ob * t.su;
@@ -591,8 +618,14 @@ __global__ void k_sw_tend(Tab<T> t, Tri<R> x, R om, R kp, R ht, const T* taux, c
             dv = -(oUm + t.fsv[vi] * Um);
             const long long hi = (long long)i * ny + j;
             const S kpd = kp(ob * t.sh + hi) - kp(ob * t.sh + hi - 1);
-            dv = dv - (t.hxy_dyp ? kpd + t.dyp[(long long)l * nx * (ny - 1) + (long long)i * (ny - 1) + j - 1] : kpd);
-            if (l == 0) dv = dv + (tauy ? tauy : t.tauy)[(long long)i * (ny - 1) + j - 1] * t.wfv[vi];
+            const long long pj = (long long)l * nx * (ny - 1) + (long long)i * (ny - 1) + j - 1;
+            if constexpr (std::is_same<S, T>::value) {
+                dv = dv - (t.hxy_dyp ? kpd + t.dyp[pj] : kpd);
+                if (l == 0) dv = dv + (tauy ? tauy : t.tauy)[(long long)i * (ny - 1) + j - 1] * t.wfv[vi];
+            } else {
+                dv = dv - ((t.hxy_dyp || t.d_dyp) ? kpd + VD_TAB(S, t.hxy_dyp ? t.dyp : nullptr, t.d_dyp, pj) : kpd);
+                if (l == 0) dv = dv + (tauy ? tauy : t.tauy)[(long long)i * (ny - 1) + j - 1] * VD_TAB(S, t.wfv, t.d_wfv, vi);
+            }
             if (l == nl - 1) dv = dv - t.drag * x.v(ob * t.sv + vi);
             if (t.visc > T(0)) {
                 const long long vb = ob * t.sv;
@@ -732,7 +765,7 @@ __global__ void k_sw_force_mc(Tab<T> t, Tri<R> x, Tri<R> F, Tri<W> out)
         const long long ui = (long long)i * ny + j, idx = ob * t.su + ui;
         const S hu = T(0.5) * (rep_pad<T, S>(t, x.h, hb, i + 1, j + 1) + rep_pad<T, S>(t, x.h, hb, i, j + 1));
         const S fu = T(0.5) * (rep_pad<T, S>(t, F.h, hb, i + 1, j + 1) + rep_pad<T, S>(t, F.h, hb, i, j + 1));
-        const S htu = sclamp(t.hrefu[(long long)l * t.su + ui] + hu, t.hmin * t.areau[ui], t.sharp);
+        const S htu = sclamp(VD_TAB(S, t.hrefu, t.d_hrefu, (long long)l * t.su + ui) + hu, t.hmin * t.areau[ui], t.sharp);
         const S u = x.u(idx);
         S n = u + dt * ((-u) / htu * fu);
         out.u(idx, n + dt * F.u(idx));
@@ -741,7 +774,7 @@ __global__ void k_sw_force_mc(Tab<T> t, Tri<R> x, Tri<R> F, Tri<W> out)
         const long long vi = (long long)i * (ny + 1) + j, idx = ob * t.sv + vi;
         const S hv = T(0.5) * (rep_pad<T, S>(t, x.h, hb, i + 1, j + 1) + rep_pad<T, S>(t, x.h, hb, i + 1, j));
         const S fv = T(0.5) * (rep_pad<T, S>(t, F.h, hb, i + 1, j + 1) + rep_pad<T, S>(t, F.h, hb, i + 1, j));
-        const S htv = sclamp(t.hrefv[(long long)l * t.sv + vi] + hv, t.hmin * t.areav[vi], t.sharp);
+        const S htv = sclamp(VD_TAB(S, t.hrefv, t.d_hrefv, (long long)l * t.sv + vi) + hv, t.hmin * t.areav[vi], t.sharp);
         const S v = x.v(idx);
         S n = v + dt * ((-v) / htv * fv);
         out.v(idx, n + dt * F.v(idx));
@@ -1267,6 +1300,10 @@ struct vd_sw_plan {
     Tab<float> tf;
     Tab<double> td;
     int has_taux, has_tauy;
+    // host copies for the tangent tables of vd_sw_set_ref_tangent
+    std::vector<double> h_area, h_dwu, h_dwv, h_gp;
+    std::vector<uint8_t> h_fu, h_fv;
+    int h_wind_mode = 0;
 };
 
 namespace {
@@ -1392,6 +1429,7 @@ static void fill_tab(Tab<T>& t, vd_sw_plan* p, const std::vector<size_t>& off)
     t.iarea = P(); t.idx2h = P(); t.idy2h = P();
     t.dwu = P(); t.dwv = P();
     t.ad_href = t.ad_hrefu = t.ad_hrefv = t.ad_dxp = t.ad_dyp = t.ad_wfu = t.ad_wfv = nullptr;
+    t.d_href = t.d_hrefu = t.d_hrefv = t.d_dxp = t.d_dyp = t.d_wfu = t.d_wfv = nullptr;
     t.fh = (const uint8_t*)(base + off[k++]);
     t.fu = (const uint8_t*)(base + off[k++]);
     t.fv = (const uint8_t*)(base + off[k++]);
@@ -1621,6 +1659,13 @@ extern "C" vd_status vd_sw_plan_create(vd_sw_plan** out, const vd_sw_desc* d)
     p->d.sponge_u_host = p->d.sponge_v_host = p->d.sponge_h_host = nullptr;
     p->d.Hwind_host = nullptr;
     p->nx = nx; p->ny = ny; p->nl = nl; p->esz = esz;
+    p->h_area = area;
+    p->h_dwu = dwu;
+    p->h_dwv = dwv;
+    p->h_gp.assign(d->g_prime_host, d->g_prime_host + nl);
+    p->h_fu.assign(M.fu.begin(), M.fu.end());
+    p->h_fv.assign(M.fv.begin(), M.fv.end());
+    p->h_wind_mode = d->h_wind_mode;
     if (cudaMalloc(&p->dev, tot) != cudaSuccess) {
         delete p;
         return VD_ERR_CUDA;
@@ -1710,6 +1755,103 @@ extern "C" vd_status vd_sw_ref_pullback(const vd_sw_plan* p, const void* buf, vo
     else go(p->tf);
     VD_LAUNCH_CHECK();
     return VD_OK;
+}
+
+// Tangent of the H / h_wind dependent tables (the same layout as the
+// cotangent buffer): the reference thickness H area and its face averages,
+// the reference pressure gradients (linear in H: eta_l = -sum_{m<l} H_m,
+// p_l = sum_{k<=l} g'_k eta_k, then differences), and the wind factors, which
+// a perturbed H leaves alone (the wind depth is the model's own, sw.py:
+// 622-630) and a perturbed h_wind moves by d(wind factor)/d(face depth) times
+// the face average of dh_wind.
+template <typename T>
+static int set_ref_tangent(vd_sw_plan* p, Tab<T>& t, const double* dH, const double* dhw, void* buf)
+{
+    if (!buf) {
+        t.d_href = t.d_hrefu = t.d_hrefv = t.d_dxp = t.d_dyp = t.d_wfu = t.d_wfv = nullptr;
+        return VD_OK;
+    }
+    const int nx = p->nx, ny = p->ny, nl = p->nl;
+    const size_t sh = (size_t)nx * ny, su = (size_t)(nx + 1) * ny, sv = (size_t)nx * (ny + 1);
+    std::vector<double> out;
+    out.reserve(ref_adj_elems(p));
+    std::vector<double> dref((size_t)nl * sh, 0.0);
+    for (int l = 0; l < nl; ++l)
+        for (size_t k = 0; k < sh; ++k) dref[(size_t)l * sh + k] = dH ? dH[(size_t)l * sh + k] * p->h_area[k] : 0.0;
+    out.insert(out.end(), dref.begin(), dref.end());
+    std::vector<double> au((size_t)nl * su), av((size_t)nl * sv);
+    for (int l = 0; l < nl; ++l) {
+        std::vector<double> hr(dref.begin() + (size_t)l * sh, dref.begin() + (size_t)(l + 1) * sh), a, b;
+        edge_avg0(hr, nx, ny, a);
+        edge_avg1(hr, nx, ny, b);
+        std::copy(a.begin(), a.end(), au.begin() + (size_t)l * su);
+        std::copy(b.begin(), b.end(), av.begin() + (size_t)l * sv);
+    }
+    out.insert(out.end(), au.begin(), au.end());
+    out.insert(out.end(), av.begin(), av.end());
+    std::vector<double> pref((size_t)nl * sh, 0.0);
+    if (dH) {
+        for (size_t k = 0; k < sh; ++k) {
+            double tot = 0;
+            for (int l = 0; l < nl; ++l) tot += dH[(size_t)l * sh + k];
+            double cs = 0, pp = 0;
+            for (int l = 0; l < nl; ++l) {
+                cs += dH[(size_t)l * sh + k];
+                const double rc = dH[(size_t)l * sh + k] + tot - cs;
+                pp += p->h_gp[l] * (-tot + rc);
+                pref[(size_t)l * sh + k] = pp;
+            }
+        }
+    }
+    for (int l = 0; l < nl; ++l)
+        for (int i = 0; i < nx - 1; ++i)
+            for (int j = 0; j < ny; ++j)
+                out.push_back(pref[(size_t)l * sh + (size_t)(i + 1) * ny + j] - pref[(size_t)l * sh + (size_t)i * ny + j]);
+    for (int l = 0; l < nl; ++l)
+        for (int i = 0; i < nx; ++i)
+            for (int j = 0; j < ny - 1; ++j)
+                out.push_back(pref[(size_t)l * sh + (size_t)i * ny + j + 1] - pref[(size_t)l * sh + (size_t)i * ny + j]);
+    std::vector<double> wu(su, 0.0), wv(sv, 0.0);
+    if (dhw && p->h_wind_mode != 0) {
+        for (int i = 1; i < nx; ++i)
+            for (int j = 0; j < ny; ++j) {
+                const size_t k = (size_t)i * ny + j;
+                if (!(p->h_fu[k] & 1)) continue;
+                const double dd = p->h_wind_mode == 1 ? dhw[0]
+                                                      : 0.5 * (dhw[(size_t)(i - 1) * ny + j] + dhw[(size_t)i * ny + j]);
+                wu[k] = p->h_dwu[k] * dd;
+            }
+        for (int i = 0; i < nx; ++i)
+            for (int j = 1; j < ny; ++j) {
+                const size_t k = (size_t)i * (ny + 1) + j;
+                if (!(p->h_fv[k] & 1)) continue;
+                const double dd = p->h_wind_mode == 1 ? dhw[0]
+                                                      : 0.5 * (dhw[(size_t)i * ny + j - 1] + dhw[(size_t)i * ny + j]);
+                wv[k] = p->h_dwv[k] * dd;
+            }
+    }
+    out.insert(out.end(), wu.begin(), wu.end());
+    out.insert(out.end(), wv.begin(), wv.end());
+    if (out.size() != ref_adj_elems(p)) return VD_ERR_ARG;
+    std::vector<T> cast(out.begin(), out.end());
+    VD_CUDA_TRY(cudaMemcpy(buf, cast.data(), cast.size() * sizeof(T), cudaMemcpyHostToDevice));
+    const long long nxl = nx, nyl = ny;
+    const T* b = (const T*)buf;
+    t.d_href = b; b += (long long)nl * t.sh;
+    t.d_hrefu = b; b += (long long)nl * t.su;
+    t.d_hrefv = b; b += (long long)nl * t.sv;
+    t.d_dxp = b; b += (long long)nl * (nxl - 1) * nyl;
+    t.d_dyp = b; b += (long long)nl * nxl * (nyl - 1);
+    t.d_wfu = b; b += t.su;
+    t.d_wfv = b;
+    return VD_OK;
+}
+
+extern "C" vd_status vd_sw_set_ref_tangent(vd_sw_plan* p, const double* dH_host, const double* dhwind_host, void* buf)
+{
+    if (!p) return VD_ERR_ARG;
+    return p->esz == 8 ? set_ref_tangent(p, p->td, dH_host, dhwind_host, buf)
+                       : set_ref_tangent(p, p->tf, dH_host, dhwind_host, buf);
 }
 
 extern "C" void vd_sw_plan_destroy(vd_sw_plan* p)

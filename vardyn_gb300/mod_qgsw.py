@@ -336,11 +336,11 @@ class Model_qgsw:
         self._state_out(State, x)
 
     def step_tgl(self, dState, State, nstep=1, t=0):
-        """mod.py:3348-3453 (tangent of state, forcing and bc parameters)."""
-        for k in ("H", "h_wind"):
-            if k in self.name_params and np.any(np.asarray(_np(dState.params.get(k, 0.0))) != 0):
-                raise NotImplementedError(f"tangent with respect to {k}")
+        """mod.py:3348-3453 (tangent of state, forcing, bc, H and h_wind
+        parameters)."""
         pl = self._plan(State)
+        dH, dhw = self._ref_params(dState)
+        dref = {k: v for k, v in (("dH", dH), ("dh_wind", dhw)) if v is not None}
         x = self._state_in(State)
         dx = self._state_in(dState)
         F, dF = self._forcing(State), self._forcing(dState)
@@ -353,7 +353,8 @@ class Model_qgsw:
             tx, ty = self._wind(t_chunk)
             xm = self._mdt(x, +1)
             dx = pl.step_tgl(*xm, *dx, nstep=n_chunk, ub=ub, vb=vb, hb=hb, dub=db[0], dvb=db[1], dhb=db[2],
-                             Fu=F[0], Fv=F[1], Fh=F[2], dFu=dF[0], dFv=dF[1], dFh=dF[2], taux=tx, tauy=ty)
+                             Fu=F[0], Fv=F[1], Fh=F[2], dFu=dF[0], dFv=dF[1], dFh=dF[2], taux=tx, tauy=ty,
+                             **dref)
             x = self._fwd(x, State, t_chunk, n_chunk, F)
         du, dv, dh = (a.cpu().numpy() for a in dx)
         if self.nl > 1:

@@ -218,13 +218,11 @@ class SW:
 
     def step_tgl(self, u0, v0, h0, du0, dv0, dh0, H=None, dH=None, nstep=1, taux=None, tauy=None, h_wind=None,
                  dh_wind=None):
-        """jax.jvp of step in (u0, v0, h0) (sw.py:906-922)."""
-        if dH is not None or dh_wind is not None:
-            raise NotImplementedError("tangent with respect to H or h_wind")
+        """jax.jvp of step in (u0, v0, h0, H, h_wind) (sw.py:906-922)."""
         pl = self._plan(self._host(H), self._host(h_wind))
         tx, ty = self._tau(taux, tauy)
         r = pl.step_tgl(self._in(u0), self._in(v0), self._in(h0), self._in(du0), self._in(dv0), self._in(dh0),
-                        nstep=nstep, taux=tx, tauy=ty)
+                        nstep=nstep, taux=tx, tauy=ty, dH=self._host(dH), dh_wind=self._host(dh_wind))
         return tuple(self._out(du0, a) for a in r)
 
     def step_adj(self, u0, v0, h0, wuT, wvT, whT, H=None, nstep=1, taux=None, tauy=None, h_wind=None):

@@ -213,7 +213,31 @@ class SWPlan:
                 self._field(Fh, sh, "Fh") if Fh is not None else z(sh))
 
     def step_tgl(self, u0, v0, h0, du0, dv0, dh0, nstep=1, ub=None, vb=None, hb=None, dub=None, dvb=None, dhb=None,
-                 Fu=None, Fv=None, Fh=None, dFu=None, dFv=None, dFh=None, taux=None, tauy=None):
+                 Fu=None, Fv=None, Fh=None, dFu=None, dFv=None, dFh=None, taux=None, tauy=None, dH=None,
+                 dh_wind=None):
+        """Tangent of :meth:`step`; ``dH`` (broadcast to [nl, nx, ny]) and
+        ``dh_wind`` ([nx, ny], or a scalar for a scalar h_wind) perturb the
+        layer thicknesses and the wind depth (vd_sw_set_ref_tangent)."""
+        if dH is not None or dh_wind is not None:
+            esz = 8 if self.dtype == torch.float64 else 4
+            buf = torch.zeros(self._lib.vd_sw_ref_adj_bytes(self._h) // esz, dtype=self.dtype, device=self.device)
+            dHh = None
+            if dH is not None:
+                a = np.asarray(dH.detach().cpu() if torch.is_tensor(dH) else dH, dtype=np.float64)
+                while a.ndim < 3:
+                    a = a[None]
+                dHh = np.ascontiguousarray(np.broadcast_to(a, (self.nl, self.nx, self.ny)))
+            dhw = None
+            if dh_wind is not None:
+                a = np.asarray(dh_wind.detach().cpu() if torch.is_tensor(dh_wind) else dh_wind, dtype=np.float64)
+                dhw = np.ascontiguousarray(a.reshape(1) if a.size == 1 else np.broadcast_to(a, (self.nx, self.ny)))
+            hp = lambda a: None if a is None else ctypes.c_void_p(a.ctypes.data)   # noqa: E731
+            _lib.call("vd_sw_set_ref_tangent", self._h, hp(dHh), hp(dhw), _ptr(buf))
+            try:
+                return self.step_tgl(u0, v0, h0, du0, dv0, dh0, nstep=nstep, ub=ub, vb=vb, hb=hb, dub=dub, dvb=dvb,
+                                     dhb=dhb, Fu=Fu, Fv=Fv, Fh=Fh, dFu=dFu, dFv=dFv, dFh=dFh, taux=taux, tauy=tauy)
+            finally:
+                _lib.call("vd_sw_set_ref_tangent", self._h, None, None, None)
         B = self._batch(u0)
         u0, v0, h0 = self._uvh(u0, v0, h0, B)
         du0, dv0, dh0 = self._uvh(du0, dv0, dh0, B, "d")
