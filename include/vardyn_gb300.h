@@ -93,6 +93,10 @@ typedef struct vd_qg1l_schedule {
     int tridiag_lean;    /* 1: the float32 16-row tridiagonal kernel capped at
                             80 registers (three CTAs per SM instead of two);
                             0 the standard kernel */
+    int stencil_loads;   /* tiles of the adjoint stage: 0 rule (bulk tensor
+                            copies when nx is a multiple of 16 and the fields
+                            are 16-byte aligned, else bounds-checked loads);
+                            1 bounds-checked loads */
 } vd_qg1l_schedule;
 
 /* ------------------------------------------------------------------------
@@ -901,7 +905,8 @@ const char* vd_version(void);
  * counts launches recorded into a CUDA graph during capture). */
 long long vd_launch_count(void);
 /* Device-side error bits set by bounded waits that ran out (1: stage
- * recycle, 2: operand arrival, 4: accumulator completion); 0 = none.
+ * recycle, 2: operand arrival, 4: accumulator completion of the tensor-core
+ * DST; 8: the staged tiles of the QG adjoint stage); 0 = none.
  * Synchronous; reset != 0 clears them. */
 vd_status vd_device_error(int* flags, int reset);
 

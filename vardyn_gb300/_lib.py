@@ -137,7 +137,7 @@ class VdSwDesc(ctypes.Structure):
 
 class VdQg1lSchedule(ctypes.Structure):
     _fields_ = [(k, ctypes.c_int) for k in ("engine", "tc_group_fwd", "tc_group_inv", "fma_rows", "tridiag_rows",
-                                             "tridiag_lean")]
+                                             "tridiag_lean", "stencil_loads")]
 
 
 class VdBmauxParams(ctypes.Structure):

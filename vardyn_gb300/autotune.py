@@ -45,6 +45,12 @@ def candidates(plan):
     return out
 
 
+def _inv_keys(plan):
+    """The schedule fields the tuner sets (the inversion's); the others keep
+    their values."""
+    return tuple(k for k in plan.SCHEDULE_KEYS if k != "stencil_loads")
+
+
 def _key(plan, batch):
     dev = plan.device
     return (torch.cuda.get_device_name(dev), plan.ny, plan.nx, str(plan.dtype), plan.dst_engine, int(batch))
@@ -69,7 +75,7 @@ def tune(plan, batch, reps=10, verbose=False):
     with _lock:
         hit = _cache.get(key)
     if hit is not None:
-        plan.set_schedule(**{k: 0 for k in plan.SCHEDULE_KEYS})
+        plan.set_schedule(**{k: 0 for k in _inv_keys(plan)})
         plan.set_schedule(**hit[0])
         return hit
     if torch.cuda.is_current_stream_capturing():
@@ -83,7 +89,7 @@ def tune(plan, batch, reps=10, verbose=False):
     best, best_ms = None, float("inf")
     for i, cand in enumerate(candidates(plan)):
         try:
-            plan.set_schedule(**{k: 0 for k in plan.SCHEDULE_KEYS})
+            plan.set_schedule(**{k: 0 for k in _inv_keys(plan)})
             plan.set_schedule(**cand)
         except RuntimeError:
             continue                           # a choice this plan cannot run
@@ -93,7 +99,7 @@ def tune(plan, batch, reps=10, verbose=False):
             print(f"  {plan.ny}x{plan.nx} b{batch} {cand or 'rule'}: {ms * 1e3:.1f} us")
         if ms < best_ms:
             best, best_ms = cand, ms
-    plan.set_schedule(**{k: 0 for k in plan.SCHEDULE_KEYS})
+    plan.set_schedule(**{k: 0 for k in _inv_keys(plan)})
     if best is None:
         plan.set_schedule(**saved)
         return saved, times

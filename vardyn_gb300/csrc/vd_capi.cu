@@ -231,6 +231,7 @@ extern "C" vd_status vd_qg1l_set_schedule(vd_qg1l_plan* p, const vd_qg1l_schedul
     if (s->tridiag_rows != 0 && s->tridiag_rows != 16 && s->tridiag_rows != 32) return VD_ERR_ARG;
     if (s->tridiag_lean != 0 && s->tridiag_lean != 1) return VD_ERR_ARG;
     if (s->tridiag_lean == 1 && p->d.dtype != VD_F32) return VD_ERR_UNSUPPORTED;
+    if (s->stencil_loads != 0 && s->stencil_loads != 1) return VD_ERR_ARG;
     if (s->engine == 2 && !p->dst.tc) return VD_ERR_UNSUPPORTED;
     if (s->fma_rows) {
         const size_t es = elem_size(p->d.dtype);

@@ -220,27 +220,25 @@ dst_gemm_kernel(GemmGeom g, const T* __restrict__ W1, const T* __restrict__ W2,
     }
 }
 
-// Chunked Thomas algorithm: 32 spectral columns per CTA (one per lane), the
-// column block staged in shared memory, warp w owning rows [32w, 32w+32).
-// Both sweeps are first-order linear recurrences with the multiplier
-// alpha_j = -a*m_j:  forward d_j = m_j F_j + alpha_j d_{j-1},
-// backward x_j = d_j + alpha_j x_{j+1}. Each warp runs its piece from a zero
-// carry while accumulating the product of its alphas, one warp chains the
-// piece-end values (at most 32 steps), and each warp adds carry * partial
-// product to its rows. |alpha| < 1 (diagonal dominance), so the products
-// only shrink.
+// Chunked Thomas algorithm. Both sweeps are first-order linear recurrences
+// with the multiplier alpha_j = -a*m_j: forward d_j = m_j F_j + alpha_j
+// d_{j-1}, backward x_j = d_j + alpha_j x_{j+1}. A row piece runs from a zero
+// carry while accumulating the product of its alphas; the true values follow
+// by adding carry * partial product. |alpha| < 1 (diagonal dominance), so
+// the products only shrink.
 // CW spectral columns per CTA; the warp's lanes are CW columns x (32/CW)
 // row pieces, so a CTA holds nw*(32/CW) pieces of CH rows per column. Each
 // thread keeps its piece (values and multipliers) in registers and runs both
 // Thomas sweeps locally (the recurrences are affine, so a piece is summarised
-// by its end value and the product of its multipliers); CW threads then chain
-// the pieces of their column through shared memory and every piece applies
-// the carry it receives. Eight columns per CTA: 1024 CTAs for 16 fields of
-// 512^2, 128 for one 1024^2 field.
+// by its end value and the product of its multipliers). The pieces of a
+// column are then combined by a scan of the affine maps (d, P) o (d', P') =
+// (d + P d', P P'): a shuffle scan over the warp's 32/CW pieces, then the
+// warp totals through shared memory; every piece applies the carry it
+// receives. Eight columns per CTA: 1024 CTAs for 16 fields of 512^2, 128 for
+// one 1024^2 field.
 // LEAN caps the registers at 80 (16-row pieces in float32 otherwise take
-// ~124): three 256-thread CTAs fit an SM instead of two, which hides the
-// barrier of the carry chain better at some shapes (a schedule choice, picked
-// by timing).
+// ~124): three 256-thread CTAs fit an SM instead of two (a schedule choice,
+// picked by timing).
 template <typename T, int CW, int CH, bool LEAN = false>
 __global__ void __maxnreg__(LEAN ? 80 : 128)
 tridiag_chunked_kernel(T* __restrict__ spec, const T* __restrict__ trim, int my, int n, int lds, T a)
@@ -248,14 +246,13 @@ tridiag_chunked_kernel(T* __restrict__ spec, const T* __restrict__ trim, int my,
     constexpr int SUB = 32 / CW;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int nw = blockDim.y;
-    const int NP = nw * SUB;
-    T* cD = reinterpret_cast<T*>(smem_raw);         // [NP][CW] piece-end values / carries
-    T* cP = cD + (size_t)NP * CW;                   // [NP][CW] piece products
+    T* wD = reinterpret_cast<T*>(smem_raw);         // [nw][CW] warp totals: end value
+    T* wP = wD + (size_t)nw * CW;                   // [nw][CW] warp totals: product
     const int f = blockIdx.y;
     const int lane = threadIdx.x, w = threadIdx.y;
-    const int tid = w * 32 + lane;
     const int c = lane % CW;
-    const int pc = w * SUB + lane / CW;
+    const int sp = lane / CW;                       // piece within the warp
+    const int pc = w * SUB + sp;
     const int t = blockIdx.x * CW + c;
     const bool col_ok = t < n;
     T* S = spec + (long long)f * my * lds + t;
@@ -282,29 +279,42 @@ tridiag_chunked_kernel(T* __restrict__ spec, const T* __restrict__ trim, int my,
             P *= al[i];
         }
     }
-    cD[pc * CW + c] = d;
-    cP[pc * CW + c] = P;
-    __syncthreads();
-    if (tid < CW) {
-        T cr = T(0);
-        for (int q = 0; q < NP; ++q) {
-            cr = cD[q * CW + tid] + cP[q * CW + tid] * cr;
-            cD[q * CW + tid] = cr;
-        }
-    }
-    __syncthreads();
-    if (pc > 0) {
-        const T cin = cD[(pc - 1) * CW + c];
-        T pr = T(1);
+    {
+        // inclusive scan over the pieces of the warp (lanes CW apart)
+        T sd = d, sP = P;
 #pragma unroll
-        for (int i = 0; i < CH; ++i) {
-            if (i < cnt) {
-                pr *= al[i];
-                x[i] += pr * cin;
+        for (int o = 1; o < SUB; o <<= 1) {
+            const T od = __shfl_up_sync(0xffffffffu, sd, o * CW);
+            const T oP = __shfl_up_sync(0xffffffffu, sP, o * CW);
+            if (sp >= o) {
+                sd = sd + sP * od;
+                sP = sP * oP;
+            }
+        }
+        if (sp == SUB - 1) {
+            wD[w * CW + c] = sd;
+            wP[w * CW + c] = sP;
+        }
+        __syncthreads();
+        // carry into this warp: the warps before it, in order
+        T cw = T(0);
+        for (int v = 0; v < w; ++v) cw = wD[v * CW + c] + wP[v * CW + c] * cw;
+        // end value of the previous piece
+        const T pd = __shfl_up_sync(0xffffffffu, sd, CW);
+        const T pP = __shfl_up_sync(0xffffffffu, sP, CW);
+        const T cin = sp == 0 ? cw : pd + pP * cw;
+        if (pc > 0) {
+            T pr = T(1);
+#pragma unroll
+            for (int i = 0; i < CH; ++i) {
+                if (i < cnt) {
+                    pr *= al[i];
+                    x[i] += pr * cin;
+                }
             }
         }
     }
-    __syncthreads();
+    __syncthreads();   // the warp totals are read before they are rewritten
 
     // backward sweep, piece-local from the piece end: x_j = d_j + (-a m_j) x_{j+1}
     T xr = T(0);
@@ -317,25 +327,36 @@ tridiag_chunked_kernel(T* __restrict__ spec, const T* __restrict__ trim, int my,
             P *= al[i];
         }
     }
-    cD[pc * CW + c] = xr;
-    cP[pc * CW + c] = P;
-    __syncthreads();
-    if (tid < CW) {
-        T cr = T(0);
-        for (int q = NP - 1; q >= 0; --q) {
-            cr = cD[q * CW + tid] + cP[q * CW + tid] * cr;
-            cD[q * CW + tid] = cr;
-        }
-    }
-    __syncthreads();
-    if (pc < NP - 1) {
-        const T cin = cD[(pc + 1) * CW + c];
-        T pr = T(1);
+    {
+        // inclusive scan from the last piece of the warp down to the first
+        T sd = xr, sP = P;
 #pragma unroll
-        for (int i = CH - 1; i >= 0; --i) {
-            if (i < cnt) {
-                pr *= al[i];
-                x[i] += pr * cin;
+        for (int o = 1; o < SUB; o <<= 1) {
+            const T od = __shfl_down_sync(0xffffffffu, sd, o * CW);
+            const T oP = __shfl_down_sync(0xffffffffu, sP, o * CW);
+            if (sp + o < SUB) {
+                sd = sd + sP * od;
+                sP = sP * oP;
+            }
+        }
+        if (sp == 0) {
+            wD[w * CW + c] = sd;
+            wP[w * CW + c] = sP;
+        }
+        __syncthreads();
+        T cw = T(0);
+        for (int v = nw - 1; v > w; --v) cw = wD[v * CW + c] + wP[v * CW + c] * cw;
+        const T nd = __shfl_down_sync(0xffffffffu, sd, CW);
+        const T nP = __shfl_down_sync(0xffffffffu, sP, CW);
+        const T cin = sp == SUB - 1 ? cw : nd + nP * cw;
+        if (pc < nw * SUB - 1) {
+            T pr = T(1);
+#pragma unroll
+            for (int i = CH - 1; i >= 0; --i) {
+                if (i < cnt) {
+                    pr *= al[i];
+                    x[i] += pr * cin;
+                }
             }
         }
     }
@@ -727,13 +748,13 @@ static int launch_tridiag(const vd_qg1l_plan* p, int nf, T* spec, cudaStream_t s
     const int nw32 = ((t.my + 31) / 32 + SUB - 1) / SUB;
     const bool want32 = p->sched.tridiag_rows == 32 && nw32 <= 16;
     if (nw16 <= 16 && !want32 && p->sched.tridiag_lean == 1 && sizeof(T) == 4) {
-        tridiag_chunked_kernel<T, CW, 16, true><<<grid, dim3(32, nw16), 2 * nw16 * SUB * CW * sizeof(T), st>>>(
+        tridiag_chunked_kernel<T, CW, 16, true><<<grid, dim3(32, nw16), 2 * nw16 * CW * sizeof(T), st>>>(
             spec, (const T*)t.trim, t.my, t.n, t.lds, a);
     } else if (nw16 <= 16 && !want32) {
-        tridiag_chunked_kernel<T, CW, 16><<<grid, dim3(32, nw16), 2 * nw16 * SUB * CW * sizeof(T), st>>>(
+        tridiag_chunked_kernel<T, CW, 16><<<grid, dim3(32, nw16), 2 * nw16 * CW * sizeof(T), st>>>(
             spec, (const T*)t.trim, t.my, t.n, t.lds, a);
     } else if (nw32 <= 16) {
-        tridiag_chunked_kernel<T, CW, 32><<<grid, dim3(32, nw32), 2 * nw32 * SUB * CW * sizeof(T), st>>>(
+        tridiag_chunked_kernel<T, CW, 32><<<grid, dim3(32, nw32), 2 * nw32 * CW * sizeof(T), st>>>(
             spec, (const T*)t.trim, t.my, t.n, t.lds, a);
     } else {
         tridiag_global_kernel<T><<<dim3((t.n + 31) / 32, nf), 32, 0, st>>>(spec, (const T*)t.trim, t.my, t.n,

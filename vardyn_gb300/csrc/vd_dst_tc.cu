@@ -761,5 +761,5 @@ extern "C" vd_status vd_device_error(int* flags, int reset)
         const int zero = 0;
         VD_CUDA_TRY(cudaMemcpyToSymbol(vd::g_tc_error, &zero, sizeof(int)));
     }
-    return VD_OK;
+    return (vd_status)vd::qg_tile_error(flags, reset);
 }

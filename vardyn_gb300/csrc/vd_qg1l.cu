@@ -14,6 +14,9 @@
 // tendency unless the caller's SSH holds NaN away from the land of the mask;
 // the adjoint kernels rely on this and omit the u, v guard.
 #include "vd_internal.cuh"
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cstring>
 #include <mutex>
 
 namespace vd {
@@ -402,20 +405,58 @@ __global__ void k_stage_tl(QGGeom G, int B, const T* __restrict__ hs, const T* _
 // quantities never leave shared memory, and phase A stores lk times the split
 // T-point velocities (lk u+, lk u-, lk v+, lk v-) so phase B's upwind
 // transpose reads them without re-splitting.
+//
+// Two forms of staging. With grids whose rows are a multiple of 16 elements
+// (and 16-byte aligned fields), one thread issues bulk tensor copies
+// (cp.async.bulk.tensor, TMA) of the h and q tiles, q + bathymetry, the stage
+// adjoints G_t, beta and the mask over the tile and its halos; the copies
+// fill out-of-grid cells with zeros, so the threads run no index arithmetic,
+// bounds checks or global loads for them. Otherwise the threads load the same
+// tiles with bounds-checked loads. Tile x origins are i0 - 4 (fields) and
+// i0 - 16 (the int8 mask), multiples of 16 bytes as a tiled copy requires.
 // ---------------------------------------------------------------------------
 constexpr int AT_Y = 32, AT_X = 32;                 // output tile
-constexpr int AH_Y = AT_Y + 6, AH_X = AT_X + 6;     // h tile (halo 3)
-constexpr int AQ_Y = AT_Y + 8, AQ_X = AT_X + 8;     // q tile (halo 4)
-constexpr int AA_Y = AT_Y + 4, AA_X = AT_X + 4;     // phase-A region (halo 2)
+constexpr int AH_Y = AT_Y + 6, AH_X = AT_X + 8;     // h tile: rows j0-3.., columns i0-4..
+constexpr int AQ_Y = AT_Y + 8, AQ_X = AT_X + 8;     // q tile: rows j0-4.., columns i0-4..
+constexpr int AA_Y = AT_Y + 4, AA_X = AT_X + 4;     // phase-A region: rows j0-2.., columns i0-2..
+constexpr int AG_Y = AA_Y, AG_X = AT_X + 8;         // G_t / beta tiles: rows j0-2.., columns i0-4..
+constexpr int AM_Y = AA_Y, AM_X = AT_X + 32;        // mask tile (bytes): rows j0-2.., columns i0-16..
 
-template <typename T>
-static size_t adj_bytes(const vd_qg1l_plan* p);
+// Tensor maps of the staged tiles (fields [nf][ny][nx]; beta, bathymetry and
+// mask [ny][nx]).
+struct AdjMaps {
+    CUtensorMap h, q, g[4], beta, fB, mask;
+};
 
-// Shared layout of one CTA: h tile, q tile, the upwind products of the
-// stage-increment adjoint lk with the split T-point velocities (lk u+, lk u-,
-// lk v+, lk v-: phase B reads them directly), the velocity adjoints aut, avt;
-// then, only when present, lk itself (the diffusion transpose) and q + f *
-// bathymetry.
+// Byte offsets of one CTA's shared regions (each 128-byte aligned, as tensor
+// copies into shared memory require): h tile, q tile, q + bathymetry (only
+// with a bathymetry term), the phase-A outputs (lk u+, lk u-, lk v+, lk v-,
+// aut, avt, and lk with diffusion) which the staged G_t and beta tiles alias
+// (they are read into registers before phase A writes), and the mask tile.
+struct AdjLayout {
+    uint32_t h, q, qa, out, beta, mask, total;
+};
+
+__host__ __device__ inline uint32_t adj_al(uint32_t x) { return (x + 127u) & ~127u; }
+
+__host__ __device__ inline AdjLayout adj_layout(int esz, bool hasK, bool hasB, bool tma, int ng, bool hasBeta)
+{
+    AdjLayout L;
+    uint32_t o = 0;
+    L.h = o; o = adj_al(o + (uint32_t)(AH_Y * AH_X * esz));
+    L.q = o; o = adj_al(o + (uint32_t)(AQ_Y * AQ_X * esz));
+    L.qa = o; if (hasB) o = adj_al(o + (uint32_t)(AQ_Y * AQ_X * esz));
+    L.out = o;
+    const uint32_t nout = (uint32_t)((6 + (hasK ? 1 : 0)) * AA_Y * AA_X * esz);
+    const uint32_t gtile = adj_al((uint32_t)(AG_Y * AG_X * esz));
+    L.beta = o + (uint32_t)ng * gtile;
+    const uint32_t nin = tma ? (uint32_t)ng * gtile + (hasBeta ? gtile : 0u) : 0u;
+    o = adj_al(o + (nout > nin ? nout : nin));
+    L.mask = o; if (tma) o = adj_al(o + (uint32_t)(AM_Y * AM_X));
+    L.total = o;
+    return L;
+}
+
 template <typename T>
 struct AdjSmem {
     T (*h)[AH_X];
@@ -430,21 +471,14 @@ struct AdjSmem {
     T (*qa)[AQ_X];           // only with a bathymetry term
 };
 
-__host__ __device__ constexpr size_t adj_smem_elems(bool hasK, bool hasB)
-{
-    return (size_t)AH_Y * AH_X + (size_t)AQ_Y * AQ_X + 6 * (size_t)AA_Y * AA_X + (hasK ? (size_t)AA_Y * AA_X : 0) +
-           (hasB ? (size_t)AQ_Y * AQ_X : 0);
-}
-
 template <typename T>
-__device__ __forceinline__ AdjSmem<T> adj_smem(unsigned char* raw, bool hasK, bool hasB)
+__device__ __forceinline__ AdjSmem<T> adj_smem(unsigned char* raw, const AdjLayout& L, bool hasK, bool hasB)
 {
-    T* b = reinterpret_cast<T*>(raw);
     AdjSmem<T> S;
-    S.h = reinterpret_cast<T(*)[AH_X]>(b);
-    b += AH_Y * AH_X;
-    S.q = reinterpret_cast<T(*)[AQ_X]>(b);
-    b += AQ_Y * AQ_X;
+    S.h = reinterpret_cast<T(*)[AH_X]>(raw + L.h);
+    S.q = reinterpret_cast<T(*)[AQ_X]>(raw + L.q);
+    S.qa = hasB ? reinterpret_cast<T(*)[AQ_X]>(raw + L.qa) : nullptr;
+    T* b = reinterpret_cast<T*>(raw + L.out);
     S.lup = reinterpret_cast<T(*)[AA_X]>(b); b += AA_Y * AA_X;
     S.lum = reinterpret_cast<T(*)[AA_X]>(b); b += AA_Y * AA_X;
     S.lvp = reinterpret_cast<T(*)[AA_X]>(b); b += AA_Y * AA_X;
@@ -452,39 +486,134 @@ __device__ __forceinline__ AdjSmem<T> adj_smem(unsigned char* raw, bool hasK, bo
     S.aut = reinterpret_cast<T(*)[AA_X]>(b); b += AA_Y * AA_X;
     S.avt = reinterpret_cast<T(*)[AA_X]>(b); b += AA_Y * AA_X;
     S.lk = hasK ? reinterpret_cast<T(*)[AA_X]>(b) : nullptr;
-    if (hasK) b += AA_Y * AA_X;
-    S.qa = hasB ? reinterpret_cast<T(*)[AQ_X]>(b) : nullptr;
     return S;
 }
 
-template <typename T>
-static size_t adj_bytes(const vd_qg1l_plan* p)
+__device__ int g_qg_tile_error = 0;
+
+__device__ __forceinline__ uint64_t qg_gtimer()
 {
-    return adj_smem_elems(p->geom.hasK != 0, p->geom.fB != nullptr) * sizeof(T);
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
 }
 
-template <typename T>
+__device__ __forceinline__ bool qg_mbar_try(uint32_t bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Wait for phase 0 of `bar`, at most `ns` nanoseconds of %globaltimer.
+__device__ __forceinline__ bool qg_mbar_wait(uint32_t bar, uint64_t ns)
+{
+    if (qg_mbar_try(bar, 0)) return true;
+    const uint64_t t0 = qg_gtimer();
+    while (!qg_mbar_try(bar, 0))
+        if (qg_gtimer() - t0 > ns) return false;
+    return true;
+}
+
+__device__ __forceinline__ void tma_tile_3d(uint32_t dst, const CUtensorMap* map, int x, int y, int z, uint32_t bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_tile_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+        "[%4];" ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+template <typename T, bool TMA>
 __global__ void __launch_bounds__(256)
 k_adj_stage_fused(QGGeom G, int nf, const T* __restrict__ hs, const T* __restrict__ qs, StageIn<T> gin,
-                  StageIn<T> gacc, T* __restrict__ adq_out, T* __restrict__ adh_out)
+                  StageIn<T> gacc, T* __restrict__ adq_out, T* __restrict__ adh_out, const __grid_constant__ AdjMaps M)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ unsigned char smem_dyn[];
+    __shared__ __align__(8) uint64_t tbar;
+    unsigned char* smem_raw = (unsigned char*)(((uintptr_t)smem_dyn + 127) & ~(uintptr_t)127);
     const bool hasB = G.fB != nullptr;
     const bool hasK = G.hasK != 0;
-    const AdjSmem<T> S = adj_smem<T>(smem_raw, hasK, hasB);
+    const bool hasBeta = G.beta != nullptr;
+    const AdjLayout L = adj_layout((int)sizeof(T), hasK, hasB, TMA, gin.nk, hasBeta);
+    const AdjSmem<T> S = adj_smem<T>(smem_raw, L, hasK, hasB);
     const int f = blockIdx.z;
     const int j0 = blockIdx.y * AT_Y, i0 = blockIdx.x * AT_X;
     const int tid = threadIdx.y * 32 + threadIdx.x;
     const long long fo = f * G.fs;
-    // ---- stage h and q: every load of the thread issued before any store ----
-    {
+    constexpr int NAL = (AA_Y * AA_X + 255) / 256;
+    T lkv[NAL], bev[NAL];
+    bool m3a[NAL];
+    if constexpr (TMA) {
+        // ---- bulk tensor copies of every staged tile, one mbarrier ----
+        const uint32_t sb = (uint32_t)__cvta_generic_to_shared(smem_raw);
+        const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&tbar);
+        const uint32_t gtile = adj_al((uint32_t)(AG_Y * AG_X * sizeof(T)));
+        if (tid == 0) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            const uint32_t bytes = (uint32_t)sizeof(T) * (AH_Y * AH_X + AQ_Y * AQ_X + (hasB ? AQ_Y * AQ_X : 0) +
+                                                          (gin.nk + (hasBeta ? 1 : 0)) * AG_Y * AG_X) +
+                                   AM_Y * AM_X;
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+            tma_tile_3d(sb + L.h, &M.h, i0 - 4, j0 - 3, f, bar);
+            tma_tile_3d(sb + L.q, &M.q, i0 - 4, j0 - 4, f, bar);
+            if (hasB) tma_tile_2d(sb + L.qa, &M.fB, i0 - 4, j0 - 4, bar);
+            for (int t = 0; t < gin.nk; ++t) tma_tile_3d(sb + L.out + t * gtile, &M.g[t], i0 - 4, j0 - 2, f, bar);
+            if (hasBeta) tma_tile_2d(sb + L.beta, &M.beta, i0 - 4, j0 - 2, bar);
+            tma_tile_2d(sb + L.mask, &M.mask, i0 - 16, j0 - 2, bar);
+        }
+        __syncthreads();   // the barrier is initialised before anyone polls it
+        const bool ok = qg_mbar_wait(bar, 2000000000ull);
+        if (!__syncthreads_and(ok)) {
+            // copies that did not arrive in 2 s: flag it, give them another
+            // bounded interval to land in this CTA's shared memory, and leave
+            if (tid == 0) {
+                atomicOr(&g_qg_tile_error, 8);
+                qg_mbar_wait(bar, 2000000000ull);
+            }
+            return;
+        }
+        if (hasB)
+            for (int e = tid; e < AQ_Y * AQ_X; e += 256) (&S.qa[0][0])[e] += (&S.q[0][0])[e];
+        const int8_t* mk = reinterpret_cast<const int8_t*>(smem_raw + L.mask);
+        const T* bt = reinterpret_cast<const T*>(smem_raw + L.beta);
+#pragma unroll
+        for (int k = 0; k < NAL; ++k) {
+            const int e = tid + 256 * k;
+            const int a = e / AA_X, b = e - a * AA_X;
+            const bool in = e < AA_Y * AA_X;
+            T lk = T(0);
+#pragma unroll
+            for (int t = 0; t < 4; ++t)
+                if (t < gin.nk && in)
+                    lk += gin.c[t] * reinterpret_cast<const T*>(smem_raw + L.out + t * gtile)[a * AG_X + b + 2];
+            lkv[k] = lk;
+            m3a[k] = in && mk[a * AM_X + b + 14] == 3;
+            bev[k] = (in && hasBeta) ? bt[a * AG_X + b + 2] : T(0);
+        }
+    } else {
+        // ---- bounds-checked loads: every load of the thread before any store ----
         constexpr int NHL = (AH_Y * AH_X + 255) / 256, NQL = (AQ_Y * AQ_X + 255) / 256;
         T hv[NHL], qv[NQL];
 #pragma unroll
         for (int k = 0; k < NHL; ++k) {
             const int e = tid + 256 * k;
             const int a = e / AH_X, b = e - a * AH_X;
-            const int j = j0 - 3 + a, i = i0 - 3 + b;
+            const int j = j0 - 3 + a, i = i0 - 4 + b;
             hv[k] = (e < AH_Y * AH_X && j >= 0 && j < G.ny && i >= 0 && i < G.nx) ? hs[fo + (long long)j * G.nx + i]
                                                                                   : T(0);
         }
@@ -514,26 +643,23 @@ k_adj_stage_fused(QGGeom G, int nf, const T* __restrict__ hs, const T* __restric
                 S.qa[a][b] = S.q[a][b] + (in ? ((const T*)G.fB)[(long long)j * G.nx + i] : T(0));
             }
         }
-    }
-    // ---- per-point inputs of phase A (tendency adjoint, interior flag, beta) ----
-    constexpr int NAL = (AA_Y * AA_X + 255) / 256;
-    T lkv[NAL], bev[NAL];
-    bool m3a[NAL];
+        // per-point inputs of phase A (tendency adjoint, interior flag, beta)
 #pragma unroll
-    for (int k = 0; k < NAL; ++k) {
-        const int e = tid + 256 * k;
-        const int a = e / AA_X, b = e - a * AA_X;
-        const int j = j0 - 2 + a, i = i0 - 2 + b;
-        const bool in = e < AA_Y * AA_X && j >= 0 && j < G.ny && i >= 0 && i < G.nx;
-        const long long g2 = (long long)j * G.nx + i;
-        const long long o = fo + g2;
-        T lk = T(0);
+        for (int k = 0; k < NAL; ++k) {
+            const int e = tid + 256 * k;
+            const int a = e / AA_X, b = e - a * AA_X;
+            const int j = j0 - 2 + a, i = i0 - 2 + b;
+            const bool in = e < AA_Y * AA_X && j >= 0 && j < G.ny && i >= 0 && i < G.nx;
+            const long long g2 = (long long)j * G.nx + i;
+            const long long o = fo + g2;
+            T lk = T(0);
 #pragma unroll
-        for (int t = 0; t < 4; ++t)
-            if (t < gin.nk && in) lk += gin.c[t] * gin.k[t][o];
-        lkv[k] = lk;
-        m3a[k] = in && G.mask[g2] == 3;
-        bev[k] = (in && G.beta) ? ((const T*)G.beta)[g2] : T(0);
+            for (int t = 0; t < 4; ++t)
+                if (t < gin.nk && in) lk += gin.c[t] * gin.k[t][o];
+            lkv[k] = lk;
+            m3a[k] = in && G.mask[g2] == 3;
+            bev[k] = (in && G.beta) ? ((const T*)G.beta)[g2] : T(0);
+        }
     }
     __syncthreads();
     // ---- phase A on the tile + halo 2 ----
@@ -546,7 +672,7 @@ k_adj_stage_fused(QGGeom G, int nf, const T* __restrict__ hs, const T* __restric
         T lk = T(0), uT = T(0), vT = T(0), aut = T(0), avt = T(0);
         if (m3a[k]) {
             lk = lkv[k];
-            const int ha = a + 1, hb = b + 1;     // h-tile index of P
+            const int ha = a + 1, hb = b + 2;     // h-tile index of P
             Vel<T> V;
             V.u0 = guard0(cu * (S.h[ha + 1][hb - 1] + S.h[ha + 1][hb] - S.h[ha - 1][hb] - S.h[ha - 1][hb - 1]));
             V.u1 = guard0(cu * (S.h[ha + 1][hb] + S.h[ha + 1][hb + 1] - S.h[ha - 1][hb + 1] - S.h[ha - 1][hb]));
@@ -599,7 +725,10 @@ k_adj_stage_fused(QGGeom G, int nf, const T* __restrict__ hs, const T* __restric
         for (int t = 0; t < 4; ++t)
             if (t < gacc.nk && in) sacc += gacc.k[t][o];
         accv[k] = sacc;
-        m3b[k] = in && G.mask[(long long)j * G.nx + i] == 3;
+        if constexpr (TMA)
+            m3b[k] = in && reinterpret_cast<const int8_t*>(smem_raw + L.mask)[(a + 2) * AM_X + b + 16] == 3;
+        else
+            m3b[k] = in && G.mask[(long long)j * G.nx + i] == 3;
     }
 #pragma unroll
     for (int k = 0; k < NBL; ++k) {
@@ -633,6 +762,113 @@ k_adj_stage_fused(QGGeom G, int nf, const T* __restrict__ hs, const T* __restric
                    + hv * (S.avt[A - 1][Bc - 1] + T(2) * S.avt[A][Bc - 1] + S.avt[A + 1][Bc - 1]
                            - S.avt[A - 1][Bc + 1] - T(2) * S.avt[A][Bc + 1] - S.avt[A + 1][Bc + 1]);
     }
+}
+
+// ---- host side of the adjoint stage ----------------------------------------
+
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+    static std::once_flag once;
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    std::call_once(once, []() {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        else
+            (void)cudaGetLastError();
+    });
+    return fn;
+}
+
+// A tiled map over [nz][ny][nx] elements of `esz` bytes (rank 3, fields z
+// apart) or [ny][nx] (rank 2), box bx x by (x 1). False when the driver
+// refuses it.
+static bool tile_map(CUtensorMap* m, const void* base, int esz, int nx, int ny, int nz, long long zstride, int bx,
+                     int by, int rank)
+{
+    auto enc = tensor_map_encoder();
+    if (!enc || !base || ((uintptr_t)base & 15)) return false;
+    const CUtensorMapDataType dt = esz == 8   ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64
+                                   : esz == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                              : CU_TENSOR_MAP_DATA_TYPE_UINT8;
+    const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
+    const cuuint64_t strides[2] = {(cuuint64_t)nx * esz, (cuuint64_t)zstride * esz};
+    const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1};
+    const cuuint32_t es[3] = {1, 1, 1};
+    return enc(m, dt, (cuuint32_t)rank, const_cast<void*>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// The staged form needs rows of a multiple of 16 elements (16-byte row
+// strides of the int8 mask and of every field, 16-byte aligned field bases).
+template <typename T>
+static bool adj_tma_maps(const vd_qg1l_plan* p, int nf, const T* hs, const T* qs, const StageIn<T>& gin,
+                         AdjMaps& M)
+{
+    const QGGeom& G = p->geom;
+    if (p->sched.stencil_loads == 1 || G.nx % 16 != 0 || G.fs % 16 != 0) return false;
+    // the field maps span the nf fields of this launch (z = field)
+    auto fmap = [&](CUtensorMap* m, const T* base, int by) {
+        return tile_map(m, base, sizeof(T), G.nx, G.ny, nf, G.fs, AG_X, by, 3);
+    };
+    if (!fmap(&M.h, hs, AH_Y) || !fmap(&M.q, qs, AQ_Y)) return false;
+    for (int t = 0; t < gin.nk; ++t)
+        if (!fmap(&M.g[t], gin.k[t], AG_Y)) return false;
+    if (G.beta && !tile_map(&M.beta, G.beta, sizeof(T), G.nx, G.ny, 1, G.fs, AG_X, AG_Y, 2)) return false;
+    if (G.fB && !tile_map(&M.fB, G.fB, sizeof(T), G.nx, G.ny, 1, G.fs, AQ_X, AQ_Y, 2)) return false;
+    return tile_map(&M.mask, G.mask, 1, G.nx, G.ny, 1, G.fs, AM_X, AM_Y, 2);
+}
+
+template <typename T>
+static cudaError_t adj_stage_attrs()
+{
+    static PerDeviceOnce once;
+    return once.run([]() -> cudaError_t {
+        const int big = (int)adj_layout(sizeof(T), true, true, true, 4, true).total + 128;
+        cudaError_t e = cudaFuncSetAttribute(k_adj_stage_fused<T, true>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+        if (!e)
+            e = cudaFuncSetAttribute(k_adj_stage_fused<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+        return e;
+    });
+}
+
+// One adjoint stage over nf fields: the staged (TMA) form when the grid
+// allows it, the bounds-checked form otherwise.
+template <typename T>
+static int launch_adj_stage(const vd_qg1l_plan* p, int nf, const T* hs, const T* qs, const StageIn<T>& gin,
+                            const StageIn<T>& gacc, T* adq_out, T* adh_out, cudaStream_t st)
+{
+    if (adj_stage_attrs<T>() != cudaSuccess) return VD_ERR_CUDA;
+    const QGGeom& G = p->geom;
+    const dim3 agrid((p->d.nx + AT_X - 1) / AT_X, (p->d.ny + AT_Y - 1) / AT_Y, nf);
+    const dim3 block(32, 8);
+    AdjMaps M;
+    std::memset(&M, 0, sizeof(M));
+    const bool tma = adj_tma_maps<T>(p, nf, hs, qs, gin, M);
+    const size_t smem = adj_layout(sizeof(T), G.hasK != 0, G.fB != nullptr, tma, gin.nk, G.beta != nullptr).total + 128;
+    if (tma)
+        k_adj_stage_fused<T, true><<<agrid, block, smem, st>>>(G, nf, hs, qs, gin, gacc, adq_out, adh_out, M);
+    else
+        k_adj_stage_fused<T, false><<<agrid, block, smem, st>>>(G, nf, hs, qs, gin, gacc, adq_out, adh_out, M);
+    VD_LAUNCH_CHECK();
+    return VD_OK;
+}
+
+int qg_tile_error(int* flags, int reset)
+{
+    int v = 0;
+    if (cudaMemcpyFromSymbol(&v, g_qg_tile_error, sizeof(int)) != cudaSuccess) return VD_ERR_CUDA;
+    *flags |= v;
+    if (reset) {
+        const int zero = 0;
+        if (cudaMemcpyToSymbol(g_qg_tile_error, &zero, sizeof(int)) != cudaSuccess) return VD_ERR_CUDA;
+    }
+    return VD_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -878,16 +1114,6 @@ int advance_adj_impl(const vd_qg1l_plan* p, int nf, const T* traj, int traj_step
     T* adhs = (T*)ws.take(fb * sizeof(T));
     T* spec = (T*)ws.take(spec_bytes(p, nf));
     if (!adql || !adhs || !spec) return VD_ERR_WORKSPACE;
-    static PerDeviceOnce attr_once;
-    const cudaError_t attr_err = attr_once.run([]() -> cudaError_t {
-        cudaError_t e = cudaFuncSetAttribute(k_adj_stage_fused<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)(adj_smem_elems(true, true) * sizeof(float)));
-        if (!e)
-            e = cudaFuncSetAttribute(k_adj_stage_fused<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)(adj_smem_elems(true, true) * sizeof(double)));
-        return e;
-    });
-    if (attr_err != cudaSuccess) return VD_ERR_CUDA;
 
     for (int n = first + nstep - 1; n >= first; --n) {
         // adjoint of h_{n+1} = I(q_{n+1}): G0 = M3*(solve(adh) + adq)
@@ -902,13 +1128,11 @@ int advance_adj_impl(const vd_qg1l_plan* p, int nf, const T* traj, int traj_step
             if (p->b[s] != 0.0) { gin.k[gin.nk] = Gb[0]; gin.c[gin.nk] = (T)p->b[s]; ++gin.nk; }
             for (int t = s + 1; t < S; ++t)
                 if (p->A[t][s] != 0.0) { gin.k[gin.nk] = Gb[t]; gin.c[gin.nk] = (T)p->A[t][s]; ++gin.nk; }
-            const dim3 agrid((p->d.nx + AT_X - 1) / AT_X, (p->d.ny + AT_Y - 1) / AT_Y, nf);
             if (s >= 1) {
                 StageIn<T> none{};
                 none.nk = 0;
-                k_adj_stage_fused<T><<<agrid, kBlock, adj_bytes<T>(p), st>>>(p->geom, nf, tv.h(n, s),
-                                                                                 tv.q(n, s), gin, none, adql, adhs);
-                VD_LAUNCH_CHECK();
+                rc = launch_adj_stage<T>(p, nf, tv.h(n, s), tv.q(n, s), gin, none, adql, adhs, st);
+                if (rc) return rc;
                 SolveArgs a;
                 a.src = adhs; a.sub = nullptr; a.sub_batches = 0;
                 a.out = Gb[s]; a.add = adql; a.add_batches = nf; a.epi = EPI_ADJQ;
@@ -918,9 +1142,8 @@ int advance_adj_impl(const vd_qg1l_plan* p, int nf, const T* traj, int traj_step
                 StageIn<T> acc{};
                 acc.nk = 0;
                 for (int t = 0; t < S; ++t) { acc.k[acc.nk] = Gb[t]; acc.c[acc.nk] = T(1); ++acc.nk; }
-                k_adj_stage_fused<T><<<agrid, kBlock, adj_bytes<T>(p), st>>>(p->geom, nf, tv.h(n, s),
-                                                                                 tv.q(n, s), gin, acc, adq, adh);
-                VD_LAUNCH_CHECK();
+                rc = launch_adj_stage<T>(p, nf, tv.h(n, s), tv.q(n, s), gin, acc, adq, adh, st);
+                if (rc) return rc;
             }
         }
     }
@@ -947,26 +1170,12 @@ template <typename T>
 int rk_stage_adj_impl(const vd_qg1l_plan* p, int nf, const T* hs, const T* qs, int ng, const T* const* g,
                       const double* c, int nacc, const T* const* acc, T* adq_out, T* adh_out, cudaStream_t st)
 {
-    static PerDeviceOnce attr_once;
-    const cudaError_t attr_err = attr_once.run([]() -> cudaError_t {
-        cudaError_t e = cudaFuncSetAttribute(k_adj_stage_fused<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)(adj_smem_elems(true, true) * sizeof(float)));
-        if (!e)
-            e = cudaFuncSetAttribute(k_adj_stage_fused<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)(adj_smem_elems(true, true) * sizeof(double)));
-        return e;
-    });
-    if (attr_err != cudaSuccess) return VD_ERR_CUDA;
     StageIn<T> gin{}, gac{};
     gin.nk = ng;
     for (int t = 0; t < ng; ++t) { gin.k[t] = g[t]; gin.c[t] = (T)c[t]; }
     gac.nk = nacc;
     for (int t = 0; t < nacc; ++t) { gac.k[t] = acc[t]; gac.c[t] = T(1); }
-    const dim3 agrid((p->d.nx + AT_X - 1) / AT_X, (p->d.ny + AT_Y - 1) / AT_Y, nf);
-    k_adj_stage_fused<T><<<agrid, kBlock, adj_bytes<T>(p), st>>>(p->geom, nf, hs, qs, gin, gac, adq_out,
-                                                                     adh_out);
-    VD_LAUNCH_CHECK();
-    return VD_OK;
+    return launch_adj_stage<T>(p, nf, hs, qs, gin, gac, adq_out, adh_out, st);
 }
 
 template <typename T>

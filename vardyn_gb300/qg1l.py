@@ -132,7 +132,8 @@ class QG1LPlan:
         return self._h
 
     # ---------------- launch schedule of the inversion ----------------
-    SCHEDULE_KEYS = ("engine", "tc_group_fwd", "tc_group_inv", "fma_rows", "tridiag_rows", "tridiag_lean")
+    SCHEDULE_KEYS = ("engine", "tc_group_fwd", "tc_group_inv", "fma_rows", "tridiag_rows", "tridiag_lean",
+                     "stencil_loads")
 
     def schedule(self):
         """The inversion's launch schedule (vd_qg1l_schedule; 0 = built-in rule)."""
