@@ -905,8 +905,9 @@ const char* vd_version(void);
  * counts launches recorded into a CUDA graph during capture). */
 long long vd_launch_count(void);
 /* Device-side error bits set by bounded waits that ran out (1: stage
- * recycle, 2: operand arrival, 4: accumulator completion of the tensor-core
- * DST; 8: the staged tiles of the QG adjoint stage); 0 = none.
+ * recycle, 2: operand arrival, 4: accumulator completion, 16: the peer
+ * CTA's half tile of the inverse pass, of the tensor-core DST; 8: the staged
+ * tiles of the QG adjoint stage); 0 = none.
  * Synchronous; reset != 0 clears them. */
 vd_status vd_device_error(int* flags, int reset);
 

@@ -21,7 +21,9 @@
 //              pre-swizzled hi/lo chunks of the DST half matrix (fullB);
 //   warp 16    owns the TMEM allocation; its lane 0 issues 3 x 4 MMAs per
 //              chunk and commits to `empty` to recycle the stage;
-//   warps 0-15 finally read the accumulators (tcgen05.ld) and write rows.
+//   warps 0-15 finally read the accumulators (tcgen05.ld) and write rows;
+//              in the inverse pass the two CTAs of a cluster (odd-k and
+//              even-k sums) first swap half tiles with one bulk copy each.
 // Every mbarrier wait is bounded (2 s of %globaltimer); a timeout sets a bit
 // in a device flag (vd_device_error) and the CTA finishes without hanging.
 #include "vd_internal.cuh"
@@ -49,7 +51,11 @@ constexpr int TILE = 32;                           // columns of one B image til
 constexpr uint32_t TILE_BYTES = TILE * 32 * 4;     // 4 KB: 32 rows of the swizzled layout
 constexpr uint32_t A_TILE = BM * KCH * 4;          // 16 KB
 constexpr size_t PIPE_BYTES = 200 * 1024;          // pipeline stages fit in this
-constexpr size_t EPI_BYTES = (size_t)BM * 257 * 4; // epilogue staging tile (reuses the stages)
+constexpr int EPI_S = 257;                          // row pitch of the epilogue staging tile
+constexpr size_t EPI_BYTES = (size_t)BM * EPI_S * 4; // epilogue staging tile (reuses the stages)
+// inverse pass: half of the peer CTA's staging tile, received after ours
+constexpr uint32_t HALF_ROWS = BM / 2;
+constexpr uint32_t HALF_BYTES = HALF_ROWS * EPI_S * 4;
 constexpr size_t SMEM_MAX = PIPE_BYTES + 1024;      // largest dynamic request of any launch
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -86,13 +92,14 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
     return ok != 0;
 }
 // Bounded wait on the phase of parity `parity`.
+// The timer is read once every 64 polls.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int code)
 {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = gtimer();
-    while (true) {
+    for (uint32_t it = 1;; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
-        if (gtimer() - t0 > 2000000000ull) {
+        if ((it & 63u) == 0 && gtimer() - t0 > 2000000000ull) {
             atomicOr(&g_tc_error, code);
             return false;
         }
@@ -106,12 +113,6 @@ __device__ __forceinline__ uint32_t mapa_shared(uint32_t addr, uint32_t rank)
     asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
     return r;
 }
-__device__ __forceinline__ float ld_cluster_f32(uint32_t addr)
-{
-    float v;
-    asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(addr) : "memory");
-    return v;
-}
 // Every thread of both CTAs arrives; shared-memory writes before the
 // barrier are visible to the peer CTA after it.
 __device__ __forceinline__ void cluster_sync_all()
@@ -124,6 +125,15 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t
 {
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
                  ::"r"(dst), "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
+// Shared memory of this CTA -> shared memory of a CTA of the cluster; the
+// bytes complete on `bar`, a barrier of the destination CTA.
+__device__ __forceinline__ void bulk_s2s_cluster(uint32_t dst, uint32_t src, uint32_t bytes, uint32_t bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(dst), "r"(src), "r"(bytes), "r"(bar)
                  : "memory");
 }
 
@@ -246,7 +256,7 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
               const float* __restrict__ add, int add_batches, const int8_t* __restrict__ mask)
 {
     extern __shared__ unsigned char smem_raw[];
-    __shared__ __align__(8) uint64_t bars[3 * MAX_STAGES + 1];
+    __shared__ __align__(8) uint64_t bars[3 * MAX_STAGES + 2];
     __shared__ uint32_t tmem_base_sh;
     unsigned char* sm = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const uint32_t sbase = smem_u32(sm);
@@ -262,6 +272,7 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
     auto fullB = [&](int s) { return bar0 + 8u * (STAGES + s); };
     auto empty = [&](int s) { return bar0 + 8u * (2 * STAGES + s); };
     const uint32_t accf = bar0 + 8u * (3 * STAGES);
+    const uint32_t rbar = bar0 + 8u * (3 * STAGES + 1);   // inverse: the peer's half tile has landed
 
     const int tid = threadIdx.x;
     const int warp = tid >> 5;
@@ -271,7 +282,8 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
     // Forward: tiles [t_first, t_first + ntl) of one output parity. Inverse:
     // the CTA pair of a cluster shares the rows and the tiles; rank 0 takes
     // the odd-k rows of the spectrum (job 0), rank 1 the even-k rows (job 1),
-    // and the epilogue combines the two through distributed shared memory.
+    // and the epilogue exchanges half tiles with one bulk copy into the
+    // peer's shared memory (distributed shared memory).
     int half = 0, t_first, ntl, cjob = 0;
     if (MODE == 0) {
         const int G = (tab.nt + tab.gf - 1) / tab.gf;
@@ -300,7 +312,10 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
             mbar_init(empty(s), 1);
         }
         mbar_init(accf, 1);
+        if (MODE == 1) mbar_init(rbar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        // armed before the cluster barrier after which the peer sends
+        if (MODE == 1) mbar_arrive_expect_tx(rbar, HALF_BYTES);
     }
     tc_fence_before();
     __syncthreads();
@@ -458,7 +473,7 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
         // the columns. All stages are free once the last MMA has completed.
         mbar_wait(accf, 0, 4);
         tc_fence_after();
-        constexpr int S = 257;
+        constexpr int S = EPI_S;
         float* ep = reinterpret_cast<float*>(sm);
         const int sp = warp & 3;
         const int hc = warp >> 2;
@@ -522,50 +537,66 @@ dst_tc_kernel(TcGeom g, TcTab tab, const float* __restrict__ img, const float* _
     __syncwarp();
     if constexpr (MODE == 1) {
         // ---------------- inverse epilogue across the CTA pair ----------------
-        // Rank 0 (odd-k sum A) writes x[p] = A + B, rank 1 (even-k sum B)
-        // writes x[n-1-p] = A - B, each reading the peer's staged
-        // accumulators. Every thread of both CTAs reaches both barriers.
+        // Rank 0 holds the odd-k sums A, rank 1 the even-k sums B of all 128
+        // rows. Each CTA sends the half of its staging tile that the peer
+        // needs with one bulk copy into the peer's free pipeline space (rank
+        // 0 its rows 64..127, rank 1 its rows 0..63), then combines its own
+        // 64 rows locally: x[p] = A + B and x[n-1-p] = A - B. Every thread of
+        // both CTAs reaches both cluster barriers.
+        constexpr int S = EPI_S;
+        const uint32_t recv = smem_u32(sm) + (uint32_t)EPI_BYTES;
+        if (warp < MMA_WARP) fence_async_smem();   // staging writes -> the copy
         cluster_sync_all();
-        if (warp < MMA_WARP) {
-            constexpr int S = 257;
+        if (tid == 0) {
+            const uint32_t src = smem_u32(sm) + (cjob == 0 ? HALF_BYTES : 0u);
+            bulk_s2s_cluster(mapa_shared(recv, (uint32_t)(cjob ^ 1)), src, HALF_BYTES,
+                             mapa_shared(rbar, (uint32_t)(cjob ^ 1)));
+        }
+        if (warp < MMA_WARP && mbar_wait(rbar, 0, 16)) {
             const float* ep = reinterpret_cast<const float*>(sm);
-            const uint32_t ep_peer = mapa_shared(smem_u32(sm), (uint32_t)(cjob ^ 1));
-            const int r0 = warp * RPW;
+            const float* pe = reinterpret_cast<const float*>(sm + EPI_BYTES);
+            constexpr int RW = (int)HALF_ROWS / NPW;    // rows per warp
             const int p0 = t_first * TILE;
-            const int lim = cjob == 0 ? ne : no;
-            for (int rr = 0; rr < RPW; ++rr) {
-                const int r = r0 + rr;
+            for (int rr = 0; rr < RW; ++rr) {
+                const int rl = warp * RW + rr;              // row in the received half
+                const int r = (int)(cjob * HALF_ROWS) + rl; // row in the 128-row block
                 const int row = blockIdx.y * BM + r;
                 if (row >= g.R) break;
                 const int f = row / g.my;
                 const int j = row - f * g.my + 1;
                 const long long base = f * g.fs + (long long)j * g.nx + 1;
                 const bool ha = add != nullptr && (EPI != EPI_H || f < add_batches);
-                float av[8], own[8], oth[8];
-                bool mk[8];
-                // all loads of the row first, then the stores
+                float va[8], vb[8], a1[8], a2[8];
+                bool m1[8], m2[8];
+                // every load of the row first, then the stores
 #pragma unroll
                 for (int u8 = 0; u8 < 8; ++u8) {
                     const int cc = lane + 32 * u8;
                     const int p = p0 + cc;
-                    const bool v = cc < N && p < lim;
-                    const int col = cjob == 0 ? p : n - 1 - p;
-                    av[u8] = (v && ha) ? add[base + col] : 0.f;
-                    mk[u8] = (EPI == EPI_ADJQ) ? (v && mask[j * g.nx + 1 + col] == 3) : v;
-                    own[u8] = v ? ep[r * S + cc] : 0.f;
-                    oth[u8] = v ? ld_cluster_f32(ep_peer + (uint32_t)(r * S + cc) * 4u) : 0.f;
+                    const bool v1 = cc < N && p < ne, v2 = cc < N && p < no;
+                    const float own = cc < N ? ep[r * S + cc] : 0.f;
+                    const float oth = cc < N ? pe[rl * S + cc] : 0.f;
+                    va[u8] = cjob == 0 ? own : oth;
+                    vb[u8] = cjob == 0 ? oth : own;
+                    const int c1 = p, c2 = n - 1 - p;
+                    a1[u8] = (v1 && ha) ? add[base + c1] : 0.f;
+                    a2[u8] = (v2 && ha) ? add[base + c2] : 0.f;
+                    m1[u8] = (EPI == EPI_ADJQ) ? (v1 && mask[j * g.nx + 1 + c1] == 3) : v1;
+                    m2[u8] = (EPI == EPI_ADJQ) ? (v2 && mask[j * g.nx + 1 + c2] == 3) : v2;
                 }
 #pragma unroll
                 for (int u8 = 0; u8 < 8; ++u8) {
                     const int cc = lane + 32 * u8;
                     const int p = p0 + cc;
-                    if (!(cc < N && p < lim)) continue;
-                    const float val = cjob == 0 ? own[u8] + (p < no ? oth[u8] : 0.f) : oth[u8] - own[u8];
-                    const int col = cjob == 0 ? p : n - 1 - p;
-                    out[base + col] = mk[u8] ? val + av[u8] : 0.f;
+                    if (cc < N && p < ne) {
+                        const float val = va[u8] + (p < no ? vb[u8] : 0.f);
+                        out[base + p] = m1[u8] ? val + a1[u8] : 0.f;
+                    }
+                    if (cc < N && p < no) out[base + (n - 1 - p)] = m2[u8] ? (va[u8] - vb[u8]) + a2[u8] : 0.f;
                 }
             }
         }
+        // the peer's copy out of this CTA's tile has landed before either exits
         cluster_sync_all();
     }
     tc_fence_before();
@@ -716,7 +747,9 @@ int dst_pass_tc(const vd_qg1l_plan* p, int nf, const SolveArgs& a, float* spec, 
     tab.b_tile = (uint32_t)gmax * TILE_BYTES;
     const size_t stage_bytes = 2 * (size_t)A_TILE + 2 * (size_t)tab.b_tile;
     tab.nst = (int)std::min<size_t>(MAX_STAGES, PIPE_BYTES / stage_bytes);
-    const size_t smem = std::max<size_t>(tab.nst * stage_bytes, EPI_BYTES) + 1024;   // <= SMEM_MAX
+    // the inverse also receives half of the peer's staging tile after its own
+    const size_t epi = fwd ? EPI_BYTES : EPI_BYTES + HALF_BYTES;
+    const size_t smem = std::max<size_t>(tab.nst * stage_bytes, epi) + 1024;   // <= SMEM_MAX
     if (fwd) {
         dim3 grid(2 * groups(tab.gf), rows);
         dst_tc_kernel<0, EPI_H><<<grid, NTHREADS, smem, st>>>(
