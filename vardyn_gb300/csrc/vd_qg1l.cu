@@ -537,8 +537,9 @@ __device__ __forceinline__ void tma_tile_2d(uint32_t dst, const CUtensorMap* map
         : "memory");
 }
 
+// Four CTAs per SM in float32 (shared memory allows four), two in float64.
 template <typename T, bool TMA>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2)
 k_adj_stage_fused(QGGeom G, int nf, const T* __restrict__ hs, const T* __restrict__ qs, StageIn<T> gin,
                   StageIn<T> gacc, T* __restrict__ adq_out, T* __restrict__ adh_out, const __grid_constant__ AdjMaps M)
 {
@@ -554,9 +555,11 @@ k_adj_stage_fused(QGGeom G, int nf, const T* __restrict__ hs, const T* __restric
     const int j0 = blockIdx.y * AT_Y, i0 = blockIdx.x * AT_X;
     const int tid = threadIdx.y * 32 + threadIdx.x;
     const long long fo = f * G.fs;
-    constexpr int NAL = (AA_Y * AA_X + 255) / 256;
-    T lkv[NAL], bev[NAL];
-    bool m3a[NAL];
+    // phase A runs on vertical pairs of points (rows a, a+1 of the region)
+    constexpr int NPA = (AA_Y / 2) * AA_X;
+    constexpr int NAL = (NPA + 255) / 256;
+    T lkv[NAL][2], bev[NAL][2];
+    bool m3a[NAL][2];
     if constexpr (TMA) {
         // ---- bulk tensor copies of every staged tile, one mbarrier ----
         const uint32_t sb = (uint32_t)__cvta_generic_to_shared(smem_raw);
@@ -594,16 +597,20 @@ k_adj_stage_fused(QGGeom G, int nf, const T* __restrict__ hs, const T* __restric
 #pragma unroll
         for (int k = 0; k < NAL; ++k) {
             const int e = tid + 256 * k;
-            const int a = e / AA_X, b = e - a * AA_X;
-            const bool in = e < AA_Y * AA_X;
-            T lk = T(0);
+            const int ap = e / AA_X, b = e - ap * AA_X;
+            const bool in = e < NPA;
 #pragma unroll
-            for (int t = 0; t < 4; ++t)
-                if (t < gin.nk && in)
-                    lk += gin.c[t] * reinterpret_cast<const T*>(smem_raw + L.out + t * gtile)[a * AG_X + b + 2];
-            lkv[k] = lk;
-            m3a[k] = in && mk[a * AM_X + b + 14] == 3;
-            bev[k] = (in && hasBeta) ? bt[a * AG_X + b + 2] : T(0);
+            for (int u = 0; u < 2; ++u) {
+                const int a = 2 * ap + u;
+                T lk = T(0);
+#pragma unroll
+                for (int t = 0; t < 4; ++t)
+                    if (t < gin.nk && in)
+                        lk += gin.c[t] * reinterpret_cast<const T*>(smem_raw + L.out + t * gtile)[a * AG_X + b + 2];
+                lkv[k][u] = lk;
+                m3a[k][u] = in && mk[a * AM_X + b + 14] == 3;
+                bev[k][u] = (in && hasBeta) ? bt[a * AG_X + b + 2] : T(0);
+            }
         }
     } else {
         // ---- bounds-checked loads: every load of the thread before any store ----
@@ -647,120 +654,189 @@ k_adj_stage_fused(QGGeom G, int nf, const T* __restrict__ hs, const T* __restric
 #pragma unroll
         for (int k = 0; k < NAL; ++k) {
             const int e = tid + 256 * k;
-            const int a = e / AA_X, b = e - a * AA_X;
-            const int j = j0 - 2 + a, i = i0 - 2 + b;
-            const bool in = e < AA_Y * AA_X && j >= 0 && j < G.ny && i >= 0 && i < G.nx;
-            const long long g2 = (long long)j * G.nx + i;
-            const long long o = fo + g2;
-            T lk = T(0);
+            const int ap = e / AA_X, b = e - ap * AA_X;
 #pragma unroll
-            for (int t = 0; t < 4; ++t)
-                if (t < gin.nk && in) lk += gin.c[t] * gin.k[t][o];
-            lkv[k] = lk;
-            m3a[k] = in && G.mask[g2] == 3;
-            bev[k] = (in && G.beta) ? ((const T*)G.beta)[g2] : T(0);
+            for (int u = 0; u < 2; ++u) {
+                const int a = 2 * ap + u;
+                const int j = j0 - 2 + a, i = i0 - 2 + b;
+                const bool in = e < NPA && j >= 0 && j < G.ny && i >= 0 && i < G.nx;
+                const long long g2 = (long long)j * G.nx + i;
+                const long long o = fo + g2;
+                T lk = T(0);
+#pragma unroll
+                for (int t = 0; t < 4; ++t)
+                    if (t < gin.nk && in) lk += gin.c[t] * gin.k[t][o];
+                lkv[k][u] = lk;
+                m3a[k][u] = in && G.mask[g2] == 3;
+                bev[k][u] = (in && G.beta) ? ((const T*)G.beta)[g2] : T(0);
+            }
         }
     }
     __syncthreads();
-    // ---- phase A on the tile + halo 2 ----
+    // ---- phase A on the tile + halo 2, two vertically adjacent points per
+    // thread: their SSH and PV stencils overlap, so the pair reads 12 h and
+    // 14 q values (each point alone 8 and 9) and then runs the single-point
+    // arithmetic on each ----
     const T cx = T(G.cx), cy = T(G.cy), cu = T(G.cu), cv = T(G.cv);
 #pragma unroll
     for (int k = 0; k < NAL; ++k) {
         const int e = tid + 256 * k;
-        if (e >= AA_Y * AA_X) break;
-        const int a = e / AA_X, b = e - a * AA_X;
-        T lk = T(0), uT = T(0), vT = T(0), aut = T(0), avt = T(0);
-        if (m3a[k]) {
-            lk = lkv[k];
-            const int ha = a + 1, hb = b + 2;     // h-tile index of P
-            Vel<T> V;
-            V.u0 = guard0(cu * (S.h[ha + 1][hb - 1] + S.h[ha + 1][hb] - S.h[ha - 1][hb] - S.h[ha - 1][hb - 1]));
-            V.u1 = guard0(cu * (S.h[ha + 1][hb] + S.h[ha + 1][hb + 1] - S.h[ha - 1][hb + 1] - S.h[ha - 1][hb]));
-            V.v0 = guard0(cv * (S.h[ha][hb + 1] + S.h[ha - 1][hb + 1] - S.h[ha - 1][hb - 1] - S.h[ha][hb - 1]));
-            V.v1 = guard0(cv * (S.h[ha + 1][hb + 1] + S.h[ha][hb + 1] - S.h[ha][hb - 1] - S.h[ha + 1][hb - 1]));
-            const int qa_ = a + 2, qb_ = b + 2;   // q-tile index of P
-            Cross<T> q;
-            q.c = S.q[qa_][qb_]; q.e1 = S.q[qa_][qb_ + 1]; q.e2 = S.q[qa_][qb_ + 2];
-            q.w1 = S.q[qa_][qb_ - 1]; q.w2 = S.q[qa_][qb_ - 2];
-            q.n1 = S.q[qa_ + 1][qb_]; q.n2 = S.q[qa_ + 2][qb_];
-            q.s1 = S.q[qa_ - 1][qb_]; q.s2 = S.q[qa_ - 2][qb_];
-            Cross<T> qa = q;
-            if (hasB) {
-                qa.c = S.qa[qa_][qb_]; qa.e1 = S.qa[qa_][qb_ + 1]; qa.e2 = S.qa[qa_][qb_ + 2];
-                qa.w1 = S.qa[qa_][qb_ - 1]; qa.w2 = S.qa[qa_][qb_ - 2];
-                qa.n1 = S.qa[qa_ + 1][qb_]; qa.n2 = S.qa[qa_ + 2][qb_];
-                qa.s1 = S.qa[qa_ - 1][qb_]; qa.s2 = S.qa[qa_ - 2][qb_];
+        if (e >= NPA) break;
+        const int ap = e / AA_X, b = e - ap * AA_X;
+        const int a0 = 2 * ap;
+        T lk[2] = {T(0), T(0)}, uT[2] = {T(0), T(0)}, vT[2] = {T(0), T(0)}, aut[2] = {T(0), T(0)},
+          avt[2] = {T(0), T(0)};
+        if (m3a[k][0] || m3a[k][1]) {
+            const int ha = a0 + 1, hb = b + 2;     // h-tile index of the first point
+            T hv[4][3];                            // rows ha-1 .. ha+2, columns hb-1 .. hb+1
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) hv[r][c] = S.h[ha - 1 + r][hb - 1 + c];
+            const int qa_ = a0 + 2, qb_ = b + 2;   // q-tile index of the first point
+            T vq[6], hq[2][4];                     // column qb_ rows qa_-2 .. qa_+3; rows qa_, qa_+1 at qb_-2, -1, +1, +2
+            T vqa[6], hqa[2][4];
+#pragma unroll
+            for (int r = 0; r < 6; ++r) vq[r] = S.q[qa_ - 2 + r][qb_];
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                hq[u][0] = S.q[qa_ + u][qb_ - 2]; hq[u][1] = S.q[qa_ + u][qb_ - 1];
+                hq[u][2] = S.q[qa_ + u][qb_ + 1]; hq[u][3] = S.q[qa_ + u][qb_ + 2];
             }
-            const T beta = bev[k];
-            if (isnan(tendency<T>(G, V, qa, q, beta))) lk = T(0);
-            uT = T(0.5) * (V.u0 + V.u1);
-            vT = T(0.5) * (V.v0 + V.v1);
-            const T gu = (uT >= T(0) ? -cx * qa.Dpx() : T(0)) + (uT <= T(0) ? cx * qa.Dmx() : T(0));
-            const T gv = (vT >= T(0) ? -cy * qa.Dpy() : T(0)) + (vT <= T(0) ? cy * qa.Dmy() : T(0));
-            aut = lk * gu;
-            avt = lk * gv - beta * lk;
+            if (hasB) {
+#pragma unroll
+                for (int r = 0; r < 6; ++r) vqa[r] = S.qa[qa_ - 2 + r][qb_];
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    hqa[u][0] = S.qa[qa_ + u][qb_ - 2]; hqa[u][1] = S.qa[qa_ + u][qb_ - 1];
+                    hqa[u][2] = S.qa[qa_ + u][qb_ + 1]; hqa[u][3] = S.qa[qa_ + u][qb_ + 2];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                if (!m3a[k][u]) continue;
+                lk[u] = lkv[k][u];
+                // rows of this point: s = u, m = u + 1, n = u + 2 in hv
+                const T(&hs_)[3] = hv[u];
+                const T(&hm_)[3] = hv[u + 1];
+                const T(&hn_)[3] = hv[u + 2];
+                Vel<T> V;
+                V.u0 = guard0(cu * (hn_[0] + hn_[1] - hs_[1] - hs_[0]));
+                V.u1 = guard0(cu * (hn_[1] + hn_[2] - hs_[2] - hs_[1]));
+                V.v0 = guard0(cv * (hm_[2] + hs_[2] - hs_[0] - hm_[0]));
+                V.v1 = guard0(cv * (hn_[2] + hm_[2] - hm_[0] - hn_[0]));
+                Cross<T> q;
+                q.c = vq[2 + u]; q.e1 = hq[u][2]; q.e2 = hq[u][3]; q.w1 = hq[u][1]; q.w2 = hq[u][0];
+                q.n1 = vq[3 + u]; q.n2 = vq[4 + u]; q.s1 = vq[1 + u]; q.s2 = vq[u];
+                Cross<T> qa = q;
+                if (hasB) {
+                    qa.c = vqa[2 + u]; qa.e1 = hqa[u][2]; qa.e2 = hqa[u][3]; qa.w1 = hqa[u][1]; qa.w2 = hqa[u][0];
+                    qa.n1 = vqa[3 + u]; qa.n2 = vqa[4 + u]; qa.s1 = vqa[1 + u]; qa.s2 = vqa[u];
+                }
+                const T beta = bev[k][u];
+                if (isnan(tendency<T>(G, V, qa, q, beta))) lk[u] = T(0);
+                uT[u] = T(0.5) * (V.u0 + V.u1);
+                vT[u] = T(0.5) * (V.v0 + V.v1);
+                const T gu = (uT[u] >= T(0) ? -cx * qa.Dpx() : T(0)) + (uT[u] <= T(0) ? cx * qa.Dmx() : T(0));
+                const T gv = (vT[u] >= T(0) ? -cy * qa.Dpy() : T(0)) + (vT[u] <= T(0) ? cy * qa.Dmy() : T(0));
+                aut[u] = lk[u] * gu;
+                avt[u] = lk[u] * gv - beta * lk[u];
+            }
         }
-        S.lup[a][b] = lk * (uT < T(0) ? T(0) : uT);
-        S.lum[a][b] = lk * (uT > T(0) ? T(0) : uT);
-        S.lvp[a][b] = lk * (vT < T(0) ? T(0) : vT);
-        S.lvm[a][b] = lk * (vT > T(0) ? T(0) : vT);
-        S.aut[a][b] = aut;
-        S.avt[a][b] = avt;
-        if (hasK) S.lk[a][b] = lk;
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int a = a0 + u;
+            S.lup[a][b] = lk[u] * (uT[u] < T(0) ? T(0) : uT[u]);
+            S.lum[a][b] = lk[u] * (uT[u] > T(0) ? T(0) : uT[u]);
+            S.lvp[a][b] = lk[u] * (vT[u] < T(0) ? T(0) : vT[u]);
+            S.lvm[a][b] = lk[u] * (vT[u] > T(0) ? T(0) : vT[u]);
+            S.aut[a][b] = aut[u];
+            S.avt[a][b] = avt[u];
+            if (hasK) S.lk[a][b] = lk[u];
+        }
     }
     __syncthreads();
-    // ---- phase B on the tile (accumulated adjoints and flags loaded first) ----
-    constexpr int NBL = (AT_Y * AT_X + 255) / 256;
-    T accv[NBL];
-    bool m3b[NBL];
+    // ---- phase B on the tile, vertical pairs of points (accumulated adjoints
+    // and flags loaded first); the pair shares its y-stencil, diffusion and
+    // h2uv-transpose reads ----
+    constexpr int NPB = (AT_Y / 2) * AT_X;
+    constexpr int NBL = (NPB + 255) / 256;
+    T accv[NBL][2];
+    bool m3b[NBL][2];
 #pragma unroll
     for (int k = 0; k < NBL; ++k) {
         const int e = tid + 256 * k;
-        const int a = e / AT_X, b = e - a * AT_X;
-        const int j = j0 + a, i = i0 + b;
-        const bool in = e < AT_Y * AT_X && j < G.ny && i < G.nx;
-        const long long o = fo + (long long)j * G.nx + i;
-        T sacc = T(0);
+        const int ap = e / AT_X, b = e - ap * AT_X;
 #pragma unroll
-        for (int t = 0; t < 4; ++t)
-            if (t < gacc.nk && in) sacc += gacc.k[t][o];
-        accv[k] = sacc;
-        if constexpr (TMA)
-            m3b[k] = in && reinterpret_cast<const int8_t*>(smem_raw + L.mask)[(a + 2) * AM_X + b + 16] == 3;
-        else
-            m3b[k] = in && G.mask[(long long)j * G.nx + i] == 3;
-    }
+        for (int u = 0; u < 2; ++u) {
+            const int a = 2 * ap + u;
+            const int j = j0 + a, i = i0 + b;
+            const bool in = e < NPB && j < G.ny && i < G.nx;
+            const long long o = fo + (long long)j * G.nx + i;
+            T sacc = T(0);
 #pragma unroll
-    for (int k = 0; k < NBL; ++k) {
-        const int e = tid + 256 * k;
-        const int a = e / AT_X, b = e - a * AT_X;
-        const int j = j0 + a, i = i0 + b;
-        if (e >= AT_Y * AT_X || j >= G.ny || i >= G.nx) continue;
-        const int A = a + 2, Bc = b + 2;    // phase-A index of X
-        auto UP = [&](int da, int db) { return S.lup[A + da][Bc + db]; };
-        auto UM = [&](int da, int db) { return S.lum[A + da][Bc + db]; };
-        auto VP = [&](int da, int db) { return S.lvp[A + da][Bc + db]; };
-        auto VM = [&](int da, int db) { return S.lvm[A + da][Bc + db]; };
-        T aq = cx * (-T(2) * UP(0, -1) - T(6) * UM(0, -1)
-                     - T(3) * UP(0, 0) + T(3) * UM(0, 0)
-                     + T(6) * UP(0, 1) + T(2) * UM(0, 1)
-                     - UP(0, 2) + UM(0, -2))
-             + cy * (-T(2) * VP(-1, 0) - T(6) * VM(-1, 0)
-                     - T(3) * VP(0, 0) + T(3) * VM(0, 0)
-                     + T(6) * VP(1, 0) + T(2) * VM(1, 0)
-                     - VP(2, 0) + VM(-2, 0));
-        if (hasK) {
-            const T lc = S.lk[A][Bc];
-            aq += T(G.Kx) * (S.lk[A][Bc - 1] + S.lk[A][Bc + 1] - T(2) * lc)
-                + T(G.Ky) * (S.lk[A - 1][Bc] + S.lk[A + 1][Bc] - T(2) * lc);
+            for (int t = 0; t < 4; ++t)
+                if (t < gacc.nk && in) sacc += gacc.k[t][o];
+            accv[k][u] = sacc;
+            if constexpr (TMA)
+                m3b[k][u] = in && reinterpret_cast<const int8_t*>(smem_raw + L.mask)[(a + 2) * AM_X + b + 16] == 3;
+            else
+                m3b[k][u] = in && G.mask[(long long)j * G.nx + i] == 3;
         }
-        const long long o = fo + (long long)j * G.nx + i;
-        adq_out[o] = m3b[k] ? aq + accv[k] : T(0);
-        const T hu = T(0.5) * cu, hv = T(0.5) * cv;
-        adh_out[o] = hu * (S.aut[A - 1][Bc - 1] + T(2) * S.aut[A - 1][Bc] + S.aut[A - 1][Bc + 1]
-                           - S.aut[A + 1][Bc - 1] - T(2) * S.aut[A + 1][Bc] - S.aut[A + 1][Bc + 1])
-                   + hv * (S.avt[A - 1][Bc - 1] + T(2) * S.avt[A][Bc - 1] + S.avt[A + 1][Bc - 1]
-                           - S.avt[A - 1][Bc + 1] - T(2) * S.avt[A][Bc + 1] - S.avt[A + 1][Bc + 1]);
+    }
+    const T hu = T(0.5) * cu, hv2 = T(0.5) * cv;
+#pragma unroll
+    for (int k = 0; k < NBL; ++k) {
+        const int e = tid + 256 * k;
+        if (e >= NPB) break;
+        const int ap = e / AT_X, b = e - ap * AT_X;
+        const int a0 = 2 * ap;
+        const int i = i0 + b;
+        if (j0 + a0 >= G.ny || i >= G.nx) continue;
+        const int A = a0 + 2, Bc = b + 2;    // phase-A index of the first point
+        T vp[5], vm[5];                      // VP rows A-1 .. A+3, VM rows A-2 .. A+2 (column Bc)
+#pragma unroll
+        for (int r = 0; r < 5; ++r) {
+            vp[r] = S.lvp[A - 1 + r][Bc];
+            vm[r] = S.lvm[A - 2 + r][Bc];
+        }
+        T at[4][3], av[4][2];                // aut rows A-1 .. A+2 x columns Bc-1 .. Bc+1; avt at Bc-1, Bc+1
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) at[r][c] = S.aut[A - 1 + r][Bc - 1 + c];
+            av[r][0] = S.avt[A - 1 + r][Bc - 1];
+            av[r][1] = S.avt[A - 1 + r][Bc + 1];
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int Au = A + u;
+            const int j = j0 + a0 + u;
+            if (j >= G.ny) break;
+            auto UP = [&](int db) { return S.lup[Au][Bc + db]; };
+            auto UM = [&](int db) { return S.lum[Au][Bc + db]; };
+            // VP(d) = vp[u + 1 + d], VM(d) = vm[u + 2 + d]
+            T aq = cx * (-T(2) * UP(-1) - T(6) * UM(-1)
+                         - T(3) * UP(0) + T(3) * UM(0)
+                         + T(6) * UP(1) + T(2) * UM(1)
+                         - UP(2) + UM(-2))
+                 + cy * (-T(2) * vp[u] - T(6) * vm[u + 1]
+                         - T(3) * vp[u + 1] + T(3) * vm[u + 2]
+                         + T(6) * vp[u + 2] + T(2) * vm[u + 3]
+                         - vp[u + 3] + vm[u]);
+            if (hasK) {
+                const T lc = S.lk[Au][Bc];
+                aq += T(G.Kx) * (S.lk[Au][Bc - 1] + S.lk[Au][Bc + 1] - T(2) * lc)
+                    + T(G.Ky) * (S.lk[Au - 1][Bc] + S.lk[Au + 1][Bc] - T(2) * lc);
+            }
+            const long long o = fo + (long long)j * G.nx + i;
+            adq_out[o] = m3b[k][u] ? aq + accv[k][u] : T(0);
+            // aut rows Au-1, Au+1 = at[u], at[u + 2]; avt rows Au-1 .. Au+1 = av[u .. u + 2]
+            adh_out[o] = hu * (at[u][0] + T(2) * at[u][1] + at[u][2]
+                               - at[u + 2][0] - T(2) * at[u + 2][1] - at[u + 2][2])
+                       + hv2 * (av[u][0] + T(2) * av[u + 1][0] + av[u + 2][0]
+                                - av[u][1] - T(2) * av[u + 1][1] - av[u + 2][1]);
+        }
     }
 }
 
