@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--profile-small", action="store_true",
                     help="short window for profiler captures (not a bench value)")
+    ap.add_argument("--schedule", default=None,
+                    help="JSON inversion schedule fields used instead of the autotuner's pick (profiler "
+                         "captures, under which the tuner's timings do not reflect the timed run)")
     ap.add_argument("--workload", default="qg512", choices=["qg512", "basis1024", "mixed64", "sw3l", "qg3l", "aux", "jqgm"],
                     help="qg512: control = initial SSH, 512^2, batched windows (the headline); "
                          "basis1024: reduced-basis control forcing the SSH, 1024^2, one window; "
@@ -392,7 +395,10 @@ def gpu_arm(args):
     # the project autotuner picks the inversion schedule for this grid and batch
     # before capture (the graph keeps it)
     from vardyn_gb300 import autotune
-    tuned_schedule, tune_times = autotune.tune(plan, B)
+    if args.schedule:
+        tuned_schedule, tune_times = plan.set_schedule(**json.loads(args.schedule)), {}
+    else:
+        tuned_schedule, tune_times = autotune.tune(plan, B)
     c0 = L.vd_launch_count()
     eng.capture()
     launches_per_eval = (L.vd_launch_count() - c0) // 2   # warm-up run + captured run
