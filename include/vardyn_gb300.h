@@ -89,7 +89,8 @@ typedef struct vd_qg1l_schedule {
     int fma_rows;        /* rows per CTA of the FMA pass: 0 rule, 16, 32 or
                             64 (float32) */
     int tridiag_rows;    /* rows per thread of the tridiagonal solve: 0 rule,
-                            16 or 32 (used when the field fits, else the rule) */
+                            8, 16 or 32 (used when the field fits, else the
+                            rule) */
     int tridiag_lean;    /* 1: the float32 16-row tridiagonal kernel capped at
                             80 registers (three CTAs per SM instead of two);
                             0 the standard kernel */

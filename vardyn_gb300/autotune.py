@@ -25,7 +25,7 @@ _cache = {}
 def candidates(plan):
     """Schedules worth timing for this plan: the built-in rule, FMA with each
     row tile, and (float32 plans with tensor-core images) tensor cores with
-    each tile group; each with both tridiagonal row counts and, in float32,
+    each tile group; each with the three tridiagonal row counts and, in float32,
     the register-capped tridiagonal kernel."""
     out = [{}]
     f32 = plan.dtype == torch.float32
@@ -36,7 +36,7 @@ def candidates(plan):
     if f32 and plan.dst_engine == "auto":
         for g in (1, 2, 4, 8):
             base.append(dict(engine=2, tc_group_fwd=g, tc_group_inv=g))
-    tri = [dict(tridiag_rows=16), dict(tridiag_rows=32)]
+    tri = [dict(tridiag_rows=8), dict(tridiag_rows=16), dict(tridiag_rows=32)]
     if f32:
         tri.append(dict(tridiag_rows=16, tridiag_lean=1))
     for b in base:

@@ -228,7 +228,8 @@ extern "C" vd_status vd_qg1l_set_schedule(vd_qg1l_plan* p, const vd_qg1l_schedul
     for (int g : {s->tc_group_fwd, s->tc_group_inv})
         if (g != 0 && g != 1 && g != 2 && g != 4 && g != 8) return VD_ERR_ARG;
     if (s->fma_rows != 0 && s->fma_rows != 16 && s->fma_rows != 32 && s->fma_rows != 64) return VD_ERR_ARG;
-    if (s->tridiag_rows != 0 && s->tridiag_rows != 16 && s->tridiag_rows != 32) return VD_ERR_ARG;
+    if (s->tridiag_rows != 0 && s->tridiag_rows != 8 && s->tridiag_rows != 16 && s->tridiag_rows != 32)
+        return VD_ERR_ARG;
     if (s->tridiag_lean != 0 && s->tridiag_lean != 1) return VD_ERR_ARG;
     if (s->tridiag_lean == 1 && p->d.dtype != VD_F32) return VD_ERR_UNSUPPORTED;
     if (s->stencil_loads != 0 && s->stencil_loads != 1) return VD_ERR_ARG;

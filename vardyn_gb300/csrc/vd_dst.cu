@@ -238,9 +238,10 @@ dst_gemm_kernel(GemmGeom g, const T* __restrict__ W1, const T* __restrict__ W2,
 // one 1024^2 field.
 // LEAN caps the registers at 80 (16-row pieces in float32 otherwise take
 // ~124): three 256-thread CTAs fit an SM instead of two (a schedule choice,
-// picked by timing).
+// picked by timing). 8-row pieces are capped at 64 registers, so two CTAs
+// of up to 512 threads fit an SM.
 template <typename T, int CW, int CH, bool LEAN = false>
-__global__ void __maxnreg__(LEAN ? 80 : 128)
+__global__ void __maxnreg__(LEAN ? 80 : (CH <= 8 ? 64 : 128))
 tridiag_chunked_kernel(T* __restrict__ spec, const T* __restrict__ trim, int my, int n, int lds, T a)
 {
     constexpr int SUB = 32 / CW;
@@ -732,7 +733,8 @@ static cudaError_t set_smem_attrs()
 }
 
 // The y-direction tridiagonal solves of nf fields: 8 columns per CTA,
-// pieces of 16 rows (32 for fields of 1025-2048 rows) in at most 16 warps;
+// pieces of 16 rows (32 for fields of 1025-2048 rows; 8, in up to 32 warps,
+// as a schedule choice for fields of up to 1024 rows) in at most 16 warps;
 // taller fields fall back to one sequential thread per column. (Measured on
 // GB300 against 32- and 16-column groups, shared-memory staging and a
 // warp-shuffle chain of the pieces: this form is the fastest or tied at both
@@ -744,10 +746,15 @@ static int launch_tridiag(const vd_qg1l_plan* p, int nf, T* spec, cudaStream_t s
     const T a = (T)t.tri_a;
     constexpr int CW = 8, SUB = 32 / CW;
     const dim3 grid((t.n + CW - 1) / CW, nf);
+    const int nw8 = ((t.my + 7) / 8 + SUB - 1) / SUB;
     const int nw16 = ((t.my + 15) / 16 + SUB - 1) / SUB;
     const int nw32 = ((t.my + 31) / 32 + SUB - 1) / SUB;
     const bool want32 = p->sched.tridiag_rows == 32 && nw32 <= 16;
-    if (nw16 <= 16 && !want32 && p->sched.tridiag_lean == 1 && sizeof(T) == 4) {
+    const bool want8 = p->sched.tridiag_rows == 8 && nw8 <= 32;
+    if (want8) {
+        tridiag_chunked_kernel<T, CW, 8><<<grid, dim3(32, nw8), 2 * nw8 * CW * sizeof(T), st>>>(
+            spec, (const T*)t.trim, t.my, t.n, t.lds, a);
+    } else if (nw16 <= 16 && !want32 && p->sched.tridiag_lean == 1 && sizeof(T) == 4) {
         tridiag_chunked_kernel<T, CW, 16, true><<<grid, dim3(32, nw16), 2 * nw16 * CW * sizeof(T), st>>>(
             spec, (const T*)t.trim, t.my, t.n, t.lds, a);
     } else if (nw16 <= 16 && !want32) {
