@@ -933,15 +933,42 @@ __global__ void k_sw_update_adj(Tab<T> t, int stage, int nf, T* adn_u, T* adn_v,
     }
 }
 
+// Atomic accumulation, used only where sums run over the batch into the H /
+// h_wind table cotangents and by the mass-consistent forcing adjoint.
 template <typename T> __device__ __forceinline__ void aadd(T* p, T v) { atomicAdd(p, v); }
 
 // Adjoint of k_sw_tend and of the divergence / diffusion part of
-// k_sw_update: scatters into the adjoints of vorticity, KE + pressure and
-// clamped thickness (adom, adkp, adht) and, directly, of u, v, h (adx).
+// k_sw_update, in two passes with no atomics.
+//
+// Pass 1 (k_sw_tend_adj_src, one thread per point): every source point of
+// the forward tendency stores the cotangents it contributes, one value per
+// (source, term): at u faces the tendency cotangent a (KE + pressure, drag),
+// a * dF/dq_k of its vorticity WENO flux (k = 0..5), the V-average term, the
+// viscosity coefficient, aF * dF/dq_k of the thickness flux through the face
+// and the face's own flux-velocity term; the same at v faces; and the
+// thickness-diffusion coefficient at h points. Every index in range is
+// written (zeros where a point contributes nothing).
+// Pass 2 (k_sw_tend_adj_gather, one thread per target point): each target
+// sums, in a fixed order, the stored terms of the sources whose stencils
+// reach it (the inverse of each forward stencil, including the clamped
+// viscosity and diffusion neighbours at the edges). The sums are therefore
+// the same on every run. The H / h_wind table cotangents (only when
+// registered) still accumulate with atomics over the batch.
+
 template <typename T>
-__global__ void k_sw_tend_adj(Tab<T> t, const T* u, const T* v, const T* h, const T* om, const T* ht,
-                              const T* adk_u, const T* adk_v, const T* adk_h, T* adom, T* adkp, T* adht, T* adu,
-                              T* adv, T* adh, const T* taux, const T* tauy)
+struct SwSrc {
+    T *ua, *uvm, *uc, *uf;   // [bl][su] u faces: a, V-average term, viscosity coefficient, own flux term
+    T *uw, *uh;              // [6][bl][su]: vorticity and thickness WENO terms
+    T *va, *vum, *vc, *vf;   // [bl][sv] v faces
+    T *vw, *vh;              // [6][bl][sv]
+    T *hd;                   // [bl][sh] thickness-diffusion coefficient
+    long long nu, nv;        // bl * su, bl * sv: stride of the six-term arrays
+};
+
+template <typename T>
+__global__ void k_sw_tend_adj_src(Tab<T> t, const T* u, const T* v, const T* h, const T* om, const T* ht,
+                                  const T* adk_u, const T* adk_v, const T* adk_h, SwSrc<T> S, const T* taux,
+                                  const T* tauy)
 {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = blockIdx.y * blockDim.y + threadIdx.y;
@@ -951,183 +978,258 @@ __global__ void k_sw_tend_adj(Tab<T> t, const T* u, const T* v, const T* h, cons
     const long long ob = bl;
     const T* hb = adk_h + ob * t.sh;
     auto mh = [&](long long k) { return (t.fh[k] & 1) ? T(1) : T(0); };
-    // ---------------- u point
-    if (j < ny && i >= 1 && i <= nx - 1) {
-        const long long ui = (long long)i * ny + j;
-        const int fl = t.fu[ui];
-        const T a = adk_u[ob * t.su + ui] * ((fl & 1) ? T(1) : T(0));
-        if (a != T(0)) {
-            const long long vb = ob * t.sv;
-            auto Vv = [&](int p, int c) {
-                const long long k = (long long)p * (ny + 1) + c;
-                return v[vb + k] * t.idyv2[k];
-            };
-            const T Vm = T(0.25) * (Vv(i, j + 1) + Vv(i, j) + Vv(i - 1, j + 1) + Vv(i - 1, j));
-            T q[6];
-            const long long wb = ob * t.sw + (long long)i * (ny + 1);
+    // ---------------- u face (i, j)
+    if (j < ny) {
+        const long long ui = (long long)i * ny + j, so = ob * t.su + ui;
+        T a_s = T(0), vm_s = T(0), c_s = T(0), f_s = T(0), w_s[6], h_s[6];
 #pragma unroll
-            for (int k = 0; k < 6; ++k) {
-                const int jj = j - 2 + k;
-                q[k] = (jj >= 0 && jj <= ny) ? om[wb + jj] : T(0);
-            }
-            T g[6], gv;
-            weno_flux_grad<T>(q, Vm, (fl >> 4) & 7, j >= 1 && j <= ny - 2, j >= 2 && j <= ny - 3, g, gv);
-#pragma unroll
-            for (int k = 0; k < 6; ++k) {
-                const int jj = j - 2 + k;
-                if (jj >= 0 && jj <= ny && g[k] != T(0)) aadd(&adom[wb + jj], a * g[k]);
-            }
-            const T aVm = T(0.25) * a * (gv + t.fsu[ui]);
-            auto addV = [&](int p, int c) {
-                const long long k = (long long)p * (ny + 1) + c;
-                aadd(&adv[vb + k], aVm * t.idyv2[k]);
-            };
-            addV(i, j + 1);
-            addV(i, j);
-            addV(i - 1, j + 1);
-            addV(i - 1, j);
-            aadd(&adkp[ob * t.sh + ui], -a);
-            aadd(&adkp[ob * t.sh + ui - ny], a);
-            // reference pressure gradient and wind factor (H / h_wind cotangents)
-            if (t.ad_dxp && t.hxy_dxp) aadd(&t.ad_dxp[(long long)l * (nx - 1) * ny + (long long)(i - 1) * ny + j], -a);
-            if (t.ad_wfu && l == 0) aadd(&t.ad_wfu[ui], a * (taux ? taux : t.taux)[(long long)(i - 1) * ny + j]);
-            const long long ub = ob * t.su;
-            if (l == nl - 1) aadd(&adu[ub + ui], -t.drag * a);
-            if (t.visc > T(0)) {
-                const T ix2 = t.idxu2[ui], iy2 = t.idyu2[ui];
-                const T c = t.visc * t.dxu[ui] * a;
-                auto addu = [&](int p, int cc, T w) {
-                    cc = cc < 0 ? 0 : (cc > ny - 1 ? ny - 1 : cc);
-                    const long long k = (long long)p * ny + cc;
-                    aadd(&adu[ub + k], c * w * t.idxu[k]);
+        for (int k = 0; k < 6; ++k) w_s[k] = h_s[k] = T(0);
+        if (i >= 1 && i <= nx - 1) {
+            const int fl = t.fu[ui];
+            const T a = adk_u[so] * ((fl & 1) ? T(1) : T(0));
+            if (a != T(0)) {
+                const long long vb = ob * t.sv;
+                auto Vv = [&](int p, int c) {
+                    const long long k = (long long)p * (ny + 1) + c;
+                    return v[vb + k] * t.idyv2[k];
                 };
-                addu(i + 1, j, ix2);
-                addu(i - 1, j, ix2);
-                addu(i, j + 1, iy2);
-                addu(i, j - 1, iy2);
-                addu(i, j, -T(2) * ix2 - T(2) * iy2);
+                const T Vm = T(0.25) * (Vv(i, j + 1) + Vv(i, j) + Vv(i - 1, j + 1) + Vv(i - 1, j));
+                T q[6];
+                const long long wb = ob * t.sw + (long long)i * (ny + 1);
+#pragma unroll
+                for (int k = 0; k < 6; ++k) {
+                    const int jj = j - 2 + k;
+                    q[k] = (jj >= 0 && jj <= ny) ? om[wb + jj] : T(0);
+                }
+                T g[6], gv;
+                weno_flux_grad<T>(q, Vm, (fl >> 4) & 7, j >= 1 && j <= ny - 2, j >= 2 && j <= ny - 3, g, gv);
+#pragma unroll
+                for (int k = 0; k < 6; ++k) {
+                    const int jj = j - 2 + k;
+                    if (jj >= 0 && jj <= ny && g[k] != T(0)) w_s[k] = a * g[k];
+                }
+                vm_s = T(0.25) * a * (gv + t.fsu[ui]);
+                a_s = a;
+                // reference pressure gradient and wind factor (H / h_wind cotangents)
+                if (t.ad_dxp && t.hxy_dxp)
+                    aadd(&t.ad_dxp[(long long)l * (nx - 1) * ny + (long long)(i - 1) * ny + j], -a);
+                if (t.ad_wfu && l == 0) aadd(&t.ad_wfu[ui], a * (taux ? taux : t.taux)[(long long)(i - 1) * ny + j]);
+                if (t.visc > T(0)) c_s = t.visc * t.dxu[ui] * a;
+            }
+            // thickness flux through u face i: dt_h[c] = -div_x[c] * mask_h[c]
+            T aF = T(0);
+            if (i - 1 >= 1 && i - 1 <= nx - 2) aF -= mh((long long)(i - 1) * ny + j) * hb[(long long)(i - 1) * ny + j];
+            if (i >= 1 && i <= nx - 2) aF += mh(ui) * hb[ui];
+            if (aF != T(0)) {
+                const T iu2 = t.idxu2[ui];
+                const T Uf = u[so] * iu2;
+                T q[6];
+#pragma unroll
+                for (int k = 0; k < 6; ++k) {
+                    const int ii = i - 3 + k;
+                    q[k] = (ii >= 0 && ii < nx) ? ht[ob * t.sh + (long long)ii * ny + j] : T(0);
+                }
+                T g[6], gv;
+                weno_flux_grad<T>(q, Uf, (fl >> 1) & 7, i >= 2 && i <= nx - 2, i >= 3 && i <= nx - 3, g, gv);
+#pragma unroll
+                for (int k = 0; k < 6; ++k) {
+                    const int ii = i - 3 + k;
+                    if (ii >= 0 && ii < nx && g[k] != T(0)) h_s[k] = aF * g[k];
+                }
+                f_s = aF * gv * iu2;
             }
         }
-        // thickness flux through u face i: dt_h[c] = -div_x[c] * mask_h[c]
-        T aF = T(0);
-        if (i - 1 >= 1 && i - 1 <= nx - 2) aF -= mh((long long)(i - 1) * ny + j) * hb[(long long)(i - 1) * ny + j];
-        if (i >= 1 && i <= nx - 2) aF += mh(ui) * hb[ui];
-        if (aF != T(0)) {
-            const T iu2 = t.idxu2[ui];
-            const T Uf = u[ob * t.su + ui] * iu2;
-            T q[6];
+        S.ua[so] = a_s;
+        S.uvm[so] = vm_s;
+        S.uc[so] = c_s;
+        S.uf[so] = f_s;
 #pragma unroll
-            for (int k = 0; k < 6; ++k) {
-                const int ii = i - 3 + k;
-                q[k] = (ii >= 0 && ii < nx) ? ht[ob * t.sh + (long long)ii * ny + j] : T(0);
-            }
-            T g[6], gv;
-            weno_flux_grad<T>(q, Uf, (fl >> 1) & 7, i >= 2 && i <= nx - 2, i >= 3 && i <= nx - 3, g, gv);
-#pragma unroll
-            for (int k = 0; k < 6; ++k) {
-                const int ii = i - 3 + k;
-                if (ii >= 0 && ii < nx && g[k] != T(0)) aadd(&adht[ob * t.sh + (long long)ii * ny + j], aF * g[k]);
-            }
-            aadd(&adu[ob * t.su + ui], aF * gv * iu2);
+        for (int k = 0; k < 6; ++k) {
+            S.uw[k * S.nu + so] = w_s[k];
+            S.uh[k * S.nu + so] = h_s[k];
         }
     }
-    // ---------------- v point
-    if (i < nx && j >= 1 && j <= ny - 1) {
-        const long long vi = (long long)i * (ny + 1) + j;
-        const int fl = t.fv[vi];
-        const T a = adk_v[ob * t.sv + vi] * ((fl & 1) ? T(1) : T(0));
-        if (a != T(0)) {
-            const long long ub = ob * t.su;
-            auto Uu = [&](int p, int c) {
-                const long long k = (long long)p * ny + c;
-                return u[ub + k] * t.idxu2[k];
-            };
-            const T Um = T(0.25) * (Uu(i + 1, j) + Uu(i + 1, j - 1) + Uu(i, j) + Uu(i, j - 1));
-            T q[6];
+    // ---------------- v face (i, j)
+    if (i < nx) {
+        const long long vi = (long long)i * (ny + 1) + j, so = ob * t.sv + vi;
+        T a_s = T(0), um_s = T(0), c_s = T(0), f_s = T(0), w_s[6], h_s[6];
 #pragma unroll
-            for (int k = 0; k < 6; ++k) {
-                const int ii = i - 2 + k;
-                q[k] = (ii >= 0 && ii <= nx) ? om[ob * t.sw + (long long)ii * (ny + 1) + j] : T(0);
-            }
-            T g[6], gv;
-            weno_flux_grad<T>(q, Um, (fl >> 4) & 7, i >= 1 && i <= nx - 2, i >= 2 && i <= nx - 3, g, gv);
-#pragma unroll
-            for (int k = 0; k < 6; ++k) {
-                const int ii = i - 2 + k;
-                if (ii >= 0 && ii <= nx && g[k] != T(0)) aadd(&adom[ob * t.sw + (long long)ii * (ny + 1) + j], -a * g[k]);
-            }
-            const T aUm = -T(0.25) * a * (gv + t.fsv[vi]);
-            auto addU = [&](int p, int c) {
-                const long long k = (long long)p * ny + c;
-                aadd(&adu[ub + k], aUm * t.idxu2[k]);
-            };
-            addU(i + 1, j);
-            addU(i + 1, j - 1);
-            addU(i, j);
-            addU(i, j - 1);
-            const long long hi = (long long)i * ny + j;
-            aadd(&adkp[ob * t.sh + hi], -a);
-            aadd(&adkp[ob * t.sh + hi - 1], a);
-            if (t.ad_dyp && t.hxy_dyp) aadd(&t.ad_dyp[(long long)l * nx * (ny - 1) + (long long)i * (ny - 1) + j - 1], -a);
-            if (t.ad_wfv && l == 0) aadd(&t.ad_wfv[vi], a * (tauy ? tauy : t.tauy)[(long long)i * (ny - 1) + j - 1]);
-            const long long vb = ob * t.sv;
-            if (l == nl - 1) aadd(&adv[vb + vi], -t.drag * a);
-            if (t.visc > T(0)) {
-                const T ix2 = t.idxv2[vi], iy2 = t.idyv2[vi];
-                const T c = t.visc * t.dyv[vi] * a;
-                auto addv = [&](int p, int cc, T w) {
-                    p = p < 0 ? 0 : (p > nx - 1 ? nx - 1 : p);
-                    const long long k = (long long)p * (ny + 1) + cc;
-                    aadd(&adv[vb + k], c * w * t.idyv[k]);
+        for (int k = 0; k < 6; ++k) w_s[k] = h_s[k] = T(0);
+        if (j >= 1 && j <= ny - 1) {
+            const int fl = t.fv[vi];
+            const T a = adk_v[so] * ((fl & 1) ? T(1) : T(0));
+            if (a != T(0)) {
+                const long long ub = ob * t.su;
+                auto Uu = [&](int p, int c) {
+                    const long long k = (long long)p * ny + c;
+                    return u[ub + k] * t.idxu2[k];
                 };
-                addv(i + 1, j, ix2);
-                addv(i - 1, j, ix2);
-                addv(i, j + 1, iy2);
-                addv(i, j - 1, iy2);
-                addv(i, j, -T(2) * ix2 - T(2) * iy2);
+                const T Um = T(0.25) * (Uu(i + 1, j) + Uu(i + 1, j - 1) + Uu(i, j) + Uu(i, j - 1));
+                T q[6];
+#pragma unroll
+                for (int k = 0; k < 6; ++k) {
+                    const int ii = i - 2 + k;
+                    q[k] = (ii >= 0 && ii <= nx) ? om[ob * t.sw + (long long)ii * (ny + 1) + j] : T(0);
+                }
+                T g[6], gv;
+                weno_flux_grad<T>(q, Um, (fl >> 4) & 7, i >= 1 && i <= nx - 2, i >= 2 && i <= nx - 3, g, gv);
+#pragma unroll
+                for (int k = 0; k < 6; ++k) {
+                    const int ii = i - 2 + k;
+                    if (ii >= 0 && ii <= nx && g[k] != T(0)) w_s[k] = -a * g[k];
+                }
+                um_s = -T(0.25) * a * (gv + t.fsv[vi]);
+                a_s = a;
+                if (t.ad_dyp && t.hxy_dyp)
+                    aadd(&t.ad_dyp[(long long)l * nx * (ny - 1) + (long long)i * (ny - 1) + j - 1], -a);
+                if (t.ad_wfv && l == 0) aadd(&t.ad_wfv[vi], a * (tauy ? tauy : t.tauy)[(long long)i * (ny - 1) + j - 1]);
+                if (t.visc > T(0)) c_s = t.visc * t.dyv[vi] * a;
+            }
+            T aF = T(0);
+            const long long hj0 = (long long)i * ny + j - 1, hj1 = (long long)i * ny + j;
+            if (j - 1 >= 1 && j - 1 <= ny - 2) aF -= mh(hj0) * hb[hj0];
+            if (j >= 1 && j <= ny - 2) aF += mh(hj1) * hb[hj1];
+            if (aF != T(0)) {
+                const T iv2 = t.idyv2[vi];
+                const T Vf = v[so] * iv2;
+                T q[6];
+#pragma unroll
+                for (int k = 0; k < 6; ++k) {
+                    const int jj = j - 3 + k;
+                    q[k] = (jj >= 0 && jj < ny) ? ht[ob * t.sh + (long long)i * ny + jj] : T(0);
+                }
+                T g[6], gv;
+                weno_flux_grad<T>(q, Vf, (fl >> 1) & 7, j >= 2 && j <= ny - 2, j >= 3 && j <= ny - 3, g, gv);
+#pragma unroll
+                for (int k = 0; k < 6; ++k) {
+                    const int jj = j - 3 + k;
+                    if (jj >= 0 && jj < ny && g[k] != T(0)) h_s[k] = aF * g[k];
+                }
+                f_s = aF * gv * iv2;
             }
         }
-        T aF = T(0);
-        const long long hj0 = (long long)i * ny + j - 1, hj1 = (long long)i * ny + j;
-        if (j - 1 >= 1 && j - 1 <= ny - 2) aF -= mh(hj0) * hb[hj0];
-        if (j >= 1 && j <= ny - 2) aF += mh(hj1) * hb[hj1];
-        if (aF != T(0)) {
-            const T iv2 = t.idyv2[vi];
-            const T Vf = v[ob * t.sv + vi] * iv2;
-            T q[6];
+        S.va[so] = a_s;
+        S.vum[so] = um_s;
+        S.vc[so] = c_s;
+        S.vf[so] = f_s;
 #pragma unroll
-            for (int k = 0; k < 6; ++k) {
-                const int jj = j - 3 + k;
-                q[k] = (jj >= 0 && jj < ny) ? ht[ob * t.sh + (long long)i * ny + jj] : T(0);
-            }
-            T g[6], gv;
-            weno_flux_grad<T>(q, Vf, (fl >> 1) & 7, j >= 2 && j <= ny - 2, j >= 3 && j <= ny - 3, g, gv);
-#pragma unroll
-            for (int k = 0; k < 6; ++k) {
-                const int jj = j - 3 + k;
-                if (jj >= 0 && jj < ny && g[k] != T(0)) aadd(&adht[ob * t.sh + (long long)i * ny + jj], aF * g[k]);
-            }
-            aadd(&adv[ob * t.sv + vi], aF * gv * iv2);
+        for (int k = 0; k < 6; ++k) {
+            S.vw[k * S.nv + so] = w_s[k];
+            S.vh[k * S.nv + so] = h_s[k];
         }
     }
-    // ---------------- thickness diffusion
-    if (i < nx && j < ny && t.diff > T(0)) {
+    // ---------------- thickness diffusion coefficient at h (i, j)
+    if (i < nx && j < ny) {
         const long long hi = (long long)i * ny + j;
-        const T a = hb[hi] * mh(hi) * t.diff * t.area[hi];
-        if (a != T(0)) {
-            const T ix2 = t.idx2h[hi], iy2 = t.idy2h[hi];
-            auto addh = [&](int p, int c, T w) {
-                p = p < 0 ? 0 : (p > nx - 1 ? nx - 1 : p);
-                c = c < 0 ? 0 : (c > ny - 1 ? ny - 1 : c);
-                const long long k = (long long)p * ny + c;
-                aadd(&adh[ob * t.sh + k], a * w * t.iarea[k]);
-            };
-            addh(i + 1, j, ix2);
-            addh(i - 1, j, ix2);
-            addh(i, j + 1, iy2);
-            addh(i, j - 1, iy2);
-            addh(i, j, -T(2) * ix2 - T(2) * iy2);
+        S.hd[ob * t.sh + hi] = t.diff > T(0) ? hb[hi] * mh(hi) * t.diff * t.area[hi] : T(0);
+    }
+}
+
+// Pass 2: every target of the tendency adjoint sums the stored terms of its
+// sources. adom, adkp, adht are written (every index once); adu, adv, adh
+// are added to.
+template <typename T>
+__global__ void k_sw_tend_adj_gather(Tab<T> t, SwSrc<T> S, T* adom, T* adkp, T* adht, T* adu, T* adv, T* adh)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    const int bl = blockIdx.z;
+    const int nx = t.nx, ny = t.ny, nl = t.nl, l = bl % nl;
+    if (i > nx || j > ny) return;
+    const long long ob = bl;
+    // stored terms of u face (p, c) / v face (p, c); 0 outside the grid
+    auto U = [&](const T* A, int p, int c) {
+        return (p >= 0 && p <= nx && c >= 0 && c < ny) ? A[ob * t.su + (long long)p * ny + c] : T(0);
+    };
+    auto V = [&](const T* A, int p, int c) {
+        return (p >= 0 && p < nx && c >= 0 && c <= ny) ? A[ob * t.sv + (long long)p * (ny + 1) + c] : T(0);
+    };
+    // ---- vorticity point (i, j): u face (i, j+2-k) and v face (i+2-k, j) reach it with term k
+    {
+        T s = T(0);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) s += U(S.uw + k * S.nu, i, j + 2 - k);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) s += V(S.vw + k * S.nv, i + 2 - k, j);
+        adom[ob * t.sw + (long long)i * (ny + 1) + j] = s;
+    }
+    // ---- h point (i, j)
+    if (i < nx && j < ny) {
+        const long long hi = (long long)i * ny + j;
+        // KE + pressure: u faces i (-a) and i+1 (+a), v faces j (-a) and j+1 (+a)
+        adkp[ob * t.sh + hi] = (-U(S.ua, i, j) + U(S.ua, i + 1, j)) + (-V(S.va, i, j) + V(S.va, i, j + 1));
+        // thickness fluxes: u face (i+3-k, j) and v face (i, j+3-k) reach it with term k
+        T sh_ = T(0);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) sh_ += U(S.uh + k * S.nu, i + 3 - k, j);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) sh_ += V(S.vh + k * S.nv, i, j + 3 - k);
+        adht[ob * t.sh + hi] = sh_;
+        if (t.diff > T(0)) {
+            // the diffusion stencil of cell (p, c): (p+-1, c), (p, c+-1) clamped to the grid, and (p, c)
+            const T* D = S.hd + ob * t.sh;
+            const T ia = t.iarea[hi];
+            T s = T(0);
+            if (i >= 1) s += D[hi - ny] * t.idx2h[hi - ny] * ia;
+            if (i + 1 <= nx - 1) s += D[hi + ny] * t.idx2h[hi + ny] * ia;
+            if (j >= 1) s += D[hi - 1] * t.idy2h[hi - 1] * ia;
+            if (j + 1 <= ny - 1) s += D[hi + 1] * t.idy2h[hi + 1] * ia;
+            const T a0 = D[hi], ix2 = t.idx2h[hi], iy2 = t.idy2h[hi];
+            s += a0 * (-T(2) * ix2 - T(2) * iy2) * ia;
+            if (i == nx - 1) s += a0 * ix2 * ia;
+            if (i == 0) s += a0 * ix2 * ia;
+            if (j == ny - 1) s += a0 * iy2 * ia;
+            if (j == 0) s += a0 * iy2 * ia;
+            adh[ob * t.sh + hi] += s;
         }
+    }
+    // ---- u face (i, j)
+    if (j < ny) {
+        const long long ui = (long long)i * ny + j;
+        const T iu2 = t.idxu2[ui];
+        // U-average of the v faces (i-1, j), (i-1, j+1), (i, j), (i, j+1)
+        T s = V(S.vum, i - 1, j) * iu2 + V(S.vum, i - 1, j + 1) * iu2 + V(S.vum, i, j) * iu2 +
+              V(S.vum, i, j + 1) * iu2;
+        const T a0 = U(S.ua, i, j);
+        if (l == nl - 1) s += -t.drag * a0;
+        if (t.visc > T(0)) {
+            // viscosity stencil of u face (p, c): (p+-1, c), (p, c+-1) with c clamped, and (p, c)
+            const T id = t.idxu[ui];
+            if (i >= 1) s += U(S.uc, i - 1, j) * t.idxu2[ui - ny] * id;
+            if (i + 1 <= nx) s += U(S.uc, i + 1, j) * t.idxu2[ui + ny] * id;
+            if (j >= 1) s += U(S.uc, i, j - 1) * t.idyu2[ui - 1] * id;
+            if (j + 1 <= ny - 1) s += U(S.uc, i, j + 1) * t.idyu2[ui + 1] * id;
+            const T c0 = U(S.uc, i, j), ix2 = t.idxu2[ui], iy2 = t.idyu2[ui];
+            s += c0 * (-T(2) * ix2 - T(2) * iy2) * id;
+            if (j == ny - 1) s += c0 * iy2 * id;
+            if (j == 0) s += c0 * iy2 * id;
+        }
+        s += U(S.uf, i, j);
+        adu[ob * t.su + ui] += s;
+    }
+    // ---- v face (i, j)
+    if (i < nx) {
+        const long long vi = (long long)i * (ny + 1) + j;
+        const T iv2 = t.idyv2[vi];
+        // V-average of the u faces (i, j-1), (i, j), (i+1, j-1), (i+1, j)
+        T s = U(S.uvm, i, j - 1) * iv2 + U(S.uvm, i, j) * iv2 + U(S.uvm, i + 1, j - 1) * iv2 +
+              U(S.uvm, i + 1, j) * iv2;
+        const T a0 = V(S.va, i, j);
+        if (l == nl - 1) s += -t.drag * a0;
+        if (t.visc > T(0)) {
+            // viscosity stencil of v face (p, c): (p+-1, c) with p clamped, (p, c+-1), and (p, c)
+            const T id = t.idyv[vi];
+            if (i >= 1) s += V(S.vc, i - 1, j) * t.idxv2[vi - (ny + 1)] * id;
+            if (i + 1 <= nx - 1) s += V(S.vc, i + 1, j) * t.idxv2[vi + (ny + 1)] * id;
+            if (j >= 1) s += V(S.vc, i, j - 1) * t.idyv2[vi - 1] * id;
+            if (j + 1 <= ny) s += V(S.vc, i, j + 1) * t.idyv2[vi + 1] * id;
+            const T c0 = V(S.vc, i, j), ix2 = t.idxv2[vi], iy2 = t.idyv2[vi];
+            s += c0 * (-T(2) * ix2 - T(2) * iy2) * id;
+            if (i == nx - 1) s += c0 * ix2 * id;
+            if (i == 0) s += c0 * ix2 * id;
+        }
+        s += V(S.vf, i, j);
+        adv[ob * t.sv + vi] += s;
     }
 }
 
@@ -1891,6 +1993,32 @@ static bool take_uvh(Arena& ws, const Sizes& s, int B, Fields<T>& f)
     return f.u && f.v && f.h;
 }
 
+// Per-source buffers of the two-pass tendency adjoint (16 values per u and v
+// face, one per h point, every field of the batch).
+template <typename T>
+static bool take_src(Arena& ws, const Sizes& s, int B, SwSrc<T>& S)
+{
+    const long long nu = s.su * B, nv = s.sv * B, nh = s.sh * B;
+    T* b = (T*)ws.take(sizeof(T) * (size_t)(16 * nu + 16 * nv + nh));
+    if (!b) return false;
+    S.nu = nu;
+    S.nv = nv;
+    S.ua = b; b += nu;
+    S.uvm = b; b += nu;
+    S.uc = b; b += nu;
+    S.uf = b; b += nu;
+    S.uw = b; b += 6 * nu;
+    S.uh = b; b += 6 * nu;
+    S.va = b; b += nv;
+    S.vum = b; b += nv;
+    S.vc = b; b += nv;
+    S.vf = b; b += nv;
+    S.vw = b; b += 6 * nv;
+    S.vh = b; b += 6 * nv;
+    S.hd = b;
+    return true;
+}
+
 struct Launch {
     dim3 grid, block;
 };
@@ -2100,8 +2228,10 @@ extern "C" size_t vd_sw_workspace_bytes(const vd_sw_plan* p, int batch, int nste
     const size_t F3 = esz * (s.su + s.sv + s.sh) * batch + 3 * 256;
     const size_t wk = (esz == 8 ? work_bytes<double>(s, batch) : work_bytes<float>(s, batch));
     // inputs (x, xb, F), their tangents / adjoints, two work sets, adjoint
-    // accumulators, and the per-step trajectory
-    return 14 * F3 + 2 * wk + (size_t)nstep * F3 + esz * (s.sw + 2 * s.sh) * batch + 64 * 256;
+    // accumulators, the per-source buffers of the tendency adjoint, and the
+    // per-step trajectory
+    return 14 * F3 + 2 * wk + (size_t)nstep * F3 + esz * (s.sw + 2 * s.sh) * batch +
+           esz * (16 * s.su + 16 * s.sv + s.sh) * batch + 64 * 256;
 }
 
 namespace {
@@ -2155,18 +2285,16 @@ static int sw_tgl_t(vd_sw_plan* p, int B, const void* u0, const void* v0, const 
 // adjoint of one right-hand side at state x (model space): adk -> adx (+=)
 template <typename T>
 static int rhs_adj(vd_sw_plan* p, int B, Fields<T> x, Fields<T> adk, Fields<T> adx, Work<T>& wk, T* adom, T* adkp,
-                   T* adht, const T* taux, const T* tauy, cudaStream_t st)
+                   T* adht, const SwSrc<T>& src, const T* taux, const T* tauy, cudaStream_t st)
 {
     Tab<T>& t = tab<T>(p);
-    const Sizes s = sizes(p);
     const Launch Ld = lgrid(p, B), Ll = lgrid(p, B * p->nl);
     k_sw_diag<T, T><<<Ld.grid, Ld.block, 0, st>>>(t, rt(x), w(wk.om), w(wk.kp), w(wk.ht));
     VD_LAUNCH_CHECK();
-    VD_CUDA_TRY(cudaMemsetAsync(adom, 0, sizeof(T) * s.sw * B, st));
-    VD_CUDA_TRY(cudaMemsetAsync(adkp, 0, sizeof(T) * s.sh * B, st));
-    VD_CUDA_TRY(cudaMemsetAsync(adht, 0, sizeof(T) * s.sh * B, st));
-    k_sw_tend_adj<T><<<Ll.grid, Ll.block, 0, st>>>(t, x.u, x.v, x.h, wk.om, wk.ht, adk.u, adk.v, adk.h, adom, adkp,
-                                                    adht, adx.u, adx.v, adx.h, taux, tauy);
+    k_sw_tend_adj_src<T><<<Ll.grid, Ll.block, 0, st>>>(t, x.u, x.v, x.h, wk.om, wk.ht, adk.u, adk.v, adk.h, src,
+                                                        taux, tauy);
+    VD_LAUNCH_CHECK();
+    k_sw_tend_adj_gather<T><<<Ll.grid, Ll.block, 0, st>>>(t, src, adom, adkp, adht, adx.u, adx.v, adx.h);
     VD_LAUNCH_CHECK();
     k_sw_diag_adj<T><<<Ld.grid, Ld.block, 0, st>>>(t, x.u, x.v, x.h, adom, adkp, adht, adx.u, adx.v, adx.h);
     VD_LAUNCH_CHECK();
@@ -2196,7 +2324,8 @@ static int sw_adj_t(vd_sw_plan* p, int B, const void* u0, const void* v0, const 
     T* adom = (T*)ws.take(sizeof(T) * s.sw * B);
     T* adkp = (T*)ws.take(sizeof(T) * s.sh * B);
     T* adht = (T*)ws.take(sizeof(T) * s.sh * B);
-    if (!adom || !adkp || !adht) return VD_ERR_WORKSPACE;
+    SwSrc<T> src;
+    if (!adom || !adkp || !adht || !take_src(ws, s, B, src)) return VD_ERR_WORKSPACE;
     // forward sweep storing the state at the start of every step
     Fields<T> xr;
     if (!take_uvh(ws, s, B, xr)) return VD_ERR_WORKSPACE;
@@ -2263,8 +2392,8 @@ static int sw_adj_t(vd_sw_plan* p, int B, const void* u0, const void* v0, const 
             k_sw_update_adj<T><<<Ll.grid, Ll.block, 0, st>>>(t, stg, B * p->nl, ad.u, ad.v, ad.h, adk.u, adk.v, adk.h,
                                                              a0.u, a0.v, a0.h, a1.u, a1.v, a1.h, adb.u, adb.v, adb.h);
             VD_LAUNCH_CHECK();
-            if ((rc = rhs_adj<T>(p, B, stages[stg], adk, ad, wk, adom, adkp, adht, (const T*)taux, (const T*)tauy,
-                                 st)))
+            if ((rc = rhs_adj<T>(p, B, stages[stg], adk, ad, wk, adom, adkp, adht, src, (const T*)taux,
+                                 (const T*)tauy, st)))
                 return rc;
         }
     }
@@ -2424,9 +2553,10 @@ static int sw_rhs_adj_t(vd_sw_plan* p, int B, const void* u, const void* v, cons
     T* adom = (T*)ws.take(sizeof(T) * s.sw * B);
     T* adkp = (T*)ws.take(sizeof(T) * s.sh * B);
     T* adht = (T*)ws.take(sizeof(T) * s.sh * B);
-    if (!adom || !adkp || !adht) return VD_ERR_WORKSPACE;
+    SwSrc<T> src;
+    if (!adom || !adkp || !adht || !take_src(ws, s, B, src)) return VD_ERR_WORKSPACE;
     Fields<T> x{(T*)u, (T*)v, (T*)h}, ak{(T*)aku, (T*)akv, (T*)akh}, ad{(T*)adu, (T*)adv, (T*)adh};
-    return rhs_adj<T>(p, B, x, ak, ad, wk, adom, adkp, adht, nullptr, nullptr, st);
+    return rhs_adj<T>(p, B, x, ak, ad, wk, adom, adkp, adht, src, nullptr, nullptr, st);
 }
 
 // elementwise stage combination: k = rhs + sponge; stage 0/1 store k
