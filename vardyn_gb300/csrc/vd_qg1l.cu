@@ -23,6 +23,10 @@ namespace vd {
 
 template <typename T> __device__ __forceinline__ T guard0(T x) { return isnan(x) ? T(0) : x; }
 
+// Plans without diffusion, bathymetry and beta run the stage kernels
+// compiled without those terms.
+static inline bool plain_geom(const QGGeom& G) { return !G.hasK && !G.fB && !G.beta; }
+
 // Round-to-nearest add / subtract that the compiler neither contracts nor
 // reassociates (the error-free transformations below rely on it).
 __device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
@@ -85,8 +89,9 @@ struct Vel {
     }
 };
 
-// Raw PV tendency at an M3 point from velocities and PV crosses.
-template <typename T>
+// Raw PV tendency at an M3 point from velocities and PV crosses. MAYK false:
+// the caller knows the plan has no diffusion.
+template <typename T, bool MAYK = true>
 __device__ __forceinline__ T tendency(const QGGeom& G, const Vel<T>& V, const Cross<T>& qa,
                                       const Cross<T>& q, T beta)
 {
@@ -99,7 +104,7 @@ __device__ __forceinline__ T tendency(const QGGeom& G, const Vel<T>& V, const Cr
     const T cx = T(G.cx), cy = T(G.cy);
     T r = -up * cx * qa.Dpx() + um * cx * qa.Dmx() - vp * cy * qa.Dpy() + vm * cy * qa.Dmy();
     r -= beta * ((V.v0 + V.v1) / T(2));
-    if (G.hasK)
+    if (MAYK && G.hasK)
         r += T(G.Kx) * (q.e1 + q.w1 - T(2) * q.c) + T(G.Ky) * (q.n1 + q.s1 - T(2) * q.c);
     return r;
 }
@@ -204,8 +209,9 @@ struct StageIn {
     int nk;
 };
 
-// One point's PV tendency, loading its own stencil (M3 points only).
-template <typename T>
+// One point's PV tendency, loading its own stencil (M3 points only). PLAIN:
+// the plan has no diffusion, bathymetry or beta term.
+template <typename T, bool PLAIN = false>
 __device__ __forceinline__ T stage_point(const QGGeom& G, const T* __restrict__ hs, const T* __restrict__ qs,
                                          long long o, long long go)
 {
@@ -215,9 +221,9 @@ __device__ __forceinline__ T stage_point(const QGGeom& G, const T* __restrict__ 
     Cross<T> q;
     q.load(qs + o, G.nx);
     Cross<T> qa = q;
-    if (G.fB) { Cross<T> b; b.load((const T*)G.fB + go, G.nx); qa.add(b); }
-    const T beta = G.beta ? ((const T*)G.beta)[go] : T(0);
-    return guard0(tendency<T>(G, V, qa, q, beta));
+    if (!PLAIN && G.fB) { Cross<T> b; b.load((const T*)G.fB + go, G.nx); qa.add(b); }
+    const T beta = (!PLAIN && G.beta) ? ((const T*)G.beta)[go] : T(0);
+    return guard0(tendency<T, !PLAIN>(G, V, qa, q, beta));
 }
 
 // The PV crosses of the points (j, i) and (j+1, i) from one column of six
@@ -238,7 +244,7 @@ __device__ __forceinline__ void cross_pair(const T* __restrict__ p, int nx, Cros
 // cover 32 x 8 points): when both are M3 points their SSH and PV stencils
 // overlap, so the pair is loaded once (12 + 14 values instead of 16 + 18) and
 // each point then runs the same arithmetic as a single point.
-template <typename T>
+template <typename T, bool PLAIN>
 __global__ void k_stage_fwd(QGGeom G, int nf, const T* __restrict__ hs, const T* __restrict__ qs,
                             const T* __restrict__ qbase, StageIn<T> kin, T cself,
                             T* __restrict__ kout, T* __restrict__ qout, T* __restrict__ qlo, int last)
@@ -265,7 +271,7 @@ __global__ void k_stage_fwd(QGGeom G, int nf, const T* __restrict__ hs, const T*
         cross_pair(qs + o, nx, q[0], q[1]);
         qa[0] = q[0];
         qa[1] = q[1];
-        if (G.fB) {
+        if (!PLAIN && G.fB) {
             Cross<T> b[2];
             cross_pair((const T*)G.fB + go, nx, b[0], b[1]);
             qa[0].add(b[0]);
@@ -275,12 +281,12 @@ __global__ void k_stage_fwd(QGGeom G, int nf, const T* __restrict__ hs, const T*
         for (int u = 0; u < 2; ++u) {
             V[u].u0 = guard0(V[u].u0); V[u].u1 = guard0(V[u].u1);
             V[u].v0 = guard0(V[u].v0); V[u].v1 = guard0(V[u].v1);
-            const T beta = G.beta ? ((const T*)G.beta)[go + u * nx] : T(0);
-            r[u] = guard0(tendency<T>(G, V[u], qa[u], q[u], beta));
+            const T beta = (!PLAIN && G.beta) ? ((const T*)G.beta)[go + u * nx] : T(0);
+            r[u] = guard0(tendency<T, !PLAIN>(G, V[u], qa[u], q[u], beta));
         }
     } else {
-        if (m0 == 3) r[0] = stage_point(G, hs, qs, o, go);
-        if (m1 == 3) r[1] = stage_point(G, hs, qs, o + nx, go + nx);
+        if (m0 == 3) r[0] = stage_point<T, PLAIN>(G, hs, qs, o, go);
+        if (m1 == 3) r[1] = stage_point<T, PLAIN>(G, hs, qs, o + nx, go + nx);
     }
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
@@ -538,7 +544,8 @@ __device__ __forceinline__ void tma_tile_2d(uint32_t dst, const CUtensorMap* map
 }
 
 // Four CTAs per SM in float32 (shared memory allows four), two in float64.
-template <typename T, bool TMA>
+// PLAIN: the plan has no diffusion, bathymetry or beta term (compiled out).
+template <typename T, bool TMA, bool PLAIN>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2)
 k_adj_stage_fused(QGGeom G, int nf, const T* __restrict__ hs, const T* __restrict__ qs, StageIn<T> gin,
                   StageIn<T> gacc, T* __restrict__ adq_out, T* __restrict__ adh_out, const __grid_constant__ AdjMaps M)
@@ -546,9 +553,9 @@ k_adj_stage_fused(QGGeom G, int nf, const T* __restrict__ hs, const T* __restric
     extern __shared__ unsigned char smem_dyn[];
     __shared__ __align__(8) uint64_t tbar;
     unsigned char* smem_raw = (unsigned char*)(((uintptr_t)smem_dyn + 127) & ~(uintptr_t)127);
-    const bool hasB = G.fB != nullptr;
-    const bool hasK = G.hasK != 0;
-    const bool hasBeta = G.beta != nullptr;
+    const bool hasB = !PLAIN && G.fB != nullptr;
+    const bool hasK = !PLAIN && G.hasK != 0;
+    const bool hasBeta = !PLAIN && G.beta != nullptr;
     const AdjLayout L = adj_layout((int)sizeof(T), hasK, hasB, TMA, gin.nk, hasBeta);
     const AdjSmem<T> S = adj_smem<T>(smem_raw, L, hasK, hasB);
     const int f = blockIdx.z;
@@ -668,7 +675,7 @@ k_adj_stage_fused(QGGeom G, int nf, const T* __restrict__ hs, const T* __restric
                     if (t < gin.nk && in) lk += gin.c[t] * gin.k[t][o];
                 lkv[k][u] = lk;
                 m3a[k][u] = in && G.mask[g2] == 3;
-                bev[k][u] = (in && G.beta) ? ((const T*)G.beta)[g2] : T(0);
+                bev[k][u] = (in && hasBeta) ? ((const T*)G.beta)[g2] : T(0);
             }
         }
     }
@@ -734,7 +741,7 @@ k_adj_stage_fused(QGGeom G, int nf, const T* __restrict__ hs, const T* __restric
                     qa.n1 = vqa[3 + u]; qa.n2 = vqa[4 + u]; qa.s1 = vqa[1 + u]; qa.s2 = vqa[u];
                 }
                 const T beta = bev[k][u];
-                if (isnan(tendency<T>(G, V, qa, q, beta))) lk[u] = T(0);
+                if (isnan(tendency<T, !PLAIN>(G, V, qa, q, beta))) lk[u] = T(0);
                 uT[u] = T(0.5) * (V.u0 + V.u1);
                 vT[u] = T(0.5) * (V.v0 + V.v1);
                 const T gu = (uT[u] >= T(0) ? -cx * qa.Dpx() : T(0)) + (uT[u] <= T(0) ? cx * qa.Dmx() : T(0));
@@ -905,10 +912,17 @@ static cudaError_t adj_stage_attrs()
     static PerDeviceOnce once;
     return once.run([]() -> cudaError_t {
         const int big = (int)adj_layout(sizeof(T), true, true, true, 4, true).total + 128;
-        cudaError_t e = cudaFuncSetAttribute(k_adj_stage_fused<T, true>,
+        cudaError_t e = cudaFuncSetAttribute(k_adj_stage_fused<T, true, false>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, big);
         if (!e)
-            e = cudaFuncSetAttribute(k_adj_stage_fused<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+            e = cudaFuncSetAttribute(k_adj_stage_fused<T, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     big);
+        if (!e)
+            e = cudaFuncSetAttribute(k_adj_stage_fused<T, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     big);
+        if (!e)
+            e = cudaFuncSetAttribute(k_adj_stage_fused<T, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     big);
         return e;
     });
 }
@@ -927,10 +941,15 @@ static int launch_adj_stage(const vd_qg1l_plan* p, int nf, const T* hs, const T*
     std::memset(&M, 0, sizeof(M));
     const bool tma = adj_tma_maps<T>(p, nf, hs, qs, gin, M);
     const size_t smem = adj_layout(sizeof(T), G.hasK != 0, G.fB != nullptr, tma, gin.nk, G.beta != nullptr).total + 128;
-    if (tma)
-        k_adj_stage_fused<T, true><<<agrid, block, smem, st>>>(G, nf, hs, qs, gin, gacc, adq_out, adh_out, M);
+    const bool plain = plain_geom(G);
+    if (tma && plain)
+        k_adj_stage_fused<T, true, true><<<agrid, block, smem, st>>>(G, nf, hs, qs, gin, gacc, adq_out, adh_out, M);
+    else if (tma)
+        k_adj_stage_fused<T, true, false><<<agrid, block, smem, st>>>(G, nf, hs, qs, gin, gacc, adq_out, adh_out, M);
+    else if (plain)
+        k_adj_stage_fused<T, false, true><<<agrid, block, smem, st>>>(G, nf, hs, qs, gin, gacc, adq_out, adh_out, M);
     else
-        k_adj_stage_fused<T, false><<<agrid, block, smem, st>>>(G, nf, hs, qs, gin, gacc, adq_out, adh_out, M);
+        k_adj_stage_fused<T, false, false><<<agrid, block, smem, st>>>(G, nf, hs, qs, gin, gacc, adq_out, adh_out, M);
     VD_LAUNCH_CHECK();
     return VD_OK;
 }
@@ -1104,9 +1123,12 @@ static int step_once(const vd_qg1l_plan* p, int nf, T* const* hsv, T* const* qsv
         if (tangent)
             k_stage_tl<T><<<pgrid(p, B), kBlock, 0, st>>>(p->geom, B, hsv[s], qsv[s], qsv[0], kin, cself, kout, qo,
                                                           qlo, last ? 1 : 0);
+        else if (plain_geom(p->geom))
+            k_stage_fwd<T, true><<<pgrid(p, nf), dim3(32, 4), 0, st>>>(p->geom, nf, hsv[s], qsv[s], qsv[0], kin, cself,
+                                                                       kout, qo, qlo, last ? 1 : 0);
         else
-            k_stage_fwd<T><<<pgrid(p, nf), dim3(32, 4), 0, st>>>(p->geom, nf, hsv[s], qsv[s], qsv[0], kin, cself, kout,
-                                                                 qo, qlo, last ? 1 : 0);
+            k_stage_fwd<T, false><<<pgrid(p, nf), dim3(32, 4), 0, st>>>(p->geom, nf, hsv[s], qsv[s], qsv[0], kin,
+                                                                        cself, kout, qo, qlo, last ? 1 : 0);
         VD_LAUNCH_CHECK();
         SolveArgs a;
         a.src = qo; a.sub = qb; a.sub_batches = B;
@@ -1236,8 +1258,12 @@ int rk_stage_impl(const vd_qg1l_plan* p, int nf, const T* hs, const T* qs, const
     StageIn<T> kin{};
     kin.nk = nk;
     for (int t = 0; t < nk; ++t) { kin.k[t] = k[t]; kin.c[t] = (T)c[t]; }
-    k_stage_fwd<T><<<pgrid(p, nf), dim3(32, 4), 0, st>>>(p->geom, nf, hs, qs, qbase, kin, (T)cself, kout, qout,
-                                                         (T*)nullptr, 0);
+    if (plain_geom(p->geom))
+        k_stage_fwd<T, true><<<pgrid(p, nf), dim3(32, 4), 0, st>>>(p->geom, nf, hs, qs, qbase, kin, (T)cself, kout,
+                                                                   qout, (T*)nullptr, 0);
+    else
+        k_stage_fwd<T, false><<<pgrid(p, nf), dim3(32, 4), 0, st>>>(p->geom, nf, hs, qs, qbase, kin, (T)cself, kout,
+                                                                    qout, (T*)nullptr, 0);
     VD_LAUNCH_CHECK();
     return VD_OK;
 }
