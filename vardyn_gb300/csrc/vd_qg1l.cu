@@ -545,11 +545,15 @@ __device__ __forceinline__ void tma_tile_2d(uint32_t dst, const CUtensorMap* map
 
 // Four CTAs per SM in float32 (shared memory allows four), two in float64.
 // PLAIN: the plan has no diffusion, bathymetry or beta term (compiled out).
-template <typename T, bool TMA, bool PLAIN>
+// NG / NA >= 0: the numbers of stage adjoints and accumulated adjoints, known
+// at compile time (the RK2 stages' forms); -1: read from gin / gacc.
+template <typename T, bool TMA, bool PLAIN, int NG = -1, int NA = -1>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2)
 k_adj_stage_fused(QGGeom G, int nf, const T* __restrict__ hs, const T* __restrict__ qs, StageIn<T> gin,
                   StageIn<T> gacc, T* __restrict__ adq_out, T* __restrict__ adh_out, const __grid_constant__ AdjMaps M)
 {
+    if constexpr (NG >= 0) gin.nk = NG;
+    if constexpr (NA >= 0) gacc.nk = NA;
     extern __shared__ unsigned char smem_dyn[];
     __shared__ __align__(8) uint64_t tbar;
     unsigned char* smem_raw = (unsigned char*)(((uintptr_t)smem_dyn + 127) & ~(uintptr_t)127);
@@ -923,6 +927,12 @@ static cudaError_t adj_stage_attrs()
         if (!e)
             e = cudaFuncSetAttribute(k_adj_stage_fused<T, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      big);
+        if (!e)
+            e = cudaFuncSetAttribute(k_adj_stage_fused<T, true, true, 1, 0>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+        if (!e)
+            e = cudaFuncSetAttribute(k_adj_stage_fused<T, true, true, 2, 2>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, big);
         return e;
     });
 }
@@ -942,7 +952,15 @@ static int launch_adj_stage(const vd_qg1l_plan* p, int nf, const T* hs, const T*
     const bool tma = adj_tma_maps<T>(p, nf, hs, qs, gin, M);
     const size_t smem = adj_layout(sizeof(T), G.hasK != 0, G.fB != nullptr, tma, gin.nk, G.beta != nullptr).total + 128;
     const bool plain = plain_geom(G);
-    if (tma && plain)
+    // the two stage forms of RK2 (s = 1: one stage adjoint; s = 0: two, plus
+    // the two accumulated adjoints) with their counts compiled in
+    if (tma && plain && gin.nk == 1 && gacc.nk == 0)
+        k_adj_stage_fused<T, true, true, 1, 0><<<agrid, block, smem, st>>>(G, nf, hs, qs, gin, gacc, adq_out, adh_out,
+                                                                           M);
+    else if (tma && plain && gin.nk == 2 && gacc.nk == 2)
+        k_adj_stage_fused<T, true, true, 2, 2><<<agrid, block, smem, st>>>(G, nf, hs, qs, gin, gacc, adq_out, adh_out,
+                                                                           M);
+    else if (tma && plain)
         k_adj_stage_fused<T, true, true><<<agrid, block, smem, st>>>(G, nf, hs, qs, gin, gacc, adq_out, adh_out, M);
     else if (tma)
         k_adj_stage_fused<T, true, false><<<agrid, block, smem, st>>>(G, nf, hs, qs, gin, gacc, adq_out, adh_out, M);
