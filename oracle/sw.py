@@ -206,6 +206,23 @@ class SWOracle:
         self.sponge_h = np.zeros((nx, ny))
         self.forcing_momentum = param.get("forcing_momentum", "direct")
         self.H = np.asarray(param["H"], dtype=np.float64)
+        # barotropic filter, spectral form (sw.py:305-320): a Neumann Helmholtz
+        # solve diagonalised by one DCT-II per direction (helmholtz.py:20-87)
+        self.barotropic_filter = bool(param.get("barotropic_filter", False))
+        if self.barotropic_filter:
+            if not param.get("barotropic_filter_spectral", False):
+                raise NotImplementedError("the exact (multigrid) barotropic filter is work in progress in the "
+                                          "reference (sw.py:712-719)")
+            if np.any(self.masks.h < 0.5):
+                raise NotImplementedError("the reference's spectral filter solver does not construct with land "
+                                          "(helmholtz.py:254 divides a face-grid difference by the [nx, ny] "
+                                          "spacing)")
+            self.tau = 2 * self.dt
+            self.g = float(self.gp.reshape(-1)[0])
+            lambd = 1.0 / (self.g * self.dt * self.tau * self.H.sum(axis=-3, keepdims=True))
+            xg, yg = np.meshgrid(np.arange(nx, dtype=np.float64), np.arange(ny, dtype=np.float64), indexing="ij")
+            self.helm_dct = (2 * (np.cos(np.pi / nx * xg) - 1) / self.dx ** 2
+                             + 2 * (np.cos(np.pi / ny * yg) - 1) / self.dy ** 2) - lambd
 
     # reference values (sw.py:385-410), as functions of H_total
     def ref_values(self, H):
@@ -217,6 +234,29 @@ class SWOracle:
         dxp = np.diff(p_ref, axis=-2) if H.shape[-2] != 1 else 0.0
         dyp = np.diff(p_ref, axis=-1) if H.shape[-1] != 1 else 0.0
         return h_ref, h_ref_u, h_ref_v, dxp, dyp
+
+    # ---- barotropic filter, spectral form (sw.py:695-725) ----
+    def neumann_solve(self, rhs):
+        """HelmholtzNeumannSolver.solve without land (helmholtz.py:80-86,
+        296-303): unnormalised DCT-II along y then x, division by the
+        operator's eigenvalues, the inverse transforms."""
+        import scipy.fft as sf
+        r = sf.dct(sf.dct(rhs, type=2, axis=-1), type=2, axis=-2)
+        return sf.idct(sf.idct(r / self.helm_dct, type=2, axis=-1), type=2, axis=-2)
+
+    def filter_barotropic(self, du, dv, dh, u, v, htu, htv):
+        m = self.masks
+        us = (u + self.dt * du) / self.dx_u
+        vs = (v + self.dt * dv) / self.dy_v
+        ub = (us * htu).sum(axis=-3, keepdims=True) / htu.sum(axis=-3, keepdims=True)
+        vb = (vs * htv).sum(axis=-3, keepdims=True) / htv.sum(axis=-3, keepdims=True)
+        rhs = 1.0 / (self.g * self.dt * self.tau) * (np.diff(ub, axis=-2) / self.dx + np.diff(vb, axis=-1) / self.dy)
+        w = self.neumann_solve(rhs)
+        pad_u = [(0, 0)] * (w.ndim - 2) + [(1, 1), (0, 0)]
+        pad_v = [(0, 0)] * (w.ndim - 2) + [(0, 0), (1, 1)]
+        fu = np.pad(-self.g * self.tau * np.diff(w, axis=-2), pad_u) * m.u
+        fv = np.pad(-self.g * self.tau * np.diff(w, axis=-1), pad_v) * m.v
+        return du + fu, dv + fv, dh
 
     def to_model(self, u, v, h):
         m = self.masks
@@ -259,8 +299,8 @@ class SWOracle:
         return wu, wv
 
     def rhs(self, u, v, h, refv, taux, tauy):
-        """compute_time_derivatives (sw.py:720-750) without the barotropic
-        filter."""
+        """compute_time_derivatives (sw.py:727-750), with the spectral
+        barotropic filter when the model has it."""
         m = self.masks
         h_ref, _, _, dxp, dyp = refv
         om = self.omega(u, v)
@@ -311,7 +351,15 @@ class SWOracle:
             dv = dv + self.visc * lv * dyv
         pad_u = [(0, 0)] * (du.ndim - 2) + [(1, 1), (0, 0)]
         pad_v = [(0, 0)] * (dv.ndim - 2) + [(0, 0), (1, 1)]
-        return np.pad(du, pad_u) * m.u, np.pad(dv, pad_v) * m.v, dth
+        du, dv = np.pad(du, pad_u) * m.u, np.pad(dv, pad_v) * m.v
+        if self.barotropic_filter:
+            # total thickness on the faces (sw.py:688-692)
+            _, h_ref_u, h_ref_v, _, _ = refv
+            hu, hv = self._h_on_uv(h)
+            htu = smooth_clamp(h_ref_u + hu, self.h_min * self.area_u, self.sharp)
+            htv = smooth_clamp(h_ref_v + hv, self.h_min * self.area_v, self.sharp)
+            du, dv, dth = self.filter_barotropic(du, dv, dth, u, v, htu, htv)
+        return du, dv, dth
 
     def _h_on_uv(self, h):
         """replicate_pad then face averages (sw.py:36-48, 711-713)."""
