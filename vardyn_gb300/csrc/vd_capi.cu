@@ -147,9 +147,8 @@ extern "C" vd_status vd_qg1l_plan_create(vd_qg1l_plan** out, const vd_qg1l_desc*
     if (d->time_scheme < VD_EULER || d->time_scheme > VD_RK4) return VD_ERR_ARG;
     if (d->dst_engine != VD_DST_AUTO && d->dst_engine != VD_DST_FMA) return VD_ERR_ARG;
     if (!(d->dx > 0) || !(d->dy > 0) || !(d->f != 0) || !(d->c > 0) || !(d->g != 0)) return VD_ERR_ARG;
-    vd_qg1l_plan* p = new (std::nothrow) vd_qg1l_plan();
+    vd_qg1l_plan* p = new (std::nothrow) vd_qg1l_plan();   // value-initialised: every member zero
     if (!p) return VD_ERR_ARG;
-    std::memset(p, 0, sizeof(*p));
     p->d = *d;
     p->d.mask_host = nullptr;
     p->d.beta_host = nullptr;
