@@ -931,7 +931,7 @@ static cudaError_t adj_stage_attrs()
             e = cudaFuncSetAttribute(k_adj_stage_fused<T, true, true, 1, 0>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, big);
         if (!e)
-            e = cudaFuncSetAttribute(k_adj_stage_fused<T, true, true, 2, 2>,
+            e = cudaFuncSetAttribute(k_adj_stage_fused<T, true, true, 1, 2>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, big);
         return e;
     });
@@ -952,13 +952,14 @@ static int launch_adj_stage(const vd_qg1l_plan* p, int nf, const T* hs, const T*
     const bool tma = adj_tma_maps<T>(p, nf, hs, qs, gin, M);
     const size_t smem = adj_layout(sizeof(T), G.hasK != 0, G.fB != nullptr, tma, gin.nk, G.beta != nullptr).total + 128;
     const bool plain = plain_geom(G);
-    // the two stage forms of RK2 (s = 1: one stage adjoint; s = 0: two, plus
-    // the two accumulated adjoints) with their counts compiled in
+    // the two stage forms of RK2 (midpoint: b = (0, dt); s = 1: one stage
+    // adjoint; s = 0: one, plus the two accumulated adjoints) with their
+    // counts compiled in
     if (tma && plain && gin.nk == 1 && gacc.nk == 0)
         k_adj_stage_fused<T, true, true, 1, 0><<<agrid, block, smem, st>>>(G, nf, hs, qs, gin, gacc, adq_out, adh_out,
                                                                            M);
-    else if (tma && plain && gin.nk == 2 && gacc.nk == 2)
-        k_adj_stage_fused<T, true, true, 2, 2><<<agrid, block, smem, st>>>(G, nf, hs, qs, gin, gacc, adq_out, adh_out,
+    else if (tma && plain && gin.nk == 1 && gacc.nk == 2)
+        k_adj_stage_fused<T, true, true, 1, 2><<<agrid, block, smem, st>>>(G, nf, hs, qs, gin, gacc, adq_out, adh_out,
                                                                            M);
     else if (tma && plain)
         k_adj_stage_fused<T, true, true><<<agrid, block, smem, st>>>(G, nf, hs, qs, gin, gacc, adq_out, adh_out, M);
