@@ -677,6 +677,31 @@ vd_status vd_cmm_correct(int dtype, int nsys, int nper, int M, long long field_e
                          const void* rhs, void* out, void* stream);
 
 /* ------------------------------------------------------------------------
+ * Spectral Helmholtz solve with Neumann boundaries on a rectangular domain
+ * (mapping/models/model_qgsw/helmholtz.py HelmholtzNeumannSolver, 187-303,
+ * on an all-ocean mask: the solve is its G alone, solve_helmholtz_dctII
+ * 81-87). Fields are [nfield][nx][ny], y contiguous.
+ * ---------------------------------------------------------------------- */
+typedef struct vd_neumann_plan vd_neumann_plan;
+/* HelmholtzNeumannSolver(nx, ny, dx, dy, lambd, dtype) (187-225): the
+ * operator's DCT-II eigenvalues compute_laplace_dctII(nx, ny, dx, dy) -
+ * lambd (22-30) at every point of [nx][ny], dx and dy scalars (element [0])
+ * or [nx][ny] fields (dxy_spatial != 0), lambd a scalar or a [nx][ny] field
+ * (lambd_spatial != 0), as the reference broadcasts them. VD_ERR_UNSUPPORTED
+ * when a transform does not fit shared memory (nx or ny above 6400 in
+ * float64, 12800 in float32), VD_ERR_ARG for a zero or non-finite
+ * eigenvalue. */
+vd_status vd_neumann_plan_create(vd_neumann_plan** out, int nx, int ny, int dtype,
+                                 const double* dx_host, const double* dy_host, int dxy_spatial,
+                                 const double* lambd_host, int lambd_spatial);
+void vd_neumann_plan_destroy(vd_neumann_plan* plan);
+/* HelmholtzNeumannSolver.solve (296-303): out = idctII2D(dctII2D(rhs) /
+ * helm) (unnormalised DCT-II pair along each axis, 33-78) for nfield fields
+ * of the plan's dtype; out may equal rhs. No workspace. */
+vd_status vd_neumann_solve(const vd_neumann_plan* plan, int nfield, const void* rhs, void* out,
+                           void* stream);
+
+/* ------------------------------------------------------------------------
  * Multilayer rotating shallow-water model (mapping/models/model_qgsw/sw.py
  * SW with masks.py, flux.py, reconstruction.py, finite_diff.py).
  * Layout is the reference's: [batch][layer][x][y], y contiguous; u fields
@@ -717,6 +742,15 @@ typedef struct vd_sw_desc {
     const double* Hwind_host;     /* h_wind_mode 0: the layer-0 thickness [nx][ny] the wind
                                      depth is taken from (sw.py:622-630 read the model's
                                      own H, not a perturbed one); NULL = this plan's H */
+    int barotropic_filter;        /* 0 off; 1 the spectral barotropic filter of every
+                                     right-hand side (sw.py:305-320, 720-750): an
+                                     all-ocean mask only (VD_ERR_UNSUPPORTED otherwise, as
+                                     the reference's solver does not construct with land) */
+    const double* bf_lambd_host;  /* the filter's lambd = 1 / (g' dt tau H_tot)
+                                     (sw.py:316-317, the model's own H, not a perturbed
+                                     one): a scalar or, with bf_lambd_spatial, [nx][ny];
+                                     NULL = from this plan's H */
+    int bf_lambd_spatial;
 } vd_sw_desc;
 
 /* Host-only: the flag bytes of the staggered masks (masks.py:57-158).

@@ -132,6 +132,7 @@ class VdSwDesc(ctypes.Structure):
         ("taux_scalar", ctypes.c_double), ("tauy_scalar", ctypes.c_double),
         ("taux_host", _DP), ("tauy_host", _DP),
         ("sponge_u_host", _DP), ("sponge_v_host", _DP), ("sponge_h_host", _DP), ("Hwind_host", _DP),
+        ("barotropic_filter", ctypes.c_int), ("bf_lambd_host", _DP), ("bf_lambd_spatial", ctypes.c_int),
     ]
 
 
@@ -235,6 +236,9 @@ SIGNATURES = {
     "vd_fill": (I, [I, LL, D, P, P]),
     "vd_edge_pad": (I, [I, I, I, I, P, P, P, P]),
     "vd_cmm_correct": (I, [I, I, I, I, LL, P, P, P, P, P, P]),
+    "vd_neumann_plan_create": (I, [ctypes.POINTER(P), I, I, I, P, P, I, P, I]),
+    "vd_neumann_plan_destroy": (None, [P]),
+    "vd_neumann_solve": (I, [P, I, P, P, P]),
     "vd_sw_masks": (I, [I, I, P, P, P, P, P]),
     "vd_sw_plan_create": (I, [ctypes.POINTER(P), ctypes.POINTER(VdSwDesc)]),
     "vd_sw_plan_destroy": (None, [P]),

@@ -121,6 +121,9 @@ bool tc_fits(const vd_qg1l_plan* p, int nf);
 // Whether the tensor-core pass runs for nf fields under the plan's schedule.
 inline bool use_tc(const vd_qg1l_plan* p, int nf) { return p->dst.tc && tc_fits(p, nf) && p->sched.engine != 1; }
 int dst_pass_tc(const vd_qg1l_plan* p, int nf, const SolveArgs& a, float* spec, bool fwd, cudaStream_t st);
+// Neumann spectral Helmholtz solve of nf [nx][ny] fields (dst may equal src).
+template <typename T>
+int neumann_solve(const vd_neumann_plan* p, int nf, const T* src, T* dst, cudaStream_t st);
 // ORs the stencil-tile error bits (8: a tile's bulk copies did not arrive)
 // into *flags; reset != 0 clears them.
 int qg_tile_error(int* flags, int reset);

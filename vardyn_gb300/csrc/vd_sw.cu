@@ -401,6 +401,7 @@ struct Tab {
     T G[MAXL];                    // G[l] = sum_{k<=l} g'_k
     T gp[MAXL];
     T drag, visc, diff, hmin, sharp, dt;
+    T bf_c, bf_gt;                // barotropic filter: 1 / (g dt tau), g tau
     int linear, has_sponge, hxy_dxp, hxy_dyp;
 };
 
@@ -1373,6 +1374,227 @@ __global__ void k_sw_force_mc_adj(Tab<T> t, const T* u, const T* v, const T* h, 
     }
 }
 
+// ------------------------------------------------------------------ barotropic filter
+// Spectral barotropic filter (sw.py:720-750, filter_barotropic_waves, with
+// the face thicknesses of compute_diagnostic_variables, 688-692): on faces
+//   u* = (u + dt du) / dx_u,  ubar = sum_l u*_l htu_l / sum_l htu_l,
+//   htu_l = smooth_clamp(h_ref_u,l + (h_l[i] + h_l[i-1]) / 2, h_min area_u, s)
+// (replicate_pad of an all-ocean mask is an edge pad: the wall faces take
+// their one cell twice), at cells
+//   rhs = (diff_x ubar / dx + diff_y vbar / dy) / (g dt tau),
+// w = the Neumann solve of rhs, and every layer's tendency gains
+// -g tau diff_x w on the interior u faces and -g tau diff_y w on the interior
+// v faces, masked. The forward and tangent kernels are templates over the
+// arithmetic type like the right-hand side's; the adjoint is hand-written
+// (the solve is symmetric, so its transpose is the same solve).
+template <typename T, typename S, typename R>
+__device__ __forceinline__ S bf_ubar(const Tab<T>& t, const Tri<R>& x, const R& tu, int b, int i, int j)
+{
+    const int nx = t.nx, ny = t.ny, nl = t.nl;
+    const int c0 = i < nx ? i : nx - 1, c1 = i > 0 ? i - 1 : 0;
+    const long long fi = (long long)i * ny + j;
+    const T xmin = t.hmin * t.areau[fi], dxu = t.dxu[fi];
+    S num = T(0) * x.u(fi), den = num;
+    for (int l = 0; l < nl; ++l) {
+        const long long ob = (long long)b * nl + l;
+        const S hu = T(0.5) * (x.h(ob * t.sh + (long long)c0 * ny + j) + x.h(ob * t.sh + (long long)c1 * ny + j));
+        const S ht = sclamp(VD_TAB(S, t.hrefu, t.d_hrefu, (long long)l * t.su + fi) + hu, xmin, t.sharp);
+        const S us = (x.u(ob * t.su + fi) + t.dt * tu(ob * t.su + fi)) / dxu;
+        num = num + us * ht;
+        den = den + ht;
+    }
+    return num / den;
+}
+
+template <typename T, typename S, typename R>
+__device__ __forceinline__ S bf_vbar(const Tab<T>& t, const Tri<R>& x, const R& tv, int b, int i, int j)
+{
+    const int ny = t.ny, nl = t.nl;
+    const int c0 = j < ny ? j : ny - 1, c1 = j > 0 ? j - 1 : 0;
+    const long long fi = (long long)i * (ny + 1) + j;
+    const T xmin = t.hmin * t.areav[fi], dyv = t.dyv[fi];
+    S num = T(0) * x.v(fi), den = num;
+    for (int l = 0; l < nl; ++l) {
+        const long long ob = (long long)b * nl + l;
+        const long long hb = ob * t.sh + (long long)i * ny;
+        const S hv = T(0.5) * (x.h(hb + c0) + x.h(hb + c1));
+        const S ht = sclamp(VD_TAB(S, t.hrefv, t.d_hrefv, (long long)l * t.sv + fi) + hv, xmin, t.sharp);
+        const S vs = (x.v(ob * t.sv + fi) + t.dt * tv(ob * t.sv + fi)) / dyv;
+        num = num + vs * ht;
+        den = den + ht;
+    }
+    return num / den;
+}
+
+// right-hand side of the filter's solve, one thread per cell and batch member
+template <typename T, typename S, typename R, typename W>
+__global__ void k_bf_rhs(Tab<T> t, Tri<R> x, R tu, R tv, W rhs)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    const int b = blockIdx.z;
+    if (i >= t.nx || j >= t.ny) return;
+    const long long hi = (long long)i * t.ny + j;
+    const S du = bf_ubar<T, S>(t, x, tu, b, i + 1, j) - bf_ubar<T, S>(t, x, tu, b, i, j);
+    const S dv = bf_vbar<T, S>(t, x, tv, b, i, j + 1) - bf_vbar<T, S>(t, x, tv, b, i, j);
+    rhs((long long)b * t.nx * t.ny + hi, t.bf_c * (du / t.dxh[hi] + dv / t.dyh[hi]));
+}
+
+// tendencies += the filter's velocity correction from the solved w
+template <typename T, typename S, typename R, typename W>
+__global__ void k_bf_apply(Tab<T> t, R w, R tu_r, R tv_r, W tu_w, W tv_w)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    const int b = blockIdx.z;
+    const int nx = t.nx, ny = t.ny, nl = t.nl;
+    if (i > nx || j > ny) return;
+    const long long wb = (long long)b * nx * ny;
+    if (j < ny && i >= 1 && i <= nx - 1 && (t.fu[(long long)i * ny + j] & 1)) {
+        const S f = (-t.bf_gt) * (w(wb + (long long)i * ny + j) - w(wb + (long long)(i - 1) * ny + j));
+        for (int l = 0; l < nl; ++l) {
+            const long long idx = ((long long)b * nl + l) * t.su + (long long)i * ny + j;
+            tu_w(idx, tu_r(idx) + f);
+        }
+    }
+    if (i < nx && j >= 1 && j <= ny - 1 && (t.fv[(long long)i * (ny + 1) + j] & 1)) {
+        const S f = (-t.bf_gt) * (w(wb + (long long)i * ny + j) - w(wb + (long long)i * ny + j - 1));
+        for (int l = 0; l < nl; ++l) {
+            const long long idx = ((long long)b * nl + l) * t.sv + (long long)i * (ny + 1) + j;
+            tv_w(idx, tv_r(idx) + f);
+        }
+    }
+}
+
+// Adjoint, step 1: cotangent of w from the tendency cotangents,
+// ad_w[i][j] = -g tau (A_u[i] - A_u[i+1] + A_v[j] - A_v[j+1]) with A the layer
+// sums of the cotangents on the interior masked faces (0 elsewhere).
+template <typename T>
+__global__ void k_bf_adw(Tab<T> t, const T* __restrict__ atu, const T* __restrict__ atv, T* __restrict__ adw)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    const int b = blockIdx.z;
+    const int nx = t.nx, ny = t.ny, nl = t.nl;
+    if (i >= nx || j >= ny) return;
+    auto Au = [&](int a) -> T {
+        if (a < 1 || a > nx - 1 || !(t.fu[(long long)a * ny + j] & 1)) return T(0);
+        T s = T(0);
+        for (int l = 0; l < nl; ++l) s += atu[((long long)b * nl + l) * t.su + (long long)a * ny + j];
+        return s;
+    };
+    auto Av = [&](int c) -> T {
+        if (c < 1 || c > ny - 1 || !(t.fv[(long long)i * (ny + 1) + c] & 1)) return T(0);
+        T s = T(0);
+        for (int l = 0; l < nl; ++l) s += atv[((long long)b * nl + l) * t.sv + (long long)i * (ny + 1) + c];
+        return s;
+    };
+    adw[(long long)b * nx * ny + (long long)i * ny + j] = -t.bf_gt * (Au(i) - Au(i + 1) + Av(j) - Av(j + 1));
+}
+
+// Adjoint, step 3 (after the solve of ad_w into ar), one thread per face
+// point and batch member: the cotangents of ubar / vbar from ar, then per
+// layer those of u / v (adu, adv +=), of the tendencies (atu2 = atu + dt ...,
+// written for every face), and of the face thicknesses through the clamp
+// (ghu / ghv, written for every face; also summed into the H table's
+// cotangent when one is registered).
+template <typename T>
+__global__ void k_bf_face_adj(Tab<T> t, const T* __restrict__ u, const T* __restrict__ v, const T* __restrict__ h,
+                              const T* __restrict__ tu, const T* __restrict__ tv, const T* __restrict__ ar,
+                              const T* __restrict__ atu, const T* __restrict__ atv, T* adu, T* adv,
+                              T* __restrict__ atu2, T* __restrict__ atv2, T* __restrict__ ghu, T* __restrict__ ghv)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    const int b = blockIdx.z;
+    const int nx = t.nx, ny = t.ny, nl = t.nl;
+    if (i > nx || j > ny) return;
+    const long long rb = (long long)b * nx * ny;
+    T ht[MAXL], tr[MAXL], z[MAXL];
+    if (j < ny) {   // u face (i, j)
+        const long long fi = (long long)i * ny + j;
+        T a = T(0);
+        if (i >= 1) a += ar[rb + (long long)(i - 1) * ny + j] / t.dxh[(long long)(i - 1) * ny + j];
+        if (i <= nx - 1) a -= ar[rb + fi] / t.dxh[fi];
+        a *= t.bf_c;
+        const int c0 = i < nx ? i : nx - 1, c1 = i > 0 ? i - 1 : 0;
+        const T xmin = t.hmin * t.areau[fi], dxu = t.dxu[fi];
+        T num = T(0), den = T(0);
+        for (int l = 0; l < nl; ++l) {
+            const long long ob = (long long)b * nl + l;
+            const T hu = T(0.5) * (h[ob * t.sh + (long long)c0 * ny + j] + h[ob * t.sh + (long long)c1 * ny + j]);
+            const T xx = t.hrefu[(long long)l * t.su + fi] + hu;
+            z[l] = (xx - xmin) * t.sharp;
+            ht[l] = sclamp(xx, xmin, t.sharp);
+            tr[l] = (u[ob * t.su + fi] + t.dt * tu[ob * t.su + fi]) / dxu;
+            num += tr[l] * ht[l];
+            den += ht[l];
+        }
+        const T bar = num / den;
+        for (int l = 0; l < nl; ++l) {
+            const long long idx = ((long long)b * nl + l) * t.su + fi;
+            const T g = a * ht[l] / den / dxu;
+            adu[idx] += g;
+            atu2[idx] = atu[idx] + t.dt * g;
+            const T gh = a * (tr[l] - bar) / den * sigmoid_v(z[l]);
+            ghu[idx] = gh;
+            if (t.ad_hrefu) aadd(t.ad_hrefu + (long long)l * t.su + fi, gh);
+        }
+    }
+    if (i < nx) {   // v face (i, j)
+        const long long fi = (long long)i * (ny + 1) + j;
+        const long long hrow = (long long)i * ny;
+        T a = T(0);
+        if (j >= 1) a += ar[rb + hrow + j - 1] / t.dyh[hrow + j - 1];
+        if (j <= ny - 1) a -= ar[rb + hrow + j] / t.dyh[hrow + j];
+        a *= t.bf_c;
+        const int c0 = j < ny ? j : ny - 1, c1 = j > 0 ? j - 1 : 0;
+        const T xmin = t.hmin * t.areav[fi], dyv = t.dyv[fi];
+        T num = T(0), den = T(0);
+        for (int l = 0; l < nl; ++l) {
+            const long long ob = (long long)b * nl + l;
+            const T hv = T(0.5) * (h[ob * t.sh + hrow + c0] + h[ob * t.sh + hrow + c1]);
+            const T xx = t.hrefv[(long long)l * t.sv + fi] + hv;
+            z[l] = (xx - xmin) * t.sharp;
+            ht[l] = sclamp(xx, xmin, t.sharp);
+            tr[l] = (v[ob * t.sv + fi] + t.dt * tv[ob * t.sv + fi]) / dyv;
+            num += tr[l] * ht[l];
+            den += ht[l];
+        }
+        const T bar = num / den;
+        for (int l = 0; l < nl; ++l) {
+            const long long idx = ((long long)b * nl + l) * t.sv + fi;
+            const T g = a * ht[l] / den / dyv;
+            adv[idx] += g;
+            atv2[idx] = atv[idx] + t.dt * g;
+            const T gh = a * (tr[l] - bar) / den * sigmoid_v(z[l]);
+            ghv[idx] = gh;
+            if (t.ad_hrefv) aadd(t.ad_hrefv + (long long)l * t.sv + fi, gh);
+        }
+    }
+}
+
+// Adjoint, step 4: the face-thickness cotangents gathered on the cells
+// (face i averages cells i - 1 and i, the wall faces their one cell twice).
+template <typename T>
+__global__ void k_bf_h_adj(Tab<T> t, const T* __restrict__ ghu, const T* __restrict__ ghv, T* adh)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    const long long bl = blockIdx.z;   // batch member * nl + layer
+    const int nx = t.nx, ny = t.ny;
+    if (i >= nx || j >= ny) return;
+    const T* gu = ghu + bl * t.su;
+    const T* gv = ghv + bl * t.sv;
+    const long long u0 = (long long)i * ny + j, v0 = (long long)i * (ny + 1) + j;
+    T g = T(0.5) * (gu[u0] + gu[u0 + ny]) + T(0.5) * (gv[v0] + gv[v0 + 1]);
+    if (i == 0) g += T(0.5) * gu[u0];
+    if (i == nx - 1) g += T(0.5) * gu[u0 + ny];
+    if (j == 0) g += T(0.5) * gv[v0];
+    if (j == ny - 1) g += T(0.5) * gv[v0 + 1];
+    adh[bl * t.sh + u0] += g;
+}
+
 template <typename T>
 __global__ void k_axpy(long long n, T a, const T* x, T* y)
 {
@@ -1406,6 +1628,7 @@ struct vd_sw_plan {
     std::vector<double> h_area, h_dwu, h_dwv, h_gp;
     std::vector<uint8_t> h_fu, h_fv;
     int h_wind_mode = 0;
+    vd_neumann_plan* bf = nullptr;   // the barotropic filter's solve (null: no filter)
 };
 
 namespace {
@@ -1563,6 +1786,7 @@ extern "C" vd_status vd_sw_plan_create(vd_sw_plan** out, const vd_sw_desc* d)
     if (!(d->dt > 0) || d->slip_coef < 0 || d->slip_coef > 1) return VD_ERR_ARG;
     if (d->forcing_momentum != 0 && d->forcing_momentum != 1) return VD_ERR_ARG;
     if (d->h_wind_mode < 0 || d->h_wind_mode > 2 || (d->h_wind_mode == 2 && !d->h_wind_host)) return VD_ERR_ARG;
+    if (d->barotropic_filter != 0 && d->barotropic_filter != 1) return VD_ERR_ARG;
     const size_t su = (size_t)(nx + 1) * ny, sv = (size_t)nx * (ny + 1), sh = (size_t)nx * ny,
                  sw = (size_t)(nx + 1) * (ny + 1);
     SWMasksHost M;
@@ -1753,6 +1977,28 @@ extern "C" vd_status vd_sw_plan_create(vd_sw_plan** out, const vd_sw_desc* d)
     std::memcpy(host.data() + off[arrs.size()], M.fh.data(), M.fh.size());
     std::memcpy(host.data() + off[arrs.size() + 1], M.fu.data(), M.fu.size());
     std::memcpy(host.data() + off[arrs.size() + 2], M.fv.data(), M.fv.size());
+    // barotropic filter (sw.py:305-320): tau = 2 dt, g = g'_0,
+    // lambd = 1 / (g dt tau H_tot) with H_tot the layer sum of the model's H
+    std::vector<double> bf_lam;
+    int bf_lam_spatial = 0;
+    const double bf_g = d->g_prime_host[0], bf_tau = 2.0 * d->dt;
+    if (d->barotropic_filter) {
+        for (size_t k = 0; k < sh; ++k)
+            if (!(M.fh[k] & 1)) return VD_ERR_UNSUPPORTED;
+        if (!(bf_g != 0.0)) return VD_ERR_ARG;
+        if (d->bf_lambd_host) {
+            bf_lam_spatial = d->bf_lambd_spatial ? 1 : 0;
+            bf_lam.assign(d->bf_lambd_host, d->bf_lambd_host + (bf_lam_spatial ? sh : 1));
+        } else {
+            bf_lam_spatial = Hs;
+            bf_lam.assign(Hs ? sh : 1, 0.0);
+            for (size_t k = 0; k < bf_lam.size(); ++k) {
+                double Ht = 0;
+                for (int l = 0; l < nl; ++l) Ht += Hf[(size_t)l * sh + k];
+                bf_lam[k] = 1.0 / (bf_g * d->dt * bf_tau * Ht);
+            }
+        }
+    }
     vd_sw_plan* p = new (std::nothrow) vd_sw_plan();
     if (!p) return VD_ERR_CUDA;
     p->d = *d;
@@ -1760,6 +2006,7 @@ extern "C" vd_status vd_sw_plan_create(vd_sw_plan** out, const vd_sw_desc* d)
     p->d.h_wind_host = p->d.taux_host = p->d.tauy_host = nullptr;
     p->d.sponge_u_host = p->d.sponge_v_host = p->d.sponge_h_host = nullptr;
     p->d.Hwind_host = nullptr;
+    p->d.bf_lambd_host = nullptr;
     p->nx = nx; p->ny = ny; p->nl = nl; p->esz = esz;
     p->h_area = area;
     p->h_dwu = dwu;
@@ -1778,6 +2025,15 @@ extern "C" vd_status vd_sw_plan_create(vd_sw_plan** out, const vd_sw_desc* d)
         delete p;
         return VD_ERR_CUDA;
     }
+    if (d->barotropic_filter) {
+        const vd_status rc = vd_neumann_plan_create(&p->bf, nx, ny, d->dtype, dx.data(), dy.data(), 1, bf_lam.data(),
+                                                    bf_lam_spatial);
+        if (rc != VD_OK) {
+            cudaFree(p->dev);
+            delete p;
+            return rc;
+        }
+    }
     auto common = [&](auto& t) {
         using TT = std::remove_reference_t<decltype(t.drag)>;
         t.nx = nx; t.ny = ny; t.nl = nl;
@@ -1794,6 +2050,8 @@ extern "C" vd_status vd_sw_plan_create(vd_sw_plan** out, const vd_sw_desc* d)
         t.sharp = (TT)(d->h_min_sharpness > 0 ? d->h_min_sharpness : 10.0); t.dt = (TT)d->dt;
         t.linear = d->flag_linear ? 1 : 0; t.has_sponge = has_sponge; t.hxy_dxp = Hs; t.hxy_dyp = Hs;
         t.wind_mode = d->h_wind_mode;
+        t.bf_c = (TT)(1.0 / (bf_g * d->dt * bf_tau));
+        t.bf_gt = (TT)(bf_g * bf_tau);
         fill_tab(t, p, off);
         if (!Hs) { t.dxp = nullptr; t.dyp = nullptr; }
     };
@@ -1959,6 +2217,7 @@ extern "C" vd_status vd_sw_set_ref_tangent(vd_sw_plan* p, const double* dH_host,
 extern "C" void vd_sw_plan_destroy(vd_sw_plan* p)
 {
     if (!p) return;
+    vd_neumann_plan_destroy(p->bf);
     if (p->dev) cudaFree(p->dev);
     delete p;
 }
@@ -2037,10 +2296,16 @@ template <typename T>
 struct Work {
     Fields<T> x1, x2, k0, k1, tuvh;   // tuvh.u/.v = tendencies, tuvh.h unused
     T *fx, *fy, *om, *kp, *ht;
+    // barotropic filter (null without one): the solve's field [B][nx][ny],
+    // the pre-filter tendency cotangents and the face-thickness cotangents
+    T *bf = nullptr, *bau = nullptr, *bav = nullptr, *ghu = nullptr, *ghv = nullptr;
 };
 
+// elements of one batch member's filter field (0: the plan has no filter)
+static long long bf_elems(const vd_sw_plan* p) { return p->bf ? (long long)p->nx * p->ny : 0; }
+
 template <typename T>
-static int take_work(Arena& ws, const Sizes& s, int B, Work<T>& w)
+static int take_work(Arena& ws, const Sizes& s, int B, Work<T>& w, long long bfn)
 {
     if (!take_uvh(ws, s, B, w.x1) || !take_uvh(ws, s, B, w.x2) || !take_uvh(ws, s, B, w.k0) ||
         !take_uvh(ws, s, B, w.k1))
@@ -2054,14 +2319,24 @@ static int take_work(Arena& ws, const Sizes& s, int B, Work<T>& w)
     w.kp = (T*)ws.take(sizeof(T) * s.sh * B);
     w.ht = (T*)ws.take(sizeof(T) * s.sh * B);
     if (!w.tuvh.u || !w.tuvh.v || !w.fx || !w.fy || !w.om || !w.kp || !w.ht) return VD_ERR_WORKSPACE;
+    if (bfn > 0) {
+        w.bf = (T*)ws.take(sizeof(T) * bfn * B);
+        w.bau = (T*)ws.take(sizeof(T) * s.su * B);
+        w.bav = (T*)ws.take(sizeof(T) * s.sv * B);
+        w.ghu = (T*)ws.take(sizeof(T) * s.su * B);
+        w.ghv = (T*)ws.take(sizeof(T) * s.sv * B);
+        if (!w.bf || !w.bau || !w.bav || !w.ghu || !w.ghv) return VD_ERR_WORKSPACE;
+    }
     return VD_OK;
 }
 
 template <typename T>
-static size_t work_bytes(const Sizes& s, int B)
+static size_t work_bytes(const Sizes& s, int B, long long bfn)
 {
     const size_t F3 = sizeof(T) * (s.su + s.sv + s.sh) * B + 3 * 256;
-    return 4 * F3 + sizeof(T) * (3 * s.su + 3 * s.sv + s.sw + 2 * s.sh) * B + 8 * 256;
+    size_t n = 4 * F3 + sizeof(T) * (3 * s.su + 3 * s.sv + s.sw + 2 * s.sh) * B + 8 * 256;
+    if (bfn > 0) n += sizeof(T) * (bfn + 2 * s.su + 2 * s.sv) * B + 5 * 256;
+    return n;
 }
 
 template <typename T>
@@ -2076,6 +2351,60 @@ template <typename T>
 static Tri<RD<T>> rtd(const Fields<T>& f, const Fields<T>& d) { return {RD<T>{f.u, d.u}, RD<T>{f.v, d.v}, RD<T>{f.h, d.h}}; }
 template <typename T>
 static Tri<WD<T>> wtd(const Fields<T>& f, const Fields<T>& d) { return {WD<T>{f.u, d.u}, WD<T>{f.v, d.v}, WD<T>{f.h, d.h}}; }
+
+// One right-hand side's diagnostics and tendencies of state cur (wk.om,
+// wk.kp, wk.ht; u / v tendencies in wk.tuvh, thickness fluxes in wk.fx /
+// wk.fy), with the barotropic filter when the plan has one.
+template <typename T>
+static int tend_fwd(vd_sw_plan* p, int B, Fields<T> cur, Work<T>& wk, const T* taux, const T* tauy, cudaStream_t st)
+{
+    Tab<T>& t = tab<T>(p);
+    const Launch Ld = lgrid(p, B), Ll = lgrid(p, B * p->nl);
+    k_sw_diag<T, T><<<Ld.grid, Ld.block, 0, st>>>(t, rt(cur), w(wk.om), w(wk.kp), w(wk.ht));
+    VD_LAUNCH_CHECK();
+    k_sw_tend<T, T><<<Ll.grid, Ll.block, 0, st>>>(t, rt(cur), r<T>(wk.om), r<T>(wk.kp), r<T>(wk.ht), taux, tauy,
+                                                   w(wk.tuvh.u), w(wk.tuvh.v), w(wk.fx), w(wk.fy));
+    VD_LAUNCH_CHECK();
+    if (p->bf) {
+        k_bf_rhs<T, T><<<Ld.grid, Ld.block, 0, st>>>(t, rt(cur), r<T>(wk.tuvh.u), r<T>(wk.tuvh.v), w(wk.bf));
+        VD_LAUNCH_CHECK();
+        const int rc = vd::neumann_solve<T>(p->bf, B, wk.bf, wk.bf, st);
+        if (rc) return rc;
+        k_bf_apply<T, T><<<Ld.grid, Ld.block, 0, st>>>(t, r<T>(wk.bf), r<T>(wk.tuvh.u), r<T>(wk.tuvh.v),
+                                                        w(wk.tuvh.u), w(wk.tuvh.v));
+        VD_LAUNCH_CHECK();
+    }
+    return VD_OK;
+}
+
+// The same with tangents (dual numbers; tangents in dk).
+template <typename T>
+static int tend_tgl(vd_sw_plan* p, int B, Fields<T> cur, Fields<T> dcur, Work<T>& wk, Work<T>& dk, const T* taux,
+                    const T* tauy, cudaStream_t st)
+{
+    Tab<T>& t = tab<T>(p);
+    const Launch Ld = lgrid(p, B), Ll = lgrid(p, B * p->nl);
+    using S = DN<T, 1>;
+    k_sw_diag<T, S><<<Ld.grid, Ld.block, 0, st>>>(t, rtd(cur, dcur), WD<T>{wk.om, dk.om}, WD<T>{wk.kp, dk.kp},
+                                                   WD<T>{wk.ht, dk.ht});
+    VD_LAUNCH_CHECK();
+    k_sw_tend<T, S><<<Ll.grid, Ll.block, 0, st>>>(
+        t, rtd(cur, dcur), RD<T>{wk.om, dk.om}, RD<T>{wk.kp, dk.kp}, RD<T>{wk.ht, dk.ht}, taux, tauy,
+        WD<T>{wk.tuvh.u, dk.tuvh.u}, WD<T>{wk.tuvh.v, dk.tuvh.v}, WD<T>{wk.fx, dk.fx}, WD<T>{wk.fy, dk.fy});
+    VD_LAUNCH_CHECK();
+    if (p->bf) {
+        k_bf_rhs<T, S><<<Ld.grid, Ld.block, 0, st>>>(t, rtd(cur, dcur), RD<T>{wk.tuvh.u, dk.tuvh.u},
+                                                      RD<T>{wk.tuvh.v, dk.tuvh.v}, WD<T>{wk.bf, dk.bf});
+        VD_LAUNCH_CHECK();
+        int rc = vd::neumann_solve<T>(p->bf, B, wk.bf, wk.bf, st);
+        if (rc || (rc = vd::neumann_solve<T>(p->bf, B, dk.bf, dk.bf, st))) return rc;
+        k_bf_apply<T, S><<<Ld.grid, Ld.block, 0, st>>>(t, RD<T>{wk.bf, dk.bf}, RD<T>{wk.tuvh.u, dk.tuvh.u},
+                                                        RD<T>{wk.tuvh.v, dk.tuvh.v}, WD<T>{wk.tuvh.u, dk.tuvh.u},
+                                                        WD<T>{wk.tuvh.v, dk.tuvh.v});
+        VD_LAUNCH_CHECK();
+    }
+    return VD_OK;
+}
 
 // forward step loop
 template <typename T>
@@ -2097,11 +2426,8 @@ static int run_fwd(vd_sw_plan* p, int B, Fields<T> x, int nstep, Fields<T> xb, F
         }
         Fields<T> cur = x;
         for (int stg = 0; stg < 3; ++stg) {
-            k_sw_diag<T, T><<<Ld.grid, Ld.block, 0, st>>>(t, rt(cur), w(wk.om), w(wk.kp), w(wk.ht));
-            VD_LAUNCH_CHECK();
-            k_sw_tend<T, T><<<Ll.grid, Ll.block, 0, st>>>(t, rt(cur), r<T>(wk.om), r<T>(wk.kp), r<T>(wk.ht), taux,
-                                                           tauy, w(wk.tuvh.u), w(wk.tuvh.v), w(wk.fx), w(wk.fy));
-            VD_LAUNCH_CHECK();
+            const int rc = tend_fwd<T>(p, B, cur, wk, taux, tauy, st);
+            if (rc) return rc;
             Fields<T> nxt = stg == 0 ? wk.x1 : (stg == 1 ? wk.x2 : (mc ? wk.x1 : x));
             StageArgs sa{stg, (stg == 2 && hasF && !mc) ? 1 : 0};
             Fields<T> ks = stg == 0 ? wk.k0 : wk.k1;
@@ -2132,13 +2458,8 @@ static int run_tgl(vd_sw_plan* p, int B, Fields<T> x, Fields<T> dx, int nstep, F
     for (int n = 0; n < nstep; ++n) {
         Fields<T> cur = x, dcur = dx;
         for (int stg = 0; stg < 3; ++stg) {
-            k_sw_diag<T, S><<<Ld.grid, Ld.block, 0, st>>>(t, rtd(cur, dcur), WD<T>{wk.om, dk.om}, WD<T>{wk.kp, dk.kp},
-                                                           WD<T>{wk.ht, dk.ht});
-            VD_LAUNCH_CHECK();
-            k_sw_tend<T, S><<<Ll.grid, Ll.block, 0, st>>>(
-                t, rtd(cur, dcur), RD<T>{wk.om, dk.om}, RD<T>{wk.kp, dk.kp}, RD<T>{wk.ht, dk.ht}, taux, tauy,
-                WD<T>{wk.tuvh.u, dk.tuvh.u}, WD<T>{wk.tuvh.v, dk.tuvh.v}, WD<T>{wk.fx, dk.fx}, WD<T>{wk.fy, dk.fy});
-            VD_LAUNCH_CHECK();
+            const int rc = tend_tgl<T>(p, B, cur, dcur, wk, dk, taux, tauy, st);
+            if (rc) return rc;
             Fields<T> nxt = stg == 0 ? wk.x1 : (stg == 1 ? wk.x2 : (mc ? wk.x1 : x));
             Fields<T> dnxt = stg == 0 ? dk.x1 : (stg == 1 ? dk.x2 : (mc ? dk.x1 : dx));
             StageArgs sa{stg, (stg == 2 && hasF && !mc) ? 1 : 0};
@@ -2226,7 +2547,8 @@ extern "C" size_t vd_sw_workspace_bytes(const vd_sw_plan* p, int batch, int nste
     const Sizes s = sizes(p);
     const size_t esz = p->esz;
     const size_t F3 = esz * (s.su + s.sv + s.sh) * batch + 3 * 256;
-    const size_t wk = (esz == 8 ? work_bytes<double>(s, batch) : work_bytes<float>(s, batch));
+    const long long bfn = bf_elems(p);
+    const size_t wk = (esz == 8 ? work_bytes<double>(s, batch, bfn) : work_bytes<float>(s, batch, bfn));
     // inputs (x, xb, F), their tangents / adjoints, two work sets, adjoint
     // accumulators, the per-source buffers of the tendency adjoint, and the
     // per-step trajectory
@@ -2245,7 +2567,7 @@ static int sw_step_t(vd_sw_plan* p, int B, const void* u0, const void* v0, const
     int rc = prep_inputs<T>(p, B, u0, v0, h0, ub, vb, hb, Fu, Fv, Fh, ws, in, st);
     if (rc) return rc;
     Work<T> wk;
-    if ((rc = take_work<T>(ws, sizes(p), B, wk))) return rc;
+    if ((rc = take_work<T>(ws, sizes(p), B, wk, bf_elems(p)))) return rc;
     rc = run_fwd<T>(p, B, in.x, nstep, in.xb, in.F, in.hasF, (const T*)taux, (const T*)tauy, wk, nullptr, st);
     if (rc) return rc;
     return scale<T>(p, B, 1, in.x.u, in.x.v, in.x.h, (T*)u1, (T*)v1, (T*)h1, st);
@@ -2275,7 +2597,7 @@ static int sw_tgl_t(vd_sw_plan* p, int B, const void* u0, const void* v0, const 
     if ((rc = zero(din.F, s, B, st))) return rc;
     if ((rc = scale<T>(p, B, 0, (const T*)dFu, (const T*)dFv, (const T*)dFh, din.F.u, din.F.v, din.F.h, st))) return rc;
     Work<T> wk, dk;
-    if ((rc = take_work<T>(ws, s, B, wk)) || (rc = take_work<T>(ws, s, B, dk))) return rc;
+    if ((rc = take_work<T>(ws, s, B, wk, bf_elems(p))) || (rc = take_work<T>(ws, s, B, dk, bf_elems(p)))) return rc;
     rc = run_tgl<T>(p, B, in.x, din.x, nstep, in.xb, din.xb, in.F, din.F, in.hasF || dFu || dFv || dFh,
                     (const T*)taux, (const T*)tauy, wk, dk, st);
     if (rc) return rc;
@@ -2291,7 +2613,26 @@ static int rhs_adj(vd_sw_plan* p, int B, Fields<T> x, Fields<T> adk, Fields<T> a
     const Launch Ld = lgrid(p, B), Ll = lgrid(p, B * p->nl);
     k_sw_diag<T, T><<<Ld.grid, Ld.block, 0, st>>>(t, rt(x), w(wk.om), w(wk.kp), w(wk.ht));
     VD_LAUNCH_CHECK();
-    k_sw_tend_adj_src<T><<<Ll.grid, Ll.block, 0, st>>>(t, x.u, x.v, x.h, wk.om, wk.ht, adk.u, adk.v, adk.h, src,
+    Fields<T> ak = adk;
+    if (p->bf) {
+        // the filter's transpose first: it needs the pre-filter tendencies of
+        // x, and leaves the cotangents of those tendencies in wk.bau / wk.bav
+        k_sw_tend<T, T><<<Ll.grid, Ll.block, 0, st>>>(t, rt(x), r<T>(wk.om), r<T>(wk.kp), r<T>(wk.ht), taux, tauy,
+                                                       w(wk.tuvh.u), w(wk.tuvh.v), w(wk.fx), w(wk.fy));
+        VD_LAUNCH_CHECK();
+        k_bf_adw<T><<<Ld.grid, Ld.block, 0, st>>>(t, adk.u, adk.v, wk.bf);
+        VD_LAUNCH_CHECK();
+        const int rc = vd::neumann_solve<T>(p->bf, B, wk.bf, wk.bf, st);
+        if (rc) return rc;
+        k_bf_face_adj<T><<<Ld.grid, Ld.block, 0, st>>>(t, x.u, x.v, x.h, wk.tuvh.u, wk.tuvh.v, wk.bf, adk.u, adk.v,
+                                                        adx.u, adx.v, wk.bau, wk.bav, wk.ghu, wk.ghv);
+        VD_LAUNCH_CHECK();
+        k_bf_h_adj<T><<<Ll.grid, Ll.block, 0, st>>>(t, wk.ghu, wk.ghv, adx.h);
+        VD_LAUNCH_CHECK();
+        ak.u = wk.bau;
+        ak.v = wk.bav;
+    }
+    k_sw_tend_adj_src<T><<<Ll.grid, Ll.block, 0, st>>>(t, x.u, x.v, x.h, wk.om, wk.ht, ak.u, ak.v, ak.h, src,
                                                         taux, tauy);
     VD_LAUNCH_CHECK();
     k_sw_tend_adj_gather<T><<<Ll.grid, Ll.block, 0, st>>>(t, src, adom, adkp, adht, adx.u, adx.v, adx.h);
@@ -2313,7 +2654,7 @@ static int sw_adj_t(vd_sw_plan* p, int B, const void* u0, const void* v0, const 
     if (rc) return rc;
     const Sizes s = sizes(p);
     Work<T> wk;
-    if ((rc = take_work<T>(ws, s, B, wk))) return rc;
+    if ((rc = take_work<T>(ws, s, B, wk, bf_elems(p)))) return rc;
     std::vector<Fields<T>> traj((size_t)(nstep > 0 ? nstep : 1));
     for (int n = 0; n < nstep; ++n)
         if (!take_uvh(ws, s, B, traj[n])) return VD_ERR_WORKSPACE;
@@ -2347,12 +2688,7 @@ static int sw_adj_t(vd_sw_plan* p, int B, const void* u0, const void* v0, const 
             Fields<T> cur = traj[n];
             const Launch Ld = lgrid(p, B);
             for (int stg = 0; stg < 2; ++stg) {
-                k_sw_diag<T, T><<<Ld.grid, Ld.block, 0, st>>>(t, rt(cur), w(wk.om), w(wk.kp), w(wk.ht));
-                VD_LAUNCH_CHECK();
-                k_sw_tend<T, T><<<Ll.grid, Ll.block, 0, st>>>(t, rt(cur), r<T>(wk.om), r<T>(wk.kp), r<T>(wk.ht),
-                                                               (const T*)taux, (const T*)tauy, w(wk.tuvh.u),
-                                                               w(wk.tuvh.v), w(wk.fx), w(wk.fy));
-                VD_LAUNCH_CHECK();
+                if ((rc = tend_fwd<T>(p, B, cur, wk, (const T*)taux, (const T*)tauy, st))) return rc;
                 Fields<T> nxt = stg == 0 ? x1 : x2;
                 StageArgs sa{stg, 0};
                 Fields<T> ks = stg == 0 ? wk.k0 : wk.k1;
@@ -2364,12 +2700,7 @@ static int sw_adj_t(vd_sw_plan* p, int B, const void* u0, const void* v0, const 
             }
             if (mc) {
                 // x3 (before the forcing) is needed by the forcing adjoint: rebuild it in wk.x1
-                k_sw_diag<T, T><<<Ld.grid, Ld.block, 0, st>>>(t, rt(x2), w(wk.om), w(wk.kp), w(wk.ht));
-                VD_LAUNCH_CHECK();
-                k_sw_tend<T, T><<<Ll.grid, Ll.block, 0, st>>>(t, rt(x2), r<T>(wk.om), r<T>(wk.kp), r<T>(wk.ht),
-                                                               (const T*)taux, (const T*)tauy, w(wk.tuvh.u),
-                                                               w(wk.tuvh.v), w(wk.fx), w(wk.fy));
-                VD_LAUNCH_CHECK();
+                if ((rc = tend_fwd<T>(p, B, x2, wk, (const T*)taux, (const T*)tauy, st))) return rc;
                 StageArgs sa{2, 0};
                 k_sw_update<T, T><<<Ll.grid, Ll.block, 0, st>>>(t, sa, rt(x2), r<T>(wk.tuvh.u), r<T>(wk.tuvh.v),
                                                                  r<T>(wk.fx), r<T>(wk.fy), rt(wk.k0), rt(wk.k1),
@@ -2418,15 +2749,11 @@ static int sw_rhs_t(vd_sw_plan* p, int B, const void* u, const void* v, const vo
     Tab<T>& t = tab<T>(p);
     const Sizes s = sizes(p);
     Work<T> wk;
-    int rc = take_work<T>(ws, s, B, wk);
+    int rc = take_work<T>(ws, s, B, wk, bf_elems(p));
     if (rc) return rc;
     const Launch Ld = lgrid(p, B), Ll = lgrid(p, B * p->nl);
     Fields<T> x{(T*)u, (T*)v, (T*)h};
-    k_sw_diag<T, T><<<Ld.grid, Ld.block, 0, st>>>(t, rt(x), w(wk.om), w(wk.kp), w(wk.ht));
-    VD_LAUNCH_CHECK();
-    k_sw_tend<T, T><<<Ll.grid, Ll.block, 0, st>>>(t, rt(x), r<T>(wk.om), r<T>(wk.kp), r<T>(wk.ht), (const T*)taux,
-                                                   (const T*)tauy, w(wk.tuvh.u), w(wk.tuvh.v), w(wk.fx), w(wk.fy));
-    VD_LAUNCH_CHECK();
+    if ((rc = tend_fwd<T>(p, B, x, wk, (const T*)taux, (const T*)tauy, st))) return rc;
     // stage-0 update with dt*k into a scratch state, k0 = tendency (no sponge: zero rates are
     // not guaranteed, so the sponge is removed by passing x as its own target)
     Fields<T> k{(T*)du, (T*)dv, (T*)dh};
@@ -2519,19 +2846,12 @@ static int sw_rhs_tgl_t(vd_sw_plan* p, int B, const void* u, const void* v, cons
     Tab<T>& t = tab<T>(p);
     const Sizes s = sizes(p);
     Work<T> wk, dk;
-    int rc = take_work<T>(ws, s, B, wk);
-    if (rc || (rc = take_work<T>(ws, s, B, dk))) return rc;
+    int rc = take_work<T>(ws, s, B, wk, bf_elems(p));
+    if (rc || (rc = take_work<T>(ws, s, B, dk, bf_elems(p)))) return rc;
     const Launch Ld = lgrid(p, B), Ll = lgrid(p, B * p->nl);
     Fields<T> x{(T*)u, (T*)v, (T*)h}, dx{(T*)du, (T*)dv, (T*)dh};
     using S = DN<T, 1>;
-    k_sw_diag<T, S><<<Ld.grid, Ld.block, 0, st>>>(t, rtd(x, dx), WD<T>{wk.om, dk.om}, WD<T>{wk.kp, dk.kp},
-                                                   WD<T>{wk.ht, dk.ht});
-    VD_LAUNCH_CHECK();
-    k_sw_tend<T, S><<<Ll.grid, Ll.block, 0, st>>>(t, rtd(x, dx), RD<T>{wk.om, dk.om}, RD<T>{wk.kp, dk.kp},
-                                                   RD<T>{wk.ht, dk.ht}, (const T*)taux, (const T*)tauy,
-                                                   WD<T>{wk.tuvh.u, dk.tuvh.u}, WD<T>{wk.tuvh.v, dk.tuvh.v},
-                                                   WD<T>{wk.fx, dk.fx}, WD<T>{wk.fy, dk.fy});
-    VD_LAUNCH_CHECK();
+    if ((rc = tend_tgl<T>(p, B, x, dx, wk, dk, (const T*)taux, (const T*)tauy, st))) return rc;
     Fields<T> k{(T*)ku, (T*)kv, (T*)kh}, dkk{(T*)dku, (T*)dkv, (T*)dkh};
     StageArgs sa{0, 0};
     k_sw_update<T, S><<<Ll.grid, Ll.block, 0, st>>>(t, sa, rtd(x, dx), RD<T>{wk.tuvh.u, dk.tuvh.u},
@@ -2548,7 +2868,7 @@ static int sw_rhs_adj_t(vd_sw_plan* p, int B, const void* u, const void* v, cons
 {
     const Sizes s = sizes(p);
     Work<T> wk;
-    int rc = take_work<T>(ws, s, B, wk);
+    int rc = take_work<T>(ws, s, B, wk, bf_elems(p));
     if (rc) return rc;
     T* adom = (T*)ws.take(sizeof(T) * s.sw * B);
     T* adkp = (T*)ws.take(sizeof(T) * s.sh * B);

@@ -15,9 +15,14 @@ every layer's thickness) and ``h_wind`` (added to the model's mixed-layer
 depth); ``step_adj`` returns their cotangents, summed to the shapes they were
 given in.
 
-Not supported (they raise): the barotropic filter (``SW`` only; its
-multigrid coefficients change every call, sw.py:335-356), open boundary
-conditions, the tangent linear with respect to ``H`` and ``h_wind``.
+The spectral barotropic filter (``barotropic_filter`` with
+``barotropic_filter_spectral``, ``SW`` only: sw.py:305-320, 720-750) runs in
+every right-hand side of the step, its tangent and its adjoint.
+
+Not supported (they raise): the filter's exact form (its multigrid solve is
+work in progress in the reference, sw.py:321-333, 736-743) and its spectral
+form with land (the reference's Neumann solver does not construct then,
+helmholtz.py:254), open boundary conditions.
 """
 import numpy as np
 import torch
@@ -54,8 +59,15 @@ class SW:
         self.param = p
         self.nx, self.ny, self.nl = int(p["nx"]), int(p["ny"]), int(p["nl"])
         self.dtype = _torch_dtype(p.get("dtype"))
+        self.barotropic_filter = False
         if p.get("barotropic_filter", False) and type(self).__name__ == "SW":
-            raise NotImplementedError("barotropic filter (sw.py:335-356)")
+            if not p.get("barotropic_filter_spectral", False):
+                raise NotImplementedError("the barotropic filter's exact form is work in progress in the "
+                                          "reference (sw.py:321-333)")
+            if p.get("mask") is not None and np.any(np.asarray(p["mask"], dtype=np.float64) < 0.5):
+                raise NotImplementedError("the spectral barotropic filter with land: the reference's Neumann "
+                                          "solver does not construct (helmholtz.py:254)")
+            self.barotropic_filter = True
         if p.get("flag_obc", False):
             raise NotImplementedError("open boundary conditions (sw.py:366-381)")
         H = np.asarray(p["H"], dtype=np.float64)
@@ -63,6 +75,12 @@ class SW:
             raise ValueError(f"H must be a nl x nx x ny array with unit axes for constant directions, got {H.shape}")
         self.H = H
         self.dt = float(p["dt"])
+        if self.barotropic_filter:
+            # tau, H_tot and lambd of sw.py:312-317, from the model's own H
+            self.tau = 2 * self.dt
+            self.g = float(np.asarray(p["g_prime"], dtype=np.float64).reshape(-1)[0])
+            self.H_tot = H.sum(axis=-3, keepdims=True)
+            self.lambd = 1.0 / (self.g * self.dt * self.tau * self.H_tot)
         self.n_ens = int(p.get("n_ens", 1))
         nx, ny = self.nx, self.ny
         self._sponge = {"u": None, "v": None, "h": None}
@@ -91,7 +109,8 @@ class SW:
                     forcing_momentum=p.get("forcing_momentum", "direct"), h_wind=p.get("h_wind", None),
                     taux=p["taux"], tauy=p["tauy"],
                     sponge_u=self._sponge["u"], sponge_v=self._sponge["v"], sponge_h=self._sponge["h"],
-                    dtype=self.dtype)
+                    dtype=self.dtype, barotropic_filter=self.barotropic_filter,
+                    bf_lambd=self.lambd if self.barotropic_filter else None)
 
     def _make_plan(self, H, h_wind=None):
         p = self.param

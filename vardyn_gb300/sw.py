@@ -67,10 +67,16 @@ class SWPlan:
     def __init__(self, nx, ny, nl, dx, dy, f, H, g_prime, dt, mask=None, slip_coef=1.0, bottom_drag_coef=0.0,
                  rho_water=1025.0, h_min=0.1, h_min_sharpness=10.0, visc_coef=0.0, diff_coef=0.0, sponge_coef=0.0,
                  flag_linear=False, forcing_momentum="direct", h_wind=None, taux=0.0, tauy=0.0, sponge_u=None,
-                 sponge_v=None, sponge_h=None, dtype=torch.float64, device=None, H_wind=None):
+                 sponge_v=None, sponge_h=None, dtype=torch.float64, device=None, H_wind=None,
+                 barotropic_filter=False, bf_lambd=None):
         """``H_wind`` (without ``h_wind``): the layer thicknesses the wind
         depth is taken from, when they differ from ``H`` (a model stepped
-        with a perturbed H keeps its own H there, sw.py:622-630)."""
+        with a perturbed H keeps its own H there, sw.py:622-630).
+
+        ``barotropic_filter``: the spectral barotropic filter in every
+        right-hand side (sw.py:305-320, 720-750), all-ocean masks only;
+        ``bf_lambd`` its ``lambd`` (a scalar or an [nx, ny] field; None: from
+        ``H``), which a model stepped with a perturbed H keeps from its own."""
         if not torch.cuda.is_available():
             raise RuntimeError("vardyn_gb300 needs a CUDA device (no CPU path)")
         self.device = torch.device(device if device is not None else "cuda")
@@ -133,6 +139,17 @@ class SWPlan:
             if val is not None:
                 setattr(d, name + "_host", _dp(k(np.ascontiguousarray(np.broadcast_to(_f64(val).reshape(
                     np.shape(val)[-2:]), shape)))))
+        if barotropic_filter:
+            d.barotropic_filter = 1
+            if bf_lambd is not None:
+                lam = _f64(bf_lambd)
+                if lam.size == 1:
+                    d.bf_lambd_host, d.bf_lambd_spatial = _dp(k(lam.reshape(1))), 0
+                else:
+                    d.bf_lambd_host = _dp(k(np.ascontiguousarray(np.broadcast_to(lam.reshape(lam.shape[-2:]),
+                                                                                   (nx, ny)))))
+                    d.bf_lambd_spatial = 1
+        self.barotropic_filter = bool(barotropic_filter)
         self.masks = SWMasks(nx, ny, mask)
         self.forcing_momentum = forcing_momentum
         handle = ctypes.c_void_p()
