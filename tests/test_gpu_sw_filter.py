@@ -151,8 +151,11 @@ def test_tangent_adjoint_and_H():
     lhs = sum(float((t * a).sum()) for t, a in zip(tl, a1))
     rhs = sum(float((d * ad[k]).sum()) for d, k in zip(dx, ("u0", "v0", "h0")))
     assert abs(lhs - rhs) / abs(lhs) < 1e-12
-    # H: the adjoint's cotangent against the tangent with respect to H
-    dH = rng.standard_normal((prm["nl"], prm["nx"], prm["ny"]))
+    # H: the adjoint's cotangent against the tangent with respect to H. The
+    # model's H has unit spatial axes, so its cotangent is that of per-layer
+    # thicknesses (the reference pressure gradients are then the constant 0,
+    # sw.py:403-404): the direction is constant in space.
+    dH = np.broadcast_to(rng.standard_normal((prm["nl"], 1, 1)), (prm["nl"], prm["nx"], prm["ny"])).copy()
     zero = [torch.zeros_like(a) for a in tx]
     tlH = pl.step_tgl(*tx, *zero, nstep=n, dH=dH)
     lhs = sum(float((t * a).sum()) for t, a in zip(tlH, a1))

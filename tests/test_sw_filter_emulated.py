@@ -351,6 +351,30 @@ def test_H_cotangent(emu):
     assert abs(sum(np.vdot(t, c) for t, c in zip(tl, a1)) - lhs) / abs(lhs) < 1e-6
 
 
+def test_H_cotangent_per_layer(emu):
+    """A model whose H has unit spatial axes: its cotangent is that of
+    per-layer thicknesses (no reference pressure gradients, sw.py:403-404),
+    checked with a direction constant in space against the tangent."""
+    prm, o, x, rng = _case(B=2)
+    nx, ny, nl = prm["nx"], prm["ny"], prm["nl"]
+    pl = Plan(emu, prm)
+    n = 2
+    a1 = [rng.standard_normal(s) for s in pl.shapes(2)]
+    buf = np.zeros(emu.vd_sw_ref_adj_bytes(pl.h) // 8)
+    ok(emu.vd_sw_set_ref_adj(pl.h, ptr(buf)), "set_ref_adj")
+    pl.adj(x, a1, n)
+    ok(emu.vd_sw_set_ref_adj(pl.h, None), "unset")
+    adH = np.zeros((nl, nx, ny))
+    ok(emu.vd_sw_ref_pullback(pl.h, ptr(buf), ptr(adH), None, None), "pullback")
+    dH = np.broadcast_to(rng.standard_normal((nl, 1, 1)), (nl, nx, ny)).copy()
+    tb = np.zeros_like(buf)
+    ok(emu.vd_sw_set_ref_tangent(pl.h, ptr(dH), None, ptr(tb)), "set_ref_tangent")
+    tl = pl.tgl(x, [np.zeros_like(a) for a in x], n)
+    ok(emu.vd_sw_set_ref_tangent(pl.h, None, None, None), "unset tangent")
+    lhs = sum(np.vdot(t, c) for t, c in zip(tl, a1))
+    assert abs(lhs - np.vdot(adH, dH)) / abs(lhs) < 1e-12
+
+
 def test_land_refused(emu):
     prm, _, _, _ = _case()
     mask = np.ones((prm["nx"], prm["ny"]))

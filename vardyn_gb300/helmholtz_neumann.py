@@ -36,8 +36,8 @@ def _flat(a, nx, ny):
     """(array, spatial flag) of a scalar or an [..., nx, ny]-broadcastable field."""
     a = np.asarray(a, dtype=np.float64)
     if a.size == 1:
-        return np.ascontiguousarray(a.reshape(1)), 0
-    return np.ascontiguousarray(np.broadcast_to(a.reshape(a.shape[-2:]), (nx, ny))), 1
+        return np.array(a.reshape(1)), 0
+    return np.array(np.broadcast_to(a.reshape(a.shape[-2:]), (nx, ny))), 1
 
 
 class HelmholtzNeumannSolver:
@@ -62,8 +62,8 @@ class HelmholtzNeumannSolver:
         dxa, sdx = _flat(dx, self.nx, self.ny)
         dya, sdy = _flat(dy, self.nx, self.ny)
         if sdx or sdy:   # one flag covers both spacings
-            dxa = np.ascontiguousarray(np.broadcast_to(dxa if sdx else dxa[0], (self.nx, self.ny)))
-            dya = np.ascontiguousarray(np.broadcast_to(dya if sdy else dya[0], (self.nx, self.ny)))
+            dxa = np.array(np.broadcast_to(dxa if sdx else dxa[0], (self.nx, self.ny)))
+            dya = np.array(np.broadcast_to(dya if sdy else dya[0], (self.nx, self.ny)))
             sdx = 1
         lam, slam = _flat(lambd, self.nx, self.ny)
         self.helmholtz_dctII = (compute_laplace_dctII(self.nx, self.ny, dxa if sdx else float(dxa[0]),
