@@ -751,6 +751,10 @@ typedef struct vd_sw_desc {
                                      one): a scalar or, with bf_lambd_spatial, [nx][ny];
                                      NULL = from this plan's H */
     int bf_lambd_spatial;
+    int flag_obc;                 /* open boundaries (sw.py:353-371): the u masks of the
+                                     west / east faces and the v masks of the south /
+                                     north faces are 1 (set after the stencil masks are
+                                     built); inflow velocities there are kept */
 } vd_sw_desc;
 
 /* Host-only: the flag bytes of the staggered masks (masks.py:57-158).

@@ -185,6 +185,17 @@ class SWOracle:
         self.area_u, self.area_v = self.dx_u * self.dy_u, self.dx_v * self.dy_v
         self.slip = float(param.get("slip_coef", 1.0))
         self.masks = SWMasks(param["mask"] if "mask" in param else np.ones((nx, ny)))
+        # open boundaries (sw.py:353-371): the u masks of the west / east
+        # faces and the v masks of the south / north faces are set to 1 after
+        # the other masks are built; the boundary arrays allocated there are
+        # never read
+        if param.get("flag_obc", False):
+            self.masks.u = self.masks.u.copy()
+            self.masks.u[0, :] = 1.0
+            self.masks.u[-1, :] = 1.0
+            self.masks.v = self.masks.v.copy()
+            self.masks.v[:, 0] = 1.0
+            self.masks.v[:, -1] = 1.0
         f = np.asarray(param["f"], dtype=np.float64)
         self.f0 = f.mean()
         self.fstar_u = 0.5 * (f[:, 1:] + f[:, :-1]) * self.area_u

@@ -5,7 +5,7 @@ the solve and the model against the reference's own outputs
 layers and 2 batch members, central differences of the tangent-linear and
 dot products of the adjoint, including the cotangent of H. The same kernel
 sources pass the same checks under the host emulation
-(tests/test_sw_filter_emulated.py)."""
+(tests/test_sw_emulated.py)."""
 import os
 
 import numpy as np

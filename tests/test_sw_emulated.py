@@ -1,17 +1,19 @@
-"""The shallow-water model's spectral barotropic filter as the library
-implements it (the Neumann solve of vardyn_gb300/csrc/vd_neumann.cu, the
-filter kernels and their wiring in vd_sw.cu), run on the CPU: the two source
-files are compiled by g++ under the host emulation of tests/host_emulation
-(every kernel body runs once per thread of its grid, or once per block for
-the solve's barrier-separated block loops), and the library's C ABI is
-called on host buffers.
+"""The shallow-water library (vardyn_gb300/csrc/vd_sw.cu with the Neumann
+solve of vd_neumann.cu) run on the CPU: the two source files are compiled by
+g++ under the host emulation of tests/host_emulation (every kernel body runs
+once per thread of its grid, or once per block for the solve's
+barrier-separated block loops), and the library's C ABI is called on host
+buffers.
 
-Checked against the reference's own outputs (tests/golden/swfilter_golden.npz:
-the solve, the right-hand side with the filter, a 3-step run), against the
-oracle (oracle/sw.py) on a non-uniform grid with 3 layers and 2 batch
-members, and for the tangent-linear (central differences) and the adjoint
-(dot products, including the cotangent of H). The same sources run on the
-GPU in tests/test_gpu_sw_filter.py."""
+The spectral barotropic filter is checked against the reference's own outputs
+(tests/golden/swfilter_golden.npz: the solve, the right-hand side with the
+filter, a 3-step run), against the oracle (oracle/sw.py) on a non-uniform
+grid with 3 layers and 2 batch members, and for the tangent-linear (central
+differences) and the adjoint (dot products, including the cotangent of H).
+Open boundaries are checked against the reference's own outputs
+(tests/golden/swobc_golden.npz), the model without either against
+tests/golden/sw_golden.npz. The same sources run on the GPU in
+tests/test_gpu_sw_filter.py and tests/test_gpu_sw.py."""
 import ctypes
 import os
 import shutil
@@ -110,6 +112,7 @@ class Plan:
             # the wind depth of a model stepped with a perturbed H stays its own (sw.py:622-630)
             d.Hwind_host = arr(np.asarray(H_wind, dtype=np.float64).reshape(nl, -1)[0], (nx, ny))
         d.barotropic_filter = 1 if prm.get("barotropic_filter") else 0
+        d.flag_obc = 1 if prm.get("flag_obc") else 0
         if bf_lambd is not None:
             lam = np.asarray(bf_lambd, dtype=np.float64)
             if lam.size == 1:
@@ -433,3 +436,48 @@ def test_unfiltered_model_golden(emu):
                            Fv=np.zeros_like(g[p + "v0"]), Fh=g[p + "Fh"], taux=g[p + "taux"], tauy=g[p + "tauy"])
     for a, k in zip(r, ["u5", "v5", "h5"]):
         assert rel(a, g[p + k]) < 1e-12, k
+
+
+# ---------------------------------------------------------------- open boundaries
+def _obc_param(g, **over):
+    p = "ob_"
+    d = dict(nx=28, ny=22, nl=2, dx=g[p + "dx"], dy=g[p + "dy"], H=g[p + "H"], g_prime=g[p + "gp"], f=g[p + "f"],
+             taux=0.04, tauy=-0.02, bottom_drag_coef=1e-6, dt=20.0, mask=g[p + "mask"], slip_coef=0.6,
+             visc_coef=20.0, diff_coef=10.0, sponge_coef=0.2, flag_obc=True, sponge_u=g[p + "sponge_u"],
+             sponge_v=g[p + "sponge_v"], sponge_h=g[p + "sponge_h"])
+    d.update(over)
+    return d
+
+
+def test_open_boundaries_golden(emu):
+    g = dict(np.load(os.path.join(HERE, "golden", "swobc_golden.npz")))
+    prm = _obc_param(g)
+    pl = Plan(emu, prm)
+    o = SWOracle(prm)
+    u, v, h = o.to_model(g["ob_u0"], g["ob_v0"], g["ob_h0"])
+    du, dv, dh = pl.rhs(u, v, h)
+    assert rel(du, g["ob_dtu"]) < 1e-12 and rel(dv, g["ob_dtv"]) < 1e-12 and rel(dh, g["ob_dth"]) < 1e-12
+    r = pl.step(*(g["ob_" + k] for k in ("u0", "v0", "h0")), 4,
+                *(g["ob_" + k] for k in ("ub", "vb", "hb", "Fu", "Fv", "Fh")))
+    for a, k in zip(r, ("u4", "v4", "h4")):
+        assert rel(a, g["ob_" + k]) < 1e-12, k
+    # the inflow velocities on the walls are kept, and relaxed by the sponge
+    assert np.abs(r[0][:, :, 0]).max() > 0 and np.abs(r[1][:, :, :, -1]).max() > 0
+
+
+def test_open_boundaries_adjoint(emu):
+    g = dict(np.load(os.path.join(HERE, "golden", "swobc_golden.npz")))
+    pl = Plan(emu, _obc_param(g))
+    rng = np.random.default_rng(3)
+    x = [g["ob_" + k] for k in ("u0", "v0", "h0")]
+    dx = [0.01 * rng.standard_normal(a.shape) for a in x]
+    tl = pl.tgl(x, dx, 2)
+    eps = 1e-6
+    p = pl.step(*[a + eps * b for a, b in zip(x, dx)], 2)
+    q = pl.step(*[a - eps * b for a, b in zip(x, dx)], 2)
+    for t, a, b in zip(tl, p, q):
+        assert rel(t, (a - b) / (2 * eps)) < 1e-6
+    a1 = [rng.standard_normal(a.shape) for a in tl]
+    ad = pl.adj(x, a1, 2)
+    lhs = sum(np.vdot(t, a) for t, a in zip(tl, a1))
+    assert abs(lhs - sum(np.vdot(d, a) for d, a in zip(dx, ad))) / abs(lhs) < 1e-12

@@ -133,6 +133,7 @@ class VdSwDesc(ctypes.Structure):
         ("taux_host", _DP), ("tauy_host", _DP),
         ("sponge_u_host", _DP), ("sponge_v_host", _DP), ("sponge_h_host", _DP), ("Hwind_host", _DP),
         ("barotropic_filter", ctypes.c_int), ("bf_lambd_host", _DP), ("bf_lambd_spatial", ctypes.c_int),
+        ("flag_obc", ctypes.c_int),
     ]
 
 

@@ -1791,6 +1791,18 @@ extern "C" vd_status vd_sw_plan_create(vd_sw_plan** out, const vd_sw_desc* d)
                  sw = (size_t)(nx + 1) * (ny + 1);
     SWMasksHost M;
     build_masks(nx, ny, d->mask_host, M);
+    if (d->flag_obc) {
+        // open boundaries: only the face masks themselves change, after the
+        // stencil selectors are built from the closed ones (sw.py:365-369)
+        for (int j = 0; j < ny; ++j) {
+            M.fu[(size_t)j] |= 1;
+            M.fu[(size_t)nx * ny + j] |= 1;
+        }
+        for (int i = 0; i < nx; ++i) {
+            M.fv[(size_t)i * (ny + 1)] |= 1;
+            M.fv[(size_t)i * (ny + 1) + ny] |= 1;
+        }
+    }
     // metrics (sw.py:147-167)
     std::vector<double> dx(d->dx_host, d->dx_host + sh), dy(d->dy_host, d->dy_host + sh), dxu, dyu, dxv, dyv;
     for (size_t k = 0; k < sh; ++k)

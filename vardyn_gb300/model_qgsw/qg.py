@@ -30,6 +30,12 @@ class QG(SW):
         kw = self._plan_kwargs()
         kw.pop("rho_water")
         kw.pop("h_wind")
+        # the barotropic filter is SW's only (sw.py:307-309); open boundaries
+        # would also have to open the projector's face masks, not built
+        for k in ("barotropic_filter", "bf_lambd"):
+            kw.pop(k)
+        if kw.pop("flag_obc"):
+            raise NotImplementedError("open boundaries in the QG model (the projector's masks)")
         H = np.asarray(self.H)
         if H.shape[-2:] != (1, 1):
             raise ValueError(f"H must be constant in space for the qg approximation, got shape {H.shape}")

@@ -22,7 +22,9 @@ every right-hand side of the step, its tangent and its adjoint.
 Not supported (they raise): the filter's exact form (its multigrid solve is
 work in progress in the reference, sw.py:321-333, 736-743) and its spectral
 form with land (the reference's Neumann solver does not construct then,
-helmholtz.py:254), open boundary conditions.
+helmholtz.py:254). Open boundaries (``flag_obc``, sw.py:353-371) open the
+outer face masks; the boundary arrays the reference allocates there are
+never read, and are not kept.
 """
 import numpy as np
 import torch
@@ -68,8 +70,6 @@ class SW:
                 raise NotImplementedError("the spectral barotropic filter with land: the reference's Neumann "
                                           "solver does not construct (helmholtz.py:254)")
             self.barotropic_filter = True
-        if p.get("flag_obc", False):
-            raise NotImplementedError("open boundary conditions (sw.py:366-381)")
         H = np.asarray(p["H"], dtype=np.float64)
         if H.ndim < 3:
             raise ValueError(f"H must be a nl x nx x ny array with unit axes for constant directions, got {H.shape}")
@@ -110,6 +110,7 @@ class SW:
                     taux=p["taux"], tauy=p["tauy"],
                     sponge_u=self._sponge["u"], sponge_v=self._sponge["v"], sponge_h=self._sponge["h"],
                     dtype=self.dtype, barotropic_filter=self.barotropic_filter,
+                    flag_obc=bool(p.get("flag_obc", False)),
                     bf_lambd=self.lambd if self.barotropic_filter else None)
 
     def _make_plan(self, H, h_wind=None):

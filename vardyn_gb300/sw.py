@@ -30,9 +30,10 @@ class SWMasks:
     """Masks of masks.py:57-158 from the library's host mask builder: float
     arrays ``h``, ``u``, ``v``, ``w``, ``psi`` (shapes of the reference without
     its two leading unit axes), the vorticity boundary classes, the WENO
-    stencil selectors and the irregular psi-boundary indices."""
+    stencil selectors and the irregular psi-boundary indices. ``obc``: the
+    open-boundary face masks of sw.py:365-369 (outer u / v faces 1)."""
 
-    def __init__(self, nx, ny, mask=None):
+    def __init__(self, nx, ny, mask=None, obc=False):
         m = None if mask is None else _f64(mask)
         if m is not None and m.shape != (nx, ny):
             raise ValueError(f"mask must be ({nx}, {ny}), got {m.shape}")
@@ -45,6 +46,9 @@ class SWMasks:
                   fv.ctypes.data_as(ctypes.c_void_p), fw.ctypes.data_as(ctypes.c_void_p))
         b = lambda f, k: ((f >> k) & 1).astype(np.float64)
         self.h, self.u, self.v = b(fh, 0), b(fu, 0), b(fv, 0)
+        if obc:
+            self.u[0, :] = self.u[-1, :] = 1.0
+            self.v[:, 0] = self.v[:, -1] = 1.0
         self.w_valid, self.w_cornerout_bound = b(fw, 0), b(fw, 1)
         self.w_vertical_bound, self.w_horizontal_bound = b(fw, 2), b(fw, 3)
         self.w, self.psi = b(fw, 4), b(fw, 5)
@@ -68,7 +72,7 @@ class SWPlan:
                  rho_water=1025.0, h_min=0.1, h_min_sharpness=10.0, visc_coef=0.0, diff_coef=0.0, sponge_coef=0.0,
                  flag_linear=False, forcing_momentum="direct", h_wind=None, taux=0.0, tauy=0.0, sponge_u=None,
                  sponge_v=None, sponge_h=None, dtype=torch.float64, device=None, H_wind=None,
-                 barotropic_filter=False, bf_lambd=None):
+                 barotropic_filter=False, bf_lambd=None, flag_obc=False):
         """``H_wind`` (without ``h_wind``): the layer thicknesses the wind
         depth is taken from, when they differ from ``H`` (a model stepped
         with a perturbed H keeps its own H there, sw.py:622-630).
@@ -76,7 +80,8 @@ class SWPlan:
         ``barotropic_filter``: the spectral barotropic filter in every
         right-hand side (sw.py:305-320, 720-750), all-ocean masks only;
         ``bf_lambd`` its ``lambd`` (a scalar or an [nx, ny] field; None: from
-        ``H``), which a model stepped with a perturbed H keeps from its own."""
+        ``H``), which a model stepped with a perturbed H keeps from its own.
+        ``flag_obc``: open boundaries (sw.py:353-371)."""
         if not torch.cuda.is_available():
             raise RuntimeError("vardyn_gb300 needs a CUDA device (no CPU path)")
         self.device = torch.device(device if device is not None else "cuda")
@@ -150,7 +155,8 @@ class SWPlan:
                                                                                    (nx, ny)))))
                     d.bf_lambd_spatial = 1
         self.barotropic_filter = bool(barotropic_filter)
-        self.masks = SWMasks(nx, ny, mask)
+        d.flag_obc = 1 if flag_obc else 0
+        self.masks = SWMasks(nx, ny, mask, obc=bool(flag_obc))
         self.forcing_momentum = forcing_momentum
         handle = ctypes.c_void_p()
         with torch.cuda.device(self.device):
