@@ -1335,6 +1335,35 @@ def gpu_arm_aux(args):
         "gpu_ms_per_dst_solve": ms_dst, "gpu_ms_per_cmm_solve": ms_cmm,
         "dst_solve_GBps": dst_bytes / (ms_dst * 1e-3) / 1e9,
         "cpu_s_per_cmm_solve": t_cpu, "cpu_s_per_dst_solve": t_cpu_dst, "cpu_note": "oracle (scipy.fft.dstn) on the host"}
+    # --- shallow-water barotropic filter (spectral form): the Neumann solve alone
+    # (1 and 16 fields), and an all-ocean 3-layer RK3 step with and without it
+    from vardyn_gb300.helmholtz_neumann import HelmholtzNeumannSolver
+    from vardyn_gb300.sw import SWPlan
+    lam_bf = 1.0 / (9.81 * 60.0 * 120.0 * float(sum(S5_H)))
+    row = {"case": f"{nx}x{ny}, uniform {S5_DX / 1e3:g} km, lambd {lam_bf:.3g}, 3 layers, all ocean"}
+    for dt_name, tdt in (("f32", torch.float32), ("f64", torch.float64)):
+        ns = HelmholtzNeumannSolver(nx, ny, S5_DX, S5_DX, lam_bf, dtype=tdt)
+        for nf in (1, 16):
+            r = torch.randn(nf, nx, ny, dtype=tdt, device="cuda")
+            ms_s = _gpu_ms(lambda: ns.solve(r), reps=20)
+            # each of the three passes reads and writes every field once
+            row[f"solve_{dt_name}_{nf}_us"] = ms_s * 1e3
+            row[f"solve_{dt_name}_{nf}_GBps"] = 6 * nf * nx * ny * r.element_size() / (ms_s * 1e-3) / 1e9
+        fs = np.full((nx + 1, ny + 1), 1e-4)
+        for bf in (False, True):
+            sp = SWPlan(nx, ny, 3, S5_DX, S5_DX, fs, np.array(S5_H).reshape(3, 1, 1), np.array(S5_GP), 60.0,
+                        bottom_drag_coef=1e-7, taux=0.05, dtype=tdt, barotropic_filter=bf,
+                        bf_lambd=lam_bf if bf else None)
+            xs = [0.01 * torch.randn(sh, dtype=tdt, device="cuda") for sh in sp.shapes(1)]
+            row[f"step_{dt_name}_{'filter' if bf else 'nofilter'}_ms"] = _gpu_ms(lambda: sp.step(*xs, nstep=1),
+                                                                                 reps=10)
+    import types as _types
+    from oracle.sw import SWOracle
+    helm_n = ns.helmholtz_dctII.cpu().numpy()
+    rn = torch.randn(1, nx, ny, dtype=torch.float64).numpy()
+    row["cpu_s_per_solve"] = _cpu_s(lambda: SWOracle.neumann_solve(_types.SimpleNamespace(helm_dct=helm_n), rn))
+    row["cpu_note"] = "oracle (scipy.fft DCT-II pair, float64) on the host, one field"
+    rows["a18_sw_barotropic_filter"] = row
     # --- QG projector (3 layers, one island), float32
     from vardyn_gb300.qg_ml import QGPlan
     yw = np.arange(ny + 1)[None, :] * S5_DX + np.zeros((nx + 1, 1))

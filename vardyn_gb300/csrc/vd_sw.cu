@@ -1426,18 +1426,36 @@ __device__ __forceinline__ S bf_vbar(const Tab<T>& t, const Tri<R>& x, const R& 
     return num / den;
 }
 
-// right-hand side of the filter's solve, one thread per cell and batch member
+// ubar on every u face and vbar on every v face of one batch member (one
+// thread per point of the (nx+1) x (ny+1) index space), into [B][nx+1][ny]
+// and [B][nx][ny+1]
 template <typename T, typename S, typename R, typename W>
-__global__ void k_bf_rhs(Tab<T> t, Tri<R> x, R tu, R tv, W rhs)
+__global__ void k_bf_bar(Tab<T> t, Tri<R> x, R tu, R tv, W ub, W vb)
 {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = blockIdx.y * blockDim.y + threadIdx.y;
     const int b = blockIdx.z;
-    if (i >= t.nx || j >= t.ny) return;
-    const long long hi = (long long)i * t.ny + j;
-    const S du = bf_ubar<T, S>(t, x, tu, b, i + 1, j) - bf_ubar<T, S>(t, x, tu, b, i, j);
-    const S dv = bf_vbar<T, S>(t, x, tv, b, i, j + 1) - bf_vbar<T, S>(t, x, tv, b, i, j);
-    rhs((long long)b * t.nx * t.ny + hi, t.bf_c * (du / t.dxh[hi] + dv / t.dyh[hi]));
+    const int nx = t.nx, ny = t.ny;
+    if (i > nx || j > ny) return;
+    if (j < ny) ub((long long)b * (nx + 1) * ny + (long long)i * ny + j, bf_ubar<T, S>(t, x, tu, b, i, j));
+    if (i < nx) vb((long long)b * nx * (ny + 1) + (long long)i * (ny + 1) + j, bf_vbar<T, S>(t, x, tv, b, i, j));
+}
+
+// right-hand side of the filter's solve from the face transports, one
+// thread per cell and batch member
+template <typename T, typename S, typename R, typename W>
+__global__ void k_bf_rhs(Tab<T> t, R ub, R vb, W rhs)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    const int b = blockIdx.z;
+    const int nx = t.nx, ny = t.ny;
+    if (i >= nx || j >= ny) return;
+    const long long hi = (long long)i * ny + j;
+    const long long u0 = (long long)b * (nx + 1) * ny + hi, v0 = (long long)b * nx * (ny + 1) + (long long)i * (ny + 1) + j;
+    const S du = ub(u0 + ny) - ub(u0);
+    const S dv = vb(v0 + 1) - vb(v0);
+    rhs((long long)b * nx * ny + hi, t.bf_c * (du / t.dxh[hi] + dv / t.dyh[hi]));
 }
 
 // tendencies += the filter's velocity correction from the solved w
@@ -2378,7 +2396,11 @@ static int tend_fwd(vd_sw_plan* p, int B, Fields<T> cur, Work<T>& wk, const T* t
                                                    w(wk.tuvh.u), w(wk.tuvh.v), w(wk.fx), w(wk.fy));
     VD_LAUNCH_CHECK();
     if (p->bf) {
-        k_bf_rhs<T, T><<<Ld.grid, Ld.block, 0, st>>>(t, rt(cur), r<T>(wk.tuvh.u), r<T>(wk.tuvh.v), w(wk.bf));
+        // face transports into the adjoint's scratch (free in a forward pass)
+        k_bf_bar<T, T><<<Ld.grid, Ld.block, 0, st>>>(t, rt(cur), r<T>(wk.tuvh.u), r<T>(wk.tuvh.v), w(wk.bau),
+                                                      w(wk.bav));
+        VD_LAUNCH_CHECK();
+        k_bf_rhs<T, T><<<Ld.grid, Ld.block, 0, st>>>(t, r<T>(wk.bau), r<T>(wk.bav), w(wk.bf));
         VD_LAUNCH_CHECK();
         const int rc = vd::neumann_solve<T>(p->bf, B, wk.bf, wk.bf, st);
         if (rc) return rc;
@@ -2405,8 +2427,12 @@ static int tend_tgl(vd_sw_plan* p, int B, Fields<T> cur, Fields<T> dcur, Work<T>
         WD<T>{wk.tuvh.u, dk.tuvh.u}, WD<T>{wk.tuvh.v, dk.tuvh.v}, WD<T>{wk.fx, dk.fx}, WD<T>{wk.fy, dk.fy});
     VD_LAUNCH_CHECK();
     if (p->bf) {
-        k_bf_rhs<T, S><<<Ld.grid, Ld.block, 0, st>>>(t, rtd(cur, dcur), RD<T>{wk.tuvh.u, dk.tuvh.u},
-                                                      RD<T>{wk.tuvh.v, dk.tuvh.v}, WD<T>{wk.bf, dk.bf});
+        k_bf_bar<T, S><<<Ld.grid, Ld.block, 0, st>>>(t, rtd(cur, dcur), RD<T>{wk.tuvh.u, dk.tuvh.u},
+                                                      RD<T>{wk.tuvh.v, dk.tuvh.v}, WD<T>{wk.bau, dk.bau},
+                                                      WD<T>{wk.bav, dk.bav});
+        VD_LAUNCH_CHECK();
+        k_bf_rhs<T, S><<<Ld.grid, Ld.block, 0, st>>>(t, RD<T>{wk.bau, dk.bau}, RD<T>{wk.bav, dk.bav},
+                                                      WD<T>{wk.bf, dk.bf});
         VD_LAUNCH_CHECK();
         int rc = vd::neumann_solve<T>(p->bf, B, wk.bf, wk.bf, st);
         if (rc || (rc = vd::neumann_solve<T>(p->bf, B, dk.bf, dk.bf, st))) return rc;
