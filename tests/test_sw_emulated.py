@@ -196,10 +196,11 @@ def ref_solve(rhs, helm):
 
 # ---------------------------------------------------------------- the solve
 @pytest.mark.parametrize("nx,ny,nf", [(8, 6, 1), (12, 10, 3), (14, 22, 2), (9, 15, 3), (6, 30, 1), (26, 39, 2),
-                                      (64, 48, 1), (11, 13, 2)])
+                                      (64, 48, 1), (11, 13, 2), (8, 6, 400), (12, 10, 161)])
 def test_neumann_solve(emu, nx, ny, nf):
     """Radix 4/2/3/5 and direct (7, 11, 13) stages, odd lengths, an odd
-    number of rows and of columns (the paired transforms' padding)."""
+    number of rows and of columns (the paired transforms' padding); the large
+    batches run 2 row pairs and 4 column pairs per CTA (small ones 1 and 1)."""
     rng = np.random.default_rng(nx * 100 + ny)
     dx = 1e4 * (1 + 0.2 * rng.random((nx, ny)))
     dy = 1.3e4 * (1 + 0.2 * rng.random((nx, ny)))

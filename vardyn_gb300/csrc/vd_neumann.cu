@@ -175,13 +175,12 @@ __device__ __forceinline__ void stage_any(const cx<T>* __restrict__ in, cx<T>* _
     }
 }
 
-// Forward FFT of pp transforms held in a; returns the buffer holding the
-// result (a or b). a must be complete (synchronised) on entry; the result is
-// synchronised on return.
+// Forward FFT of pp transforms held in a, twiddles tw (shared or global
+// memory); returns the buffer holding the result (a or b). a must be
+// complete (synchronised) on entry; the result is synchronised on return.
 template <typename T>
-__device__ cx<T>* fft(cx<T>* a, cx<T>* b, const Dir& D, int pp)
+__device__ cx<T>* fft(cx<T>* a, cx<T>* b, const cx<T>* tw, const Dir& D, int pp)
 {
-    const cx<T>* tw = static_cast<const cx<T>*>(D.tw);
     int Ns = 1;
     for (int s = 0; s < D.nst; ++s) {
         const int R = D.rad[s];
@@ -199,6 +198,27 @@ __device__ cx<T>* fft(cx<T>* a, cx<T>* b, const Dir& D, int pp)
         Ns *= R;
     }
     return a;
+}
+
+// Shared memory of a pass: the twiddle and E tables when they fit (stw),
+// then the two buffers of g transforms. Returns the buffers' start; tw / E
+// point at the tables the pass reads (shared copies once synchronised).
+template <typename T>
+__device__ __forceinline__ cx<T>* stage_tables(unsigned char* raw, const Dir& D, int stw, const cx<T>*& tw,
+                                               const cx<T>*& E)
+{
+    const int N = D.N;
+    tw = static_cast<const cx<T>*>(D.tw);
+    E = static_cast<const cx<T>*>(D.E);
+    cx<T>* base = reinterpret_cast<cx<T>*>(raw);
+    if (!stw) return base;
+    for (int k = threadIdx.x; k < N; k += blockDim.x) {
+        base[k] = tw[k];
+        base[N + k] = E[k];
+    }
+    tw = base;
+    E = base + N;
+    return base + 2 * N;
 }
 
 // position of sequence element p in the reordered sequence
@@ -231,11 +251,12 @@ __device__ __forceinline__ cx<T> pack_inv(cx<T> E, T ak, T akr, T bk, T bkr)
 // DCT-II along the rows (length D.N) of nrows rows; rows 2q, 2q+1 of the
 // CTA's group share one transform.
 template <typename T>
-__global__ void __launch_bounds__(256) k_dct_rows_fwd(Dir D, long long nrows, int pp, const T* src, T* dst)
+__global__ void __launch_bounds__(256) k_dct_rows_fwd(Dir D, long long nrows, int pp, int stw, const T* src, T* dst)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int N = D.N;
-    cx<T>* a = reinterpret_cast<cx<T>*>(smem_raw);
+    const cx<T>*tw, *E;
+    cx<T>* a = stage_tables<T>(smem_raw, D, stw, tw, E);
     cx<T>* b = a + (size_t)pp * N;
     const long long r0 = 2LL * blockIdx.x * pp;
     for (int idx = threadIdx.x; idx < pp * N; idx += blockDim.x) {
@@ -247,8 +268,7 @@ __global__ void __launch_bounds__(256) k_dct_rows_fwd(Dir D, long long nrows, in
         a[(size_t)q * N + perm(p, N)] = mk(xa, xb);
     }
     __syncthreads();
-    const cx<T>* Z = fft<T>(a, b, D, pp);
-    const cx<T>* E = static_cast<const cx<T>*>(D.E);
+    const cx<T>* Z = fft<T>(a, b, tw, D, pp);
     for (int idx = threadIdx.x; idx < pp * N; idx += blockDim.x) {
         const int q = idx / N;
         const int k = idx - q * N;
@@ -263,14 +283,15 @@ __global__ void __launch_bounds__(256) k_dct_rows_fwd(Dir D, long long nrows, in
 
 // Inverse DCT-II along the rows.
 template <typename T>
-__global__ void __launch_bounds__(256) k_dct_rows_inv(Dir D, long long nrows, int pp, const T* src, T* dst)
+__global__ void __launch_bounds__(256) k_dct_rows_inv(Dir D, long long nrows, int pp, int stw, const T* src, T* dst)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int N = D.N;
-    cx<T>* a = reinterpret_cast<cx<T>*>(smem_raw);
+    const cx<T>*tw, *Es;
+    cx<T>* a = stage_tables<T>(smem_raw, D, stw, tw, Es);
     cx<T>* b = a + (size_t)pp * N;
     const long long r0 = 2LL * blockIdx.x * pp;
-    const cx<T>* E = static_cast<const cx<T>*>(D.E);
+    const cx<T>* E = static_cast<const cx<T>*>(D.E);   // read before the tables are synchronised
     for (int idx = threadIdx.x; idx < pp * N; idx += blockDim.x) {
         const int q = idx / N;
         const int k = idx - q * N;
@@ -288,7 +309,7 @@ __global__ void __launch_bounds__(256) k_dct_rows_inv(Dir D, long long nrows, in
         a[(size_t)q * N + k] = pack_inv(E[k], ak, akr, bk, bkr);
     }
     __syncthreads();
-    const cx<T>* O = fft<T>(a, b, D, pp);
+    const cx<T>* O = fft<T>(a, b, tw, D, pp);
     const T iN = T(1) / T(N);
     for (int idx = threadIdx.x; idx < pp * N; idx += blockDim.x) {
         const int q = idx / N;
@@ -304,11 +325,12 @@ __global__ void __launch_bounds__(256) k_dct_rows_inv(Dir D, long long nrows, in
 // DCT-II along x (length D.N = nx), division by helm (stored transposed,
 // helmT[j][k]), inverse along x; in place on s[f] = [nx][ny].
 template <typename T>
-__global__ void __launch_bounds__(256) k_dct_cols(Dir D, int ny, int cp, const T* __restrict__ helmT, T* s)
+__global__ void __launch_bounds__(256) k_dct_cols(Dir D, int ny, int cp, int stw, const T* __restrict__ helmT, T* s)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int N = D.N;
-    cx<T>* a = reinterpret_cast<cx<T>*>(smem_raw);
+    const cx<T>*tw, *E;
+    cx<T>* a = stage_tables<T>(smem_raw, D, stw, tw, E);
     cx<T>* b = a + (size_t)cp * N;
     const int j0 = blockIdx.x * 2 * cp;
     T* S = s + (size_t)blockIdx.y * N * ny;
@@ -322,9 +344,8 @@ __global__ void __launch_bounds__(256) k_dct_cols(Dir D, int ny, int cp, const T
         slot[c & 1] = v;
     }
     __syncthreads();
-    cx<T>* Z = fft<T>(a, b, D, cp);
+    cx<T>* Z = fft<T>(a, b, tw, D, cp);
     cx<T>* Wb = (Z == a) ? b : a;
-    const cx<T>* E = static_cast<const cx<T>*>(D.E);
     for (int idx = threadIdx.x; idx < cp * N; idx += blockDim.x) {
         const int q = idx / N;
         const int k = idx - q * N;
@@ -344,7 +365,7 @@ __global__ void __launch_bounds__(256) k_dct_cols(Dir D, int ny, int cp, const T
         Wb[(size_t)q * N + k] = pack_inv(E[k], ak, akr, bk, bkr);
     }
     __syncthreads();
-    const cx<T>* O = fft<T>(Wb, Z, D, cp);
+    const cx<T>* O = fft<T>(Wb, Z, tw, D, cp);
     const T iN = T(1) / T(N);
     for (int idx = threadIdx.x; idx < N * w2; idx += blockDim.x) {
         const int i = idx / w2;
@@ -457,7 +478,8 @@ extern "C" vd_status vd_neumann_plan_create(vd_neumann_plan** out, int nx, int n
     p->dx.N = nx;
     p->dy.N = ny;
     // row pairs per CTA (2 when two CTAs of them fit an SM), column pairs
-    // per CTA (4, 2 or 1: 8, 4 or 2 consecutive values of a row per load)
+    // per CTA (4, 2 or 1: 8, 4 or 2 consecutive values of a row per load);
+    // the solve lowers both for small batches (more CTAs)
     const size_t row1 = 2 * (size_t)ny * csz, col1 = 2 * (size_t)nx * csz;
     if (row1 > SMEM_MAX || col1 > SMEM_MAX) {
         delete p;
@@ -537,16 +559,25 @@ int neumann_solve(const vd_neumann_plan* p, int nf, const T* src, T* dst, cudaSt
     const int nx = p->nx, ny = p->ny;
     const long long nrows = (long long)nf * nx;
     const size_t csz = 2 * sizeof(T);
-    const long long rb = (nrows + 2LL * p->pp - 1) / (2LL * p->pp);
+    // fewer sequences per CTA while a pass would have under two CTAs an SM
+    constexpr long long kFill = 2 * 152;
+    int pp = p->pp, cp = p->cp;
+    while (pp > 1 && (nrows + 2LL * pp - 1) / (2LL * pp) < kFill) pp /= 2;
+    while (cp > 1 && (long long)((ny + 2 * cp - 1) / (2 * cp)) * nf < kFill) cp /= 2;
+    const long long rb = (nrows + 2LL * pp - 1) / (2LL * pp);
     if (rb > 0x7fffffffLL) return VD_ERR_UNSUPPORTED;
-    const size_t rsm = 2 * (size_t)p->pp * ny * csz;
-    nm::k_dct_rows_fwd<T><<<(unsigned)rb, 256, rsm, st>>>(p->dy, nrows, p->pp, src, dst);
+    // twiddle and E tables in shared memory when they fit beside the buffers
+    size_t rsm = 2 * (size_t)pp * ny * csz, csm = 2 * (size_t)cp * nx * csz;
+    const int rstw = rsm + 2 * (size_t)ny * csz <= nm::SMEM_MAX ? 1 : 0;
+    const int cstw = csm + 2 * (size_t)nx * csz <= nm::SMEM_MAX ? 1 : 0;
+    rsm += rstw ? 2 * (size_t)ny * csz : 0;
+    csm += cstw ? 2 * (size_t)nx * csz : 0;
+    nm::k_dct_rows_fwd<T><<<(unsigned)rb, 256, rsm, st>>>(p->dy, nrows, pp, rstw, src, dst);
     VD_LAUNCH_CHECK();
-    const dim3 cg((unsigned)((ny + 2 * p->cp - 1) / (2 * p->cp)), (unsigned)nf);
-    const size_t csm = 2 * (size_t)p->cp * nx * csz;
-    nm::k_dct_cols<T><<<cg, 256, csm, st>>>(p->dx, ny, p->cp, static_cast<const T*>(p->helmT), dst);
+    const dim3 cg((unsigned)((ny + 2 * cp - 1) / (2 * cp)), (unsigned)nf);
+    nm::k_dct_cols<T><<<cg, 256, csm, st>>>(p->dx, ny, cp, cstw, static_cast<const T*>(p->helmT), dst);
     VD_LAUNCH_CHECK();
-    nm::k_dct_rows_inv<T><<<(unsigned)rb, 256, rsm, st>>>(p->dy, nrows, p->pp, dst, dst);
+    nm::k_dct_rows_inv<T><<<(unsigned)rb, 256, rsm, st>>>(p->dy, nrows, pp, rstw, dst, dst);
     VD_LAUNCH_CHECK();
     return VD_OK;
 }
