@@ -322,6 +322,24 @@ def test_tangent_and_adjoint(emu):
     assert abs(lhs - rhs) / abs(lhs) < 1e-12
 
 
+def test_tangent_and_adjoint_float32(emu):
+    """The float32 plan: the tangent against the float64 tangent, the
+    adjoint by a dot product in float64 sums."""
+    prm, o, x, rng = _case()
+    m = o.masks
+    dx = (0.01 * rng.standard_normal(x[0].shape) * m.u, 0.01 * rng.standard_normal(x[1].shape) * m.v,
+          0.1 * rng.standard_normal(x[2].shape))
+    p32, p64 = Plan(emu, prm, dtype=np.float32), Plan(emu, prm)
+    tl32, tl64 = p32.tgl(x, dx, 2), p64.tgl(x, dx, 2)
+    for a, b, k in zip(tl32, tl64, "uvh"):
+        assert rel(a, b) < 1e-3, k
+    a1 = [rng.standard_normal(s) for s in p32.shapes(2)]
+    ad = p32.adj(x, a1, 2)
+    lhs = sum(np.vdot(t.astype(np.float64), a) for t, a in zip(tl32, a1))
+    rhs = sum(np.vdot(d, a.astype(np.float64)) for d, a in zip(dx, ad))
+    assert abs(lhs - rhs) / abs(lhs) < 1e-4
+
+
 def test_H_cotangent(emu):
     """The adjoint's cotangent of H (through the face thicknesses of the
     filter as well as the rest of the step) against central differences of
