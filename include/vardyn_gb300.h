@@ -817,8 +817,10 @@ vd_status vd_sw_step_tgl(vd_sw_plan* plan, int batch, const void* u0, const void
 /* Adjoint of vd_sw_step (jax.vjp, sw.py:924-938): overwrites adu0/adv0/adh0;
  * writes the adjoints of the sponge targets and of the forcing when asked
  * (when the targets default to the initial state their adjoint is part of
- * adu0/adv0/adh0). Atomic accumulation: results agree to rounding, not bit
- * for bit, between runs. */
+ * adu0/adv0/adh0). No atomics on the state and forcing cotangents: repeated
+ * runs agree bit for bit. The H / h_wind table cotangents of a registered
+ * vd_sw_set_ref_adj buffer are summed over the batch with atomics (bit for
+ * bit for batch 1, to rounding otherwise). */
 vd_status vd_sw_step_adj(vd_sw_plan* plan, int batch, const void* u0, const void* v0,
                          const void* h0, const void* adu1, const void* adv1,
                          const void* adh1, int nstep, const void* ub, const void* vb,

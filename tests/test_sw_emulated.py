@@ -500,3 +500,39 @@ def test_open_boundaries_adjoint(emu):
     ad = pl.adj(x, a1, 2)
     lhs = sum(np.vdot(t, a) for t, a in zip(tl, a1))
     assert abs(lhs - sum(np.vdot(d, a) for d, a in zip(dx, ad))) / abs(lhs) < 1e-12
+
+
+# ---------------------------------------------------------------- mass-consistent forcing
+def test_mass_consistent_forcing_adjoint(emu):
+    """The forcing adjoint's gather (no atomics) with land next to the faces
+    it averages over: dot products of the step's tangent (state and forcing
+    directions) against its adjoint (state and forcing cotangents)."""
+    g = dict(np.load(os.path.join(HERE, "golden", "sw_golden.npz")))
+    p = "swa_"
+    prm = dict(nx=28, ny=22, nl=2, dx=g[p + "dx"], dy=g[p + "dy"], f=g[p + "f"], H=g[p + "H"], g_prime=g[p + "gp"],
+               dt=15.0, mask=g[p + "mask"], slip_coef=0.5, bottom_drag_coef=2e-7, visc_coef=30.0, diff_coef=20.0,
+               taux=0.03, tauy=-0.01, forcing_momentum="mass_consistent")
+    pl = Plan(emu, prm)
+    rng = np.random.default_rng(11)
+    B, n = 2, 2
+    shp = pl.shapes(B)
+    c = pl.c
+    x = [c(0.1 * rng.standard_normal(s)) for s in shp]
+    F = [c(np.zeros(shp[0])), c(np.zeros(shp[1])), c(1e-4 * rng.standard_normal(shp[2]))]
+    dx = [c(0.01 * rng.standard_normal(s)) for s in shp]
+    dF = [c(np.zeros(shp[0])), c(np.zeros(shp[1])), c(1e-5 * rng.standard_normal(shp[2]))]
+    tl = [np.empty(s) for s in shp]
+    w = pl.ws(B, n)
+    ok(emu.vd_sw_step_tgl(pl.h, B, *map(ptr, x), *map(ptr, dx), n, None, None, None, None, None, None,
+                          *map(ptr, F), *map(ptr, dF), None, None, *map(ptr, tl), ptr(w), w.nbytes, None), "tgl")
+    a1 = [c(rng.standard_normal(s)) for s in shp]
+    ad = [np.empty(s) for s in shp]
+    adF = [np.empty(s) for s in shp]
+    w = pl.ws(B, n)
+    ok(emu.vd_sw_step_adj(pl.h, B, *map(ptr, x), *map(ptr, a1), n, None, None, None, *map(ptr, F), None, None,
+                          *map(ptr, ad), None, None, None, *map(ptr, adF), ptr(w), w.nbytes, None), "adj")
+    lhs = sum(np.vdot(t, a) for t, a in zip(tl, a1))
+    rhs = sum(np.vdot(d, a) for d, a in zip(dx, ad)) + sum(np.vdot(d, a) for d, a in zip(dF, adF))
+    assert abs(lhs - rhs) / abs(lhs) < 1e-12
+    # the forcing's own cotangent is exercised (nonzero on ocean cells)
+    assert np.abs(adF[2]).max() > 0

@@ -1296,81 +1296,141 @@ __global__ void k_sw_diag_adj(Tab<T> t, const T* u, const T* v, const T* h, cons
 // Adjoint of k_sw_force_mc (scatter to the thickness and Fh of the replicate
 // padding stencil, atomics). adn: adjoint of the output (in place: becomes the
 // adjoint of the input u, v, h direct paths).
+// Adjoint of the mass-consistent forcing (sw.py:880-898), without atomics:
+// the face terms (the cotangents the face's thickness and forcing averages
+// hand to each of their two padded cells) are recomputed where they are
+// gathered. mc_face_u / mc_face_v give them for one face from the face's
+// incoming velocity cotangent.
 template <typename T>
-__device__ __forceinline__ void rep_pad_adj(const Tab<T>& t, T* ad, long long base, int pi, int pj, T a)
+__device__ __forceinline__ void mc_face_u(const Tab<T>& t, const T* u, const T* h, const T* Fh, const T* adu,
+                                          long long bl, int i, int j, T& gh, T& gf, T& fu, T& htu, T& sz)
 {
-    const int nx = t.nx, ny = t.ny;
-    auto cl = [](int q, int n) { return q < 0 ? 0 : (q > n - 1 ? n - 1 : q); };
-    const int ci = cl(pi - 1, nx), cj = cl(pj - 1, ny);
-    if (t.fh[(long long)ci * ny + cj] & 1) {
-        aadd(&ad[base + (long long)ci * ny + cj], a);
-        return;
-    }
-    int ms = 0;
-    for (int p = pi - 1; p <= pi + 1; ++p)
-        for (int c = pj - 1; c <= pj + 1; ++c) {
-            if (p < 0 || p > nx + 1 || c < 0 || c > ny + 1) continue;
-            ms += (t.fh[(long long)cl(p - 1, nx) * ny + cl(c - 1, ny)] & 1);
-        }
-    const T w = a / T(ms > 1 ? ms : 1);
-    for (int p = pi - 1; p <= pi + 1; ++p)
-        for (int c = pj - 1; c <= pj + 1; ++c) {
-            if (p < 0 || p > nx + 1 || c < 0 || c > ny + 1) continue;
-            aadd(&ad[base + (long long)cl(p - 1, nx) * ny + cl(c - 1, ny)], w);
-        }
+    const int ny = t.ny, l = (int)(bl % t.nl);
+    const long long ui = (long long)i * ny + j, idx = bl * t.su + ui, hb = bl * t.sh;
+    R1<T> H{h}, FH{Fh};
+    const T hu = T(0.5) * (rep_pad<T, T>(t, H, hb, i + 1, j + 1) + rep_pad<T, T>(t, H, hb, i, j + 1));
+    fu = T(0.5) * (rep_pad<T, T>(t, FH, hb, i + 1, j + 1) + rep_pad<T, T>(t, FH, hb, i, j + 1));
+    const T xmin = t.hmin * t.areau[ui];
+    const T zz = (t.hrefu[(long long)l * t.su + ui] + hu - xmin) * t.sharp;
+    htu = xmin + softplus_v(zz) / t.sharp;
+    sz = sigmoid_v(zz);
+    const T a = adu[idx], uu = u[idx];
+    gh = T(0.5) * (a * t.dt * uu * fu / (htu * htu) * sz);
+    gf = T(0.5) * (-a * t.dt * uu / htu);
 }
 
 template <typename T>
-__global__ void k_sw_force_mc_adj(Tab<T> t, const T* u, const T* v, const T* h, const T* Fh, T* adu, T* adv,
-                                  T* adh_acc, T* adFh)
+__device__ __forceinline__ void mc_face_v(const Tab<T>& t, const T* v, const T* h, const T* Fh, const T* adv,
+                                          long long bl, int i, int j, T& gh, T& gf, T& fv, T& htv, T& sz)
+{
+    const int ny = t.ny, l = (int)(bl % t.nl);
+    const long long vi = (long long)i * (ny + 1) + j, idx = bl * t.sv + vi, hb = bl * t.sh;
+    R1<T> H{h}, FH{Fh};
+    const T hv = T(0.5) * (rep_pad<T, T>(t, H, hb, i + 1, j + 1) + rep_pad<T, T>(t, H, hb, i + 1, j));
+    fv = T(0.5) * (rep_pad<T, T>(t, FH, hb, i + 1, j + 1) + rep_pad<T, T>(t, FH, hb, i + 1, j));
+    const T xmin = t.hmin * t.areav[vi];
+    const T zz = (t.hrefv[(long long)l * t.sv + vi] + hv - xmin) * t.sharp;
+    htv = xmin + softplus_v(zz) / t.sharp;
+    sz = sigmoid_v(zz);
+    const T a = adv[idx], vv = v[idx];
+    gh = T(0.5) * (a * t.dt * vv * fv / (htv * htv) * sz);
+    gf = T(0.5) * (-a * t.dt * vv / htv);
+}
+
+// Step 1, one thread per cell (i, j) and field: the cotangents of h and Fh.
+// A padded cell (pi, pj) of replicate_pad (sw.py:36-48) takes its clamped
+// cell when that is ocean, else the mean over the ocean count of its 3 x 3
+// clamped neighbourhood; it is read by up to two u faces and two v faces.
+// The cell gathers, over the padded cells within reach, its multiplicity in
+// each padded cell's value times that padded cell's face terms, in a fixed
+// order. Must run before step 2, which overwrites adu / adv.
+template <typename T>
+__global__ void k_sw_force_mc_adj_h(Tab<T> t, const T* u, const T* v, const T* h, const T* Fh, const T* adu,
+                                    const T* adv, T* adh_acc, T* adFh)
 {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = blockIdx.y * blockDim.y + threadIdx.y;
-    const int bl = blockIdx.z, l = bl % t.nl;
+    const long long bl = blockIdx.z;
+    const int nx = t.nx, ny = t.ny;
+    if (i >= nx || j >= ny) return;
+    auto cl = [](int q, int n) { return q < 0 ? 0 : (q > n - 1 ? n - 1 : q); };
+    T sh = T(0), sf = T(0);
+    for (int pi = (i > 0 ? i - 1 : 0); pi <= (i + 3 < nx + 1 ? i + 3 : nx + 1); ++pi)
+        for (int pj = (j > 0 ? j - 1 : 0); pj <= (j + 3 < ny + 1 ? j + 3 : ny + 1); ++pj) {
+            const int ci = cl(pi - 1, nx), cj = cl(pj - 1, ny);
+            T wgt;
+            if (t.fh[(long long)ci * ny + cj] & 1) {
+                if (ci != i || cj != j) continue;
+                wgt = T(1);
+            } else {
+                int cnt = 0, ms = 0;
+                for (int a = pi - 1; a <= pi + 1; ++a)
+                    for (int c = pj - 1; c <= pj + 1; ++c) {
+                        if (a < 0 || a > nx + 1 || c < 0 || c > ny + 1) continue;
+                        const int ai = cl(a - 1, nx), aj = cl(c - 1, ny);
+                        ms += (t.fh[(long long)ai * ny + aj] & 1);
+                        cnt += (ai == i && aj == j);
+                    }
+                if (!cnt) continue;
+                wgt = T(cnt) / T(ms > 1 ? ms : 1);
+            }
+            T gh = T(0), gf = T(0), a, b, f, ht, sz;
+            if (pj >= 1 && pj <= ny) {   // u faces (pi - 1, pj - 1) and (pi, pj - 1)
+                if (pi >= 1) {
+                    mc_face_u(t, u, h, Fh, adu, bl, pi - 1, pj - 1, a, b, f, ht, sz);
+                    gh += a;
+                    gf += b;
+                }
+                if (pi <= nx) {
+                    mc_face_u(t, u, h, Fh, adu, bl, pi, pj - 1, a, b, f, ht, sz);
+                    gh += a;
+                    gf += b;
+                }
+            }
+            if (pi >= 1 && pi <= nx) {   // v faces (pi - 1, pj - 1) and (pi - 1, pj)
+                if (pj >= 1) {
+                    mc_face_v(t, v, h, Fh, adv, bl, pi - 1, pj - 1, a, b, f, ht, sz);
+                    gh += a;
+                    gf += b;
+                }
+                if (pj <= ny) {
+                    mc_face_v(t, v, h, Fh, adv, bl, pi - 1, pj, a, b, f, ht, sz);
+                    gh += a;
+                    gf += b;
+                }
+            }
+            sh += wgt * gh;
+            sf += wgt * gf;
+        }
+    const long long o = bl * t.sh + (long long)i * ny + j;
+    adh_acc[o] += sh;
+    if (adFh) adFh[o] += sf;
+}
+
+// Step 2, one thread per face point: u_new = u - dt u Fh_u / htot_u, so
+// adu <- adu (1 - dt Fh_u / htot_u) in place; the face thickness cotangent
+// also goes to the H table's cotangent when one is registered.
+template <typename T>
+__global__ void k_sw_force_mc_adj(Tab<T> t, const T* u, const T* v, const T* h, const T* Fh, T* adu, T* adv)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    const long long bl = blockIdx.z;
+    const int l = (int)(bl % t.nl);
     const int nx = t.nx, ny = t.ny;
     if (i > nx || j > ny) return;
-    const long long ob = bl, hb = ob * t.sh;
-    const T dt = t.dt;
-    R1<T> H{h}, FH{Fh};
+    T gh, gf, f, ht, sz;
     if (j < ny) {
-        const long long ui = (long long)i * ny + j, idx = ob * t.su + ui;
-        const T hu = T(0.5) * (rep_pad<T, T>(t, H, hb, i + 1, j + 1) + rep_pad<T, T>(t, H, hb, i, j + 1));
-        const T fu = T(0.5) * (rep_pad<T, T>(t, FH, hb, i + 1, j + 1) + rep_pad<T, T>(t, FH, hb, i, j + 1));
-        const T xmin = t.hmin * t.areau[ui];
-        const T zz = (t.hrefu[(long long)l * t.su + ui] + hu - xmin) * t.sharp;
-        const T htu = xmin + softplus_v(zz) / t.sharp;
-        const T a = adu[idx];
-        const T uu = u[idx];
-        adu[idx] = a * (T(1) - dt * fu / htu);
-        const T aht = a * dt * uu * fu / (htu * htu) * sigmoid_v(zz);
-        const T afu = -a * dt * uu / htu;
-        if (t.ad_hrefu) aadd(&t.ad_hrefu[(long long)l * t.su + ui], aht);
-        rep_pad_adj(t, adh_acc, hb, i + 1, j + 1, T(0.5) * aht);
-        rep_pad_adj(t, adh_acc, hb, i, j + 1, T(0.5) * aht);
-        if (adFh) {
-            rep_pad_adj(t, adFh, hb, i + 1, j + 1, T(0.5) * afu);
-            rep_pad_adj(t, adFh, hb, i, j + 1, T(0.5) * afu);
-        }
+        const long long ui = (long long)i * ny + j, idx = bl * t.su + ui;
+        mc_face_u(t, u, h, Fh, adu, bl, i, j, gh, gf, f, ht, sz);
+        if (t.ad_hrefu) aadd(&t.ad_hrefu[(long long)l * t.su + ui], T(2) * gh);
+        adu[idx] = adu[idx] * (T(1) - t.dt * f / ht);
     }
     if (i < nx) {
-        const long long vi = (long long)i * (ny + 1) + j, idx = ob * t.sv + vi;
-        const T hv = T(0.5) * (rep_pad<T, T>(t, H, hb, i + 1, j + 1) + rep_pad<T, T>(t, H, hb, i + 1, j));
-        const T fv = T(0.5) * (rep_pad<T, T>(t, FH, hb, i + 1, j + 1) + rep_pad<T, T>(t, FH, hb, i + 1, j));
-        const T xmin = t.hmin * t.areav[vi];
-        const T zz = (t.hrefv[(long long)l * t.sv + vi] + hv - xmin) * t.sharp;
-        const T htv = xmin + softplus_v(zz) / t.sharp;
-        const T a = adv[idx];
-        const T vv = v[idx];
-        adv[idx] = a * (T(1) - dt * fv / htv);
-        const T aht = a * dt * vv * fv / (htv * htv) * sigmoid_v(zz);
-        const T afv = -a * dt * vv / htv;
-        if (t.ad_hrefv) aadd(&t.ad_hrefv[(long long)l * t.sv + vi], aht);
-        rep_pad_adj(t, adh_acc, hb, i + 1, j + 1, T(0.5) * aht);
-        rep_pad_adj(t, adh_acc, hb, i + 1, j, T(0.5) * aht);
-        if (adFh) {
-            rep_pad_adj(t, adFh, hb, i + 1, j + 1, T(0.5) * afv);
-            rep_pad_adj(t, adFh, hb, i + 1, j, T(0.5) * afv);
-        }
+        const long long vi = (long long)i * (ny + 1) + j, idx = bl * t.sv + vi;
+        mc_face_v(t, v, h, Fh, adv, bl, i, j, gh, gf, f, ht, sz);
+        if (t.ad_hrefv) aadd(&t.ad_hrefv[(long long)l * t.sv + vi], T(2) * gh);
+        adv[idx] = adv[idx] * (T(1) - t.dt * f / ht);
     }
 }
 
@@ -2752,8 +2812,10 @@ static int sw_adj_t(vd_sw_plan* p, int B, const void* u0, const void* v0, const 
         }
         if (mc) {
             // u_new = u3 - dt u3 Fh_u / htot_u(h3): ad -> ad(u3), ad(h3) (+= into ad.h), ad(Fh)
-            k_sw_force_mc_adj<T><<<Ll.grid, Ll.block, 0, st>>>(t, wk.x1.u, wk.x1.v, wk.x1.h, in.F.h, ad.u, ad.v,
-                                                               ad.h, adF.h);
+            k_sw_force_mc_adj_h<T><<<Ll.grid, Ll.block, 0, st>>>(t, wk.x1.u, wk.x1.v, wk.x1.h, in.F.h, ad.u, ad.v,
+                                                                 ad.h, adF.h);
+            VD_LAUNCH_CHECK();
+            k_sw_force_mc_adj<T><<<Ll.grid, Ll.block, 0, st>>>(t, wk.x1.u, wk.x1.v, wk.x1.h, in.F.h, ad.u, ad.v);
             VD_LAUNCH_CHECK();
         }
         if ((rc = zero(a0, s, B, st)) || (rc = zero(a1, s, B, st))) return rc;
@@ -3025,8 +3087,12 @@ template <typename T>
 static int sw_force_mc_adj_t(vd_sw_plan* p, int B, const void* const* f, cudaStream_t st)
 {
     const Launch L = lgrid(p, B * p->nl);
+    k_sw_force_mc_adj_h<T><<<L.grid, L.block, 0, st>>>(tab<T>(p), (const T*)f[0], (const T*)f[1], (const T*)f[2],
+                                                       (const T*)f[3], (const T*)f[4], (const T*)f[5], (T*)f[6],
+                                                       (T*)f[7]);
+    VD_LAUNCH_CHECK();
     k_sw_force_mc_adj<T><<<L.grid, L.block, 0, st>>>(tab<T>(p), (const T*)f[0], (const T*)f[1], (const T*)f[2],
-                                                     (const T*)f[3], (T*)f[4], (T*)f[5], (T*)f[6], (T*)f[7]);
+                                                     (const T*)f[3], (T*)f[4], (T*)f[5]);
     VD_LAUNCH_CHECK();
     return VD_OK;
 }
