@@ -205,8 +205,7 @@ def test_adjoint_is_bit_reproducible(g, dtype):
     """The tendency adjoint runs in two passes without atomics (per-source
     terms, then a fixed-order gather per target), so repeated adjoints agree
     bit for bit (two layers, land, viscosity, diffusion, drag, sponge, wind,
-    boundary fields and forcing; mass-consistent forcing is not used here: its
-    adjoint still scatters with atomics)."""
+    boundary fields and forcing)."""
     pl = plan_a(g, dtype)
     p = "swa_"
     t = lambda k: T(g[p + k], dtype)
@@ -219,4 +218,25 @@ def test_adjoint_is_bit_reproducible(g, dtype):
     a1 = pl.step_adj(*x, *w, nstep=3, **kw)
     a2 = pl.step_adj(*x, *w, nstep=3, **kw)
     for k in ("u0", "v0", "h0", "ub", "vb", "hb", "Fu", "Fv", "Fh"):
+        assert torch.equal(a1[k], a2[k]), k
+
+
+def test_mass_consistent_adjoint_is_bit_reproducible(g):
+    """The mass-consistent forcing adjoint gathers over the replicate-padded
+    cells in a fixed order (no atomics): with land next to the forced faces,
+    repeated adjoints agree bit for bit."""
+    from vardyn_gb300.sw import SWPlan
+    p = "swa_"
+    pl = SWPlan(28, 22, 2, g[p + "dx"], g[p + "dy"], g[p + "f"], g[p + "H"], g[p + "gp"], 15.0, mask=g[p + "mask"],
+                slip_coef=0.5, bottom_drag_coef=2e-7, visc_coef=30.0, diff_coef=20.0,
+                forcing_momentum="mass_consistent", dtype=torch.float64)
+    t = lambda k: T(g[p + k])
+    rng = np.random.default_rng(15)
+    x = [t("u0"), t("v0"), t("h0")]
+    m = pl.masks
+    w = [T(_rand_like(a.shape, rng, mk)) for a, mk in zip(x, (m.u, m.v, m.h))]
+    kw = dict(Fh=T(1e-4 * rng.standard_normal(g[p + "h0"].shape)), want_forcing=True)
+    a1 = pl.step_adj(*x, *w, nstep=3, **kw)
+    a2 = pl.step_adj(*x, *w, nstep=3, **kw)
+    for k in ("u0", "v0", "h0", "Fh"):
         assert torch.equal(a1[k], a2[k]), k
