@@ -58,3 +58,13 @@ def test_rhs_and_steps(g):
     c = oracle(g, flag_obc=False).step(g["ob_u0"], g["ob_v0"], g["ob_h0"], nstep=4, u_b=g["ob_ub"],
                                        v_b=g["ob_vb"], h_b=g["ob_hb"], Fu=g["ob_Fu"], Fv=g["ob_Fv"], Fh=g["ob_Fh"])
     assert rel(c[0], g["ob_u4"]) > 1e-3
+
+
+def test_library_host_masks(g):
+    """The library's host mask builder with open boundaries (no GPU): the
+    face masks equal the reference's."""
+    from vardyn_gb300.sw import SWMasks
+    m = SWMasks(28, 22, g["ob_mask"], obc=True)
+    assert np.array_equal(m.u, g["ob_mask_u"]) and np.array_equal(m.v, g["ob_mask_v"])
+    c = SWMasks(28, 22, g["ob_mask"])
+    assert not np.array_equal(c.u, g["ob_mask_u"])
